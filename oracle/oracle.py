@@ -1,0 +1,605 @@
+"""ORACLE — test infrastructure only.
+
+ctypes binding of the FP64 CPU restatement in ``parcop_oracle.cpp`` plus a
+numpy restatement of pyranda's Python driver layer (``pyrandaSim`` with its
+EOM/IC string translator, LSRK(5,4) ``rk4``, the ``Timestep`` and ``BC``
+packages).  It exists so the test-suite can check the CUDA library and the
+product's ``pyrandaSim`` against an independent CPU computation, and so that
+``bench.py`` can time a CPU baseline.  The product never imports this module.
+
+Reference files restated here (paths within the pyranda project):
+  pyranda/pyranda.py:34-131 (init), :231-370 (EOM/setIC), :376-428
+  (updateFlux/updateVars), :607-736 (operators), :758-810 (rk4), :812-869 (sMap)
+  pyranda/pyrandaUtils.py:22-141 (fortran3d, findVar)
+  pyranda/pyrandaEq.py:16-48, pyranda/pyrandaMesh.py:33-56,214-233
+  pyranda/pyrandaTimestep.py:42-77, pyranda/pyrandaBC.py:58-160
+  pyranda/pyrandaMPI.py:307-326 (sum3D/max3D/min3D on one rank)
+"""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libparcop_oracle.so")
+_lib = None
+
+
+def build():
+    """Compile the oracle library (make in this directory)."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = ctypes.CDLL(_LIB_PATH)
+        P = ctypes.c_void_p
+        D = ctypes.POINTER(ctypes.c_double)
+        I = ctypes.POINTER(ctypes.c_int)
+        L.og_create.argtypes = [I, I, D, D, ctypes.POINTER(P)]
+        L.og_destroy.argtypes = [P]
+        L.og_apply.argtypes = [P, ctypes.c_int, ctypes.c_int, D, D]
+        L.og_filter3.argtypes = [P, ctypes.c_int, D, D]
+        L.og_ring.argtypes = [P, D, D, ctypes.c_int]
+        L.og_ringv.argtypes = [P, D, D, D, D, ctypes.c_int]
+        L.og_grad.argtypes = [P, D, D, D, D]
+        L.og_div.argtypes = [P, D, D, D, D]
+        L.og_mesh.argtypes = [P, ctypes.c_int, D]
+        L.og_spacing.argtypes = [P, D, D]
+        L.og_dense.argtypes = [P, ctypes.c_int, ctypes.c_int, D]
+        L.og_threads.restype = ctypes.c_int
+        L.og_set_threads.argtypes = [ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _f64(a):
+    """F-ordered float64 copy/view of a (nx,ny,nz) array (the parcop layout)."""
+    return numpy.asfortranarray(numpy.asarray(a, dtype=numpy.float64))
+
+
+OP_D1, OP_D8, OP_SF, OP_GF = 0, 1, 2, 3
+
+
+class OracleGrid:
+    """One parcop patch: parcop.f90:23-61 ``setup`` on a Cartesian mesh."""
+
+    def __init__(self, n, periodic, x1, xn):
+        L = lib()
+        n = (ctypes.c_int * 3)(*[int(v) for v in n])
+        per = (ctypes.c_int * 3)(*[1 if p else 0 for p in periodic])
+        a = (ctypes.c_double * 3)(*[float(v) for v in x1])
+        b = (ctypes.c_double * 3)(*[float(v) for v in xn])
+        h = ctypes.c_void_p()
+        rc = L.og_create(n, per, a, b, ctypes.byref(h))
+        if rc != 0:
+            raise ValueError("oracle: bad grid")
+        self.h = h
+        self.shape = (n[0], n[1], n[2])
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().og_destroy(self.h)
+        except Exception:
+            pass
+
+    def _out(self):
+        return numpy.zeros(self.shape, dtype=numpy.float64, order="F")
+
+    def apply(self, op, direction, v):
+        v = _f64(v)
+        out = self._out()
+        lib().og_apply(self.h, op, direction, _dp(v), _dp(out))
+        return out
+
+    def ddx(self, v):
+        return self.apply(OP_D1, 0, v)
+
+    def ddy(self, v):
+        return self.apply(OP_D1, 1, v)
+
+    def ddz(self, v):
+        return self.apply(OP_D1, 2, v)
+
+    def dd8(self, direction, v):
+        return self.apply(OP_D8, direction, v)
+
+    def sfilter(self, v):
+        v = _f64(v)
+        out = self._out()
+        lib().og_filter3(self.h, OP_SF, _dp(v), _dp(out))
+        return out
+
+    def gfilter(self, v):
+        v = _f64(v)
+        out = self._out()
+        lib().og_filter3(self.h, OP_GF, _dp(v), _dp(out))
+        return out
+
+    def gfilterdir(self, v, direction):
+        return self.apply(OP_GF, direction, v)
+
+    def sfilterdir(self, v, direction):
+        return self.apply(OP_SF, direction, v)
+
+    def ring(self, v, L=2):
+        v = _f64(v)
+        out = self._out()
+        lib().og_ring(self.h, _dp(v), _dp(out), L)
+        return out
+
+    def ringv(self, f, g, h, L=1):
+        f, g, h = _f64(f), _f64(g), _f64(h)
+        out = self._out()
+        lib().og_ringv(self.h, _dp(f), _dp(g), _dp(h), _dp(out), L)
+        return out
+
+    def grad(self, v):
+        v = _f64(v)
+        gx, gy, gz = self._out(), self._out(), self._out()
+        lib().og_grad(self.h, _dp(v), _dp(gx), _dp(gy), _dp(gz))
+        return gx, gy, gz
+
+    def div(self, fx, fy, fz):
+        fx, fy, fz = _f64(fx), _f64(fy), _f64(fz)
+        out = self._out()
+        lib().og_div(self.h, _dp(fx), _dp(fy), _dp(fz), _dp(out))
+        return out
+
+    def mesh(self, which):
+        out = self._out()
+        lib().og_mesh(self.h, which, _dp(out))
+        return out
+
+    def spacing(self):
+        pd = (ctypes.c_double * 3)()
+        md = (ctypes.c_double * 3)()
+        lib().og_spacing(self.h, pd, md)
+        return list(pd), list(md)
+
+    def dense(self, op, direction):
+        n = self.shape[direction]
+        D = numpy.zeros((n, n), dtype=numpy.float64)
+        rc = lib().og_dense(self.h, op, direction, _dp(D))
+        if rc != 0:
+            raise ValueError("oracle: null operator")
+        return D
+
+
+def set_threads(t):
+    lib().og_set_threads(int(t))
+
+
+def threads():
+    return int(lib().og_threads())
+
+
+# ---------------------------------------------------------------------------
+# String translator: pyrandaUtils.py:22-141
+# ---------------------------------------------------------------------------
+def find_var_scalar(string):
+    out = []
+    for nv in re.findall(":.*?:", string):
+        if not any(ch in nv for ch in "[]{}#%*@"):
+            out.append(nv.replace(":", ""))
+    return out
+
+
+def find_var_vector(string):
+    return [s.replace(":[", "").replace("]:", "") for s in re.findall(r":\[.*?\]:", string)]
+
+
+def find_var(string, kind, unique=True):
+    v = find_var_scalar(string) if kind == "scalar" else find_var_vector(string)
+    return list(set(v)) if unique else v
+
+
+def fortran3d(form, smap):
+    form = form.replace(" ", "").strip()
+    var_data = 'self.variables["%s"].data'
+    for ivar in find_var(form, "scalar"):
+        k = ":%s:" % ivar
+        if k not in smap:
+            smap[k] = var_data % ivar
+    for ivar in find_var(form, "vector"):
+        k = ":[%s]:" % ivar
+        if k not in smap:
+            smap[k] = var_data % ivar
+    for m in smap:
+        form = form.replace(m, smap[m])
+    return form
+
+
+def split_lines(s):
+    lines = [el.replace(" ", "") for el in s.split("\n") if el]
+    lines = [el for el in lines if el]
+    return [el for el in lines if el.strip()[0] != "#"]
+
+
+class _Var:
+    def __init__(self, name):
+        self.name = name
+        self.data = None
+
+    def sum(self):
+        return float(numpy.sum(self.data))
+
+
+class _Eq:
+    """pyrandaEq.py:16-48"""
+
+    def __init__(self, eqstr, smap):
+        self.eqstr = eqstr
+        self.kind = "ALG"
+        self.rank = 1
+        if "=" in eqstr:
+            self.LHS = find_var(eqstr.split("=")[0], "scalar", unique=False)
+            self.rank = len(self.LHS)
+        else:
+            self.LHS = None
+        srhs = fortran3d(eqstr.split("=")[1] if self.LHS else eqstr, smap)
+        self.RHS = eval("lambda self: " + srhs, _EVAL_GLOBALS)
+        if "ddt(" in eqstr:
+            self.kind = "PDE"
+
+
+class _Timestep:
+    """pyrandaTimestep.py:42-77 (Cartesian)"""
+
+    name = "Timestep"
+
+    def __init__(self, sim):
+        self.sim = sim
+        self.sMap = {"dt.courant(": "self.packages['Timestep'].courant(",
+                     "dt.diff(": "self.packages['Timestep'].diff(",
+                     "dt.diffDir(": "self.packages['Timestep'].diffDir("}
+
+    def courant(self, u, v, w, c):
+        s = self.sim
+        vrate = numpy.abs(u) / s.d1 + numpy.abs(v) / s.d2 + numpy.abs(w) / s.d3
+        crate = numpy.abs(c) / s.GridLen
+        return 1.0 / numpy.max(vrate + crate)
+
+    def diff(self, bulk, density):
+        delta = self.sim.GridLen
+        drate = density * delta * delta / numpy.maximum(1.0e-12, bulk)
+        return numpy.min(drate)
+
+    def diffDir(self, bulk, density, delta):
+        drate = density * delta * delta / numpy.maximum(1.0e-12, bulk)
+        return numpy.min(drate)
+
+
+class _BC:
+    """pyrandaBC.py:58-160 (extrap / const on one rank)"""
+
+    name = "BC"
+
+    def __init__(self, sim):
+        self.sim = sim
+        self.sMap = {"bc.extrap(": "self.packages['BC'].extrap(",
+                     "bc.const(": "self.packages['BC'].const("}
+
+    @staticmethod
+    def _slice(direction, k):
+        ax = "xyz".index(direction[0])
+        idx = [slice(None)] * 3
+        idx[ax] = k
+        return tuple(idx)
+
+    def extrap(self, var, direction, order=2):
+        var = var if isinstance(var, list) else [var]
+        direction = direction if isinstance(direction, list) else [direction]
+        for d in direction:
+            for v in var:
+                a = self.sim.variables[v].data
+                if self.sim.shape["xyz".index(d[0])] <= 1:
+                    continue
+                if d[1] == "1":
+                    t, s1, s2 = 0, 1, 2
+                else:
+                    t, s1, s2 = -1, -2, -3
+                if order == 2:
+                    a[self._slice(d, t)] = 2 * a[self._slice(d, s1)] - a[self._slice(d, s2)]
+                else:
+                    a[self._slice(d, t)] = a[self._slice(d, s1)]
+
+    def const(self, var, direction, val):
+        var = var if isinstance(var, list) else [var]
+        direction = direction if isinstance(direction, list) else [direction]
+        for d in direction:
+            for v in var:
+                if self.sim.shape["xyz".index(d[0])] <= 1:
+                    continue
+                a = self.sim.variables[v].data
+                a[self._slice(d, 0 if d[1] == "1" else -1)] = val
+
+
+_EVAL_GLOBALS = {"numpy": numpy}
+try:
+    import scipy.special  # noqa: F401  (erf in the sMap)
+    import scipy
+    _EVAL_GLOBALS["scipy"] = scipy
+except Exception:  # pragma: no cover
+    pass
+
+
+def default_mesh_options():
+    """pyrandaMesh.py:214-233"""
+    return {"x1": [0.0, 0.0, 0.0], "xn": [1, 1, 1], "nn": [1, 1, 1],
+            "periodic": [False, False, False]}
+
+
+class OracleSim:
+    """numpy restatement of pyrandaSim (pyranda.py) on the oracle operators."""
+
+    def __init__(self, name, mesh_str):
+        self.name = name
+        opts = default_mesh_options()
+
+        def set_options(ind, x1, xn, nn, periodic=False):
+            opts["x1"][ind] = x1
+            opts["xn"][ind] = xn
+            opts["nn"][ind] = nn
+            opts["periodic"][ind] = periodic
+
+        msmap = {"xdom=(": "set_options(0,", "ydom=(": "set_options(1,", "zdom=(": "set_options(2,"}
+        for line in split_lines(mesh_str):
+            exec(fortran3d(line, dict(msmap)), {"set_options": set_options, "numpy": numpy})
+        self.options = opts
+        self.nx, self.ny, self.nz = opts["nn"]
+        self.npts = self.nx * self.ny * self.nz
+        self.dx = (opts["xn"][0] - opts["x1"][0]) / max(self.nx - 1, 1)
+        self.dy = (opts["xn"][1] - opts["x1"][1]) / max(self.ny - 1, 1)
+        self.dz = (opts["xn"][2] - opts["x1"][2]) / max(self.nz - 1, 1)
+        self.shape = (self.nx, self.ny, self.nz)
+        self.grid = OracleGrid(self.shape, opts["periodic"], opts["x1"], opts["xn"])
+        self.meshx = self.grid.mesh(0)
+        self.meshy = self.grid.mesh(1)
+        self.meshz = self.grid.mesh(2)
+        self.d1 = self.grid.mesh(3)
+        self.d2 = self.grid.mesh(4)
+        self.d3 = self.grid.mesh(5)
+        self.GridLen = self.grid.mesh(6)
+        self.zero = numpy.zeros(self.shape, order="F")
+        self.equations = []
+        self.conserved = []
+        self.variables = {}
+        self.packages = {}
+        self.nPDE = 0
+        self.time = 0.0
+        self.deltat = 0.0
+        self.cycle = 0
+        self._smap()
+
+    # pyranda.py:812-869
+    def _smap(self):
+        s = {}
+        s["div("] = "self.div("
+        s["ddx("] = "self.ddx("
+        s["ddy("] = "self.ddy("
+        s["ddz("] = "self.ddz("
+        s["fbar("] = "self.filter("
+        s["gbar("] = "self.gfilter("
+        s["gbarx("] = "self.gfilterx("
+        s["gbary("] = "self.gfiltery("
+        s["gbarz("] = "self.gfilterz("
+        s["grad("] = "self.grad("
+        s["simtime"] = "self.time"
+        s["deltat"] = "self.deltat"
+        s["ring("] = "self.ring("
+        s["ringV("] = "self.ringV("
+        s["dd8x("] = "self.dd8x("
+        s["dd8y("] = "self.dd8y("
+        s["dd8z("] = "self.dd8z("
+        s["sum("] = "self.sum3D("
+        s["mean("] = "1.0/float(self.npts) * self.sum3D("
+        s["sign("] = "numpy.sign("
+        s["dot("] = "numpy.dot("
+        s["abs("] = "numpy.abs("
+        s["sqrt("] = "numpy.sqrt("
+        s["sin("] = "numpy.sin("
+        s["cos("] = "numpy.cos("
+        s["tanh("] = "numpy.tanh("
+        s["exp("] = "numpy.exp("
+        s["where("] = "numpy.where("
+        s["max("] = "self.max3D("
+        s["min("] = "self.min3D("
+        s["3d("] = "self.emptyScalar("
+        s["pi"] = "numpy.pi"
+        s["gridLen"] = "self.GridLen"
+        s["erf("] = "scipy.special.erf("
+        s["meshx"] = "self.meshx"
+        s["meshy"] = "self.meshy"
+        s["meshz"] = "self.meshz"
+        self.sMap = s
+
+    def addPackage(self, kind):
+        pkg = _Timestep(self) if kind == "Timestep" else _BC(self)
+        self.packages[pkg.name] = pkg
+        self.sMap.update(pkg.sMap)
+
+    def emptyScalar(self, val=0.0):
+        return numpy.zeros(self.shape, order="F") + val
+
+    def sum3D(self, a):
+        return numpy.sum(a)
+
+    def max3D(self, a):
+        return numpy.max(a)
+
+    def min3D(self, a):
+        return numpy.min(a)
+
+    def var(self, name):
+        return self.variables[name]
+
+    def eval(self, expr):
+        return eval(fortran3d(expr, self.sMap), _EVAL_GLOBALS, {"self": self})
+
+    # pyranda.py:607-736
+    def ddx(self, v):
+        return 0.0 if self.nx <= 1 else self.grid.ddx(v)
+
+    def ddy(self, v):
+        return 0.0 if self.ny <= 1 else self.grid.ddy(v)
+
+    def ddz(self, v):
+        return 0.0 if self.nz <= 1 else self.grid.ddz(v)
+
+    def dd8x(self, v):
+        return self.grid.dd8(0, v)
+
+    def dd8y(self, v):
+        return self.grid.dd8(1, v)
+
+    def dd8z(self, v):
+        return self.grid.dd8(2, v)
+
+    def div(self, f1, f2=None, f3=None):
+        z = self.zero
+        if f2 is None and f3 is None:
+            if self.nx > 1:
+                return self.grid.div(f1, z, z)
+            if self.ny > 1:
+                return self.grid.div(z, f1, z)
+            if self.nz > 1:
+                return self.grid.div(z, z, f1)
+            return 0.0
+        if f3 is None:
+            if self.nx > 1 and self.ny > 1:
+                return self.grid.div(f1, f2, z)
+            if self.nz > 1 and self.ny > 1:
+                return self.grid.div(z, f1, f2)
+            if self.nz > 1 and self.nx > 1:
+                return self.grid.div(f1, z, f2)
+            if self.nx > 1:
+                return self.grid.div(f1, z, z)
+            if self.ny > 1:
+                return self.grid.div(z, f1, z)
+            if self.nz > 1:
+                return self.grid.div(z, z, f1)
+            return 0.0
+        return self.grid.div(f1, f2, f3)
+
+    def grad(self, v):
+        return list(self.grid.grad(v))
+
+    def ring(self, v):
+        return self.grid.ring(v, 2)
+
+    def ringV(self, vx, vy, vz):
+        return self.grid.ringv(vx, vy, vz, 1)
+
+    def filter(self, v):
+        return self.grid.sfilter(v)
+
+    def gfilter(self, v):
+        return self.grid.gfilter(v)
+
+    def gfilterx(self, v):
+        return self.grid.gfilterdir(v, 0)
+
+    def gfiltery(self, v):
+        return self.grid.gfilterdir(v, 1)
+
+    def gfilterz(self, v):
+        return self.grid.gfilterdir(v, 2)
+
+    def _addvar(self, name):
+        if name not in self.variables:
+            v = _Var(name)
+            v.data = self.emptyScalar()
+            self.variables[name] = v
+
+    # pyranda.py:231-285
+    def EOM(self, eom, eomDict=None):
+        if eomDict:
+            for item in eomDict:
+                eom = eom.replace(item, str(eomDict[item]))
+        lines = [el for el in eom.split("\n") if el]
+        lines = [el for el in lines if el.strip()[0] != "#"]
+        names = []
+        for eq in lines:
+            names += find_var(eq, "scalar")
+        for n in sorted(set(names)):
+            self._addvar(n)
+        for eq in lines:
+            peq = _Eq(eq, self.sMap)
+            self.equations.append(peq)
+            if peq.kind == "PDE":
+                self.nPDE += 1
+                self.conserved.append(peq.LHS[0])
+
+    # pyranda.py:305-370
+    def setIC(self, ics, icDict=None):
+        if icDict:
+            for item in icDict:
+                ics = ics.replace(item, str(icDict[item]))
+        lines = split_lines(ics)
+        names = []
+        for eq in lines:
+            names += find_var(eq, "scalar")
+        for n in sorted(set(names)):
+            self._addvar(n)
+        ns = {"self": self}
+        for ic in lines:
+            exec(fortran3d(ic, self.sMap), _EVAL_GLOBALS, ns)
+        self.updateVars()
+
+    def updateFlux(self):
+        flux = {}
+        for eq in self.equations:
+            if eq.kind == "PDE":
+                flux[eq.LHS[0]] = eq.RHS(self)
+        return flux
+
+    def updateVars(self):
+        for eq in self.equations:
+            if eq.kind != "ALG":
+                continue
+            rhs = eq.RHS(self)
+            if not eq.LHS:
+                continue
+            if eq.rank == 1:
+                self.variables[eq.LHS[0]].data = rhs
+            else:
+                for ii in range(len(rhs)):
+                    self.variables[eq.LHS[ii]].data = rhs[ii]
+
+    # pyranda.py:758-810: Carpenter-Kennedy LSRK(5,4), ALG update after every stage
+    ARK = [0.0, -6234157559845. / 12983515589748., -6194124222391. / 4410992767914.,
+           -31623096876824. / 15682348800105., -12251185447671. / 11596622555746.]
+    BRK = [494393426753. / 4806282396855., 4047970641027. / 5463924506627.,
+           9795748752853. / 13190207949281., 4009051133189. / 8539092990294.,
+           1348533437543. / 7166442652324.]
+    ETA = [494393426753. / 4806282396855., 4702696611523. / 9636871101405.,
+           3614488396635. / 5249666457482., 9766892798963. / 10823461281321., 1.0]
+
+    def rk4(self, time, dt):
+        phi = {U: numpy.zeros(self.shape, order="F") for U in self.conserved}
+        time_i = time
+        self.deltat = dt
+        for ii in range(5):
+            flux = self.updateFlux()
+            for U in self.conserved:
+                tmp1 = self.ARK[ii] * phi[U]
+                phi[U] = dt * flux[U] + tmp1
+                tmp2 = self.BRK[ii] * phi[U]
+                self.variables[U].data = self.variables[U].data + tmp2
+            time = time_i + self.ETA[ii] * dt
+            self.time = time
+            self.updateVars()
+        self.cycle += 1
+        return time

@@ -1,0 +1,705 @@
+// ORACLE — test infrastructure only.
+//
+// A plain FP64 CPU restatement of pyranda's parcop compact-operator path, used
+// by the test-suite as the checker for the CUDA library, by smoke() as the
+// reference answer, and by bench.py as the timed CPU baseline.  Nothing in the
+// product links or calls this file.
+//
+// Every routine names the reference Fortran it restates (paths relative to the
+// pyranda project).  The arithmetic follows the reference loop by loop (same
+// operand order, same summation grouping) so that results agree to rounding.
+//
+// Scope: Cartesian meshes, np = 1 (no MPI decomposition), boundary codes
+// PERI (periodic) and NONE (one-sided closures, mbc = 0).
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Weight tables: pyranda/parcop/stencils.f90
+// Rows are stored 0-based: alb1[j][l] is Fortran alb1(l+1, j+1, 0).
+// ---------------------------------------------------------------------------
+struct Weight {
+  int nol, nor, ncl, ncr, nbc1, nbc2, null_option;
+  bool implicit_op;
+  double ali[5], ari[9];
+  double alb1[4][5], alb2[4][5], arb1[4][9], arb2[4][9];
+};
+
+void mirror_rows(Weight& w, double rsign) {
+  // alb2(:,j) = alb1(ncl:1:-1, 5-j) ; arb2(:,j) = rsign*arb1(ncr:1:-1, 5-j)
+  for (int j = 0; j < 4; j++) {
+    for (int l = 0; l < w.ncl; l++) w.alb2[j][l] = w.alb1[3 - j][w.ncl - 1 - l];
+    for (int l = 0; l < w.ncr; l++) w.arb2[j][l] = rsign * w.arb1[3 - j][w.ncr - 1 - l];
+  }
+}
+
+// c10d1: stencils.f90:207-277 (interior :236-237, one-sided rows :239-254)
+Weight make_c10d1() {
+  Weight w{};
+  w.nol = 2; w.nor = 3; w.ncl = 5; w.ncr = 7; w.nbc1 = 4; w.nbc2 = 4;
+  w.null_option = 0; w.implicit_op = true;
+  const double ali[5] = {0.45, 4.5, 9.0, 4.5, 0.45};
+  const double ari[7] = {-0.015, -1.515, -6.375, 0.0, 6.375, 1.515, 0.015};
+  std::memcpy(w.ali, ali, sizeof ali); std::memcpy(w.ari, ari, sizeof ari);
+  const double alb1[4][5] = {{0.0, 0.0, 4.725, 9.45, 0.0},
+                             {0.0, 1.94578125, 7.783125, 1.94578125, 0.0},
+                             {0.2964375, 4.743, 10.67175, 4.743, 0.2964375},
+                             {0.451390625, 4.63271875, 9.38146875, 4.63271875, 0.451390625}};
+  const double arb1[4][7] = {{0.0, 0.0, 0.0, -11.8125, 9.45, 2.3625, 0.0},
+                             {0.0, 0.0, -5.83734375, 0.0, 5.83734375, 0.0, 0.0},
+                             {0.0, -1.23515625, -7.905, 0.0, 7.905, 1.23515625, 0.0},
+                             {-0.015, -1.53, -6.66984375, 0.0, 6.66984375, 1.53, 0.015}};
+  for (int j = 0; j < 4; j++) {
+    for (int l = 0; l < 5; l++) w.alb1[j][l] = alb1[j][l];
+    for (int l = 0; l < 7; l++) w.arb1[j][l] = arb1[j][l];
+  }
+  mirror_rows(w, -1.0);
+  return w;
+}
+
+// c10d8: stencils.f90:515-621 (interior :519-526,:573-574, one-sided :576-591)
+Weight make_c10d8() {
+  Weight w{};
+  w.nol = 2; w.nor = 4; w.ncl = 5; w.ncr = 9; w.nbc1 = 4; w.nbc2 = 4;
+  w.null_option = 0; w.implicit_op = true;
+  const double zeta = 29.0, alpha = 14.0, beta = 1.5;
+  const double aa = 4200.0, bb = -3360.0, cc = 1680.0, dd = -480.0, ee = 60.0;
+  const double alpha2 = beta + alpha, zeta1 = alpha + zeta, alpha1 = beta + alpha;
+  const double dd4 = ee + dd, cc3 = dd + cc, bb3 = ee + bb, bb2 = cc + bb, aa2 = dd + aa,
+               b22 = ee + bb, aa1 = bb + aa, bb1 = cc + bb, cc1 = dd + cc, dd1 = ee + dd;
+  const double ali[5] = {beta, alpha, zeta, alpha, beta};
+  const double ari[9] = {ee, dd, cc, bb, aa, bb, cc, dd, ee};
+  std::memcpy(w.ali, ali, sizeof ali); std::memcpy(w.ari, ari, sizeof ari);
+  const double alb1[4][5] = {{0.0, 0.0, zeta1, alpha1, beta},
+                             {0.0, alpha2, zeta, alpha, beta},
+                             {beta, alpha, zeta, alpha, beta},
+                             {beta, alpha, zeta, alpha, beta}};
+  const double arb1[4][9] = {{0.0, 0.0, 0.0, 0.0, aa1, bb1, cc1, dd1, ee},
+                             {0.0, 0.0, 0.0, bb2, aa2, b22, cc, dd, ee},
+                             {0.0, 0.0, cc3, bb3, aa, bb, cc, dd, ee},
+                             {0.0, dd4, cc, bb, aa, bb, cc, dd, ee}};
+  for (int j = 0; j < 4; j++) {
+    for (int l = 0; l < 5; l++) w.alb1[j][l] = alb1[j][l];
+    for (int l = 0; l < 9; l++) w.arb1[j][l] = arb1[j][l];
+  }
+  mirror_rows(w, 1.0);
+  return w;
+}
+
+// c8ff8 (sfspec = 2): stencils.f90:713-835, stored as RHS - LHS (:832-834)
+Weight make_c8ff8() {
+  Weight w{};
+  w.nol = 2; w.nor = 4; w.ncl = 5; w.ncr = 9; w.nbc1 = 4; w.nbc2 = 4;
+  w.null_option = 1; w.implicit_op = true;
+  const double beta = 1.6688e-1, alpha = 6.6624e-1, zeta = 1.0;
+  const double aa = 9.9965e-1, bb = 6.6652e-1, cc = 1.6674e-1, dd = 4.0e-5, ee = -5.0e-6;
+  const double ali[5] = {beta, alpha, zeta, alpha, beta};
+  const double ari[9] = {ee, dd, cc, bb, aa, bb, cc, dd, ee};
+  std::memcpy(w.ali, ali, sizeof ali); std::memcpy(w.ari, ari, sizeof ari);
+  const double alb1[4][5] = {{0.0, 0.0, 1.0, 0.0, 0.0},
+                             {0.0, 4.997e-1, 1.0, 4.997e-1, 0.0},
+                             {1.6688e-1, 6.6624e-1, 1.0, 6.6624e-1, 1.6688e-1},
+                             {1.6688e-1, 6.6624e-1, 1.0, 6.6624e-1, 1.6688e-1}};
+  const double arb1[4][9] = {
+      {0.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 0.0},
+      {0.0, 0.0, 0.0, 4.9985e-1, 9.997e-1, 4.9985e-1, 0.0, 0.0, 0.0},
+      {0.0, 0.0, 1.668e-1, 6.6656e-1, 9.9952e-1, 6.6656e-1, 1.668e-1, 0.0, 0.0},
+      {0.0, 4.0e-5, 1.6672e-1, 6.6652e-1, 9.9968e-1, 6.6652e-1, 1.6672e-1, 4.0e-5, 0.0}};
+  for (int j = 0; j < 4; j++) {
+    for (int l = 0; l < 5; l++) w.alb1[j][l] = alb1[j][l];
+    for (int l = 0; l < 9; l++) w.arb1[j][l] = arb1[j][l];
+  }
+  mirror_rows(w, 1.0);
+  // difference form: ari(3:7) -= ali(1:5), same for the boundary rows
+  for (int l = 0; l < 5; l++) w.ari[2 + l] -= w.ali[l];
+  for (int j = 0; j < 4; j++)
+    for (int l = 0; l < 5; l++) {
+      w.arb1[j][2 + l] -= w.alb1[j][l];
+      w.arb2[j][2 + l] -= w.alb2[j][l];
+    }
+  return w;
+}
+
+// cgfs4 (gfspec = 6): stencils.f90:1387-1476, explicit, difference form (:1472-1475)
+Weight make_cgfs4() {
+  Weight w{};
+  w.nol = 0; w.nor = 4; w.ncl = 1; w.ncr = 9; w.nbc1 = 4; w.nbc2 = 4;
+  w.null_option = 1; w.implicit_op = false;
+  const double agau = 3565.0 / 10368.0, bgau = 3091.0 / 12960.0, cgau = 1997.0 / 25920.0,
+               dgau = 149.0 / 12960.0, egau = 107.0 / 103680.0;
+  const double dg14 = dgau + egau, cg13 = cgau + dgau, bg23 = bgau + egau, bg12 = bgau + cgau,
+               ag22 = agau + dgau, bg32 = bgau + egau, ag11 = agau + bgau, bg21 = bgau + cgau,
+               cg31 = cgau + dgau, dg41 = dgau + egau;
+  w.ali[0] = 1.0;
+  const double ari[9] = {egau, dgau, cgau, bgau, agau, bgau, cgau, dgau, egau};
+  std::memcpy(w.ari, ari, sizeof ari);
+  const double arb1[4][9] = {{0.0, 0.0, 0.0, 0.0, ag11, bg21, cg31, dg41, egau},
+                             {0.0, 0.0, 0.0, bg12, ag22, bg32, cgau, dgau, egau},
+                             {0.0, 0.0, cg13, bg23, agau, bgau, cgau, dgau, egau},
+                             {0.0, dg14, cgau, bgau, agau, bgau, cgau, dgau, egau}};
+  for (int j = 0; j < 4; j++) {
+    w.alb1[j][0] = 1.0;
+    for (int l = 0; l < 9; l++) w.arb1[j][l] = arb1[j][l];
+  }
+  mirror_rows(w, 1.0);
+  w.ari[4] -= w.ali[0];
+  for (int j = 0; j < 4; j++) {
+    w.arb1[j][4] -= w.alb1[j][0];
+    w.arb2[j][4] -= w.alb2[j][0];
+  }
+  return w;
+}
+
+// ---------------------------------------------------------------------------
+// One operator along one direction: compact_basetype.f90:65-209 (np = 1)
+// ---------------------------------------------------------------------------
+struct Op1 {
+  bool null_op = true, periodic = false, implicit_op = false;
+  int kind = 0;  // 1 = d1 evaluator (compact_d1.f90), 4 = r4 evaluator (compact_r4.f90)
+  int null_option = 0, n = 0, nal = 0;
+  std::vector<double> al;  // al(i, c) -> al[(c-1)*n + (i-1)], factored
+  std::vector<double> ar;  // ar(l, i) -> ar[(i-1)*ncr + (l-1)]
+  int ncr = 0;
+  double& AL(int i, int c) { return al[(size_t)(c - 1) * n + (i - 1)]; }
+  double AL(int i, int c) const { return al[(size_t)(c - 1) * n + (i - 1)]; }
+  double AR(int l, int i) const { return ar[(size_t)(i - 1) * ncr + (l - 1)]; }
+};
+
+// bpentLUD1: pentadiagonal.f90:18-39
+void bpentLUD1(Op1& o) {
+  const int n = o.n;
+  for (int i = 1; i <= n - 2; i++) {
+    o.AL(i + 1, 2) = o.AL(i + 1, 2) / o.AL(i, 3);
+    o.AL(i + 1, 3) = o.AL(i + 1, 3) - o.AL(i, 4) * o.AL(i + 1, 2);
+    o.AL(i + 1, 4) = o.AL(i + 1, 4) - o.AL(i, 5) * o.AL(i + 1, 2);
+    o.AL(i + 2, 1) = o.AL(i + 2, 1) / o.AL(i, 3);
+    o.AL(i + 2, 2) = o.AL(i + 2, 2) - o.AL(i, 4) * o.AL(i + 2, 1);
+    o.AL(i + 2, 3) = o.AL(i + 2, 3) - o.AL(i, 5) * o.AL(i + 2, 1);
+  }
+  o.AL(n, 2) = o.AL(n, 2) / o.AL(n - 1, 3);
+  o.AL(n, 3) = o.AL(n, 3) - o.AL(n - 1, 4) * o.AL(n, 2);
+  for (int i = 1; i <= n; i++) o.AL(i, 3) = 1.0 / o.AL(i, 3);
+}
+
+// ppentLUD1: pentadiagonal.f90:64-135 (cyclic pentadiagonal, bordered LU)
+void ppentLUD1(Op1& o) {
+  const int N = o.n;
+  auto c = [&](int i, int j) -> double& { return o.AL(i, j); };
+  const double one = 1.0;
+  c(1, 8) = c(1, 1);
+  c(1, 9) = c(1, 2);
+  c(1, 3) = one / c(1, 3);
+  c(1, 6) = c(N - 1, 5) * c(1, 3);
+  c(1, 7) = c(N, 4) * c(1, 3);
+  c(2, 2) = c(2, 2) * c(1, 3);
+  c(2, 3) = c(2, 3) - c(2, 2) * c(1, 4);
+  c(2, 4) = c(2, 4) - c(2, 2) * c(1, 5);
+  c(2, 8) = -c(2, 2) * c(1, 8);
+  c(2, 9) = c(2, 1) - c(2, 2) * c(1, 9);
+  c(2, 3) = one / c(2, 3);
+  c(2, 6) = -c(1, 6) * c(1, 4) * c(2, 3);
+  c(2, 7) = (c(N, 5) - c(1, 7) * c(1, 4)) * c(2, 3);
+  for (int K = 3; K <= N - 4; K++) {
+    c(K, 1) = c(K, 1) * c(K - 2, 3);
+    c(K, 2) = (c(K, 2) - c(K, 1) * c(K - 2, 4)) * c(K - 1, 3);
+    c(K, 3) = c(K, 3) - (c(K, 2) * c(K - 1, 4) + c(K, 1) * c(K - 2, 5));
+    c(K, 4) = c(K, 4) - c(K, 2) * c(K - 1, 5);
+    c(K, 8) = -(c(K, 2) * c(K - 1, 8) + c(K, 1) * c(K - 2, 8));
+    c(K, 9) = -(c(K, 2) * c(K - 1, 9) + c(K, 1) * c(K - 2, 9));
+    c(K, 3) = one / c(K, 3);
+    c(K, 6) = -(c(K - 1, 6) * c(K - 1, 4) + c(K - 2, 6) * c(K - 2, 5)) * c(K, 3);
+    c(K, 7) = -(c(K - 1, 7) * c(K - 1, 4) + c(K - 2, 7) * c(K - 2, 5)) * c(K, 3);
+  }
+  c(N - 3, 1) = c(N - 3, 1) * c(N - 5, 3);
+  c(N - 3, 2) = (c(N - 3, 2) - c(N - 3, 1) * c(N - 5, 4)) * c(N - 4, 3);
+  c(N - 3, 3) = c(N - 3, 3) - (c(N - 3, 2) * c(N - 4, 4) + c(N - 3, 1) * c(N - 5, 5));
+  c(N - 3, 4) = c(N - 3, 4) - c(N - 3, 2) * c(N - 4, 5);
+  c(N - 3, 8) = c(N - 3, 5) - (c(N - 3, 2) * c(N - 4, 8) + c(N - 3, 1) * c(N - 5, 8));
+  c(N - 3, 9) = -(c(N - 3, 2) * c(N - 4, 9) + c(N - 3, 1) * c(N - 5, 9));
+  c(N - 3, 3) = one / c(N - 3, 3);
+  c(N - 3, 6) = (c(N - 1, 1) - (c(N - 4, 6) * c(N - 4, 4) + c(N - 5, 6) * c(N - 5, 5))) * c(N - 3, 3);
+  c(N - 3, 7) = -(c(N - 4, 7) * c(N - 4, 4) + c(N - 5, 7) * c(N - 5, 5)) * c(N - 3, 3);
+  c(N - 2, 1) = c(N - 2, 1) * c(N - 4, 3);
+  c(N - 2, 2) = (c(N - 2, 2) - c(N - 2, 1) * c(N - 4, 4)) * c(N - 3, 3);
+  c(N - 2, 3) = c(N - 2, 3) - (c(N - 2, 2) * c(N - 3, 4) + c(N - 2, 1) * c(N - 4, 5));
+  c(N - 2, 8) = c(N - 2, 4) - (c(N - 2, 2) * c(N - 3, 8) + c(N - 2, 1) * c(N - 4, 8));
+  c(N - 2, 9) = c(N - 2, 5) - (c(N - 2, 2) * c(N - 3, 9) + c(N - 2, 1) * c(N - 4, 9));
+  c(N - 2, 3) = one / c(N - 2, 3);
+  c(N - 2, 6) = (c(N - 1, 2) - c(N - 3, 6) * c(N - 3, 4) - c(N - 4, 6) * c(N - 4, 5)) * c(N - 2, 3);
+  c(N - 2, 7) = (c(N, 1) - c(N - 3, 7) * c(N - 3, 4) - c(N - 4, 7) * c(N - 4, 5)) * c(N - 2, 3);
+  for (int K = 1; K <= N - 2; K++) {
+    c(N - 1, 3) = c(N - 1, 3) - c(K, 6) * c(K, 8);
+    c(N - 1, 4) = c(N - 1, 4) - c(K, 6) * c(K, 9);
+  }
+  c(N - 1, 9) = c(N - 1, 4);
+  for (int K = 1; K <= N - 2; K++) c(N, 2) = c(N, 2) - c(K, 7) * c(K, 8);
+  c(N - 1, 3) = one / c(N - 1, 3);
+  c(N - 1, 7) = c(N, 2) * c(N - 1, 3);
+  for (int K = 1; K <= N - 1; K++) c(N, 3) = c(N, 3) - c(K, 7) * c(K, 9);
+  c(N, 3) = one / c(N, 3);
+}
+
+// setup_compact_op1: compact_basetype.f90:65-170 for np = 1
+Op1 setup_op(const Weight& w, int kind, int n, bool periodic) {
+  Op1 o;
+  o.kind = kind;
+  o.n = n;
+  o.periodic = periodic;
+  o.null_option = w.null_option;
+  o.implicit_op = w.implicit_op;
+  o.ncr = w.ncr;
+  o.null_op = (n < 4);  // compact.f90:95-97, compact_basetype.f90:100-104
+  if (o.null_op) return o;
+  o.nal = periodic ? w.ncl + 4 : w.ncl;
+  // gal(1:ncl, i) = ali, gar(:, i) = ari; one-sided rows patched at the ends
+  std::vector<double> gal((size_t)o.nal * n, 0.0), gar((size_t)w.ncr * n, 0.0);
+  for (int i = 0; i < n; i++) {
+    for (int l = 0; l < w.ncl; l++) gal[(size_t)i * o.nal + l] = w.ali[l];
+    for (int l = 0; l < w.ncr; l++) gar[(size_t)i * w.ncr + l] = w.ari[l];
+  }
+  if (!periodic) {
+    for (int j = 0; j < w.nbc1; j++) {
+      for (int l = 0; l < w.ncl; l++) gal[(size_t)j * o.nal + l] = w.alb1[j][l];
+      for (int l = 0; l < w.ncr; l++) gar[(size_t)j * w.ncr + l] = w.arb1[j][l];
+    }
+    for (int j = 0; j < w.nbc2; j++) {
+      const int i = n - w.nbc2 + j;
+      for (int l = 0; l < w.ncl; l++) gal[(size_t)i * o.nal + l] = w.alb2[j][l];
+      for (int l = 0; l < w.ncr; l++) gar[(size_t)i * w.ncr + l] = w.arb2[j][l];
+    }
+  }
+  o.al.assign((size_t)n * o.nal, 0.0);
+  for (int i = 1; i <= n; i++)
+    for (int c = 1; c <= o.nal; c++) o.AL(i, c) = gal[(size_t)(i - 1) * o.nal + (c - 1)];
+  o.ar = gar;
+  if (o.implicit_op) {
+    if (periodic) ppentLUD1(o);
+    else bpentLUD1(o);
+  }
+  return o;
+}
+
+// ---------------------------------------------------------------------------
+// Line evaluators.  v and dv are 1-based views of one line (v[1..n]).
+// ---------------------------------------------------------------------------
+
+// d1 RHS: compact_d1.f90:100-193 (periodic halo or one-sided bc = 0 ends)
+void rhs_d1(const Op1& o, const double* v, double* dv) {
+  const int ax = o.n;
+  auto a = [&](int l, int i) { return o.AR(l, i); };
+  if (o.periodic) {
+    // vbr1(1:3) = v(ax-2:ax), vbr2(1:3) = v(1:3)  (:100-110)
+    const double b11 = v[ax - 2], b12 = v[ax - 1], b13 = v[ax];
+    const double b21 = v[1], b22 = v[2], b23 = v[3];
+    dv[1] = a(5, 1) * (v[2] - b13) + a(6, 1) * (v[3] - b12) + a(7, 1) * (v[4] - b11);
+    dv[2] = a(5, 2) * (v[3] - v[1]) + a(6, 2) * (v[4] - b13) + a(7, 2) * (v[5] - b12);
+    dv[3] = a(5, 3) * (v[4] - v[2]) + a(6, 3) * (v[5] - v[1]) + a(7, 3) * (v[6] - b13);
+    for (int i = 4; i <= ax - 3; i++)
+      dv[i] = a(5, i) * (v[i + 1] - v[i - 1]) + a(6, i) * (v[i + 2] - v[i - 2]) + a(7, i) * (v[i + 3] - v[i - 3]);
+    dv[ax - 2] = a(5, ax - 2) * (v[ax - 1] - v[ax - 3]) + a(6, ax - 2) * (v[ax] - v[ax - 4]) + a(7, ax - 2) * (b21 - v[ax - 5]);
+    dv[ax - 1] = a(5, ax - 1) * (v[ax] - v[ax - 2]) + a(6, ax - 1) * (b21 - v[ax - 3]) + a(7, ax - 1) * (b22 - v[ax - 4]);
+    dv[ax] = a(5, ax) * (b21 - v[ax - 1]) + a(6, ax) * (b22 - v[ax - 2]) + a(7, ax) * (b23 - v[ax - 3]);
+    return;
+  }
+  // one-sided, bc = 0  (:131-139, :175-183)
+  {
+    double s = 0.0;
+    for (int l = 5; l <= 7; l++) s += a(l, 1) * (v[l - 3] - v[1]);
+    dv[1] = s;
+    s = 0.0;
+    for (int l = 4; l <= 7; l++) s += a(l, 2) * (v[l - 2] - v[1]);
+    dv[2] = s;
+    dv[3] = a(5, 3) * (v[4] - v[2]) + a(6, 3) * (v[5] - v[1]) + a(7, 3) * (v[6] - v[1]);
+  }
+  for (int i = 4; i <= ax - 3; i++)
+    dv[i] = a(5, i) * (v[i + 1] - v[i - 1]) + a(6, i) * (v[i + 2] - v[i - 2]) + a(7, i) * (v[i + 3] - v[i - 3]);
+  {
+    dv[ax - 2] = a(1, ax - 2) * (v[ax - 5] - v[ax]) + a(2, ax - 2) * (v[ax - 4] - v[ax]) + a(3, ax - 2) * (v[ax - 3] - v[ax - 1]);
+    double s = 0.0;
+    for (int l = 1; l <= 4; l++) s += a(l, ax - 1) * (v[ax - 5 + l] - v[ax]);
+    dv[ax - 1] = s;
+    s = 0.0;
+    for (int l = 1; l <= 3; l++) s += a(l, ax) * (v[ax - 4 + l] - v[ax]);
+    dv[ax] = s;
+  }
+}
+
+// r4 RHS: compact_r4.f90:77-193 (9-point difference form)
+void rhs_r4(const Op1& o, const double* v, double* dv) {
+  const int ax = o.n;
+  auto a = [&](int l, int i) { return o.AR(l, i); };
+  if (o.periodic) {
+    // vbr1(1:4) = v(ax-3:ax), vbr2(1:4) = v(1:4)  (:97-104)
+    double b1[5], b2[5];
+    for (int q = 1; q <= 4; q++) { b1[q] = v[ax - 4 + q]; b2[q] = v[q]; }
+    for (int i = 1; i <= 4; i++) {
+      // sum(ar(1:5-i,i)*(vbr1(i:4)-v(i))) + sum(ar(6-i:9,i)*(v(1:4+i)-v(i)))
+      double s1 = 0.0, s2 = 0.0;
+      for (int l = 1; l <= 5 - i; l++) s1 += a(l, i) * (b1[i - 1 + l] - v[i]);
+      for (int l = 6 - i; l <= 9; l++) s2 += a(l, i) * (v[l + i - 5] - v[i]);
+      dv[i] = s1 + s2;
+    }
+  } else {
+    for (int i = 1; i <= 4; i++) {
+      // sum(ar(7-i:9,i)*(v(2:4+i)-v(1)))  (:120-125)
+      double s = 0.0;
+      for (int l = 7 - i; l <= 9; l++) s += a(l, i) * (v[l + i - 5] - v[1]);
+      dv[i] = s;
+    }
+  }
+  for (int i = 5; i <= ax - 4; i++) {
+    double s = 0.0;
+    const double vc = v[i];
+    for (int l = 1; l <= 9; l++) s = s + (v[l + i - 5] - vc) * a(l, i);
+    dv[i] = s;
+  }
+  if (o.periodic) {
+    double b2[5];
+    for (int q = 1; q <= 4; q++) b2[q] = v[q];
+    for (int q = 3; q >= 0; q--) {
+      const int i = ax - q;
+      // sum(ar(1:5+q,i)*(v(i-4:ax)-v(i))) + sum(ar(6+q:9,i)*(vbr2(1:4-q)-v(i)))  (:180-189)
+      double s1 = 0.0, s2 = 0.0;
+      for (int l = 1; l <= 5 + q; l++) s1 += a(l, i) * (v[i - 5 + l] - v[i]);
+      for (int l = 6 + q; l <= 9; l++) s2 += a(l, i) * (b2[l - 5 - q] - v[i]);
+      dv[i] = s1 + s2;
+    }
+  } else {
+    for (int q = 3; q >= 0; q--) {
+      const int i = ax - q;
+      // sum(ar(1:4+q,i)*(v(i-4:ax-1)-v(ax)))  (:166-171)
+      double s = 0.0;
+      for (int l = 1; l <= 4 + q; l++) s += a(l, i) * (v[i - 5 + l] - v[ax]);
+      dv[i] = s;
+    }
+  }
+}
+
+// bpentLUS3x for one line: pentadiagonal.f90:629-651
+void solve_b(const Op1& o, double* r) {
+  const int n = o.n;
+  for (int i = 1; i <= n - 2; i++) {
+    r[i + 1] = r[i + 1] - r[i] * o.AL(i + 1, 2);
+    r[i + 2] = r[i + 2] - r[i] * o.AL(i + 2, 1);
+  }
+  r[n] = (r[n] - r[n - 1] * o.AL(n, 2)) * o.AL(n, 3);
+  r[n - 1] = (r[n - 1] - o.AL(n - 1, 4) * r[n]) * o.AL(n - 1, 3);
+  for (int i = n - 2; i >= 1; i--)
+    r[i] = (r[i] - o.AL(i, 4) * r[i + 1] - o.AL(i, 5) * r[i + 2]) * o.AL(i, 3);
+}
+
+// ppentLUS3x for one line: pentadiagonal.f90:654-684
+void solve_p(const Op1& o, double* r) {
+  const int N = o.n;
+  auto c = [&](int i, int j) { return o.AL(i, j); };
+  r[2] = r[2] - c(2, 2) * r[1];
+  double tmp1 = c(1, 6) * r[1] + c(2, 6) * r[2];
+  double tmp2 = c(1, 7) * r[1] + c(2, 7) * r[2];
+  for (int i = 3; i <= N - 2; i++) {
+    r[i] = r[i] - (c(i, 2) * r[i - 1] + c(i, 1) * r[i - 2]);
+    tmp1 = tmp1 + c(i, 6) * r[i];
+    tmp2 = tmp2 + c(i, 7) * r[i];
+  }
+  r[N - 1] = r[N - 1] - tmp1;
+  r[N] = (r[N] - tmp2 - c(N - 1, 7) * r[N - 1]) * c(N, 3);
+  r[N - 1] = (r[N - 1] - c(N - 1, 9) * r[N]) * c(N - 1, 3);
+  r[N - 2] = (r[N - 2] - c(N - 2, 8) * r[N - 1] - c(N - 2, 9) * r[N]) * c(N - 2, 3);
+  r[N - 3] = (r[N - 3] - (c(N - 3, 4) * r[N - 2] + c(N - 3, 8) * r[N - 1] + c(N - 3, 9) * r[N])) * c(N - 3, 3);
+  for (int i = N - 4; i >= 1; i--)
+    r[i] = (r[i] - (c(i, 4) * r[i + 1] + c(i, 5) * r[i + 2] + c(i, 8) * r[N - 1] + c(i, 9) * r[N])) * c(i, 3);
+}
+
+// Full line evaluation (eval_compact_op1x_d1 / _r4), np = 1, then the d1 metric scale
+// (compact_operators.f90:41-46) when scale != 0.
+void eval_line(const Op1& o, const double* v, double* dv, double scale) {
+  if (o.kind == 1) rhs_d1(o, v, dv);
+  else rhs_r4(o, v, dv);
+  if (o.implicit_op) {
+    if (o.periodic) solve_p(o, dv);
+    else solve_b(o, dv);
+  }
+  if (o.null_option == 1)
+    for (int i = 1; i <= o.n; i++) dv[i] = dv[i] + v[i];
+  if (scale != 0.0)
+    for (int i = 1; i <= o.n; i++) dv[i] = dv[i] / scale;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Handle: one grid (one pyranda patch), all operators for x, y, z.
+// ---------------------------------------------------------------------------
+struct og_handle {
+  int n[3];
+  int periodic[3];
+  double d[3];     // patch spacing dx, dy, dz (patch.f90:83-85)
+  double dmesh[3]; // mesh d1, d2, d3 (mesh.f90:192-209)
+  double x1f[3];   // lower face coordinates (parcop.f90:51-56)
+  Op1 d1[3], d8[3], sf[3], gf[3];
+};
+
+namespace {
+
+enum { OP_D1 = 0, OP_D8 = 1, OP_SF = 2, OP_GF = 3 };
+
+const Op1& pick(const og_handle* h, int op, int dir) {
+  switch (op) {
+    case OP_D1: return h->d1[dir];
+    case OP_D8: return h->d8[dir];
+    case OP_SF: return h->sf[dir];
+    default: return h->gf[dir];
+  }
+}
+
+// Apply one operator along direction dir over a Fortran-ordered (nx,ny,nz) field.
+// Null ops follow compact_operators.f90: derivatives give 0 (:24-29, :288-294),
+// filters copy (:396-401).
+void apply_dir(const og_handle* h, int op, int dir, const double* in, double* out) {
+  const int nx = h->n[0], ny = h->n[1], nz = h->n[2];
+  const size_t npts = (size_t)nx * ny * nz;
+  const Op1& o = pick(h, op, dir);
+  if (o.null_op) {
+    if (op == OP_SF || op == OP_GF) std::memcpy(out, in, npts * sizeof(double));
+    else std::memset(out, 0, npts * sizeof(double));
+    return;
+  }
+  const double scale = (op == OP_D1) ? h->d[dir] : 0.0;
+  const int n = h->n[dir];
+  size_t stride, nlines;
+  if (dir == 0) { stride = 1; nlines = (size_t)ny * nz; }
+  else if (dir == 1) { stride = nx; nlines = (size_t)nx * nz; }
+  else { stride = (size_t)nx * ny; nlines = (size_t)nx * ny; }
+  const int B = 8;  // lines gathered together for the strided directions
+  const long nblk = (long)((nlines + B - 1) / B);
+#pragma omp parallel
+  {
+    std::vector<double> vb((size_t)B * (n + 1)), db((size_t)B * (n + 1));
+#pragma omp for schedule(static)
+    for (long blk = 0; blk < nblk; blk++) {
+      const size_t l0 = (size_t)blk * B;
+      const int nb = (int)std::min<size_t>(B, nlines - l0);
+      size_t base[8];
+      for (int b = 0; b < nb; b++) {
+        const size_t L = l0 + b;
+        if (dir == 0) base[b] = L * nx;
+        else if (dir == 1) base[b] = (L / nx) * (size_t)nx * ny + (L % nx);
+        else base[b] = L;
+      }
+      for (int i = 0; i < n; i++)
+        for (int b = 0; b < nb; b++) vb[(size_t)b * (n + 1) + i + 1] = in[base[b] + i * stride];
+      for (int b = 0; b < nb; b++) eval_line(o, &vb[(size_t)b * (n + 1)], &db[(size_t)b * (n + 1)], scale);
+      for (int i = 0; i < n; i++)
+        for (int b = 0; b < nb; b++) out[base[b] + i * stride] = db[(size_t)b * (n + 1) + i + 1];
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+// parcop.f90:23-61 (setup: node extents -> faces) + patch.f90:83-85 + mesh.f90:169-211
+int og_create(const int* n, const int* periodic, const double* x1, const double* xn, og_handle** out) {
+  if (!n || !periodic || !x1 || !xn || !out) return 1;
+  og_handle* h = new og_handle();
+  for (int d = 0; d < 3; d++) {
+    if (n[d] < 1) { delete h; return 1; }
+    h->n[d] = n[d];
+    h->periodic[d] = periodic[d] ? 1 : 0;
+    const double dn = (xn[d] - x1[d]) / (double)std::max(n[d] - 1, 1);
+    const double f1 = x1[d] - dn / 2.0, fn = xn[d] + dn / 2.0;
+    h->x1f[d] = f1;
+    h->d[d] = (fn - f1) / (double)n[d];
+  }
+  for (int d = 0; d < 3; d++) {
+    if (h->n[d] == 1) {
+      const int a = (d + 1) % 3, b = (d + 2) % 3;
+      const int lo = std::min(a, b), hi = std::max(a, b);
+      h->dmesh[d] = std::max(h->d[lo], h->d[hi]);
+    } else {
+      h->dmesh[d] = h->d[d];
+    }
+  }
+  static const Weight wd1 = make_c10d1(), wd8 = make_c10d8(), wsf = make_c8ff8(), wgf = make_cgfs4();
+  for (int d = 0; d < 3; d++) {
+    const bool per = h->periodic[d] != 0;
+    h->d1[d] = setup_op(wd1, 1, h->n[d], per);
+    h->d8[d] = setup_op(wd8, 4, h->n[d], per);
+    h->sf[d] = setup_op(wsf, 4, h->n[d], per);
+    h->gf[d] = setup_op(wgf, 4, h->n[d], per);
+  }
+  *out = h;
+  return 0;
+}
+
+void og_destroy(og_handle* h) { delete h; }
+
+int og_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+void og_set_threads(int t) {
+#ifdef _OPENMP
+  if (t > 0) omp_set_num_threads(t);
+#else
+  (void)t;
+#endif
+}
+
+// op: 0 = d1 (ddx/ddy/ddz), 1 = d8 (dd8x..), 2 = compact filter c8ff8, 3 = gaussian cgfs4
+int og_apply(const og_handle* h, int op, int dir, const double* in, double* out) {
+  if (!h || op < 0 || op > 3 || dir < 0 || dir > 2) return 1;
+  apply_dir(h, op, dir, in, out);
+  return 0;
+}
+
+// sFilter / gFilter: operators.f90:848-853, :860-875 (x -> y -> z with a temporary)
+int og_filter3(const og_handle* h, int op, const double* in, double* out) {
+  if (!h || (op != 2 && op != 3)) return 1;
+  const size_t np = (size_t)h->n[0] * h->n[1] * h->n[2];
+  std::vector<double> tmp(np);
+  apply_dir(h, op, 0, in, out);
+  apply_dir(h, op, 1, out, tmp.data());
+  apply_dir(h, op, 2, tmp.data(), out);
+  return 0;
+}
+
+// ringS: operators.f90:615-643 with ringx/y/z (:701-753); L = 0, 1 or 2
+int og_ring(const og_handle* h, const double* f, double* out, int L) {
+  if (!h) return 1;
+  const size_t np = (size_t)h->n[0] * h->n[1] * h->n[2];
+  std::vector<double> r1(np), r2(np), r3(np);
+  double* rs[3] = {r1.data(), r2.data(), r3.data()};
+  for (int d = 0; d < 3; d++) {
+    if (h->n[d] == 1) std::memset(rs[d], 0, np * sizeof(double));
+    else apply_dir(h, OP_D8, d, f, rs[d]);
+  }
+  double s[3];
+  for (int d = 0; d < 3; d++) s[d] = (L == 0) ? 1.0 : (L == 1 ? h->dmesh[d] : h->dmesh[d] * h->dmesh[d]);
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < (long)np; i++) {
+    double a, b, c;
+    if (L == 0) { a = std::fabs(r1[i]); b = std::fabs(r2[i]); c = std::fabs(r3[i]); }
+    else { a = std::fabs(r1[i]) * s[0]; b = std::fabs(r2[i]) * s[1]; c = std::fabs(r3[i]) * s[2]; }
+    out[i] = std::max(std::max(a, b), c);
+  }
+  return 0;
+}
+
+// ringV: operators.f90:645-699
+int og_ringv(const og_handle* h, const double* f, const double* g, const double* q, double* out, int L) {
+  if (!h) return 1;
+  const size_t np = (size_t)h->n[0] * h->n[1] * h->n[2];
+  std::vector<double> r(9 * np);
+  const double* src[3] = {f, g, q};
+  for (int c = 0; c < 3; c++)
+    for (int d = 0; d < 3; d++) {
+      double* dst = &r[(size_t)(c * 3 + d) * np];
+      if (h->n[d] == 1) std::memset(dst, 0, np * sizeof(double));
+      else apply_dir(h, OP_D8, d, src[c], dst);
+    }
+  double s[3];
+  for (int d = 0; d < 3; d++) s[d] = (L == 0) ? 1.0 : (L == 1 ? h->dmesh[d] : h->dmesh[d] * h->dmesh[d]);
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < (long)np; i++) {
+    double m[3];
+    for (int d = 0; d < 3; d++) {
+      const double a = std::fabs(r[(size_t)(0 + d) * np + i]), b = std::fabs(r[(size_t)(3 + d) * np + i]),
+                   c = std::fabs(r[(size_t)(6 + d) * np + i]);
+      m[d] = std::max(std::max(a, b), c);
+      if (L != 0) m[d] = m[d] * s[d];
+    }
+    out[i] = std::max(std::max(m[0], m[1]), m[2]);
+  }
+  return 0;
+}
+
+// gradS (Cartesian): operators.f90:184-191
+int og_grad(const og_handle* h, const double* f, double* gx, double* gy, double* gz) {
+  if (!h) return 1;
+  apply_dir(h, OP_D1, 0, f, gx);
+  apply_dir(h, OP_D1, 1, f, gy);
+  apply_dir(h, OP_D1, 2, f, gz);
+  return 0;
+}
+
+// divV (Cartesian): operators.f90:38-53
+int og_div(const og_handle* h, const double* fx, const double* fy, const double* fz, double* out) {
+  if (!h) return 1;
+  const size_t np = (size_t)h->n[0] * h->n[1] * h->n[2];
+  std::vector<double> a(np), b(np);
+  apply_dir(h, OP_D1, 0, fx, out);
+  apply_dir(h, OP_D1, 1, fy, a.data());
+  apply_dir(h, OP_D1, 2, fz, b.data());
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < (long)np; i++) out[i] = out[i] + a[i] + b[i];
+  return 0;
+}
+
+// Mesh quantities (mesh.f90:169-211, Cartesian):
+// which = 0,1,2 -> x,y,z grid; 3,4,5 -> d1,d2,d3; 6 -> GridLen; 7 -> CellVol
+int og_mesh(const og_handle* h, int which, double* out) {
+  if (!h || which < 0 || which > 7) return 1;
+  const int nx = h->n[0], ny = h->n[1], nz = h->n[2];
+  const double gl = std::min(std::min(h->dmesh[0], h->dmesh[1]), h->dmesh[2]);
+  const double cv = h->d[0] * h->d[1] * h->d[2];
+  for (int k = 0; k < nz; k++)
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++) {
+        const size_t p = ((size_t)k * ny + j) * nx + i;
+        double v = 0.0;
+        switch (which) {
+          case 0: v = h->x1f[0] + (double)(2 * (i + 1) - 1) * 0.5 * h->d[0]; break;
+          case 1: v = h->x1f[1] + (double)(2 * (j + 1) - 1) * 0.5 * h->d[1]; break;
+          case 2: v = h->x1f[2] + (double)(2 * (k + 1) - 1) * 0.5 * h->d[2]; break;
+          case 3: case 4: case 5: v = h->dmesh[which - 3]; break;
+          case 6: v = gl; break;
+          default: v = cv; break;
+        }
+        out[p] = v;
+      }
+  return 0;
+}
+
+// Spacing used by the d1 metric (patch dx), and the mesh d1..d3.
+int og_spacing(const og_handle* h, double* patch_d, double* mesh_d) {
+  if (!h) return 1;
+  for (int d = 0; d < 3; d++) {
+    if (patch_d) patch_d[d] = h->d[d];
+    if (mesh_d) mesh_d[d] = h->dmesh[d];
+  }
+  return 0;
+}
+
+// Dense operator matrix D (n x n, row-major, D[i][j] = d out_i / d in_j) of one
+// operator along one direction, formed by applying the line evaluator to unit
+// vectors (the same matrix compact_basetype.f90:199-205 stores as sm).
+int og_dense(const og_handle* h, int op, int dir, double* D) {
+  if (!h || op < 0 || op > 3 || dir < 0 || dir > 2) return 1;
+  const Op1& o = pick(h, op, dir);
+  const int n = h->n[dir];
+  if (o.null_op) return 2;
+  const double scale = (op == OP_D1) ? h->d[dir] : 0.0;
+  std::vector<double> v(n + 1), dv(n + 1);
+  for (int j = 0; j < n; j++) {
+    std::fill(v.begin(), v.end(), 0.0);
+    v[j + 1] = 1.0;
+    eval_line(o, v.data(), dv.data(), scale);
+    for (int i = 0; i < n; i++) D[(size_t)i * n + j] = dv[i + 1];
+  }
+  return 0;
+}
+
+}  // extern "C"

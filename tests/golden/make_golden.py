@@ -1,0 +1,40 @@
+"""Extract the reference's own golden scalars for the compact-operator path.
+
+Reads the reference test-case files as text (they are Python fragments that
+``tests/run_tests.py`` executes) and writes ``reference_scalars.json``.  Run it
+where the reference tree is mounted:
+
+    python tests/golden/make_golden.py /path/to/pyranda
+"""
+import json
+import os
+import sys
+
+CASES = {
+    "test1DAdvection.py": ["advec-1d-50", "advec-1d-100", "advec-1d-200", "advec-1d-300", "advec-1d-400"],
+    "testUnit.py": ["unit-test-3D"],
+    "testTaylorGreen.py": ["taylorgreen"],
+    "testShuOsher.py": ["shu-osher-CR"],
+}
+
+
+def main(root):
+    out = {"source": "pyranda tests/cases (baselines blocks)", "tolerance_rel": 1.0e-4, "values": {}}
+    for fname, names in CASES.items():
+        path = os.path.join(root, "tests", "cases", fname)
+        text = open(path).read()
+        block = text.split('baselines = """')[1].split('"""')[0]
+        for line in block.split("\n"):
+            if "--" not in line:
+                continue
+            name, val = [s.strip() for s in line.split("--")[:2]]
+            if name in names:
+                out["values"][name] = {"value": float(val), "file": "tests/cases/" + fname}
+    dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_scalars.json")
+    with open(dst, "w") as f:
+        json.dump(out, f, indent=1, sort_keys=True)
+    print("wrote", dst)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
