@@ -1,0 +1,146 @@
+/*
+ * pyranda_gpu.h — C ABI of the GB300 compact-operator library.
+ *
+ * Drop-in replacement for the f2py module `pyranda.parcop.parcop`
+ * (pyranda/parcop/parcop.f90) on one GPU with no MPI decomposition.
+ *
+ * Conventions
+ *  - A field is a contiguous FP64 array of nx*ny*nz values in Fortran order
+ *    (x fastest), i.e. the memory of numpy's F-ordered (nx,ny,nz) array that
+ *    parcop receives (pyranda/pyrandaMPI.py:249-250).
+ *  - Pointers are DEVICE pointers unless the function name ends in `_host`.
+ *  - The caller owns inputs and outputs; the library never allocates per call
+ *    (parcop's f2py wrappers allocated a new output on every call,
+ *    parcop.f90:225-253 `intent(out)`).  Workspaces belong to the handle.
+ *  - `stream` is a cudaStream_t passed as void*; NULL is the legacy stream.
+ *    Calls are stream-ordered and never synchronise, so they can be recorded
+ *    into a CUDA graph.
+ *  - Every call returns a pg_status.  The library never exits the process
+ *    (parcop printed and called `stop` on a size mismatch,
+ *    pyranda/parcop/compact_d1.f90:65-72).
+ *  - Null operators keep parcop's semantics: a direction with fewer than 4
+ *    points yields zero for derivatives and a copy for filters
+ *    (pyranda/parcop/compact.f90:95-97, compact_operators.f90:24-29,396-401).
+ */
+#ifndef PYRANDA_GPU_H
+#define PYRANDA_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  PG_OK = 0,
+  PG_EBADSHAPE = 1, /* unsupported extent (e.g. 4 <= n < 8 on a non-null direction) */
+  PG_ENULLOP = 2,   /* operator requested on a null direction where no result exists */
+  PG_ECUDA = 3,     /* a CUDA runtime call failed; see pg_last_error() */
+  PG_ENAN = 4,      /* a non-finite value was found by pg_check_finite */
+  PG_ETIMEOUT = 5,  /* a bounded device wait gave up */
+  PG_EINVAL = 6,    /* bad argument (NULL pointer, bad enum) */
+  PG_ENOMEM = 7     /* allocation of handle workspace failed */
+} pg_status;
+
+/* Arithmetic of the compact sweeps.  PG_FP64 follows the reference
+ * arithmetic; PG_FP32 evaluates the sweeps in single precision on FP64
+ * inputs/outputs (the fast path; FP64 state is kept by the caller). */
+typedef enum { PG_FP64 = 0, PG_FP32 = 1 } pg_precision;
+
+typedef enum { PG_SPECTRAL = 0, PG_GAUSSIAN = 1 } pg_filter_kind;
+
+enum { PG_DIR_X = 0, PG_DIR_Y = 1, PG_DIR_Z = 2, PG_DIR_ALL = 3 };
+
+/* Mesh quantities for pg_mesh (parcop.f90:84-191). */
+typedef enum {
+  PG_MESH_X = 0, PG_MESH_Y = 1, PG_MESH_Z = 2,
+  PG_MESH_D1 = 3, PG_MESH_D2 = 4, PG_MESH_D3 = 5,
+  PG_MESH_GRIDLEN = 6, PG_MESH_CELLVOL = 7
+} pg_mesh_var;
+
+typedef struct {
+  int n[3];        /* nx, ny, nz (global = local: one GPU) */
+  int periodic[3]; /* 1 = PERI, 0 = NONE (one-sided closures) */
+  double x1[3];    /* first node coordinate per direction */
+  double xn[3];    /* last node coordinate per direction */
+  int precision;   /* pg_precision */
+} pg_grid;
+
+typedef struct pg_handle pg_handle;
+
+/* setup (parcop.f90:23-61) + setup_mesh (parcop.f90:64-70):
+ * node extents -> face extents, operator assembly and LU factorisation
+ * for d1 (c10d1), d8 (c10d8), compact filter (c8ff8) and Gaussian (cgfs4). */
+int pg_create(const pg_grid* grid, pg_handle** out);
+/* Frees the handle and its device workspace. */
+int pg_destroy(pg_handle* h);
+/* Switch the arithmetic of later sweeps on this handle (pg_precision). */
+int pg_set_precision(pg_handle* h, int precision);
+/* Patch spacing (used by the d1 metric) and mesh spacing d1..d3. */
+int pg_get_spacing(const pg_handle* h, double* patch_d, double* mesh_d);
+/* Text of the last error on this thread (static storage). */
+const char* pg_last_error(void);
+/* Library version string. */
+const char* pg_version(void);
+
+/* ddx / ddy / ddz (parcop.f90:225-253 -> compact_operators.f90:13-128):
+ * 10th-order Pade first derivative, divided by the grid spacing. */
+int pg_d1(pg_handle* h, int dir, const double* in, double* out, void* stream);
+/* dd8x / dd8y / dd8z (parcop.f90:279-301 -> compact_operators.f90:280-383):
+ * 8th derivative, no metric. */
+int pg_d8(pg_handle* h, int dir, const double* in, double* out, void* stream);
+/* sFilter / gFilter / gFilterDir (parcop.f90:337-368 -> operators.f90:755-896).
+ * dir = PG_DIR_ALL gives the x->y->z sweep sequence of `filter`. */
+int pg_filter(pg_handle* h, int kind, int dir, const double* in, double* out, void* stream);
+/* pRing (parcop.f90:313-322 -> operators.f90:615-643 with L = 2). */
+int pg_ring(pg_handle* h, const double* in, double* out, void* stream);
+/* pRingV (parcop.f90:324-333 -> operators.f90:645-699 with L = 1). */
+int pg_ringv(pg_handle* h, const double* vx, const double* vy, const double* vz, double* out,
+             void* stream);
+/* gradS (parcop.f90:371-379 -> operators.f90:184-212, Cartesian). */
+int pg_grad(pg_handle* h, const double* in, double* gx, double* gy, double* gz, void* stream);
+/* divergence (parcop.f90:202-211 -> operators.f90:38-53, Cartesian). */
+int pg_div(pg_handle* h, const double* fx, const double* fy, const double* fz, double* out,
+           void* stream);
+/* xGrid/yGrid/zGrid/dxGrid/.../mesh_getGridLen/mesh_getCellVol
+ * (parcop.f90:130-191 -> mesh.f90:169-211, Cartesian). */
+int pg_mesh(pg_handle* h, int which, double* out, void* stream);
+
+/* One stage of the LSRK(5,4) update of pyranda.py:797-804 for nvar conserved
+ * fields, fused:  PHI = A*PHI + dt*F ;  U = U + B*PHI.
+ * U, PHI, F are arrays of nvar device pointers (host arrays of pointers);
+ * dt is a device scalar so the step can be captured in a CUDA graph. */
+int pg_rk_stage(pg_handle* h, int nvar, double* const* U, double* const* PHI,
+                const double* const* F, const double* dt, double A, double B, void* stream);
+
+/* pyrandaTimestep.courant (pyranda/pyrandaTimestep.py:42-67, Cartesian):
+ * out[0] = 1 / max(|u|/d1 + |v|/d2 + |w|/d3 + |c|/GridLen).  v or w may be
+ * NULL, meaning the constant vconst/wconst (scripts pass 0.0). */
+int pg_courant(pg_handle* h, const double* u, const double* v, const double* w, const double* c,
+               double vconst, double wconst, double* out, void* stream);
+/* pyrandaTimestep.diff (pyranda/pyrandaTimestep.py:71-77):
+ * out[0] = min(rho * GridLen^2 / max(1e-12, bulk)). */
+int pg_diff(pg_handle* h, const double* bulk, const double* rho, double* out, void* stream);
+/* Global reductions (pyrandaMPI.py:307-326 sum3D/max3D/min3D on one GPU):
+ * op 0 = sum, 1 = max, 2 = min over n values; out is a device scalar. */
+int pg_reduce(pg_handle* h, int op, const double* in, int64_t n, double* out, void* stream);
+/* Writes 1 to *flag (device int) if any of n values is not finite, else
+ * leaves it unchanged (pyranda.py:359-369 checked for NaN on the host). */
+int pg_check_finite(const double* in, int64_t n, int* flag, void* stream);
+
+/* Host-pointer variants: copy in, run on an internal stream, copy out,
+ * synchronise.  For tests and for callers that hold host arrays. */
+int pg_d1_host(pg_handle* h, int dir, const double* in, double* out);
+int pg_d8_host(pg_handle* h, int dir, const double* in, double* out);
+int pg_filter_host(pg_handle* h, int kind, int dir, const double* in, double* out);
+int pg_ring_host(pg_handle* h, const double* in, double* out);
+
+/* Number of kernels this library has launched since load (for accounting). */
+uint64_t pg_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PYRANDA_GPU_H */

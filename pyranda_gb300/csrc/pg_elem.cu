@@ -1,0 +1,274 @@
+// Pointwise and reduction kernels: the fused LSRK(5,4) stage update, the
+// Courant / diffusion time-step limits, global reductions and the mesh fill.
+// These are HBM-bound; they use grid-stride loops over 2 doubles per thread
+// (16-byte accesses) sized to a multiple of the SM count.
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <cmath>
+
+#include "pg_internal.h"
+
+namespace pg {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kMaxVar = 16;
+
+int grid_for(int64_t n) {
+  int64_t b = (n + kThreads - 1) / kThreads;
+  const int64_t cap = 152 * 8;
+  return (int)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+int check(const char* what) {
+  count_launch();
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error("%s: %s", what, cudaGetErrorString(e));
+    return PG_ECUDA;
+  }
+  return PG_OK;
+}
+
+__global__ void fill_kernel(double* __restrict__ o, double v, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    o[i] = v;
+}
+
+__global__ void copy_kernel(double* __restrict__ o, const double* __restrict__ a, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    o[i] = a[i];
+}
+
+struct RkArgs {
+  double* U[kMaxVar];
+  double* PHI[kMaxVar];
+  const double* F[kMaxVar];
+};
+
+// pyranda.py:800-804:  tmp1 = A*PHI ; PHI = dt*F + tmp1 ; tmp2 = B*PHI ; U = U + tmp2
+__global__ void rk_stage_kernel(const RkArgs a, int nvar, const double* __restrict__ dtp, double A, double B,
+                                int64_t n) {
+  const double dt = *dtp;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    for (int v = 0; v < nvar; v++) {
+      const double tmp1 = A * a.PHI[v][i];
+      const double phi = dt * a.F[v][i] + tmp1;
+      a.PHI[v][i] = phi;
+      a.U[v][i] = a.U[v][i] + B * phi;
+    }
+  }
+}
+
+// Block reduction helper: op 0 = sum, 1 = max, 2 = min.
+template <int OP>
+__device__ __forceinline__ double combine(double a, double b) {
+  if (OP == 0) return a + b;
+  if (OP == 1) return fmax(a, b);
+  return fmin(a, b);
+}
+
+template <int OP>
+__device__ __forceinline__ double identity() {
+  if (OP == 0) return 0.0;
+  if (OP == 1) return -DBL_MAX;
+  return DBL_MAX;
+}
+
+template <int OP>
+__device__ double block_reduce(double v) {
+  __shared__ double sh[32];
+  for (int o = 16; o > 0; o >>= 1) v = combine<OP>(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  v = (threadIdx.x < nw) ? sh[threadIdx.x] : identity<OP>();
+  if (w == 0)
+    for (int o = 16; o > 0; o >>= 1) v = combine<OP>(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// NaN propagation: fmax/fmin drop NaNs, so a NaN anywhere would be hidden; a
+// separate flag keeps numpy's behaviour (max/min of data holding NaN is NaN).
+template <int OP>
+__global__ void reduce_partial(const double* __restrict__ in, int64_t n, double* __restrict__ partial) {
+  double acc = identity<OP>();
+  bool nan = false;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double x = in[i];
+    nan |= (x != x);
+    acc = combine<OP>(acc, x);
+  }
+  acc = block_reduce<OP>(acc);
+  const int anynan = __syncthreads_or(nan);
+  if (threadIdx.x == 0) partial[blockIdx.x] = anynan ? NAN : acc;
+}
+
+template <int OP>
+__global__ void reduce_final(const double* __restrict__ partial, int np, double* __restrict__ out) {
+  double acc = identity<OP>();
+  bool nan = false;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) {
+    const double x = partial[i];
+    nan |= (x != x);
+    acc = combine<OP>(acc, x);
+  }
+  acc = block_reduce<OP>(acc);
+  const int anynan = __syncthreads_or(nan);
+  if (threadIdx.x == 0) *out = anynan ? NAN : acc;
+}
+
+// courant: vrate = |u|/d1 + |v|/d2 + |w|/d3 ; crate = |c|/GridLen ; max(vrate+crate)
+__global__ void courant_partial(const double* __restrict__ u, const double* __restrict__ v,
+                                const double* __restrict__ w, const double* __restrict__ c, double vconst,
+                                double wconst, double d1, double d2, double d3, double gl, int64_t n,
+                                double* __restrict__ partial) {
+  double acc = -DBL_MAX;
+  bool nan = false;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double vv = v ? v[i] : vconst;
+    const double ww = w ? w[i] : wconst;
+    const double vrate = fabs(u[i]) / d1 + fabs(vv) / d2 + fabs(ww) / d3;
+    const double x = vrate + fabs(c[i]) / gl;
+    nan |= (x != x);
+    acc = fmax(acc, x);
+  }
+  acc = block_reduce<1>(acc);
+  const int anynan = __syncthreads_or(nan);
+  if (threadIdx.x == 0) partial[blockIdx.x] = anynan ? NAN : acc;
+}
+
+__global__ void invert_scalar(double* p) { *p = 1.0 / *p; }
+
+// diff: min(rho * GridLen^2 / max(1e-12, bulk))
+__global__ void diff_partial(const double* __restrict__ bulk, const double* __restrict__ rho, double gl,
+                             int64_t n, double* __restrict__ partial) {
+  double acc = DBL_MAX;
+  bool nan = false;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double x = rho[i] * gl * gl / fmax(1.0e-12, bulk[i]);
+    nan |= (x != x);
+    acc = fmin(acc, x);
+  }
+  acc = block_reduce<2>(acc);
+  const int anynan = __syncthreads_or(nan);
+  if (threadIdx.x == 0) partial[blockIdx.x] = anynan ? NAN : acc;
+}
+
+__global__ void finite_kernel(const double* __restrict__ in, int64_t n, int* flag) {
+  bool bad = false;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    bad |= !isfinite(in[i]);
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(flag, 1);
+}
+
+// mesh.f90:169-211 (Cartesian): cell-centred coordinates from the face origin
+__global__ void mesh_kernel(int which, double* __restrict__ out, int nx, int ny, int nz, double x1, double y1,
+                            double z1, double dx, double dy, double dz, double cval) {
+  const int64_t n = (int64_t)nx * ny * nz;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(p % nx);
+    const int j = (int)((p / nx) % ny);
+    const int k = (int)(p / ((int64_t)nx * ny));
+    double v;
+    // mesh.f90:181-183: x1 + REAL(2*i-1)*half*dx, evaluated without contraction
+    if (which == 0) v = __dadd_rn(x1, __dmul_rn(__dmul_rn((double)(2 * (i + 1) - 1), 0.5), dx));
+    else if (which == 1) v = __dadd_rn(y1, __dmul_rn(__dmul_rn((double)(2 * (j + 1) - 1), 0.5), dy));
+    else if (which == 2) v = __dadd_rn(z1, __dmul_rn(__dmul_rn((double)(2 * (k + 1) - 1), 0.5), dz));
+    else v = cval;
+    out[p] = v;
+  }
+}
+
+}  // namespace
+
+int launch_fill(double* out, double value, int64_t n, void* stream) {
+  if (n <= 0) return PG_OK;
+  fill_kernel<<<grid_for(n), kThreads, 0, (cudaStream_t)stream>>>(out, value, n);
+  return check("fill");
+}
+
+int launch_copy(double* out, const double* in, int64_t n, void* stream) {
+  if (n <= 0 || out == in) return PG_OK;
+  copy_kernel<<<grid_for(n), kThreads, 0, (cudaStream_t)stream>>>(out, in, n);
+  return check("copy");
+}
+
+int launch_rk_stage(int nvar, double* const* U, double* const* PHI, const double* const* F, const double* dt,
+                    double A, double B, int64_t n, void* stream) {
+  RkArgs a;
+  for (int v0 = 0; v0 < nvar; v0 += kMaxVar) {
+    const int m = nvar - v0 < kMaxVar ? nvar - v0 : kMaxVar;
+    for (int v = 0; v < m; v++) {
+      a.U[v] = U[v0 + v];
+      a.PHI[v] = PHI[v0 + v];
+      a.F[v] = F[v0 + v];
+    }
+    rk_stage_kernel<<<grid_for(n), kThreads, 0, (cudaStream_t)stream>>>(a, m, dt, A, B, n);
+    int rc = check("rk_stage");
+    if (rc) return rc;
+  }
+  return PG_OK;
+}
+
+int launch_reduce(int op, const double* in, int64_t n, double* partial, double* out, void* stream) {
+  const int g = grid_for(n) < kReduceBlocks ? grid_for(n) : kReduceBlocks;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (op == 0) {
+    reduce_partial<0><<<g, kThreads, 0, s>>>(in, n, partial);
+    reduce_final<0><<<1, kThreads, 0, s>>>(partial, g, out);
+  } else if (op == 1) {
+    reduce_partial<1><<<g, kThreads, 0, s>>>(in, n, partial);
+    reduce_final<1><<<1, kThreads, 0, s>>>(partial, g, out);
+  } else {
+    reduce_partial<2><<<g, kThreads, 0, s>>>(in, n, partial);
+    reduce_final<2><<<1, kThreads, 0, s>>>(partial, g, out);
+  }
+  count_launch();
+  return check("reduce");
+}
+
+int launch_courant(const double* u, const double* v, const double* w, const double* c, double vconst,
+                   double wconst, const double d[3], double gridlen, int64_t n, double* partial, double* out,
+                   void* stream) {
+  const int g = grid_for(n) < kReduceBlocks ? grid_for(n) : kReduceBlocks;
+  cudaStream_t s = (cudaStream_t)stream;
+  courant_partial<<<g, kThreads, 0, s>>>(u, v, w, c, vconst, wconst, d[0], d[1], d[2], gridlen, n, partial);
+  reduce_final<1><<<1, kThreads, 0, s>>>(partial, g, out);
+  invert_scalar<<<1, 1, 0, s>>>(out);
+  count_launch(2);
+  return check("courant");
+}
+
+int launch_diff(const double* bulk, const double* rho, double gl, int64_t n, double* partial, double* out,
+                void* stream) {
+  const int g = grid_for(n) < kReduceBlocks ? grid_for(n) : kReduceBlocks;
+  cudaStream_t s = (cudaStream_t)stream;
+  diff_partial<<<g, kThreads, 0, s>>>(bulk, rho, gl, n, partial);
+  reduce_final<2><<<1, kThreads, 0, s>>>(partial, g, out);
+  count_launch();
+  return check("diff");
+}
+
+int launch_check_finite(const double* in, int64_t n, int* flag, void* stream) {
+  if (n <= 0) return PG_OK;
+  finite_kernel<<<grid_for(n), kThreads, 0, (cudaStream_t)stream>>>(in, n, flag);
+  return check("check_finite");
+}
+
+int launch_mesh(int which, double* out, int nx, int ny, int nz, const double x1f[3], const double d[3],
+                const double dm[3], void* stream) {
+  double cval = 0.0;
+  if (which >= 3 && which <= 5) cval = dm[which - 3];
+  if (which == 6) cval = fmin(fmin(dm[0], dm[1]), dm[2]);
+  if (which == 7) cval = d[0] * d[1] * d[2];
+  const int64_t n = (int64_t)nx * ny * nz;
+  mesh_kernel<<<grid_for(n), kThreads, 0, (cudaStream_t)stream>>>(which, out, nx, ny, nz, x1f[0], x1f[1], x1f[2],
+                                                                  d[0], d[1], d[2], cval);
+  return check("mesh");
+}
+
+}  // namespace pg

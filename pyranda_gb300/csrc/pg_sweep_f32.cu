@@ -1,0 +1,11 @@
+// FP32 instantiation of the directional sweeps (the fast path: single-precision
+// arithmetic on FP64 inputs and outputs).
+#include "pg_sweep.cuh"
+
+namespace pg {
+
+int launch_sweep_f32(const DevOp& op, const KParams& P, int dir, int epi, int lb, int64_t nb, void* st) {
+  return dispatch_kind<float>(op, P, dir, epi, lb, nb, st);
+}
+
+}  // namespace pg

@@ -1,0 +1,224 @@
+"""Device-side grid: one pg_handle plus the field conventions of pyranda.
+
+Fields are torch float64 tensors of shape (nx, ny, nz) laid out in Fortran
+order (x fastest, strides (1, nx, nx*ny)) on the current CUDA device, which is
+the memory layout of the F-ordered numpy arrays pyranda hands to parcop
+(pyranda/pyrandaMPI.py:249-250).  Every operator here is one or more calls
+into ``libpyranda_gpu.so`` on the current torch stream; outputs are allocated
+by torch's caching allocator (or passed in), never by the library.
+"""
+import ctypes
+
+import torch
+
+from . import _lib
+
+_DIRS = {"x": 0, "y": 1, "z": 2}
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+class Grid:
+    """A Cartesian pyranda patch on one GPU (parcop.f90:23-70 setup + setup_mesh)."""
+
+    def __init__(self, n, periodic, x1, xn, precision="fp64", device=None):
+        if not torch.cuda.is_available():
+            raise RuntimeError("pyranda_gb300 needs a CUDA device; there is no CPU fallback")
+        self.lib = _lib.load()
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.n = tuple(int(v) for v in n)
+        self.shape = self.n
+        self.npts = self.n[0] * self.n[1] * self.n[2]
+        self.periodic = tuple(bool(p) for p in periodic)
+        g = _lib.pg_grid()
+        for d in range(3):
+            g.n[d] = self.n[d]
+            g.periodic[d] = 1 if self.periodic[d] else 0
+            g.x1[d] = float(x1[d])
+            g.xn[d] = float(xn[d])
+        self.precision = precision
+        g.precision = _lib.PG_FP32 if precision == "fp32" else _lib.PG_FP64
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.pg_create(ctypes.byref(g), ctypes.byref(h)), "pg_create")
+        self.h = h
+        pd = (ctypes.c_double * 3)()
+        md = (ctypes.c_double * 3)()
+        self.lib.pg_get_spacing(self.h, pd, md)
+        self.patch_d = list(pd)  # dx, dy, dz of the d1 metric
+        self.mesh_d = list(md)   # mesh d1, d2, d3
+        self.gridlen = min(self.mesh_d)
+        self._scalar_pool = []
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                self.lib.pg_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    def set_precision(self, precision):
+        self.precision = precision
+        _lib.check(self.lib.pg_set_precision(self.h, _lib.PG_FP32 if precision == "fp32" else _lib.PG_FP64),
+                   "pg_set_precision")
+
+    # ------------------------------------------------------------------ fields
+    def empty(self):
+        nx, ny, nz = self.n
+        return torch.empty((nz, ny, nx), dtype=torch.float64, device=self.device).permute(2, 1, 0)
+
+    def zeros(self):
+        t = self.empty()
+        t.zero_()
+        return t
+
+    def _fortran_ok(self, t):
+        # a tensor whose storage order is x-fastest (any size-1 dims may carry odd strides)
+        nx, ny, nz = self.n
+        exp = (1, nx, nx * ny)
+        for d in range(3):
+            if self.n[d] > 1 and t.stride(d) != exp[d]:
+                return False
+        return True
+
+    def field(self, v):
+        """Return v as a device field in the library layout (copying only if needed)."""
+        if isinstance(v, torch.Tensor) and v.dtype == torch.float64 and v.device == self.device \
+                and tuple(v.shape) == self.n and self._fortran_ok(v):
+            return v
+        out = self.empty()
+        if isinstance(v, torch.Tensor):
+            out.copy_(v.to(device=self.device, dtype=torch.float64).expand(self.n))
+        else:
+            import numpy
+            a = numpy.asarray(v, dtype=numpy.float64)
+            if a.ndim == 0:
+                out.fill_(float(a))
+            else:
+                out.copy_(torch.from_numpy(numpy.ascontiguousarray(numpy.broadcast_to(a, self.n))).to(self.device))
+        return out
+
+    def _out(self, out):
+        if out is None:
+            return self.empty()
+        if not self._fortran_ok(out):
+            raise ValueError("output field must be float64 (nx,ny,nz) in Fortran order")
+        return out
+
+    # --------------------------------------------------------------- operators
+    def d1(self, direction, v, out=None):
+        v = self.field(v)
+        out = self._out(out)
+        _lib.check(self.lib.pg_d1(self.h, direction, _ptr(v), _ptr(out), _stream()), "pg_d1")
+        return out
+
+    def ddx(self, v, out=None):
+        return self.d1(0, v, out)
+
+    def ddy(self, v, out=None):
+        return self.d1(1, v, out)
+
+    def ddz(self, v, out=None):
+        return self.d1(2, v, out)
+
+    def d8(self, direction, v, out=None):
+        v = self.field(v)
+        out = self._out(out)
+        _lib.check(self.lib.pg_d8(self.h, direction, _ptr(v), _ptr(out), _stream()), "pg_d8")
+        return out
+
+    def filter(self, kind, v, direction=_lib.PG_DIR_ALL, out=None):
+        """kind 'spectral' (c8ff8, fbar) or 'gaussian' (cgfs4, gbar)."""
+        v = self.field(v)
+        out = self._out(out)
+        k = _lib.PG_SPECTRAL if kind == "spectral" else _lib.PG_GAUSSIAN
+        _lib.check(self.lib.pg_filter(self.h, k, direction, _ptr(v), _ptr(out), _stream()), "pg_filter")
+        return out
+
+    def ring(self, v, out=None):
+        v = self.field(v)
+        out = self._out(out)
+        _lib.check(self.lib.pg_ring(self.h, _ptr(v), _ptr(out), _stream()), "pg_ring")
+        return out
+
+    def ringv(self, vx, vy, vz, out=None):
+        vx, vy, vz = self.field(vx), self.field(vy), self.field(vz)
+        out = self._out(out)
+        _lib.check(self.lib.pg_ringv(self.h, _ptr(vx), _ptr(vy), _ptr(vz), _ptr(out), _stream()), "pg_ringv")
+        return out
+
+    def grad(self, v):
+        v = self.field(v)
+        gx, gy, gz = self.empty(), self.empty(), self.empty()
+        _lib.check(self.lib.pg_grad(self.h, _ptr(v), _ptr(gx), _ptr(gy), _ptr(gz), _stream()), "pg_grad")
+        return [gx, gy, gz]
+
+    def div(self, fx, fy, fz, out=None):
+        fx, fy, fz = self.field(fx), self.field(fy), self.field(fz)
+        out = self._out(out)
+        _lib.check(self.lib.pg_div(self.h, _ptr(fx), _ptr(fy), _ptr(fz), _ptr(out), _stream()), "pg_div")
+        return out
+
+    def mesh(self, which):
+        out = self.empty()
+        _lib.check(self.lib.pg_mesh(self.h, which, _ptr(out), _stream()), "pg_mesh")
+        return out
+
+    # ---------------------------------------------------- time step and reductions
+    def scalar(self):
+        return torch.empty((), dtype=torch.float64, device=self.device)
+
+    def courant(self, u, v, w, c, out=None):
+        u, c = self.field(u), self.field(c)
+        vp, vc = (None, 0.0)
+        wp, wc = (None, 0.0)
+        if isinstance(v, torch.Tensor) and v.dim() > 0:
+            v = self.field(v)
+            vp = _ptr(v)
+        else:
+            vc = float(v)
+        if isinstance(w, torch.Tensor) and w.dim() > 0:
+            w = self.field(w)
+            wp = _ptr(w)
+        else:
+            wc = float(w)
+        out = self.scalar() if out is None else out
+        _lib.check(self.lib.pg_courant(self.h, _ptr(u), vp, wp, _ptr(c), vc, wc, _ptr(out), _stream()),
+                   "pg_courant")
+        return out
+
+    def diff(self, bulk, rho, out=None):
+        bulk, rho = self.field(bulk), self.field(rho)
+        out = self.scalar() if out is None else out
+        _lib.check(self.lib.pg_diff(self.h, _ptr(bulk), _ptr(rho), _ptr(out), _stream()), "pg_diff")
+        return out
+
+    def reduce(self, op, v, out=None):
+        """op: 0 sum, 1 max, 2 min over a field (or any float64 device tensor)."""
+        if not isinstance(v, torch.Tensor):
+            return float(v)
+        if v.dtype != torch.float64 or v.device != self.device or not v.is_contiguous():
+            if not (tuple(v.shape) == self.n and self._fortran_ok(v) and v.dtype == torch.float64):
+                v = v.to(device=self.device, dtype=torch.float64).contiguous()
+        out = self.scalar() if out is None else out
+        _lib.check(self.lib.pg_reduce(self.h, op, _ptr(v), v.numel(), _ptr(out), _stream()), "pg_reduce")
+        return out
+
+    def rk_stage(self, U, PHI, F, dt, A, B):
+        n = len(U)
+        arr = ctypes.c_void_p * n
+        u = arr(*[t.data_ptr() for t in U])
+        p = arr(*[t.data_ptr() for t in PHI])
+        f = arr(*[t.data_ptr() for t in F])
+        _lib.check(self.lib.pg_rk_stage(self.h, n, u, p, f, _ptr(dt), float(A), float(B), _stream()),
+                   "pg_rk_stage")
+
+    def check_finite(self, v, flag):
+        _lib.check(self.lib.pg_check_finite(_ptr(v), v.numel(), _ptr(flag), _stream()), "pg_check_finite")

@@ -1,0 +1,693 @@
+"""pyrandaSim on one GB300: the EOM/setIC/rk4/ddx/filter API of pyranda.
+
+Mirrors pyranda/pyranda.py (class pyrandaSim) with device-resident fields:
+every variable's ``data`` is a torch float64 tensor of shape (nx, ny, nz) in
+Fortran order on the GPU, the compact operators run in ``libpyranda_gpu.so``,
+the LSRK(5,4) update is one fused kernel per stage, and global reductions
+(``sum``/``max``/``min`` and the time-step limits) return device scalars so a
+whole RK step can be recorded in a CUDA graph (``pyrandaSim.use_graphs``).
+"""
+import math
+
+import numpy
+import torch
+
+from . import pgmath
+from ._lib import PG_DIR_ALL
+from .grid import Grid
+from .pyrandaUtils import findVar, fortran3d, splitLines
+
+# LSRK(5,4) of Carpenter & Kennedy (pyranda.py:760-779)
+ARK = [0.0, -6234157559845. / 12983515589748., -6194124222391. / 4410992767914.,
+       -31623096876824. / 15682348800105., -12251185447671. / 11596622555746.]
+BRK = [494393426753. / 4806282396855., 4047970641027. / 5463924506627.,
+       9795748752853. / 13190207949281., 4009051133189. / 8539092990294.,
+       1348533437543. / 7166442652324.]
+ETA = [494393426753. / 4806282396855., 4702696611523. / 9636871101405.,
+       3614488396635. / 5249666457482., 9766892798963. / 10823461281321., 1.0]
+
+EVAL_GLOBALS = {"numpy": pgmath, "scipy": pgmath.scipy, "torch": torch, "math": math}
+
+
+def defaultMeshOptions():
+    """pyranda/pyrandaMesh.py:214-233"""
+    return {"x1": [0.0, 0.0, 0.0], "xn": [1, 1, 1], "nn": [1, 1, 1],
+            "periodic": [False, False, False], "periodicGrid": True,
+            "symmetric": [[False, False], [False, False], [False, False]],
+            "dim": 1, "coordsys": 0, "function": None, "id": 0, "pn": [0, 0, 0]}
+
+
+class pyrandaVar:
+    """pyranda/pyrandaVar.py: a named field with global reductions."""
+
+    def __init__(self, name, kind=None, rank="scalar"):
+        self.name = name
+        self.kind = kind
+        self.rank = rank
+        self.data = None
+        self.allocated = False
+        self.sim = None
+
+    def __allocate__(self, sim):
+        if self.allocated:
+            return
+        self.sim = sim
+        self.data = sim.emptyScalar()
+        self.allocated = True
+
+    def _reduce(self, op, data=None):
+        d = self.data if data is None else data
+        if not isinstance(d, torch.Tensor):
+            n = self.sim.npts
+            return float(d) * n if op == 0 else float(d)
+        return float(self.sim.grid.reduce(op, d))
+
+    def sum(self, axis=None, idata=None):
+        d = self.data if idata is None else idata
+        if axis is None:
+            return self._reduce(0, d)
+        return self.sim.PyMPI._axis_sum(d, axis)
+
+    def mean(self, axis=None, idata=None):
+        s = self.sum(axis=axis, idata=idata)
+        if axis is None:
+            return s / float(self.sim.npts)
+        s = numpy.asarray(s)
+        return s * s.size / float(self.sim.npts)
+
+    def var(self, axis=None):
+        bar = self.mean(axis=axis)
+        bar2 = self.mean(axis=axis, idata=self.data ** 2)
+        return bar2 - bar * bar
+
+    def numpy(self):
+        """Host copy (numpy, F-ordered) of the device field."""
+        d = self.data
+        if isinstance(d, torch.Tensor):
+            return numpy.asfortranarray(d.detach().cpu().numpy())
+        return d
+
+    def __getitem__(self, given):
+        return numpy.squeeze(self.numpy()[given])
+
+
+class pyrandaEq:
+    """pyranda/pyrandaEq.py:16-48: one EOM line compiled to a lambda."""
+
+    def __init__(self, eqstr, sMap):
+        self.eqstr = eqstr
+        self.kind = "ALG"
+        self.active = True
+        self.rank = 1
+        if "=" in eqstr:
+            self.LHS = findVar(eqstr.split("=")[0], "scalar", unique=False)
+            self.rank = len(self.LHS)
+        else:
+            self.LHS = None
+        srhs = fortran3d(eqstr.split("=")[1] if self.LHS else eqstr, sMap)
+        self.sRHS = srhs
+        self.RHS = eval("lambda self: " + srhs, EVAL_GLOBALS)
+        if "ddt(" in eqstr:
+            self.kind = "PDE"
+
+
+class _Mesh:
+    """Mesh data of pyrandaMesh (pyranda/pyrandaMesh.py:58-208), Cartesian."""
+
+    def __init__(self):
+        self.options = {}
+        self.coords = None
+        self.shape = None
+        self.coordsys = 0
+
+
+class pyrandaGPU:
+    """The single-GPU counterpart of pyrandaMPI: reductions and layout helpers.
+
+    One rank owns the whole grid, so every processor-boundary flag is true and
+    the reductions of pyrandaMPI.py:307-326 are device reductions.
+    """
+
+    def __init__(self, sim):
+        self.sim = sim
+        self.grid = sim.grid
+        self.nx, self.ny, self.nz = sim.nx, sim.ny, sim.nz
+        self.ax, self.ay, self.az = sim.nx, sim.ny, sim.nz
+        self.px = self.py = self.pz = 1
+        self.master = True
+        self.periodic = sim.meshOptions["periodic"]
+        per = self.periodic
+        self.x1proc = self.xnproc = (not per[0]) and self.nx > 1
+        self.y1proc = self.ynproc = (not per[1]) and self.ny > 1
+        self.z1proc = self.znproc = (not per[2]) and self.nz > 1
+        self.chunk_3d_lo = numpy.zeros(3, dtype=numpy.int32)
+        self.chunk_3d_hi = numpy.array([self.nx - 1, self.ny - 1, self.nz - 1], dtype=numpy.int32)
+        self.chunk_3d_size = numpy.array([self.nx, self.ny, self.nz], dtype=numpy.int32)
+
+    def setPatch(self):
+        """parcop kept one active patch; every call here names its grid, so this is a no-op."""
+
+    def emptyScalar(self):
+        return self.grid.zeros()
+
+    def sum3D(self, data):
+        return self.grid.reduce(0, data) if isinstance(data, torch.Tensor) else data * self.sim.npts
+
+    def max3D(self, data):
+        return self.grid.reduce(1, data) if isinstance(data, torch.Tensor) else data
+
+    def min3D(self, data):
+        return self.grid.reduce(2, data) if isinstance(data, torch.Tensor) else data
+
+    def mean3D(self, data):
+        return self.sum3D(data) / float(self.sim.npts)
+
+    def _axis_sum(self, data, axis):
+        d = data if isinstance(data, torch.Tensor) else torch.as_tensor(data)
+        if isinstance(axis, (tuple, list)):
+            axis = tuple(axis)
+        return d.sum(dim=axis).cpu().numpy()
+
+    # pyrandaMPI.py:353-470 line/plane sums, returned on the host
+    def xsum(self, data):
+        return self._axis_sum(data, 0)
+
+    def ysum(self, data):
+        return self._axis_sum(data, 1)
+
+    def zsum(self, data):
+        return self._axis_sum(data, 2)
+
+    def xysum(self, data):
+        return self._axis_sum(data, (0, 1))
+
+    def xzsum(self, data):
+        return self._axis_sum(data, (0, 2))
+
+    def yzsum(self, data):
+        return self._axis_sum(data, (1, 2))
+
+    xbar, ybar, zbar = xsum, ysum, zsum
+
+    def subsum3xz(self, data):
+        return self.xzsum(data)
+
+
+class pyrandaSim:
+    """pyranda/pyranda.py:34-131 on one GPU.
+
+    Extra keyword arguments (not in the reference):
+      precision: 'fp64' (reference arithmetic) or 'fp32' (single-precision
+                 compact sweeps on FP64 fields; FP64 RK state and reductions)
+      device:    torch device of the fields (default: current CUDA device)
+    """
+
+    def __init__(self, name, meshOptions, silent=False, precision="fp64", device=None):
+        self.name = name
+        self.silent = silent
+        self.mesh = _Mesh()
+        if isinstance(meshOptions, str):
+            meshOptions = self._parse_mesh(meshOptions)
+        opts = defaultMeshOptions()
+        opts.update(meshOptions)
+        if opts.get("coordsys", 0) != 0:
+            raise ValueError("only Cartesian meshes (coordsys=0) are supported")
+        if any(any(s) for s in opts["symmetric"]):
+            raise ValueError("SYMM boundaries are not supported; use periodic or one-sided (NONE)")
+        self.meshOptions = opts
+        self.mesh.options = opts
+        self.mesh.coordsys = 0
+        nx, ny, nz = [int(v) for v in opts["nn"]]
+        self.nx, self.ny, self.nz = nx, ny, nz
+        self.npts = nx * ny * nz
+        self.dx = (opts["xn"][0] - opts["x1"][0]) / max(nx - 1, 1)
+        self.dy = (opts["xn"][1] - opts["x1"][1]) / max(ny - 1, 1)
+        self.dz = (opts["xn"][2] - opts["x1"][2]) / max(nz - 1, 1)
+        self.precision = precision
+        self.grid = Grid((nx, ny, nz), opts["periodic"], opts["x1"], opts["xn"], precision=precision, device=device)
+        self.PyMPI = pyrandaGPU(self)
+        self.mesh.PyMPI = self.PyMPI
+        self._make_mesh()
+        self.zero = self.grid.zeros()
+        self.equations = []
+        self.conserved = []
+        self.variables = {}
+        self.initial_conditions = []
+        self.nPDE = self.nALG = self.nELP = 0
+        self.packages = {}
+        self.userDefined = {}
+        self.time = 0.0
+        self.cycle = 0
+        self.deltat = 0.0
+        self._phi = None
+        self._graph = None
+        self._graphs_enabled = False
+        self.get_sMap()
+
+    # ------------------------------------------------------------ mesh set-up
+    def _parse_mesh(self, mesh_str):
+        """pyrandaMesh.makeMeshStr / set_options (pyranda/pyrandaMesh.py:33-49)."""
+        opts = defaultMeshOptions()
+
+        def set_options(ind, x1, xn, nn, periodic=False):
+            opts["x1"][ind] = x1
+            opts["xn"][ind] = xn
+            opts["nn"][ind] = nn
+            opts["periodic"][ind] = periodic
+
+        smap = {"xdom=(": "set_options(0,", "ydom=(": "set_options(1,", "zdom=(": "set_options(2,"}
+        ns = {"set_options": set_options, "numpy": numpy, "pi": math.pi}
+        for line in splitLines(mesh_str):
+            exec(fortran3d(line, dict(smap)), ns, ns)
+        return opts
+
+    def _make_mesh(self):
+        g = self.grid
+        self.mesh.coords = [pyrandaVar("x", "mesh"), pyrandaVar("y", "mesh"), pyrandaVar("z", "mesh")]
+        for i, c in enumerate(self.mesh.coords):
+            c.sim = self
+            c.allocated = True
+            c.data = g.mesh(i)
+        self.mesh.shape = [self.nx, self.ny, self.nz]
+        self.mesh.nn = self.meshOptions["nn"]
+        self.mesh.d1 = g.mesh(3)
+        self.mesh.d2 = g.mesh(4)
+        self.mesh.d3 = g.mesh(5)
+        self.mesh.GridLen = g.mesh(6)
+        self.mesh.CellVol = g.mesh(7)
+        ii = torch.arange(self.nx, dtype=torch.float64, device=g.device).view(-1, 1, 1)
+        jj = torch.arange(self.ny, dtype=torch.float64, device=g.device).view(1, -1, 1)
+        kk = torch.arange(self.nz, dtype=torch.float64, device=g.device).view(1, 1, -1)
+        self.mesh.indices = []
+        for name, a in (("iloc", ii), ("jloc", jj), ("kloc", kk)):
+            v = pyrandaVar(name, "mesh")
+            v.sim = self
+            v.allocated = True
+            v.data = g.field(a.expand(self.nx, self.ny, self.nz))
+            self.mesh.indices.append(v)
+
+    # ------------------------------------------------------------------- sMap
+    def get_sMap(self):
+        """pyranda.py:812-869 with the same keys; targets run on the device."""
+        s = {}
+        s["div("] = "self.div("
+        s["ddx("] = "self.ddx("
+        s["ddy("] = "self.ddy("
+        s["ddz("] = "self.ddz("
+        s["fbar("] = "self.filter("
+        s["gbar("] = "self.gfilter("
+        s["gbarx("] = "self.gfilterx("
+        s["gbary("] = "self.gfiltery("
+        s["gbarz("] = "self.gfilterz("
+        s["grad("] = "self.grad("
+        s["simtime"] = "self.time"
+        s["deltat"] = "self.deltat"
+        s["ring("] = "self.ring("
+        s["ringV("] = "self.ringV("
+        s["dd8x("] = "self.dd8x("
+        s["dd8y("] = "self.dd8y("
+        s["dd8z("] = "self.dd8z("
+        s["sum("] = "self.PyMPI.sum3D("
+        s["mean("] = "1.0/float(self.npts) * self.PyMPI.sum3D("
+        s["mean3D("] = "self.PyMPI.mean3D("
+        s["sign("] = "numpy.sign("
+        s["dot("] = "numpy.dot("
+        s["abs("] = "numpy.abs("
+        s["sqrt("] = "numpy.sqrt("
+        s["sin("] = "numpy.sin("
+        s["cos("] = "numpy.cos("
+        s["tanh("] = "numpy.tanh("
+        s["exp("] = "numpy.exp("
+        s["where("] = "numpy.where("
+        s["max("] = "self.PyMPI.max3D("
+        s["min("] = "self.PyMPI.min3D("
+        s["3d("] = "self.emptyScalar("
+        s["pi"] = "numpy.pi"
+        s["gridLen"] = "self.mesh.GridLen"
+        s["random3D()"] = "self.random3D()"
+        s["erf("] = "scipy.special.erf("
+        s["meshx"] = "self.mesh.coords[0].data"
+        s["meshy"] = "self.mesh.coords[1].data"
+        s["meshz"] = "self.mesh.coords[2].data"
+        s["meshi"] = "self.mesh.indices[0].data"
+        s["meshj"] = "self.mesh.indices[1].data"
+        s["meshk"] = "self.mesh.indices[2].data"
+        self.sMap = s
+
+    def addPackage(self, package):
+        self.packages[package.name] = package
+        package.get_sMap()
+        self.sMap.update(package.sMap)
+
+    def addUserDefinedFunction(self, name, equation):
+        self.userDefined[name] = equation
+        self.sMap.update({"%s(" % name: "self.userDefined['%s'](self," % name})
+
+    # -------------------------------------------------------------- variables
+    def iprint(self, sprnt, wpm=0):
+        if not self.silent:
+            print(sprnt, flush=True)
+
+    def allocate(self):
+        for v in self.variables.values():
+            v.__allocate__(self)
+
+    def var(self, name):
+        if name in self.variables:
+            return self.variables[name]
+        raise ValueError("Error: variable name: %s not found in database" % name)
+
+    def x(self):
+        return self.mesh.coords[0]
+
+    def y(self):
+        return self.mesh.coords[1]
+
+    def z(self):
+        return self.mesh.coords[2]
+
+    def emptyScalar(self, val=0.0):
+        t = self.grid.zeros()
+        if val != 0.0:
+            t.fill_(val)
+        return t
+
+    def random3D(self):
+        t = self.grid.empty()
+        t.uniform_()
+        return t
+
+    def eval(self, expression):
+        return eval(fortran3d(expression, self.sMap), EVAL_GLOBALS, {"self": self})
+
+    def parse(self, expression, parseDict=None):
+        if parseDict:
+            expression = self.updateStringFromDictionary(expression, parseDict, "parse")
+        exec(fortran3d(expression, self.sMap), EVAL_GLOBALS, {"self": self})
+
+    def addVar(self, name, kind=None, rank="scalar"):
+        if name not in self.variables:
+            self.variables[name] = pyrandaVar(name, kind, rank)
+
+    def addEqu(self, equation):
+        peq = pyrandaEq(equation, self.sMap)
+        self.equations.append(peq)
+        if peq.kind == "PDE":
+            self.nPDE += 1
+            self.conserved.append(peq.LHS[0])
+            if len(peq.LHS) > 1:
+                raise ValueError("only single return values for PDEs allowed")
+        else:
+            self.nALG += 1
+
+    def updateStringFromDictionary(self, string, dictionary, handle):
+        for item in dictionary:
+            if item in string:
+                string = string.replace(item, str(dictionary[item]))
+        return string
+
+    def EOM(self, eom, eomDict=False):
+        """pyranda.py:231-285"""
+        if eomDict:
+            eom = self.updateStringFromDictionary(eom, eomDict, "EOM")
+        self.eom = eom
+        lines = [el for el in eom.split("\n") if el]
+        lines = [el for el in lines if el.strip() and el.strip()[0] != "#"]
+        names = []
+        for eq in lines:
+            names += findVar(eq, "scalar")
+        for v in sorted(set(names)):
+            self.addVar(v, kind="conserved")
+        for eq in lines:
+            self.addEqu(eq)
+        self.allocate()
+        self.variables["meshx"] = self.mesh.coords[0]
+        self.variables["meshy"] = self.mesh.coords[1]
+        self.variables["meshz"] = self.mesh.coords[2]
+
+    def checkForNan(self, names=None):
+        """Names of variables holding NaN (pyranda.py:287-303)."""
+        names = names or list(self.variables)
+        bad = []
+        for n in names:
+            d = self.variables[n].data
+            if isinstance(d, torch.Tensor):
+                if d.is_floating_point() and bool(torch.isnan(d).any()):
+                    bad.append(n)
+            elif isinstance(d, float) and math.isnan(d):
+                bad.append(n)
+        return " ".join(bad)
+
+    def setIC(self, ics, icDict=False, addOnly=False, verbose=False):
+        """pyranda.py:305-370"""
+        if icDict:
+            ics = self.updateStringFromDictionary(ics, icDict, "ICs")
+        self.ics = ics
+        lines = splitLines(ics)
+        names = []
+        for eq in lines:
+            names += findVar(eq, "scalar")
+        for v in sorted(set(names)):
+            self.addVar(v, kind="conserved")
+        self.allocate()
+        self.initial_conditions += lines
+        if addOnly:
+            return
+        ns = {"self": self}
+        for ic in lines:
+            exec(fortran3d(ic, self.sMap), EVAL_GLOBALS, ns)
+        self._unalias()
+        bad = self.checkForNan(sorted(set(names)))
+        if bad:
+            raise FloatingPointError("Found some nans in inits: %s" % bad)
+        self.updateVars()
+        bad = self.checkForNan()
+        if bad:
+            raise FloatingPointError("Found some nans in Update after init: %s" % bad)
+
+    # -------------------------------------------------------------- operators
+    # pyranda.py:607-736; a direction of one point returns 0.0 as the reference
+    def ddx(self, val):
+        return 0.0 if self.nx <= 1 else self.grid.ddx(val)
+
+    def ddy(self, val):
+        return 0.0 if self.ny <= 1 else self.grid.ddy(val)
+
+    def ddz(self, val):
+        return 0.0 if self.nz <= 1 else self.grid.ddz(val)
+
+    def dd8x(self, val):
+        return self.grid.d8(0, val)
+
+    def dd8y(self, val):
+        return self.grid.d8(1, val)
+
+    def dd8z(self, val):
+        return self.grid.d8(2, val)
+
+    def div(self, f1, f2=None, f3=None):
+        z = self.zero
+        g = self.grid
+        if f2 is None and f3 is None:
+            if self.nx > 1:
+                return g.div(f1, z, z)
+            if self.ny > 1:
+                return g.div(z, f1, z)
+            if self.nz > 1:
+                return g.div(z, z, f1)
+            return 0.0
+        if f3 is None:
+            if self.nx > 1 and self.ny > 1:
+                return g.div(f1, f2, z)
+            if self.nz > 1 and self.ny > 1:
+                return g.div(z, f1, f2)
+            if self.nz > 1 and self.nx > 1:
+                return g.div(f1, z, f2)
+            if self.nx > 1:
+                return g.div(f1, z, z)
+            if self.ny > 1:
+                return g.div(z, f1, z)
+            if self.nz > 1:
+                return g.div(z, z, f1)
+            return 0.0
+        return g.div(f1, f2, f3)
+
+    def grad(self, val):
+        return self.grid.grad(val)
+
+    def ring(self, val):
+        return self.grid.ring(val)
+
+    def ringV(self, vx, vy, vz):
+        return self.grid.ringv(vx, vy, vz)
+
+    def filter(self, val):
+        return self.grid.filter("spectral", val, PG_DIR_ALL)
+
+    def gfilter(self, val):
+        return self.grid.filter("gaussian", val, PG_DIR_ALL)
+
+    def gfilterx(self, val):
+        return self.grid.filter("gaussian", val, 0)
+
+    def gfiltery(self, val):
+        return self.grid.filter("gaussian", val, 1)
+
+    def gfilterz(self, val):
+        return self.grid.filter("gaussian", val, 2)
+
+    def filterx(self, val):
+        return self.grid.filter("spectral", val, 0)
+
+    def filtery(self, val):
+        return self.grid.filter("spectral", val, 1)
+
+    def filterz(self, val):
+        return self.grid.filter("spectral", val, 2)
+
+    def getVar(self, vname):
+        table = {"x": 0, "y": 1, "z": 2, "d1": 3, "d2": 4, "d3": 5}
+        if vname not in table:
+            raise ValueError("mesh variable %s is not available on Cartesian meshes" % vname)
+        return self.grid.mesh(table[vname])
+
+    # --------------------------------------------------------------- stepping
+    def _unalias(self):
+        """Give every variable its own storage (the RK update works in place)."""
+        seen = {}
+        for v in self.variables.values():
+            d = v.data
+            if isinstance(d, torch.Tensor) and d.dim() > 0:
+                key = d.data_ptr()
+                if key in seen and seen[key] is not v:
+                    v.data = d.clone()
+                else:
+                    seen[key] = v
+
+    def updateFlux(self):
+        flux = {}
+        for eq in self.equations:
+            if eq.kind == "PDE":
+                flux[eq.LHS[0]] = eq.RHS(self)
+        return flux
+
+    def updateVars(self, verbose=False):
+        """pyranda.py:393-428: evaluate every ALG line in order."""
+        for eq in self.equations:
+            if not eq.active or eq.kind != "ALG":
+                continue
+            rhs = eq.RHS(self)
+            if not eq.LHS:
+                continue
+            if eq.rank == 1:
+                self._assign(eq.LHS[0], rhs)
+            else:
+                for ii in range(len(rhs)):
+                    self._assign(eq.LHS[ii], rhs[ii])
+
+    def _assign(self, name, value):
+        var = self.variables[name]
+        if isinstance(value, torch.Tensor):
+            for other in self.variables.values():
+                if other is not var and other.data is value:
+                    value = value.clone()
+                    break
+        var.data = value
+
+    def _field_of(self, name):
+        v = self.variables[name]
+        d = v.data
+        if not (isinstance(d, torch.Tensor) and tuple(d.shape) == self.grid.n and self.grid._fortran_ok(d)
+                and d.dtype == torch.float64):
+            v.data = self.grid.field(d)
+        return v.data
+
+    def rk4(self, time, dt):
+        """One LSRK(5,4) step (pyranda.py:758-810), ALG update after every stage."""
+        if self._graphs_enabled:
+            return self._rk4_graph(time, dt)
+        return self._rk4_eager(time, dt)
+
+    def _dt_tensor(self, dt):
+        if isinstance(dt, torch.Tensor):
+            return dt.to(device=self.grid.device, dtype=torch.float64).reshape(())
+        return torch.full((), float(dt), dtype=torch.float64, device=self.grid.device)
+
+    def _rk4_eager(self, time, dt, dt_dev=None):
+        names = self.conserved
+        if self._phi is None or set(self._phi) != set(names):
+            self._phi = {U: self.grid.empty() for U in names}
+        for U in names:
+            self._phi[U].zero_()
+        if dt_dev is None:
+            dt_dev = self._dt_tensor(dt)
+        time_i = time
+        self.deltat = dt
+        for ii in range(5):
+            flux = self.updateFlux()
+            U = [self._field_of(n) for n in names]
+            F = [self.grid.field(flux[n]) for n in names]
+            PHI = [self._phi[n] for n in names]
+            self.grid.rk_stage(U, PHI, F, dt_dev, ARK[ii], BRK[ii])
+            time = time_i + ETA[ii] * dt
+            self.time = time
+            self.updateVars()
+        self.cycle += 1
+        return time
+
+    # ----------------------------------------------------------- CUDA graphs
+    def use_graphs(self, enable=True):
+        """Record one whole rk4 step in a CUDA graph and replay it afterwards.
+
+        The EOM must not read ``simtime`` as a Python number and must keep the
+        same set of conserved variables.  The first rk4 call after enabling
+        runs eagerly (allocating every variable), the second records the graph.
+        """
+        self._graphs_enabled = bool(enable)
+        self._graph = None
+        self._graph_warm = False
+
+    def _rk4_graph(self, time, dt):
+        if not getattr(self, "_graph_warm", False):
+            self._graph_warm = True
+            return self._rk4_eager(time, dt)
+        if self._graph is None:
+            self._capture(time, dt)
+        self._g_dt.copy_(self._dt_tensor(dt))
+        self._g_t0.fill_(float(time)) if not isinstance(time, torch.Tensor) else self._g_t0.copy_(time)
+        self._graph.replay()
+        self.cycle += 1
+        self.deltat = dt
+        t = time + dt
+        self.time = t
+        return t
+
+    def _capture(self, time, dt):
+        self._unalias()
+        for n in self.conserved:
+            self._field_of(n)
+        before = {n: v.data for n, v in self.variables.items()}
+        self._g_dt = self._dt_tensor(dt).clone()
+        self._g_t0 = torch.zeros((), dtype=torch.float64, device=self.grid.device)
+        self._phi = {U: self.grid.empty() for U in self.conserved}
+        stream = torch.cuda.Stream(device=self.grid.device)
+        stream.wait_stream(torch.cuda.current_stream())
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(stream):
+            with torch.cuda.graph(g, stream=stream):
+                self._rk4_eager(self._g_t0, self._g_dt, dt_dev=self._g_dt)
+                # carry every rebound variable back into the storage the next
+                # replay reads
+                for n, v in self.variables.items():
+                    old = before.get(n)
+                    new = v.data
+                    if isinstance(old, torch.Tensor) and isinstance(new, torch.Tensor) and old is not new:
+                        if old.shape == new.shape or old.dim() == 0:
+                            old.copy_(new)
+        torch.cuda.current_stream().wait_stream(stream)
+        self.cycle -= 1
+        for n, old in before.items():
+            if isinstance(old, torch.Tensor):
+                self.variables[n].data = old
+        self._graph = g
+        # the capture itself did not advance the state: replay once for this step

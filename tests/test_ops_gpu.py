@@ -1,0 +1,177 @@
+"""Parity of the CUDA compact operators with the oracle, through the C ABI.
+
+Bar: relative L2 <= 1e-12 against the FP64 oracle for every operator, on
+periodic and one-sided (NONE) directions, on tile-aligned and ragged sizes, on
+null directions (n = 1 and n < 4) and on long lines (tile widths 32/16/8).
+"""
+import ctypes
+
+import numpy
+import pytest
+
+from tests.helpers import rel_l2, smooth_field, to_dev, to_host
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+TOL = 1.0e-12
+
+CASES = [
+    # (shape, periodic)
+    ((32, 32, 32), (True, True, True)),
+    ((40, 24, 16), (True, False, True)),
+    ((24, 40, 12), (False, True, False)),
+    ((9, 13, 11), (False, False, False)),
+    ((8, 8, 8), (True, True, True)),
+    ((100, 1, 1), (False, False, False)),
+    ((64, 64, 1), (True, False, False)),
+    ((48, 3, 10), (True, True, True)),
+    ((300, 4, 3), (True, False, False)),
+    ((600, 2, 9), (False, False, True)),
+    ((1024, 2, 1), (True, False, False)),
+]
+
+
+def _ids(c):
+    return "x".join(map(str, c[0])) + "-" + "".join("P" if p else "N" for p in c[1])
+
+
+@pytest.fixture(scope="module")
+def grids(oracle):
+    from pyranda_gb300.grid import Grid
+    out = {}
+    for shape, per in CASES:
+        x1 = (0.0, -0.5, 0.25)
+        xn = (1.0, 2.0, 3.0)
+        out[(shape, per)] = (Grid(shape, per, x1, xn), oracle.OracleGrid(shape, per, x1, xn))
+    return out
+
+
+@pytest.mark.parametrize("case", CASES, ids=_ids)
+def test_d1_d8_filters(grids, case):
+    g, o = grids[case]
+    v = smooth_field(case[0], seed=1)
+    dv = to_dev(v, torch)
+    for d in range(3):
+        assert rel_l2(to_host(g.d1(d, dv)), o.apply(0, d, v)) <= TOL, ("d1", d)
+        assert rel_l2(to_host(g.d8(d, dv)), o.apply(1, d, v)) <= TOL, ("d8", d)
+        assert rel_l2(to_host(g.filter("spectral", dv, d)), o.apply(2, d, v)) <= TOL, ("sf", d)
+        assert rel_l2(to_host(g.filter("gaussian", dv, d)), o.apply(3, d, v)) <= TOL, ("gf", d)
+
+
+@pytest.mark.parametrize("case", CASES, ids=_ids)
+def test_composites(grids, case):
+    g, o = grids[case]
+    v = smooth_field(case[0], seed=2)
+    w = smooth_field(case[0], seed=3)
+    q = smooth_field(case[0], seed=4)
+    dv, dw, dq = (to_dev(a, torch) for a in (v, w, q))
+    assert rel_l2(to_host(g.filter("spectral", dv)), o.sfilter(v)) <= TOL
+    assert rel_l2(to_host(g.filter("gaussian", dv)), o.gfilter(v)) <= TOL
+    assert rel_l2(to_host(g.ring(dv)), o.ring(v, 2)) <= TOL
+    assert rel_l2(to_host(g.ringv(dv, dw, dq)), o.ringv(v, w, q, 1)) <= TOL
+    for a, b in zip(g.grad(dv), o.grad(v)):
+        assert rel_l2(to_host(a), b) <= TOL
+    assert rel_l2(to_host(g.div(dv, dw, dq)), o.div(v, w, q)) <= TOL
+
+
+@pytest.mark.parametrize("case", CASES[:4], ids=_ids)
+def test_mesh(grids, case):
+    g, o = grids[case]
+    for which in range(8):
+        assert numpy.array_equal(to_host(g.mesh(which)), o.mesh(which)), which
+
+
+def test_in_place(grids):
+    """out may alias in for single sweeps and the 3-sweep filters (tile-local)."""
+    g, o = grids[CASES[1]]
+    v = smooth_field(CASES[1][0], seed=5)
+    for d in range(3):
+        t = to_dev(v, torch)
+        g.d1(d, t, out=t)
+        assert rel_l2(to_host(t), o.apply(0, d, v)) <= TOL
+    t = to_dev(v, torch)
+    g.filter("spectral", t, out=t)
+    assert rel_l2(to_host(t), o.sfilter(v)) <= TOL
+
+
+def test_constants_preserved(grids):
+    """Filters keep constants and d1/d8 of a constant vanish (difference form)."""
+    for (shape, per), (g, _) in grids.items():
+        c = g.field(torch.full(shape, 3.25, dtype=torch.float64, device="cuda"))
+        assert torch.equal(g.filter("spectral", c), c)
+        assert torch.equal(g.filter("gaussian", c), c)
+        assert float(g.d1(0, c).abs().max()) == 0.0
+        assert float(g.d8(0, c).abs().max()) == 0.0
+
+
+def test_host_variants(grids):
+    from pyranda_gb300 import _lib
+    g, o = grids[CASES[1]]
+    L = _lib.load()
+    v = smooth_field(CASES[1][0], seed=6)
+    out = numpy.zeros_like(v)
+    P = ctypes.POINTER(ctypes.c_double)
+    vin = v.ctypes.data_as(P)
+    vout = out.ctypes.data_as(P)
+    _lib.check(L.pg_d1_host(g.h, 1, vin, vout), "pg_d1_host")
+    assert rel_l2(out, o.apply(0, 1, v)) <= TOL
+    _lib.check(L.pg_d8_host(g.h, 2, vin, vout), "pg_d8_host")
+    assert rel_l2(out, o.apply(1, 2, v)) <= TOL
+    _lib.check(L.pg_filter_host(g.h, 0, 3, vin, vout), "pg_filter_host")
+    assert rel_l2(out, o.sfilter(v)) <= TOL
+    _lib.check(L.pg_ring_host(g.h, vin, vout), "pg_ring_host")
+    assert rel_l2(out, o.ring(v, 2)) <= TOL
+
+
+def test_errors_do_not_exit(grids):
+    """Bad arguments come back as a status, never a process exit (compact_d1.f90:65-72 stopped)."""
+    from pyranda_gb300 import _lib
+    L = _lib.load()
+    g, _ = grids[CASES[0]]
+    assert L.pg_d1(g.h, 7, None, None, None) == _lib.PG_EINVAL
+    assert L.pg_filter(g.h, 5, 0, None, None, None) == _lib.PG_EINVAL
+    h = ctypes.c_void_p()
+    grid = _lib.pg_grid()
+    grid.n[0], grid.n[1], grid.n[2] = 6, 1, 1  # 4 <= n < 8 has no valid stencil
+    assert L.pg_create(ctypes.byref(grid), ctypes.byref(h)) == _lib.PG_EBADSHAPE
+    grid.n[0] = 0
+    assert L.pg_create(ctypes.byref(grid), ctypes.byref(h)) == _lib.PG_EBADSHAPE
+
+
+def test_reductions_and_timestep(grids):
+    g, o = grids[CASES[0]]
+    shape = CASES[0][0]
+    u, v, w = (smooth_field(shape, s) for s in (7, 8, 9))
+    c = 2.0 + numpy.abs(smooth_field(shape, 10))
+    du, dvv, dw, dc = (to_dev(a, torch) for a in (u, v, w, c))
+    d1, d2, d3 = o.spacing()[1]
+    gl = min(d1, d2, d3)
+    ref = 1.0 / numpy.max(numpy.abs(u) / d1 + numpy.abs(v) / d2 + numpy.abs(w) / d3 + numpy.abs(c) / gl)
+    assert abs(float(g.courant(du, dvv, dw, dc)) - ref) <= 1e-15 * ref
+    assert abs(float(g.courant(du, 0.0, 0.0, dc)) - 1.0 / numpy.max(numpy.abs(u) / d1 + numpy.abs(c) / gl)) <= 1e-15
+    bulk = numpy.abs(w) * 1e-3
+    ref = numpy.min(c * gl * gl / numpy.maximum(1e-12, bulk))
+    assert abs(float(g.diff(to_dev(bulk, torch), dc)) - ref) <= 1e-14 * ref
+    assert abs(float(g.reduce(0, du)) - u.sum()) <= 1e-12 * numpy.abs(u).sum()
+    assert float(g.reduce(1, du)) == u.max()
+    assert float(g.reduce(2, du)) == u.min()
+    du[3, 4, 5] = float("nan")
+    assert numpy.isnan(float(g.reduce(1, du)))
+
+
+def test_rk_stage(grids):
+    g, _ = grids[CASES[0]]
+    shape = CASES[0][0]
+    U = [smooth_field(shape, s) for s in (11, 12)]
+    PHI = [smooth_field(shape, s) for s in (13, 14)]
+    F = [smooth_field(shape, s) for s in (15, 16)]
+    dt, A, B = 0.01, -0.48, 0.74
+    dU = [to_dev(a, torch) for a in U]
+    dP = [to_dev(a, torch) for a in PHI]
+    dF = [to_dev(a, torch) for a in F]
+    g.rk_stage(dU, dP, dF, torch.tensor(dt, dtype=torch.float64, device="cuda"), A, B)
+    for k in range(2):
+        phi = dt * F[k] + A * PHI[k]
+        assert rel_l2(to_host(dP[k]), phi) <= 1e-15
+        assert rel_l2(to_host(dU[k]), U[k] + B * phi) <= 1e-15

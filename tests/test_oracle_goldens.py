@@ -1,0 +1,66 @@
+"""The oracle against the reference's own golden scalars (tests/cases/*.py).
+
+The oracle is a CPU restatement of parcop and of pyranda's Python driver; these
+tests pin it to the values the reference test-suite records, with the
+reference's tolerance (1e-4 relative, tests/run_tests.py:84).
+"""
+import json
+import os
+
+import numpy
+import pytest
+
+from tests import scripts
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_scalars.json")))["values"]
+TOL = 1.0e-4
+
+
+def _close(v, name):
+    g = GOLD[name]["value"]
+    assert abs(v - g) / abs(g) < TOL, (name, v, g)
+    return abs(v - g) / abs(g)
+
+
+def test_unit_test_3d(oracle):
+    err = scripts.unit_test(oracle.OracleSim)
+    # the restatement reproduces the reference value far inside its tolerance
+    assert _close(err, "unit-test-3D") < 1e-9
+
+
+@pytest.mark.parametrize("n", [50, 100, 200, 300, 400])
+def test_advection_1d(oracle, n):
+    err = scripts.advection_1d(oracle.OracleSim, n)
+    _close(err, "advec-1d-%d" % n)
+
+
+def test_taylor_green_32(oracle):
+    enst = scripts.taylor_green(oracle.OracleSim, 32, tstop=0.1, timestep=lambda s: s.addPackage("Timestep"))
+    assert _close(enst, "taylorgreen") < 1e-9
+
+
+def test_shu_osher(oracle):
+    cr = scripts.shu_osher(oracle.OracleSim, packages=lambda s: (s.addPackage("BC"), s.addPackage("Timestep")))
+    assert _close(cr, "shu-osher-CR") < 1e-8
+
+
+def test_dense_operator_matches_banded(oracle):
+    """A . (A^-1 B v) = B v: the dense D = A^-1 B of the line evaluator
+    reproduces the banded solve applied to a field (compact_basetype.f90:199-205)."""
+    g = oracle.OracleGrid((24, 1, 1), (True, False, False), (0, 0, 0), (1, 0, 0))
+    r = numpy.random.default_rng(3)
+    v = numpy.asfortranarray(r.standard_normal((24, 1, 1)))
+    for op in (0, 1, 2, 3):
+        D = g.dense(op, 0)
+        ref = g.apply(op, 0, v)[:, 0, 0]
+        assert numpy.allclose(D @ v[:, 0, 0], ref, rtol=0, atol=1e-12 * max(1.0, abs(ref).max()))
+
+
+def test_oracle_polynomial_exactness(oracle):
+    """One-sided d1 closures differentiate x, x^2, x^3 exactly (examples/unit_test.py:67-80)."""
+    n = 32
+    g = oracle.OracleGrid((n, 1, 1), (False, False, False), (0, 0, 0), (1, 0, 0))
+    x = g.mesh(0)
+    for p in (1, 2, 3):
+        d = g.ddx(x ** p)
+        assert numpy.abs(d - p * x ** (p - 1)).max() < 1e-12
