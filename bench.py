@@ -1,0 +1,376 @@
+"""Throughput of the 256^3 compressible Taylor-Green RK step on GB300.
+
+Metric: Mpoint-RK-steps/s = nx*ny*nz*steps / seconds / 1e6 for the
+Taylor-Green EOM of pyranda's examples/TaylorGreen.py (Navier-Stokes with
+LAD artificial viscosity, compact filters, 10th-order Pade derivatives,
+LSRK(5,4) with the ALG update after every stage) on a periodic 256^3 grid.
+
+Headline (``value``): the fast path -- single-precision compact sweeps on FP64
+fields, FP64 RK state and reductions, the whole step recorded in a CUDA graph.
+The same line reports the plain FP64 path (reference arithmetic) and the field
+L2 error of the fast path against it.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Under torchrun each rank runs an independent replica (the path does not shard:
+one grid per GPU), value = all ranks' points*steps / max-over-ranks time.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mpoint-RK-steps/s at 256³ TGV on 1 GB300: plain FP64 vs split-FP32+graphs, at L2 err"
+UNIT = "Mpoint-RK-steps/s"
+CFL = 0.5
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--n", type=int, default=256, help="grid points per direction")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
+    return p.parse_args()
+
+
+# --------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------- CPU baseline
+def _cpu_worker(args):
+    """One oracle process: TGV on its own sub-grid, single-threaded OpenMP."""
+    shape, steps, warmup = args
+    os.environ["OMP_NUM_THREADS"] = "1"
+    sys.path.insert(0, ROOT)
+    from oracle import oracle
+    from tests import scripts
+    oracle.set_threads(1)
+    import numpy
+
+    mesh = "\n".join("%sdom = (0.0, %r, %d, periodic=True)" % (ax, 2 * math.pi * (n - 1) / n, n)
+                     for ax, n in zip("xyz", shape))
+    ss = oracle.OracleSim("TG", mesh)
+    ss.addPackage("Timestep")
+    ss.EOM(scripts.TGV_EOM)
+    ss.setIC(scripts.TGV_IC)
+    dt = ss.variables["dt"].data * CFL
+    t = 0.0
+    for _ in range(warmup):
+        t = ss.rk4(t, dt)
+        dt = ss.variables["dt"].data * CFL
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        t = ss.rk4(t, dt)
+        dt = ss.variables["dt"].data * CFL
+    wall = time.perf_counter() - t0
+    return int(numpy.prod(shape)), steps, wall
+
+
+def cpu_baseline(steps, warmup, shape=(128, 128, 64)):
+    """The oracle (a CPU port of parcop + pyranda's driver) on every host core.
+
+    One single-threaded process per core, each on its own periodic sub-grid
+    of the Taylor-Green problem (the per-point work of a decomposed run
+    without its halo exchange).  Returns (Mpoint-RK-steps/s, cores, sample).
+    """
+    import multiprocessing as mp
+    from oracle import oracle
+    oracle.build()
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_cpu_worker, [(shape, steps, warmup)] * cores)
+    pts = sum(r[0] * r[1] for r in res)
+    wall = max(r[2] for r in res)
+    sample = ("%d processes x TGV %dx%dx%d periodic, %d timed RK steps each after %d warm-up, "
+              "oracle (CPU port of parcop, FP64), 1 thread per process" % (cores, *shape, steps, warmup))
+    return pts / wall / 1e6, cores, sample, wall
+
+
+# --------------------------------------------------------------------------- distributed
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    k = max(1, args.steps)
+    w = max(0, args.warmup)
+    # size the per-step sample so the whole run stays within a few minutes
+    est_us_per_pt_step = 6.0
+    budget_s = 150.0 / (k + w)
+    shapes = [(128, 128, 64), (96, 96, 64), (64, 64, 64), (64, 64, 32), (32, 32, 32)]
+    shape = shapes[-1]
+    for s in shapes:
+        if s[0] * s[1] * s[2] * est_us_per_pt_step * 1e-6 <= budget_s:
+            shape = s
+            break
+    v, cores, sample, wall = cpu_baseline(k, w, shape)
+    line = {"metric": METRIC, "value": round(v, 4), "unit": UNIT, "n_gpus": args.gpus, "steps": k, "warmup": w,
+            "ms_per_step": round(wall / k * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (Taylor-Green initial condition)",
+            "impl": "reference",
+            "config": {"workload": "compressible Taylor-Green vortex, periodic, LAD + compact filters, LSRK(5,4)",
+                       "grid": [args.n] * 3, "cpu_sample_grid": list(shape)},
+            "cpu_baseline": {"value": round(v, 4), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------------------ GPU
+def make_sim(n, precision, graphs):
+    from pyranda_gb300 import pyrandaSim, pyrandaTimestep
+    from tests import scripts
+    ss = scripts.make_tgv(pyrandaSim, n, lambda s: s.addPackage(pyrandaTimestep(s)), silent=True,
+                          precision=precision)
+    if graphs:
+        ss.use_graphs(True)
+    return ss
+
+
+def run_steps(ss, k, t0=0.0):
+    t = t0
+    for _ in range(k):
+        dt = ss.variables["dt"].data * CFL
+        t = ss.rk4(t, dt)
+    return t
+
+
+def time_steps(ss, k, torch, dist_on):
+    """CUDA-event time of k steps on the current stream, barrier + sync around."""
+    if dist_on:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    run_steps(ss, k)
+    e.record()
+    torch.cuda.synchronize()
+    if dist_on:
+        dist.barrier()
+    return s.elapsed_time(e) / 1e3
+
+
+def sweep_roofline(ss, torch, reps=20):
+    """Average CUDA-event duration of each sweep kernel class on one 256^3 field."""
+    g = ss.grid
+    v = ss.variables["rho"].data
+    out = g.empty()
+    res = {}
+    cases = {
+        "d1": lambda d: g.d1(d, v, out=out),
+        "sfilter": lambda d: g.filter("spectral", v, d, out=out),
+        "d8": lambda d: g.d8(d, v, out=out),
+        "gfilter": lambda d: g.filter("gaussian", v, d, out=out),
+    }
+    for name, f in cases.items():
+        for d in range(3):
+            f(d)
+            torch.cuda.synchronize()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            for _ in range(reps):
+                f(d)
+            e.record()
+            torch.cuda.synchronize()
+            res["%s_%s" % (name, "xyz"[d])] = s.elapsed_time(e) / reps / 1e3
+    return res
+
+
+def l2_errors(a, b, names):
+    out = {}
+    for n in names:
+        x, y = a.variables[n].data, b.variables[n].data
+        out[n] = float(((x - y).norm() / y.norm()).item())
+    return out
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    world, rank, local = dist_setup()
+    dist_on = world > 1
+    if dist_on:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.cuda.current_device()
+
+    # CPU baseline before any forked process could inherit a CUDA context
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, cores, sample, _ = cpu_baseline(2, 1)
+        cpu = {"value": round(v, 4), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+
+    from pyranda_gb300 import _lib
+    n = args.n
+    npts = n ** 3
+    k, w = args.steps, max(3, args.warmup)
+
+    # ---- headline: FP32 sweeps + CUDA graph
+    fast = make_sim(n, "fp32", graphs=True)
+    c0 = _lib.launch_count()
+    run_steps(fast, 1)             # eager step (first graph-mode call)
+    launches_per_step = _lib.launch_count() - c0
+    run_steps(fast, w - 1)          # capture + replays
+    clocks = ClockSampler(dev)
+    clocks.start()
+    t_fast = time_steps(fast, k, torch, dist_on)
+    ck = clocks.stop()
+    if dist_on:
+        tt = torch.tensor([t_fast], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_fast = float(tt)
+    value = npts * k * world / t_fast / 1e6
+
+    # ---- plain FP64 path, same IC, same number of steps (no graph)
+    extra = {}
+    if not args.no_fp64:
+        plain = make_sim(n, "fp64", graphs=False)
+        run_steps(plain, w)
+        t64 = time_steps(plain, k, torch, dist_on)
+        extra["fp64_plain"] = {"value": round(npts * k * world / t64 / 1e6, 4), "unit": UNIT,
+                               "ms_per_step": round(t64 / k * 1e3, 3)}
+        # accuracy of the fast path: both sims advanced w + k steps from the same IC
+        errs = l2_errors(fast, plain, ["rho", "rhou", "rhov", "rhow", "Et"])
+        extra["l2_err_vs_fp64"] = {kk: float("%.3e" % vv) for kk, vv in errs.items()}
+        extra["l2_err_steps"] = w + k
+        del plain
+        torch.cuda.empty_cache()
+
+    # ---- dominant-kernel roofline (sweeps on one 256^3 field, FP32 arithmetic)
+    import json as _json
+    peaks = {}
+    try:
+        peaks = _json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    sw = sweep_roofline(fast, torch)
+    dom = "sfilter_y"
+    dur = sw[dom]
+    achieved = 16.0 * npts / dur / 1e9
+    roof = {"bound": "hbm", "kernel": "sweep_kernel<float,r4,periodic,implicit,addback,dir=y>",
+            "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
+            "traffic": None, "algorithmic_bytes_per_launch": 16 * npts,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s",
+            "sweep_ms": {kk: round(vv * 1e3, 4) for kk, vv in sw.items()}}
+
+    # ---- end to end: host state in pinned memory, copied in and out every step
+    names = fast.conserved
+    host = {nm: torch.empty((n, n, n), dtype=torch.float64).pin_memory() for nm in names}
+    for nm in names:
+        host[nm].copy_(fast.variables[nm].data.permute(2, 1, 0))
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(k):
+        for nm in names:
+            fast.variables[nm].data.permute(2, 1, 0).copy_(host[nm], non_blocking=True)
+        run_steps(fast, 1)
+        for nm in names:
+            host[nm].copy_(fast.variables[nm].data.permute(2, 1, 0), non_blocking=True)
+    e.record()
+    torch.cuda.synchronize()
+    t_e2e = s.elapsed_time(e) / 1e3
+    if dist_on:
+        tt = torch.tensor([t_e2e], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = float(tt)
+    nbytes = len(names) * npts * 8
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": k, "warmup": w,
+            "ms_per_step": round(t_fast / k * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 sweeps / f64 state",
+            "data": "synthetic (Taylor-Green initial condition of examples/TaylorGreen.py)",
+            "config": {"workload": "compressible Taylor-Green vortex %d^3 periodic, LAD + compact filters, "
+                                   "LSRK(5,4), CFL 0.5" % n,
+                       "grid": [n, n, n], "path": "fp32 sweeps + CUDA graph per RK step",
+                       "l2": "inputs larger than L2 (~40 fields of %d MiB)" % (npts * 8 >> 20),
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(npts * k * world / t_e2e / 1e6, 4), "unit": UNIT,
+                    "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+            "gpu_launches": int(launches_per_step * k),
+            "clocks": ck,
+        }
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+    if dist_on:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

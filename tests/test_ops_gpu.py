@@ -26,7 +26,7 @@ CASES = [
     ((100, 1, 1), (False, False, False)),
     ((64, 64, 1), (True, False, False)),
     ((48, 3, 10), (True, True, True)),
-    ((300, 4, 3), (True, False, False)),
+    ((300, 3, 2), (True, False, False)),
     ((600, 2, 9), (False, False, True)),
     ((1024, 2, 1), (True, False, False)),
 ]

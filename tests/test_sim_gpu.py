@@ -1,0 +1,124 @@
+"""End-to-end pyrandaSim on the GPU against the reference goldens and the oracle.
+
+The scripts are the reference's regression scripts (tests/scripts.py); the
+product must reproduce the reference's golden scalars within the reference's
+tolerance (1e-4 relative) and the oracle's fields to relative L2 <= 1e-12.
+"""
+import json
+import os
+
+import numpy
+import pytest
+
+from tests import scripts
+from tests.helpers import rel_l2, to_host
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_scalars.json")))["values"]
+
+
+def _close(v, name, tol=1.0e-4):
+    g = GOLD[name]["value"]
+    rel = abs(v - g) / abs(g)
+    assert rel < tol, (name, v, g, rel)
+    return rel
+
+
+def _ts(ss):
+    from pyranda_gb300 import pyrandaTimestep
+    ss.addPackage(pyrandaTimestep(ss))
+
+
+def _bc_ts(ss):
+    from pyranda_gb300 import pyrandaBC, pyrandaTimestep
+    ss.addPackage(pyrandaBC(ss))
+    ss.addPackage(pyrandaTimestep(ss))
+
+
+def test_unit_test_golden():
+    from pyranda_gb300 import pyrandaSim
+    err = scripts.unit_test(pyrandaSim, silent=True)
+    assert _close(err, "unit-test-3D") < 1e-9
+
+
+@pytest.mark.parametrize("n", [50, 100, 200, 300, 400])
+def test_advection_golden(n):
+    from pyranda_gb300 import pyrandaSim
+    err = scripts.advection_1d(pyrandaSim, n, silent=True)
+    _close(err, "advec-1d-%d" % n)
+
+
+def test_taylor_green_golden():
+    from pyranda_gb300 import pyrandaSim
+    enst = scripts.taylor_green(pyrandaSim, 32, 0.1, _ts, silent=True)
+    assert _close(enst, "taylorgreen") < 1e-9
+
+
+def test_shu_osher_golden():
+    from pyranda_gb300 import pyrandaSim
+    cr = scripts.shu_osher(pyrandaSim, _bc_ts, silent=True)
+    assert _close(cr, "shu-osher-CR") < 1e-8
+
+
+def test_taylor_green_fields_match_oracle(oracle):
+    """Every TGV field after 3 RK steps agrees with the oracle to 1e-12 (relative L2)."""
+    from pyranda_gb300 import pyrandaSim
+    ss = scripts.make_tgv(pyrandaSim, 24, _ts, silent=True)
+    so = scripts.make_tgv(oracle.OracleSim, 24, lambda s: s.addPackage("Timestep"))
+    dt = float(ss.variables["dt"].data) * 0.5
+    dto = so.variables["dt"].data * 0.5
+    assert abs(dt - dto) <= 1e-14 * dto
+    t = to = 0.0
+    for _ in range(3):
+        t = ss.rk4(t, dt)
+        to = so.rk4(to, dto)
+        dt = float(ss.variables["dt"].data) * 0.5
+        dto = so.variables["dt"].data * 0.5
+    for name in ["rho", "rhou", "rhov", "rhow", "Et", "u", "p", "mu", "tauxx", "enst"]:
+        a = to_host(ss.variables[name].data)
+        b = so.variables[name].data
+        assert rel_l2(a, b) <= 1e-12, (name, rel_l2(a, b))
+    # beta = gbar(|ring(div)| rho): the TGV dilatation is analytically zero, so
+    # div is a sum of O(1) terms cancelling to rounding level and ring() takes
+    # its 8th derivative; the bound scales with that cancellation.
+    ux, vy, wz, div = (so.variables[k].data for k in ("ux", "vy", "wz", "div"))
+    cancel = numpy.abs(ux).max() / max(numpy.abs(div).max(), 1e-300)
+    e = rel_l2(to_host(ss.variables["beta"].data), so.variables["beta"].data)
+    assert e <= 1e-13 * cancel * 4200.0, (e, cancel)
+
+
+def test_fp32_path_error_bound():
+    """The single-precision sweeps stay within 1e-6 (relative L2) of FP64 over 10 TGV steps."""
+    from pyranda_gb300 import pyrandaSim
+    s64 = scripts.make_tgv(pyrandaSim, 32, _ts, silent=True)
+    s32 = scripts.make_tgv(pyrandaSim, 32, _ts, silent=True, precision="fp32")
+    dt = float(s64.variables["dt"].data) * 0.5
+    t = 0.0
+    for _ in range(10):
+        s64.rk4(t, dt)
+        t = s32.rk4(t, dt)
+    for name in ["rho", "rhou", "rhov", "Et"]:
+        e = rel_l2(to_host(s32.variables[name].data), to_host(s64.variables[name].data))
+        assert e <= 1e-6, (name, e)
+
+
+def test_graph_replay_matches_eager():
+    """A CUDA-graph replayed rk4 step gives the eager result bit for bit."""
+    from pyranda_gb300 import pyrandaSim
+    se = scripts.make_tgv(pyrandaSim, 24, _ts, silent=True)
+    sg = scripts.make_tgv(pyrandaSim, 24, _ts, silent=True)
+    sg.use_graphs(True)
+    dt = se.variables["dt"].data * 0.5
+    dtg = sg.variables["dt"].data * 0.5
+    t = tg = 0.0
+    for _ in range(4):
+        t = se.rk4(t, dt)
+        tg = sg.rk4(tg, dtg)
+        dt = se.variables["dt"].data * 0.5
+        dtg = sg.variables["dt"].data * 0.5
+    torch.cuda.synchronize()
+    for name in ["rho", "rhou", "Et", "u", "mu", "dt"]:
+        a, b = se.variables[name].data, sg.variables[name].data
+        assert torch.equal(a, b), name
