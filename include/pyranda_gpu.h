@@ -129,6 +129,23 @@ int pg_reduce(pg_handle* h, int op, const double* in, int64_t n, double* out, vo
  * leaves it unchanged (pyranda.py:359-369 checked for NaN on the host). */
 int pg_check_finite(const double* in, int64_t n, int* flag, void* stream);
 
+/* Allocation-free reduction.  No counterpart in the reference: parcop's
+ * reductions ran through MPI on the host (pyrandaMPI.py:307-326).
+ * For callers that cannot allocate device memory (a host framework whose
+ * allocator forbids cudaMalloc, or code that never creates a pg_handle and so
+ * owns no workspace): same result as pg_reduce (op 0 = sum, 1 = max, 2 = min
+ * of n values into the device scalar *out) with its per-block partials kept in
+ * a static device array of PG_NOALLOC_MAX_BLOCKS doubles (32 KiB) that every
+ * GPU holds from library load to process exit.  n is limited to
+ * PG_NOALLOC_MAX_VALUES; larger n returns PG_EBADSHAPE without launching.
+ * The first call on a device looks up the array's address there; make it
+ * before starting any stream capture.  All calls share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller. */
+#define PG_NOALLOC_CHUNK 8192
+#define PG_NOALLOC_MAX_BLOCKS 4096
+#define PG_NOALLOC_MAX_VALUES ((int64_t)PG_NOALLOC_CHUNK * PG_NOALLOC_MAX_BLOCKS)
+int pg_reduce_noalloc(int op, const double* in, int64_t n, double* out, void* stream);
+
 /* Host-pointer variants: copy in, run on an internal stream, copy out,
  * synchronise.  For tests and for callers that hold host arrays. */
 int pg_d1_host(pg_handle* h, int dir, const double* in, double* out);
