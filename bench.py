@@ -41,6 +41,11 @@ def parse():
     p.add_argument("--n", type=int, default=256, help="grid points per direction")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
+    p.add_argument("--mode", default="step", choices=["step", "sweeps", "profile"],
+                   help="sweeps: time every directional sweep kernel alone on one n^3 field; "
+                        "profile: one eager RK step between cudaProfilerStart/Stop (for ncu)")
+    p.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    p.add_argument("--reps", type=int, default=20)
     return p.parse_args()
 
 
@@ -249,10 +254,44 @@ def l2_errors(a, b, names):
     return out
 
 
+def sweeps_only(args):
+    """Per-sweep CUDA-event timings on one periodic n^3 TGV field, both precisions."""
+    import torch
+    torch.cuda.set_device(0)
+    npts = args.n ** 3
+    out = {"n": args.n}
+    for prec in ("fp32", "fp64"):
+        ss = make_sim(args.n, prec, graphs=False)
+        sw = sweep_roofline(ss, torch, reps=args.reps)
+        out[prec] = {k: {"ms": round(v * 1e3, 4), "GB/s": round(16.0 * npts / v / 1e9, 1)} for k, v in sw.items()}
+        del ss
+        torch.cuda.empty_cache()
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def profile_step(args):
+    """One eager TGV RK step inside a profiler range, after 2 warm-up steps."""
+    import torch
+    torch.cuda.set_device(0)
+    ss = make_sim(args.n, args.precision, graphs=False)
+    run_steps(ss, 2)
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStart()
+    run_steps(ss, 1)
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStop()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.mode == "sweeps":
+        return sweeps_only(args)
+    if args.mode == "profile":
+        return profile_step(args)
     import torch
     world, rank, local = dist_setup()
     dist_on = world > 1

@@ -75,6 +75,10 @@ typedef struct pg_handle pg_handle;
 int pg_create(const pg_grid* grid, pg_handle** out);
 /* Frees the handle and its device workspace. */
 int pg_destroy(pg_handle* h);
+/* Reads and clears the handle's device status word (synchronises with the
+ * device).  *status is PG_OK, or PG_ETIMEOUT when a kernel's bounded wait on
+ * an asynchronous copy gave up (the affected output is then not valid). */
+int pg_device_status(pg_handle* h, int* status);
 /* Switch the arithmetic of later sweeps on this handle (pg_precision). */
 int pg_set_precision(pg_handle* h, int precision);
 /* Patch spacing (used by the d1 metric) and mesh spacing d1..d3. */

@@ -41,6 +41,7 @@ SIGNATURES = [
     ("pg_create", I, [ctypes.POINTER(pg_grid), ctypes.POINTER(P)]),
     ("pg_destroy", I, [P]),
     ("pg_set_precision", I, [P, I]),
+    ("pg_device_status", I, [P, ctypes.POINTER(ctypes.c_int)]),
     ("pg_get_spacing", I, [P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     ("pg_last_error", ctypes.c_char_p, []),
     ("pg_version", ctypes.c_char_p, []),

@@ -43,7 +43,9 @@ struct pg_handle {
   DevOp ops[2][OPK_COUNT][3];
   void* tables = nullptr;
   double* work = nullptr;     // one field: temporary of the 3-sweep filters
+  double* work2 = nullptr;    // one field: forward-elimination values of a sweep
   double* partial = nullptr;  // reduction partials
+  int* status = nullptr;      // device status word (PG_ETIMEOUT from a bounded wait)
   double* host_in = nullptr;  // device buffers of the host-pointer variants
   double* host_out = nullptr;
   cudaStream_t stream = nullptr;
@@ -67,7 +69,7 @@ bool bad_dir(int d) { return d < 0 || d > 2; }
 
 int sweep(pg_handle* h, int kind, int dir, const double* in, double* out, int epi, double scale, void* st) {
   const DevOp& op = h->ops[h->precision][kind][dir];
-  SweepLaunch s{in, out, h->n[0], h->n[1], h->n[2], dir, scale, epi};
+  SweepLaunch s{in, out, h->n[0], h->n[1], h->n[2], dir, scale, epi, h->status, h->work2};
   return launch_sweep(op, h->precision, s, st);
 }
 
@@ -169,7 +171,7 @@ int pg_create(const pg_grid* g, pg_handle** out) {
         set_error("pg_create: direction %d has %d points; a non-null direction needs at least 8", d, g->n[d]);
         return rc;
       }
-      total += (size_t)h->n[d] * 9 * 2 * (sizeof(double) + sizeof(float));
+      total += (size_t)h->n[d] * (9 + 12) * (sizeof(double) + sizeof(float)) + 64;
     }
   cudaError_t e = cudaMalloc(&h->tables, total);
   if (e != cudaSuccess) {
@@ -180,6 +182,7 @@ int pg_create(const pg_grid* g, pg_handle** out) {
   std::vector<unsigned char> host(total);
   size_t off = 0;
   auto put = [&](const std::vector<double>& v, bool f32) -> const void* {
+    off = (off + 15) & ~(size_t)15;  // 16-byte aligned rows for vector loads
     const void* dptr = (unsigned char*)h->tables + off;
     if (f32) {
       for (size_t i = 0; i < v.size(); i++) {
@@ -205,13 +208,22 @@ int pg_create(const pg_grid* g, pg_handle** out) {
         op.addback = t.addback;
         op.null_op = t.null_op;
         op.rhs = put(t.rhs, p == PG_FP32);
-        op.lu = put(t.lu, p == PG_FP32);
+        // solve coefficients regrouped 12 per row for vector loads:
+        // [c1 c2 c6 c7 | c3 c4 c5 c8 | c9 0 0 0]
+        std::vector<double> lu12((size_t)t.n * 12, 0.0);
+        static const int order[9] = {0, 1, 5, 6, 2, 3, 4, 7, 8};
+        for (int i = 0; i < t.n && !t.null_op; i++)
+          for (int q = 0; q < 9; q++) lu12[(size_t)i * 12 + q] = t.lu[(size_t)i * 9 + order[q]];
+        op.lu = put(lu12, p == PG_FP32);
         const int mid = t.n / 2;
         for (int l = 0; l < 9; l++) op.rhs_in[l] = t.null_op ? 0.0 : t.rhs[(size_t)mid * 9 + l];
       }
   e = cudaMemcpy(h->tables, host.data(), total, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMalloc(&h->work, (size_t)h->npts * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&h->work2, (size_t)h->npts * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&h->partial, (size_t)kReduceBlocks * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&h->status, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(h->status, 0, sizeof(int));
   if (e != cudaSuccess) {
     set_error("pg_create: %s", cudaGetErrorString(e));
     pg_destroy(h);
@@ -225,11 +237,22 @@ int pg_destroy(pg_handle* h) {
   if (!h) return PG_OK;
   if (h->tables) cudaFree(h->tables);
   if (h->work) cudaFree(h->work);
+  if (h->work2) cudaFree(h->work2);
   if (h->partial) cudaFree(h->partial);
+  if (h->status) cudaFree(h->status);
   if (h->host_in) cudaFree(h->host_in);
   if (h->host_out) cudaFree(h->host_out);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
+  return PG_OK;
+}
+
+int pg_device_status(pg_handle* h, int* status) {
+  if (!h || !status) return PG_EINVAL;
+  int v = 0;
+  PG_CUDA(cudaMemcpy(&v, h->status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (v != 0) PG_CUDA(cudaMemset(h->status, 0, sizeof(int)));
+  *status = v;
   return PG_OK;
 }
 

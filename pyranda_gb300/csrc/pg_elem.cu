@@ -121,18 +121,21 @@ __global__ void reduce_final(const double* __restrict__ partial, int np, double*
   if (threadIdx.x == 0) *out = anynan ? NAN : acc;
 }
 
-// courant: vrate = |u|/d1 + |v|/d2 + |w|/d3 ; crate = |c|/GridLen ; max(vrate+crate)
+// courant: vrate = |u|/d1 + |v|/d2 + |w|/d3 ; crate = |c|/GridLen ; max(vrate+crate).
+// The spacings are uniform, so each division is a multiplication by the
+// reciprocal computed once on the host (FP64 division costs ~10 FP64-pipe
+// instructions on GB300; the product differs from the quotient by <= 1 ulp).
 __global__ void courant_partial(const double* __restrict__ u, const double* __restrict__ v,
                                 const double* __restrict__ w, const double* __restrict__ c, double vconst,
-                                double wconst, double d1, double d2, double d3, double gl, int64_t n,
+                                double wconst, double r1, double r2, double r3, double rgl, int64_t n,
                                 double* __restrict__ partial) {
   double acc = -DBL_MAX;
   bool nan = false;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double vv = v ? v[i] : vconst;
     const double ww = w ? w[i] : wconst;
-    const double vrate = fabs(u[i]) / d1 + fabs(vv) / d2 + fabs(ww) / d3;
-    const double x = vrate + fabs(c[i]) / gl;
+    const double vrate = fabs(u[i]) * r1 + fabs(vv) * r2 + fabs(ww) * r3;
+    const double x = vrate + fabs(c[i]) * rgl;
     nan |= (x != x);
     acc = fmax(acc, x);
   }
@@ -236,7 +239,8 @@ int launch_courant(const double* u, const double* v, const double* w, const doub
                    void* stream) {
   const int g = grid_for(n) < kReduceBlocks ? grid_for(n) : kReduceBlocks;
   cudaStream_t s = (cudaStream_t)stream;
-  courant_partial<<<g, kThreads, 0, s>>>(u, v, w, c, vconst, wconst, d[0], d[1], d[2], gridlen, n, partial);
+  courant_partial<<<g, kThreads, 0, s>>>(u, v, w, c, vconst, wconst, 1.0 / d[0], 1.0 / d[1], 1.0 / d[2],
+                                         1.0 / gridlen, n, partial);
   reduce_final<1><<<1, kThreads, 0, s>>>(partial, g, out);
   invert_scalar<<<1, 1, 0, s>>>(out);
   count_launch(2);

@@ -45,6 +45,8 @@ struct SweepLaunch {
   int dir;
   double epi_scale;  // ring scale
   int epi;           // EPI_*
+  int* status;       // device status word of the handle
+  void* scratch;     // one field of forward-elimination values (handle workspace)
 };
 
 // Launches one directional sweep.  Returns a pg_status.

@@ -1,25 +1,33 @@
-// Directional compact-operator sweeps for sm_103a.
+// Directional compact-operator sweeps for sm_103a (templates; instantiated in
+// pg_sweep_f64.cu and pg_sweep_f32.cu).
 //
-// One CTA owns a tile of LB lines (LB = blockDim.x, one thread per line) and
-// the whole length n of those lines.  The tile is staged in shared memory with
-// coalesced loads (x lines: each line is contiguous; y/z lines: the LB lines
-// are LB consecutive x positions), then every thread evaluates its own line
-// in place in shared memory:
-//   1. RHS stencil      compact_d1.f90:113-193 (d1) / compact_r4.f90:106-193 (r4)
-//   2. banded solve     pentadiagonal.f90:629-651 (bpentLUS3x)
-//      or cyclic solve  pentadiagonal.f90:654-684 (ppentLUS3x)
-//   3. fused epilogue   filter add-back (compact_r4.f90:209-234), ring max
-//                       (operators.f90:636-639), divergence accumulation
-// and the tile is written back coalesced.  The d1 metric 1/dx is folded into
-// the RHS weights on the host.
+// One thread owns one grid line and streams it once forward and once
+// backward:
+//   forward:  RHS stencil through a register window (compact_d1.f90:113-193,
+//             compact_r4.f90:106-193) fused with the forward elimination of
+//             the banded (bpentLUS3x, pentadiagonal.f90:629-651) or cyclic
+//             (ppentLUS3x, :654-684) solve; the eliminated values go to a
+//             scratch array laid out [position][line], so every access to it is
+//             coalesced whatever the sweep direction;
+//   backward: back substitution, fused with the epilogue (filter add-back
+//             compact_r4.f90:209-234, ring max operators.f90:636-639,
+//             divergence accumulation) and the store.
+// Nothing is staged in shared memory, so occupancy is bounded only by the
+// number of lines and by registers.  y/z sweeps read and write coalesced (the
+// 32 lines of a warp are 32 x-neighbours); x sweeps read each line's 32-byte
+// sectors through L1.  The forward window lives in a 16-slot register ring
+// that doubles as the prefetch queue; the backward loop prefetches 8 rows
+// ahead.  Offsets along a line are 32-bit (fields hold fewer than 2^31
+// points).  The d1 metric 1/dx is folded into the RHS weights on the host.
 //
-// On GB300 FP64 issues at ~1/58 of the FP32 rate (measured 1.2 TFLOP/s), so
-// these sweeps are bound by FP64 instruction count, not by HBM; the kernel is
-// written to keep the FP64 work per point minimal (FMA-contracted forms) and
-// leaves loads, address arithmetic and the tile transpose to the other pipes.
+// On GB300 FP64 issues at ~1/58 of the FP32 rate (measured 1.2 TFLOP/s): the
+// FP64 sweeps are bound by FP64 instruction count, the FP32 sweeps (fast path)
+// by HBM.  The FP32 path converts FP64<->FP32 with integer bit operations,
+// because GB300 runs F2F conversions on the FP64 pipe.
+#pragma once
 #include <cuda_runtime.h>
 
-#pragma once
+#include <cstdint>
 #include <cstdio>
 
 #include "pg_internal.h"
@@ -29,349 +37,361 @@ namespace pg {
 struct KParams {
   const double* __restrict__ in;
   double* __restrict__ out;
-  const void* rhs;  // n x 9 per-row RHS weights (T)
-  const void* lu;   // n x 9 per-row solve coefficients (T)
+  void* __restrict__ scratch;  // n x nlines forward-elimination values (T), [position][line]
+  const void* rhs;             // n x 9 per-row RHS weights (T)
+  const void* lu;              // n x 12 per-row solve coefficients (T): c1 c2 c6 c7 | c3 c4 c5 c8 | c9
   int n, nx, ny, nz;
-  int tiles_i;      // y/z sweeps: number of LB-wide tiles along x
+  int64_t nlines;
   double epi_scale;
-  double ri[9];     // interior RHS weights
+  double ri[9];                // interior RHS weights
 };
 
+constexpr int kSweepThreads = 128;
+
 namespace {
-
-
 
 template <typename T>
 __device__ __forceinline__ T ldc(const T* p) { return __ldg(p); }
 
-// ---------------------------------------------------------------------------
-// RHS of one line, in place on a shared-memory column c[p*lds].
-// Edge rows (4 per side) are evaluated first from the untouched column and
-// kept in registers; the interior rows then stream through a register window.
-// ---------------------------------------------------------------------------
-template <typename T, bool PER>
-__device__ __forceinline__ void rhs_d1(T* c, int lds, int n, const T* __restrict__ R,
-                                       const T a5, const T a6, const T a7) {
-  auto V = [&](int p) -> T { return c[p * lds]; };
-  auto W = [&](int p) -> T { return c[((p % n + n) % n) * lds]; };
-  T e[8];
-  if (PER) {
-#pragma unroll
-    for (int q = 0; q < 8; q++) {
-      const int i = q < 4 ? q : n - 8 + q;
-      const T* r = R + i * 9;
-      e[q] = ldc(r + 4) * (W(i + 1) - W(i - 1)) + ldc(r + 5) * (W(i + 2) - W(i - 2)) +
-             ldc(r + 6) * (W(i + 3) - W(i - 3));
-    }
-  } else {
-    // one-sided closures, boundary code 0 (compact_d1.f90:131-139, :175-183)
-    const T* r0 = R;
-    const T* r1 = R + 9;
-    const T* r2 = R + 18;
-    const T* r3 = R + 27;
-    const T v0 = V(0), v1 = V(1), v2 = V(2), v3 = V(3), v4 = V(4), v5 = V(5), v6 = V(6);
-    T s = T(0);
-    s += ldc(r0 + 4) * (v1 - v0);
-    s += ldc(r0 + 5) * (v2 - v0);
-    s += ldc(r0 + 6) * (v3 - v0);
-    e[0] = s;
-    s = T(0);
-    s += ldc(r1 + 3) * (v1 - v0);
-    s += ldc(r1 + 4) * (v2 - v0);
-    s += ldc(r1 + 5) * (v3 - v0);
-    s += ldc(r1 + 6) * (v4 - v0);
-    e[1] = s;
-    e[2] = ldc(r2 + 4) * (v3 - v1) + ldc(r2 + 5) * (v4 - v0) + ldc(r2 + 6) * (v5 - v0);
-    e[3] = ldc(r3 + 4) * (v4 - v2) + ldc(r3 + 5) * (v5 - v1) + ldc(r3 + 6) * (v6 - v0);
-    const int m = n - 1;
-    const T u0 = V(m), u1 = V(m - 1), u2 = V(m - 2), u3 = V(m - 3), u4 = V(m - 4), u5 = V(m - 5),
-            u6 = V(m - 6);
-    const T* q4 = R + (m - 3) * 9;
-    const T* q5 = R + (m - 2) * 9;
-    const T* q6 = R + (m - 1) * 9;
-    const T* q7 = R + m * 9;
-    e[4] = ldc(q4 + 4) * (u2 - u4) + ldc(q4 + 5) * (u1 - u5) + ldc(q4 + 6) * (u0 - u6);
-    e[5] = ldc(q5 + 0) * (u5 - u0) + ldc(q5 + 1) * (u4 - u0) + ldc(q5 + 2) * (u3 - u1);
-    s = T(0);
-    s += ldc(q6 + 0) * (u4 - u0);
-    s += ldc(q6 + 1) * (u3 - u0);
-    s += ldc(q6 + 2) * (u2 - u0);
-    s += ldc(q6 + 3) * (u1 - u0);
-    e[6] = s;
-    s = T(0);
-    s += ldc(q7 + 0) * (u3 - u0);
-    s += ldc(q7 + 1) * (u2 - u0);
-    s += ldc(q7 + 2) * (u1 - u0);
-    e[7] = s;
-  }
-  // interior rows 4 .. n-5 through a 7-point register window
-  T w0 = V(1), w1 = V(2), w2 = V(3), w3 = V(4), w4 = V(5), w5 = V(6), w6 = V(7);
-  for (int i = 4; i <= n - 5; i++) {
-    const T r = a5 * (w4 - w2) + a6 * (w5 - w1) + a7 * (w6 - w0);
-    const T nxt = (i + 4 < n) ? V(i + 4) : T(0);
-    c[i * lds] = r;
-    w0 = w1; w1 = w2; w2 = w3; w3 = w4; w4 = w5; w5 = w6; w6 = nxt;
-  }
-#pragma unroll
-  for (int q = 0; q < 8; q++) c[(q < 4 ? q : n - 8 + q) * lds] = e[q];
+// FP64 -> FP32 by integer operations (GB300 runs F2F on its FP64 pipe): the
+// exponent is re-biased in the high word and the mantissa rounded to nearest
+// (ties away from zero).  Values below the FP32 normal range flush to signed
+// zero; the fast path only sees finite field values inside the FP32 range
+// (infinities and NaNs of the FP64 fields are caught by pg_check_finite).
+__device__ __forceinline__ float d2f_bits(double d) {
+  const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+  const unsigned mag = hi & 0x7fffffffu;
+  unsigned f = ((mag - (896u << 20)) << 3) | (lo >> 29);
+  f += (lo >> 28) & 1u;
+  f = (mag < (897u << 20)) ? 0u : f;
+  return __uint_as_float(f | (hi & 0x80000000u));
 }
 
-template <typename T, bool PER>
-__device__ __forceinline__ void rhs_r4(T* c, int lds, int n, const T* __restrict__ R, const T* ai) {
-  auto V = [&](int p) -> T { return c[p * lds]; };
-  T e[8];
-  if (PER) {
-    // periodic halo rows: two partial sums as compact_r4.f90:131-138, :180-189
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-      const T* r = R + i * 9;
-      const T vc = V(i);
-      T s1 = T(0), s2 = T(0);
-      for (int l = 0; l <= 3 - i; l++) s1 += ldc(r + l) * (V(i + l - 4 + n) - vc);
-      for (int l = 4 - i; l <= 8; l++) s2 += ldc(r + l) * (V(i + l - 4) - vc);
-      e[i] = s1 + s2;
-    }
-#pragma unroll
-    for (int q = 3; q >= 0; q--) {
-      const int i = n - 1 - q;
-      const T* r = R + i * 9;
-      const T vc = V(i);
-      T s1 = T(0), s2 = T(0);
-      for (int l = 0; l <= 4 + q; l++) s1 += ldc(r + l) * (V(i + l - 4) - vc);
-      for (int l = 5 + q; l <= 8; l++) s2 += ldc(r + l) * (V(i + l - 4 - n) - vc);
-      e[7 - q] = s1 + s2;
-    }
-  } else {
-    // one-sided closures (compact_r4.f90:120-125, :166-171)
-    const T v0 = V(0), vn = V(n - 1);
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-      const T* r = R + i * 9;
-      T s = T(0);
-      for (int l = 5 - i; l <= 8; l++) s += ldc(r + l) * (V(l + i - 4) - v0);
-      e[i] = s;
-    }
-#pragma unroll
-    for (int q = 3; q >= 0; q--) {
-      const int i = n - 1 - q;
-      const T* r = R + i * 9;
-      T s = T(0);
-      for (int l = 0; l <= 3 + q; l++) s += ldc(r + l) * (V(i + l - 4) - vn);
-      e[7 - q] = s;
-    }
-  }
-  // interior rows 4 .. n-5: sum_l (v[i+l-4] - v[i]) * a_l   (compact_r4.f90:144-156)
-  T w[9];
-#pragma unroll
-  for (int k = 0; k < 9; k++) w[k] = (k < n) ? V(k) : T(0);  // n == 8 has no interior row
-  for (int i = 4; i <= n - 5; i++) {
-    const T vc = w[4];
-    T s = T(0);
-    s += (w[0] - vc) * ai[0];
-    s += (w[1] - vc) * ai[1];
-    s += (w[2] - vc) * ai[2];
-    s += (w[3] - vc) * ai[3];
-    s += (w[5] - vc) * ai[5];
-    s += (w[6] - vc) * ai[6];
-    s += (w[7] - vc) * ai[7];
-    s += (w[8] - vc) * ai[8];
-    const T nxt = (i + 5 < n) ? V(i + 5) : T(0);
-    c[i * lds] = s;
-#pragma unroll
-    for (int k = 0; k < 8; k++) w[k] = w[k + 1];
-    w[8] = nxt;
-  }
-#pragma unroll
-  for (int q = 0; q < 8; q++) c[(q < 4 ? q : n - 8 + q) * lds] = e[q];
+// FP32 -> FP64 by integer operations: exact for normal numbers, zero stays
+// zero (FP32 subnormals flush to zero).
+__device__ __forceinline__ double f2d_bits(float x) {
+  const unsigned u = __float_as_uint(x);
+  const unsigned mag = u & 0x7fffffffu;
+  unsigned hi = ((mag >> 3) + (896u << 20)) | (u & 0x80000000u);
+  unsigned lo = u << 29;
+  if (mag < 0x00800000u) { hi = u & 0x80000000u; lo = 0u; }
+  return __hiloint2double((int)hi, (int)lo);
 }
 
-// bpentLUS3x on one column (pentadiagonal.f90:629-651), pull form of the
-// forward elimination: r_k -= r_{k-2} c1_k ; r_k -= r_{k-1} c2_k.
 template <typename T>
-__device__ __forceinline__ void solve_banded(T* c, int lds, int n, const T* __restrict__ L) {
-  T rm2 = c[0];
-  T rm1 = c[lds] - rm2 * ldc(L + 9 + 1);
-  c[lds] = rm1;
-  for (int i = 2; i < n; i++) {
-    const T* l = L + i * 9;
-    const T r = (c[i * lds] - rm2 * ldc(l + 0)) - rm1 * ldc(l + 1);
-    c[i * lds] = r;
-    rm2 = rm1;
-    rm1 = r;
-  }
-  T x2 = rm1 * ldc(L + (n - 1) * 9 + 2);
-  c[(n - 1) * lds] = x2;
-  T x1 = (rm2 - ldc(L + (n - 2) * 9 + 3) * x2) * ldc(L + (n - 2) * 9 + 2);
-  c[(n - 2) * lds] = x1;
-  for (int i = n - 3; i >= 0; i--) {
-    const T* l = L + i * 9;
-    const T x = (c[i * lds] - ldc(l + 3) * x1 - ldc(l + 4) * x2) * ldc(l + 2);
-    c[i * lds] = x;
-    x2 = x1;
-    x1 = x;
-  }
-}
-
-// ppentLUS3x on one column (pentadiagonal.f90:654-684): bordered LU of the
-// cyclic pentadiagonal system.
+__device__ __forceinline__ T from_f64(double v) { return (T)v; }
+template <>
+__device__ __forceinline__ float from_f64<float>(double v) { return d2f_bits(v); }
 template <typename T>
-__device__ __forceinline__ void solve_cyclic(T* c, int lds, int n, const T* __restrict__ L) {
-  T rm2 = c[0];
-  T rm1 = c[lds] - ldc(L + 9 + 1) * rm2;
-  c[lds] = rm1;
-  T t1 = ldc(L + 5) * rm2 + ldc(L + 9 + 5) * rm1;
-  T t2 = ldc(L + 6) * rm2 + ldc(L + 9 + 6) * rm1;
-  for (int i = 2; i <= n - 3; i++) {
-    const T* l = L + i * 9;
-    const T r = c[i * lds] - ldc(l + 1) * rm1 - ldc(l + 0) * rm2;
-    c[i * lds] = r;
-    t1 += ldc(l + 5) * r;
-    t2 += ldc(l + 6) * r;
-    rm2 = rm1;
-    rm1 = r;
-  }
-  const T* la = L + (n - 2) * 9;
-  const T* lb = L + (n - 1) * 9;
-  const T rN1 = c[(n - 2) * lds] - t1;
-  const T xN = (c[(n - 1) * lds] - t2 - ldc(la + 6) * rN1) * ldc(lb + 2);
-  const T xN1 = (rN1 - ldc(la + 8) * xN) * ldc(la + 2);
-  c[(n - 1) * lds] = xN;
-  c[(n - 2) * lds] = xN1;
-  T x1 = xN1, x2 = xN;
-  for (int i = n - 3; i >= 0; i--) {
-    const T* l = L + i * 9;
-    const T x = (c[i * lds] - ldc(l + 3) * x1 - ldc(l + 4) * x2 - ldc(l + 7) * xN1 - ldc(l + 8) * xN) *
-                ldc(l + 2);
-    c[i * lds] = x;
-    x2 = x1;
-    x1 = x;
-  }
-}
+__device__ __forceinline__ double to_f64(T v) { return (double)v; }
+template <>
+__device__ __forceinline__ double to_f64<float>(float v) { return f2d_bits(v); }
 
 template <int EPI>
-__device__ __forceinline__ double epilogue(double r, double v_in, double* o, double scale, bool addback) {
+__device__ __forceinline__ double epilogue(double r, double v_in, double o, double scale, bool addback) {
   const double val = addback ? r + v_in : r;
   if (EPI == EPI_STORE) return val;
-  if (EPI == EPI_ADD) return *o + val;
+  if (EPI == EPI_ADD) return o + val;
   if (EPI == EPI_RING_SET) return fabs(val) * scale;
-  return fmax(*o, fabs(val) * scale);
+  return fmax(o, fabs(val) * scale);
+}
+
+constexpr int kRing = 16;  // ring-buffer slots of the forward window (window + prefetch)
+constexpr int kPFB = 8;    // prefetch distance of the backward loop
+
+template <typename T> struct V4;
+template <> struct V4<float> {
+  float a, b, c, d;
+  static __device__ __forceinline__ V4 ld(const float* p) {
+    const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+    return V4{v.x, v.y, v.z, v.w};
+  }
+};
+template <> struct V4<double> {
+  double a, b, c, d;
+  static __device__ __forceinline__ V4 ld(const double* p) {
+    const double2 u = __ldg(reinterpret_cast<const double2*>(p));
+    const double2 w = __ldg(reinterpret_cast<const double2*>(p) + 1);
+    return V4{u.x, u.y, w.x, w.y};
+  }
+};
+
+// Access to one line of the input field (32-bit offsets from the line base).
+template <typename T>
+struct Line {
+  const double* __restrict__ in;  // first point of the line
+  int stride, n;
+  __device__ __forceinline__ T v(int p) const { return from_f64<T>(in[p * stride]); }
+  __device__ __forceinline__ T w(int p) const {  // periodic wrap
+    const int q = p < 0 ? p + n : (p >= n ? p - n : p);
+    return v(q);
+  }
+};
+
+// RHS of one edge row (rows 0..3 and n-4..n-1) straight from global memory,
+// with the reference's periodic-halo or one-sided (boundary code 0) formulas.
+template <typename T, int KIND, bool PER>
+__device__ __forceinline__ T edge_rhs(const Line<T>& ln, int i, const T* __restrict__ R) {
+  const int n = ln.n;
+  const T* r = R + i * 9;
+  if (KIND == 1) {
+    if (PER)  // compact_d1.f90:141-147, :185-191 (the halo is the wrapped line)
+      return ldc(r + 4) * (ln.w(i + 1) - ln.w(i - 1)) + ldc(r + 5) * (ln.w(i + 2) - ln.w(i - 2)) +
+             ldc(r + 6) * (ln.w(i + 3) - ln.w(i - 3));
+    if (i == 0 || i == 1) {  // compact_d1.f90:131-134
+      const T v0 = ln.v(0);
+      T s = T(0);
+      for (int l = (i == 0 ? 4 : 3); l <= 6; l++) s += ldc(r + l) * (ln.v(l - 3 + i) - v0);
+      return s;
+    }
+    if (i == 2)  // compact_d1.f90:135
+      return ldc(r + 4) * (ln.v(3) - ln.v(1)) + ldc(r + 5) * (ln.v(4) - ln.v(0)) + ldc(r + 6) * (ln.v(5) - ln.v(0));
+    if (i == 3 || i == n - 4)  // interior formula with the boundary rows' weights
+      return ldc(r + 4) * (ln.v(i + 1) - ln.v(i - 1)) + ldc(r + 5) * (ln.v(i + 2) - ln.v(i - 2)) +
+             ldc(r + 6) * (ln.v(i + 3) - ln.v(i - 3));
+    const T vn = ln.v(n - 1);
+    if (i == n - 3)  // compact_d1.f90:178
+      return ldc(r + 0) * (ln.v(n - 6) - vn) + ldc(r + 1) * (ln.v(n - 5) - vn) +
+             ldc(r + 2) * (ln.v(n - 4) - ln.v(n - 2));
+    T s = T(0);  // rows n-2, n-1 (compact_d1.f90:179-180)
+    const int top = (i == n - 2) ? 3 : 2;
+    for (int l = 0; l <= top; l++) s += ldc(r + l) * (ln.v(i - 3 + l) - vn);
+    return s;
+  }
+  if (PER) {  // two partial sums (compact_r4.f90:131-138, :180-189)
+    const T vc = ln.v(i);
+    T s1 = T(0), s2 = T(0);
+    if (i < 4) {
+      for (int l = 0; l <= 3 - i; l++) s1 += ldc(r + l) * (ln.v(i + l - 4 + n) - vc);
+      for (int l = 4 - i; l <= 8; l++) s2 += ldc(r + l) * (ln.v(i + l - 4) - vc);
+    } else {
+      const int q = n - 1 - i;
+      for (int l = 0; l <= 4 + q; l++) s1 += ldc(r + l) * (ln.v(i + l - 4) - vc);
+      for (int l = 5 + q; l <= 8; l++) s2 += ldc(r + l) * (ln.v(i + l - 4 - n) - vc);
+    }
+    return s1 + s2;
+  }
+  T s = T(0);  // one-sided closures (compact_r4.f90:120-125, :166-171)
+  if (i < 4) {
+    const T v0 = ln.v(0);
+    for (int l = 5 - i; l <= 8; l++) s += ldc(r + l) * (ln.v(l + i - 4) - v0);
+  } else {
+    const T vn = ln.v(n - 1);
+    const int q = n - 1 - i;
+    for (int l = 0; l <= 3 + q; l++) s += ldc(r + l) * (ln.v(i + l - 4) - vn);
+  }
+  return s;
+}
+
+// Interior RHS from the ring: the window of row i starts at slot k.
+template <typename T, int KIND>
+__device__ __forceinline__ T ring_rhs(const T* ring, int k, const T* ai) {
+  if (KIND == 1) {
+    return ai[4] * (ring[(k + 4) % kRing] - ring[(k + 2) % kRing]) +
+           ai[5] * (ring[(k + 5) % kRing] - ring[(k + 1) % kRing]) +
+           ai[6] * (ring[(k + 6) % kRing] - ring[(k + 0) % kRing]);
+  }
+  const T vc = ring[(k + 4) % kRing];
+  T s = T(0);
+  s += (ring[(k + 0) % kRing] - vc) * ai[0];
+  s += (ring[(k + 1) % kRing] - vc) * ai[1];
+  s += (ring[(k + 2) % kRing] - vc) * ai[2];
+  s += (ring[(k + 3) % kRing] - vc) * ai[3];
+  s += (ring[(k + 5) % kRing] - vc) * ai[5];
+  s += (ring[(k + 6) % kRing] - vc) * ai[6];
+  s += (ring[(k + 7) % kRing] - vc) * ai[7];
+  s += (ring[(k + 8) % kRing] - vc) * ai[8];
+  return s;
 }
 
 // KIND: 1 = d1 evaluator, 4 = r4 evaluator.  DIR: 0 = x, 1 = y, 2 = z.
 template <typename T, int KIND, bool PER, bool IMPL, bool ADDBACK, int DIR, int EPI>
-__global__ void __launch_bounds__(32) sweep_kernel(const KParams P) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* s = reinterpret_cast<T*>(smem_raw);
-  const int lb = blockDim.x;
-  const int lds = lb + 1;
-  const int t = threadIdx.x;
-  const int n = P.n, nx = P.nx, ny = P.ny;
-
-  // tile decode
-  int64_t base_t;   // base offset of this thread's line
-  int64_t stride;   // element stride along the line
-  bool valid;
-  int64_t line0 = 0;
-  int nlines = 0;
+__global__ void __launch_bounds__(kSweepThreads) sweep_kernel(const KParams P) {
+  const int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (L >= P.nlines) return;
+  const int n = P.n;
+  int64_t base;
+  int st;
   if (DIR == 0) {
-    const int64_t total = (int64_t)ny * P.nz;
-    line0 = (int64_t)blockIdx.x * lb;
-    nlines = (int)(total - line0 < (int64_t)lb ? total - line0 : (int64_t)lb);
-    valid = t < nlines;
-    base_t = (line0 + t) * nx;
-    stride = 1;
+    base = L * P.nx;
+    st = 1;
+  } else if (DIR == 1) {
+    base = (L / P.nx) * (int64_t)P.nx * P.ny + (L % P.nx);
+    st = P.nx;
   } else {
-    const int b = blockIdx.x;
-    const int ti = b % P.tiles_i;
-    const int outer = b / P.tiles_i;
-    const int i = ti * lb + t;
-    valid = i < nx;
-    if (DIR == 1) {
-      base_t = (int64_t)outer * nx * ny + i;
-      stride = nx;
-    } else {
-      base_t = (int64_t)outer * nx + i;
-      stride = (int64_t)nx * ny;
-    }
+    base = (L / P.nx) * (int64_t)P.nx + (L % P.nx);
+    st = P.nx * P.ny;
   }
-
-  // stage the tile
-  if (DIR == 0) {
-    for (int l = 0; l < nlines; l++) {
-      const double* src = P.in + (line0 + l) * nx;
-      for (int p = t; p < n; p += lb) s[p * lds + l] = (T)src[p];
-    }
-  } else if (valid) {
-    const double* src = P.in + base_t;
-    int p = 0;
-    for (; p + 4 <= n; p += 4) {
-      const double a0 = src[(int64_t)p * stride], a1 = src[(int64_t)(p + 1) * stride];
-      const double a2 = src[(int64_t)(p + 2) * stride], a3 = src[(int64_t)(p + 3) * stride];
-      s[p * lds + t] = (T)a0;
-      s[(p + 1) * lds + t] = (T)a1;
-      s[(p + 2) * lds + t] = (T)a2;
-      s[(p + 3) * lds + t] = (T)a3;
-    }
-    for (; p < n; p++) s[p * lds + t] = (T)src[(int64_t)p * stride];
-  }
-  __syncthreads();
-
-  if (valid) {
-    T* c = s + t;
-    const T* R = reinterpret_cast<const T*>(P.rhs);
-    const T* L = reinterpret_cast<const T*>(P.lu);
-    if (KIND == 1) {
-      rhs_d1<T, PER>(c, lds, n, R, (T)P.ri[4], (T)P.ri[5], (T)P.ri[6]);
-    } else {
-      T ai[9];
-#pragma unroll
-      for (int k = 0; k < 9; k++) ai[k] = (T)P.ri[k];
-      rhs_r4<T, PER>(c, lds, n, R, ai);
-    }
-    if (IMPL) {
-      if (PER) solve_cyclic<T>(c, lds, n, L);
-      else solve_banded<T>(c, lds, n, L);
-    }
-  }
-  __syncthreads();
-
-  // write back with the fused epilogue
+  const double* __restrict__ pin = P.in + base;
+  double* __restrict__ pout = P.out + base;
+  const Line<T> ln{pin, st, n};
+  const T* __restrict__ R = reinterpret_cast<const T*>(P.rhs);
+  const T* __restrict__ C = reinterpret_cast<const T*>(P.lu);  // 12 per row
+  T* __restrict__ ps = reinterpret_cast<T*>(P.scratch) + L;     // row i at ps[i * nl]
+  const int nl = (int)P.nlines;
+  constexpr bool kReadOut = (EPI == EPI_ADD || EPI == EPI_RING_MAX);
   const double sc = P.epi_scale;
-  if (DIR == 0) {
-    for (int l = 0; l < nlines; l++) {
-      const int64_t off = (line0 + l) * nx;
-      for (int p = t; p < n; p += lb) {
-        const double r = (double)s[p * lds + l];
-        const double vin = ADDBACK ? P.in[off + p] : 0.0;
-        P.out[off + p] = epilogue<EPI>(r, vin, P.out + off + p, sc, ADDBACK);
+  constexpr int H = (KIND == 1) ? 3 : 4;  // stencil half width
+
+  // edge rows first: they may need wrapped values of the far end of the line
+  T e[8];
+#pragma unroll
+  for (int q = 0; q < 8; q++) e[q] = edge_rhs<T, KIND, PER>(ln, q < 4 ? q : n - 8 + q, R);
+
+  auto put = [&](int p, T x, double vin, double o) {
+    pout[p * st] = epilogue<EPI>(to_f64<T>(x), vin, o, sc, ADDBACK);
+  };
+  auto put_load = [&](int p, T x) {
+    const double vin = ADDBACK ? pin[p * st] : 0.0;
+    const double o = kReadOut ? pout[p * st] : 0.0;
+    put(p, x, vin, o);
+  };
+
+  // ---------------------------------------------------------------- forward
+  T rm1 = T(0), rm2 = T(0), t1 = T(0), t2 = T(0), rN1 = T(0), rN = T(0);
+  // edge rows, with the reference's special first rows and closing rows
+  auto fwd_edge = [&](int i, T rhs) {
+    if (!IMPL) {
+      put_load(i, rhs);
+      return;
+    }
+    const V4<T> f = V4<T>::ld(C + i * 12);  // c1 c2 c6 c7
+    T r;
+    if (PER) {
+      if (i >= n - 2) {  // the last two rows are closed by the border sums
+        if (i == n - 2) rN1 = rhs;
+        else rN = rhs;
+        return;
+      }
+      if (i == 0) r = rhs;
+      else if (i == 1) r = rhs - f.b * rm1;
+      else r = rhs - f.b * rm1 - f.a * rm2;
+      t1 += f.c * r;
+      t2 += f.d * r;
+    } else {
+      if (i == 0) r = rhs;
+      else if (i == 1) r = rhs - rm1 * f.b;
+      else r = (rhs - rm2 * f.a) - rm1 * f.b;
+    }
+    if (i < n - 2) ps[i * nl] = r;
+    rm2 = rm1;
+    rm1 = r;
+  };
+  // interior rows (2 <= i <= n-3): no special cases
+  auto fwd_in = [&](int i, T rhs) {
+    if (!IMPL) {
+      put_load(i, rhs);
+      return;
+    }
+    const V4<T> f = V4<T>::ld(C + i * 12);
+    T r;
+    if (PER) {
+      r = rhs - f.b * rm1 - f.a * rm2;
+      t1 += f.c * r;
+      t2 += f.d * r;
+    } else {
+      r = (rhs - rm2 * f.a) - rm1 * f.b;
+    }
+    ps[i * nl] = r;
+    rm2 = rm1;
+    rm1 = r;
+  };
+
+#pragma unroll
+  for (int q = 0; q < 4; q++) fwd_edge(q, e[q]);
+
+  // interior rows 4 .. n-5: ring[s] holds v[i0 - H + s] at the start of a block
+  // of kRing rows; the slot of the oldest value is refilled kRing positions ahead
+  {
+    T ai[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) ai[k] = (T)P.ri[k];
+    T ring[kRing];
+#pragma unroll
+    for (int s2 = 0; s2 < kRing; s2++) {
+      const int p = 4 - H + s2;
+      ring[s2] = (p < n) ? ln.v(p) : T(0);
+    }
+    int i0 = 4;
+    for (; i0 + kRing <= n - 4; i0 += kRing) {  // whole blocks: no guards
+#pragma unroll
+      for (int k = 0; k < kRing; k++) {
+        const int i = i0 + k;
+        const T rhs = ring_rhs<T, KIND>(ring, k, ai);
+        const int p = i - H + kRing;
+        ring[k] = (p < n) ? ln.v(p) : T(0);
+        fwd_in(i, rhs);
       }
     }
-  } else if (valid) {
-    for (int p = 0; p < n; p++) {
-      const int64_t off = base_t + (int64_t)p * stride;
-      const double r = (double)s[p * lds + t];
-      const double vin = ADDBACK ? P.in[off] : 0.0;
-      P.out[off] = epilogue<EPI>(r, vin, P.out + off, sc, ADDBACK);
+#pragma unroll
+    for (int k = 0; k < kRing; k++) {  // last partial block
+      const int i = i0 + k;
+      if (i <= n - 5) {
+        const T rhs = ring_rhs<T, KIND>(ring, k, ai);
+        const int p = i - H + kRing;
+        ring[k] = (p < n) ? ln.v(p) : T(0);
+        fwd_in(i, rhs);
+      }
+    }
+  }
+
+#pragma unroll
+  for (int q = 4; q < 8; q++) fwd_edge(n - 8 + q, e[q]);
+  if (!IMPL) return;
+
+  // --------------------------------------------------------------- backward
+  T x1, x2, xN1 = T(0), xN = T(0);
+  if (PER) {  // ppentLUS3x :673-676
+    const T* ca = C + (n - 2) * 12;
+    const T* cb = C + (n - 1) * 12;
+    const T r1 = rN1 - t1;
+    xN = (rN - t2 - ldc(ca + 3) * r1) * ldc(cb + 4);
+    xN1 = (r1 - ldc(ca + 8) * xN) * ldc(ca + 4);
+    x1 = xN1;
+    x2 = xN;
+  } else {  // bpentLUS3x :640-641 (the last two forward values are still in registers)
+    x2 = rm1 * ldc(C + (n - 1) * 12 + 4);
+    x1 = (rm2 - ldc(C + (n - 2) * 12 + 5) * x2) * ldc(C + (n - 2) * 12 + 4);
+  }
+  put_load(n - 1, x2);
+  put_load(n - 2, x1);
+  T pr[kPFB];
+  double pv[kPFB], po[kPFB];
+#pragma unroll
+  for (int k = 0; k < kPFB; k++) {
+    const int p = n - 3 - k;
+    pr[k] = (p >= 0) ? ps[p * nl] : T(0);
+    pv[k] = (ADDBACK && p >= 0) ? pin[p * st] : 0.0;
+    po[k] = (kReadOut && p >= 0) ? pout[p * st] : 0.0;
+  }
+  for (int i = n - 3; i >= 0; i -= kPFB) {
+#pragma unroll
+    for (int k = 0; k < kPFB; k++) {
+      const int ii = i - k;
+      if (ii >= 0) {
+        const T r = pr[k];
+        const double vin = pv[k], o = po[k];
+        const int p = ii - kPFB;
+        pr[k] = (p >= 0) ? ps[p * nl] : T(0);
+        if (ADDBACK) pv[k] = (p >= 0) ? pin[p * st] : 0.0;
+        if (kReadOut) po[k] = (p >= 0) ? pout[p * st] : 0.0;
+        const V4<T> g = V4<T>::ld(C + ii * 12 + 4);  // c3 c4 c5 c8
+        T part;
+        if (PER) part = r - g.d * xN1 - ldc(C + ii * 12 + 8) * xN - g.c * x2;
+        else part = r - g.c * x2;
+        const T x = (part - g.b * x1) * g.a;  // short chain through x1
+        x2 = x1;
+        x1 = x;
+        put(ii, x, vin, o);
+      }
     }
   }
 }
 
 template <typename T, int KIND, bool PER, bool IMPL, bool ADDBACK, int DIR, int EPI>
-int launch_t(const KParams& P, int lb, int64_t nblocks, void* stream) {
-  auto kern = sweep_kernel<T, KIND, PER, IMPL, ADDBACK, DIR, EPI>;
-  const size_t smem = (size_t)P.n * (lb + 1) * sizeof(T);
-  static bool attr_set = false;
-  static size_t attr_val = 0;
-  if (!attr_set || attr_val < smem) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) {
-      set_error("cudaFuncSetAttribute(smem=%zu): %s", smem, cudaGetErrorString(e));
-      return PG_ECUDA;
-    }
-    attr_set = true;
-    attr_val = smem;
-  }
-  kern<<<(unsigned)nblocks, lb, smem, (cudaStream_t)stream>>>(P);
+int launch_t(const KParams& P, void* stream) {
+  const int64_t nb = (P.nlines + kSweepThreads - 1) / kSweepThreads;
+  sweep_kernel<T, KIND, PER, IMPL, ADDBACK, DIR, EPI><<<(unsigned)nb, kSweepThreads, 0, (cudaStream_t)stream>>>(P);
   count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
@@ -382,13 +402,13 @@ int launch_t(const KParams& P, int lb, int64_t nblocks, void* stream) {
 }
 
 template <typename T, int KIND, bool PER, bool IMPL, bool ADDBACK>
-int dispatch_dir_epi(const KParams& P, int dir, int epi, int lb, int64_t nb, void* st) {
-#define PG_EPI_CASES(D)                                                                   \
-  switch (epi) {                                                                          \
-    case EPI_STORE: return launch_t<T, KIND, PER, IMPL, ADDBACK, D, EPI_STORE>(P, lb, nb, st);       \
-    case EPI_ADD: return launch_t<T, KIND, PER, IMPL, ADDBACK, D, EPI_ADD>(P, lb, nb, st);           \
-    case EPI_RING_SET: return launch_t<T, KIND, PER, IMPL, ADDBACK, D, EPI_RING_SET>(P, lb, nb, st); \
-    default: return launch_t<T, KIND, PER, IMPL, ADDBACK, D, EPI_RING_MAX>(P, lb, nb, st);           \
+int dispatch_dir_epi(const KParams& P, int dir, int epi, void* st) {
+#define PG_EPI_CASES(D)                                                                      \
+  switch (epi) {                                                                             \
+    case EPI_STORE: return launch_t<T, KIND, PER, IMPL, ADDBACK, D, EPI_STORE>(P, st);       \
+    case EPI_ADD: return launch_t<T, KIND, PER, IMPL, ADDBACK, D, EPI_ADD>(P, st);           \
+    case EPI_RING_SET: return launch_t<T, KIND, PER, IMPL, ADDBACK, D, EPI_RING_SET>(P, st); \
+    default: return launch_t<T, KIND, PER, IMPL, ADDBACK, D, EPI_RING_MAX>(P, st);           \
   }
   if (dir == 0) { PG_EPI_CASES(0) }
   if (dir == 1) { PG_EPI_CASES(1) }
@@ -397,20 +417,20 @@ int dispatch_dir_epi(const KParams& P, int dir, int epi, int lb, int64_t nb, voi
 }
 
 template <typename T>
-int dispatch_kind(const DevOp& op, const KParams& P, int dir, int epi, int lb, int64_t nb, void* st) {
+int dispatch_kind(const DevOp& op, const KParams& P, int dir, int epi, void* st) {
   switch (op.kind) {
     case OPK_D1:
-      return op.periodic ? dispatch_dir_epi<T, 1, true, true, false>(P, dir, epi, lb, nb, st)
-                         : dispatch_dir_epi<T, 1, false, true, false>(P, dir, epi, lb, nb, st);
+      return op.periodic ? dispatch_dir_epi<T, 1, true, true, false>(P, dir, epi, st)
+                         : dispatch_dir_epi<T, 1, false, true, false>(P, dir, epi, st);
     case OPK_D8:
-      return op.periodic ? dispatch_dir_epi<T, 4, true, true, false>(P, dir, epi, lb, nb, st)
-                         : dispatch_dir_epi<T, 4, false, true, false>(P, dir, epi, lb, nb, st);
+      return op.periodic ? dispatch_dir_epi<T, 4, true, true, false>(P, dir, epi, st)
+                         : dispatch_dir_epi<T, 4, false, true, false>(P, dir, epi, st);
     case OPK_SF:
-      return op.periodic ? dispatch_dir_epi<T, 4, true, true, true>(P, dir, epi, lb, nb, st)
-                         : dispatch_dir_epi<T, 4, false, true, true>(P, dir, epi, lb, nb, st);
+      return op.periodic ? dispatch_dir_epi<T, 4, true, true, true>(P, dir, epi, st)
+                         : dispatch_dir_epi<T, 4, false, true, true>(P, dir, epi, st);
     default:
-      return op.periodic ? dispatch_dir_epi<T, 4, true, false, true>(P, dir, epi, lb, nb, st)
-                         : dispatch_dir_epi<T, 4, false, false, true>(P, dir, epi, lb, nb, st);
+      return op.periodic ? dispatch_dir_epi<T, 4, true, false, true>(P, dir, epi, st)
+                         : dispatch_dir_epi<T, 4, false, false, true>(P, dir, epi, st);
   }
 }
 

@@ -4,8 +4,8 @@
 
 namespace pg {
 
-int launch_sweep_f32(const DevOp& op, const KParams& P, int dir, int epi, int lb, int64_t nb, void* st) {
-  return dispatch_kind<float>(op, P, dir, epi, lb, nb, st);
+int launch_sweep_f32(const DevOp& op, const KParams& P, int dir, int epi, void* st) {
+  return dispatch_kind<float>(op, P, dir, epi, st);
 }
 
 }  // namespace pg

@@ -3,12 +3,13 @@
 
 namespace pg {
 
-int launch_sweep_f32(const DevOp& op, const KParams& P, int dir, int epi, int lb, int64_t nb, void* st);
+int launch_sweep_f32(const DevOp& op, const KParams& P, int dir, int epi, void* st);
 
 int launch_sweep(const DevOp& op, int precision, const SweepLaunch& s, void* stream) {
   KParams P;
   P.in = s.in;
   P.out = s.out;
+  P.scratch = s.scratch;
   P.rhs = op.rhs;
   P.lu = op.lu;
   P.n = op.n;
@@ -17,25 +18,17 @@ int launch_sweep(const DevOp& op, int precision, const SweepLaunch& s, void* str
   P.nz = s.nz;
   P.epi_scale = s.epi_scale;
   for (int k = 0; k < 9; k++) P.ri[k] = op.rhs_in[k];
-  const size_t esz = precision == PG_FP32 ? 4 : 8;
-  // lines per CTA: 32 while the tile fits twice per SM, else 16, else 8
-  int lb = 32;
-  while (lb > 8 && (size_t)op.n * (lb + 1) * esz > 110 * 1024) lb /= 2;
-  if ((size_t)op.n * (lb + 1) * esz > 220 * 1024) {
-    set_error("line length %d too long for one tile", op.n);
+  if (s.dir == 0) P.nlines = (int64_t)s.ny * s.nz;
+  else if (s.dir == 1) P.nlines = (int64_t)s.nx * s.nz;
+  else P.nlines = (int64_t)s.nx * s.ny;
+  if (P.nlines <= 0) return PG_OK;
+  if ((int64_t)s.nx * s.ny * s.nz >= ((int64_t)1 << 31)) {
+    set_error("field of %lld points: the sweeps address fields of fewer than 2^31 points",
+              (long long)s.nx * s.ny * s.nz);
     return PG_EBADSHAPE;
   }
-  int64_t nblocks;
-  if (s.dir == 0) {
-    nblocks = ((int64_t)s.ny * s.nz + lb - 1) / lb;
-    P.tiles_i = 1;
-  } else {
-    P.tiles_i = (s.nx + lb - 1) / lb;
-    nblocks = (int64_t)P.tiles_i * (s.dir == 1 ? s.nz : s.ny);
-  }
-  if (nblocks <= 0) return PG_OK;
-  if (precision == PG_FP32) return launch_sweep_f32(op, P, s.dir, s.epi, lb, nblocks, stream);
-  return dispatch_kind<double>(op, P, s.dir, s.epi, lb, nblocks, stream);
+  if (precision == PG_FP32) return launch_sweep_f32(op, P, s.dir, s.epi, stream);
+  return dispatch_kind<double>(op, P, s.dir, s.epi, stream);
 }
 
 }  // namespace pg

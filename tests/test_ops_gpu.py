@@ -149,7 +149,7 @@ def test_reductions_and_timestep(grids):
     gl = min(d1, d2, d3)
     ref = 1.0 / numpy.max(numpy.abs(u) / d1 + numpy.abs(v) / d2 + numpy.abs(w) / d3 + numpy.abs(c) / gl)
     assert abs(float(g.courant(du, dvv, dw, dc)) - ref) <= 1e-15 * ref
-    assert abs(float(g.courant(du, 0.0, 0.0, dc)) - 1.0 / numpy.max(numpy.abs(u) / d1 + numpy.abs(c) / gl)) <= 1e-15
+    assert abs(float(g.courant(du, 0.0, 0.0, dc)) - 1.0 / numpy.max(numpy.abs(u) / d1 + numpy.abs(c) / gl)) <= 1e-16
     bulk = numpy.abs(w) * 1e-3
     ref = numpy.min(c * gl * gl / numpy.maximum(1e-12, bulk))
     assert abs(float(g.diff(to_dev(bulk, torch), dc)) - ref) <= 1e-14 * ref
@@ -175,3 +175,23 @@ def test_rk_stage(grids):
         phi = dt * F[k] + A * PHI[k]
         assert rel_l2(to_host(dP[k]), phi) <= 1e-15
         assert rel_l2(to_host(dU[k]), U[k] + B * phi) <= 1e-15
+
+
+@pytest.mark.parametrize("case", [CASES[0], CASES[1], CASES[3], CASES[9]], ids=_ids)
+def test_fp32_sweeps_track_fp64(oracle, case):
+    """The fast path (FP32 arithmetic, bit-level FP64<->FP32 conversion) stays
+    within single-precision error of the oracle on every operator."""
+    from pyranda_gb300.grid import Grid
+    shape, per = case
+    g = Grid(shape, per, (0.0, -0.5, 0.25), (1.0, 2.0, 3.0), precision="fp32")
+    o = oracle.OracleGrid(shape, per, (0.0, -0.5, 0.25), (1.0, 2.0, 3.0))
+    v = smooth_field(shape, seed=21)
+    dv = to_dev(v, torch)
+    for d in range(3):
+        assert rel_l2(to_host(g.d1(d, dv)), o.apply(0, d, v)) <= 1e-5, ("d1", d)
+        assert rel_l2(to_host(g.d8(d, dv)), o.apply(1, d, v)) <= 1e-5, ("d8", d)
+        assert rel_l2(to_host(g.filter("spectral", dv, d)), o.apply(2, d, v)) <= 1e-6, ("sf", d)
+        assert rel_l2(to_host(g.filter("gaussian", dv, d)), o.apply(3, d, v)) <= 1e-6, ("gf", d)
+    c = g.field(torch.full(shape, 3.25, dtype=torch.float64, device="cuda"))
+    assert torch.equal(g.filter("spectral", c), c)
+    assert float(g.d1(0, c).abs().max()) == 0.0
