@@ -204,6 +204,22 @@ def run_steps(ss, k, t0=0.0):
     return t
 
 
+def max_over_ranks(seconds, dist_on, device=None):
+    """Largest per-rank time (the job's time) under torch.distributed, else itself."""
+    if not dist_on:
+        return float(seconds)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(npts, steps, world, seconds):
+    """Whole-job Mpoint-RK-steps/s: every rank advances its own replica."""
+    return npts * steps * world / seconds / 1e6
+
+
 def time_steps(ss, k, torch, dist_on):
     """CUDA-event time of k steps on the current stream, barrier + sync around."""
     if dist_on:
@@ -324,11 +340,8 @@ def main():
     clocks.start()
     t_fast = time_steps(fast, k, torch, dist_on)
     ck = clocks.stop()
-    if dist_on:
-        tt = torch.tensor([t_fast], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_fast = float(tt)
-    value = npts * k * world / t_fast / 1e6
+    t_fast = max_over_ranks(t_fast, dist_on, "cuda")
+    value = job_value(npts, k, world, t_fast)
 
     # ---- plain FP64 path, same IC, same number of steps (no graph)
     extra = {}
@@ -336,7 +349,8 @@ def main():
         plain = make_sim(n, "fp64", graphs=False)
         run_steps(plain, w)
         t64 = time_steps(plain, k, torch, dist_on)
-        extra["fp64_plain"] = {"value": round(npts * k * world / t64 / 1e6, 4), "unit": UNIT,
+        t64 = max_over_ranks(t64, dist_on, "cuda")
+        extra["fp64_plain"] = {"value": round(job_value(npts, k, world, t64), 4), "unit": UNIT,
                                "ms_per_step": round(t64 / k * 1e3, 3)}
         # accuracy of the fast path: both sims advanced w + k steps from the same IC
         errs = l2_errors(fast, plain, ["rho", "rhou", "rhov", "rhow", "Et"])
@@ -379,11 +393,7 @@ def main():
             host[nm].copy_(fast.variables[nm].data.permute(2, 1, 0), non_blocking=True)
     e.record()
     torch.cuda.synchronize()
-    t_e2e = s.elapsed_time(e) / 1e3
-    if dist_on:
-        tt = torch.tensor([t_e2e], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_e2e = float(tt)
+    t_e2e = max_over_ranks(s.elapsed_time(e) / 1e3, dist_on, "cuda")
     nbytes = len(names) * npts * 8
 
     if rank == 0:
@@ -399,7 +409,7 @@ def main():
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": roof,
             "cpu_baseline": cpu,
-            "e2e": {"value": round(npts * k * world / t_e2e / 1e6, 4), "unit": UNIT,
+            "e2e": {"value": round(job_value(npts, k, world, t_e2e), 4), "unit": UNIT,
                     "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
             "gpu_launches": int(launches_per_step * k),
             "clocks": ck,

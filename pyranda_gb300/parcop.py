@@ -1,0 +1,173 @@
+"""``parcop.parcop`` drop-in: the f2py module's names over libpyranda_gpu.so.
+
+pyranda's Python layer talks to the Fortran library through the f2py module
+``pyranda.parcop.parcop`` (built from pyranda/parcop/parcop.f90), e.g.
+``parcop.parcop.ddx(val)`` (pyrandaMPI.py:669-740).  This module offers the
+same entry points, argument order and return values:
+
+    from pyranda_gb300.parcop import parcop
+    parcop.setup(patch, level, comm, nx, ny, nz, px, py, pz, coordsys,
+                 x1, xn, y1, yn, z1, zn, bx1, bxn, by1, byn, bz1, bzn)
+    parcop.set_patch(patch, level)
+    dval = parcop.ddx(val)
+
+Arrays may be numpy arrays (copied to the GPU and back, returning a new
+F-ordered numpy array as f2py does) or torch CUDA tensors in the (nx,ny,nz)
+Fortran layout (kept on the device).  As in parcop, the (patch, level) pair
+selected by ``set_patch`` is the active grid; ``setup`` makes the new grid
+active (objects.f90:35-49, :77-89).
+
+Scope: one GPU (px = py = pz = 1), Cartesian meshes (coordsys 0), boundary
+codes PERI and NONE.  Other codes raise instead of silently misbehaving.
+"""
+import numpy
+import torch
+
+from .grid import Grid
+
+
+class _Parcop:
+    def __init__(self):
+        self._grids = {}
+        self._active = None
+
+    # parcop.f90:23-61
+    def setup(self, patch, level, comm, nx, ny, nz, px, py, pz, coordsys, x1, xn, y1, yn, z1, zn,
+              bx1, bxn, by1, byn, bz1, bzn):
+        if px * py * pz != 1:
+            raise ValueError("one GPU holds the whole grid: px*py*pz must be 1")
+        if coordsys != 0:
+            raise ValueError("only Cartesian meshes (coordsys 0) are supported")
+        per = []
+        for lo, hi in ((bx1, bxn), (by1, byn), (bz1, bzn)):
+            lo, hi = str(lo).strip().upper(), str(hi).strip().upper()
+            if "SYMM" in (lo, hi) or "XTND" in (lo, hi):
+                raise ValueError("boundary codes SYMM/XTND are not supported (PERI and NONE are)")
+            per.append(lo == "PERI")
+        g = Grid((nx, ny, nz), per, (x1, y1, z1), (xn, yn, zn))
+        self._grids[(patch, level)] = g
+        self._active = g
+
+    def setup_mesh(self, patch, level):
+        """parcop.f90:64-70: the Cartesian mesh is generated on demand."""
+        if (patch, level) not in self._grids:
+            raise KeyError("patch %s level %s was not set up" % (patch, level))
+
+    def set_patch(self, patch, level):
+        self._active = self._grids[(patch, level)]
+
+    def remove(self, patch, level):
+        self._grids.pop((patch, level), None)
+
+    # ---------------------------------------------------------------- helpers
+    def _g(self):
+        if self._active is None:
+            raise RuntimeError("parcop.setup has not been called")
+        return self._active
+
+    def _in(self, v):
+        g = self._g()
+        if isinstance(v, torch.Tensor):
+            return g.field(v), True
+        return g.field(numpy.asfortranarray(numpy.asarray(v, dtype=numpy.float64))), False
+
+    @staticmethod
+    def _out(t, device):
+        if device:
+            return t
+        return numpy.asfortranarray(t.permute(2, 1, 0).cpu().numpy().transpose(2, 1, 0))
+
+    def _unary(self, fn, val):
+        v, dev = self._in(val)
+        return self._out(fn(v), dev)
+
+    # ------------------------------------------------------------- operators
+    def ddx(self, val, nx=None, ny=None, nz=None):  # parcop.f90:225-233
+        return self._unary(self._g().ddx, val)
+
+    def ddy(self, val, nx=None, ny=None, nz=None):  # parcop.f90:235-243
+        return self._unary(self._g().ddy, val)
+
+    def ddz(self, val, nx=None, ny=None, nz=None):  # parcop.f90:245-253
+        return self._unary(self._g().ddz, val)
+
+    def dd8x(self, val, nx=None, ny=None, nz=None):  # parcop.f90:279-285
+        return self._unary(lambda v: self._g().d8(0, v), val)
+
+    def dd8y(self, val, nx=None, ny=None, nz=None):
+        return self._unary(lambda v: self._g().d8(1, v), val)
+
+    def dd8z(self, val, nx=None, ny=None, nz=None):
+        return self._unary(lambda v: self._g().d8(2, v), val)
+
+    def pring(self, val, nx=None, ny=None, nz=None):  # parcop.f90:313-322
+        return self._unary(self._g().ring, val)
+
+    def pringv(self, vx, vy, vz, nx=None, ny=None, nz=None):  # parcop.f90:324-333
+        a, dev = self._in(vx)
+        b, _ = self._in(vy)
+        c, _ = self._in(vz)
+        return self._out(self._g().ringv(a, b, c), dev)
+
+    def sfilter(self, val, nx=None, ny=None, nz=None):  # parcop.f90:337-346
+        return self._unary(lambda v: self._g().filter("spectral", v), val)
+
+    def gfilter(self, val, nx=None, ny=None, nz=None):  # parcop.f90:348-357
+        return self._unary(lambda v: self._g().filter("gaussian", v), val)
+
+    def gfilterdir(self, val, direction, nx=None, ny=None, nz=None):  # parcop.f90:359-368
+        return self._unary(lambda v: self._g().filter("gaussian", v, int(direction) - 1), val)
+
+    def grads(self, val, nx=None, ny=None, nz=None):  # parcop.f90:371-379
+        v, dev = self._in(val)
+        return tuple(self._out(t, dev) for t in self._g().grad(v))
+
+    def divergence(self, fx, fy, fz, nx=None, ny=None, nz=None):  # parcop.f90:202-211
+        a, dev = self._in(fx)
+        b, _ = self._in(fy)
+        c, _ = self._in(fz)
+        return self._out(self._g().div(a, b, c), dev)
+
+    # ------------------------------------------------------------------ mesh
+    def _mesh(self, which):
+        return self._out(self._g().mesh(which), False)
+
+    def xgrid(self, nx=None, ny=None, nz=None):  # parcop.f90:130-135
+        return self._mesh(0)
+
+    def ygrid(self, nx=None, ny=None, nz=None):
+        return self._mesh(1)
+
+    def zgrid(self, nx=None, ny=None, nz=None):
+        return self._mesh(2)
+
+    def dxgrid(self, nx=None, ny=None, nz=None):  # parcop.f90:154-159
+        return self._mesh(3)
+
+    def dygrid(self, nx=None, ny=None, nz=None):
+        return self._mesh(4)
+
+    def dzgrid(self, nx=None, ny=None, nz=None):
+        return self._mesh(5)
+
+    def mesh_getgridlen(self, nx=None, ny=None, nz=None):  # parcop.f90:186-191
+        return self._mesh(6)
+
+    def mesh_getcellvol(self, nx=None, ny=None, nz=None):  # parcop.f90:179-184
+        return self._mesh(7)
+
+    def getvar(self, vname, nx=None, ny=None, nz=None):  # parcop.f90:84-128 (Cartesian names)
+        table = {"x": 0, "y": 1, "z": 2, "d1": 3, "d2": 4, "d3": 5}
+        key = str(vname).strip()
+        if key not in table:
+            raise ValueError("mesh variable %r is not available on a Cartesian mesh" % key)
+        return self._mesh(table[key])
+
+    # single-process communicators (comm.f90): every rank id is 0
+    def commx(self):
+        return 0
+
+    commy = commz = commxy = commyz = commxz = commx
+
+
+parcop = _Parcop()

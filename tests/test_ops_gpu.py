@@ -195,3 +195,29 @@ def test_fp32_sweeps_track_fp64(oracle, case):
     c = g.field(torch.full(shape, 3.25, dtype=torch.float64, device="cuda"))
     assert torch.equal(g.filter("spectral", c), c)
     assert float(g.d1(0, c).abs().max()) == 0.0
+
+
+def test_parcop_shim_numpy_roundtrip(oracle):
+    """The f2py-named shim: setup/set_patch/ddx/sfilter/pring/... on numpy arrays."""
+    from pyranda_gb300.parcop import parcop
+    shape = (40, 24, 16)
+    parcop.setup(0, 0, 0, 40, 24, 16, 1, 1, 1, 0, 0.0, 1.0, -0.5, 2.0, 0.25, 3.0,
+                 "PERI", "PERI", "NONE", "NONE", "PERI", "PERI")
+    parcop.setup(1, 0, 0, 16, 16, 16, 1, 1, 1, 0, 0.0, 1.0, 0.0, 1.0, 0.0, 1.0,
+                 "NONE", "NONE", "NONE", "NONE", "NONE", "NONE")
+    parcop.set_patch(0, 0)
+    o = oracle.OracleGrid(shape, (True, False, True), (0.0, -0.5, 0.25), (1.0, 2.0, 3.0))
+    v = smooth_field(shape, seed=31)
+    assert rel_l2(parcop.ddx(v), o.ddx(v)) <= TOL
+    assert rel_l2(parcop.ddy(v), o.ddy(v)) <= TOL
+    assert rel_l2(parcop.dd8z(v), o.dd8(2, v)) <= TOL
+    assert rel_l2(parcop.sfilter(v), o.sfilter(v)) <= TOL
+    assert rel_l2(parcop.gfilter(v), o.gfilter(v)) <= TOL
+    assert rel_l2(parcop.gfilterdir(v, 2), o.gfilterdir(v, 1)) <= TOL
+    assert rel_l2(parcop.pring(v), o.ring(v, 2)) <= TOL
+    gx, gy, gz = parcop.grads(v)
+    assert rel_l2(gz, o.ddz(v)) <= TOL
+    assert numpy.array_equal(parcop.xgrid(), o.mesh(0))
+    assert numpy.array_equal(parcop.mesh_getgridlen(), o.mesh(6))
+    with pytest.raises(ValueError):
+        parcop.setup(2, 0, 0, 16, 16, 16, 1, 1, 1, 0, 0, 1, 0, 1, 0, 1, "SYMM", "NONE", "NONE", "NONE", "NONE", "NONE")
