@@ -41,9 +41,11 @@ def parse():
     p.add_argument("--n", type=int, default=256, help="grid points per direction")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
-    p.add_argument("--mode", default="step", choices=["step", "sweeps", "profile"],
+    p.add_argument("--mode", default="step", choices=["step", "sweeps", "profile", "peaks", "shock"],
                    help="sweeps: time every directional sweep kernel alone on one n^3 field; "
-                        "profile: one eager RK step between cudaProfilerStart/Stop (for ncu)")
+                        "profile: one eager RK step between cudaProfilerStart/Stop (for ncu); "
+                        "peaks: HBM copy, FP64 and FP32 GEMM rates; "
+                        "shock: throughput of the 512x128x128 shock-interface problem")
     p.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     p.add_argument("--reps", type=int, default=20)
     return p.parse_args()
@@ -105,7 +107,7 @@ def _cpu_worker(args):
     os.environ["OMP_NUM_THREADS"] = "1"
     sys.path.insert(0, ROOT)
     from oracle import oracle
-    from tests import scripts
+    from pyranda_gb300 import problems
     oracle.set_threads(1)
     import numpy
 
@@ -113,8 +115,8 @@ def _cpu_worker(args):
                      for ax, n in zip("xyz", shape))
     ss = oracle.OracleSim("TG", mesh)
     ss.addPackage("Timestep")
-    ss.EOM(scripts.TGV_EOM)
-    ss.setIC(scripts.TGV_IC)
+    ss.EOM(problems.TGV_EOM)
+    ss.setIC(problems.TGV_IC)
     dt = ss.variables["dt"].data * CFL
     t = 0.0
     for _ in range(warmup):
@@ -187,10 +189,9 @@ def run_reference(args):
 
 # ------------------------------------------------------------------------------ GPU
 def make_sim(n, precision, graphs):
-    from pyranda_gb300 import pyrandaSim, pyrandaTimestep
-    from tests import scripts
-    ss = scripts.make_tgv(pyrandaSim, n, lambda s: s.addPackage(pyrandaTimestep(s)), silent=True,
-                          precision=precision)
+    from pyranda_gb300 import pyrandaSim, pyrandaTimestep, problems
+    ss = problems.build_tgv(pyrandaSim, n, lambda s: s.addPackage(pyrandaTimestep(s)), silent=True,
+                            precision=precision)
     if graphs:
         ss.use_graphs(True)
     return ss
@@ -300,8 +301,73 @@ def profile_step(args):
     return 0
 
 
+def measure_peaks():
+    """Device ceilings measured with library routines (copy, DGEMM, SGEMM)."""
+    import torch
+    torch.cuda.set_device(0)
+    torch.backends.cuda.matmul.allow_tf32 = False
+    out = {}
+
+    def best(f, reps=10):
+        f()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            f()
+            e.record()
+            torch.cuda.synchronize()
+            ts.append(s.elapsed_time(e) / 1e3)
+        return min(ts)
+
+    a = torch.empty(1 << 28, dtype=torch.float64, device="cuda")
+    b = torch.empty_like(a)
+    a.fill_(1.0)
+    out["hbm_copy_GBps"] = round(2 * a.numel() * 8 / best(lambda: b.copy_(a)) / 1e9, 1)
+    del a, b
+    for dt, key, n in ((torch.float64, "fp64_gemm_TFLOPs", 8192), (torch.float32, "fp32_gemm_TFLOPs", 8192)):
+        x = torch.randn(n, n, dtype=dt, device="cuda")
+        y = torch.randn(n, n, dtype=dt, device="cuda")
+        out[key] = round(2 * n ** 3 / best(lambda: torch.mm(x, y), 5) / 1e12, 2)
+        del x, y
+    out["device"] = torch.cuda.get_device_name(0)
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def shock_throughput(args):
+    """Mpoint-RK-steps/s of the 512x128x128 shock-interface problem (FP64 and fast path)."""
+    import torch
+    from pyranda_gb300 import pyrandaSim, pyrandaBC, pyrandaTimestep, problems
+    torch.cuda.set_device(0)
+
+    def packs(s):
+        s.addPackage(pyrandaBC(s))
+        s.addPackage(pyrandaTimestep(s))
+
+    out = {"workload": "shock-interface 512x128x128, x one-sided, y/z periodic, LAD", "steps": args.steps}
+    npts = 512 * 128 * 128
+    for prec, graphs in (("fp64", False), ("fp32", True)):
+        ss = problems.build_shock(pyrandaSim, 512, 128, 128, packs, silent=True, precision=prec)
+        if graphs:
+            ss.use_graphs(True)
+        run_steps(ss, max(3, args.warmup))
+        sec = time_steps(ss, args.steps, torch, False)
+        out[prec + ("+graphs" if graphs else "")] = {"value": round(job_value(npts, args.steps, 1, sec), 3),
+                                                     "unit": UNIT, "ms_per_step": round(sec / args.steps * 1e3, 3)}
+        del ss
+        torch.cuda.empty_cache()
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.mode == "peaks":
+        return measure_peaks()
+    if args.mode == "shock":
+        return shock_throughput(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.mode == "sweeps":

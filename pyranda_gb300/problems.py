@@ -1,0 +1,226 @@
+"""Benchmark and acceptance problems as pyranda input strings.
+
+Each problem is the mesh, EOM and IC text a pyranda user writes, plus a
+``build(Sim, ...)`` helper that feeds it to any simulation class with the
+pyrandaSim API (this package's, or a CPU restatement used to check it).
+
+- Taylor-Green vortex: pyranda's examples/TaylorGreen.py (EOM and IC verbatim).
+- 3-D advection of a Gaussian shell with the compact filter every stage.
+- Shock-interface: Mach 1.5 planar shock into a density-ratio-3 perturbed
+  interface, single-fluid Euler with LAD, one-sided closures in x, periodic
+  in y and z (the structure of examples/RM3D.py without species).
+"""
+import math
+
+# --------------------------------------------------------------- Taylor-Green
+TGV_EOM = """
+# Primary Equations of motion here
+ddt(:rho:)  =  -ddx(:rho:*:u:)            - ddy(:rho:*:v:)               - ddz(:rho:*:w:)
+ddt(:rhou:) =  -ddx(:rhou:*:u: - :tauxx:) - ddy(:rhou:*:v: - :tauxy:)    - ddz(:rhou:*:w: - :tauxz:)
+ddt(:rhov:) =  -ddx(:rhov:*:u: - :tauxy:) - ddy(:rhov:*:v: - :tauyy:)    - ddz(:rhov:*:w: - :tauyz:)
+ddt(:rhow:) =  -ddx(:rhow:*:u: - :tauxz:) - ddy(:rhow:*:v: - :tauyz:)    - ddz(:rhow:*:w: - :tauzz:)
+ddt(:Et:)   =  -ddx( (:Et: - :tauxx:)*:u: - :tauxy:*:v: - :tauxz:*:w: )  - ddy( (:Et: - :tauyy:)*:v: -:tauxy:*:u: - :tauyz:*:w:) - ddz( (:Et: - :tauzz:)*:w: - :tauxz:*:u: - :tauyz:*:v: )
+# Conservative filter of the EoM
+:rho:       =  fbar( :rho:  )
+:rhou:      =  fbar( :rhou: )
+:rhov:      =  fbar( :rhov: )
+:rhow:      =  fbar( :rhow: )
+:Et:        =  fbar( :Et:   )
+# Update the primatives and enforce the EOS
+:u:         =  :rhou: / :rho:
+:v:         =  :rhov: / :rho:
+:w:         =  :rhow: / :rho:
+:p:         =  ( :Et: - .5*:rho:*(:u:*:u: + :v:*:v: + :w:*:w:) ) * ( :gamma: - 1.0 )
+# Artificial bulk viscosity
+:ux:        =  ddx(:u:)
+:vy:        =  ddy(:v:)
+:wz:        =  ddz(:w:)
+:div:       =  :ux: + :vy: + :wz:
+# Remaining cross derivatives
+:uy:        =  ddy(:u:)
+:uz:        =  ddz(:u:)
+:vx:        =  ddx(:v:)
+:vz:        =  ddz(:v:)
+:wy:        =  ddy(:w:)
+:wx:        =  ddx(:w:)
+:enst:      = sqrt( (:uy:-:vx:)**2 + (:uz: - :wx:)**2 + (:vz:-:wy:)**2 )
+:tke:       = :rho:*(:u:*:u: + :v:*:v: + :w:*:w:)
+:S:         = sqrt( :ux:*:ux: + :vy:*:vy: + :wz:*:wz: + .5*((:uy:+:vx:)**2 + (:uz: + :wx:)**2 + (:vz:+:wy:)**2) )
+:mu:        =  gbar( abs(ring(:S:  )) ) * :rho: * 1.0e-4
+:beta:      =  gbar( abs(ring(:div:)) * :rho: )  * 7.0e-3
+:taudia:    =  (:beta:-2./3.*:mu:) *:div: - :p:
+:tauxx:     =  2.0*:mu:*:ux:   + :taudia:
+:tauyy:     =  2.0*:mu:*:vy:   + :taudia:
+:tauzz:     =  2.0*:mu:*:wz:   + :taudia:
+:tauxy:     = :mu:*(:uy:+:vx:)
+:tauxz:     = :mu:*(:uz:+:wx:)
+:tauyz:     = :mu:*(:vz:+:wz:)
+:cs:  = sqrt( :p: / :rho: * :gamma: )
+:dt: = dt.courant(:u:,:v:,:w:,:cs:)*1.0
+:dt: = numpy.minimum(:dt:,0.2 * dt.diff(:beta:,:rho:))
+:dt: = numpy.minimum(:dt:,0.2 * dt.diff(:mu:,:rho:))
+"""
+
+TGV_IC = """
+:gamma: = 1.4
+u0 = 1.0
+p0 = 100.0
+rho0 = 1.0
+L = 1.0
+:u: =  u0*sin(meshx/L)*cos(meshy/L)*cos(meshz/L)
+:v: = -u0*cos(meshx/L)*sin(meshy/L)*cos(meshz/L)
+:w: = 0.0*:u:
+:p:  = p0 + rho0/16.0*( ( cos(2.*meshx/L) + cos(2.*meshy/L) ) * ( cos(2.*meshz/L) + 2.0 ) - 2.0 )
+:rho: = rho0 + 0.0*:u:
+:rhou: = :rho:*:u:
+:rhov: = :rho:*:v:
+:rhow: = :rho:*:w:
+:Et:  = :p: / (:gamma:-1.0) + 0.5*:rho:*(:u:*:u: + :v:*:v: + :w:*:w:)
+:cs:  = sqrt( :p: / :rho: * :gamma: )
+:tke: = :rho:*(:u:*:u: + :v:*:v: + :w:*:w:)
+:dt: = dt.courant(:u:,:v:,:w:,:cs:)
+"""
+
+
+def tgv_mesh(npts):
+    """examples/TaylorGreen.py: periodic [0, 2 pi) in every direction."""
+    return """
+xdom = (0.0, 2*pi*FF,  Npts, periodic=True)
+ydom = (0.0, 2*pi*FF,  Npts, periodic=True)
+zdom = (0.0, 2*pi*FF,  Npts, periodic=True)
+""".replace("Npts", str(npts)).replace("pi", str(math.pi)).replace("FF", str(float(npts - 1) / npts))
+
+
+def build_tgv(Sim, npts, timestep, **kw):
+    ss = Sim("TGvortex", tgv_mesh(npts), **kw)
+    timestep(ss)
+    ss.EOM(TGV_EOM)
+    ss.setIC(TGV_IC)
+    return ss
+
+
+# ------------------------------------------------------------ 3-D advection
+ADVECTION3D_EOM = """
+ddt(:phi:)  =  -ddx(:phi:) - ddy(:phi:) - ddz(:phi:)
+:phi:       =  fbar( :phi: )
+"""
+
+ADVECTION3D_IC = """
+r     = sqrt( (meshx-0.5)**2 + (meshy-0.5)**2 + (meshz-0.5)**2 )
+:phi: = 1.0 + 0.1*exp( -(r-0.5)**2/0.1**2 )
+:phi0: = 1.0*:phi:
+"""
+
+
+def advection3d_mesh(npts):
+    """Periodic [0, 1)^3 as pyranda nodes: x1 = 0, xn = (n-1)/n."""
+    xn = repr(float(npts - 1) / npts)
+    return "\n".join("%sdom = (0.0, %s, %d, periodic=True)" % (ax, xn, npts) for ax in "xyz")
+
+
+def build_advection3d(Sim, npts, **kw):
+    ss = Sim("advection3d", advection3d_mesh(npts), **kw)
+    ss.EOM(ADVECTION3D_EOM)
+    ss.setIC(ADVECTION3D_IC)
+    return ss
+
+
+# ---------------------------------------------------------- shock-interface
+# Rankine-Hugoniot state behind a Mach 1.5 shock moving in +x into gas at
+# rest with rho = 1, p = 1, gamma = 1.4.
+GAMMA = 1.4
+MACH = 1.5
+P_RATIO = 1.0 + 2.0 * GAMMA / (GAMMA + 1.0) * (MACH ** 2 - 1.0)
+RHO_RATIO = (GAMMA + 1.0) * MACH ** 2 / ((GAMMA - 1.0) * MACH ** 2 + 2.0)
+SHOCK_SPEED = MACH * math.sqrt(GAMMA)
+U_POST = SHOCK_SPEED * (1.0 - 1.0 / RHO_RATIO)
+
+SHOCK_EOM = """
+# Euler with LAD (the structure of examples/RM3D.py for one fluid)
+ddt(:rho:)  =  -ddx(:rho:*:u:)            - ddy(:rho:*:v:)               - ddz(:rho:*:w:)
+ddt(:rhou:) =  -ddx(:rhou:*:u: - :tauxx:) - ddy(:rhou:*:v: - :tauxy:)    - ddz(:rhou:*:w: - :tauxz:)
+ddt(:rhov:) =  -ddx(:rhov:*:u: - :tauxy:) - ddy(:rhov:*:v: - :tauyy:)    - ddz(:rhov:*:w: - :tauyz:)
+ddt(:rhow:) =  -ddx(:rhow:*:u: - :tauxz:) - ddy(:rhow:*:v: - :tauyz:)    - ddz(:rhow:*:w: - :tauzz:)
+ddt(:Et:)   =  -ddx( (:Et: - :tauxx:)*:u: - :tauxy:*:v: - :tauxz:*:w: )  - ddy( (:Et: - :tauyy:)*:v: -:tauxy:*:u: - :tauyz:*:w:) - ddz( (:Et: - :tauzz:)*:w: - :tauxz:*:u: - :tauyz:*:v: )
+:rho:       =  fbar( :rho:  )
+:rhou:      =  fbar( :rhou: )
+:rhov:      =  fbar( :rhov: )
+:rhow:      =  fbar( :rhow: )
+:Et:        =  fbar( :Et:   )
+:u:         =  :rhou: / :rho:
+:v:         =  :rhov: / :rho:
+:w:         =  :rhow: / :rho:
+:p:         =  ( :Et: - .5*:rho:*(:u:*:u: + :v:*:v: + :w:*:w:) ) * ( :gamma: - 1.0 )
+:ux:        =  ddx(:u:)
+:vy:        =  ddy(:v:)
+:wz:        =  ddz(:w:)
+:div:       =  :ux: + :vy: + :wz:
+:uy:        =  ddy(:u:)
+:uz:        =  ddz(:u:)
+:vx:        =  ddx(:v:)
+:vz:        =  ddz(:v:)
+:wy:        =  ddy(:w:)
+:wx:        =  ddx(:w:)
+:S:         = sqrt( :ux:*:ux: + :vy:*:vy: + :wz:*:wz: + .5*((:uy:+:vx:)**2 + (:uz: + :wx:)**2 + (:vz:+:wy:)**2) )
+:mu:        =  gbar( abs(ring(:S:  )) ) * :rho: * 1.0e-4
+:beta:      =  gbar( abs(ring(:div:)) * :rho: )  * 7.0e-2
+:taudia:    =  (:beta:-2./3.*:mu:) *:div: - :p:
+:tauxx:     =  2.0*:mu:*:ux:   + :taudia:
+:tauyy:     =  2.0*:mu:*:vy:   + :taudia:
+:tauzz:     =  2.0*:mu:*:wz:   + :taudia:
+:tauxy:     = :mu:*(:uy:+:vx:)
+:tauxz:     = :mu:*(:uz:+:wx:)
+:tauyz:     = :mu:*(:vz:+:wy:)
+:cs:        = sqrt( :p: / :rho: * :gamma: )
+:dt:        = dt.courant(:u:,:v:,:w:,:cs:)*1.0
+:dt:        = numpy.minimum(:dt:,0.2 * dt.diff(:beta:,:rho:))
+:dt:        = numpy.minimum(:dt:,0.2 * dt.diff(:mu:,:rho:))
+# x boundaries: extrapolate the state, no transverse velocity
+bc.extrap(['rho','Et','u'],['x1','xn'])
+bc.const(['v','w'],['x1','xn'],0.0)
+:rhou: = :rho:*:u:
+:rhov: = :rho:*:v:
+:rhow: = :rho:*:w:
+"""
+
+# Shock at x = 0.5, interface at x = 1.0 + 0.05 sin(2*2 pi y) sin(2*2 pi z),
+# density 1 -> 3 across the interface (pressure equal), tanh profiles of
+# width 2 grid spacings.
+SHOCK_IC = """
+:gamma: = GAMMA
+delta = 2.0*DX
+xs = 0.5
+xi = 1.0 + 0.05*sin(4.0*pi*meshy)*sin(4.0*pi*meshz)
+hs = 0.5*(1.0 - tanh( (meshx - xs)/delta ))
+hi = 0.5*(1.0 + tanh( (meshx - xi)/delta ))
+:rho: = (1.0 + 2.0*hi)*(1.0 - hs) + RHOP*hs
+:u:   = UP*hs
+:v:   = 0.0*meshx
+:w:   = 0.0*meshx
+:p:   = 1.0 + (PP - 1.0)*hs
+:rhou: = :rho:*:u:
+:rhov: = :rho:*:v:
+:rhow: = :rho:*:w:
+:Et:  = :p:/(:gamma:-1.0) + 0.5*:rho:*(:u:*:u: + :v:*:v: + :w:*:w:)
+:cs:  = sqrt( :p: / :rho: * :gamma: )
+:dt:  = dt.courant(:u:,:v:,:w:,:cs:)
+"""
+
+
+def shock_mesh(nx, ny, nz, lx=4.0):
+    """x in [0, lx] with one-sided closures; y, z periodic on [0, 1)."""
+    return "\n".join([
+        "xdom = (0.0, %r, %d)" % (lx, nx),
+        "ydom = (0.0, %r, %d, periodic=True)" % (float(ny - 1) / ny, ny),
+        "zdom = (0.0, %r, %d, periodic=True)" % (float(nz - 1) / nz, nz),
+    ])
+
+
+def build_shock(Sim, nx, ny, nz, packages, lx=4.0, **kw):
+    ss = Sim("shock", shock_mesh(nx, ny, nz, lx), **kw)
+    packages(ss)
+    ss.EOM(SHOCK_EOM)
+    ic = SHOCK_IC.replace("GAMMA", repr(GAMMA)).replace("DX", repr(lx / (nx - 1)))
+    ic = ic.replace("RHOP", repr(RHO_RATIO)).replace("UP", repr(U_POST)).replace("PP", repr(P_RATIO))
+    ss.setIC(ic)
+    return ss

@@ -8,6 +8,8 @@ two share.  Mesh and EOM strings are the reference scripts' own inputs.
 """
 import numpy
 
+from pyranda_gb300.problems import TGV_EOM, TGV_IC, tgv_mesh  # noqa: F401  (problem strings)
+
 
 def _f(x):
     """float() of a Python number, numpy scalar or 0-d torch tensor."""
@@ -90,89 +92,9 @@ r   = sqrt( (meshx-pi)**2  )
     return _sumsq_diff(ss.variables["phi"].data, ss.variables["phi2"].data)
 
 
-TGV_EOM = """
-# Primary Equations of motion here
-ddt(:rho:)  =  -ddx(:rho:*:u:)            - ddy(:rho:*:v:)               - ddz(:rho:*:w:)
-ddt(:rhou:) =  -ddx(:rhou:*:u: - :tauxx:) - ddy(:rhou:*:v: - :tauxy:)    - ddz(:rhou:*:w: - :tauxz:)
-ddt(:rhov:) =  -ddx(:rhov:*:u: - :tauxy:) - ddy(:rhov:*:v: - :tauyy:)    - ddz(:rhov:*:w: - :tauyz:)
-ddt(:rhow:) =  -ddx(:rhow:*:u: - :tauxz:) - ddy(:rhow:*:v: - :tauyz:)    - ddz(:rhow:*:w: - :tauzz:)
-ddt(:Et:)   =  -ddx( (:Et: - :tauxx:)*:u: - :tauxy:*:v: - :tauxz:*:w: )  - ddy( (:Et: - :tauyy:)*:v: -:tauxy:*:u: - :tauyz:*:w:) - ddz( (:Et: - :tauzz:)*:w: - :tauxz:*:u: - :tauyz:*:v: )
-# Conservative filter of the EoM
-:rho:       =  fbar( :rho:  )
-:rhou:      =  fbar( :rhou: )
-:rhov:      =  fbar( :rhov: )
-:rhow:      =  fbar( :rhow: )
-:Et:        =  fbar( :Et:   )
-# Update the primatives and enforce the EOS
-:u:         =  :rhou: / :rho:
-:v:         =  :rhov: / :rho:
-:w:         =  :rhow: / :rho:
-:p:         =  ( :Et: - .5*:rho:*(:u:*:u: + :v:*:v: + :w:*:w:) ) * ( :gamma: - 1.0 )
-# Artificial bulk viscosity
-:ux:        =  ddx(:u:)
-:vy:        =  ddy(:v:)
-:wz:        =  ddz(:w:)
-:div:       =  :ux: + :vy: + :wz:
-# Remaining cross derivatives
-:uy:        =  ddy(:u:)
-:uz:        =  ddz(:u:)
-:vx:        =  ddx(:v:)
-:vz:        =  ddz(:v:)
-:wy:        =  ddy(:w:)
-:wx:        =  ddx(:w:)
-:enst:      = sqrt( (:uy:-:vx:)**2 + (:uz: - :wx:)**2 + (:vz:-:wy:)**2 )
-:tke:       = :rho:*(:u:*:u: + :v:*:v: + :w:*:w:)
-:S:         = sqrt( :ux:*:ux: + :vy:*:vy: + :wz:*:wz: + .5*((:uy:+:vx:)**2 + (:uz: + :wx:)**2 + (:vz:+:wy:)**2) )
-:mu:        =  gbar( abs(ring(:S:  )) ) * :rho: * 1.0e-4
-:beta:      =  gbar( abs(ring(:div:)) * :rho: )  * 7.0e-3
-:taudia:    =  (:beta:-2./3.*:mu:) *:div: - :p:
-:tauxx:     =  2.0*:mu:*:ux:   + :taudia:
-:tauyy:     =  2.0*:mu:*:vy:   + :taudia:
-:tauzz:     =  2.0*:mu:*:wz:   + :taudia:
-:tauxy:     = :mu:*(:uy:+:vx:)
-:tauxz:     = :mu:*(:uz:+:wx:)
-:tauyz:     = :mu:*(:vz:+:wz:)
-:cs:  = sqrt( :p: / :rho: * :gamma: )
-:dt: = dt.courant(:u:,:v:,:w:,:cs:)*1.0
-:dt: = numpy.minimum(:dt:,0.2 * dt.diff(:beta:,:rho:))
-:dt: = numpy.minimum(:dt:,0.2 * dt.diff(:mu:,:rho:))
-"""
-
-TGV_IC = """
-:gamma: = 1.4
-u0 = 1.0
-p0 = 100.0
-rho0 = 1.0
-L = 1.0
-:u: =  u0*sin(meshx/L)*cos(meshy/L)*cos(meshz/L)
-:v: = -u0*cos(meshx/L)*sin(meshy/L)*cos(meshz/L)
-:w: = 0.0*:u:
-:p:  = p0 + rho0/16.0*( ( cos(2.*meshx/L) + cos(2.*meshy/L) ) * ( cos(2.*meshz/L) + 2.0 ) - 2.0 )
-:rho: = rho0 + 0.0*:u:
-:rhou: = :rho:*:u:
-:rhov: = :rho:*:v:
-:rhow: = :rho:*:w:
-:Et:  = :p: / (:gamma:-1.0) + 0.5*:rho:*(:u:*:u: + :v:*:v: + :w:*:w:)
-:cs:  = sqrt( :p: / :rho: * :gamma: )
-:tke: = :rho:*(:u:*:u: + :v:*:v: + :w:*:w:)
-:dt: = dt.courant(:u:,:v:,:w:,:cs:)
-"""
-
-
-def tgv_mesh(Npts):
-    return """
-xdom = (0.0, 2*pi*FF,  Npts, periodic=True)
-ydom = (0.0, 2*pi*FF,  Npts, periodic=True)
-zdom = (0.0, 2*pi*FF,  Npts, periodic=True)
-""".replace("Npts", str(Npts)).replace("pi", str(numpy.pi)).replace("FF", str(float(Npts - 1) / Npts))
-
-
 def make_tgv(Sim, Npts, timestep, **kw):
-    ss = Sim("TGvortex", tgv_mesh(Npts), **kw)
-    timestep(ss)
-    ss.EOM(TGV_EOM)
-    ss.setIC(TGV_IC)
-    return ss
+    from pyranda_gb300.problems import build_tgv
+    return build_tgv(Sim, Npts, timestep, **kw)
 
 
 def taylor_green(Sim, Npts, tstop, timestep, steps=None, **kw):
