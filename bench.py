@@ -41,11 +41,13 @@ def parse():
     p.add_argument("--n", type=int, default=256, help="grid points per direction")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
-    p.add_argument("--mode", default="step", choices=["step", "sweeps", "profile", "peaks", "shock"],
+    p.add_argument("--mode", default="step", choices=["step", "sweeps", "profile", "peaks", "shock", "ensemble"],
                    help="sweeps: time every directional sweep kernel alone on one n^3 field; "
                         "profile: one eager RK step between cudaProfilerStart/Stop (for ncu); "
                         "peaks: HBM copy, FP64 and FP32 GEMM rates; "
-                        "shock: throughput of the 512x128x128 shock-interface problem")
+                        "shock: throughput of the 512x128x128 shock-interface problem; "
+                        "ensemble: 64 Kelvin-Helmholtz 2-D runs of seeded sizes advanced together")
+    p.add_argument("--members", type=int, default=64, help="ensemble mode: number of members")
     p.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     p.add_argument("--reps", type=int, default=20)
     return p.parse_args()
@@ -362,12 +364,107 @@ def shock_throughput(args):
     return 0
 
 
+def ensemble_throughput(args):
+    """Mpoint-RK-steps/s of 64 Kelvin-Helmholtz runs (n^2, n from {128..512}, seeded) in one ensemble.
+
+    Runs the FP64 ensemble eagerly and the fast path (FP32 sweeps, CUDA graph
+    per step), the fast path's field error against FP64 after the same steps,
+    the average duration of one x and one y derivative sweep over all members,
+    and the members one at a time (one graph-captured simulation per distinct
+    size, times its count) for comparison.
+    """
+    import torch
+    from pyranda_gb300 import pyrandaSim, pyrandaBC, pyrandaTimestep, problems
+    from pyranda_gb300.ensemble import pyrandaEnsemble
+    torch.cuda.set_device(0)
+
+    def packs(s):
+        s.addPackage(pyrandaTimestep(s))
+        s.addPackage(pyrandaBC(s))
+
+    sizes = problems.kh_sizes(args.members)
+    npts = sum(n * n for n in sizes)
+    k, w = args.steps, max(3, args.warmup)
+    out = {"workload": "Kelvin-Helmholtz 2-D ensemble, %d members n^2 with n from %s (default_rng(0))"
+                       % (len(sizes), list(problems.KH_SIZES)),
+           "points": npts, "steps": k}
+
+    def run(ens, nsteps, dt):
+        t = torch.zeros(ens.M, dtype=torch.float64, device="cuda")
+        for _ in range(nsteps):
+            t = ens.rk4(t, dt)
+            dt = torch.minimum(ens.variables["dt"].data, 1.1 * dt)
+        return dt
+
+    res = {}
+    for prec, graphs in (("fp64", False), ("fp32", True)):
+        ens = problems.build_kh_ensemble(pyrandaEnsemble, sizes, packs, silent=True, precision=prec)
+        if graphs:
+            ens.use_graphs(True)
+        dt0 = ens.variables["dt"].data.clone()
+        dt = run(ens, w, dt0.clone())
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        run(ens, k, dt)
+        e.record()
+        torch.cuda.synchronize()
+        sec = s.elapsed_time(e) / 1e3
+        out[prec + ("+graphs" if graphs else "")] = {"value": round(npts * k / sec / 1e6, 3), "unit": UNIT,
+                                                     "ms_per_step": round(sec / k * 1e3, 3)}
+        res[prec] = ens
+    # the two precisions took the same number of steps from the same IC
+    out["fp32_vs_fp64_rel_l2"] = {n: float(((res["fp32"].variables[n].data - res["fp64"].variables[n].data).norm()
+                                            / res["fp64"].variables[n].data.norm()).item())
+                                  for n in ("rho", "rhou", "rhov", "Et")}
+    g = res["fp32"].grid
+    v = res["fp32"].variables["rho"].data
+    o = g.empty()
+    for d in (0, 1):
+        g.d1(d, v, out=o)
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        for _ in range(args.reps):
+            g.d1(d, v, out=o)
+        e.record()
+        torch.cuda.synchronize()
+        ms = s.elapsed_time(e) / args.reps
+        out["d1_%s_fp32" % "xy"[d]] = {"ms": round(ms, 4), "GB/s": round(16.0 * npts / (ms * 1e-3) / 1e9, 1)}
+    del res, g, v, o
+    torch.cuda.empty_cache()
+    # one member at a time: every distinct size once, weighted by its count
+    seq = 0.0
+    for n in sorted(set(sizes)):
+        ss = problems.build_kh(pyrandaSim, n, packs, silent=True, precision="fp32")
+        ss.use_graphs(True)
+        dt = ss.variables["dt"].data.clone()
+        t = 0.0
+        for _ in range(w):
+            t = ss.rk4(t, dt)
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        for _ in range(k):
+            t = ss.rk4(t, dt)
+        e.record()
+        torch.cuda.synchronize()
+        seq += s.elapsed_time(e) / 1e3 * sizes.count(n)
+        del ss
+    out["one_at_a_time_fp32+graphs"] = {"value": round(npts * k / seq / 1e6, 3), "unit": UNIT,
+                                        "ms_per_step": round(seq / k * 1e3, 3)}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.mode == "peaks":
         return measure_peaks()
     if args.mode == "shock":
         return shock_throughput(args)
+    if args.mode == "ensemble":
+        return ensemble_throughput(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.mode == "sweeps":

@@ -133,6 +133,44 @@ int pg_reduce(pg_handle* h, int op, const double* in, int64_t n, double* out, vo
  * leaves it unchanged (pyranda.py:359-369 checked for NaN on the host). */
 int pg_check_finite(const double* in, int64_t n, int* flag, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Ensembles: many independent grids advanced together.  No counterpart in
+ * parcop, which holds one patch per (patch, level) and runs them one at a time.
+ * The members' fields are stored back to back in one flat FP64 buffer (member
+ * m occupies points [offsets[m], offsets[m+1]) in its own Fortran order), and
+ * every operator is one launch over the lines of all members, so small grids
+ * fill the GPU together.  Members may differ in size but must share
+ * periodicity and null directions.  Reductions give one value per member,
+ * broadcast to the member's points (a per-point field) so that expressions
+ * and the RK update can use them pointwise. */
+typedef struct pg_ensemble pg_ensemble;
+int pg_ens_create(int m, const pg_grid* grids, pg_ensemble** out);
+int pg_ens_destroy(pg_ensemble* e);
+/* Total points; fills offsets[0..m] when not NULL. */
+int64_t pg_ens_points(const pg_ensemble* e, int64_t* offsets);
+int pg_ens_set_precision(pg_ensemble* e, int precision);
+int pg_ens_spacing(const pg_ensemble* e, int member, double* patch_d, double* mesh_d);
+int pg_ens_d1(pg_ensemble* e, int dir, const double* in, double* out, void* stream);
+int pg_ens_d8(pg_ensemble* e, int dir, const double* in, double* out, void* stream);
+int pg_ens_filter(pg_ensemble* e, int kind, int dir, const double* in, double* out, void* stream);
+int pg_ens_ring(pg_ensemble* e, const double* in, double* out, void* stream);
+int pg_ens_ringv(pg_ensemble* e, const double* vx, const double* vy, const double* vz, double* out,
+                 void* stream);
+int pg_ens_grad(pg_ensemble* e, const double* in, double* gx, double* gy, double* gz, void* stream);
+int pg_ens_div(pg_ensemble* e, const double* fx, const double* fy, const double* fz, double* out,
+               void* stream);
+int pg_ens_mesh(pg_ensemble* e, int which, double* out, void* stream);
+/* The LSRK stage with dt_field holding each point's time step. */
+int pg_ens_rk_stage(pg_ensemble* e, int nvar, double* const* U, double* const* PHI,
+                    const double* const* F, const double* dt_field, double A, double B, void* stream);
+int pg_ens_courant(pg_ensemble* e, const double* u, const double* v, const double* w, const double* c,
+                   double vconst, double wconst, double* out_field, void* stream);
+int pg_ens_diff(pg_ensemble* e, const double* bulk, const double* rho, double* out_field, void* stream);
+/* out_field (per point) and/or out_member (m values) may be NULL. */
+int pg_ens_reduce(pg_ensemble* e, int op, const double* in, double* out_field, double* out_member,
+                  void* stream);
+int pg_ens_device_status(pg_ensemble* e, int* status);
+
 /* Allocation-free reduction.  No counterpart in the reference: parcop's
  * reductions ran through MPI on the host (pyrandaMPI.py:307-326).
  * For callers that cannot allocate device memory (a host framework whose

@@ -64,6 +64,25 @@ SIGNATURES = [
     ("pg_filter_host", I, [P, I, I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     ("pg_ring_host", I, [P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     ("pg_launch_count", ctypes.c_uint64, []),
+    ("pg_ens_create", I, [I, ctypes.POINTER(pg_grid), ctypes.POINTER(P)]),
+    ("pg_ens_destroy", I, [P]),
+    ("pg_ens_points", ctypes.c_int64, [P, ctypes.POINTER(ctypes.c_int64)]),
+    ("pg_ens_set_precision", I, [P, I]),
+    ("pg_ens_spacing", I, [P, I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    ("pg_ens_d1", I, [P, I, D, D, P]),
+    ("pg_ens_d8", I, [P, I, D, D, P]),
+    ("pg_ens_filter", I, [P, I, I, D, D, P]),
+    ("pg_ens_ring", I, [P, D, D, P]),
+    ("pg_ens_ringv", I, [P, D, D, D, D, P]),
+    ("pg_ens_grad", I, [P, D, D, D, D, P]),
+    ("pg_ens_div", I, [P, D, D, D, D, P]),
+    ("pg_ens_mesh", I, [P, I, D, P]),
+    ("pg_ens_rk_stage", I, [P, I, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
+                            ctypes.POINTER(ctypes.c_void_p), D, ctypes.c_double, ctypes.c_double, P]),
+    ("pg_ens_courant", I, [P, D, D, D, D, ctypes.c_double, ctypes.c_double, D, P]),
+    ("pg_ens_diff", I, [P, D, D, D, P]),
+    ("pg_ens_reduce", I, [P, I, D, D, D, P]),
+    ("pg_ens_device_status", I, [P, ctypes.POINTER(ctypes.c_int)]),
 ]
 
 

@@ -2,7 +2,10 @@
 //
 // A pg_handle replaces one pyranda patch of the parcop module: where parcop
 // kept global tables selected by set_patch (pyranda/parcop/objects.f90:22-30,
-// :77-89), every call here names its handle explicitly.
+// :77-89), every call here names its handle explicitly.  A pg_ensemble holds
+// many independent grids of different sizes whose fields are stored back to
+// back in one flat buffer; every operator on it is one launch over the lines
+// of all members.  A handle is the one-member case of the same machinery.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -29,29 +32,6 @@ void set_error(const char* fmt, ...) {
 
 void count_launch(uint64_t k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 
-}  // namespace pg
-
-using namespace pg;
-
-struct pg_handle {
-  int n[3];
-  int periodic[3];
-  int precision;
-  double d[3];    // patch spacing used by the d1 metric
-  double dm[3];   // mesh d1, d2, d3
-  double x1f[3];  // lower face coordinates
-  DevOp ops[2][OPK_COUNT][3];
-  void* tables = nullptr;
-  double* work = nullptr;     // one field: temporary of the 3-sweep filters
-  double* work2 = nullptr;    // one field: forward-elimination values of a sweep
-  double* partial = nullptr;  // reduction partials
-  int* status = nullptr;      // device status word (PG_ETIMEOUT from a bounded wait)
-  double* host_in = nullptr;  // device buffers of the host-pointer variants
-  double* host_out = nullptr;
-  cudaStream_t stream = nullptr;
-  int64_t npts = 0;
-};
-
 namespace {
 
 int cuda_fail(cudaError_t e, const char* what) {
@@ -59,175 +39,376 @@ int cuda_fail(cudaError_t e, const char* what) {
   return PG_ECUDA;
 }
 
-#define PG_CUDA(call)                                        \
-  do {                                                       \
-    cudaError_t e_ = (call);                                 \
-    if (e_ != cudaSuccess) return cuda_fail(e_, #call);      \
+#define PG_CUDA(call)                                   \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
   } while (0)
+
+// One grid: spacings (parcop.f90:47-56, patch.f90:83-85, mesh.f90:192-209)
+// and the host tables of every operator.
+struct GridInfo {
+  int n[3];
+  int periodic[3];
+  double d[3];    // patch spacing (the d1 metric)
+  double dm[3];   // mesh d1, d2, d3
+  double x1f[3];  // lower face coordinates
+  int64_t npts;
+  OpTables tab[OPK_COUNT][3];
+};
+
+int grid_info(const pg_grid* g, GridInfo& gi, const char* who) {
+  for (int d = 0; d < 3; d++) {
+    if (g->n[d] < 1) {
+      set_error("%s: n[%d] = %d", who, d, g->n[d]);
+      return PG_EBADSHAPE;
+    }
+    gi.n[d] = g->n[d];
+    gi.periodic[d] = g->periodic[d] ? 1 : 0;
+    const double dn = (g->xn[d] - g->x1[d]) / (double)std::max(g->n[d] - 1, 1);
+    const double f1 = g->x1[d] - dn / 2.0, fn = g->xn[d] + dn / 2.0;
+    gi.x1f[d] = f1;
+    gi.d[d] = (fn - f1) / (double)g->n[d];
+  }
+  for (int d = 0; d < 3; d++) {
+    if (gi.n[d] == 1) {
+      const int a = (d + 1) % 3, b = (d + 2) % 3;
+      gi.dm[d] = std::max(gi.d[std::min(a, b)], gi.d[std::max(a, b)]);
+    } else {
+      gi.dm[d] = gi.d[d];
+    }
+  }
+  gi.npts = (int64_t)gi.n[0] * gi.n[1] * gi.n[2];
+  if (gi.npts >= ((int64_t)1 << 31)) {
+    set_error("%s: %lld points; a field must hold fewer than 2^31 points", who, (long long)gi.npts);
+    return PG_EBADSHAPE;
+  }
+  for (int k = 0; k < OPK_COUNT; k++)
+    for (int d = 0; d < 3; d++) {
+      const double scale = (k == OPK_D1) ? gi.d[d] : 0.0;
+      int rc = build_operator(k, gi.n[d], gi.periodic[d] != 0, scale, gi.tab[k][d]);
+      if (rc != PG_OK) {
+        set_error("%s: direction %d has %d points; a non-null direction needs at least 8", who, d, gi.n[d]);
+        return rc;
+      }
+    }
+  return PG_OK;
+}
+
+// Device state shared by handles and ensembles.
+struct Ctx {
+  int precision = PG_FP64;
+  int nmem = 0;
+  int64_t npts = 0;
+  OpRef ops[2][OPK_COUNT][3];
+  void* blob = nullptr;          // coefficient tables and member-op arrays
+  double* work = nullptr;        // one field: x->y->z filter ping-pong
+  double* work2 = nullptr;       // one field: forward-elimination scratch of a sweep
+  double* partial = nullptr;     // reduction partials (+ per-member results)
+  int* status = nullptr;         // device status word
+  long long* moff = nullptr;     // ensembles: member point offsets (nmem + 1)
+  double* mconst = nullptr;      // ensembles: per member 1/d1 1/d2 1/d3 1/GridLen GridLen
+  double* host_in = nullptr;     // host-pointer variants
+  double* host_out = nullptr;
+  cudaStream_t stream = nullptr;
+};
+
+void free_ctx(Ctx& c) {
+  if (c.blob) cudaFree(c.blob);
+  if (c.work) cudaFree(c.work);
+  if (c.work2) cudaFree(c.work2);
+  if (c.partial) cudaFree(c.partial);
+  if (c.status) cudaFree(c.status);
+  if (c.moff) cudaFree(c.moff);
+  if (c.mconst) cudaFree(c.mconst);
+  if (c.host_in) cudaFree(c.host_in);
+  if (c.host_out) cudaFree(c.host_out);
+  if (c.stream) cudaStreamDestroy(c.stream);
+  c = Ctx();
+}
+
+// Upload the tables of every member, build the member-op arrays and
+// allocate the workspaces.
+int build_ctx(Ctx& c, const std::vector<GridInfo>& g, int precision, const char* who) {
+  const int M = (int)g.size();
+  c.precision = precision;
+  c.nmem = M;
+  for (int m = 1; m < M; m++)
+    for (int d = 0; d < 3; d++) {
+      if (g[m].periodic[d] != g[0].periodic[d] || (g[m].n[d] < 4) != (g[0].n[d] < 4) ||
+          (g[m].n[d] == 1) != (g[0].n[d] == 1)) {
+        set_error("%s: member %d differs from member 0 in periodicity or null directions", who, m);
+        return PG_EINVAL;
+      }
+    }
+  std::vector<long long> off(M + 1, 0);
+  for (int m = 0; m < M; m++) off[m + 1] = off[m] + g[m].npts;
+  c.npts = off[M];
+  // layout of the blob: [tables ...][member ops (2 x 4 x 3 x M)]
+  auto align = [](size_t x) { return (x + 15) & ~(size_t)15; };
+  size_t total = 0;
+  for (int m = 0; m < M; m++)
+    for (int k = 0; k < OPK_COUNT; k++)
+      for (int d = 0; d < 3; d++) {
+        const size_t n = (size_t)g[m].n[d];
+        total += align(n * 9 * 8) + align(n * 12 * 8) + align(n * 9 * 4) + align(n * 12 * 4);
+      }
+  const size_t ops_off = align(total);
+  total = ops_off + sizeof(MemberOp) * (size_t)M * 2 * OPK_COUNT * 3;
+  cudaError_t e = cudaMalloc(&c.blob, total);
+  if (e != cudaSuccess) {
+    set_error("%s: cudaMalloc tables: %s", who, cudaGetErrorString(e));
+    return PG_ENOMEM;
+  }
+  std::vector<unsigned char> host(total, 0);
+  size_t pos = 0;
+  auto put = [&](const std::vector<double>& v, bool f32) -> const void* {
+    pos = align(pos);
+    const void* dptr = (unsigned char*)c.blob + pos;
+    if (f32) {
+      for (size_t i = 0; i < v.size(); i++) {
+        const float x = (float)v[i];
+        std::memcpy(&host[pos + i * 4], &x, 4);
+      }
+      pos += v.size() * 4;
+    } else {
+      std::memcpy(&host[pos], v.data(), v.size() * 8);
+      pos += v.size() * 8;
+    }
+    return dptr;
+  };
+  std::vector<MemberOp> mops((size_t)M * 2 * OPK_COUNT * 3);
+  auto mindex = [&](int p, int k, int d, int m) { return (((size_t)p * OPK_COUNT + k) * 3 + d) * M + m; };
+  static const int order[9] = {0, 1, 5, 6, 2, 3, 4, 7, 8};  // c1 c2 c6 c7 | c3 c4 c5 c8 | c9
+  for (int m = 0; m < M; m++)
+    for (int k = 0; k < OPK_COUNT; k++)
+      for (int d = 0; d < 3; d++) {
+        const OpTables& t = g[m].tab[k][d];
+        std::vector<double> lu12((size_t)t.n * 12, 0.0);
+        for (int i = 0; i < t.n && !t.null_op; i++)
+          for (int q = 0; q < 9; q++) lu12[(size_t)i * 12 + q] = t.lu[(size_t)i * 9 + order[q]];
+        for (int p = 0; p < 2; p++) {
+          MemberOp& o = mops[mindex(p, k, d, m)];
+          o.rhs = put(t.rhs, p == PG_FP32);
+          o.lu = put(lu12, p == PG_FP32);
+          o.n = g[m].n[d];
+          o.nx = g[m].n[0];
+          o.ny = g[m].n[1];
+          o.pad = 0;
+          o.lines = g[m].npts / g[m].n[d];
+          o.off = off[m];
+          const int mid = t.n / 2;
+          for (int l = 0; l < 9; l++) o.ri[l] = t.null_op ? 0.0 : t.rhs[(size_t)mid * 9 + l];
+          o.dm = g[m].dm[d];
+        }
+      }
+  for (int p = 0; p < 2; p++)
+    for (int k = 0; k < OPK_COUNT; k++)
+      for (int d = 0; d < 3; d++) {
+        long long line0 = 0;
+        for (int m = 0; m < M; m++) {
+          MemberOp& o = mops[mindex(p, k, d, m)];
+          o.line0 = line0;
+          line0 += o.lines;
+        }
+        OpRef& r = c.ops[p][k][d];
+        const OpTables& t = g[0].tab[k][d];
+        r.dev = reinterpret_cast<const MemberOp*>((unsigned char*)c.blob + ops_off) + mindex(p, k, d, 0);
+        r.nops = M;
+        r.nlines = line0;
+        r.kind = k;
+        r.periodic = t.periodic;
+        r.implicit = t.implicit;
+        r.addback = t.addback;
+        r.null_op = t.null_op;
+      }
+  std::memcpy(&host[ops_off], mops.data(), sizeof(MemberOp) * mops.size());
+  e = cudaMemcpy(c.blob, host.data(), total, cudaMemcpyHostToDevice);
+  const size_t nbytes = (size_t)c.npts * sizeof(double);
+  if (e == cudaSuccess) e = cudaMalloc(&c.work, nbytes);
+  if (e == cudaSuccess) e = cudaMalloc(&c.work2, nbytes);
+  const size_t npart = std::max((size_t)kReduceBlocks, (size_t)M * kSegBlocks + 2 * (size_t)M);
+  if (e == cudaSuccess) e = cudaMalloc(&c.partial, npart * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&c.status, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(c.status, 0, sizeof(int));
+  {  // per-member offsets and spacings (used by the ensemble reductions)
+    std::vector<double> mc((size_t)M * 5);
+    for (int m = 0; m < M; m++) {
+      const double gl = std::min(std::min(g[m].dm[0], g[m].dm[1]), g[m].dm[2]);
+      mc[(size_t)m * 5 + 0] = 1.0 / g[m].dm[0];
+      mc[(size_t)m * 5 + 1] = 1.0 / g[m].dm[1];
+      mc[(size_t)m * 5 + 2] = 1.0 / g[m].dm[2];
+      mc[(size_t)m * 5 + 3] = 1.0 / gl;
+      mc[(size_t)m * 5 + 4] = gl;
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&c.moff, sizeof(long long) * (M + 1));
+    if (e == cudaSuccess) e = cudaMemcpy(c.moff, off.data(), sizeof(long long) * (M + 1), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&c.mconst, sizeof(double) * mc.size());
+    if (e == cudaSuccess) e = cudaMemcpy(c.mconst, mc.data(), sizeof(double) * mc.size(), cudaMemcpyHostToDevice);
+  }
+  if (e != cudaSuccess) {
+    set_error("%s: %s", who, cudaGetErrorString(e));
+    free_ctx(c);
+    return PG_ENOMEM;
+  }
+  return PG_OK;
+}
 
 bool bad_dir(int d) { return d < 0 || d > 2; }
 
-int sweep(pg_handle* h, int kind, int dir, const double* in, double* out, int epi, double scale, void* st) {
-  const DevOp& op = h->ops[h->precision][kind][dir];
-  SweepLaunch s{in, out, h->n[0], h->n[1], h->n[2], dir, scale, epi, h->status, h->work2};
-  return launch_sweep(op, h->precision, s, st);
+int sweep(Ctx& c, int kind, int dir, const double* in, double* out, int epi, int scale_pow, void* st) {
+  SweepLaunch s{in, out, c.work2, &c.ops[c.precision][kind][dir], dir, epi, scale_pow};
+  return launch_sweep(c.precision, s, st);
 }
 
 // null-op semantics of compact_operators.f90: derivatives -> 0, filters -> copy
-int null_result(pg_handle* h, int kind, const double* in, double* out, void* st) {
-  if (kind == OPK_SF || kind == OPK_GF) return launch_copy(out, in, h->npts, st);
-  return launch_fill(out, 0.0, h->npts, st);
+int apply_one(Ctx& c, int kind, int dir, const double* in, double* out, void* st) {
+  if (c.ops[c.precision][kind][dir].null_op) {
+    if (kind == OPK_SF || kind == OPK_GF) return launch_copy(out, in, c.npts, st);
+    return launch_fill(out, 0.0, c.npts, st);
+  }
+  return sweep(c, kind, dir, in, out, EPI_STORE, 0, st);
 }
 
-int apply_one(pg_handle* h, int kind, int dir, const double* in, double* out, void* st) {
-  if (h->ops[h->precision][kind][dir].null_op) return null_result(h, kind, in, out, st);
-  return sweep(h, kind, dir, in, out, EPI_STORE, 0.0, st);
+// operators.f90:848-853 / :872-875: x -> y -> z, null directions copy
+int filter_all(Ctx& c, int k, const double* in, double* out, void* st) {
+  int dirs[3], nd = 0;
+  for (int d = 0; d < 3; d++)
+    if (!c.ops[c.precision][k][d].null_op) dirs[nd++] = d;
+  if (nd == 0) return launch_copy(out, in, c.npts, st);
+  const double* src = in;
+  for (int q = 0; q < nd; q++) {  // ping-pong so that the last sweep lands in `out`
+    double* dst = ((nd - 1 - q) % 2 == 0) ? out : c.work;
+    int rc = sweep(c, k, dirs[q], src, dst, EPI_STORE, 0, st);
+    if (rc) return rc;
+    src = dst;
+  }
+  return PG_OK;
 }
 
-}  // namespace
+// ringS with L = 2 (operators.f90:615-643); a direction of one point, or a
+// null d8, contributes 0 and max(x, 0) = x for x >= 0 (operators.f90:701-753).
+int ring(Ctx& c, const double* in, double* out, void* st) {
+  bool first = true;
+  for (int d = 0; d < 3; d++) {
+    if (c.ops[c.precision][OPK_D8][d].null_op) continue;
+    int rc = sweep(c, OPK_D8, d, in, out, first ? EPI_RING_SET : EPI_RING_MAX, 2, st);
+    if (rc) return rc;
+    first = false;
+  }
+  if (first) return launch_fill(out, 0.0, c.npts, st);
+  return PG_OK;
+}
 
-// ---------------------------------------------------------------------------
-// host-pointer variants
-// ---------------------------------------------------------------------------
-static int host_prepare(pg_handle* h) {
-  if (!h->stream) PG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
-  if (!h->host_in) PG_CUDA(cudaMalloc(&h->host_in, (size_t)h->npts * sizeof(double)));
-  if (!h->host_out) PG_CUDA(cudaMalloc(&h->host_out, (size_t)h->npts * sizeof(double)));
+// ringV with L = 1 (operators.f90:645-699): max over components then times
+// d equals max over (component, direction) of |d8| d, rounding being monotonic
+int ringv(Ctx& c, const double* vx, const double* vy, const double* vz, double* out, void* st) {
+  const double* src[3] = {vx, vy, vz};
+  bool first = true;
+  for (int d = 0; d < 3; d++) {
+    if (c.ops[c.precision][OPK_D8][d].null_op) continue;
+    for (int q = 0; q < 3; q++) {
+      int rc = sweep(c, OPK_D8, d, src[q], out, first ? EPI_RING_SET : EPI_RING_MAX, 1, st);
+      if (rc) return rc;
+      first = false;
+    }
+  }
+  if (first) return launch_fill(out, 0.0, c.npts, st);
+  return PG_OK;
+}
+
+int grad(Ctx& c, const double* in, double* gx, double* gy, double* gz, void* st) {
+  int rc = apply_one(c, OPK_D1, 0, in, gx, st);
+  if (!rc) rc = apply_one(c, OPK_D1, 1, in, gy, st);
+  if (!rc) rc = apply_one(c, OPK_D1, 2, in, gz, st);
+  return rc;
+}
+
+// divV, Cartesian (operators.f90:38-53): df = fA + fB + fC
+int divergence(Ctx& c, const double* fx, const double* fy, const double* fz, double* out, void* st) {
+  const double* f[3] = {fx, fy, fz};
+  bool first = true;
+  for (int d = 0; d < 3; d++) {
+    if (c.ops[c.precision][OPK_D1][d].null_op) continue;  // contributes exactly 0
+    int rc = sweep(c, OPK_D1, d, f[d], out, first ? EPI_STORE : EPI_ADD, 0, st);
+    if (rc) return rc;
+    first = false;
+  }
+  if (first) return launch_fill(out, 0.0, c.npts, st);
+  return PG_OK;
+}
+
+int host_prepare(Ctx& c) {
+  if (!c.stream) PG_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+  if (!c.host_in) PG_CUDA(cudaMalloc(&c.host_in, (size_t)c.npts * sizeof(double)));
+  if (!c.host_out) PG_CUDA(cudaMalloc(&c.host_out, (size_t)c.npts * sizeof(double)));
   return PG_OK;
 }
 
 template <typename F>
-static int host_call(pg_handle* h, const double* in, double* out, F&& f) {
-  if (!h || !in || !out) return PG_EINVAL;
-  int rc = host_prepare(h);
+int host_call(Ctx& c, const double* in, double* out, F&& f) {
+  if (!in || !out) return PG_EINVAL;
+  int rc = host_prepare(c);
   if (rc) return rc;
-  const size_t bytes = (size_t)h->npts * sizeof(double);
-  PG_CUDA(cudaMemcpyAsync(h->host_in, in, bytes, cudaMemcpyHostToDevice, h->stream));
-  rc = f(h->host_in, h->host_out, (void*)h->stream);
+  const size_t bytes = (size_t)c.npts * sizeof(double);
+  PG_CUDA(cudaMemcpyAsync(c.host_in, in, bytes, cudaMemcpyHostToDevice, c.stream));
+  rc = f(c.host_in, c.host_out, (void*)c.stream);
   if (rc) {
-    cudaStreamSynchronize(h->stream);
+    cudaStreamSynchronize(c.stream);
     return rc;
   }
-  PG_CUDA(cudaMemcpyAsync(out, h->host_out, bytes, cudaMemcpyDeviceToHost, h->stream));
-  PG_CUDA(cudaStreamSynchronize(h->stream));
+  PG_CUDA(cudaMemcpyAsync(out, c.host_out, bytes, cudaMemcpyDeviceToHost, c.stream));
+  PG_CUDA(cudaStreamSynchronize(c.stream));
   return PG_OK;
 }
 
+int read_status(Ctx& c, int* status) {
+  int v = 0;
+  PG_CUDA(cudaMemcpy(&v, c.status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (v != 0) PG_CUDA(cudaMemset(c.status, 0, sizeof(int)));
+  *status = v;
+  return PG_OK;
+}
+
+}  // namespace
+}  // namespace pg
+
+using namespace pg;
+
+struct pg_handle {
+  GridInfo g;
+  Ctx c;
+};
+
+struct pg_ensemble {
+  std::vector<GridInfo> g;
+  Ctx c;
+};
 
 extern "C" {
 
 const char* pg_last_error(void) { return g_err; }
 
-const char* pg_version(void) { return "pyranda_gb300 0.1 (sm_103a)"; }
+const char* pg_version(void) { return "pyranda_gb300 0.2 (sm_103a)"; }
 
 uint64_t pg_launch_count(void) { return g_launches.load(); }
 
-int pg_create(const pg_grid* g, pg_handle** out) {
-  if (!g || !out) {
+int pg_create(const pg_grid* grid, pg_handle** out) {
+  if (!grid || !out) {
     set_error("pg_create: NULL argument");
     return PG_EINVAL;
   }
   *out = nullptr;
-  if (g->precision != PG_FP64 && g->precision != PG_FP32) {
-    set_error("pg_create: bad precision %d", g->precision);
+  if (grid->precision != PG_FP64 && grid->precision != PG_FP32) {
+    set_error("pg_create: bad precision %d", grid->precision);
     return PG_EINVAL;
   }
   pg_handle* h = new pg_handle();
-  h->precision = g->precision;
-  for (int d = 0; d < 3; d++) {
-    if (g->n[d] < 1) {
-      delete h;
-      set_error("pg_create: n[%d] = %d", d, g->n[d]);
-      return PG_EBADSHAPE;
-    }
-    h->n[d] = g->n[d];
-    h->periodic[d] = g->periodic[d] ? 1 : 0;
-    // parcop.f90:47-56 node extents -> faces; patch.f90:83-85 spacing
-    const double dn = (g->xn[d] - g->x1[d]) / (double)std::max(g->n[d] - 1, 1);
-    const double f1 = g->x1[d] - dn / 2.0, fn = g->xn[d] + dn / 2.0;
-    h->x1f[d] = f1;
-    h->d[d] = (fn - f1) / (double)g->n[d];
-  }
-  // mesh.f90:192-209: a direction of one point takes the larger other spacing
-  for (int d = 0; d < 3; d++) {
-    if (h->n[d] == 1) {
-      const int a = (d + 1) % 3, b = (d + 2) % 3;
-      h->dm[d] = std::max(h->d[std::min(a, b)], h->d[std::max(a, b)]);
-    } else {
-      h->dm[d] = h->d[d];
-    }
-  }
-  h->npts = (int64_t)h->n[0] * h->n[1] * h->n[2];
-
-  // assemble and factor every operator on the host
-  OpTables tab[OPK_COUNT][3];
-  size_t total = 0;
-  for (int k = 0; k < OPK_COUNT; k++)
-    for (int d = 0; d < 3; d++) {
-      const double scale = (k == OPK_D1) ? h->d[d] : 0.0;
-      int rc = build_operator(k, h->n[d], h->periodic[d] != 0, scale, tab[k][d]);
-      if (rc != PG_OK) {
-        delete h;
-        set_error("pg_create: direction %d has %d points; a non-null direction needs at least 8", d, g->n[d]);
-        return rc;
-      }
-      total += (size_t)h->n[d] * (9 + 12) * (sizeof(double) + sizeof(float)) + 64;
-    }
-  cudaError_t e = cudaMalloc(&h->tables, total);
-  if (e != cudaSuccess) {
+  int rc = grid_info(grid, h->g, "pg_create");
+  if (rc == PG_OK) rc = build_ctx(h->c, std::vector<GridInfo>{h->g}, grid->precision, "pg_create");
+  if (rc != PG_OK) {
     delete h;
-    set_error("pg_create: cudaMalloc tables: %s", cudaGetErrorString(e));
-    return PG_ENOMEM;
-  }
-  std::vector<unsigned char> host(total);
-  size_t off = 0;
-  auto put = [&](const std::vector<double>& v, bool f32) -> const void* {
-    off = (off + 15) & ~(size_t)15;  // 16-byte aligned rows for vector loads
-    const void* dptr = (unsigned char*)h->tables + off;
-    if (f32) {
-      for (size_t i = 0; i < v.size(); i++) {
-        float x = (float)v[i];
-        std::memcpy(&host[off + i * 4], &x, 4);
-      }
-      off += v.size() * 4;
-    } else {
-      std::memcpy(&host[off], v.data(), v.size() * 8);
-      off += v.size() * 8;
-    }
-    return dptr;
-  };
-  for (int p = 0; p < 2; p++)
-    for (int k = 0; k < OPK_COUNT; k++)
-      for (int d = 0; d < 3; d++) {
-        const OpTables& t = tab[k][d];
-        DevOp& op = h->ops[p][k][d];
-        op.kind = k;
-        op.n = t.n;
-        op.periodic = t.periodic;
-        op.implicit = t.implicit;
-        op.addback = t.addback;
-        op.null_op = t.null_op;
-        op.rhs = put(t.rhs, p == PG_FP32);
-        // solve coefficients regrouped 12 per row for vector loads:
-        // [c1 c2 c6 c7 | c3 c4 c5 c8 | c9 0 0 0]
-        std::vector<double> lu12((size_t)t.n * 12, 0.0);
-        static const int order[9] = {0, 1, 5, 6, 2, 3, 4, 7, 8};
-        for (int i = 0; i < t.n && !t.null_op; i++)
-          for (int q = 0; q < 9; q++) lu12[(size_t)i * 12 + q] = t.lu[(size_t)i * 9 + order[q]];
-        op.lu = put(lu12, p == PG_FP32);
-        const int mid = t.n / 2;
-        for (int l = 0; l < 9; l++) op.rhs_in[l] = t.null_op ? 0.0 : t.rhs[(size_t)mid * 9 + l];
-      }
-  e = cudaMemcpy(h->tables, host.data(), total, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMalloc(&h->work, (size_t)h->npts * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc(&h->work2, (size_t)h->npts * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc(&h->partial, (size_t)kReduceBlocks * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc(&h->status, sizeof(int));
-  if (e == cudaSuccess) e = cudaMemset(h->status, 0, sizeof(int));
-  if (e != cudaSuccess) {
-    set_error("pg_create: %s", cudaGetErrorString(e));
-    pg_destroy(h);
-    return PG_ENOMEM;
+    return rc;
   }
   *out = h;
   return PG_OK;
@@ -235,73 +416,46 @@ int pg_create(const pg_grid* g, pg_handle** out) {
 
 int pg_destroy(pg_handle* h) {
   if (!h) return PG_OK;
-  if (h->tables) cudaFree(h->tables);
-  if (h->work) cudaFree(h->work);
-  if (h->work2) cudaFree(h->work2);
-  if (h->partial) cudaFree(h->partial);
-  if (h->status) cudaFree(h->status);
-  if (h->host_in) cudaFree(h->host_in);
-  if (h->host_out) cudaFree(h->host_out);
-  if (h->stream) cudaStreamDestroy(h->stream);
+  free_ctx(h->c);
   delete h;
   return PG_OK;
 }
 
 int pg_device_status(pg_handle* h, int* status) {
   if (!h || !status) return PG_EINVAL;
-  int v = 0;
-  PG_CUDA(cudaMemcpy(&v, h->status, sizeof(int), cudaMemcpyDeviceToHost));
-  if (v != 0) PG_CUDA(cudaMemset(h->status, 0, sizeof(int)));
-  *status = v;
-  return PG_OK;
+  return read_status(h->c, status);
 }
 
 int pg_set_precision(pg_handle* h, int precision) {
   if (!h || (precision != PG_FP64 && precision != PG_FP32)) return PG_EINVAL;
-  h->precision = precision;
+  h->c.precision = precision;
   return PG_OK;
 }
 
 int pg_get_spacing(const pg_handle* h, double* patch_d, double* mesh_d) {
   if (!h) return PG_EINVAL;
   for (int d = 0; d < 3; d++) {
-    if (patch_d) patch_d[d] = h->d[d];
-    if (mesh_d) mesh_d[d] = h->dm[d];
+    if (patch_d) patch_d[d] = h->g.d[d];
+    if (mesh_d) mesh_d[d] = h->g.dm[d];
   }
   return PG_OK;
 }
 
 int pg_d1(pg_handle* h, int dir, const double* in, double* out, void* stream) {
   if (!h || !in || !out || bad_dir(dir)) return PG_EINVAL;
-  return apply_one(h, OPK_D1, dir, in, out, stream);
+  return apply_one(h->c, OPK_D1, dir, in, out, stream);
 }
 
 int pg_d8(pg_handle* h, int dir, const double* in, double* out, void* stream) {
   if (!h || !in || !out || bad_dir(dir)) return PG_EINVAL;
-  return apply_one(h, OPK_D8, dir, in, out, stream);
+  return apply_one(h->c, OPK_D8, dir, in, out, stream);
 }
 
 int pg_filter(pg_handle* h, int kind, int dir, const double* in, double* out, void* stream) {
   if (!h || !in || !out || (kind != PG_SPECTRAL && kind != PG_GAUSSIAN) || dir < 0 || dir > 3) return PG_EINVAL;
   const int k = kind == PG_SPECTRAL ? OPK_SF : OPK_GF;
-  if (dir < 3) return apply_one(h, k, dir, in, out, stream);
-  // operators.f90:848-853 / :872-875: x -> y -> z, null directions copy
-  int dirs[3], nd = 0;
-  for (int d = 0; d < 3; d++)
-    if (!h->ops[h->precision][k][d].null_op) dirs[nd++] = d;
-  if (nd == 0) return launch_copy(out, in, h->npts, stream);
-  // ping-pong so that the last sweep lands in `out`
-  const double* src = in;
-  for (int q = 0; q < nd; q++) {
-    const bool last = (q == nd - 1);
-    // with an odd number of remaining sweeps write `out`, else the workspace
-    double* dst = ((nd - 1 - q) % 2 == 0) ? out : h->work;
-    (void)last;
-    int rc = sweep(h, k, dirs[q], src, dst, EPI_STORE, 0.0, stream);
-    if (rc) return rc;
-    src = dst;
-  }
-  return PG_OK;
+  if (dir < 3) return apply_one(h->c, k, dir, in, out, stream);
+  return filter_all(h->c, k, in, out, stream);
 }
 
 int pg_ring(pg_handle* h, const double* in, double* out, void* stream) {
@@ -310,18 +464,7 @@ int pg_ring(pg_handle* h, const double* in, double* out, void* stream) {
     set_error("pg_ring: in and out must differ");
     return PG_EINVAL;
   }
-  bool first = true;
-  for (int d = 0; d < 3; d++) {
-    // ringx: a direction of one point contributes 0 (operators.f90:706-711);
-    // d8 on a null direction is also 0 and max(x, 0) = x for x >= 0.
-    if (h->n[d] == 1 || h->ops[h->precision][OPK_D8][d].null_op) continue;
-    const double s = h->dm[d] * h->dm[d];
-    int rc = sweep(h, OPK_D8, d, in, out, first ? EPI_RING_SET : EPI_RING_MAX, s, stream);
-    if (rc) return rc;
-    first = false;
-  }
-  if (first) return launch_fill(out, 0.0, h->npts, stream);
-  return PG_OK;
+  return ring(h->c, in, out, stream);
 }
 
 int pg_ringv(pg_handle* h, const double* vx, const double* vy, const double* vz, double* out, void* stream) {
@@ -330,26 +473,12 @@ int pg_ringv(pg_handle* h, const double* vx, const double* vy, const double* vz,
     set_error("pg_ringv: out must not alias an input");
     return PG_EINVAL;
   }
-  const double* src[3] = {vx, vy, vz};
-  bool first = true;
-  for (int d = 0; d < 3; d++) {
-    if (h->n[d] == 1 || h->ops[h->precision][OPK_D8][d].null_op) continue;
-    for (int c = 0; c < 3; c++) {
-      int rc = sweep(h, OPK_D8, d, src[c], out, first ? EPI_RING_SET : EPI_RING_MAX, h->dm[d], stream);
-      if (rc) return rc;
-      first = false;
-    }
-  }
-  if (first) return launch_fill(out, 0.0, h->npts, stream);
-  return PG_OK;
+  return ringv(h->c, vx, vy, vz, out, stream);
 }
 
 int pg_grad(pg_handle* h, const double* in, double* gx, double* gy, double* gz, void* stream) {
   if (!h || !in || !gx || !gy || !gz) return PG_EINVAL;
-  int rc = apply_one(h, OPK_D1, 0, in, gx, stream);
-  if (!rc) rc = apply_one(h, OPK_D1, 1, in, gy, stream);
-  if (!rc) rc = apply_one(h, OPK_D1, 2, in, gz, stream);
-  return rc;
+  return grad(h->c, in, gx, gy, gz, stream);
 }
 
 int pg_div(pg_handle* h, const double* fx, const double* fy, const double* fz, double* out, void* stream) {
@@ -358,46 +487,40 @@ int pg_div(pg_handle* h, const double* fx, const double* fy, const double* fz, d
     set_error("pg_div: out must not alias fy or fz");
     return PG_EINVAL;
   }
-  const double* f[3] = {fx, fy, fz};
-  bool first = true;
-  for (int d = 0; d < 3; d++) {
-    if (h->ops[h->precision][OPK_D1][d].null_op) continue;  // contributes exactly 0
-    int rc = sweep(h, OPK_D1, d, f[d], out, first ? EPI_STORE : EPI_ADD, 0.0, stream);
-    if (rc) return rc;
-    first = false;
-  }
-  if (first) return launch_fill(out, 0.0, h->npts, stream);
-  return PG_OK;
+  return divergence(h->c, fx, fy, fz, out, stream);
 }
 
 int pg_mesh(pg_handle* h, int which, double* out, void* stream) {
   if (!h || !out || which < 0 || which > 7) return PG_EINVAL;
-  return launch_mesh(which, out, h->n[0], h->n[1], h->n[2], h->x1f, h->d, h->dm, stream);
+  const GridInfo& g = h->g;
+  return launch_mesh(which, out, g.n[0], g.n[1], g.n[2], g.x1f, g.d, g.dm, stream);
 }
 
 int pg_rk_stage(pg_handle* h, int nvar, double* const* U, double* const* PHI, const double* const* F,
                 const double* dt, double A, double B, void* stream) {
   if (!h || nvar < 0 || (nvar > 0 && (!U || !PHI || !F || !dt))) return PG_EINVAL;
   if (nvar == 0) return PG_OK;
-  return launch_rk_stage(nvar, U, PHI, F, dt, A, B, h->npts, stream);
+  return launch_rk_stage(nvar, U, PHI, F, dt, A, B, h->c.npts, 0, stream);
 }
 
 int pg_courant(pg_handle* h, const double* u, const double* v, const double* w, const double* c, double vconst,
                double wconst, double* out, void* stream) {
   if (!h || !u || !c || !out) return PG_EINVAL;
-  const double gl = std::min(std::min(h->dm[0], h->dm[1]), h->dm[2]);
-  return launch_courant(u, v, w, c, vconst, wconst, h->dm, gl, h->npts, h->partial, out, stream);
+  const GridInfo& g = h->g;
+  const double gl = std::min(std::min(g.dm[0], g.dm[1]), g.dm[2]);
+  return launch_courant(u, v, w, c, vconst, wconst, g.dm, gl, h->c.npts, h->c.partial, out, stream);
 }
 
 int pg_diff(pg_handle* h, const double* bulk, const double* rho, double* out, void* stream) {
   if (!h || !bulk || !rho || !out) return PG_EINVAL;
-  const double gl = std::min(std::min(h->dm[0], h->dm[1]), h->dm[2]);
-  return launch_diff(bulk, rho, gl, h->npts, h->partial, out, stream);
+  const GridInfo& g = h->g;
+  const double gl = std::min(std::min(g.dm[0], g.dm[1]), g.dm[2]);
+  return launch_diff(bulk, rho, gl, h->c.npts, h->c.partial, out, stream);
 }
 
 int pg_reduce(pg_handle* h, int op, const double* in, int64_t n, double* out, void* stream) {
   if (!h || !in || !out || op < 0 || op > 2 || n <= 0) return PG_EINVAL;
-  return launch_reduce(op, in, n, h->partial, out, stream);
+  return launch_reduce(op, in, n, h->c.partial, out, stream);
 }
 
 int pg_check_finite(const double* in, int64_t n, int* flag, void* stream) {
@@ -406,20 +529,168 @@ int pg_check_finite(const double* in, int64_t n, int* flag, void* stream) {
 }
 
 int pg_d1_host(pg_handle* h, int dir, const double* in, double* out) {
-  return host_call(h, in, out, [&](const double* a, double* b, void* s) { return pg_d1(h, dir, a, b, s); });
+  if (!h) return PG_EINVAL;
+  return host_call(h->c, in, out, [&](const double* a, double* b, void* s) { return pg_d1(h, dir, a, b, s); });
 }
 
 int pg_d8_host(pg_handle* h, int dir, const double* in, double* out) {
-  return host_call(h, in, out, [&](const double* a, double* b, void* s) { return pg_d8(h, dir, a, b, s); });
+  if (!h) return PG_EINVAL;
+  return host_call(h->c, in, out, [&](const double* a, double* b, void* s) { return pg_d8(h, dir, a, b, s); });
 }
 
 int pg_filter_host(pg_handle* h, int kind, int dir, const double* in, double* out) {
-  return host_call(h, in, out,
+  if (!h) return PG_EINVAL;
+  return host_call(h->c, in, out,
                    [&](const double* a, double* b, void* s) { return pg_filter(h, kind, dir, a, b, s); });
 }
 
 int pg_ring_host(pg_handle* h, const double* in, double* out) {
-  return host_call(h, in, out, [&](const double* a, double* b, void* s) { return pg_ring(h, a, b, s); });
+  if (!h) return PG_EINVAL;
+  return host_call(h->c, in, out, [&](const double* a, double* b, void* s) { return pg_ring(h, a, b, s); });
+}
+
+// ---------------------------------------------------------------------------
+// ensembles
+// ---------------------------------------------------------------------------
+int pg_ens_create(int m, const pg_grid* grids, pg_ensemble** out) {
+  if (m < 1 || !grids || !out) {
+    set_error("pg_ens_create: bad argument");
+    return PG_EINVAL;
+  }
+  *out = nullptr;
+  pg_ensemble* e = new pg_ensemble();
+  e->g.resize(m);
+  for (int i = 0; i < m; i++) {
+    if (grids[i].precision != grids[0].precision || (grids[i].precision != PG_FP64 && grids[i].precision != PG_FP32)) {
+      delete e;
+      set_error("pg_ens_create: members must share one valid precision");
+      return PG_EINVAL;
+    }
+    int rc = grid_info(&grids[i], e->g[i], "pg_ens_create");
+    if (rc != PG_OK) {
+      delete e;
+      return rc;
+    }
+  }
+  int rc = build_ctx(e->c, e->g, grids[0].precision, "pg_ens_create");
+  if (rc != PG_OK) {
+    delete e;
+    return rc;
+  }
+  *out = e;
+  return PG_OK;
+}
+
+int pg_ens_destroy(pg_ensemble* e) {
+  if (!e) return PG_OK;
+  free_ctx(e->c);
+  delete e;
+  return PG_OK;
+}
+
+int64_t pg_ens_points(const pg_ensemble* e, int64_t* offsets) {
+  if (!e) return -1;
+  if (offsets) {
+    int64_t o = 0;
+    for (size_t i = 0; i < e->g.size(); i++) {
+      offsets[i] = o;
+      o += e->g[i].npts;
+    }
+    offsets[e->g.size()] = o;
+  }
+  return e->c.npts;
+}
+
+int pg_ens_set_precision(pg_ensemble* e, int precision) {
+  if (!e || (precision != PG_FP64 && precision != PG_FP32)) return PG_EINVAL;
+  e->c.precision = precision;
+  return PG_OK;
+}
+
+int pg_ens_spacing(const pg_ensemble* e, int member, double* patch_d, double* mesh_d) {
+  if (!e || member < 0 || member >= (int)e->g.size()) return PG_EINVAL;
+  for (int d = 0; d < 3; d++) {
+    if (patch_d) patch_d[d] = e->g[member].d[d];
+    if (mesh_d) mesh_d[d] = e->g[member].dm[d];
+  }
+  return PG_OK;
+}
+
+int pg_ens_d1(pg_ensemble* e, int dir, const double* in, double* out, void* stream) {
+  if (!e || !in || !out || bad_dir(dir)) return PG_EINVAL;
+  return apply_one(e->c, OPK_D1, dir, in, out, stream);
+}
+
+int pg_ens_d8(pg_ensemble* e, int dir, const double* in, double* out, void* stream) {
+  if (!e || !in || !out || bad_dir(dir)) return PG_EINVAL;
+  return apply_one(e->c, OPK_D8, dir, in, out, stream);
+}
+
+int pg_ens_filter(pg_ensemble* e, int kind, int dir, const double* in, double* out, void* stream) {
+  if (!e || !in || !out || (kind != PG_SPECTRAL && kind != PG_GAUSSIAN) || dir < 0 || dir > 3) return PG_EINVAL;
+  const int k = kind == PG_SPECTRAL ? OPK_SF : OPK_GF;
+  if (dir < 3) return apply_one(e->c, k, dir, in, out, stream);
+  return filter_all(e->c, k, in, out, stream);
+}
+
+int pg_ens_ring(pg_ensemble* e, const double* in, double* out, void* stream) {
+  if (!e || !in || !out || in == out) return PG_EINVAL;
+  return ring(e->c, in, out, stream);
+}
+
+int pg_ens_ringv(pg_ensemble* e, const double* vx, const double* vy, const double* vz, double* out, void* stream) {
+  if (!e || !vx || !vy || !vz || !out || out == vx || out == vy || out == vz) return PG_EINVAL;
+  return ringv(e->c, vx, vy, vz, out, stream);
+}
+
+int pg_ens_grad(pg_ensemble* e, const double* in, double* gx, double* gy, double* gz, void* stream) {
+  if (!e || !in || !gx || !gy || !gz) return PG_EINVAL;
+  return grad(e->c, in, gx, gy, gz, stream);
+}
+
+int pg_ens_div(pg_ensemble* e, const double* fx, const double* fy, const double* fz, double* out, void* stream) {
+  if (!e || !fx || !fy || !fz || !out || out == fy || out == fz) return PG_EINVAL;
+  return divergence(e->c, fx, fy, fz, out, stream);
+}
+
+int pg_ens_mesh(pg_ensemble* e, int which, double* out, void* stream) {
+  if (!e || !out || which < 0 || which > 7) return PG_EINVAL;
+  int64_t o = 0;
+  for (const GridInfo& g : e->g) {
+    int rc = launch_mesh(which, out + o, g.n[0], g.n[1], g.n[2], g.x1f, g.d, g.dm, stream);
+    if (rc) return rc;
+    o += g.npts;
+  }
+  return PG_OK;
+}
+
+int pg_ens_rk_stage(pg_ensemble* e, int nvar, double* const* U, double* const* PHI, const double* const* F,
+                    const double* dt_field, double A, double B, void* stream) {
+  if (!e || nvar < 0 || (nvar > 0 && (!U || !PHI || !F || !dt_field))) return PG_EINVAL;
+  if (nvar == 0) return PG_OK;
+  return launch_rk_stage(nvar, U, PHI, F, dt_field, A, B, e->c.npts, 1, stream);
+}
+
+int pg_ens_courant(pg_ensemble* e, const double* u, const double* v, const double* w, const double* c,
+                   double vconst, double wconst, double* out_field, void* stream) {
+  if (!e || !u || !c || !out_field) return PG_EINVAL;
+  return launch_seg_courant(u, v, w, c, vconst, wconst, e->c.mconst, e->c.moff, e->c.nmem, e->c.npts,
+                            e->c.partial, out_field, stream);
+}
+
+int pg_ens_diff(pg_ensemble* e, const double* bulk, const double* rho, double* out_field, void* stream) {
+  if (!e || !bulk || !rho || !out_field) return PG_EINVAL;
+  return launch_seg_diff(bulk, rho, e->c.mconst, e->c.moff, e->c.nmem, e->c.npts, e->c.partial, out_field, stream);
+}
+
+int pg_ens_reduce(pg_ensemble* e, int op, const double* in, double* out_field, double* out_member, void* stream) {
+  if (!e || !in || (!out_field && !out_member) || op < 0 || op > 2) return PG_EINVAL;
+  return launch_seg_reduce(op, in, e->c.moff, e->c.nmem, e->c.npts, e->c.partial, out_field, out_member, stream);
+}
+
+int pg_ens_device_status(pg_ensemble* e, int* status) {
+  if (!e || !status) return PG_EINVAL;
+  return read_status(e->c, status);
 }
 
 }  // extern "C"

@@ -49,10 +49,13 @@ struct RkArgs {
 };
 
 // pyranda.py:800-804:  tmp1 = A*PHI ; PHI = dt*F + tmp1 ; tmp2 = B*PHI ; U = U + tmp2
+// DT_FIELD: one dt per point (an ensemble advances each member with its own dt)
+template <bool DT_FIELD>
 __global__ void rk_stage_kernel(const RkArgs a, int nvar, const double* __restrict__ dtp, double A, double B,
                                 int64_t n) {
-  const double dt = *dtp;
+  const double dt0 = DT_FIELD ? 0.0 : *dtp;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double dt = DT_FIELD ? dtp[i] : dt0;
     for (int v = 0; v < nvar; v++) {
       const double tmp1 = A * a.PHI[v][i];
       const double phi = dt * a.F[v][i] + tmp1;
@@ -186,6 +189,98 @@ __global__ void mesh_kernel(int which, double* __restrict__ out, int nx, int ny,
   }
 }
 
+// ---------------------------------------------------------------------------
+// Ensemble (segmented) reductions: block b works on member b / kSegBlocks.
+// ---------------------------------------------------------------------------
+enum { SEG_SUM = 0, SEG_MAX = 1, SEG_MIN = 2, SEG_COURANT = 3, SEG_DIFF = 4 };
+
+template <int KIND>
+__global__ void seg_partial(const double* __restrict__ a, const double* __restrict__ b,
+                            const double* __restrict__ w, const double* __restrict__ c, double vconst,
+                            double wconst, const double* __restrict__ mconst, const long long* __restrict__ moff,
+                            double* __restrict__ partial) {
+  constexpr int OP = (KIND == SEG_SUM) ? 0 : ((KIND == SEG_MAX || KIND == SEG_COURANT) ? 1 : 2);
+  const int m = blockIdx.x / kSegBlocks, sub = blockIdx.x % kSegBlocks;
+  const long long lo = moff[m], hi = moff[m + 1];
+  double r1 = 0, r2 = 0, r3 = 0, rgl = 0, gl = 0;
+  if (KIND == SEG_COURANT) {
+    r1 = mconst[m * 5 + 0];
+    r2 = mconst[m * 5 + 1];
+    r3 = mconst[m * 5 + 2];
+    rgl = mconst[m * 5 + 3];
+  }
+  if (KIND == SEG_DIFF) gl = mconst[m * 5 + 4];
+  double acc = identity<OP>();
+  bool nan = false;
+  for (long long i = lo + (long long)sub * blockDim.x + threadIdx.x; i < hi; i += (long long)kSegBlocks * blockDim.x) {
+    double x;
+    if (KIND == SEG_COURANT) {
+      const double vv = b ? b[i] : vconst;
+      const double ww = w ? w[i] : wconst;
+      x = fabs(a[i]) * r1 + fabs(vv) * r2 + fabs(ww) * r3 + fabs(c[i]) * rgl;
+    } else if (KIND == SEG_DIFF) {
+      x = b[i] * gl * gl / fmax(1.0e-12, a[i]);
+    } else {
+      x = a[i];
+    }
+    nan |= (x != x);
+    acc = combine<OP>(acc, x);
+  }
+  acc = block_reduce<OP>(acc);
+  const int anynan = __syncthreads_or(nan);
+  if (threadIdx.x == 0) partial[blockIdx.x] = anynan ? NAN : acc;
+}
+
+template <int OP>
+__global__ void seg_final(const double* __restrict__ partial, int invert, double* __restrict__ member) {
+  const int m = blockIdx.x;
+  double acc = identity<OP>();
+  bool nan = false;
+  for (int i = threadIdx.x; i < kSegBlocks; i += blockDim.x) {
+    const double x = partial[m * kSegBlocks + i];
+    nan |= (x != x);
+    acc = combine<OP>(acc, x);
+  }
+  acc = block_reduce<OP>(acc);
+  const int anynan = __syncthreads_or(nan);
+  if (threadIdx.x == 0) member[m] = anynan ? NAN : (invert ? 1.0 / acc : acc);
+}
+
+__global__ void seg_broadcast(const double* __restrict__ member, const long long* __restrict__ moff, int nmem,
+                              int64_t n, double* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    int lo = 0, hi = nmem - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (moff[mid] <= i) lo = mid;
+      else hi = mid - 1;
+    }
+    out[i] = member[lo];
+  }
+}
+
+template <int KIND>
+int seg_run(const double* a, const double* b, const double* w, const double* c, double vconst, double wconst,
+            const double* mconst, const long long* moff, int nmem, int64_t npts, double* partial,
+            double* out_field, double* out_member, void* stream) {
+  constexpr int OP = (KIND == SEG_SUM) ? 0 : ((KIND == SEG_MAX || KIND == SEG_COURANT) ? 1 : 2);
+  cudaStream_t s = (cudaStream_t)stream;
+  double* member = out_member ? out_member : partial + (size_t)nmem * kSegBlocks;
+  seg_partial<KIND><<<nmem * kSegBlocks, kThreads, 0, s>>>(a, b, w, c, vconst, wconst, mconst, moff, partial);
+  seg_final<OP><<<nmem, kThreads, 0, s>>>(partial, KIND == SEG_COURANT ? 1 : 0, member);
+  count_launch(2);
+  if (out_field) {
+    seg_broadcast<<<grid_for(npts), kThreads, 0, s>>>(member, moff, nmem, npts, out_field);
+    count_launch();
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error("segmented reduction: %s", cudaGetErrorString(e));
+    return PG_ECUDA;
+  }
+  return PG_OK;
+}
+
 }  // namespace
 
 int launch_fill(double* out, double value, int64_t n, void* stream) {
@@ -201,7 +296,7 @@ int launch_copy(double* out, const double* in, int64_t n, void* stream) {
 }
 
 int launch_rk_stage(int nvar, double* const* U, double* const* PHI, const double* const* F, const double* dt,
-                    double A, double B, int64_t n, void* stream) {
+                    double A, double B, int64_t n, int dt_is_field, void* stream) {
   RkArgs a;
   for (int v0 = 0; v0 < nvar; v0 += kMaxVar) {
     const int m = nvar - v0 < kMaxVar ? nvar - v0 : kMaxVar;
@@ -210,7 +305,8 @@ int launch_rk_stage(int nvar, double* const* U, double* const* PHI, const double
       a.PHI[v] = PHI[v0 + v];
       a.F[v] = F[v0 + v];
     }
-    rk_stage_kernel<<<grid_for(n), kThreads, 0, (cudaStream_t)stream>>>(a, m, dt, A, B, n);
+    if (dt_is_field) rk_stage_kernel<true><<<grid_for(n), kThreads, 0, (cudaStream_t)stream>>>(a, m, dt, A, B, n);
+    else rk_stage_kernel<false><<<grid_for(n), kThreads, 0, (cudaStream_t)stream>>>(a, m, dt, A, B, n);
     int rc = check("rk_stage");
     if (rc) return rc;
   }
@@ -273,6 +369,33 @@ int launch_mesh(int which, double* out, int nx, int ny, int nz, const double x1f
   mesh_kernel<<<grid_for(n), kThreads, 0, (cudaStream_t)stream>>>(which, out, nx, ny, nz, x1f[0], x1f[1], x1f[2],
                                                                   d[0], d[1], d[2], cval);
   return check("mesh");
+}
+
+}  // namespace pg
+
+namespace pg {
+
+int launch_seg_reduce(int op, const double* in, const long long* moff, int nmem, int64_t npts, double* partial,
+                      double* out_field, double* out_member, void* stream) {
+  if (op == 0) return seg_run<SEG_SUM>(in, nullptr, nullptr, nullptr, 0, 0, nullptr, moff, nmem, npts, partial,
+                                        out_field, out_member, stream);
+  if (op == 1) return seg_run<SEG_MAX>(in, nullptr, nullptr, nullptr, 0, 0, nullptr, moff, nmem, npts, partial,
+                                        out_field, out_member, stream);
+  return seg_run<SEG_MIN>(in, nullptr, nullptr, nullptr, 0, 0, nullptr, moff, nmem, npts, partial, out_field,
+                          out_member, stream);
+}
+
+int launch_seg_courant(const double* u, const double* v, const double* w, const double* c, double vconst,
+                       double wconst, const double* mconst, const long long* moff, int nmem, int64_t npts,
+                       double* partial, double* out_field, void* stream) {
+  return seg_run<SEG_COURANT>(u, v, w, c, vconst, wconst, mconst, moff, nmem, npts, partial, out_field, nullptr,
+                              stream);
+}
+
+int launch_seg_diff(const double* bulk, const double* rho, const double* mconst, const long long* moff, int nmem,
+                    int64_t npts, double* partial, double* out_field, void* stream) {
+  return seg_run<SEG_DIFF>(bulk, rho, nullptr, nullptr, 0, 0, mconst, moff, nmem, npts, partial, out_field,
+                           nullptr, stream);
 }
 
 }  // namespace pg

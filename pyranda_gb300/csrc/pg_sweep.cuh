@@ -37,13 +37,11 @@ namespace pg {
 struct KParams {
   const double* __restrict__ in;
   double* __restrict__ out;
-  void* __restrict__ scratch;  // n x nlines forward-elimination values (T), [position][line]
-  const void* rhs;             // n x 9 per-row RHS weights (T)
-  const void* lu;              // n x 12 per-row solve coefficients (T): c1 c2 c6 c7 | c3 c4 c5 c8 | c9
-  int n, nx, ny, nz;
-  int64_t nlines;
-  double epi_scale;
-  double ri[9];                // interior RHS weights
+  void* __restrict__ scratch;  // forward-elimination values (T); member m's lines at [off_m + position*lines_m + line]
+  const MemberOp* ops;         // one entry per grid of the launch
+  int nops;
+  long long nlines;            // lines over all grids
+  int scale_pow;               // ring epilogues: scale = dm^scale_pow
 };
 
 constexpr int kSweepThreads = 128;
@@ -209,28 +207,43 @@ template <typename T, int KIND, bool PER, bool IMPL, bool ADDBACK, int DIR, int 
 __global__ void __launch_bounds__(kSweepThreads) sweep_kernel(const KParams P) {
   const int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (L >= P.nlines) return;
-  const int n = P.n;
+  // the grid (ensemble member) owning this line: last entry with line0 <= L
+  int m = 0;
+  if (P.nops > 1) {
+    int lo = 0, hi = P.nops - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (P.ops[mid].line0 <= L) lo = mid;
+      else hi = mid - 1;
+    }
+    m = lo;
+  }
+  const MemberOp& op = P.ops[m];
+  const int64_t Lm = L - op.line0;
+  const int n = op.n;
+  const int nx = op.nx, ny = op.ny;
   int64_t base;
   int st;
   if (DIR == 0) {
-    base = L * P.nx;
+    base = Lm * nx;
     st = 1;
   } else if (DIR == 1) {
-    base = (L / P.nx) * (int64_t)P.nx * P.ny + (L % P.nx);
-    st = P.nx;
+    base = (Lm / nx) * (int64_t)nx * ny + (Lm % nx);
+    st = nx;
   } else {
-    base = (L / P.nx) * (int64_t)P.nx + (L % P.nx);
-    st = P.nx * P.ny;
+    base = (Lm / nx) * (int64_t)nx + (Lm % nx);
+    st = nx * ny;
   }
+  base += op.off;
   const double* __restrict__ pin = P.in + base;
   double* __restrict__ pout = P.out + base;
   const Line<T> ln{pin, st, n};
-  const T* __restrict__ R = reinterpret_cast<const T*>(P.rhs);
-  const T* __restrict__ C = reinterpret_cast<const T*>(P.lu);  // 12 per row
-  T* __restrict__ ps = reinterpret_cast<T*>(P.scratch) + L;     // row i at ps[i * nl]
-  const int nl = (int)P.nlines;
+  const T* __restrict__ R = reinterpret_cast<const T*>(op.rhs);
+  const T* __restrict__ C = reinterpret_cast<const T*>(op.lu);  // 12 per row
+  T* __restrict__ ps = reinterpret_cast<T*>(P.scratch) + op.off + Lm;  // row i at ps[i * nl]
+  const int nl = (int)op.lines;
   constexpr bool kReadOut = (EPI == EPI_ADD || EPI == EPI_RING_MAX);
-  const double sc = P.epi_scale;
+  const double sc = (P.scale_pow == 2) ? op.dm * op.dm : (P.scale_pow == 1 ? op.dm : 1.0);
   constexpr int H = (KIND == 1) ? 3 : 4;  // stencil half width
 
   // edge rows first: they may need wrapped values of the far end of the line
@@ -305,7 +318,7 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_kernel(const KParams P) {
   {
     T ai[9];
 #pragma unroll
-    for (int k = 0; k < 9; k++) ai[k] = (T)P.ri[k];
+    for (int k = 0; k < 9; k++) ai[k] = (T)op.ri[k];
     T ring[kRing];
 #pragma unroll
     for (int s2 = 0; s2 < kRing; s2++) {
@@ -417,7 +430,7 @@ int dispatch_dir_epi(const KParams& P, int dir, int epi, void* st) {
 }
 
 template <typename T>
-int dispatch_kind(const DevOp& op, const KParams& P, int dir, int epi, void* st) {
+int dispatch_kind(const OpRef& op, const KParams& P, int dir, int epi, void* st) {
   switch (op.kind) {
     case OPK_D1:
       return op.periodic ? dispatch_dir_epi<T, 1, true, true, false>(P, dir, epi, st)

@@ -4,7 +4,7 @@
 
 namespace pg {
 
-int launch_sweep_f32(const DevOp& op, const KParams& P, int dir, int epi, void* st) {
+int launch_sweep_f32(const OpRef& op, const KParams& P, int dir, int epi, void* st) {
   return dispatch_kind<float>(op, P, dir, epi, st);
 }
 

@@ -211,6 +211,22 @@ class Grid:
         _lib.check(self.lib.pg_reduce(self.h, op, _ptr(v), v.numel(), _ptr(out), _stream()), "pg_reduce")
         return out
 
+    @property
+    def member_points(self):
+        return float(self.npts)
+
+    def reduce_value(self, op, v):
+        """Host value of a global reduction (a number times npts for sums of constants)."""
+        if not isinstance(v, torch.Tensor):
+            return float(v) * self.npts if op == 0 else float(v)
+        return float(self.reduce(op, v))
+
+    def plane(self, axis, k):
+        """Index of plane k (negative counts from the end) along an axis."""
+        idx = [slice(None)] * 3
+        idx[_DIRS[axis] if isinstance(axis, str) else int(axis)] = k
+        return tuple(idx)
+
     def rk_stage(self, U, PHI, F, dt, A, B):
         n = len(U)
         arr = ctypes.c_void_p * n

@@ -9,8 +9,13 @@ pyrandaSim API (this package's, or a CPU restatement used to check it).
 - Shock-interface: Mach 1.5 planar shock into a density-ratio-3 perturbed
   interface, single-fluid Euler with LAD, one-sided closures in x, periodic
   in y and z (the structure of examples/RM3D.py without species).
+- Kelvin-Helmholtz (2-D): the Euler + AFLES EOM of examples/KH.py with one
+  tanh shear layer, periodic in x and walls (one-sided closures) in y; the
+  ensemble benchmark advances 64 of these with seeded sizes together.
 """
 import math
+
+import numpy
 
 # --------------------------------------------------------------- Taylor-Green
 TGV_EOM = """
@@ -224,3 +229,104 @@ def build_shock(Sim, nx, ny, nz, packages, lx=4.0, **kw):
     ic = ic.replace("RHOP", repr(RHO_RATIO)).replace("UP", repr(U_POST)).replace("PP", repr(P_RATIO))
     ss.setIC(ic)
     return ss
+
+
+# ------------------------------------------------------------ Kelvin-Helmholtz
+# examples/KH.py:8-21 constants
+KH_GAMMA = 5.0 / 3.0
+KH_P0 = 2.5
+KH_R = 1.0
+KH_CV = KH_R / (1.0 - 1.0 / KH_GAMMA) - KH_R
+KH_DELTA = 1.0 / 28.0      # shear-layer thickness
+KH_AMP = 0.01              # amplitude of the v perturbation
+KH_SIZES = (128, 192, 256, 384, 512)
+
+# examples/KH.py:61-99 (gamma, R0 and cv substituted by the EOM dictionary),
+# with wall conditions on the y faces in the form of the shock problem's
+KH_EOM = """
+# Primary Equations of motion here
+ddt(:rho:)  =  -ddx(:rho:*:u:)            - ddy(:rho:*:v:)
+ddt(:rhou:) =  -ddx(:rhou:*:u: - :tauxx:) - ddy(:rhou:*:v: - :tauxy:)
+ddt(:rhov:) =  -ddx(:rhov:*:u: - :tauxy:) - ddy(:rhov:*:v: - :tauyy:)
+ddt(:Et:)   =  -ddx( (:Et: - :tauxx:)*:u: - :tauxy:*:v:  - :tx:*:kappa: )  - ddy( (:Et: - :tauyy:)*:v: -:tauxy:*:u:- :ty:*:kappa: )
+# Conservative filter of the EoM
+:rho:       =  fbar( :rho:  )
+:rhou:      =  fbar( :rhou: )
+:rhov:      =  fbar( :rhov: )
+:Et:        =  fbar( :Et:   )
+# Update the primatives and enforce the EOS
+:u:         =  :rhou: / :rho:
+:v:         =  :rhov: / :rho:
+:p:         =  ( :Et: - .5*:rho:*(:u:*:u: + :v:*:v:) ) * ( gamma - 1.0 )
+# Artificial bulk viscosity
+:ux:        =  ddx(:u:)
+:vy:        =  ddy(:v:)
+:div:       =  :ux: + :vy:
+# Remaining cross derivatives
+:uy:        =  ddy(:u:)
+:vx:        =  ddx(:v:)
+:enst:      = sqrt( (:uy:-:vx:)**2 )
+:tke:       = :rho:*(:u:*:u: + :v:*:v: )
+:S:         = sqrt( :ux:*:ux: + :vy:*:vy:  + .5*((:uy:+:vx:)**2  ) )
+:mu:        =  gbar( abs(ring(:S:  )) ) * :rho: * 1.0e-4
+:beta:      =  gbar( abs(ring(:div:)) * :rho: )  * 7.0e-3
+:taudia:    =  (:beta:-2./3.*:mu:) *:div: - :p:
+:tauxx:     =  2.0*:mu:*:ux:   + :taudia:
+:tauyy:     =  2.0*:mu:*:vy:   + :taudia:
+:tauxy:     = :mu:*(:uy:+:vx:)
+:T:         = :p: / (:rho: * R0 )
+[:tx:,:ty:,:tz:] = grad(:T:)
+:kappa:     = gbar( ring(:T:)* :rho:*cv/(:T: * :dt: ) ) * 1.0e-3
+:cs:  = sqrt( :p: / :rho: * gamma )
+:dt: = dt.courant(:u:,:v:,:w:,:cs:)*1.0
+:dt: = numpy.minimum(:dt:,0.2 * dt.diff(:beta:,:rho:))
+:dt: = numpy.minimum(:dt:,0.2 * dt.diff(:mu:,:rho:))
+# y walls: extrapolate the state, no normal velocity
+bc.extrap(['rho','Et','u'],['y1','yn'])
+bc.const(['v'],['y1','yn'],0.0)
+:rhou: = :rho:*:u:
+:rhov: = :rho:*:v:
+"""
+
+# One shear layer at y = 1/2 of thickness delta: u = +-1/2, rho = 1 above and
+# 2 below, uniform pressure, v' = amp sin(2 pi x) exp(-((y - 1/2)/delta)^2).
+KH_IC = """
+hy = tanh( (meshy-0.5)/delta )
+:u: = 0.5*hy
+:rho: = 1.5 - 0.5*hy
+:v: = amp*sin( 2.0*pi*meshx )*exp( -((meshy-0.5)/delta)**2 )
+:p: = p0 + 0.0*meshx
+:Et: = :p:/( gamma - 1.0 ) + .5*:rho:*(:u:*:u: + :v:*:v:)
+:rhou: = :rho:*:u:
+:rhov: = :rho:*:v:
+:cs:  = sqrt( :p: / :rho: * gamma )
+:dt: = dt.courant(:u:,:v:,:w:,:cs:)*.1
+"""
+
+
+def kh_mesh(n):
+    """n x n: x periodic on [0, 1) (pyranda nodes), y in [0, 1] with one-sided closures."""
+    return "xdom = (0.0, %r, %d, periodic=True)\nydom = (0.0, 1.0, %d)" % (float(n - 1) / n, n, n)
+
+
+def kh_sizes(count=64, seed=0):
+    """Member sizes of the ensemble: n drawn uniformly from KH_SIZES by a seeded generator."""
+    return [int(v) for v in numpy.random.default_rng(seed=seed).choice(list(KH_SIZES), count)]
+
+
+def _kh_setup(ss, packages):
+    packages(ss)
+    ss.EOM(KH_EOM, {"gamma": repr(KH_GAMMA), "R0": repr(KH_R), "cv": repr(KH_CV)})
+    ss.setIC(KH_IC, {"gamma": repr(KH_GAMMA), "p0": repr(KH_P0), "delta": repr(KH_DELTA),
+                     "amp": repr(KH_AMP)})
+    return ss
+
+
+def build_kh(Sim, n, packages, **kw):
+    """One n x n Kelvin-Helmholtz simulation."""
+    return _kh_setup(Sim("kh", kh_mesh(n), **kw), packages)
+
+
+def build_kh_ensemble(Ens, sizes, packages, **kw):
+    """len(sizes) Kelvin-Helmholtz simulations, member m of size sizes[m]^2, in one ensemble."""
+    return _kh_setup(Ens("kh", [kh_mesh(n) for n in sizes], **kw), packages)

@@ -57,10 +57,7 @@ class pyrandaVar:
 
     def _reduce(self, op, data=None):
         d = self.data if data is None else data
-        if not isinstance(d, torch.Tensor):
-            n = self.sim.npts
-            return float(d) * n if op == 0 else float(d)
-        return float(self.sim.grid.reduce(op, d))
+        return self.sim.grid.reduce_value(op, d)
 
     def sum(self, axis=None, idata=None):
         d = self.data if idata is None else idata
@@ -71,7 +68,7 @@ class pyrandaVar:
     def mean(self, axis=None, idata=None):
         s = self.sum(axis=axis, idata=idata)
         if axis is None:
-            return s / float(self.sim.npts)
+            return s / self.sim.grid.member_points
         s = numpy.asarray(s)
         return s * s.size / float(self.sim.npts)
 
@@ -613,6 +610,23 @@ class pyrandaSim:
             return dt.to(device=self.grid.device, dtype=torch.float64).reshape(())
         return torch.full((), float(dt), dtype=torch.float64, device=self.grid.device)
 
+    def _time_tensor(self, time):
+        return time
+
+    def _time_buffer(self):
+        """Device storage of the simulation time read by a recorded step."""
+        return torch.zeros((), dtype=torch.float64, device=self.grid.device)
+
+    def _load_time(self, buf, time):
+        if isinstance(time, torch.Tensor):
+            buf.copy_(time)
+        else:
+            buf.fill_(float(time))
+
+    def _stage_time(self, time_i, eta, dt, dt_dev):
+        """t = t0 + eta_k dt (pyranda.py:805)."""
+        return time_i + eta * dt
+
     def _rk4_eager(self, time, dt, dt_dev=None):
         names = self.conserved
         if self._phi is None or set(self._phi) != set(names):
@@ -621,7 +635,7 @@ class pyrandaSim:
             self._phi[U].zero_()
         if dt_dev is None:
             dt_dev = self._dt_tensor(dt)
-        time_i = time
+        time_i = self._time_tensor(time)
         self.deltat = dt
         for ii in range(5):
             flux = self.updateFlux()
@@ -629,7 +643,7 @@ class pyrandaSim:
             F = [self.grid.field(flux[n]) for n in names]
             PHI = [self._phi[n] for n in names]
             self.grid.rk_stage(U, PHI, F, dt_dev, ARK[ii], BRK[ii])
-            time = time_i + ETA[ii] * dt
+            time = self._stage_time(time_i, ETA[ii], dt, dt_dev)
             self.time = time
             self.updateVars()
         self.cycle += 1
@@ -654,11 +668,11 @@ class pyrandaSim:
         if self._graph is None:
             self._capture(time, dt)
         self._g_dt.copy_(self._dt_tensor(dt))
-        self._g_t0.fill_(float(time)) if not isinstance(time, torch.Tensor) else self._g_t0.copy_(time)
+        self._load_time(self._g_t0, time)
         self._graph.replay()
         self.cycle += 1
         self.deltat = dt
-        t = time + dt
+        t = self._stage_time(self._time_tensor(time), 1.0, dt, self._g_dt)
         self.time = t
         return t
 
@@ -668,7 +682,7 @@ class pyrandaSim:
             self._field_of(n)
         before = {n: v.data for n, v in self.variables.items()}
         self._g_dt = self._dt_tensor(dt).clone()
-        self._g_t0 = torch.zeros((), dtype=torch.float64, device=self.grid.device)
+        self._g_t0 = self._time_buffer()
         self._phi = {U: self.grid.empty() for U in self.conserved}
         stream = torch.cuda.Stream(device=self.grid.device)
         stream.wait_stream(torch.cuda.current_stream())

@@ -6,9 +6,6 @@ the processor-boundary tests of the reference are the non-periodic tests.
 """
 from .pyrandaPackage import pyrandaPackage
 
-_AX = {"x": 0, "y": 1, "z": 2}
-
-
 class pyrandaBC(pyrandaPackage):
 
     def __init__(self, pysim):
@@ -24,11 +21,8 @@ class pyrandaBC(pyrandaPackage):
         p = self.pyranda.PyMPI
         return getattr(p, direction[0] + ("1proc" if direction[1] == "1" else "nproc"))
 
-    @staticmethod
-    def _plane(direction, k):
-        idx = [slice(None)] * 3
-        idx[_AX[direction[0]]] = k
-        return tuple(idx)
+    def _plane(self, direction, k):
+        return self.pyranda.grid.plane(direction[0], k)
 
     def extrap(self, var, direction, order=2):
         var = var if isinstance(var, list) else [var]

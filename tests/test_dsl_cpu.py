@@ -31,3 +31,11 @@ def test_sim_smap_matches_reference_keys():
            "random3D()", "erf(", "meshx", "meshy", "meshz", "meshi", "meshj", "meshk"]
     found = [k for k in keys if isinstance(k, str) and k in ref]
     assert found == ref
+
+
+def test_kh_sizes_are_seeded():
+    """The ensemble's member sizes: 64 draws from {128,...,512} by default_rng(seed=0)."""
+    from pyranda_gb300.problems import kh_sizes
+    s = kh_sizes()
+    assert len(s) == 64 and set(s) <= {128, 192, 256, 384, 512}
+    assert s == kh_sizes()
