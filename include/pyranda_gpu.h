@@ -45,8 +45,14 @@ typedef enum {
 
 /* Arithmetic of the compact sweeps.  PG_FP64 follows the reference
  * arithmetic; PG_FP32 evaluates the sweeps in single precision on FP64
- * inputs/outputs (the fast path; FP64 state is kept by the caller). */
-typedef enum { PG_FP64 = 0, PG_FP32 = 1 } pg_precision;
+ * inputs/outputs (the fast path; FP64 state is kept by the caller).
+ * PG_DENSE applies d1, d8 and the compact filter as dense n x n operators
+ * D = A^-1 B (the reference's `sm`, compact_basetype.f90:199-205) on the
+ * tensor cores in split TF32 (hi.hi + hi.lo + lo.hi, FP32 accumulation) for
+ * directions of 16..1024 points, and the FP32 banded sweeps elsewhere; the
+ * filters' add-back of v stays in FP64.  Selecting it builds the dense
+ * tables once (allocates and synchronises). */
+typedef enum { PG_FP64 = 0, PG_FP32 = 1, PG_DENSE = 2 } pg_precision;
 
 typedef enum { PG_SPECTRAL = 0, PG_GAUSSIAN = 1 } pg_filter_kind;
 
@@ -170,6 +176,56 @@ int pg_ens_diff(pg_ensemble* e, const double* bulk, const double* rho, double* o
 int pg_ens_reduce(pg_ensemble* e, int op, const double* in, double* out_field, double* out_member,
                   void* stream);
 int pg_ens_device_status(pg_ensemble* e, int* status);
+
+/* ---------------------------------------------------------------------------
+ * Learned LAD closure (no counterpart in the reference, which evaluates the
+ * plain LAD operators of examples/ISSW_cyl.py:101-104 every stage).  A small
+ * MLP predicts the artificial bulk viscosity beta and conductivity kappa from
+ * the 27-point stencils of div(u)*D and |grad rho|*D plus D (D = GridLen):
+ * PG_LAD_IN inputs padded to PG_LAD_K, three hidden layers of PG_LAD_HIDDEN
+ * (ReLU), PG_LAD_OUT outputs; BF16 weights and activations, FP32 accumulation.
+ * Outputs y are normalised:  beta = (y0*ys0 + ym0) * rho * D  and
+ * kappa = (y1*ys1 + ym1) * rho * cv * D^2 / dt.
+ * Parameters: one FP32 buffer of PG_LAD_NPARAM values laid out
+ * [w1 64x64 | w2 64x64 | w3 64x64 | w4 2x64 | b1 64 | b2 64 | b3 64 | b4 2]
+ * (weights row = output unit), and BF16 copies of its first PG_LAD_NWEIGHT
+ * values (the weights, same order). */
+#define PG_LAD_IN 55
+#define PG_LAD_K 64
+#define PG_LAD_HIDDEN 64
+#define PG_LAD_OUT 2
+#define PG_LAD_NWEIGHT (3 * 64 * 64 + 2 * 64)
+#define PG_LAD_NPARAM (PG_LAD_NWEIGHT + 3 * 64 + 2)
+typedef struct pg_lad_model {
+  const void* wbf16;     /* PG_LAD_NWEIGHT BF16 weights (device) */
+  const float* params;   /* PG_LAD_NPARAM FP32 parameters (device; biases read here) */
+  const float* xmean;    /* PG_LAD_K input means (device) */
+  const float* xinvstd;  /* PG_LAD_K input 1/std (device) */
+  float ym[2], ys[2];    /* output de-normalisation */
+  float ylo[2], yhi[2];  /* accepted range of the raw outputs (training range + margin) */
+} pg_lad_model;
+/* beta and kappa of every point of the grid.  dt is a device scalar; *flag
+ * (device int) is set to 1 when any raw output leaves [ylo, yhi], i.e. the
+ * closure was asked outside its training range and the caller should fall
+ * back to the plain LAD operators. */
+int pg_lad_closure(pg_handle* h, const pg_lad_model* m, const double* div, const double* gmag, const double* rho,
+                   const double* dt, double cv, double* beta, double* kappa, int* flag, void* stream);
+/* Raw (unnormalised) feature rows of ns points (flat indices pts): raw[ns][PG_LAD_K]. */
+int pg_lad_features(pg_handle* h, const double* div, const double* gmag, const int64_t* pts, int64_t ns,
+                    float* raw, void* stream);
+/* X[ns][PG_LAD_K] (BF16) = (raw - xmean) * xinvstd. */
+int pg_lad_normalize(const float* raw, int64_t ns, const float* xmean, const float* xinvstd, void* X,
+                     void* stream);
+/* Adds the gradient of  mean((y - T)^2)  over rows x outputs of one batch
+ * (X BF16 [rows][PG_LAD_K], T FP32 [rows][PG_LAD_OUT]) to grad (FP32,
+ * parameter layout); adds the loss to *loss and writes outputs to Y when
+ * those are not NULL.  inv_count is 1 / (rows of the whole batch * PG_LAD_OUT). */
+int pg_lad_train_step(const pg_lad_model* m, const void* X, const float* T, int64_t rows, float inv_count,
+                      float* grad, float* loss, float* Y, void* stream);
+/* One Adam step on n FP32 parameters (moments m, v), then BF16 copies of the
+ * first nbf of them into pbf. */
+int pg_lad_adam(float* params, float* m, float* v, const float* grad, int n, float lr, float beta1, float beta2,
+                float eps, int step, void* pbf, int nbf, void* stream);
 
 /* Allocation-free reduction.  No counterpart in the reference: parcop's
  * reductions ran through MPI on the host (pyrandaMPI.py:307-326).

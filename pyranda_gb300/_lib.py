@@ -9,7 +9,18 @@ import os
 from . import build as _build
 
 PG_OK, PG_EBADSHAPE, PG_ENULLOP, PG_ECUDA, PG_ENAN, PG_ETIMEOUT, PG_EINVAL, PG_ENOMEM = range(8)
-PG_FP64, PG_FP32 = 0, 1
+PG_FP64, PG_FP32, PG_DENSE = 0, 1, 2
+_PRECISIONS = {"fp64": PG_FP64, "fp32": PG_FP32, "dense": PG_DENSE}
+
+
+def precision_code(name):
+    """'fp64' (reference arithmetic), 'fp32' (FP32 banded sweeps) or 'dense' (split-TF32 tensor-core operators)."""
+    try:
+        return _PRECISIONS[name]
+    except KeyError:
+        raise ValueError("precision must be one of %s, not %r" % (sorted(_PRECISIONS), name)) from None
+
+
 PG_SPECTRAL, PG_GAUSSIAN = 0, 1
 PG_DIR_ALL = 3
 
@@ -29,6 +40,17 @@ class pg_grid(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int * 3), ("periodic", ctypes.c_int * 3),
                 ("x1", ctypes.c_double * 3), ("xn", ctypes.c_double * 3),
                 ("precision", ctypes.c_int)]
+
+
+PG_LAD_IN, PG_LAD_K, PG_LAD_HIDDEN, PG_LAD_OUT = 55, 64, 64, 2
+PG_LAD_NWEIGHT = 3 * 64 * 64 + 2 * 64
+PG_LAD_NPARAM = PG_LAD_NWEIGHT + 3 * 64 + 2
+
+
+class pg_lad_model(ctypes.Structure):
+    _fields_ = [("wbf16", ctypes.c_void_p), ("params", ctypes.c_void_p), ("xmean", ctypes.c_void_p),
+                ("xinvstd", ctypes.c_void_p), ("ym", ctypes.c_float * 2), ("ys", ctypes.c_float * 2),
+                ("ylo", ctypes.c_float * 2), ("yhi", ctypes.c_float * 2)]
 
 
 _lib = None
@@ -83,6 +105,11 @@ SIGNATURES = [
     ("pg_ens_diff", I, [P, D, D, D, P]),
     ("pg_ens_reduce", I, [P, I, D, D, D, P]),
     ("pg_ens_device_status", I, [P, ctypes.POINTER(ctypes.c_int)]),
+    ("pg_lad_closure", I, [P, ctypes.POINTER(pg_lad_model), D, D, D, D, ctypes.c_double, D, D, D, P]),
+    ("pg_lad_features", I, [P, D, D, D, ctypes.c_int64, D, P]),
+    ("pg_lad_normalize", I, [D, ctypes.c_int64, D, D, D, P]),
+    ("pg_lad_train_step", I, [ctypes.POINTER(pg_lad_model), D, D, ctypes.c_int64, ctypes.c_float, D, D, D, P]),
+    ("pg_lad_adam", I, [D, D, D, D, I, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, I, D, I, P]),
 ]
 
 

@@ -111,6 +111,14 @@ struct Ctx {
   double* host_in = nullptr;     // host-pointer variants
   double* host_out = nullptr;
   cudaStream_t stream = nullptr;
+  std::vector<MemberOp> mops;    // host copy of the member-op arrays
+  // dense split-TF32 operators (PG_DENSE): used for d1, d8 and the compact
+  // filter where built; the Gaussian filter and every other case run the
+  // FP32 banded sweeps
+  bool dense = false;
+  bool dense_built = false;
+  DenseSet dsets[OPK_COUNT][3];
+  void* dense_blob = nullptr;
 };
 
 void free_ctx(Ctx& c) {
@@ -124,6 +132,7 @@ void free_ctx(Ctx& c) {
   if (c.host_in) cudaFree(c.host_in);
   if (c.host_out) cudaFree(c.host_out);
   if (c.stream) cudaStreamDestroy(c.stream);
+  if (c.dense_blob) cudaFree(c.dense_blob);
   c = Ctx();
 }
 
@@ -223,6 +232,7 @@ int build_ctx(Ctx& c, const std::vector<GridInfo>& g, int precision, const char*
         r.null_op = t.null_op;
       }
   std::memcpy(&host[ops_off], mops.data(), sizeof(MemberOp) * mops.size());
+  c.mops = mops;
   e = cudaMemcpy(c.blob, host.data(), total, cudaMemcpyHostToDevice);
   const size_t nbytes = (size_t)c.npts * sizeof(double);
   if (e == cudaSuccess) e = cudaMalloc(&c.work, nbytes);
@@ -256,7 +266,201 @@ int build_ctx(Ctx& c, const std::vector<GridInfo>& g, int precision, const char*
 
 bool bad_dir(int d) { return d < 0 || d > 2; }
 
+// Dense form of the d1, d8 and compact-filter operators of every member: D is
+// the banded FP64 operator itself, applied to an identity (line k = e_k), so
+// the dense and banded paths implement one matrix.  Members with identical
+// tables share one split copy of D.
+int build_dense(Ctx& c, const std::vector<GridInfo>& g) {
+  if (c.dense_built) return PG_OK;
+  const int M = (int)g.size();
+  const int kinds[3] = {OPK_D1, OPK_D8, OPK_SF};
+  struct Uniq {
+    int k, d, m, rows, kchunks;
+    std::vector<uint32_t> planes;
+    size_t off;
+  };
+  std::vector<Uniq> uniq;
+  std::vector<int> which((size_t)OPK_COUNT * 3 * M, -1);  // unique entry of (kind, dir, member)
+  int nmax = 0;
+  for (int k : kinds)
+    for (int d = 0; d < 3; d++) {
+      if (c.ops[PG_FP64][k][d].null_op) continue;
+      bool fits = true;
+      for (int m = 0; m < M; m++) fits = fits && g[m].n[d] >= 16 && g[m].n[d] <= 1024;
+      if (!fits) continue;
+      for (int m = 0; m < M; m++) {
+        const OpTables& t = g[m].tab[k][d];
+        int u = -1;
+        for (size_t q = 0; q < uniq.size() && u < 0; q++) {
+          const Uniq& e = uniq[q];
+          const OpTables& o = g[e.m].tab[k][d];
+          if (e.k == k && e.d == d && o.n == t.n && o.rhs == t.rhs && o.lu == t.lu) u = (int)q;
+        }
+        if (u < 0) {
+          uniq.push_back(Uniq{k, d, m, 0, 0, {}, 0});
+          u = (int)uniq.size() - 1;
+          nmax = std::max(nmax, t.n);
+        }
+        which[((size_t)k * 3 + d) * M + m] = u;
+      }
+    }
+  if (uniq.empty()) {
+    c.dense_built = true;
+    return PG_OK;
+  }
+  // D of each unique operator: the FP64 banded sweep of an identity field
+  const size_t nn = (size_t)nmax * nmax;
+  double *ident = nullptr, *dout = nullptr, *scr = nullptr;
+  MemberOp* tmp = nullptr;
+  cudaError_t e = cudaMalloc(&ident, nn * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&dout, nn * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&scr, nn * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&tmp, sizeof(MemberOp));
+  int rc = (e == cudaSuccess) ? PG_OK : PG_ENOMEM;
+  if (rc) set_error("dense operators: %s", cudaGetErrorString(e));
+  std::vector<double> eye, Dt, D;
+  for (size_t q = 0; q < uniq.size() && rc == PG_OK; q++) {
+    Uniq& u = uniq[q];
+    const int n = g[u.m].n[u.d];
+    eye.assign((size_t)n * n, 0.0);
+    for (int i = 0; i < n; i++) eye[(size_t)i * n + i] = 1.0;
+    const size_t mi = ((((size_t)PG_FP64 * OPK_COUNT + u.k) * 3 + u.d) * M) + u.m;
+    MemberOp mo = c.mops[mi];
+    mo.nx = n;
+    mo.ny = n;
+    mo.lines = n;
+    mo.line0 = 0;
+    mo.off = 0;
+    OpRef ref = c.ops[PG_FP64][u.k][u.d];
+    ref.dev = tmp;
+    ref.nops = 1;
+    ref.nlines = n;
+    e = cudaMemcpy(ident, eye.data(), eye.size() * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(tmp, &mo, sizeof(MemberOp), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      set_error("dense operators: %s", cudaGetErrorString(e));
+      rc = PG_ECUDA;
+      break;
+    }
+    SweepLaunch s{ident, dout, scr, &ref, 0, EPI_STORE, 0};
+    rc = launch_sweep(PG_FP64, s, nullptr);
+    if (rc) break;
+    Dt.resize((size_t)n * n);
+    e = cudaMemcpy(Dt.data(), dout, Dt.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+      set_error("dense operators: %s", cudaGetErrorString(e));
+      rc = PG_ECUDA;
+      break;
+    }
+    // line k of the output is column k of D
+    D.assign((size_t)n * n, 0.0);
+    for (int k = 0; k < n; k++)
+      for (int i = 0; i < n; i++) D[(size_t)i * n + k] = Dt[(size_t)k * n + i];
+    if (ref.addback)
+      for (int i = 0; i < n; i++) D[(size_t)i * n + i] -= 1.0;
+    split_dense(D, n, u.planes, u.rows, u.kchunks);
+  }
+  cudaFree(ident);
+  cudaFree(dout);
+  cudaFree(scr);
+  cudaFree(tmp);
+  if (rc) return rc;
+  // one blob: [planes ...][DenseOp arrays][DenseTile arrays]
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  size_t total = 0;
+  for (auto& u : uniq) {
+    u.off = total;
+    total = al(total + u.planes.size() * 4);
+  }
+  std::vector<DenseOp> dops;
+  std::vector<DenseTile> dtiles;
+  size_t set_ops[OPK_COUNT][3] = {}, set_tiles[OPK_COUNT][3] = {};
+  int set_nt[OPK_COUNT][3] = {};
+  for (int k : kinds)
+    for (int d = 0; d < 3; d++) {
+      if (which[((size_t)k * 3 + d) * M] < 0) continue;
+      set_ops[k][d] = dops.size();
+      set_tiles[k][d] = dtiles.size();
+      for (int m = 0; m < M; m++) {
+        const Uniq& u = uniq[which[((size_t)k * 3 + d) * M + m]];
+        const int n = g[m].n[d];
+        DenseOp o{};
+        o.dsw = reinterpret_cast<const uint32_t*>(u.off);  // relocated below
+        o.off = (long long)c.mops[(((size_t)PG_FP64 * OPK_COUNT + k) * 3 + d) * M + m].off;
+        o.n = n;
+        o.nx = g[m].n[0];
+        o.ny = g[m].n[1];
+        o.kchunks = u.kchunks;
+        o.rows = u.rows;
+        o.dm = g[m].dm[d];
+        dops.push_back(o);
+        const int lines = (int)(g[m].npts / n);
+        const int lt = (d == 0) ? 128 : 256;
+        const int parts = (d == 0) ? (((n + 15) & ~15) + 255) / 256 : (n + 127) / 128;
+        for (int l0 = 0; l0 < lines; l0 += lt)
+          for (int p = 0; p < parts; p++)
+            dtiles.push_back(DenseTile{m, l0, std::min(lt, lines - l0), p});
+      }
+      set_nt[k][d] = (int)(dtiles.size() - set_tiles[k][d]);
+    }
+  const size_t ops_at = total;
+  const size_t tiles_at = al(ops_at + dops.size() * sizeof(DenseOp));
+  total = tiles_at + dtiles.size() * sizeof(DenseTile);
+  e = cudaMalloc(&c.dense_blob, total);
+  if (e != cudaSuccess) {
+    set_error("dense operators: cudaMalloc: %s", cudaGetErrorString(e));
+    return PG_ENOMEM;
+  }
+  unsigned char* base = (unsigned char*)c.dense_blob;
+  for (auto& o : dops) o.dsw = reinterpret_cast<const uint32_t*>(base + (size_t)o.dsw);
+  std::vector<unsigned char> host(total, 0);
+  for (auto& u : uniq) std::memcpy(&host[u.off], u.planes.data(), u.planes.size() * 4);
+  std::memcpy(&host[ops_at], dops.data(), dops.size() * sizeof(DenseOp));
+  std::memcpy(&host[tiles_at], dtiles.data(), dtiles.size() * sizeof(DenseTile));
+  e = cudaMemcpy(c.dense_blob, host.data(), total, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    set_error("dense operators: %s", cudaGetErrorString(e));
+    return PG_ECUDA;
+  }
+  for (int k : kinds)
+    for (int d = 0; d < 3; d++) {
+      if (which[((size_t)k * 3 + d) * M] < 0) continue;
+      DenseSet& ds = c.dsets[k][d];
+      ds.ops = reinterpret_cast<const DenseOp*>(base + ops_at) + set_ops[k][d];
+      ds.tiles = reinterpret_cast<const DenseTile*>(base + tiles_at) + set_tiles[k][d];
+      ds.ntiles = set_nt[k][d];
+      ds.ok = true;
+      ds.addback = c.ops[PG_FP64][k][d].addback;
+    }
+  c.dense_built = true;
+  return PG_OK;
+}
+
+// Arithmetic of later sweeps: PG_FP64 / PG_FP32 banded, or PG_DENSE (dense
+// split-TF32 operators where built, FP32 banded elsewhere).
+int set_precision(Ctx& c, const std::vector<GridInfo>& g, int precision) {
+  if (precision == PG_DENSE) {
+    int rc = build_dense(c, g);
+    if (rc) return rc;
+    c.precision = PG_FP32;
+    c.dense = true;
+    return PG_OK;
+  }
+  if (precision != PG_FP64 && precision != PG_FP32) return PG_EINVAL;
+  c.precision = precision;
+  c.dense = false;
+  return PG_OK;
+}
+
 int sweep(Ctx& c, int kind, int dir, const double* in, double* out, int epi, int scale_pow, void* st) {
+  if (c.dense && c.dsets[kind][dir].ok) {
+    if (in == out) {  // tiles read whole lines that other tiles write: work on a copy
+      int rc = launch_copy(c.work2, in, c.npts, st);
+      if (rc) return rc;
+      in = c.work2;
+    }
+    return launch_dense(c.dsets[kind][dir], in, out, dir, epi, scale_pow, c.status, st);
+  }
   SweepLaunch s{in, out, c.work2, &c.ops[c.precision][kind][dir], dir, epi, scale_pow};
   return launch_sweep(c.precision, s, st);
 }
@@ -399,14 +603,16 @@ int pg_create(const pg_grid* grid, pg_handle** out) {
     return PG_EINVAL;
   }
   *out = nullptr;
-  if (grid->precision != PG_FP64 && grid->precision != PG_FP32) {
+  if (grid->precision != PG_FP64 && grid->precision != PG_FP32 && grid->precision != PG_DENSE) {
     set_error("pg_create: bad precision %d", grid->precision);
     return PG_EINVAL;
   }
   pg_handle* h = new pg_handle();
   int rc = grid_info(grid, h->g, "pg_create");
-  if (rc == PG_OK) rc = build_ctx(h->c, std::vector<GridInfo>{h->g}, grid->precision, "pg_create");
+  if (rc == PG_OK) rc = build_ctx(h->c, std::vector<GridInfo>{h->g}, PG_FP64, "pg_create");
+  if (rc == PG_OK) rc = set_precision(h->c, std::vector<GridInfo>{h->g}, grid->precision);
   if (rc != PG_OK) {
+    free_ctx(h->c);
     delete h;
     return rc;
   }
@@ -427,9 +633,8 @@ int pg_device_status(pg_handle* h, int* status) {
 }
 
 int pg_set_precision(pg_handle* h, int precision) {
-  if (!h || (precision != PG_FP64 && precision != PG_FP32)) return PG_EINVAL;
-  h->c.precision = precision;
-  return PG_OK;
+  if (!h) return PG_EINVAL;
+  return set_precision(h->c, std::vector<GridInfo>{h->g}, precision);
 }
 
 int pg_get_spacing(const pg_handle* h, double* patch_d, double* mesh_d) {
@@ -561,7 +766,8 @@ int pg_ens_create(int m, const pg_grid* grids, pg_ensemble** out) {
   pg_ensemble* e = new pg_ensemble();
   e->g.resize(m);
   for (int i = 0; i < m; i++) {
-    if (grids[i].precision != grids[0].precision || (grids[i].precision != PG_FP64 && grids[i].precision != PG_FP32)) {
+    if (grids[i].precision != grids[0].precision ||
+        (grids[i].precision != PG_FP64 && grids[i].precision != PG_FP32 && grids[i].precision != PG_DENSE)) {
       delete e;
       set_error("pg_ens_create: members must share one valid precision");
       return PG_EINVAL;
@@ -572,8 +778,10 @@ int pg_ens_create(int m, const pg_grid* grids, pg_ensemble** out) {
       return rc;
     }
   }
-  int rc = build_ctx(e->c, e->g, grids[0].precision, "pg_ens_create");
+  int rc = build_ctx(e->c, e->g, PG_FP64, "pg_ens_create");
+  if (rc == PG_OK) rc = set_precision(e->c, e->g, grids[0].precision);
   if (rc != PG_OK) {
+    free_ctx(e->c);
     delete e;
     return rc;
   }
@@ -602,9 +810,8 @@ int64_t pg_ens_points(const pg_ensemble* e, int64_t* offsets) {
 }
 
 int pg_ens_set_precision(pg_ensemble* e, int precision) {
-  if (!e || (precision != PG_FP64 && precision != PG_FP32)) return PG_EINVAL;
-  e->c.precision = precision;
-  return PG_OK;
+  if (!e) return PG_EINVAL;
+  return set_precision(e->c, e->g, precision);
 }
 
 int pg_ens_spacing(const pg_ensemble* e, int member, double* patch_d, double* mesh_d) {
@@ -686,6 +893,56 @@ int pg_ens_diff(pg_ensemble* e, const double* bulk, const double* rho, double* o
 int pg_ens_reduce(pg_ensemble* e, int op, const double* in, double* out_field, double* out_member, void* stream) {
   if (!e || !in || (!out_field && !out_member) || op < 0 || op > 2) return PG_EINVAL;
   return launch_seg_reduce(op, in, e->c.moff, e->c.nmem, e->c.npts, e->c.partial, out_field, out_member, stream);
+}
+
+// ------------------------------------------------------------ learned LAD
+namespace {
+LadGrid lad_grid(const GridInfo& g) {
+  LadGrid lg;
+  for (int d = 0; d < 3; d++) {
+    lg.n[d] = g.n[d];
+    lg.per[d] = g.periodic[d];
+  }
+  lg.delta = std::min(std::min(g.dm[0], g.dm[1]), g.dm[2]);
+  return lg;
+}
+}  // namespace
+
+int pg_lad_closure(pg_handle* h, const pg_lad_model* m, const double* div, const double* gmag, const double* rho,
+                   const double* dt, double cv, double* beta, double* kappa, int* flag, void* stream) {
+  if (!h || !m || !m->wbf16 || !m->params || !m->xmean || !m->xinvstd || !div || !gmag || !rho || !dt || !beta ||
+      !kappa || !flag)
+    return PG_EINVAL;
+  LadInferArgs a{*m, lad_grid(h->g), div, gmag, rho, dt, cv, beta, kappa, flag};
+  return launch_lad_infer(a, stream);
+}
+
+int pg_lad_features(pg_handle* h, const double* div, const double* gmag, const int64_t* pts, int64_t ns,
+                    float* raw, void* stream) {
+  if (!h || !div || !gmag || !pts || !raw || ns < 0) return PG_EINVAL;
+  if (ns == 0) return PG_OK;
+  return launch_lad_features(div, gmag, lad_grid(h->g), pts, ns, raw, stream);
+}
+
+int pg_lad_normalize(const float* raw, int64_t ns, const float* xmean, const float* xinvstd, void* X,
+                     void* stream) {
+  if (!raw || !xmean || !xinvstd || !X || ns < 0) return PG_EINVAL;
+  if (ns == 0) return PG_OK;
+  return launch_lad_normalize(raw, ns, xmean, xinvstd, X, stream);
+}
+
+int pg_lad_train_step(const pg_lad_model* m, const void* X, const float* T, int64_t rows, float inv_count,
+                      float* grad, float* loss, float* Y, void* stream) {
+  if (!m || !m->wbf16 || !m->params || !X || !T || !grad || rows < 0) return PG_EINVAL;
+  LadTrainArgs a{*m, X, T, rows, inv_count, grad, loss, Y};
+  return launch_lad_train(a, stream);
+}
+
+int pg_lad_adam(float* params, float* m, float* v, const float* grad, int n, float lr, float beta1, float beta2,
+                float eps, int step, void* pbf, int nbf, void* stream) {
+  if (!params || !m || !v || !grad || n <= 0 || step < 1 || nbf < 0 || nbf > n || (nbf > 0 && !pbf))
+    return PG_EINVAL;
+  return launch_lad_adam(params, m, v, grad, n, lr, beta1, beta2, eps, step, pbf, nbf, stream);
 }
 
 int pg_ens_device_status(pg_ensemble* e, int* status) {

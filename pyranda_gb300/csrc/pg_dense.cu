@@ -1,0 +1,495 @@
+// Dense compact operators on the tensor cores (tcgen05, split TF32).
+//
+// For a line of n <= 1024 points every compact operator of this library is a
+// fixed linear map out = D v with D = A^-1 B (the reference builds the same
+// matrix as `sm` in compact_basetype.f90:199-205).  Applying D to all lines
+// of a field is a GEMM:
+//   x lines (contiguous):     OUT[lines, pos] = V[lines, k] . D^T[k, pos]
+//   y / z lines (strided):    OUT[pos, lines] = D[pos, k]   . V^T[k, lines]
+// Both run here as tcgen05.mma kind::tf32 with FP32 accumulators in tensor
+// memory.  TF32 keeps 11 significant bits, so D and v are each split into
+// hi + lo TF32 parts and the product is hi.hi + hi.lo + lo.hi (three MMAs per
+// K step; the dropped lo.lo term is ~2^-22 relative).  D is split once on the
+// host into hi/lo planes already in the shared-memory layout the MMA reads
+// (K-major, 128-byte swizzle) and copied per K chunk with cp.async.bulk; the
+// FP64 field is converted and split while it is staged.  The epilogue goes
+// through shared memory so that global stores are coalesced, and applies the
+// same fused epilogues as the banded sweeps (store / accumulate / ring, with
+// the filters' FP64 add-back of v).
+//
+// One CTA computes one output tile: 128 lines x up to 256 positions (x), or
+// 128 positions x up to 256 lines (y, z), over the full K = n in chunks of 32,
+// double buffered.  Every wait is bounded; on a time-out the kernel records
+// PG_ETIMEOUT in the status word, stops issuing work and still frees its
+// tensor memory.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "pg_internal.h"
+#include "pg_sweep.cuh"
+
+namespace pg {
+namespace {
+
+constexpr int kDenseThreads = 256;
+constexpr int kKC = 32;               // K elements per chunk: one 128-byte row of TF32
+constexpr int kStageBytes = 98304;    // V hi/lo + D hi/lo of one chunk
+constexpr int kStages = 2;
+constexpr int kSmemBytes = kStages * kStageBytes + 1024;  // + alignment slack
+constexpr int kTmemCols = 256;
+constexpr unsigned long long kWaitNs = 2000000000ull;     // 2 s bound on any wait
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+// Bounded wait for the phase with the given parity; false on time-out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+  const uint32_t a = smem_u32(bar);
+  unsigned long long t0 = 0;
+  for (unsigned it = 0;; it++) {
+    unsigned done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.b32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((it & 1023u) == 0) {
+      const unsigned long long t = globaltimer();
+      if (it == 0) t0 = t;
+      else if (t - t0 > kWaitNs) return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void bulk_copy(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (start and offsets in 16-byte units).
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// Instruction descriptor of kind::tf32: FP32 accumulator, TF32 A and B, both
+// K-major, M = 128, N = n (multiple of 16, <= 256).
+__device__ __forceinline__ uint32_t idesc_tf32(int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, int acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* r) {
+  uint32_t u[8];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 8; i++) r[i] = __uint_as_float(u[i]);
+}
+
+// FP64 -> FP32 value + FP32 residual, without the FP64 pipe: hi is d2f_bits(d)
+// and r = d - hi is read from the 29 mantissa bits hi dropped (minus 2^29 when
+// hi rounded up), scaled by the exponent.  hi + r carries ~48 bits of d;
+// residuals of |d| < 2^-76 flush to zero.
+__device__ __forceinline__ float2 split_f64(double d) {
+  const unsigned dh = (unsigned)__double2hiint(d), dl = (unsigned)__double2loint(d);
+  const int e = (int)((dh >> 20) & 0x7ffu);
+  const int low = (int)((dl & 0x1FFFFFFFu) - (((dl >> 28) & 1u) << 29));
+  float r = (float)low * __uint_as_float((unsigned)max(e - 948, 0) << 23);
+  r = (e >= 948) ? r : 0.0f;
+  r = (dh >> 31) ? -r : r;
+  return make_float2(d2f_bits(d), r);
+}
+
+// TF32 of an FP32 value: round the low 13 mantissa bits to nearest (ties away).
+__device__ __forceinline__ uint32_t tf32_bits(float x) {
+  return (__float_as_uint(x) + 0x1000u) & 0xFFFFE000u;
+}
+
+// byte offset of 16-byte chunk q of row r in a K-major 128B-swizzled tile
+__device__ __forceinline__ uint32_t swz(int r, int q) {
+  return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((q ^ (r & 7)) << 4));
+}
+
+__device__ __forceinline__ int64_t line_base(const DenseOp& op, int dir, int64_t l) {
+  if (dir == 0) return op.off + l * op.nx;
+  if (dir == 1) return op.off + (l / op.nx) * (int64_t)op.nx * op.ny + (l % op.nx);
+  return op.off + l;
+}
+
+struct DParams {
+  const double* in;
+  double* out;
+  const DenseOp* ops;
+  const DenseTile* tiles;
+  int* status;
+  int scale_pow;
+};
+
+// ORIENT 0: lines are the MMA's M (x direction); 1: lines are its N (y, z).
+template <int ORIENT, int DIR, int EPI, bool ADDBACK>
+__global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P) {
+  extern __shared__ uint8_t dsm_raw[];
+  __shared__ __align__(8) uint64_t full_bar[kStages];
+  __shared__ __align__(8) uint64_t mma_bar[kStages];
+  __shared__ uint32_t tmem_slot;
+  __shared__ int s_bad;
+  __shared__ float2 s_ref[256];  // per line: its first value split as (hi, residual)
+  uint8_t* smem = dsm_raw + ((1024u - (smem_u32(dsm_raw) & 1023u)) & 1023u);
+
+  const DenseTile tile = P.tiles[blockIdx.x];
+  const DenseOp op = P.ops[tile.op];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int n = op.n;
+  const int st = (DIR == 0) ? 1 : (DIR == 1 ? op.nx : op.nx * op.ny);
+
+  // tile geometry: V rows are lines, D rows are output positions
+  int drow0, drows, vrows, N;
+  if (ORIENT == 0) {
+    drow0 = tile.part * 256;
+    drows = min(256, ((n + 15) & ~15) - drow0);
+    vrows = 128;
+    N = drows;
+  } else {
+    drow0 = tile.part * 128;
+    drows = 128;
+    vrows = (tile.nlines + 15) & ~15;
+    N = vrows;
+  }
+  const uint32_t vbytes = (ORIENT == 0) ? 16384u : 32768u;  // one V plane of a stage
+  const uint32_t dbytes = (ORIENT == 0) ? 32768u : 16384u;  // one D plane of a stage
+  const uint32_t dcopy = (uint32_t)drows * 128u;             // bytes of the D rows this tile reads
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < kStages; s++) {
+      mbar_init(&full_bar[s], 1);
+      mbar_init(&mma_bar[s], 1);
+    }
+    s_bad = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // Every operator here annihilates constants (D 1 = 0), so D v = D (v - c)
+  // for any per-line constant c; subtracting the line's first value before
+  // the split keeps the FP32 accumulation free of the lines' mean level.
+  {
+    const int nlv = (ORIENT == 0) ? 128 : 256;
+    if (tid < nlv) {
+      const bool ok = tid < tile.nlines;
+      s_ref[tid] = ok ? split_f64(__ldg(P.in + line_base(op, DIR, tile.line0 + tid))) : make_float2(0.f, 0.f);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const uint32_t idesc = idesc_tf32(N);
+  const int kchunks = op.kchunks;
+  bool bad = false;
+  int issued = -1, committed = -1;  // thread 0: last chunk whose D copy / MMAs were issued
+
+  for (int c = 0; c < kchunks && !bad; c++) {
+    const int s = c & 1;
+    uint8_t* st_base = smem + s * kStageBytes;
+    uint8_t* v_hi = st_base;
+    uint8_t* v_lo = st_base + vbytes;
+    uint8_t* d_hi = st_base + 2 * vbytes;
+    uint8_t* d_lo = d_hi + dbytes;
+    // the MMAs that last read this stage (chunk c - 2) must be complete
+    if (c >= 2 && !mbar_wait(&mma_bar[s], ((c >> 1) + 1) & 1)) bad = true;
+    if (__syncthreads_or(bad)) break;
+    if (tid == 0) {
+      const uint32_t* plane = op.dsw + (size_t)c * 2 * op.rows * 32;
+      mbar_expect_tx(&full_bar[s], 2 * dcopy);
+      bulk_copy(d_hi, plane + (size_t)drow0 * 32, dcopy, &full_bar[s]);
+      bulk_copy(d_lo, plane + (size_t)op.rows * 32 + (size_t)drow0 * 32, dcopy, &full_bar[s]);
+      issued = c;
+    }
+    // stage V: 16-byte chunks of 4 consecutive k, split into TF32 hi / lo
+    const int k0 = c * kKC;
+    if (ORIENT == 0) {
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        const int idx = tid + kDenseThreads * i;
+        const int r = idx >> 3, q = idx & 7;
+        const bool ok = r < tile.nlines;
+        const double* p = P.in + (ok ? line_base(op, DIR, tile.line0 + r) : 0);
+        const float2 c = s_ref[r];
+        uint32_t h[4], l[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const int k = k0 + q * 4 + j;
+          float f = 0.0f;
+          if (ok && k < n) {
+            const float2 v = split_f64(__ldg(p + k));
+            f = (v.x - c.x) + (v.y - c.y);
+          }
+          h[j] = tf32_bits(f);
+          l[j] = tf32_bits(f - __uint_as_float(h[j]));
+        }
+        *reinterpret_cast<uint4*>(v_hi + swz(r, q)) = make_uint4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<uint4*>(v_lo + swz(r, q)) = make_uint4(l[0], l[1], l[2], l[3]);
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        const int idx = tid + kDenseThreads * i;
+        const int r = idx & 255, q = idx >> 8;
+        if (r < vrows) {
+          const bool ok = r < tile.nlines;
+          const double* p = P.in + (ok ? line_base(op, DIR, tile.line0 + r) : 0);
+          const float2 c = s_ref[r];
+          uint32_t h[4], l[4];
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            const int k = k0 + q * 4 + j;
+            float f = 0.0f;
+            if (ok && k < n) {
+              const float2 v = split_f64(__ldg(p + (int64_t)k * st));
+              f = (v.x - c.x) + (v.y - c.y);
+            }
+            h[j] = tf32_bits(f);
+            l[j] = tf32_bits(f - __uint_as_float(h[j]));
+          }
+          *reinterpret_cast<uint4*>(v_hi + swz(r, q)) = make_uint4(h[0], h[1], h[2], h[3]);
+          *reinterpret_cast<uint4*>(v_lo + swz(r, q)) = make_uint4(l[0], l[1], l[2], l[3]);
+        }
+      }
+    }
+    fence_proxy_async();
+    __syncthreads();
+    if (tid == 0) {
+      if (!mbar_wait(&full_bar[s], (c >> 1) & 1)) {
+        s_bad = 1;
+      } else {
+        tc_fence_after();
+        const uint32_t a_hi = smem_u32(ORIENT == 0 ? v_hi : d_hi), a_lo = smem_u32(ORIENT == 0 ? v_lo : d_lo);
+        const uint32_t b_hi = smem_u32(ORIENT == 0 ? d_hi : v_hi), b_lo = smem_u32(ORIENT == 0 ? d_lo : v_lo);
+#pragma unroll
+        for (int kk = 0; kk < kKC / 8; kk++) {
+          const uint32_t o = kk * 32;  // 8 TF32 = 32 bytes along K
+          mma_tf32(tmem, sdesc(a_hi + o), sdesc(b_lo + o), idesc, (c > 0 || kk > 0) ? 1 : 0);
+          mma_tf32(tmem, sdesc(a_lo + o), sdesc(b_hi + o), idesc, 1);
+          mma_tf32(tmem, sdesc(a_hi + o), sdesc(b_hi + o), idesc, 1);
+        }
+        mma_commit(&mma_bar[s]);
+        committed = c;
+      }
+    }
+    __syncthreads();
+    bad = s_bad != 0;
+  }
+  // all MMAs complete (the last commit covers every earlier one)
+  if (!bad) {
+    const int cl = kchunks - 1;
+    if (!mbar_wait(&mma_bar[cl & 1], (cl >> 1) & 1)) bad = true;
+  }
+  tc_fence_after();
+  if (__syncthreads_or(bad)) {
+    if (tid == 0) {
+      atomicExch(P.status, (int)PG_ETIMEOUT);
+      // let this CTA's own copies and MMAs in flight finish (bounded) before
+      // its shared and tensor memory go away
+      if (issued > committed) mbar_wait(&full_bar[issued & 1], (issued >> 1) & 1);
+      if (committed >= 0) mbar_wait(&mma_bar[committed & 1], (committed >> 1) & 1);
+      tc_fence_after();
+    }
+    __syncthreads();
+  } else {
+    // tensor memory -> shared tile T[row][col] (row = TMEM lane), padded rows
+    float* T = reinterpret_cast<float*>(smem);
+    const int ld = N + 1;
+    const int q = warp & 3, h = warp >> 2;
+    const int row = q * 32 + lane;
+    for (int col = h * (N >> 1); col < (h + 1) * (N >> 1); col += 8) {
+      float r[8];
+      tmem_ld8(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)col, r);
+#pragma unroll
+      for (int i = 0; i < 8; i++) T[row * ld + col + i] = r[i];
+    }
+    __syncthreads();
+    const double sc = (P.scale_pow == 2) ? op.dm * op.dm : (P.scale_pow == 1 ? op.dm : 1.0);
+    constexpr bool kReadOut = (EPI == EPI_ADD || EPI == EPI_RING_MAX);
+    if (ORIENT == 0) {
+      const int nl = tile.nlines, npos = min(N, n - drow0);
+      for (int idx = tid; idx < nl * N; idx += kDenseThreads) {
+        const int r = idx / N, col = idx - r * N;
+        if (col < npos) {
+          const int64_t a = line_base(op, DIR, tile.line0 + r) + drow0 + col;
+          const double vin = ADDBACK ? P.in[a] : 0.0;
+          const double o = kReadOut ? P.out[a] : 0.0;
+          P.out[a] = epilogue<EPI>(f2d_bits(T[r * ld + col]), vin, o, sc, ADDBACK);
+        }
+      }
+    } else {
+      const int nl = tile.nlines, npos = min(128, n - drow0);
+      for (int idx = tid; idx < npos * N; idx += kDenseThreads) {
+        const int r = idx / N, col = idx - r * N;
+        if (col < nl) {
+          const int64_t a = line_base(op, DIR, tile.line0 + col) + (int64_t)(drow0 + r) * st;
+          const double vin = ADDBACK ? P.in[a] : 0.0;
+          const double o = kReadOut ? P.out[a] : 0.0;
+          P.out[a] = epilogue<EPI>(f2d_bits(T[r * ld + col]), vin, o, sc, ADDBACK);
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+  }
+}
+
+template <int ORIENT, int DIR, int EPI, bool ADDBACK>
+int launch_one(const DParams& p, int ntiles, cudaStream_t st) {
+  static bool attr = false;
+  auto k = dense_kernel<ORIENT, DIR, EPI, ADDBACK>;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    if (e != cudaSuccess) {
+      set_error("dense sweep: %s", cudaGetErrorString(e));
+      return PG_ECUDA;
+    }
+    attr = true;
+  }
+  k<<<ntiles, kDenseThreads, kSmemBytes, st>>>(p);
+  count_launch();
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error("dense sweep: %s", cudaGetErrorString(e));
+    return PG_ECUDA;
+  }
+  return PG_OK;
+}
+
+template <int ORIENT, int DIR>
+int launch_epi(const DParams& p, int ntiles, int epi, bool addback, cudaStream_t st) {
+  if (addback) {
+    if (epi != EPI_STORE) {
+      set_error("dense sweep: add-back operators only store");
+      return PG_EINVAL;
+    }
+    return launch_one<ORIENT, DIR, EPI_STORE, true>(p, ntiles, st);
+  }
+  switch (epi) {
+    case EPI_STORE: return launch_one<ORIENT, DIR, EPI_STORE, false>(p, ntiles, st);
+    case EPI_ADD: return launch_one<ORIENT, DIR, EPI_ADD, false>(p, ntiles, st);
+    case EPI_RING_SET: return launch_one<ORIENT, DIR, EPI_RING_SET, false>(p, ntiles, st);
+    default: return launch_one<ORIENT, DIR, EPI_RING_MAX, false>(p, ntiles, st);
+  }
+}
+
+}  // namespace
+
+int launch_dense(const DenseSet& ds, const double* in, double* out, int dir, int epi, int scale_pow, int* status,
+                 void* stream) {
+  if (ds.ntiles == 0) return PG_OK;
+  DParams p{in, out, ds.ops, ds.tiles, status, scale_pow};
+  cudaStream_t st = (cudaStream_t)stream;
+  if (dir == 0) return launch_epi<0, 0>(p, ds.ntiles, epi, ds.addback, st);
+  if (dir == 1) return launch_epi<1, 1>(p, ds.ntiles, epi, ds.addback, st);
+  return launch_epi<1, 2>(p, ds.ntiles, epi, ds.addback, st);
+}
+
+// ---------------------------------------------------------------------------
+// Host side: D from the banded operator, split into the swizzled TF32 planes.
+// ---------------------------------------------------------------------------
+namespace {
+
+uint32_t host_tf32(float x) {
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+  return (u + 0x1000u) & 0xFFFFE000u;
+}
+
+float host_f(uint32_t u) {
+  float x;
+  std::memcpy(&x, &u, 4);
+  return x;
+}
+
+}  // namespace
+
+// D (row-major n x n, FP64) -> [kchunk][hi, lo][rows][32] TF32 words, rows
+// padded to a multiple of 128 with zeros, each 8-row group 128B-swizzled.
+void split_dense(const std::vector<double>& D, int n, std::vector<uint32_t>& out, int& rows, int& kchunks) {
+  rows = (n + 127) / 128 * 128;
+  kchunks = (n + kKC - 1) / kKC;
+  out.assign((size_t)kchunks * 2 * rows * kKC, 0u);
+  for (int c = 0; c < kchunks; c++)
+    for (int r = 0; r < n; r++)
+      for (int k = 0; k < kKC; k++) {
+        const int col = c * kKC + k;
+        if (col >= n) continue;
+        const double v = D[(size_t)r * n + col];
+        const uint32_t hb = host_tf32((float)v);
+        const uint32_t lb = host_tf32((float)(v - (double)host_f(hb)));
+        const int q = (k >> 2) ^ (r & 7);
+        const size_t w = (size_t)r * kKC + q * 4 + (k & 3);
+        out[((size_t)c * 2 + 0) * rows * kKC + w] = hb;
+        out[((size_t)c * 2 + 1) * rows * kKC + w] = lb;
+      }
+}
+
+}  // namespace pg

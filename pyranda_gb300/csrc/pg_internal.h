@@ -67,6 +67,41 @@ struct SweepLaunch {
 
 // Launches one directional sweep over every member.  Returns a pg_status.
 int launch_sweep(int precision, const SweepLaunch& s, void* stream);
+
+// Dense operator of one member along one direction (device memory): D split
+// into TF32 hi/lo planes laid out as [kchunk][hi, lo][rows][32] words, each
+// 8-row group 128B-swizzled (the shared-memory layout the MMA reads).
+struct DenseOp {
+  const uint32_t* dsw;
+  long long off;    // first point of the member in the flat field
+  int n;            // points per line
+  int nx, ny;       // member extents (to decode a line index)
+  int kchunks;      // ceil(n / 32)
+  int rows;         // rows of each plane: n padded to a multiple of 128
+  int pad;
+  double dm;        // mesh spacing along the direction (ring scale)
+};
+// One CTA's output tile: lines [line0, line0 + nlines) of member `op`;
+// part = which 256 positions (x) or 128 positions (y, z) of the line.
+struct DenseTile {
+  int op;
+  int line0;
+  int nlines;
+  int part;
+};
+// Host view of the dense form of one (kind, direction) operator.
+struct DenseSet {
+  const DenseOp* ops = nullptr;
+  const DenseTile* tiles = nullptr;
+  int ntiles = 0;
+  bool ok = false;       // dense form built (every member has 16 <= n <= 1024)
+  bool addback = false;  // filters: out = v + D v with D = A^-1 (B - A)
+};
+// Split a row-major n x n FP64 matrix into the DenseOp plane layout.
+void split_dense(const std::vector<double>& D, int n, std::vector<uint32_t>& out, int& rows, int& kchunks);
+// One dense sweep (tcgen05 split-TF32 GEMM) with a fused epilogue.
+int launch_dense(const DenseSet& ds, const double* in, double* out, int dir, int epi, int scale_pow, int* status,
+                 void* stream);
 int launch_fill(double* out, double value, int64_t n, void* stream);
 int launch_copy(double* out, const double* in, int64_t n, void* stream);
 // dt_is_field = 0: dt is one device scalar; 1: dt is a field (one value per point)
@@ -99,6 +134,38 @@ int launch_seg_courant(const double* u, const double* v, const double* w, const 
                        double* partial, double* out_field, void* stream);
 int launch_seg_diff(const double* bulk, const double* rho, const double* mconst, const long long* moff, int nmem,
                     int64_t npts, double* partial, double* out_field, void* stream);
+
+// Learned LAD closure (pg_lad.cu).
+struct LadGrid {
+  int n[3];
+  int per[3];
+  double delta;  // GridLen
+};
+struct LadInferArgs {
+  pg_lad_model model;
+  LadGrid grid;
+  const double *div, *gmag, *rho, *dt;
+  double cv;
+  double *beta, *kappa;
+  int* flag;
+};
+struct LadTrainArgs {
+  pg_lad_model model;
+  const void* X;     // BF16 [rows][PG_LAD_K]
+  const float* T;    // [rows][PG_LAD_OUT]
+  long long rows;
+  float inv_count;
+  float* grad;       // parameter layout
+  float* loss;
+  float* Y;
+};
+int launch_lad_infer(const LadInferArgs& a, void* stream);
+int launch_lad_features(const double* div, const double* gmag, const LadGrid& g, const int64_t* pts, int64_t ns,
+                        float* raw, void* stream);
+int launch_lad_normalize(const float* raw, int64_t ns, const float* xm, const float* xs, void* X, void* stream);
+int launch_lad_train(const LadTrainArgs& a, void* stream);
+int launch_lad_adam(float* p, float* m, float* v, const float* g, int n, float lr, float b1, float b2, float eps,
+                    int step, void* pbf, int nbf, void* stream);
 
 void set_error(const char* fmt, ...);
 void count_launch(uint64_t k = 1);

@@ -52,7 +52,7 @@ class EnsembleGrid:
                 arr[i].periodic[d] = 1 if periodic[d] else 0
                 arr[i].x1[d] = float(x1[d])
                 arr[i].xn[d] = float(xn[d])
-            arr[i].precision = _lib.PG_FP32 if precision == "fp32" else _lib.PG_FP64
+            arr[i].precision = _lib.precision_code(precision)
         self.periodic = tuple(bool(p) for p in members[0][1])
         self.precision = precision
         h = ctypes.c_void_p()
@@ -89,7 +89,7 @@ class EnsembleGrid:
 
     def set_precision(self, precision):
         self.precision = precision
-        _lib.check(self.lib.pg_ens_set_precision(self.h, _lib.PG_FP32 if precision == "fp32" else _lib.PG_FP64),
+        _lib.check(self.lib.pg_ens_set_precision(self.h, _lib.precision_code(precision)),
                    "pg_ens_set_precision")
 
     # ------------------------------------------------------------------ fields
@@ -161,6 +161,17 @@ class EnsembleGrid:
                 idx.append(numpy.sort(flat.ravel()) + self.offsets[m])
             self._planes[key] = torch.as_tensor(numpy.concatenate(idx), dtype=torch.int64, device=self.device)
         return self._planes[key]
+
+    def get_plane(self, a, axis, k):
+        return a.index_select(0, self.plane(axis, k))
+
+    def set_plane(self, a, axis, k, value):
+        """Plane k of every member := value (a number or get_plane's layout); graph-safe."""
+        idx = self.plane(axis, k)
+        if isinstance(value, torch.Tensor) and value.dim() > 0:
+            a.index_copy_(0, idx, value)
+        else:
+            a.index_fill_(0, idx, float(value))
 
     def _out(self, out):
         if out is None:
@@ -419,7 +430,8 @@ class pyrandaEnsemble(pyrandaSim):
         if isinstance(time, torch.Tensor):
             t.copy_(time.expand(self.M))
         else:
-            t.copy_(torch.as_tensor(numpy.broadcast_to(numpy.asarray(time, dtype=numpy.float64), (self.M,))))
+            t.copy_(torch.from_numpy(numpy.array(numpy.broadcast_to(numpy.asarray(time, dtype=numpy.float64),
+                                                                    (self.M,)))))
         return t
 
     def _time_buffer(self):

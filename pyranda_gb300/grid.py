@@ -43,7 +43,7 @@ class Grid:
             g.x1[d] = float(x1[d])
             g.xn[d] = float(xn[d])
         self.precision = precision
-        g.precision = _lib.PG_FP32 if precision == "fp32" else _lib.PG_FP64
+        g.precision = _lib.precision_code(precision)
         h = ctypes.c_void_p()
         with torch.cuda.device(self.device):
             _lib.check(self.lib.pg_create(ctypes.byref(g), ctypes.byref(h)), "pg_create")
@@ -66,7 +66,7 @@ class Grid:
 
     def set_precision(self, precision):
         self.precision = precision
-        _lib.check(self.lib.pg_set_precision(self.h, _lib.PG_FP32 if precision == "fp32" else _lib.PG_FP64),
+        _lib.check(self.lib.pg_set_precision(self.h, _lib.precision_code(precision)),
                    "pg_set_precision")
 
     # ------------------------------------------------------------------ fields
@@ -226,6 +226,13 @@ class Grid:
         idx = [slice(None)] * 3
         idx[_DIRS[axis] if isinstance(axis, str) else int(axis)] = k
         return tuple(idx)
+
+    def get_plane(self, a, axis, k):
+        return a[self.plane(axis, k)]
+
+    def set_plane(self, a, axis, k, value):
+        """a[plane] = value (a number or a plane of values); no host copies, so it records in a CUDA graph."""
+        a[self.plane(axis, k)] = value
 
     def rk_stage(self, U, PHI, F, dt, A, B):
         n = len(U)

@@ -135,10 +135,19 @@ def build_advection3d(Sim, npts, **kw):
 # rest with rho = 1, p = 1, gamma = 1.4.
 GAMMA = 1.4
 MACH = 1.5
-P_RATIO = 1.0 + 2.0 * GAMMA / (GAMMA + 1.0) * (MACH ** 2 - 1.0)
-RHO_RATIO = (GAMMA + 1.0) * MACH ** 2 / ((GAMMA - 1.0) * MACH ** 2 + 2.0)
-SHOCK_SPEED = MACH * math.sqrt(GAMMA)
-U_POST = SHOCK_SPEED * (1.0 - 1.0 / RHO_RATIO)
+AMP = 0.05
+CV = 1.0 / (GAMMA - 1.0)   # gas constant R = 1
+
+
+def rankine_hugoniot(mach, gamma=GAMMA):
+    """Post-shock (pressure ratio, density ratio, velocity) for a shock of Mach `mach` into rho = p = 1 at rest."""
+    p_ratio = 1.0 + 2.0 * gamma / (gamma + 1.0) * (mach ** 2 - 1.0)
+    rho_ratio = (gamma + 1.0) * mach ** 2 / ((gamma - 1.0) * mach ** 2 + 2.0)
+    u_post = mach * math.sqrt(gamma) * (1.0 - 1.0 / rho_ratio)
+    return p_ratio, rho_ratio, u_post
+
+
+P_RATIO, RHO_RATIO, U_POST = rankine_hugoniot(MACH)
 
 SHOCK_EOM = """
 # Euler with LAD (the structure of examples/RM3D.py for one fluid)
@@ -146,7 +155,7 @@ ddt(:rho:)  =  -ddx(:rho:*:u:)            - ddy(:rho:*:v:)               - ddz(:
 ddt(:rhou:) =  -ddx(:rhou:*:u: - :tauxx:) - ddy(:rhou:*:v: - :tauxy:)    - ddz(:rhou:*:w: - :tauxz:)
 ddt(:rhov:) =  -ddx(:rhov:*:u: - :tauxy:) - ddy(:rhov:*:v: - :tauyy:)    - ddz(:rhov:*:w: - :tauyz:)
 ddt(:rhow:) =  -ddx(:rhow:*:u: - :tauxz:) - ddy(:rhow:*:v: - :tauyz:)    - ddz(:rhow:*:w: - :tauzz:)
-ddt(:Et:)   =  -ddx( (:Et: - :tauxx:)*:u: - :tauxy:*:v: - :tauxz:*:w: )  - ddy( (:Et: - :tauyy:)*:v: -:tauxy:*:u: - :tauyz:*:w:) - ddz( (:Et: - :tauzz:)*:w: - :tauxz:*:u: - :tauyz:*:v: )
+ddt(:Et:)   =  -ddx( (:Et: - :tauxx:)*:u: - :tauxy:*:v: - :tauxz:*:w: - :tx:*:kappa: )  - ddy( (:Et: - :tauyy:)*:v: -:tauxy:*:u: - :tauyz:*:w: - :ty:*:kappa: ) - ddz( (:Et: - :tauzz:)*:w: - :tauxz:*:u: - :tauyz:*:v: - :tz:*:kappa: )
 :rho:       =  fbar( :rho:  )
 :rhou:      =  fbar( :rhou: )
 :rhov:      =  fbar( :rhov: )
@@ -168,7 +177,9 @@ ddt(:Et:)   =  -ddx( (:Et: - :tauxx:)*:u: - :tauxy:*:v: - :tauxz:*:w: )  - ddy( 
 :wx:        =  ddx(:w:)
 :S:         = sqrt( :ux:*:ux: + :vy:*:vy: + :wz:*:wz: + .5*((:uy:+:vx:)**2 + (:uz: + :wx:)**2 + (:vz:+:wy:)**2) )
 :mu:        =  gbar( abs(ring(:S:  )) ) * :rho: * 1.0e-4
-:beta:      =  gbar( abs(ring(:div:)) * :rho: )  * 7.0e-2
+:T:         = :p: / :rho:
+[:tx:,:ty:,:tz:] = grad(:T:)
+LAD_CLOSURE
 :taudia:    =  (:beta:-2./3.*:mu:) *:div: - :p:
 :tauxx:     =  2.0*:mu:*:ux:   + :taudia:
 :tauyy:     =  2.0*:mu:*:vy:   + :taudia:
@@ -188,14 +199,20 @@ bc.const(['v','w'],['x1','xn'],0.0)
 :rhow: = :rho:*:w:
 """
 
-# Shock at x = 0.5, interface at x = 1.0 + 0.05 sin(2*2 pi y) sin(2*2 pi z),
+# The plain LAD closure of the bulk viscosity and conductivity (beta with the
+# coefficient of the shock problem, kappa in the form of examples/KH.py:94).
+PLAIN_LAD = """:beta:      =  gbar( abs(ring(:div:)) * :rho: )  * 7.0e-2
+:kappa:     =  gbar( ring(:T:)* :rho:*CV/(:T: * :dt: ) ) * 1.0e-3"""
+SHOCK_EOM = SHOCK_EOM.replace("LAD_CLOSURE", PLAIN_LAD.replace("CV", repr(CV)))
+
+# Shock at x = 0.5, interface at x = 1.0 + AMP sin(2*2 pi y) sin(2*2 pi z),
 # density 1 -> 3 across the interface (pressure equal), tanh profiles of
 # width 2 grid spacings.
 SHOCK_IC = """
 :gamma: = GAMMA
 delta = 2.0*DX
 xs = 0.5
-xi = 1.0 + 0.05*sin(4.0*pi*meshy)*sin(4.0*pi*meshz)
+xi = 1.0 + AMP*sin(4.0*pi*meshy)*sin(4.0*pi*meshz)
 hs = 0.5*(1.0 - tanh( (meshx - xs)/delta ))
 hi = 0.5*(1.0 + tanh( (meshx - xi)/delta ))
 :rho: = (1.0 + 2.0*hi)*(1.0 - hs) + RHOP*hs
@@ -221,12 +238,14 @@ def shock_mesh(nx, ny, nz, lx=4.0):
     ])
 
 
-def build_shock(Sim, nx, ny, nz, packages, lx=4.0, **kw):
+def build_shock(Sim, nx, ny, nz, packages, lx=4.0, mach=MACH, amp=AMP, eom=None, **kw):
+    """The shock-interface problem; `eom` replaces SHOCK_EOM (e.g. with a learned closure)."""
     ss = Sim("shock", shock_mesh(nx, ny, nz, lx), **kw)
     packages(ss)
-    ss.EOM(SHOCK_EOM)
-    ic = SHOCK_IC.replace("GAMMA", repr(GAMMA)).replace("DX", repr(lx / (nx - 1)))
-    ic = ic.replace("RHOP", repr(RHO_RATIO)).replace("UP", repr(U_POST)).replace("PP", repr(P_RATIO))
+    ss.EOM(SHOCK_EOM if eom is None else eom)
+    p_ratio, rho_ratio, u_post = rankine_hugoniot(mach)
+    ic = SHOCK_IC.replace("GAMMA", repr(GAMMA)).replace("DX", repr(lx / (nx - 1))).replace("AMP", repr(amp))
+    ic = ic.replace("RHOP", repr(rho_ratio)).replace("UP", repr(u_post)).replace("PP", repr(p_ratio))
     ss.setIC(ic)
     return ss
 

@@ -688,7 +688,7 @@ class pyrandaSim:
         stream.wait_stream(torch.cuda.current_stream())
         g = torch.cuda.CUDAGraph()
         with torch.cuda.stream(stream):
-            with torch.cuda.graph(g, stream=stream):
+            with torch.cuda.graph(g, stream=stream, capture_error_mode="thread_local"):
                 self._rk4_eager(self._g_t0, self._g_dt, dt_dev=self._g_dt)
                 # carry every rebound variable back into the storage the next
                 # replay reads

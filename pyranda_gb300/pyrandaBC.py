@@ -6,6 +6,7 @@ the processor-boundary tests of the reference are the non-periodic tests.
 """
 from .pyrandaPackage import pyrandaPackage
 
+
 class pyrandaBC(pyrandaPackage):
 
     def __init__(self, pysim):
@@ -21,8 +22,6 @@ class pyrandaBC(pyrandaPackage):
         p = self.pyranda.PyMPI
         return getattr(p, direction[0] + ("1proc" if direction[1] == "1" else "nproc"))
 
-    def _plane(self, direction, k):
-        return self.pyranda.grid.plane(direction[0], k)
 
     def extrap(self, var, direction, order=2):
         var = var if isinstance(var, list) else [var]
@@ -34,12 +33,14 @@ class pyrandaBC(pyrandaPackage):
     def extrapolate(self, var, direction, order):
         if not self._owns(direction):
             return
+        g = self.pyranda.grid
         a = self.pyranda.variables[var].data
+        ax = direction[0]
         t, s1, s2 = (0, 1, 2) if direction[1] == "1" else (-1, -2, -3)
         if order == 2:
-            a[self._plane(direction, t)] = 2 * a[self._plane(direction, s1)] - a[self._plane(direction, s2)]
+            g.set_plane(a, ax, t, 2 * g.get_plane(a, ax, s1) - g.get_plane(a, ax, s2))
         else:
-            a[self._plane(direction, t)] = a[self._plane(direction, s1)]
+            g.set_plane(a, ax, t, g.get_plane(a, ax, s1))
 
     def const(self, var, direction, val):
         var = var if isinstance(var, list) else [var]
@@ -52,4 +53,4 @@ class pyrandaBC(pyrandaPackage):
         if not self._owns(direction):
             return
         a = self.pyranda.variables[var].data
-        a[self._plane(direction, 0 if direction[1] == "1" else -1)] = val
+        self.pyranda.grid.set_plane(a, direction[0], 0 if direction[1] == "1" else -1, val)
