@@ -41,12 +41,21 @@ def parse():
     p.add_argument("--n", type=int, default=256, help="grid points per direction")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
-    p.add_argument("--mode", default="step", choices=["step", "sweeps", "profile", "peaks", "shock", "ensemble"],
+    p.add_argument("--no-fusion", action="store_true", help="fast paths without the fused EOM kernels")
+    p.add_argument("--mode", default="step", choices=["step", "sweeps", "profile", "peaks", "shock", "ensemble",
+                                                      "shock-learned", "kernels"],
                    help="sweeps: time every directional sweep kernel alone on one n^3 field; "
                         "profile: one eager RK step between cudaProfilerStart/Stop (for ncu); "
                         "peaks: HBM copy, FP64 and FP32 GEMM rates; "
                         "shock: throughput of the 512x128x128 shock-interface problem; "
-                        "ensemble: 64 Kelvin-Helmholtz 2-D runs of seeded sizes advanced together")
+                        "ensemble: 64 Kelvin-Helmholtz 2-D runs of seeded sizes advanced together; "
+                        "shock-learned: 512x128x128 shock-interface with the learned LAD closure against "
+                        "the plain one (trains the closure first when no trained model is found); "
+                        "kernels: d1 and compact-filter sweeps on one periodic n^3 field at --precision "
+                        "(a light target for profilers)")
+    p.add_argument("--model", default=None, help="shock-learned: trained closure (.npz); default: the packaged one")
+    p.add_argument("--train-runs", type=int, default=20, help="shock-learned: training runs when training")
+    p.add_argument("--train-iters", type=int, default=3000, help="shock-learned: Adam iterations when training")
     p.add_argument("--members", type=int, default=64, help="ensemble mode: number of members")
     p.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "dense", "fp32-only"],
                    help="profile mode: arithmetic of the profiled step; step mode: 'fp32-only' skips the dense run")
@@ -191,12 +200,14 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------------------ GPU
-def make_sim(n, precision, graphs):
+def make_sim(n, precision, graphs, fusion=False):
     from pyranda_gb300 import pyrandaSim, pyrandaTimestep, problems
     ss = problems.build_tgv(pyrandaSim, n, lambda s: s.addPackage(pyrandaTimestep(s)), silent=True,
                             precision=precision)
     if graphs:
         ss.use_graphs(True)
+    if fusion:
+        ss.use_fusion(True)
     return ss
 
 
@@ -280,13 +291,40 @@ def sweeps_only(args):
     torch.cuda.set_device(0)
     npts = args.n ** 3
     out = {"n": args.n}
-    for prec in ("fp32", "fp64"):
+    for prec in ("fp32", "dense", "fp64"):
         ss = make_sim(args.n, prec, graphs=False)
         sw = sweep_roofline(ss, torch, reps=args.reps)
         out[prec] = {k: {"ms": round(v * 1e3, 4), "GB/s": round(16.0 * npts / v / 1e9, 1)} for k, v in sw.items()}
         del ss
         torch.cuda.empty_cache()
     print(json.dumps(out), flush=True)
+    return 0
+
+
+def kernel_sweeps(args):
+    """d1 and compact-filter sweeps in x, y, z on one periodic n^3 field (two fields on the device)."""
+    import torch
+    from pyranda_gb300.grid import Grid
+    torch.cuda.set_device(0)
+    n = args.n
+    g = Grid((n, n, n), (True, True, True), (0, 0, 0), (2 * math.pi * (n - 1) / n,) * 3, precision=args.precision)
+    v = g.mesh(0)
+    v.copy_(torch.sin(v) + 2.0)
+    out = g.empty()
+    res = {}
+    for name, f in (("d1", lambda d: g.d1(d, v, out=out)), ("sfilter", lambda d: g.filter("spectral", v, d, out=out))):
+        for d in range(3):
+            f(d)
+            torch.cuda.synchronize()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            for _ in range(args.reps):
+                f(d)
+            e.record()
+            torch.cuda.synchronize()
+            ms = s.elapsed_time(e) / args.reps
+            res["%s_%s" % (name, "xyz"[d])] = {"ms": round(ms, 4), "GB/s": round(16.0 * n ** 3 / ms / 1e6, 1)}
+    print(json.dumps({"n": n, "precision": args.precision, "sweeps": res}), flush=True)
     return 0
 
 
@@ -458,6 +496,97 @@ def ensemble_throughput(args):
     return 0
 
 
+def shock_learned(args):
+    """C5: the learned LAD closure on the 512x128x128 shock-interface problem.
+
+    Both runs use the fast path (FP32 sweeps, FP64 state, one CUDA graph per
+    RK step) and the same dt sequence (the plain run's), so the density error
+    compares the closures alone.  Without a trained model the closure is
+    first trained here: 2000 snapshots of 20 seeded 128x64x64 runs (Mach in
+    [1.2, 3], amplitude in [0.01, 0.1], default_rng(1)), then Adam.
+    """
+    import torch
+    from pyranda_gb300 import pyrandaSim, pyrandaBC, pyrandaTimestep, problems
+    from pyranda_gb300 import learned_lad as LL
+    torch.cuda.set_device(0)
+    out = {"workload": "shock-interface 512x128x128 (Mach 1.5, amplitude 0.05), learned vs plain LAD closure",
+           "steps": args.steps}
+    path = args.model or LL.DEFAULT_MODEL
+    if os.path.exists(path):
+        model = LL.LadModel.load(path)
+        out["model"] = os.path.relpath(path, ROOT)
+    else:
+        t0 = time.time()
+        raw, T, meta = LL.shock_training_set(runs=args.train_runs, snapshots_per_run=2000 // args.train_runs)
+        t1 = time.time()
+        model = LL.LadModel("cuda", seed=0)
+        Tn = LL.fit_normalisation(model, raw, T)
+        X = LL.normalize(raw, model)
+        hist = LL.train(model, X, Tn, iters=args.train_iters, batch=8192, lr=1e-3, log_every=500)
+        torch.cuda.synchronize()
+        t2 = time.time()
+        os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
+        model.save(os.path.join(ROOT, "gpurun_out", "lad_shock.npz"))
+        out["training"] = {"samples": int(raw.shape[0]), "snapshots": sum(m[2] for m in meta),
+                           "runs": [[round(a, 4), round(b, 4), c] for a, b, c in meta],
+                           "data_s": round(t1 - t0, 1), "train_s": round(t2 - t1, 1), "loss": hist}
+        del raw, T, X, Tn
+    npts = 512 * 128 * 128
+    k, w = args.steps, max(3, args.warmup)
+
+    def build(mode):
+        def packs(ss):
+            ss.addPackage(pyrandaBC(ss))
+            ss.addPackage(pyrandaTimestep(ss))
+            ss.addPackage(LL.pyrandaLearnedLAD(ss, model, problems.CV, mode=mode))
+        ss = problems.build_shock(pyrandaSim, 512, 128, 128, packs, eom=LL.learned_shock_eom(), silent=True,
+                                  precision="fp32")
+        ss.use_graphs(True)
+        return ss
+
+    plain = build("plain")
+    dts = []
+    t = 0.0
+    for _ in range(w):
+        dts.append(plain.variables["dt"].data.clone())
+        t = plain.rk4(t, dts[-1])
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(k):
+        dts.append(plain.variables["dt"].data.clone())
+        t = plain.rk4(t, dts[-1])
+    e.record()
+    torch.cuda.synchronize()
+    t_plain = s.elapsed_time(e) / 1e3
+    rho_plain = plain.variables["rho"].data.clone()
+    del plain
+    torch.cuda.empty_cache()
+    learned = build("learned")
+    lad = learned.packages["LAD"]
+    t = 0.0
+    for i in range(w):
+        t = lad.step(t, dts[i])
+    torch.cuda.synchronize()
+    s.record()
+    for i in range(k):
+        t = lad.step(t, dts[w + i])
+    e.record()
+    torch.cuda.synchronize()
+    t_learn = s.elapsed_time(e) / 1e3
+    rho = learned.variables["rho"].data
+    l1 = float(((rho - rho_plain).abs().sum() / rho_plain.abs().sum()).item())
+    out["plain_lad"] = {"value": round(npts * k / t_plain / 1e6, 3), "unit": UNIT,
+                        "ms_per_step": round(t_plain / k * 1e3, 3)}
+    out["learned_lad"] = {"value": round(npts * k / t_learn / 1e6, 3), "unit": UNIT,
+                          "ms_per_step": round(t_learn / k * 1e3, 3), "fallback_steps": lad.fallbacks}
+    out["speedup"] = round(t_plain / t_learn, 3)
+    out["density_l1_vs_plain"] = l1
+    out["note"] = "learned-closure timing includes the per-step state snapshot and fallback-flag read"
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.mode == "peaks":
@@ -466,6 +595,10 @@ def main():
         return shock_throughput(args)
     if args.mode == "ensemble":
         return ensemble_throughput(args)
+    if args.mode == "shock-learned":
+        return shock_learned(args)
+    if args.mode == "kernels":
+        return kernel_sweeps(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.mode == "sweeps":
@@ -498,11 +631,13 @@ def main():
     # FP32 banded sweeps, and dense split-TF32 operators on the tensor cores
     fast_runs = {}
     for prec in (["fp32"] if args.precision == "fp32-only" else ["fp32", "dense"]):
-        sim = make_sim(n, prec, graphs=True)
+        sim = make_sim(n, prec, graphs=True, fusion=not args.no_fusion)
+        run_steps(sim, 1)             # eager step (records the fused kernels, then compiles them)
         c0 = _lib.launch_count()
-        run_steps(sim, 1)             # eager step (first graph-mode call)
-        lps = _lib.launch_count() - c0
-        run_steps(sim, w - 1)         # capture + replays
+        f0 = sim._fuse.fused_calls if sim._fuse is not None else 0
+        run_steps(sim, 1)             # records the step's graph (counts this library's and the fused launches)
+        lps = _lib.launch_count() - c0 + ((sim._fuse.fused_calls - f0) if sim._fuse is not None else 0)
+        run_steps(sim, w - 2)         # capture + replays
         clocks = ClockSampler(dev)
         clocks.start()
         t = time_steps(sim, k, torch, dist_on)

@@ -35,7 +35,7 @@
 namespace pg {
 namespace {
 
-constexpr int kDenseThreads = 256;
+constexpr int kDenseThreads = 512;  // 16 warps: latency hiding for the staging and the epilogue
 constexpr int kKC = 32;               // K elements per chunk: one 128-byte row of TF32
 constexpr int kStageBytes = 98304;    // V hi/lo + D hi/lo of one chunk
 constexpr int kStages = 2;
@@ -189,7 +189,8 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
   __shared__ __align__(8) uint64_t mma_bar[kStages];
   __shared__ uint32_t tmem_slot;
   __shared__ int s_bad;
-  __shared__ float2 s_ref[256];  // per line: its first value split as (hi, residual)
+  __shared__ float2 s_ref[256];     // per line: its first value split as (hi, residual)
+  __shared__ long long s_base[256];  // per line: offset of its first point
   uint8_t* smem = dsm_raw + ((1024u - (smem_u32(dsm_raw) & 1023u)) & 1023u);
 
   const DenseTile tile = P.tiles[blockIdx.x];
@@ -236,7 +237,9 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
     const int nlv = (ORIENT == 0) ? 128 : 256;
     if (tid < nlv) {
       const bool ok = tid < tile.nlines;
-      s_ref[tid] = ok ? split_f64(__ldg(P.in + line_base(op, DIR, tile.line0 + tid))) : make_float2(0.f, 0.f);
+      const long long b = ok ? line_base(op, DIR, tile.line0 + tid) : 0;
+      s_base[tid] = b;
+      s_ref[tid] = ok ? split_f64(__ldg(P.in + b)) : make_float2(0.f, 0.f);
     }
   }
   tc_fence_before();
@@ -269,11 +272,11 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
     const int k0 = c * kKC;
     if (ORIENT == 0) {
 #pragma unroll
-      for (int i = 0; i < 4; i++) {
+      for (int i = 0; i < 1024 / kDenseThreads; i++) {  // 128 rows x 8 chunks
         const int idx = tid + kDenseThreads * i;
         const int r = idx >> 3, q = idx & 7;
         const bool ok = r < tile.nlines;
-        const double* p = P.in + (ok ? line_base(op, DIR, tile.line0 + r) : 0);
+        const double* p = P.in + s_base[r];
         const float2 c = s_ref[r];
         uint32_t h[4], l[4];
 #pragma unroll
@@ -292,12 +295,12 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
       }
     } else {
 #pragma unroll
-      for (int i = 0; i < 8; i++) {
+      for (int i = 0; i < 2048 / kDenseThreads; i++) {  // 256 rows x 8 chunks
         const int idx = tid + kDenseThreads * i;
         const int r = idx & 255, q = idx >> 8;
         if (r < vrows) {
           const bool ok = r < tile.nlines;
-          const double* p = P.in + (ok ? line_base(op, DIR, tile.line0 + r) : 0);
+          const double* p = P.in + s_base[r];
           const float2 c = s_ref[r];
           uint32_t h[4], l[4];
 #pragma unroll
@@ -359,9 +362,10 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
     // tensor memory -> shared tile T[row][col] (row = TMEM lane), padded rows
     float* T = reinterpret_cast<float*>(smem);
     const int ld = N + 1;
+    // warp w reads TMEM lanes 32 (w % 4) ..; the warp groups w / 4 take turns over 8-column blocks
     const int q = warp & 3, h = warp >> 2;
     const int row = q * 32 + lane;
-    for (int col = h * (N >> 1); col < (h + 1) * (N >> 1); col += 8) {
+    for (int col = 8 * h; col < N; col += 8 * (kDenseThreads / 128)) {
       float r[8];
       tmem_ld8(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)col, r);
 #pragma unroll
@@ -375,7 +379,7 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
       for (int idx = tid; idx < nl * N; idx += kDenseThreads) {
         const int r = idx / N, col = idx - r * N;
         if (col < npos) {
-          const int64_t a = line_base(op, DIR, tile.line0 + r) + drow0 + col;
+          const int64_t a = s_base[r] + drow0 + col;
           const double vin = ADDBACK ? P.in[a] : 0.0;
           const double o = kReadOut ? P.out[a] : 0.0;
           P.out[a] = epilogue<EPI>(f2d_bits(T[r * ld + col]), vin, o, sc, ADDBACK);
@@ -386,7 +390,7 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
       for (int idx = tid; idx < npos * N; idx += kDenseThreads) {
         const int r = idx / N, col = idx - r * N;
         if (col < nl) {
-          const int64_t a = line_base(op, DIR, tile.line0 + col) + (int64_t)(drow0 + r) * st;
+          const int64_t a = s_base[col] + (int64_t)(drow0 + r) * st;
           const double vin = ADDBACK ? P.in[a] : 0.0;
           const double o = kReadOut ? P.out[a] : 0.0;
           P.out[a] = epilogue<EPI>(f2d_bits(T[r * ld + col]), vin, o, sc, ADDBACK);

@@ -24,7 +24,7 @@ import numpy
 import torch
 
 from . import _lib
-from .grid import _ptr, _stream
+from .grid import _ptr, _stream, flush_pending, release
 from .pyranda import defaultMeshOptions, pyrandaGPU, pyrandaSim, pyrandaVar
 
 _AX = {"x": 0, "y": 1, "z": 2}
@@ -38,6 +38,7 @@ class EnsembleGrid:
         if not torch.cuda.is_available():
             raise RuntimeError("pyranda_gb300 needs a CUDA device; there is no CPU fallback")
         self.lib = _lib.load()
+        flush_pending()
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.m = len(members)
         if self.m < 1:
@@ -82,7 +83,7 @@ class EnsembleGrid:
     def __del__(self):
         try:
             if getattr(self, "h", None):
-                self.lib.pg_ens_destroy(self.h)
+                release(self.lib, "pg_ens_destroy", self.h)
                 self.h = None
         except Exception:
             pass

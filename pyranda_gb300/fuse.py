@@ -1,0 +1,290 @@
+"""Fusion of the EOM's elementwise arithmetic into generated CUDA kernels.
+
+pyranda evaluates every EOM line as numpy expressions, one temporary array
+per operation (pyranda/pyrandaEq.py:16-48, pyranda.py:376-428).  Here each
+maximal elementwise subtree of an equation's right-hand side (arithmetic,
+constant powers and the numpy functions of the string language) becomes one
+CUDA kernel that reads each field once and writes its result once; the
+compact operators (ddx, fbar, ring, ...) and the reductions stay calls into
+the library and become the kernels' inputs.
+
+The kernels repeat torch's per-operation rounding: every product, quotient
+and sum is rounded separately (no FMA contraction), x**2 is x*x, x**0.5 is
+sqrt(x), x**-1 is 1/x (torch's pow special cases), and minimum/maximum
+propagate NaN, so a fused step reproduces the unfused one bit for bit.  All
+kernels of a simulation are generated into one source file, compiled once
+with nvcc for sm_103a and cached under pyranda_gb300/_build/jit by the
+source's hash.
+"""
+import ast
+import copy
+import ctypes
+import hashlib
+import os
+import subprocess
+
+import torch
+
+from .build import ARCH, OUT, nvcc
+
+JIT_DIR = os.path.join(OUT, "jit")
+
+_UNARY = {"sqrt": "sqrt({0})", "abs": "fabs({0})", "absolute": "fabs({0})", "exp": "exp({0})",
+          "log": "log({0})", "sin": "sin({0})", "cos": "cos({0})", "tan": "tan({0})", "tanh": "tanh({0})",
+          "sinh": "sinh({0})", "cosh": "cosh({0})", "arctan": "atan({0})", "arcsin": "asin({0})",
+          "arccos": "acos({0})", "log10": "log10({0})", "floor": "floor({0})", "ceil": "ceil({0})",
+          "sign": "pg_sign({0})"}
+_BINARY = {"minimum": "pg_min({0}, {1})", "maximum": "pg_max({0}, {1})"}
+_ARITH = {ast.Add: "__dadd_rn({0}, {1})", ast.Sub: "__dsub_rn({0}, {1})", ast.Mult: "__dmul_rn({0}, {1})",
+          ast.Div: "__ddiv_rn({0}, {1})"}
+
+PRELUDE = r"""#include <cstdint>
+#include <cmath>
+#include <cuda_runtime.h>
+__device__ __forceinline__ double pg_min(double a, double b) { return (a != a) ? a : ((b != b) ? b : (a < b ? a : b)); }
+__device__ __forceinline__ double pg_max(double a, double b) { return (a != a) ? a : ((b != b) ? b : (a > b ? a : b)); }
+__device__ __forceinline__ double pg_sign(double a) { return (a > 0.0) ? 1.0 : ((a < 0.0) ? -1.0 : a); }
+"""
+
+
+def _const(node):
+    if isinstance(node, ast.Constant) and isinstance(node.value, (int, float)) and not isinstance(node.value, bool):
+        return float(node.value)
+    if isinstance(node, ast.UnaryOp) and isinstance(node.op, ast.USub):
+        c = _const(node.operand)
+        return None if c is None else -c
+    return None
+
+
+def _is_numpy(f):
+    return isinstance(f, ast.Attribute) and isinstance(f.value, ast.Name) and f.value.id == "numpy"
+
+
+def _elementwise(node):
+    """True when the generator fuses this node (otherwise it is a leaf)."""
+    if isinstance(node, ast.BinOp):
+        return type(node.op) in _ARITH or (isinstance(node.op, ast.Pow))
+    if isinstance(node, ast.UnaryOp):
+        return isinstance(node.op, (ast.USub, ast.UAdd))
+    if isinstance(node, ast.Call) and _is_numpy(node.func) and not node.keywords:
+        return (node.func.attr in _UNARY and len(node.args) == 1) or (node.func.attr in _BINARY and len(node.args) == 2)
+    return False
+
+
+def _children(node):
+    if isinstance(node, ast.BinOp):
+        return [node.left, node.right]
+    if isinstance(node, ast.UnaryOp):
+        return [node.operand]
+    return list(node.args)
+
+
+def _ops(node):
+    return (1 + sum(_ops(k) for k in _children(node))) if _elementwise(node) else 0
+
+
+def _pow(x, c):
+    # torch's pow(tensor, scalar) special cases
+    if c == 2.0:
+        return "__dmul_rn(%s, %s)" % (x, x)
+    if c == 3.0:
+        return "__dmul_rn(__dmul_rn(%s, %s), %s)" % (x, x, x)
+    if c == 0.5:
+        return "sqrt(%s)" % x
+    if c == -0.5:
+        return "rsqrt(%s)" % x
+    if c == -1.0:
+        return "__ddiv_rn(1.0, %s)" % x
+    if c == -2.0:
+        return "__ddiv_rn(1.0, __dmul_rn(%s, %s))" % (x, x)
+    if c == 1.0:
+        return x
+    return "pow(%s, %r)" % (x, float(c))
+
+
+class _Gen:
+    """C expression and Python AST (leaves renamed L0..Ln) of one elementwise subtree."""
+
+    def __init__(self):
+        self.leaves = []
+
+    def emit(self, node):
+        c = _const(node)
+        if c is not None and not isinstance(node, ast.UnaryOp):
+            return "(%r)" % c, copy.copy(node)
+        if isinstance(node, ast.Attribute) and _is_numpy(node) and node.attr == "pi":
+            return "(%r)" % 3.141592653589793, copy.copy(node)
+        if _elementwise(node):
+            if isinstance(node, ast.UnaryOp):
+                cx, px = self.emit(node.operand)
+                return ("(-%s)" % cx if isinstance(node.op, ast.USub) else cx), ast.UnaryOp(op=node.op, operand=px)
+            if isinstance(node, ast.BinOp):
+                cl, pl = self.emit(node.left)
+                if isinstance(node.op, ast.Pow) and _const(node.right) is not None:
+                    return _pow(cl, _const(node.right)), ast.BinOp(left=pl, op=node.op, right=copy.copy(node.right))
+                cr, pr = self.emit(node.right)
+                fmt = _ARITH.get(type(node.op), "pow({0}, {1})")
+                return fmt.format(cl, cr), ast.BinOp(left=pl, op=node.op, right=pr)
+            args = [self.emit(a) for a in node.args]
+            fmt = _UNARY.get(node.func.attr) if len(args) == 1 else _BINARY[node.func.attr]
+            return fmt.format(*[a[0] for a in args]), ast.Call(func=copy.copy(node.func), args=[a[1] for a in args],
+                                                               keywords=[])
+        self.leaves.append(node)
+        name = "L%d" % (len(self.leaves) - 1)
+        return name, ast.Name(id=name, ctx=ast.Load())
+
+
+class Kernel:
+    """One fused subtree: C expression, Python form, leaf kinds and compiled launcher."""
+
+    def __init__(self, index, expr, pyform, nleaves, globals_):
+        self.index, self.expr, self.nleaves = index, expr, nleaves
+        lam = ast.Expression(body=ast.Lambda(
+            args=ast.arguments(posonlyargs=[], args=[ast.arg(arg="L%d" % i) for i in range(nleaves)],
+                               kwonlyargs=[], kw_defaults=[], defaults=[]), body=pyform))
+        ast.fix_missing_locations(lam)
+        self.eager = eval(compile(lam, "<fused %d>" % index, "eval"), globals_)
+        self.sig = None      # leaf kinds of the recording call: f field, s device scalar, c number
+        self.fn = None
+
+    def name(self):
+        return "pg_fused_%d" % self.index
+
+    def source(self):
+        args, defs, call = [], [], []
+        for i, k in enumerate(self.sig):
+            if k in "fs":
+                args.append("const double* __restrict__ p%d" % i)
+                defs.append("const double L%d = p%d[%s];" % (i, i, "i" if k == "f" else "0"))
+                call.append("p%d" % i)
+            else:
+                args.append("double L%d" % i)
+                call.append("L%d" % i)
+        params = ", ".join(["int64_t n", "double* __restrict__ out"] + args)
+        return ('extern "C" __global__ void %(k)s(%(p)s) {\n'
+                "  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;"
+                " i += (int64_t)gridDim.x * blockDim.x) {\n    %(d)s\n    out[i] = %(e)s;\n  }\n}\n"
+                'extern "C" int %(k)s_launch(%(p)s, void* stream) {\n'
+                "  if (n <= 0) return 0;\n"
+                "  int64_t b = (n + 255) / 256;\n  if (b > 152 * 16) b = 152 * 16;\n"
+                "  %(k)s<<<(unsigned)b, 256, 0, (cudaStream_t)stream>>>(n, out%(c)s);\n"
+                "  return (int)cudaGetLastError();\n}\n") % {
+                    "k": self.name(), "p": params, "d": " ".join(defs), "e": self.expr,
+                    "c": "".join(", " + c for c in call)}
+
+
+class Fuser:
+    """Rewrites a simulation's EOM right-hand sides to use fused kernels.
+
+    ``install(globals_)`` rewrites every equation; the first evaluation of
+    each fused subtree records its leaf kinds and runs unfused (torch);
+    ``build()`` compiles all recorded kernels in one nvcc call, after which
+    they run fused.  A call whose leaves do not match the recorded kinds, or
+    whose fields are not in the grid's layout, runs unfused.
+    """
+
+    def __init__(self, sim, min_ops=2):
+        self.sim = sim
+        self.min_ops = min_ops
+        self.kernels = []
+        self.lib = None
+        self.fused_calls = 0
+
+    def rewrite(self, src, globals_):
+        tree = ast.parse(src, mode="eval")
+        fuser = self
+
+        class T(ast.NodeTransformer):
+            def visit(self, node):
+                if _elementwise(node) and _ops(node) >= fuser.min_ops:
+                    g = _Gen()
+                    expr, pyform = g.emit(node)
+                    leaves = [self.visit(lf) for lf in g.leaves]
+                    k = Kernel(len(fuser.kernels), expr, pyform, len(leaves), globals_)
+                    fuser.kernels.append(k)
+                    call = ast.Call(func=ast.Attribute(value=ast.Attribute(value=ast.Name(id="self", ctx=ast.Load()),
+                                                                           attr="_fuse", ctx=ast.Load()),
+                                                       attr="run", ctx=ast.Load()),
+                                    args=[ast.Constant(k.index)] + leaves, keywords=[])
+                    return ast.copy_location(call, node)
+                return self.generic_visit(node)
+
+        body = T().visit(tree.body)
+        lam = ast.Expression(body=ast.Lambda(args=ast.arguments(posonlyargs=[], args=[ast.arg(arg="self")],
+                                                                kwonlyargs=[], kw_defaults=[], defaults=[]),
+                                             body=body))
+        ast.fix_missing_locations(lam)
+        return eval(compile(lam, "<fused equation>", "eval"), globals_)
+
+    def install(self, globals_):
+        for eq in self.sim.equations:
+            eq.RHS = self.rewrite(eq.sRHS, globals_)
+
+    def run(self, index, *leaves):
+        k = self.kernels[index]
+        g = self.sim.grid
+        kinds, args = [], []
+        for v in leaves:
+            if isinstance(v, torch.Tensor) and v.dim() > 0:
+                if not (v.dtype == torch.float64 and v.device == g.device and tuple(v.shape) == g.n
+                        and g._fortran_ok(v)):
+                    return k.eager(*leaves)
+                kinds.append("f")
+                args.append(ctypes.c_void_p(v.data_ptr()))
+            elif isinstance(v, torch.Tensor):
+                if v.dtype != torch.float64 or v.device != g.device:
+                    return k.eager(*leaves)
+                kinds.append("s")
+                args.append(ctypes.c_void_p(v.data_ptr()))
+            elif isinstance(v, (int, float)) and not isinstance(v, bool):
+                kinds.append("c")
+                args.append(ctypes.c_double(float(v)))
+            else:
+                return k.eager(*leaves)
+        sig = "".join(kinds)
+        if "f" not in sig:
+            return k.eager(*leaves)
+        if k.sig is None:
+            k.sig = sig
+        if k.fn is None or k.sig != sig:
+            return k.eager(*leaves)
+        out = g.empty()
+        rc = k.fn(ctypes.c_int64(g.npts), ctypes.c_void_p(out.data_ptr()), *args,
+                  ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        if rc != 0:
+            raise RuntimeError("fused kernel %s failed with CUDA error %d" % (k.name(), rc))
+        self.fused_calls += 1
+        return out
+
+    def source(self):
+        ks = [k for k in self.kernels if k.sig is not None]
+        # loads every kernel now: a first launch inside a graph capture would load its module there
+        pre = ('extern "C" int pg_fused_preload() {\n  cudaFuncAttributes a;\n  int rc = 0;\n%s  return rc;\n}\n'
+               % "".join("  rc |= (int)cudaFuncGetAttributes(&a, %s);\n" % k.name() for k in ks))
+        return PRELUDE + "".join(k.source() for k in ks) + pre
+
+    def build(self):
+        """Compile every recorded kernel (once per distinct source) and bind them; returns the .so path."""
+        src = self.source()
+        h = hashlib.sha1(src.encode()).hexdigest()[:16]
+        os.makedirs(JIT_DIR, exist_ok=True)
+        so = os.path.join(JIT_DIR, "fused_%s.so" % h)
+        if not os.path.exists(so):
+            cu = os.path.join(JIT_DIR, "fused_%s.cu" % h)
+            with open(cu, "w") as f:
+                f.write(src)
+            tmp = so + ".%d.tmp" % os.getpid()
+            cmd = [nvcc()] + ARCH + ["-O3", "-fmad=false", "-shared", "-Xcompiler", "-fPIC", "-o", tmp, cu]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError("nvcc failed on the fused EOM kernels:\n" + r.stderr[-3000:])
+            os.replace(tmp, so)
+        self.lib = ctypes.CDLL(so)
+        if self.lib.pg_fused_preload() != 0:
+            raise RuntimeError("loading the fused EOM kernels failed")
+        for k in self.kernels:
+            if k.sig is not None:
+                fn = getattr(self.lib, k.name() + "_launch")
+                fn.restype = ctypes.c_int
+                k.fn = fn
+        return so

@@ -24,6 +24,40 @@ def _ptr(t):
     return ctypes.c_void_p(t.data_ptr())
 
 
+# Handles whose owner was collected while a CUDA graph was being recorded.
+# Destroying a handle frees device memory, which is not allowed during stream
+# capture, and Python's cyclic collector can finalise an old grid at any
+# allocation -- also inside another simulation's capture.  Such handles wait
+# here until the next safe point (a new grid, or the end of a capture).
+_PENDING = []
+
+
+def _capturing():
+    try:
+        return torch.cuda.is_available() and torch.cuda.is_current_stream_capturing()
+    except Exception:
+        return True
+
+
+def release(lib, destroy, h):
+    """Destroy a handle now, or later when a capture is in progress."""
+    if _capturing():
+        _PENDING.append((destroy, h))
+        return
+    getattr(lib, destroy)(h)
+
+
+def flush_pending():
+    """Destroy the handles deferred during a capture (call outside captures)."""
+    if _capturing():
+        return
+    from . import _lib
+    lib = _lib.load()
+    while _PENDING:
+        destroy, h = _PENDING.pop()
+        getattr(lib, destroy)(h)
+
+
 class Grid:
     """A Cartesian pyranda patch on one GPU (parcop.f90:23-70 setup + setup_mesh)."""
 
@@ -31,6 +65,7 @@ class Grid:
         if not torch.cuda.is_available():
             raise RuntimeError("pyranda_gb300 needs a CUDA device; there is no CPU fallback")
         self.lib = _lib.load()
+        flush_pending()
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.n = tuple(int(v) for v in n)
         self.shape = self.n
@@ -59,7 +94,7 @@ class Grid:
     def __del__(self):
         try:
             if getattr(self, "h", None):
-                self.lib.pg_destroy(self.h)
+                release(self.lib, "pg_destroy", self.h)
                 self.h = None
         except Exception:
             pass

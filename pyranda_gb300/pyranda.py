@@ -14,7 +14,7 @@ import torch
 
 from . import pgmath
 from ._lib import PG_DIR_ALL
-from .grid import Grid
+from .grid import Grid, flush_pending
 from .pyrandaUtils import findVar, fortran3d, splitLines
 
 # LSRK(5,4) of Carpenter & Kennedy (pyranda.py:760-779)
@@ -239,6 +239,8 @@ class pyrandaSim:
         self._phi = None
         self._graph = None
         self._graphs_enabled = False
+        self._fuse = None
+        self._fuse_wanted = False
         self.get_sMap()
 
     # ------------------------------------------------------------ mesh set-up
@@ -601,9 +603,32 @@ class pyrandaSim:
 
     def rk4(self, time, dt):
         """One LSRK(5,4) step (pyranda.py:758-810), ALG update after every stage."""
+        if self._fuse_wanted and self._fuse is None:
+            from .fuse import Fuser
+            self._fuse = Fuser(self)
+            self._fuse.install(EVAL_GLOBALS)
         if self._graphs_enabled:
-            return self._rk4_graph(time, dt)
-        return self._rk4_eager(time, dt)
+            t = self._rk4_graph(time, dt)
+        else:
+            t = self._rk4_eager(time, dt)
+        if self._fuse is not None and self._fuse.lib is None:
+            self._fuse.build()   # after the recording step, before any capture
+        return t
+
+    def use_fusion(self, enable=True):
+        """Evaluate the EOM's elementwise arithmetic in generated CUDA kernels.
+
+        Each maximal elementwise subtree of every equation becomes one kernel
+        (pyranda_gb300.fuse).  The next rk4 step records the kernels' argument
+        kinds and runs unfused; the kernels are then compiled once (nvcc,
+        cached by source hash) and used from the following step on, with the
+        same results bit for bit.
+        """
+        self._fuse_wanted = bool(enable)
+        if not enable and self._fuse is not None:
+            self._fuse = None
+            for eq in self.equations:
+                eq.RHS = eval("lambda self: " + eq.sRHS, EVAL_GLOBALS)
 
     def _dt_tensor(self, dt):
         if isinstance(dt, torch.Tensor):
@@ -699,6 +724,7 @@ class pyrandaSim:
                         if old.shape == new.shape or old.dim() == 0:
                             old.copy_(new)
         torch.cuda.current_stream().wait_stream(stream)
+        flush_pending()
         self.cycle -= 1
         for n, old in before.items():
             if isinstance(old, torch.Tensor):

@@ -134,9 +134,11 @@ def test_fallback_flag_reruns_the_step_with_the_plain_closure():
     from pyranda_gb300.learned_lad import learned_shock_eom
     m = _model(5)
     m.ylo, m.yhi = [1e9, 1e9], [2e9, 2e9]   # every prediction is out of range
-    a = _shock(learned_shock_eom(), "learned", m)
+    # both start from the plain closure's initial state; a then predicts
+    a = _shock(learned_shock_eom(), "plain", m)
     b = _shock(learned_shock_eom(), "plain", m)
     lad = a.packages["LAD"]
+    lad.mode = "learned"
     ta, tb = 0.0, 0.0
     for _ in range(2):
         dt = a.variables["dt"].data.clone()
@@ -163,14 +165,16 @@ def test_trained_closure_beats_untrained_and_none():
     untrained.xinvstd.copy_(m.xinvstd)
     untrained.ym, untrained.ys = m.ym, m.ys
     steps = 40
-    runs = {}
+    runs, dts = {}, []
     for name, mode, model in (("plain", "plain", m), ("learned", "learned", m), ("untrained", "learned", untrained),
                               ("off", "off", m)):
-        ss = _shock(learned_shock_eom(), mode, model, mach=2.2, amp=0.07)
+        ss = _shock(learned_shock_eom(), "plain", model, mach=2.2, amp=0.07)   # same initial state
+        ss.packages["LAD"].mode = mode
         t = 0.0
-        dt = ss.variables["dt"].data.clone() * 0.5
-        for _ in range(steps):   # one common step size so the runs stay comparable
-            t = ss.rk4(t, dt)
+        for i in range(steps):   # every run follows the plain run's time steps
+            if name == "plain":
+                dts.append(ss.variables["dt"].data.clone())
+            t = ss.rk4(t, dts[i])
         runs[name] = ss.variables["rho"].data
     ref = runs["plain"]
     err = {k: float((v - ref).abs().sum() / ref.abs().sum()) if bool(torch.isfinite(v).all()) else float("inf")
