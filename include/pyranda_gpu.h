@@ -184,8 +184,8 @@ int pg_ens_device_status(pg_ensemble* e, int* status);
  * the 27-point stencils of div(u)*D and |grad rho|*D plus D (D = GridLen):
  * PG_LAD_IN inputs padded to PG_LAD_K, three hidden layers of PG_LAD_HIDDEN
  * (ReLU), PG_LAD_OUT outputs; BF16 weights and activations, FP32 accumulation.
- * Outputs y are normalised:  beta = (y0*ys0 + ym0) * rho * D  and
- * kappa = (y1*ys1 + ym1) * rho * cv * D^2 / dt.
+ * Outputs y are normalised:  beta = max(0, y0*ys0 + ym0) * rho * D  and
+ * kappa = max(0, y1*ys1 + ym1) * rho * cv * D^2 / dt.
  * Parameters: one FP32 buffer of PG_LAD_NPARAM values laid out
  * [w1 64x64 | w2 64x64 | w3 64x64 | w4 2x64 | b1 64 | b2 64 | b3 64 | b4 2]
  * (weights row = output unit), and BF16 copies of its first PG_LAD_NWEIGHT

@@ -395,8 +395,8 @@ int build_dense(Ctx& c, const std::vector<GridInfo>& g) {
         o.dm = g[m].dm[d];
         dops.push_back(o);
         const int lines = (int)(g[m].npts / n);
-        const int lt = (d == 0) ? 128 : 256;
-        const int parts = (d == 0) ? (((n + 15) & ~15) + 255) / 256 : (n + 127) / 128;
+        const int lt = 128;                                  // lines per tile
+        const int parts = (((n + 15) & ~15) + 255) / 256;    // 256 positions per tile
         for (int l0 = 0; l0 < lines; l0 += lt)
           for (int p = 0; p < parts; p++)
             dtiles.push_back(DenseTile{m, l0, std::min(lt, lines - l0), p});

@@ -17,9 +17,10 @@
 // same fused epilogues as the banded sweeps (store / accumulate / ring, with
 // the filters' FP64 add-back of v).
 //
-// One CTA computes one output tile: 128 lines x up to 256 positions (x), or
-// 128 positions x up to 256 lines (y, z), over the full K = n in chunks of 32,
-// double buffered.  Every wait is bounded; on a time-out the kernel records
+// One CTA computes one output tile of 128 lines x up to 256 positions: for x
+// lines one accumulator (M = lines, N = positions), for y and z lines up to
+// two (M = 128 positions each, N = lines), over the full K = n in chunks of
+// 32, double buffered.  Every wait is bounded; on a time-out the kernel records
 // PG_ETIMEOUT in the status word, stops issuing work and still frees its
 // tensor memory.
 #include <cuda_runtime.h>
@@ -199,22 +200,26 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
   const int n = op.n;
   const int st = (DIR == 0) ? 1 : (DIR == 1 ? op.nx : op.nx * op.ny);
 
-  // tile geometry: V rows are lines, D rows are output positions
-  int drow0, drows, vrows, N;
+  // Tile geometry: V rows are the tile's 128 lines, D rows its output
+  // positions [drow0, drow0 + 256).  x: one accumulator, N = positions.
+  // y, z: NP accumulators (one per 128 positions, M = 128 each), N = lines,
+  // so the lines are staged once for all 256 positions.
+  int drow0, drows, vrows, N, NP;
+  drow0 = tile.part * 256;
   if (ORIENT == 0) {
-    drow0 = tile.part * 256;
     drows = min(256, ((n + 15) & ~15) - drow0);
     vrows = 128;
     N = drows;
+    NP = 1;
   } else {
-    drow0 = tile.part * 128;
-    drows = 128;
+    NP = min(2, (n - drow0 + 127) / 128);
+    drows = NP * 128;
     vrows = (tile.nlines + 15) & ~15;
     N = vrows;
   }
-  const uint32_t vbytes = (ORIENT == 0) ? 16384u : 32768u;  // one V plane of a stage
-  const uint32_t dbytes = (ORIENT == 0) ? 32768u : 16384u;  // one D plane of a stage
-  const uint32_t dcopy = (uint32_t)drows * 128u;             // bytes of the D rows this tile reads
+  constexpr uint32_t vbytes = 16384u;  // one V plane of a stage: 128 rows
+  constexpr uint32_t dbytes = 32768u;  // one D plane of a stage: 256 rows
+  const uint32_t dcopy = (uint32_t)drows * 128u;  // bytes of the D rows this tile reads
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
@@ -234,7 +239,7 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
   // for any per-line constant c; subtracting the line's first value before
   // the split keeps the FP32 accumulation free of the lines' mean level.
   {
-    const int nlv = (ORIENT == 0) ? 128 : 256;
+    const int nlv = 128;
     if (tid < nlv) {
       const bool ok = tid < tile.nlines;
       const long long b = ok ? line_base(op, DIR, tile.line0 + tid) : 0;
@@ -295,9 +300,9 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
       }
     } else {
 #pragma unroll
-      for (int i = 0; i < 2048 / kDenseThreads; i++) {  // 256 rows x 8 chunks
+      for (int i = 0; i < 1024 / kDenseThreads; i++) {  // 128 rows x 8 chunks
         const int idx = tid + kDenseThreads * i;
-        const int r = idx & 255, q = idx >> 8;
+        const int r = idx & 127, q = idx >> 7;
         if (r < vrows) {
           const bool ok = r < tile.nlines;
           const double* p = P.in + s_base[r];
@@ -326,14 +331,20 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
         s_bad = 1;
       } else {
         tc_fence_after();
-        const uint32_t a_hi = smem_u32(ORIENT == 0 ? v_hi : d_hi), a_lo = smem_u32(ORIENT == 0 ? v_lo : d_lo);
-        const uint32_t b_hi = smem_u32(ORIENT == 0 ? d_hi : v_hi), b_lo = smem_u32(ORIENT == 0 ? d_lo : v_lo);
+        for (int pp = 0; pp < NP; pp++) {
+          // y, z: accumulator pp (TMEM columns 128 pp ..) takes D rows 128 pp ..
+          const uint32_t dofs = (ORIENT == 0) ? 0u : (uint32_t)pp * 16384u;
+          const uint32_t a_hi = smem_u32(ORIENT == 0 ? v_hi : d_hi) + dofs;
+          const uint32_t a_lo = smem_u32(ORIENT == 0 ? v_lo : d_lo) + dofs;
+          const uint32_t b_hi = smem_u32(ORIENT == 0 ? d_hi : v_hi), b_lo = smem_u32(ORIENT == 0 ? d_lo : v_lo);
+          const uint32_t acc = tmem + (uint32_t)(pp * 128);
 #pragma unroll
-        for (int kk = 0; kk < kKC / 8; kk++) {
-          const uint32_t o = kk * 32;  // 8 TF32 = 32 bytes along K
-          mma_tf32(tmem, sdesc(a_hi + o), sdesc(b_lo + o), idesc, (c > 0 || kk > 0) ? 1 : 0);
-          mma_tf32(tmem, sdesc(a_lo + o), sdesc(b_hi + o), idesc, 1);
-          mma_tf32(tmem, sdesc(a_hi + o), sdesc(b_hi + o), idesc, 1);
+          for (int kk = 0; kk < kKC / 8; kk++) {
+            const uint32_t o = kk * 32;  // 8 TF32 = 32 bytes along K
+            mma_tf32(acc, sdesc(a_hi + o), sdesc(b_lo + o), idesc, (c > 0 || kk > 0) ? 1 : 0);
+            mma_tf32(acc, sdesc(a_lo + o), sdesc(b_hi + o), idesc, 1);
+            mma_tf32(acc, sdesc(a_hi + o), sdesc(b_hi + o), idesc, 1);
+          }
         }
         mma_commit(&mma_bar[s]);
         committed = c;
@@ -361,11 +372,12 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
   } else {
     // tensor memory -> shared tile T[row][col] (row = TMEM lane), padded rows
     float* T = reinterpret_cast<float*>(smem);
-    const int ld = N + 1;
+    const int ncol = (ORIENT == 0) ? N : NP * 128;  // TMEM columns in use (y, z: accumulator pp at 128 pp)
+    const int ld = ncol + 1;
     // warp w reads TMEM lanes 32 (w % 4) ..; the warp groups w / 4 take turns over 8-column blocks
     const int q = warp & 3, h = warp >> 2;
     const int row = q * 32 + lane;
-    for (int col = 8 * h; col < N; col += 8 * (kDenseThreads / 128)) {
+    for (int col = 8 * h; col < ncol; col += 8 * (kDenseThreads / 128)) {
       float r[8];
       tmem_ld8(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)col, r);
 #pragma unroll
@@ -386,14 +398,16 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
         }
       }
     } else {
-      const int nl = tile.nlines, npos = min(128, n - drow0);
+      // position drow0 + 128 pp + r of line col is T[r][128 pp + col]
+      const int nl = tile.nlines, npos = min(NP * 128, n - drow0);
       for (int idx = tid; idx < npos * N; idx += kDenseThreads) {
-        const int r = idx / N, col = idx - r * N;
+        const int pr = idx / N, col = idx - pr * N;
         if (col < nl) {
-          const int64_t a = s_base[col] + (int64_t)(drow0 + r) * st;
+          const int pp = pr >> 7, r = pr & 127;
+          const int64_t a = s_base[col] + (int64_t)(drow0 + pr) * st;
           const double vin = ADDBACK ? P.in[a] : 0.0;
           const double o = kReadOut ? P.out[a] : 0.0;
-          P.out[a] = epilogue<EPI>(f2d_bits(T[r * ld + col]), vin, o, sc, ADDBACK);
+          P.out[a] = epilogue<EPI>(f2d_bits(T[r * ld + pp * 128 + col]), vin, o, sc, ADDBACK);
         }
       }
     }

@@ -81,8 +81,8 @@ struct DenseOp {
   int pad;
   double dm;        // mesh spacing along the direction (ring scale)
 };
-// One CTA's output tile: lines [line0, line0 + nlines) of member `op`;
-// part = which 256 positions (x) or 128 positions (y, z) of the line.
+// One CTA's output tile: lines [line0, line0 + nlines) of member `op`
+// (at most 128); part = which 256 positions of the lines.
 struct DenseTile {
   int op;
   int line0;

@@ -13,7 +13,7 @@
 // are normalised targets
 //   y0 = beta / (rho D)             (a velocity scale)
 //   y1 = kappa dt / (rho cv D^2)    (dimensionless)
-// so that   beta = (y0 s0 + m0) rho D,   kappa = (y1 s1 + m1) rho cv D^2 / dt.
+// so that   beta = max(0, y0 s0 + m0) rho D,   kappa = max(0, y1 s1 + m1) rho cv D^2 / dt.
 //
 // Inference (lad_infer_kernel) fuses the feature gather with the network on
 // the tensor cores (mma.sync m16n8k16 BF16 -> FP32; each layer's accumulator
@@ -191,8 +191,9 @@ __global__ void __launch_bounds__(kInferThreads) lad_infer_kernel(const LadInfer
           out_of_range |= !(y0 >= M.ylo[0] && y0 <= M.yhi[0] && y1 >= M.ylo[1] && y1 <= M.yhi[1]);
           const double rho = A.rho[p];
           const double d = G.delta;
-          A.beta[p] = ((double)y0 * M.ys[0] + M.ym[0]) * rho * d;
-          A.kappa[p] = ((double)y1 * M.ys[1] + M.ym[1]) * rho * A.cv * d * d / A.dt[0];
+          // artificial viscosity and conductivity are non-negative (the plain operators are)
+          A.beta[p] = fmax(0.0, (double)y0 * M.ys[0] + M.ym[0]) * rho * d;
+          A.kappa[p] = fmax(0.0, (double)y1 * M.ys[1] + M.ym[1]) * rho * A.cv * d * d / A.dt[0];
         }
       }
     }

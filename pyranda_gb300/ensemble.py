@@ -381,6 +381,8 @@ class pyrandaEnsemble(pyrandaSim):
         self._phi = None
         self._graph = None
         self._graphs_enabled = False
+        self._fuse = None
+        self._fuse_wanted = False
         self.get_sMap()
 
     def _make_mesh(self):

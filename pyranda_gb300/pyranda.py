@@ -7,6 +7,7 @@ the LSRK(5,4) update is one fused kernel per stage, and global reductions
 (``sum``/``max``/``min`` and the time-step limits) return device scalars so a
 whole RK step can be recorded in a CUDA graph (``pyrandaSim.use_graphs``).
 """
+import gc
 import math
 
 import numpy
@@ -712,17 +713,19 @@ class pyrandaSim:
         stream = torch.cuda.Stream(device=self.grid.device)
         stream.wait_stream(torch.cuda.current_stream())
         g = torch.cuda.CUDAGraph()
-        with torch.cuda.stream(stream):
-            with torch.cuda.graph(g, stream=stream, capture_error_mode="thread_local"):
-                self._rk4_eager(self._g_t0, self._g_dt, dt_dev=self._g_dt)
-                # carry every rebound variable back into the storage the next
-                # replay reads
-                for n, v in self.variables.items():
-                    old = before.get(n)
-                    new = v.data
-                    if isinstance(old, torch.Tensor) and isinstance(new, torch.Tensor) and old is not new:
-                        if old.shape == new.shape or old.dim() == 0:
-                            old.copy_(new)
+        # Python's cyclic collector may finalise an older simulation at any
+        # allocation; destroying its graph or its library handle calls CUDA
+        # APIs that are not allowed while a stream is being captured.
+        gc_was_enabled = gc.isenabled()
+        gc.collect()
+        gc.disable()
+        try:
+            with torch.cuda.stream(stream):
+                with torch.cuda.graph(g, stream=stream, capture_error_mode="thread_local"):
+                    self._capture_body(before)
+        finally:
+            if gc_was_enabled:
+                gc.enable()
         torch.cuda.current_stream().wait_stream(stream)
         flush_pending()
         self.cycle -= 1
@@ -731,3 +734,13 @@ class pyrandaSim:
                 self.variables[n].data = old
         self._graph = g
         # the capture itself did not advance the state: replay once for this step
+
+    def _capture_body(self, before):
+        """The recorded work: one eager step, then the rebound variables copied back into the replay's storage."""
+        self._rk4_eager(self._g_t0, self._g_dt, dt_dev=self._g_dt)
+        for n, v in self.variables.items():
+            old = before.get(n)
+            new = v.data
+            if isinstance(old, torch.Tensor) and isinstance(new, torch.Tensor) and old is not new:
+                if old.shape == new.shape or old.dim() == 0:
+                    old.copy_(new)

@@ -5,12 +5,14 @@
   FP64 accumulation; a hidden activation can land on the other side of a
   BF16 rounding boundary);
 * pg_lad_closure's outputs equal the oracle forward on the oracle's own
-  27-point feature gather: median relative difference <= 1e-3;
+  27-point feature gather: differences <= 1e-4 (median) and 1e-2 (99th
+  percentile) of the field's scale;
 * Adam on the FP32 master weights matches the textbook update;
 * training reduces the loss; out-of-range predictions raise the fallback
   flag and the step is re-run with the plain closure;
-* on a small shock problem, the trained closure's density is much closer
-  to the plain-LAD run than an untrained network's or no closure's.
+* on a small shock problem, the trained closure stays within 2% (density
+  L1) of the plain-LAD run, closer than the same network untrained, while
+  the run without a closure does not survive.
 """
 import ctypes
 
@@ -70,14 +72,15 @@ def test_closure_inference_matches_oracle():
     Xn = (raw - m.xmean.cpu().numpy()) * m.xinvstd.cpu().numpy()
     y, _ = L.forward(m.params.cpu().numpy(), Xn)
     rf = rho.ravel(order="F")
-    b_ref = (y[:, 0] * m.ys[0] + m.ym[0]) * rf * g.gridlen
-    k_ref = (y[:, 1] * m.ys[1] + m.ym[1]) * rf * 2.5 * g.gridlen ** 2 / 2e-3
+    b_ref = numpy.maximum(0.0, y[:, 0] * m.ys[0] + m.ym[0]) * rf * g.gridlen
+    k_ref = numpy.maximum(0.0, y[:, 1] * m.ys[1] + m.ym[1]) * rf * 2.5 * g.gridlen ** 2 / 2e-3
     b = to_host(beta).ravel(order="F")
     k = to_host(kappa).ravel(order="F")
-    rb = numpy.abs(b - b_ref) / numpy.maximum(numpy.abs(b_ref), 1e-3 * numpy.abs(b_ref).max())
-    rk = numpy.abs(k - k_ref) / numpy.maximum(numpy.abs(k_ref), 1e-3 * numpy.abs(k_ref).max())
-    assert numpy.median(rb) < 1e-3 and numpy.median(rk) < 1e-3
-    assert numpy.quantile(rb, 0.99) < 3e-2 and numpy.quantile(rk, 0.99) < 3e-2
+    # relative to the field's scale: clamped points are zero in both
+    rb = numpy.abs(b - b_ref) / max(numpy.abs(b_ref).max(), 1e-300)
+    rk = numpy.abs(k - k_ref) / max(numpy.abs(k_ref).max(), 1e-300)
+    assert numpy.median(rb) < 1e-4 and numpy.median(rk) < 1e-4
+    assert numpy.quantile(rb, 0.99) < 1e-2 and numpy.quantile(rk, 0.99) < 1e-2
 
 
 def test_adam_matches_textbook_update():
@@ -164,21 +167,25 @@ def test_trained_closure_beats_untrained_and_none():
     untrained.xmean.copy_(m.xmean)
     untrained.xinvstd.copy_(m.xinvstd)
     untrained.ym, untrained.ys = m.ym, m.ys
-    steps = 40
-    runs, dts = {}, []
+    t_end = 0.35    # the shock has crossed the interface
+    runs = {}
     for name, mode, model in (("plain", "plain", m), ("learned", "learned", m), ("untrained", "learned", untrained),
                               ("off", "off", m)):
         ss = _shock(learned_shock_eom(), "plain", model, mach=2.2, amp=0.07)   # same initial state
         ss.packages["LAD"].mode = mode
-        t = 0.0
-        for i in range(steps):   # every run follows the plain run's time steps
-            if name == "plain":
-                dts.append(ss.variables["dt"].data.clone())
-            t = ss.rk4(t, dts[i])
+        t, n = 0.0, 0
+        # each run takes its own CFL / diffusion steps to the same time (the reference scripts' loop)
+        while t < t_end - 1e-12 and n < 2000:
+            dt = min(float(ss.variables["dt"].data), t_end - t)
+            t = float(ss.rk4(t, dt))
+            n += 1
+            if not bool(torch.isfinite(ss.variables["rho"].data).all()):
+                break
         runs[name] = ss.variables["rho"].data
     ref = runs["plain"]
     err = {k: float((v - ref).abs().sum() / ref.abs().sum()) if bool(torch.isfinite(v).all()) else float("inf")
            for k, v in runs.items() if k != "plain"}
     print("density L1 error vs plain LAD:", err)
-    assert err["learned"] < 0.5 * err["off"], err
-    assert err["learned"] < 0.5 * err["untrained"], err
+    assert err["learned"] < 0.02, err               # within 2% of the plain closure (density L1)
+    assert err["learned"] < err["off"], err         # better than no closure (which here does not survive)
+    assert err["learned"] < err["untrained"], err   # and better than the same network untrained
