@@ -332,7 +332,7 @@ def profile_step(args):
     """One eager TGV RK step inside a profiler range, after 2 warm-up steps."""
     import torch
     torch.cuda.set_device(0)
-    ss = make_sim(args.n, args.precision, graphs=False)
+    ss = make_sim(args.n, args.precision, graphs=False, fusion=not args.no_fusion and args.precision != "fp64")
     run_steps(ss, 2)
     torch.cuda.synchronize()
     torch.cuda.cudart().cudaProfilerStart()
@@ -539,9 +539,11 @@ def shock_learned(args):
         def packs(ss):
             ss.addPackage(pyrandaBC(ss))
             ss.addPackage(pyrandaTimestep(ss))
-            ss.addPackage(LL.pyrandaLearnedLAD(ss, model, problems.CV, mode=mode))
+            ss.addPackage(LL.pyrandaLearnedLAD(ss, model, problems.CV, mode="plain"))
+        # the initial state always comes from the plain closure; the run then uses `mode`
         ss = problems.build_shock(pyrandaSim, 512, 128, 128, packs, eom=LL.learned_shock_eom(), silent=True,
                                   precision="fp32")
+        ss.packages["LAD"].mode = mode
         ss.use_graphs(True)
         return ss
 

@@ -181,7 +181,8 @@ int pg_ens_device_status(pg_ensemble* e, int* status);
  * Learned LAD closure (no counterpart in the reference, which evaluates the
  * plain LAD operators of examples/ISSW_cyl.py:101-104 every stage).  A small
  * MLP predicts the artificial bulk viscosity beta and conductivity kappa from
- * the 27-point stencils of div(u)*D and |grad rho|*D plus D (D = GridLen):
+ * the 27-point stencils of div(u)*D and |grad rho|*D plus D (D = the largest
+ * mesh spacing):
  * PG_LAD_IN inputs padded to PG_LAD_K, three hidden layers of PG_LAD_HIDDEN
  * (ReLU), PG_LAD_OUT outputs; BF16 weights and activations, FP32 accumulation.
  * Outputs y are normalised:  beta = max(0, y0*ys0 + ym0) * rho * D  and

@@ -9,7 +9,8 @@ its mean-squared-error loss over rows x outputs and the gradient of that loss
 with respect to every parameter, and the 27-point feature gather:
   features of point (i, j, k) = div*D at the 27 neighbours (di, dj, dk in
   {-1, 0, 1}, index s = (di+1) + 3 (dj+1) + 9 (dk+1)), then |grad rho|*D at
-  the same neighbours, then D, then zeros up to 64; periodic directions wrap,
+  the same neighbours, then D (the largest mesh spacing), then zeros up to
+  64; periodic directions wrap,
   one-sided directions clamp, a direction of one point repeats the point.
 The reference has no learned closure; parity here is between the CUDA
 kernels and this restatement of their stated arithmetic, plus a

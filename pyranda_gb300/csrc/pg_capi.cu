@@ -266,6 +266,38 @@ int build_ctx(Ctx& c, const std::vector<GridInfo>& g, int precision, const char*
 
 bool bad_dir(int d) { return d < 0 || d > 2; }
 
+// The dense operator in terms of first differences.  Every operator here
+// annihilates constants (D 1 = 0), so row i of D v equals
+// sum_j D_ij (v_j - v_i), and each v_j - v_i is a sum of the differences
+// w_m = v_m - v_{m-1} along the shorter way from i to j (w_0 = v_0 - v_{n-1}
+// on periodic lines; on one-sided lines the path never wraps and w_0 is
+// unused).  The result D' (OUT = D' w) is local around the diagonal in every
+// row, including the rows next to a periodic wrap, so its products are of
+// the size of the result and the FP32 accumulation sees no cancellation --
+// the property the banded sweeps get from their difference-form stencils.
+std::vector<double> difference_form(const std::vector<double>& D, int n, bool periodic) {
+  std::vector<double> W((size_t)n * n, 0.0);
+  for (int i = 0; i < n; i++) {
+    const double* d = &D[(size_t)i * n];
+    double* w = &W[(size_t)i * n];
+    const int fwd = periodic ? n / 2 : n - 1 - i;        // forward partners i+1 .. i+fwd
+    const int bwd = periodic ? n - 1 - n / 2 : i;        // backward partners i-1 .. i-bwd
+    // v_{i+k} - v_i = sum_{l=1..k} w_{i+l}: w_{i+l} collects D_{i,i+k} for k >= l
+    double acc = 0.0;
+    for (int k = fwd; k >= 1; k--) {
+      acc += d[(i + k) % n];
+      w[(i + k) % n] += acc;
+    }
+    // v_{i-k} - v_i = -sum_{l=0..k-1} w_{i-l}: w_{i-l} collects -D_{i,i-k} for k > l
+    acc = 0.0;
+    for (int k = bwd; k >= 1; k--) {
+      acc += d[(i - k + n) % n];
+      w[(i - k + 1 + n) % n] -= acc;
+    }
+  }
+  return W;
+}
+
 // Dense form of the d1, d8 and compact-filter operators of every member: D is
 // the banded FP64 operator itself, applied to an identity (line k = e_k), so
 // the dense and banded paths implement one matrix.  Members with identical
@@ -358,7 +390,7 @@ int build_dense(Ctx& c, const std::vector<GridInfo>& g) {
       for (int i = 0; i < n; i++) D[(size_t)i * n + k] = Dt[(size_t)k * n + i];
     if (ref.addback)
       for (int i = 0; i < n; i++) D[(size_t)i * n + i] -= 1.0;
-    split_dense(D, n, u.planes, u.rows, u.kchunks);
+    split_dense(difference_form(D, n, ref.periodic), n, u.planes, u.rows, u.kchunks);
   }
   cudaFree(ident);
   cudaFree(dout);
@@ -392,6 +424,7 @@ int build_dense(Ctx& c, const std::vector<GridInfo>& g) {
         o.ny = g[m].n[1];
         o.kchunks = u.kchunks;
         o.rows = u.rows;
+        o.periodic = g[m].periodic[d];
         o.dm = g[m].dm[d];
         dops.push_back(o);
         const int lines = (int)(g[m].npts / n);
@@ -903,7 +936,7 @@ LadGrid lad_grid(const GridInfo& g) {
     lg.n[d] = g.n[d];
     lg.per[d] = g.periodic[d];
   }
-  lg.delta = std::min(std::min(g.dm[0], g.dm[1]), g.dm[2]);
+  lg.delta = std::max(std::max(g.dm[0], g.dm[1]), g.dm[2]);  // the largest mesh spacing
   return lg;
 }
 }  // namespace

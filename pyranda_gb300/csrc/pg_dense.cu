@@ -162,6 +162,34 @@ __device__ __forceinline__ uint32_t tf32_bits(float x) {
   return (__float_as_uint(x) + 0x1000u) & 0xFFFFE000u;
 }
 
+// The four differences w_k = v_k - v_{k-1}, k = kb .. kb+3, of one line (v at
+// p[k * stride]) as TF32 hi / lo.  w_0 is the wrap difference v_0 - v_{n-1}
+// on periodic lines and 0 otherwise; k >= n gives 0.  Each v is split into
+// FP32 value + residual first, so a difference keeps ~48 bits of v before
+// its own rounding to FP32.
+template <int UNIT>
+__device__ __forceinline__ void stage_differences(const double* __restrict__ p, bool ok, int kb, int n, int periodic,
+                                                  uint32_t* h, uint32_t* l, int stride = 1) {
+  const int64_t st = UNIT ? 1 : stride;
+  float2 prev = make_float2(0.f, 0.f);
+  if (ok) {
+    const int km1 = (kb > 0) ? kb - 1 : (periodic ? n - 1 : -1);
+    if (km1 >= 0 && km1 < n) prev = split_f64(__ldg(p + km1 * st));
+  }
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const int k = kb + j;
+    float f = 0.0f;
+    if (ok && k < n) {
+      const float2 v = split_f64(__ldg(p + k * st));
+      if (k > 0 || periodic) f = (v.x - prev.x) + (v.y - prev.y);
+      prev = v;
+    }
+    h[j] = tf32_bits(f);
+    l[j] = tf32_bits(f - __uint_as_float(h[j]));
+  }
+}
+
 // byte offset of 16-byte chunk q of row r in a K-major 128B-swizzled tile
 __device__ __forceinline__ uint32_t swz(int r, int q) {
   return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((q ^ (r & 7)) << 4));
@@ -190,8 +218,7 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
   __shared__ __align__(8) uint64_t mma_bar[kStages];
   __shared__ uint32_t tmem_slot;
   __shared__ int s_bad;
-  __shared__ float2 s_ref[256];     // per line: its first value split as (hi, residual)
-  __shared__ long long s_base[256];  // per line: offset of its first point
+  __shared__ long long s_base[128];  // per line: offset of its first point
   uint8_t* smem = dsm_raw + ((1024u - (smem_u32(dsm_raw) & 1023u)) & 1023u);
 
   const DenseTile tile = P.tiles[blockIdx.x];
@@ -235,18 +262,7 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
     s_bad = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // Every operator here annihilates constants (D 1 = 0), so D v = D (v - c)
-  // for any per-line constant c; subtracting the line's first value before
-  // the split keeps the FP32 accumulation free of the lines' mean level.
-  {
-    const int nlv = 128;
-    if (tid < nlv) {
-      const bool ok = tid < tile.nlines;
-      const long long b = ok ? line_base(op, DIR, tile.line0 + tid) : 0;
-      s_base[tid] = b;
-      s_ref[tid] = ok ? split_f64(__ldg(P.in + b)) : make_float2(0.f, 0.f);
-    }
-  }
+  if (tid < 128) s_base[tid] = (tid < tile.nlines) ? line_base(op, DIR, tile.line0 + tid) : 0;
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -281,20 +297,8 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
         const int idx = tid + kDenseThreads * i;
         const int r = idx >> 3, q = idx & 7;
         const bool ok = r < tile.nlines;
-        const double* p = P.in + s_base[r];
-        const float2 c = s_ref[r];
         uint32_t h[4], l[4];
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-          const int k = k0 + q * 4 + j;
-          float f = 0.0f;
-          if (ok && k < n) {
-            const float2 v = split_f64(__ldg(p + k));
-            f = (v.x - c.x) + (v.y - c.y);
-          }
-          h[j] = tf32_bits(f);
-          l[j] = tf32_bits(f - __uint_as_float(h[j]));
-        }
+        stage_differences<1>(P.in + s_base[r], ok, k0 + q * 4, n, op.periodic, h, l);
         *reinterpret_cast<uint4*>(v_hi + swz(r, q)) = make_uint4(h[0], h[1], h[2], h[3]);
         *reinterpret_cast<uint4*>(v_lo + swz(r, q)) = make_uint4(l[0], l[1], l[2], l[3]);
       }
@@ -305,20 +309,8 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
         const int r = idx & 127, q = idx >> 7;
         if (r < vrows) {
           const bool ok = r < tile.nlines;
-          const double* p = P.in + s_base[r];
-          const float2 c = s_ref[r];
           uint32_t h[4], l[4];
-#pragma unroll
-          for (int j = 0; j < 4; j++) {
-            const int k = k0 + q * 4 + j;
-            float f = 0.0f;
-            if (ok && k < n) {
-              const float2 v = split_f64(__ldg(p + (int64_t)k * st));
-              f = (v.x - c.x) + (v.y - c.y);
-            }
-            h[j] = tf32_bits(f);
-            l[j] = tf32_bits(f - __uint_as_float(h[j]));
-          }
+          stage_differences<0>(P.in + s_base[r], ok, k0 + q * 4, n, op.periodic, h, l, st);
           *reinterpret_cast<uint4*>(v_hi + swz(r, q)) = make_uint4(h[0], h[1], h[2], h[3]);
           *reinterpret_cast<uint4*>(v_lo + swz(r, q)) = make_uint4(l[0], l[1], l[2], l[3]);
         }

@@ -68,9 +68,10 @@ struct SweepLaunch {
 // Launches one directional sweep over every member.  Returns a pg_status.
 int launch_sweep(int precision, const SweepLaunch& s, void* stream);
 
-// Dense operator of one member along one direction (device memory): D split
-// into TF32 hi/lo planes laid out as [kchunk][hi, lo][rows][32] words, each
-// 8-row group 128B-swizzled (the shared-memory layout the MMA reads).
+// Dense operator of one member along one direction (device memory): the
+// difference form D' of D (OUT = D' w, w_k = v_k - v_{k-1}) split into TF32
+// hi/lo planes laid out as [kchunk][hi, lo][rows][32] words, each 8-row
+// group 128B-swizzled (the shared-memory layout the MMA reads).
 struct DenseOp {
   const uint32_t* dsw;
   long long off;    // first point of the member in the flat field
@@ -78,7 +79,7 @@ struct DenseOp {
   int nx, ny;       // member extents (to decode a line index)
   int kchunks;      // ceil(n / 32)
   int rows;         // rows of each plane: n padded to a multiple of 128
-  int pad;
+  int periodic;     // 1: w_0 = v_0 - v_{n-1} (the wrap difference)
   double dm;        // mesh spacing along the direction (ring scale)
 };
 // One CTA's output tile: lines [line0, line0 + nlines) of member `op`
@@ -139,7 +140,7 @@ int launch_seg_diff(const double* bulk, const double* rho, const double* mconst,
 struct LadGrid {
   int n[3];
   int per[3];
-  double delta;  // GridLen
+  double delta;  // largest mesh spacing
 };
 struct LadInferArgs {
   pg_lad_model model;

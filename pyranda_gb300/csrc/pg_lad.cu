@@ -4,8 +4,9 @@
 // Features of a point (kLadIn = 55, padded to kLadK = 64 inputs): the
 // 27-point (3 x 3 x 3) stencils of  div(u) * D  and  |grad rho| * D  around
 // it (periodic directions wrap, one-sided directions clamp, a direction of one
-// point repeats the point), then D itself, where D = GridLen (the smallest
-// mesh spacing).  Each input is normalised, x = (f - mean) / std, with the
+// point repeats the point), then D itself, where D is the largest mesh
+// spacing (the spacing across the shocks of the training problems, so that
+// features and targets keep their scale between grids of other aspect ratios).  Each input is normalised, x = (f - mean) / std, with the
 // training set's statistics.
 //
 // Network: 64 -> 64 -> 64 -> 64 -> 2, ReLU on the hidden layers, BF16 weights

@@ -209,7 +209,7 @@ def shock_training_set(runs=20, snapshots_per_run=100, shape=(128, 64, 64), poin
         ss = problems.build_shock(pyrandaSim, *shape, packs, mach=mach, amp=amp, silent=True, precision=precision)
         ss.use_graphs(True)
         g = ss.grid
-        delta = g.gridlen
+        delta = max(g.mesh_d)      # the closure's length scale (pg_lad_closure)
         gen = torch.Generator(device=g.device).manual_seed(int(rng.integers(1 << 30)))
         t = 0.0
         for s in range(snapshots_per_run):

@@ -58,7 +58,8 @@ def test_closure_inference_matches_oracle():
     gm = numpy.asfortranarray(numpy.abs(r.standard_normal(n)))
     rho = numpy.asfortranarray(1.0 + r.random(n))
     m = _model(2)
-    raw = L.features(div, gm, per, g.gridlen)
+    delta = max(g.mesh_d)
+    raw = L.features(div, gm, per, delta)
     fit_normalisation(m, torch.from_numpy(raw.astype(numpy.float32)).cuda(),
                       torch.from_numpy(r.random((raw.shape[0], 2)).astype(numpy.float32)).cuda())
     dt = torch.full((), 2e-3, dtype=torch.float64, device="cuda")
@@ -72,8 +73,8 @@ def test_closure_inference_matches_oracle():
     Xn = (raw - m.xmean.cpu().numpy()) * m.xinvstd.cpu().numpy()
     y, _ = L.forward(m.params.cpu().numpy(), Xn)
     rf = rho.ravel(order="F")
-    b_ref = numpy.maximum(0.0, y[:, 0] * m.ys[0] + m.ym[0]) * rf * g.gridlen
-    k_ref = numpy.maximum(0.0, y[:, 1] * m.ys[1] + m.ym[1]) * rf * 2.5 * g.gridlen ** 2 / 2e-3
+    b_ref = numpy.maximum(0.0, y[:, 0] * m.ys[0] + m.ym[0]) * rf * delta
+    k_ref = numpy.maximum(0.0, y[:, 1] * m.ys[1] + m.ym[1]) * rf * 2.5 * delta ** 2 / 2e-3
     b = to_host(beta).ravel(order="F")
     k = to_host(kappa).ravel(order="F")
     # relative to the field's scale: clamped points are zero in both
