@@ -50,9 +50,11 @@ typedef enum {
  * D = A^-1 B (the reference's `sm`, compact_basetype.f90:199-205) on the
  * tensor cores in split TF32 (hi.hi + hi.lo + lo.hi, FP32 accumulation) for
  * directions of 16..1024 points, and the FP32 banded sweeps elsewhere; the
- * filters' add-back of v stays in FP64.  Selecting it builds the dense
- * tables once (allocates and synchronises). */
-typedef enum { PG_FP64 = 0, PG_FP32 = 1, PG_DENSE = 2 } pg_precision;
+ * filters' add-back of v stays in FP64.  PG_AUTO builds the same tables and
+ * then, per operator and direction, times the dense kernel against the FP32
+ * banded sweep on the handle's own grid and keeps the faster.  Selecting
+ * either builds the tables once (allocates and synchronises). */
+typedef enum { PG_FP64 = 0, PG_FP32 = 1, PG_DENSE = 2, PG_AUTO = 3 } pg_precision;
 
 typedef enum { PG_SPECTRAL = 0, PG_GAUSSIAN = 1 } pg_filter_kind;
 
@@ -87,6 +89,9 @@ int pg_destroy(pg_handle* h);
 int pg_device_status(pg_handle* h, int* status);
 /* Switch the arithmetic of later sweeps on this handle (pg_precision). */
 int pg_set_precision(pg_handle* h, int precision);
+/* The sweep plan of PG_DENSE / PG_AUTO: plan[op * 3 + dir] = 1 where the
+ * dense kernel runs (op 0 d1, 1 d8, 2 compact filter, 3 Gaussian filter). */
+int pg_dense_plan(const pg_handle* h, int* plan);
 /* Patch spacing (used by the d1 metric) and mesh spacing d1..d3. */
 int pg_get_spacing(const pg_handle* h, double* patch_d, double* mesh_d);
 /* Text of the last error on this thread (static storage). */

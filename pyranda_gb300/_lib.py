@@ -9,12 +9,13 @@ import os
 from . import build as _build
 
 PG_OK, PG_EBADSHAPE, PG_ENULLOP, PG_ECUDA, PG_ENAN, PG_ETIMEOUT, PG_EINVAL, PG_ENOMEM = range(8)
-PG_FP64, PG_FP32, PG_DENSE = 0, 1, 2
-_PRECISIONS = {"fp64": PG_FP64, "fp32": PG_FP32, "dense": PG_DENSE}
+PG_FP64, PG_FP32, PG_DENSE, PG_AUTO = 0, 1, 2, 3
+_PRECISIONS = {"fp64": PG_FP64, "fp32": PG_FP32, "dense": PG_DENSE, "auto": PG_AUTO}
 
 
 def precision_code(name):
-    """'fp64' (reference arithmetic), 'fp32' (FP32 banded sweeps) or 'dense' (split-TF32 tensor-core operators)."""
+    """'fp64' (reference arithmetic), 'fp32' (FP32 banded sweeps), 'dense' (split-TF32 tensor-core operators)
+    or 'auto' (per operator and direction the faster of dense and FP32 banded, timed on the grid)."""
     try:
         return _PRECISIONS[name]
     except KeyError:
@@ -65,6 +66,7 @@ SIGNATURES = [
     ("pg_set_precision", I, [P, I]),
     ("pg_device_status", I, [P, ctypes.POINTER(ctypes.c_int)]),
     ("pg_get_spacing", I, [P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    ("pg_dense_plan", I, [P, ctypes.POINTER(ctypes.c_int)]),
     ("pg_last_error", ctypes.c_char_p, []),
     ("pg_version", ctypes.c_char_p, []),
     ("pg_d1", I, [P, I, D, D, P]),

@@ -118,6 +118,7 @@ struct Ctx {
   bool dense = false;
   bool dense_built = false;
   DenseSet dsets[OPK_COUNT][3];
+  bool use_dense[OPK_COUNT][3] = {};  // the sweep plan: dense kernel or FP32 banded
   void* dense_blob = nullptr;
 };
 
@@ -469,14 +470,67 @@ int build_dense(Ctx& c, const std::vector<GridInfo>& g) {
   return PG_OK;
 }
 
-// Arithmetic of later sweeps: PG_FP64 / PG_FP32 banded, or PG_DENSE (dense
-// split-TF32 operators where built, FP32 banded elsewhere).
+// Autotuning of PG_AUTO: for every (operator, direction) with a dense form,
+// time the dense kernel and the FP32 banded sweep on this grid (CUDA events,
+// median of 3 after one warm-up launch each) and keep the faster.
+int autotune_dense(Ctx& c) {
+  double* out = nullptr;
+  cudaEvent_t e0, e1;
+  if (cudaMalloc(&out, (size_t)c.npts * sizeof(double)) != cudaSuccess) {
+    set_error("autotune: cudaMalloc failed");
+    return PG_ENOMEM;
+  }
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaMemset(c.work, 0, (size_t)c.npts * sizeof(double));
+  int rc = PG_OK;
+  for (int k = 0; k < OPK_COUNT && rc == PG_OK; k++)
+    for (int d = 0; d < 3 && rc == PG_OK; d++) {
+      DenseSet& ds = c.dsets[k][d];
+      c.use_dense[k][d] = ds.ok;
+      if (!ds.ok) continue;
+      float t[2];
+      for (int way = 0; way < 2 && rc == PG_OK; way++) {
+        float best[3];
+        for (int rep = 0; rep < 4 && rc == PG_OK; rep++) {
+          cudaEventRecord(e0, 0);
+          if (way == 0) rc = launch_dense(ds, c.work, out, d, EPI_STORE, 0, c.status, nullptr);
+          else {
+            SweepLaunch s{c.work, out, c.work2, &c.ops[PG_FP32][k][d], d, EPI_STORE, 0};
+            rc = launch_sweep(PG_FP32, s, nullptr);
+          }
+          cudaEventRecord(e1, 0);
+          cudaEventSynchronize(e1);
+          if (rep > 0) cudaEventElapsedTime(&best[rep - 1], e0, e1);
+        }
+        std::sort(best, best + 3);
+        t[way] = best[1];
+      }
+      c.use_dense[k][d] = t[0] < t[1];
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  cudaError_t e = cudaGetLastError();
+  if (rc == PG_OK && e != cudaSuccess) {
+    set_error("autotune: %s", cudaGetErrorString(e));
+    rc = PG_ECUDA;
+  }
+  return rc;
+}
+
+// Arithmetic of later sweeps: PG_FP64 / PG_FP32 banded; PG_DENSE (dense
+// split-TF32 operators wherever built, FP32 banded elsewhere); PG_AUTO (per
+// operator and direction the faster of the two, measured on this grid).
 int set_precision(Ctx& c, const std::vector<GridInfo>& g, int precision) {
-  if (precision == PG_DENSE) {
+  if (precision == PG_DENSE || precision == PG_AUTO) {
     int rc = build_dense(c, g);
     if (rc) return rc;
     c.precision = PG_FP32;
     c.dense = true;
+    if (precision == PG_AUTO) return autotune_dense(c);
+    for (int k = 0; k < OPK_COUNT; k++)
+      for (int d = 0; d < 3; d++) c.use_dense[k][d] = c.dsets[k][d].ok;
     return PG_OK;
   }
   if (precision != PG_FP64 && precision != PG_FP32) return PG_EINVAL;
@@ -486,7 +540,7 @@ int set_precision(Ctx& c, const std::vector<GridInfo>& g, int precision) {
 }
 
 int sweep(Ctx& c, int kind, int dir, const double* in, double* out, int epi, int scale_pow, void* st) {
-  if (c.dense && c.dsets[kind][dir].ok) {
+  if (c.dense && c.use_dense[kind][dir]) {
     if (in == out) {  // tiles read whole lines that other tiles write: work on a copy
       int rc = launch_copy(c.work2, in, c.npts, st);
       if (rc) return rc;
@@ -636,7 +690,7 @@ int pg_create(const pg_grid* grid, pg_handle** out) {
     return PG_EINVAL;
   }
   *out = nullptr;
-  if (grid->precision != PG_FP64 && grid->precision != PG_FP32 && grid->precision != PG_DENSE) {
+  if (grid->precision < PG_FP64 || grid->precision > PG_AUTO) {
     set_error("pg_create: bad precision %d", grid->precision);
     return PG_EINVAL;
   }
@@ -668,6 +722,13 @@ int pg_device_status(pg_handle* h, int* status) {
 int pg_set_precision(pg_handle* h, int precision) {
   if (!h) return PG_EINVAL;
   return set_precision(h->c, std::vector<GridInfo>{h->g}, precision);
+}
+
+int pg_dense_plan(const pg_handle* h, int* plan) {
+  if (!h || !plan) return PG_EINVAL;
+  for (int k = 0; k < OPK_COUNT; k++)
+    for (int d = 0; d < 3; d++) plan[k * 3 + d] = (h->c.dense && h->c.use_dense[k][d]) ? 1 : 0;
+  return PG_OK;
 }
 
 int pg_get_spacing(const pg_handle* h, double* patch_d, double* mesh_d) {
@@ -800,7 +861,7 @@ int pg_ens_create(int m, const pg_grid* grids, pg_ensemble** out) {
   e->g.resize(m);
   for (int i = 0; i < m; i++) {
     if (grids[i].precision != grids[0].precision ||
-        (grids[i].precision != PG_FP64 && grids[i].precision != PG_FP32 && grids[i].precision != PG_DENSE)) {
+        grids[i].precision < PG_FP64 || grids[i].precision > PG_AUTO) {
       delete e;
       set_error("pg_ens_create: members must share one valid precision");
       return PG_EINVAL;

@@ -99,6 +99,13 @@ class Grid:
         except Exception:
             pass
 
+    def dense_plan(self):
+        """{(operator, direction): True where the dense kernel runs} (operators 'd1', 'd8', 'sf', 'gf')."""
+        plan = (ctypes.c_int * 12)()
+        _lib.check(self.lib.pg_dense_plan(self.h, plan), "pg_dense_plan")
+        return {(op, "xyz"[d]): bool(plan[k * 3 + d]) for k, op in enumerate(("d1", "d8", "sf", "gf"))
+                for d in range(3)}
+
     def set_precision(self, precision):
         self.precision = precision
         _lib.check(self.lib.pg_set_precision(self.h, _lib.precision_code(precision)),
