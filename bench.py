@@ -583,6 +583,21 @@ def shock_learned(args):
     t_learn = s.elapsed_time(e) / 1e3
     rho = learned.variables["rho"].data
     l1 = float(((rho - rho_plain).abs().sum() / rho_plain.abs().sum()).item())
+    # the closure alone on the final state: learned (|grad rho| + fused gather/MLP) vs plain (2 rings + 2 filters)
+    V = learned.variables
+    closure_ms = {}
+    for mode in ("learned", "plain"):
+        lad.mode = mode
+        lad.closure(V["div"].data, V["rho"].data, V["T"].data, V["dt"].data)
+        torch.cuda.synchronize()
+        s.record()
+        for _ in range(args.reps):
+            lad.closure(V["div"].data, V["rho"].data, V["T"].data, V["dt"].data)
+        e.record()
+        torch.cuda.synchronize()
+        closure_ms[mode] = round(s.elapsed_time(e) / args.reps, 4)
+    lad.mode = "learned"
+    out["closure_ms_per_call"] = closure_ms
     out["t_end"] = t_end
     out["plain_lad"] = {"value": round(npts * k_plain / t_plain / 1e6, 3), "unit": UNIT, "steps": k_plain,
                         "ms_per_step": round(t_plain / k_plain * 1e3, 3),

@@ -5,7 +5,7 @@ The package keeps pyranda's user API (``pyrandaSim`` with ``EOM``, ``setIC``,
 ``pyrandaTimestep`` and ``pyrandaBC`` packages) and runs it on the GPU through
 the C ABI of ``libpyranda_gpu.so`` (include/pyranda_gpu.h).
 """
-from .pyranda import pyrandaSim, pyrandaVar, pyrandaEq, defaultMeshOptions  # noqa: F401
+from .pyranda import pyrandaSim, pyrandaVar, pyrandaEq, pyrandaRestart, defaultMeshOptions  # noqa: F401
 from .pyrandaTimestep import pyrandaTimestep  # noqa: F401
 from .pyrandaBC import pyrandaBC  # noqa: F401
 from .pyrandaPackage import pyrandaPackage  # noqa: F401

@@ -12,7 +12,8 @@ gradient (three first-derivative sweeps, for |grad rho|) and one fused
 feature-gather + MLP kernel (``pg_lad_closure``).  The plain closure stays
 both the judge of the learned one's error and its fallback: the kernel raises
 a flag when a prediction leaves the training range, and
-``pyrandaLearnedLAD.step`` then re-runs that RK step with the plain closure.
+``pyrandaLearnedLAD.step`` then re-runs that RK step with the plain closure
+from the step's conserved state.
 
 Network inputs, outputs and normalisation are documented with the C ABI
 (include/pyranda_gpu.h, ``pg_lad_*``).
@@ -274,10 +275,38 @@ class pyrandaLearnedLAD(pyrandaPackage):
                    "pg_lad_closure")
         return [beta, kappa]
 
+    def _state_names(self):
+        """The state a step starts from: conserved variables, and the variables the
+        algebraic equations read before writing (or never write), e.g. :dt: in kappa."""
+        if getattr(self, "_state", None) is None:
+            from .pyrandaUtils import findVar
+            ss = self.pyranda
+            written, lagged = set(), set()
+            for eq in ss.equations:
+                if eq.kind != "ALG":
+                    continue
+                rhs = eq.eqstr.split("=", 1)[1] if eq.LHS else eq.eqstr
+                for v in findVar(rhs, "scalar"):
+                    if v not in written and v not in ss.conserved:
+                        lagged.add(v)
+                written.update(eq.LHS or [])
+            self._state = list(ss.conserved) + sorted(v for v in lagged if v in ss.variables)
+        return self._state
+
     def step(self, time, dt):
-        """One rk4 step with the learned closure; re-run with the plain one if the flag was raised."""
+        """One rk4 step with the learned closure; if the flag was raised, redo it with the plain closure.
+
+        The step's starting state (conserved variables plus the variables the
+        algebraic equations read before writing) is kept.  On a fallback it
+        is restored, the algebraic state is re-evaluated from it with the
+        plain closure (pyranda.py:393-428), and the step is run again with the
+        plain closure (eagerly; a recorded graph's storage is refreshed
+        afterwards).
+        """
         ss = self.pyranda
-        saved = {n: v.data.clone() for n, v in ss.variables.items() if isinstance(v.data, torch.Tensor)}
+        saved = {n: ss.variables[n].data.clone() for n in self._state_names()
+                 if isinstance(ss.variables[n].data, torch.Tensor)}
+        dt_saved = dt.clone() if isinstance(dt, torch.Tensor) else dt
         self.flag.zero_()
         t = ss.rk4(time, dt)
         if int(self.flag.item()) == 0:
@@ -293,10 +322,13 @@ class pyrandaLearnedLAD(pyrandaPackage):
         ss._graphs_enabled = False
         self.mode = "plain"
         try:
-            t = ss.rk4(time, dt)
+            ss.updateVars()
+            t = ss.rk4(time, dt_saved)
         finally:
             self.mode = "learned"
             ss._graphs_enabled = graphs
+            if graphs:
+                ss.sync_graph_storage()
         return t
 
 

@@ -9,6 +9,7 @@ whole RK step can be recorded in a CUDA graph (``pyrandaSim.use_graphs``).
 """
 import gc
 import math
+import os
 
 import numpy
 import torch
@@ -28,6 +29,56 @@ ETA = [494393426753. / 4806282396855., 4702696611523. / 9636871101405.,
        3614488396635. / 5249666457482., 9766892798963. / 10823461281321., 1.0]
 
 EVAL_GLOBALS = {"numpy": pgmath, "scipy": pgmath.scipy, "torch": torch, "math": math}
+
+
+def _num(x):
+    """A Python number from a number or a 0-d tensor."""
+    if isinstance(x, torch.Tensor):
+        return float(x.reshape(-1)[0].item())
+    return float(x) if x is not None else 0.0
+
+
+def pyrandaRestart(rootname, suffix=None, precision="fp64", device=None):
+    """pyranda.py:979-1072: a pyrandaSim from a restart (this library's or the reference's).
+
+    Returns [pysim, local_vars] as the reference does.  Packages are mapped
+    by module name onto this library's (pyrandaTimestep, pyrandaBC).
+    """
+    from . import restart
+    from .pyrandaBC import pyrandaBC
+    from .pyrandaTimestep import pyrandaTimestep
+    dump = restart.find_dump(rootname, suffix)
+    serial = restart.read_serial(dump)
+    local = {}
+    if "local_vars" in serial:
+        lv = serial.pop("local_vars")
+        for name, fn in lv.pop("numpyArrays", {}).items():
+            local[name] = numpy.load(fn + ".npy")
+        local.update(lv)
+    sim = pyrandaSim(rootname, serial["mesh"], precision=precision, device=device)
+    known = {"pyrandaTimestep": pyrandaTimestep, "pyrandaBC": pyrandaBC}
+    for pack in serial["packages"]:
+        base = pack.split(".")[-1]
+        if base not in known:
+            raise ValueError("restart needs package %s, which this library does not provide" % pack)
+        sim.addPackage(known[base](sim))
+    sim.sMap = serial["sMap"]
+    sim.EOM(serial["EOM"])
+    sim.setIC(serial["ICs"], addOnly=True)
+    sim.time = serial["time"]
+    sim.deltat = serial["deltat"]
+    sim.cycle = serial["cycle"]
+    sim.vizDumpHistory = serial.get("vizDumpHistory", [])
+    data = restart.read_blocks(dump, serial, (sim.nx, sim.ny, sim.nz))
+    scalars = set(serial.get("scalars", []))
+    for name in serial["vars"]:
+        if name in sim.variables:
+            if name in scalars:
+                sim.variables[name].data = torch.full((), float(data[name].flat[0]), dtype=torch.float64,
+                                                      device=sim.grid.device)
+            else:
+                sim.variables[name].data = sim.grid.field(numpy.ascontiguousarray(data[name]))
+    return [sim, local]
 
 
 def defaultMeshOptions():
@@ -336,6 +387,9 @@ class pyrandaSim:
 
     def addPackage(self, package):
         self.packages[package.name] = package
+        self.packagesRestart = getattr(self, "packagesRestart", [])
+        base = type(package).__module__.rsplit(".", 1)[-1]
+        self.packagesRestart.append("pyranda." + base)   # the reference's module name (pyranda.py:152)
         package.get_sMap()
         self.sMap.update(package.sMap)
 
@@ -551,6 +605,47 @@ class pyrandaSim:
             raise ValueError("mesh variable %s is not available on Cartesian meshes" % vname)
         return self.grid.mesh(table[vname])
 
+    # ---------------------------------------------------------------- restart
+    def writeRestart(self, ivars=None, suffix=None, wVars=None):
+        """pyranda.py:475-589: the simulation state in pyranda's restart format (pyranda_gb300.restart).
+
+        The directory is ``<name>/restart_<cycle>``; ivars (a dict) adds
+        numbers, strings, lists and numpy arrays of the caller to the restart.
+        """
+        from . import restart
+        wVars = list(wVars) if wVars else list(self.variables)
+        dump = restart.restart_dir(self.name, self.cycle, suffix)
+        os.makedirs(dump, exist_ok=True)
+        serial = {}
+        if ivars:
+            serial["local_vars"] = {"numpyArrays": {}}
+            for k, v in ivars.items():
+                if isinstance(v, numpy.ndarray):
+                    fn = os.path.join(dump, k)
+                    serial["local_vars"]["numpyArrays"][k] = fn
+                    numpy.save(fn, v)
+                elif v is None or isinstance(v, (str, int, float, bool, list, dict)):
+                    serial["local_vars"][k] = v
+        mesh = dict(self.meshOptions)
+        mesh["function"] = None
+        nx, ny, nz = self.nx, self.ny, self.nz
+        serial.update({
+            "mesh": mesh, "EOM": getattr(self, "eom", ""), "ICs": getattr(self, "ics", ""),
+            "decomp": [1, 1, 1],
+            "procMap": {"0-g1": numpy.zeros(3, dtype=numpy.int32),
+                        "0-gn": numpy.array([nx - 1, ny - 1, nz - 1], dtype=numpy.int32)},
+            "packages": list(getattr(self, "packagesRestart", [])),
+            "time": _num(self.time), "deltat": _num(self.deltat), "cycle": int(self.cycle),
+            "vizDumpHistory": list(getattr(self, "vizDumpHistory", [])), "sMap": dict(self.sMap)})
+        arrays = {}
+        for n in wVars:
+            d = self.variables[n].data
+            arrays[n] = self.variables[n].numpy() if isinstance(d, torch.Tensor) and d.dim() > 0 else _num(d)
+        # which variables were single numbers (an extra key; the reference's reader ignores it)
+        serial["scalars"] = sorted(n for n in wVars if not isinstance(arrays[n], numpy.ndarray))
+        restart.write_files(dump, serial, arrays, (nx, ny, nz))
+        return dump
+
     # --------------------------------------------------------------- stepping
     def _unalias(self):
         """Give every variable its own storage (the RK update works in place)."""
@@ -632,8 +727,11 @@ class pyrandaSim:
                 eq.RHS = eval("lambda self: " + eq.sRHS, EVAL_GLOBALS)
 
     def _dt_tensor(self, dt):
+        """The time step as a device scalar (a field -- e.g. a reference restart's dt -- gives its first value)."""
         if isinstance(dt, torch.Tensor):
-            return dt.to(device=self.grid.device, dtype=torch.float64).reshape(())
+            return dt.to(device=self.grid.device, dtype=torch.float64).reshape(-1)[0].reshape(())
+        if isinstance(dt, numpy.ndarray):
+            return torch.full((), float(dt.flat[0]), dtype=torch.float64, device=self.grid.device)
         return torch.full((), float(dt), dtype=torch.float64, device=self.grid.device)
 
     def _time_tensor(self, time):
@@ -732,8 +830,21 @@ class pyrandaSim:
         for n, old in before.items():
             if isinstance(old, torch.Tensor):
                 self.variables[n].data = old
+        self._g_storage = {n: t for n, t in before.items() if isinstance(t, torch.Tensor)}
         self._graph = g
         # the capture itself did not advance the state: replay once for this step
+
+    def sync_graph_storage(self):
+        """After eager work on a graph-recorded simulation: put every variable back into the storage the graph reads."""
+        for n, t in getattr(self, "_g_storage", {}).items():
+            v = self.variables.get(n)
+            if v is None or v.data is t:
+                continue
+            if isinstance(v.data, torch.Tensor) and (v.data.shape == t.shape or t.dim() == 0):
+                t.copy_(v.data.reshape(t.shape) if t.dim() == 0 else v.data)
+            elif not isinstance(v.data, torch.Tensor):
+                t.fill_(float(v.data))
+            v.data = t
 
     def _capture_body(self, before):
         """The recorded work: one eager step, then the rebound variables copied back into the replay's storage."""

@@ -134,7 +134,8 @@ def _shock(eom, mode, model, shape=(64, 32, 32), mach=1.8, amp=0.05):
                                 precision="fp64")
 
 
-def test_fallback_flag_reruns_the_step_with_the_plain_closure():
+@pytest.mark.parametrize("graphs", [False, True])
+def test_fallback_flag_reruns_the_step_with_the_plain_closure(graphs):
     from pyranda_gb300.learned_lad import learned_shock_eom
     m = _model(5)
     m.ylo, m.yhi = [1e9, 1e9], [2e9, 2e9]   # every prediction is out of range
@@ -143,13 +144,16 @@ def test_fallback_flag_reruns_the_step_with_the_plain_closure():
     b = _shock(learned_shock_eom(), "plain", m)
     lad = a.packages["LAD"]
     lad.mode = "learned"
+    if graphs:
+        a.use_graphs(True)
     ta, tb = 0.0, 0.0
-    for _ in range(2):
-        dt = a.variables["dt"].data.clone()
+    for _ in range(3):
+        dt = b.variables["dt"].data.clone()
         ta = lad.step(ta, dt)
         tb = b.rk4(tb, dt)
-    assert lad.fallbacks == 2
-    assert torch.equal(a.variables["rho"].data, b.variables["rho"].data)
+    assert lad.fallbacks == 3
+    for name in ("rho", "rhou", "Et", "beta", "kappa"):
+        assert torch.equal(a.variables[name].data, b.variables[name].data), name
 
 
 @pytest.mark.slow

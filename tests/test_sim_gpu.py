@@ -193,3 +193,24 @@ def test_shock_interface_full_size_runs():
         assert float(rho.min()) > 0.5 and float(p.min()) > 0.5
         del ss
         torch.cuda.empty_cache()
+
+
+def test_restart_round_trip(tmp_path, monkeypatch):
+    """A run interrupted by writeRestart / pyrandaRestart continues bit for bit."""
+    from pyranda_gb300 import pyrandaRestart, pyrandaSim, pyrandaTimestep
+    from pyranda_gb300.problems import build_tgv
+    monkeypatch.chdir(tmp_path)
+    a = build_tgv(pyrandaSim, 24, lambda s: s.addPackage(pyrandaTimestep(s)), silent=True)
+    t = 0.0
+    for _ in range(3):
+        t = a.rk4(t, a.variables["dt"].data * 0.5)
+    a.writeRestart(ivars={"note": "x", "arr": numpy.arange(3.0)})
+    [b, local] = pyrandaRestart(a.name)
+    assert local["note"] == "x" and numpy.array_equal(local["arr"], numpy.arange(3.0))
+    assert b.cycle == a.cycle and b.time == pytest.approx(float(t))
+    ta, tb = float(t), float(b.time)
+    for _ in range(2):
+        ta = a.rk4(ta, a.variables["dt"].data * 0.5)
+        tb = b.rk4(tb, b.variables["dt"].data * 0.5)
+    for name in ("rho", "rhou", "rhov", "rhow", "Et"):
+        assert torch.equal(a.variables[name].data, b.variables[name].data), name
