@@ -7,7 +7,8 @@ points (inputs, weights, hidden activations), the network
   layout [w1 | w2 | w3 | w4 | b1 | b2 | b3 | b4] (weight rows = output unit),
 its mean-squared-error loss over rows x outputs and the gradient of that loss
 with respect to every parameter, and the 27-point feature gather:
-  features of point (i, j, k) = div*D at the 27 neighbours (di, dj, dk in
+  features of point (i, j, k) = f32(div)*f32(D) (an FP32 product) at the 27
+  neighbours (di, dj, dk in
   {-1, 0, 1}, index s = (di+1) + 3 (dj+1) + 9 (dk+1)), then |grad rho|*D at
   the same neighbours, then D (the largest mesh spacing), then zeros up to
   64; periodic directions wrap,
@@ -107,8 +108,9 @@ def features(div, gmag, periodic, delta):
     for s in range(27):
         di, dj, dk = s % 3 - 1, (s // 3) % 3 - 1, s // 9 - 1
         cols.append((idx(ii, di, nx, periodic[0]), idx(jj, dj, ny, periodic[1]), idx(kk, dk, nz, periodic[2])))
+    d32 = numpy.float32(delta)
     for s, (a, b, c) in enumerate(cols):
-        out[:, s] = (div[a, b, c] * delta).ravel(order="F")
-        out[:, 27 + s] = (gmag[a, b, c] * delta).ravel(order="F")
-    out[:, NIN - 1] = delta
+        out[:, s] = (div[a, b, c].astype(numpy.float32) * d32).ravel(order="F")
+        out[:, 27 + s] = (gmag[a, b, c].astype(numpy.float32) * d32).ravel(order="F")
+    out[:, NIN - 1] = d32
     return out.astype(numpy.float32).astype(numpy.float64)

@@ -162,26 +162,32 @@ __device__ __forceinline__ uint32_t tf32_bits(float x) {
   return (__float_as_uint(x) + 0x1000u) & 0xFFFFE000u;
 }
 
-// The four differences w_k = v_k - v_{k-1}, k = kb .. kb+3, of one line (v at
-// p[k * stride]) as TF32 hi / lo.  w_0 is the wrap difference v_0 - v_{n-1}
-// on periodic lines and 0 otherwise; k >= n gives 0.  Each v is split into
-// FP32 value + residual first, so a difference keeps ~48 bits of v before
-// its own rounding to FP32.
-template <int UNIT>
-__device__ __forceinline__ void stage_differences(const double* __restrict__ p, bool ok, int kb, int n, int periodic,
-                                                  uint32_t* h, uint32_t* l, int stride = 1) {
-  const int64_t st = UNIT ? 1 : stride;
-  float2 prev = make_float2(0.f, 0.f);
-  if (ok) {
-    const int km1 = (kb > 0) ? kb - 1 : (periodic ? n - 1 : -1);
-    if (km1 >= 0 && km1 < n) prev = split_f64(__ldg(p + km1 * st));
-  }
+// One staging item: v_{kb-1} and v_kb .. v_kb+3 of one line (v at p[k * st]).
+struct Item {
+  double v[5];
+};
+
+__device__ __forceinline__ void load_item(const double* __restrict__ p, bool ok, int kb, int n, int periodic,
+                                          int64_t st, Item& it) {
+  const int km1 = (kb > 0) ? kb - 1 : (periodic ? n - 1 : -1);
+  it.v[0] = (ok && km1 >= 0 && km1 < n) ? __ldg(p + km1 * st) : 0.0;
+#pragma unroll
+  for (int j = 0; j < 4; j++) it.v[j + 1] = (ok && kb + j < n) ? __ldg(p + (kb + j) * st) : 0.0;
+}
+
+// The four differences w_k = v_k - v_{k-1}, k = kb .. kb+3, as TF32 hi / lo.
+// w_0 is the wrap difference v_0 - v_{n-1} on periodic lines and 0
+// otherwise; k >= n gives 0.  Each v is split into FP32 value + residual
+// first, so a difference keeps ~48 bits of v before its own rounding to FP32.
+__device__ __forceinline__ void difference_item(const Item& it, bool ok, int kb, int n, int periodic, uint32_t* h,
+                                                uint32_t* l) {
+  float2 prev = split_f64(it.v[0]);
 #pragma unroll
   for (int j = 0; j < 4; j++) {
     const int k = kb + j;
     float f = 0.0f;
     if (ok && k < n) {
-      const float2 v = split_f64(__ldg(p + k * st));
+      const float2 v = split_f64(it.v[j + 1]);
       if (k > 0 || periodic) f = (v.x - prev.x) + (v.y - prev.y);
       prev = v;
     }
@@ -271,6 +277,20 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
   const int kchunks = op.kchunks;
   bool bad = false;
   int issued = -1, committed = -1;  // thread 0: last chunk whose D copy / MMAs were issued
+  // this thread's staging items: the same (row, 16-byte chunk) in every K chunk
+  constexpr int kItems = 1024 / kDenseThreads;
+  int item_r[kItems], item_q[kItems];
+#pragma unroll
+  for (int i = 0; i < kItems; i++) {
+    const int idx = tid + kDenseThreads * i;
+    item_r[i] = (ORIENT == 0) ? (idx >> 3) : (idx & 127);
+    item_q[i] = (ORIENT == 0) ? (idx & 7) : (idx >> 7);
+  }
+  const int64_t vst = (ORIENT == 0) ? 1 : st;
+  Item cur[kItems], nxt[kItems];
+#pragma unroll
+  for (int i = 0; i < kItems; i++)
+    load_item(P.in + s_base[item_r[i]], item_r[i] < tile.nlines, item_q[i] * 4, n, op.periodic, vst, cur[i]);
 
   for (int c = 0; c < kchunks && !bad; c++) {
     const int s = c & 1;
@@ -279,6 +299,13 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
     uint8_t* v_lo = st_base + vbytes;
     uint8_t* d_hi = st_base + 2 * vbytes;
     uint8_t* d_lo = d_hi + dbytes;
+    // the next chunk's loads go out first, so they are in flight across this chunk's work
+    if (c + 1 < kchunks) {
+#pragma unroll
+      for (int i = 0; i < kItems; i++)
+        load_item(P.in + s_base[item_r[i]], item_r[i] < tile.nlines, (c + 1) * kKC + item_q[i] * 4, n, op.periodic,
+                  vst, nxt[i]);
+    }
     // the MMAs that last read this stage (chunk c - 2) must be complete
     if (c >= 2 && !mbar_wait(&mma_bar[s], ((c >> 1) + 1) & 1)) bad = true;
     if (__syncthreads_or(bad)) break;
@@ -289,33 +316,20 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
       bulk_copy(d_lo, plane + (size_t)op.rows * 32 + (size_t)drow0 * 32, dcopy, &full_bar[s]);
       issued = c;
     }
-    // stage V: 16-byte chunks of 4 consecutive k, split into TF32 hi / lo
+    // stage V: 16-byte chunks of 4 consecutive k (differences, split into TF32 hi / lo)
     const int k0 = c * kKC;
-    if (ORIENT == 0) {
 #pragma unroll
-      for (int i = 0; i < 1024 / kDenseThreads; i++) {  // 128 rows x 8 chunks
-        const int idx = tid + kDenseThreads * i;
-        const int r = idx >> 3, q = idx & 7;
-        const bool ok = r < tile.nlines;
-        uint32_t h[4], l[4];
-        stage_differences<1>(P.in + s_base[r], ok, k0 + q * 4, n, op.periodic, h, l);
+    for (int i = 0; i < kItems; i++) {
+      const int r = item_r[i], q = item_q[i];
+      uint32_t h[4], l[4];
+      difference_item(cur[i], r < tile.nlines, k0 + q * 4, n, op.periodic, h, l);
+      if (ORIENT == 0 || r < vrows) {
         *reinterpret_cast<uint4*>(v_hi + swz(r, q)) = make_uint4(h[0], h[1], h[2], h[3]);
         *reinterpret_cast<uint4*>(v_lo + swz(r, q)) = make_uint4(l[0], l[1], l[2], l[3]);
       }
-    } else {
-#pragma unroll
-      for (int i = 0; i < 1024 / kDenseThreads; i++) {  // 128 rows x 8 chunks
-        const int idx = tid + kDenseThreads * i;
-        const int r = idx & 127, q = idx >> 7;
-        if (r < vrows) {
-          const bool ok = r < tile.nlines;
-          uint32_t h[4], l[4];
-          stage_differences<0>(P.in + s_base[r], ok, k0 + q * 4, n, op.periodic, h, l, st);
-          *reinterpret_cast<uint4*>(v_hi + swz(r, q)) = make_uint4(h[0], h[1], h[2], h[3]);
-          *reinterpret_cast<uint4*>(v_lo + swz(r, q)) = make_uint4(l[0], l[1], l[2], l[3]);
-        }
-      }
     }
+#pragma unroll
+    for (int i = 0; i < kItems; i++) cur[i] = nxt[i];
     fence_proxy_async();
     __syncthreads();
     if (tid == 0) {

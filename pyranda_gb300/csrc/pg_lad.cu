@@ -30,6 +30,7 @@
 #include <cstdint>
 
 #include "pg_internal.h"
+#include "pg_sweep.cuh"  // d2f_bits: FP64 -> FP32 without the FP64 pipe
 
 namespace pg {
 namespace {
@@ -38,7 +39,7 @@ constexpr int kIn = PG_LAD_IN;        // 55 features
 constexpr int kK = PG_LAD_K;          // 64 padded inputs
 constexpr int kH = PG_LAD_HIDDEN;     // 64
 constexpr int kOut = PG_LAD_OUT;      // 2
-constexpr int kInferThreads = 128;    // 4 warps, 16 points per warp per pass
+constexpr int kInferThreads = 256;    // 8 warps x 16 points = one 128-point row tile
 constexpr int kTrainRows = 64;        // rows of a training CTA
 constexpr int kTrainThreads = 256;
 
@@ -52,13 +53,13 @@ __device__ __forceinline__ int wrapc(int i, int n, int per) {
 __device__ __forceinline__ float feature(const double* __restrict__ div, const double* __restrict__ gmag,
                                          const LadGrid& g, int i, int j, int k, int f) {
   if (f >= kIn) return 0.0f;
-  if (f == kIn - 1) return (float)g.delta;
+  if (f == kIn - 1) return (float)g.delta;  // raw features are f32(v) * f32(D), in FP32
   const int s = f % 27;
   const int di = s % 3 - 1, dj = (s / 3) % 3 - 1, dk = s / 9 - 1;
   const int64_t p = (int64_t)wrapc(i + di, g.n[0], g.per[0]) +
                     (int64_t)g.n[0] * (wrapc(j + dj, g.n[1], g.per[1]) + (int64_t)g.n[1] * wrapc(k + dk, g.n[2], g.per[2]));
   const double v = (f < 27) ? div[p] : gmag[p];
-  return (float)(v * g.delta);
+  return d2f_bits(v) * (float)g.delta;
 }
 
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
@@ -83,7 +84,6 @@ struct InferSmem {
   __nv_bfloat16 w4[8][kH + 8];   // rows >= kOut are zero
   float b1[kH], b2[kH], b3[kH], b4[8];
   float xm[kK], xs[kK];          // input mean and 1/std
-  __nv_bfloat16 x[4][16][kK + 8];  // per-warp input tile
 };
 
 // one hidden layer: A fragments (4 k-tiles) -> ReLU(W A + b) as next A fragments
@@ -116,15 +116,22 @@ constexpr int kW1 = 0, kW2 = kH * kK, kW3 = kW2 + kH * kH, kW4 = kW3 + kH * kH, 
               kB2 = kB1 + kH, kB3 = kB2 + kH, kB4 = kB3 + kH;
 static_assert(kB1 == PG_LAD_NWEIGHT && kB4 + kOut == PG_LAD_NPARAM, "parameter layout");
 
+// One CTA = 128 consecutive x-points of one (j, k) row.  The 3 x 3 rows
+// around it (130 points each: one halo point per side) of div*D and
+// |grad rho|*D are staged once in shared memory; every warp then builds the
+// features of its 16 points from there and runs the network.
+constexpr int kTileX = 128;
+constexpr int kHaloX = kTileX + 2;
+
 __global__ void __launch_bounds__(kInferThreads) lad_infer_kernel(const LadInferArgs A) {
   extern __shared__ __align__(16) unsigned char lad_smem[];
   InferSmem& S = *reinterpret_cast<InferSmem*>(lad_smem);
+  float (*nb)[9][kHaloX] = reinterpret_cast<float (*)[9][kHaloX]>(lad_smem + sizeof(InferSmem));
   const pg_lad_model& M = A.model;
   const __nv_bfloat16* W = reinterpret_cast<const __nv_bfloat16*>(M.wbf16);
   const float* P = M.params;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int g = lane >> 2, t = lane & 3;
-  // network -> shared memory
   for (int i = tid; i < kH * kK; i += blockDim.x) S.w1[i / kK][i % kK] = W[kW1 + i];
   for (int i = tid; i < kH * kH; i += blockDim.x) {
     S.w2[i / kH][i % kH] = W[kW2 + i];
@@ -142,63 +149,77 @@ __global__ void __launch_bounds__(kInferThreads) lad_infer_kernel(const LadInfer
     S.xm[i] = M.xmean[i];
     S.xs[i] = M.xinvstd[i];
   }
-  __syncthreads();
   const LadGrid& G = A.grid;
-  const int64_t npts = (int64_t)G.n[0] * G.n[1] * G.n[2];
+  const int nx = G.n[0], ny = G.n[1], nz = G.n[2];
+  const int nxb = (nx + kTileX - 1) / kTileX;
+  const long long ntiles = (long long)nxb * ny * nz;
+  const float dl = (float)G.delta;
   bool out_of_range = false;
-  // each warp walks 16-point tiles
-  for (int64_t base = ((int64_t)blockIdx.x * 4 + warp) * 16; base < npts; base += (int64_t)gridDim.x * 64) {
-    // gather 16 points x 64 inputs (2 per lane per row pass)
-    for (int r = 0; r < 16; r++) {
-      const int64_t p = base + r;
-      float f0 = 0.f, f1 = 0.f;
-      if (p < npts) {
-        const int i = (int)(p % G.n[0]);
-        const int j = (int)((p / G.n[0]) % G.n[1]);
-        const int k = (int)(p / ((int64_t)G.n[0] * G.n[1]));
-        const int c0 = 2 * lane, c1 = 2 * lane + 1;
-        f0 = (feature(A.div, A.gmag, G, i, j, k, c0) - S.xm[c0]) * S.xs[c0];
-        f1 = (feature(A.div, A.gmag, G, i, j, k, c1) - S.xm[c1]) * S.xs[c1];
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int xb = (int)(tile % nxb);
+    const long long row = tile / nxb;
+    const int j = (int)(row % ny), k = (int)(row / ny);
+    const int x0 = xb * kTileX;
+    __syncthreads();  // the previous tile's neighbourhood is no longer read
+    for (int q = tid; q < 2 * 9 * kHaloX; q += blockDim.x) {
+      const int f = q / (9 * kHaloX), rem = q - f * 9 * kHaloX;
+      const int rr = rem / kHaloX, xx = rem - rr * kHaloX;
+      const int jj = wrapc(j + rr % 3 - 1, ny, G.per[1]), kk = wrapc(k + rr / 3 - 1, nz, G.per[2]);
+      const int x = wrapc(x0 - 1 + xx, nx, G.per[0]);
+      const int64_t p = (int64_t)x + (int64_t)nx * (jj + (int64_t)ny * kk);
+      nb[f][rr][xx] = d2f_bits(f == 0 ? A.div[p] : A.gmag[p]) * dl;
+    }
+    __syncthreads();
+    const int lx0 = warp * 16;
+    if (x0 + lx0 < nx) {
+      // A fragments straight from the neighbourhood: column c of row r is feature c of point lx0 + r
+      auto feat = [&](int r, int c) -> float {
+        float v;
+        if (c < 2 * 27) {
+          const int f = c / 27, s2 = c - f * 27;
+          v = nb[f][s2 / 3][lx0 + r + 1 + s2 % 3 - 1];
+        } else {
+          v = (c == kIn - 1) ? dl : 0.0f;
+        }
+        return (v - S.xm[c]) * S.xs[c];
+      };
+      uint32_t a0[4][4], a1[4][4];
+#pragma unroll
+      for (int kt = 0; kt < 4; kt++) {
+        const int c = kt * 16 + 2 * t;
+        a0[kt][0] = pack_bf16(feat(g, c), feat(g, c + 1));
+        a0[kt][1] = pack_bf16(feat(g + 8, c), feat(g + 8, c + 1));
+        a0[kt][2] = pack_bf16(feat(g, c + 8), feat(g, c + 9));
+        a0[kt][3] = pack_bf16(feat(g + 8, c + 8), feat(g + 8, c + 9));
       }
-      *reinterpret_cast<uint32_t*>(&S.x[warp][r][2 * lane]) = pack_bf16(f0, f1);
-    }
-    __syncwarp();
-    uint32_t a0[4][4], a1[4][4];
+      layer_relu<4>(a0, a1, S.w1, S.b1, g, t);
+      layer_relu<4>(a1, a0, S.w2, S.b2, g, t);
+      layer_relu<4>(a0, a1, S.w3, S.b3, g, t);
+      float c[4] = {S.b4[2 * t], S.b4[2 * t + 1], S.b4[2 * t], S.b4[2 * t + 1]};
 #pragma unroll
-    for (int kt = 0; kt < 4; kt++) {
-      a0[kt][0] = *reinterpret_cast<const uint32_t*>(&S.x[warp][g][kt * 16 + 2 * t]);
-      a0[kt][1] = *reinterpret_cast<const uint32_t*>(&S.x[warp][g + 8][kt * 16 + 2 * t]);
-      a0[kt][2] = *reinterpret_cast<const uint32_t*>(&S.x[warp][g][kt * 16 + 2 * t + 8]);
-      a0[kt][3] = *reinterpret_cast<const uint32_t*>(&S.x[warp][g + 8][kt * 16 + 2 * t + 8]);
-    }
-    __syncwarp();
-    layer_relu<4>(a0, a1, S.w1, S.b1, g, t);
-    layer_relu<4>(a1, a0, S.w2, S.b2, g, t);
-    layer_relu<4>(a0, a1, S.w3, S.b3, g, t);
-    float c[4] = {S.b4[2 * t], S.b4[2 * t + 1], S.b4[2 * t], S.b4[2 * t + 1]};
+      for (int kt = 0; kt < 4; kt++) {
+        const uint32_t w0 = *reinterpret_cast<const uint32_t*>(&S.w4[g][kt * 16 + 2 * t]);
+        const uint32_t w1 = *reinterpret_cast<const uint32_t*>(&S.w4[g][kt * 16 + 2 * t + 8]);
+        mma_bf16(c, a1[kt], w0, w1);
+      }
+      // lanes with t == 0 hold outputs 0 and 1 of rows g and g + 8
+      if (t == 0) {
 #pragma unroll
-    for (int kt = 0; kt < 4; kt++) {
-      const uint32_t w0 = *reinterpret_cast<const uint32_t*>(&S.w4[g][kt * 16 + 2 * t]);
-      const uint32_t w1 = *reinterpret_cast<const uint32_t*>(&S.w4[g][kt * 16 + 2 * t + 8]);
-      mma_bf16(c, a1[kt], w0, w1);
-    }
-    // lanes with t == 0 hold outputs 0 and 1 of rows g and g + 8
-    if (t == 0) {
-#pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const int64_t p = base + g + 8 * h;
-        if (p < npts) {
-          const float y0 = c[2 * h], y1 = c[2 * h + 1];
-          out_of_range |= !(y0 >= M.ylo[0] && y0 <= M.yhi[0] && y1 >= M.ylo[1] && y1 <= M.yhi[1]);
-          const double rho = A.rho[p];
-          const double d = G.delta;
-          // artificial viscosity and conductivity are non-negative (the plain operators are)
-          A.beta[p] = fmax(0.0, (double)y0 * M.ys[0] + M.ym[0]) * rho * d;
-          A.kappa[p] = fmax(0.0, (double)y1 * M.ys[1] + M.ym[1]) * rho * A.cv * d * d / A.dt[0];
+        for (int h = 0; h < 2; h++) {
+          const int x = x0 + lx0 + g + 8 * h;
+          if (x < nx) {
+            const int64_t p = (int64_t)x + (int64_t)nx * (j + (int64_t)ny * k);
+            const float y0 = c[2 * h], y1 = c[2 * h + 1];
+            out_of_range |= !(y0 >= M.ylo[0] && y0 <= M.yhi[0] && y1 >= M.ylo[1] && y1 <= M.yhi[1]);
+            const double rho = A.rho[p];
+            const double d = G.delta;
+            // artificial viscosity and conductivity are non-negative (the plain operators are)
+            A.beta[p] = fmax(0.0, (double)y0 * M.ys[0] + M.ym[0]) * rho * d;
+            A.kappa[p] = fmax(0.0, (double)y1 * M.ys[1] + M.ym[1]) * rho * A.cv * d * d / A.dt[0];
+          }
         }
       }
     }
-    __syncwarp();
   }
   if (__syncthreads_or(out_of_range) && tid == 0) atomicExch(A.flag, 1);
 }
@@ -406,7 +427,7 @@ int lad_check(const char* what) {
 
 int launch_lad_infer(const LadInferArgs& a, void* stream) {
   static bool attr = false;
-  const int smem = (int)sizeof(InferSmem);
+  const int smem = (int)(sizeof(InferSmem) + 2 * 9 * kHaloX * sizeof(float));
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(lad_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) {
@@ -415,9 +436,8 @@ int launch_lad_infer(const LadInferArgs& a, void* stream) {
     }
     attr = true;
   }
-  const int64_t npts = (int64_t)a.grid.n[0] * a.grid.n[1] * a.grid.n[2];
-  const int64_t tiles = (npts + 63) / 64;
-  const int blocks = (int)(tiles < 152 * 8 ? tiles : 152 * 8);
+  const int64_t tiles = (int64_t)((a.grid.n[0] + kTileX - 1) / kTileX) * a.grid.n[1] * a.grid.n[2];
+  const int blocks = (int)(tiles < 152 * 4 ? tiles : 152 * 4);
   lad_infer_kernel<<<blocks, kInferThreads, smem, (cudaStream_t)stream>>>(a);
   count_launch();
   return lad_check("lad inference");

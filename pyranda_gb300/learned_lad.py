@@ -276,32 +276,32 @@ class pyrandaLearnedLAD(pyrandaPackage):
         return [beta, kappa]
 
     def _state_names(self):
-        """The state a step starts from: conserved variables, and the variables the
-        algebraic equations read before writing (or never write), e.g. :dt: in kappa."""
+        """The state a step reads before writing: the conserved variables, the
+        variables the PDE right-hand sides read (the first stage uses them as
+        the previous step left them), and the variables the algebraic
+        equations read before writing or never write (e.g. :dt: in kappa)."""
         if getattr(self, "_state", None) is None:
             from .pyrandaUtils import findVar
             ss = self.pyranda
-            written, lagged = set(), set()
+            need = set(ss.conserved)
+            written = set()
             for eq in ss.equations:
-                if eq.kind != "ALG":
-                    continue
                 rhs = eq.eqstr.split("=", 1)[1] if eq.LHS else eq.eqstr
-                for v in findVar(rhs, "scalar"):
-                    if v not in written and v not in ss.conserved:
-                        lagged.add(v)
+                if eq.kind == "PDE":
+                    need.update(findVar(rhs, "scalar"))
+                    continue
+                need.update(v for v in findVar(rhs, "scalar") if v not in written)
                 written.update(eq.LHS or [])
-            self._state = list(ss.conserved) + sorted(v for v in lagged if v in ss.variables)
+            self._state = sorted(v for v in need if v in ss.variables)
         return self._state
 
     def step(self, time, dt):
         """One rk4 step with the learned closure; if the flag was raised, redo it with the plain closure.
 
-        The step's starting state (conserved variables plus the variables the
-        algebraic equations read before writing) is kept.  On a fallback it
-        is restored, the algebraic state is re-evaluated from it with the
-        plain closure (pyranda.py:393-428), and the step is run again with the
-        plain closure (eagerly; a recorded graph's storage is refreshed
-        afterwards).
+        What the step reads before writing is kept (``_state_names``).  On a
+        fallback it is restored and the step runs again with the plain
+        closure (eagerly; a recorded graph's storage is refreshed afterwards),
+        so the result equals a plain-closure step from the same state.
         """
         ss = self.pyranda
         saved = {n: ss.variables[n].data.clone() for n in self._state_names()
@@ -322,7 +322,6 @@ class pyrandaLearnedLAD(pyrandaPackage):
         ss._graphs_enabled = False
         self.mode = "plain"
         try:
-            ss.updateVars()
             t = ss.rk4(time, dt_saved)
         finally:
             self.mode = "learned"
