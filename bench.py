@@ -436,10 +436,11 @@ def ensemble_throughput(args):
         return dt
 
     res = {}
-    for prec, graphs in (("fp64", False), ("fp32", True)):
+    for prec, graphs in (("fp64", False), ("fp32", True), ("auto", True)):
         ens = problems.build_kh_ensemble(pyrandaEnsemble, sizes, packs, silent=True, precision=prec)
         if graphs:
             ens.use_graphs(True)
+            ens.use_fusion(True)
         dt0 = ens.variables["dt"].data.clone()
         dt = run(ens, w, dt0.clone())
         torch.cuda.synchronize()
@@ -449,13 +450,15 @@ def ensemble_throughput(args):
         e.record()
         torch.cuda.synchronize()
         sec = s.elapsed_time(e) / 1e3
-        out[prec + ("+graphs" if graphs else "")] = {"value": round(npts * k / sec / 1e6, 3), "unit": UNIT,
-                                                     "ms_per_step": round(sec / k * 1e3, 3)}
+        out[prec + ("+graphs+fusion" if graphs else "")] = {"value": round(npts * k / sec / 1e6, 3), "unit": UNIT,
+                                                            "ms_per_step": round(sec / k * 1e3, 3)}
         res[prec] = ens
-    # the two precisions took the same number of steps from the same IC
-    out["fp32_vs_fp64_rel_l2"] = {n: float(((res["fp32"].variables[n].data - res["fp64"].variables[n].data).norm()
-                                            / res["fp64"].variables[n].data.norm()).item())
-                                  for n in ("rho", "rhou", "rhov", "Et")}
+    # every precision took the same number of steps from the same IC
+    for p in ("fp32", "auto"):
+        out["%s_vs_fp64_rel_l2" % p] = {n: float(((res[p].variables[n].data - res["fp64"].variables[n].data).norm()
+                                                 / res["fp64"].variables[n].data.norm()).item())
+                                       for n in ("rho", "rhou", "rhov", "Et")}
+    del res["auto"]
     g = res["fp32"].grid
     v = res["fp32"].variables["rho"].data
     o = g.empty()

@@ -149,19 +149,68 @@ __global__ void courant_partial(const double* __restrict__ u, const double* __re
 
 __global__ void invert_scalar(double* p) { *p = 1.0 / *p; }
 
-// diff: min(rho * GridLen^2 / max(1e-12, bulk))
-__global__ void diff_partial(const double* __restrict__ bulk, const double* __restrict__ rho, double gl,
-                             int64_t n, double* __restrict__ partial) {
-  double acc = DBL_MAX;
+// The diffusion limit min(rho GridLen^2 / max(1e-12, bulk)) in two passes.
+// FP64 division runs on GB300's slow FP64 pipe (~10 instructions each), so
+// pass 1 estimates every quotient in FP32 (integer FP64->FP32 conversion,
+// correctly rounded FP32 divide; relative error < 4e-7) and pass 2 evaluates
+// the FP64 quotient only where the estimate is within 1e-5 of the smallest
+// estimate: the true minimiser is always among those, so the result is the
+// exact FP64 minimum.  Points whose values are not finite or beyond 2^60 in
+// magnitude are always evaluated exactly.  As in the one-pass form, NaN in
+// rho makes the result NaN and a NaN bulk is floored by fmax.
+struct DiffEst {
+  float e;
+  bool exact;
+  bool nan;
+};
+
+__device__ __forceinline__ float d2f_int(double d) {  // FP64 -> FP32 by integer operations
+  const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+  const unsigned mag = hi & 0x7fffffffu;
+  unsigned f = ((mag - (896u << 20)) << 3) | (lo >> 29);
+  f += (lo >> 28) & 1u;
+  f = (mag < (897u << 20)) ? 0u : f;
+  return __uint_as_float(f | (hi & 0x80000000u));
+}
+
+__device__ __forceinline__ DiffEst diff_estimate(double rho, double bulk, float gl2) {
+  const unsigned rh = (unsigned)__double2hiint(rho), rl = (unsigned)__double2loint(rho);
+  const unsigned bh = (unsigned)__double2hiint(bulk);
+  const unsigned re = (rh >> 20) & 0x7ffu, be = (bh >> 20) & 0x7ffu;
+  DiffEst d;
+  d.nan = (re == 0x7ffu) && (((rh & 0xfffffu) | rl) != 0u);
+  d.exact = (re >= 1023u + 60u) || (be >= 1023u + 60u);
+  d.e = (d2f_int(rho) * gl2) / fmaxf(1.0e-12f, d2f_int(bulk));
+  return d;
+}
+
+__global__ void diff_estimate_partial(const double* __restrict__ bulk, const double* __restrict__ rho, float gl2,
+                                      int64_t n, double* __restrict__ partial) {
+  float acc = FLT_MAX;
   bool nan = false;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double x = rho[i] * gl * gl / fmax(1.0e-12, bulk[i]);
-    nan |= (x != x);
-    acc = fmin(acc, x);
+    const DiffEst d = diff_estimate(rho[i], bulk[i], gl2);
+    nan |= d.nan;
+    if (!d.exact) acc = fminf(acc, d.e);
+  }
+  double v = block_reduce<2>((double)acc);
+  const int anynan = __syncthreads_or(nan);
+  if (threadIdx.x == 0) partial[blockIdx.x] = anynan ? NAN : v;
+}
+
+__global__ void diff_exact_partial(const double* __restrict__ bulk, const double* __restrict__ rho, double gl,
+                                   float gl2, int64_t n, const double* __restrict__ est_min,
+                                   double* __restrict__ partial) {
+  const double m = *est_min;
+  const float lim = (float)(m + fabs(m) * 1.0e-5 + 1.0e-38);
+  double acc = DBL_MAX;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double r = rho[i], b = bulk[i];
+    const DiffEst d = diff_estimate(r, b, gl2);
+    if (d.exact || d.e <= lim) acc = fmin(acc, r * gl * gl / fmax(1.0e-12, b));
   }
   acc = block_reduce<2>(acc);
-  const int anynan = __syncthreads_or(nan);
-  if (threadIdx.x == 0) partial[blockIdx.x] = anynan ? NAN : acc;
+  if (threadIdx.x == 0) partial[blockIdx.x] = (m != m) ? NAN : acc;
 }
 
 __global__ void finite_kernel(const double* __restrict__ in, int64_t n, int* flag) {
@@ -347,9 +396,13 @@ int launch_diff(const double* bulk, const double* rho, double gl, int64_t n, dou
                 void* stream) {
   const int g = grid_for(n) < kReduceBlocks ? grid_for(n) : kReduceBlocks;
   cudaStream_t s = (cudaStream_t)stream;
-  diff_partial<<<g, kThreads, 0, s>>>(bulk, rho, gl, n, partial);
+  // pass 1: FP32 estimates -> *out holds their minimum (or NaN)
+  diff_estimate_partial<<<g, kThreads, 0, s>>>(bulk, rho, (float)(gl * gl), n, partial);
   reduce_final<2><<<1, kThreads, 0, s>>>(partial, g, out);
-  count_launch();
+  // pass 2: the exact FP64 quotient where the estimate is within 1e-5 of that minimum
+  diff_exact_partial<<<g, kThreads, 0, s>>>(bulk, rho, gl, (float)(gl * gl), n, out, partial);
+  reduce_final<2><<<1, kThreads, 0, s>>>(partial, g, out);
+  count_launch(4);
   return check("diff");
 }
 

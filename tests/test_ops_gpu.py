@@ -221,3 +221,22 @@ def test_parcop_shim_numpy_roundtrip(oracle):
     assert numpy.array_equal(parcop.mesh_getgridlen(), o.mesh(6))
     with pytest.raises(ValueError):
         parcop.setup(2, 0, 0, 16, 16, 16, 1, 1, 1, 0, 0, 1, 0, 1, 0, 1, "SYMM", "NONE", "NONE", "NONE", "NONE", "NONE")
+
+
+def test_diff_is_exact(grids):
+    """The two-pass diffusion limit (FP32 candidates, FP64 quotients) equals the FP64 minimum bit for bit."""
+    g, o = grids[CASES[0]]
+    shape = CASES[0][0]
+    r = numpy.random.default_rng(3)
+    gl = min(o.spacing()[1])
+    cases = [(1.0 + r.random(shape), r.random(shape) * 1e-3),
+             (numpy.full(shape, 1.5), numpy.full(shape, 2e-3)),      # every point is a candidate
+             (1.0 + r.random(shape), numpy.zeros(shape)),            # floored bulk
+             (1.0 + r.random(shape), numpy.abs(r.standard_normal(shape)) * 1e5)]
+    for rho, bulk in cases:
+        ref = numpy.min(rho * gl * gl / numpy.maximum(1e-12, bulk))
+        assert float(g.diff(to_dev(bulk, torch), to_dev(rho, torch))) == ref
+    rho, bulk = cases[0]
+    rho = rho.copy()
+    rho[1, 2, 3] = float("nan")
+    assert numpy.isnan(float(g.diff(to_dev(bulk, torch), to_dev(rho, torch))))
