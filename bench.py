@@ -57,7 +57,7 @@ def parse():
     p.add_argument("--train-runs", type=int, default=20, help="shock-learned: training runs when training")
     p.add_argument("--train-iters", type=int, default=3000, help="shock-learned: Adam iterations when training")
     p.add_argument("--members", type=int, default=64, help="ensemble mode: number of members")
-    p.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "dense", "fp32-only"],
+    p.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "dense", "auto", "fp32-only"],
                    help="profile mode: arithmetic of the profiled step; step mode: 'fp32-only' skips the dense run")
     p.add_argument("--reps", type=int, default=20)
     return p.parse_args()
@@ -389,14 +389,18 @@ def shock_throughput(args):
 
     out = {"workload": "shock-interface 512x128x128, x one-sided, y/z periodic, LAD", "steps": args.steps}
     npts = 512 * 128 * 128
-    for prec, graphs in (("fp64", False), ("fp32", True)):
+    for prec, graphs in (("fp64", False), ("fp32", True), ("auto", True)):
         ss = problems.build_shock(pyrandaSim, 512, 128, 128, packs, silent=True, precision=prec)
         if graphs:
             ss.use_graphs(True)
+            ss.use_fusion(True)
         run_steps(ss, max(3, args.warmup))
         sec = time_steps(ss, args.steps, torch, False)
-        out[prec + ("+graphs" if graphs else "")] = {"value": round(job_value(npts, args.steps, 1, sec), 3),
-                                                     "unit": UNIT, "ms_per_step": round(sec / args.steps * 1e3, 3)}
+        key = prec + ("+graphs+fusion" if graphs else "")
+        out[key] = {"value": round(job_value(npts, args.steps, 1, sec), 3), "unit": UNIT,
+                    "ms_per_step": round(sec / args.steps * 1e3, 3)}
+        if prec == "auto":
+            out[key]["dense_plan"] = {"%s_%s" % k: v for k, v in ss.grid.dense_plan().items() if k[0] != "gf"}
         del ss
         torch.cuda.empty_cache()
     print(json.dumps(out), flush=True)
@@ -545,9 +549,10 @@ def shock_learned(args):
             ss.addPackage(LL.pyrandaLearnedLAD(ss, model, problems.CV, mode="plain"))
         # the initial state always comes from the plain closure; the run then uses `mode`
         ss = problems.build_shock(pyrandaSim, 512, 128, 128, packs, eom=LL.learned_shock_eom(), silent=True,
-                                  precision="fp32")
+                                  precision="auto")
         ss.packages["LAD"].mode = mode
         ss.use_graphs(True)
+        ss.use_fusion(True)
         return ss
 
     def advance(ss, step, t, t_end=None, nmax=None):
@@ -600,7 +605,28 @@ def shock_learned(args):
         torch.cuda.synchronize()
         closure_ms[mode] = round(s.elapsed_time(e) / args.reps, 4)
     lad.mode = "learned"
+    # its parts: |grad rho| (three d1 sweeps) and the fused feature-gather + network kernel
+    g = learned.grid
+    gm = LL.grad_magnitude(g, V["rho"].data)
+    beta, kappa = g.empty(), g.empty()
+    import ctypes
+    from pyranda_gb300.grid import _ptr, _stream
+    parts = {"grad_magnitude": lambda: LL.grad_magnitude(g, V["rho"].data),
+             "lad_kernel": lambda: g.lib.pg_lad_closure(g.h, ctypes.byref(lad._m), _ptr(V["div"].data), _ptr(gm),
+                                                       _ptr(V["rho"].data), _ptr(V["dt"].data.reshape(())),
+                                                       problems.CV, _ptr(beta), _ptr(kappa), _ptr(lad.flag),
+                                                       _stream())}
+    for name, f in parts.items():
+        f()
+        torch.cuda.synchronize()
+        s.record()
+        for _ in range(args.reps):
+            f()
+        e.record()
+        torch.cuda.synchronize()
+        closure_ms[name] = round(s.elapsed_time(e) / args.reps, 4)
     out["closure_ms_per_call"] = closure_ms
+    out["precision"] = learned.precision
     out["t_end"] = t_end
     out["plain_lad"] = {"value": round(npts * k_plain / t_plain / 1e6, 3), "unit": UNIT, "steps": k_plain,
                         "ms_per_step": round(t_plain / k_plain * 1e3, 3),
@@ -720,11 +746,17 @@ def main():
     dense_y = best != "fp32" and fast.grid.dense_plan()[("sf", "y")]
     kname = ("dense_kernel<lines as N, dir=y, store, add-back> (tcgen05 kind::tf32, 3 products)" if dense_y
              else "sweep_kernel<float,r4,periodic,implicit,addback,dir=y>")
+    if dense_y:   # the tensor-core work of the same launch: 3 TF32 products of 2n flops per point
+        roof_extra = {"tensor_tflops": round(3 * 2 * n * npts / dur / 1e12, 1),
+                      "tensor_peak_note": "TF32 dense nominal ~1100 TFLOP/s (no measured TF32 peak in MEASURED_PEAKS.json)"}
+    else:
+        roof_extra = {}
     roof = {"bound": "hbm", "kernel": kname,
             "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
             "traffic": None, "algorithmic_bytes_per_launch": 16 * npts,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s",
             "sweep_ms": {kk: round(vv * 1e3, 4) for kk, vv in sw.items()}}
+    roof.update(roof_extra)
 
     # ---- end to end: host state in pinned memory, copied in and out every step
     names = fast.conserved

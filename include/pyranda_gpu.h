@@ -89,6 +89,11 @@ int pg_destroy(pg_handle* h);
 int pg_device_status(pg_handle* h, int* status);
 /* Switch the arithmetic of later sweeps on this handle (pg_precision). */
 int pg_set_precision(pg_handle* h, int precision);
+/* Failure-detection self-test: launches one CTA that waits on a barrier
+ * nothing arrives at; after limit_ms (1..10000) the wait gives up and the
+ * handle's status word reads PG_ETIMEOUT (pg_device_status), as after a
+ * dense sweep whose copies or MMAs never complete.  The context stays usable. */
+int pg_wait_selftest(pg_handle* h, unsigned limit_ms, void* stream);
 /* The sweep plan of PG_DENSE / PG_AUTO: plan[op * 3 + dir] = 1 where the
  * dense kernel runs (op 0 d1, 1 d8, 2 compact filter, 3 Gaussian filter). */
 int pg_dense_plan(const pg_handle* h, int* plan);

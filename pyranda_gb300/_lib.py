@@ -67,6 +67,7 @@ SIGNATURES = [
     ("pg_device_status", I, [P, ctypes.POINTER(ctypes.c_int)]),
     ("pg_get_spacing", I, [P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     ("pg_dense_plan", I, [P, ctypes.POINTER(ctypes.c_int)]),
+    ("pg_wait_selftest", I, [P, ctypes.c_uint, P]),
     ("pg_last_error", ctypes.c_char_p, []),
     ("pg_version", ctypes.c_char_p, []),
     ("pg_d1", I, [P, I, D, D, P]),

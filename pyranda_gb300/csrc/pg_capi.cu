@@ -724,6 +724,11 @@ int pg_set_precision(pg_handle* h, int precision) {
   return set_precision(h->c, std::vector<GridInfo>{h->g}, precision);
 }
 
+int pg_wait_selftest(pg_handle* h, unsigned limit_ms, void* stream) {
+  if (!h || limit_ms == 0 || limit_ms > 10000) return PG_EINVAL;
+  return launch_wait_selftest(h->c.status, limit_ms, stream);
+}
+
 int pg_dense_plan(const pg_handle* h, int* plan) {
   if (!h || !plan) return PG_EINVAL;
   for (int k = 0; k < OPK_COUNT; k++)

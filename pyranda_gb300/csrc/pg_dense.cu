@@ -64,7 +64,7 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
 }
 
 // Bounded wait for the phase with the given parity; false on time-out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsigned long long limit_ns = kWaitNs) {
   const uint32_t a = smem_u32(bar);
   unsigned long long t0 = 0;
   for (unsigned it = 0;; it++) {
@@ -80,7 +80,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
     if ((it & 1023u) == 0) {
       const unsigned long long t = globaltimer();
       if (it == 0) t0 = t;
-      else if (t - t0 > kWaitNs) return false;
+      else if (t - t0 > limit_ns) return false;
     }
   }
 }
@@ -425,6 +425,21 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
   }
 }
 
+// The bounded-wait path on its own: one CTA waits on an mbarrier that
+// nothing ever arrives at, gives up after limit_ns and records PG_ETIMEOUT
+// in the status word -- what the dense kernel does when a copy or an MMA
+// never completes.  No copies are in flight and no tensor memory is held.
+__global__ void wait_selftest_kernel(int* status, unsigned long long limit_ns) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const bool ok = mbar_wait(&bar, 0, limit_ns);
+  if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicExch(status, (int)PG_ETIMEOUT);
+}
+
 template <int ORIENT, int DIR, int EPI, bool ADDBACK>
 int launch_one(const DParams& p, int ntiles, cudaStream_t st) {
   static bool attr = false;
@@ -465,6 +480,17 @@ int launch_epi(const DParams& p, int ntiles, int epi, bool addback, cudaStream_t
 }
 
 }  // namespace
+
+int launch_wait_selftest(int* status, unsigned limit_ms, void* stream) {
+  wait_selftest_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(status, (unsigned long long)limit_ms * 1000000ull);
+  count_launch();
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error("wait self-test: %s", cudaGetErrorString(e));
+    return PG_ECUDA;
+  }
+  return PG_OK;
+}
 
 int launch_dense(const DenseSet& ds, const double* in, double* out, int dir, int epi, int scale_pow, int* status,
                  void* stream) {

@@ -100,6 +100,8 @@ struct DenseSet {
 };
 // Split a row-major n x n FP64 matrix into the DenseOp plane layout.
 void split_dense(const std::vector<double>& D, int n, std::vector<uint32_t>& out, int& rows, int& kchunks);
+// A bounded wait that is never satisfied: records PG_ETIMEOUT after limit_ms.
+int launch_wait_selftest(int* status, unsigned limit_ms, void* stream);
 // One dense sweep (tcgen05 split-TF32 GEMM) with a fused epilogue.
 int launch_dense(const DenseSet& ds, const double* in, double* out, int dir, int epi, int scale_pow, int* status,
                  void* stream);

@@ -173,6 +173,149 @@ class Kernel:
                     "c": "".join(", " + c for c in call)}
 
 
+def _varname(node):
+    """'x' for the translated variable reference self.variables["x"].data, else None."""
+    if (isinstance(node, ast.Attribute) and node.attr == "data" and isinstance(node.value, ast.Subscript)
+            and isinstance(node.value.value, ast.Attribute) and node.value.value.attr == "variables"
+            and isinstance(node.value.value.value, ast.Name) and node.value.value.value.id == "self"):
+        sl = node.value.slice
+        if isinstance(sl, ast.Constant) and isinstance(sl.value, str):
+            return sl.value
+    return None
+
+
+def _pure(node):
+    """True when every leaf of an elementwise tree is a variable reference or a constant."""
+    if _elementwise(node):
+        return all(_pure(k) for k in _children(node))
+    if _varname(node) is not None or _const(node) is not None:
+        return True
+    return isinstance(node, ast.Attribute) and _is_numpy(node) and node.attr == "pi"
+
+
+class Group:
+    """Consecutive algebraic equations with purely elementwise right-hand sides, fused into one kernel.
+
+    The kernel loads every input variable once, keeps the values the group
+    assigns in registers for the later equations, and writes each equation's
+    result to its own output field.
+    """
+
+    def __init__(self, index, eqs):
+        self.index, self.eqs = index, eqs
+        self.inputs = []          # variable names read before the group assigns them
+        self.exprs = []           # C expression of each equation
+        self.refs = []            # variables each equation reads
+        assigned = {}
+        for k, eq in enumerate(eqs):
+            node = ast.parse(eq.sRHS, mode="eval").body
+            self.exprs.append(self._emit(node, assigned))
+            self.refs.append({_varname(x) for x in ast.walk(node)} - {None})
+            assigned[eq.LHS[0]] = "o%d" % k
+        self.sig = None
+        self.fn = None
+
+    def _emit(self, node, assigned):
+        name = _varname(node)
+        if name is not None:
+            if name in assigned:
+                return assigned[name]
+            if name not in self.inputs:
+                self.inputs.append(name)
+            return "L%d" % self.inputs.index(name)
+        c = _const(node)
+        if c is not None and not isinstance(node, ast.UnaryOp):
+            return "(%r)" % c
+        if isinstance(node, ast.Attribute):
+            return "(%r)" % 3.141592653589793
+        if isinstance(node, ast.UnaryOp):
+            x = self._emit(node.operand, assigned)
+            return "(-%s)" % x if isinstance(node.op, ast.USub) else x
+        if isinstance(node, ast.BinOp):
+            left = self._emit(node.left, assigned)
+            if isinstance(node.op, ast.Pow) and _const(node.right) is not None:
+                return _pow(left, _const(node.right))
+            return _ARITH.get(type(node.op), "pow({0}, {1})").format(left, self._emit(node.right, assigned))
+        args = [self._emit(a, assigned) for a in node.args]
+        fmt = _UNARY.get(node.func.attr) if len(args) == 1 else _BINARY[node.func.attr]
+        return fmt.format(*args)
+
+    def name(self):
+        return "pg_fused_group_%d" % self.index
+
+    def source(self):
+        args, defs, call = [], [], []
+        for i, k in enumerate(self.sig):
+            if k in "fs":
+                args.append("const double* __restrict__ p%d" % i)
+                defs.append("const double L%d = p%d[%s];" % (i, i, "i" if k == "f" else "0"))
+                call.append("p%d" % i)
+            else:
+                args.append("double L%d" % i)
+                call.append("L%d" % i)
+        outs = ["double* __restrict__ out%d" % k for k in range(len(self.eqs))]
+        params = ", ".join(["int64_t n"] + outs + args)
+        body = " ".join(defs) + " " + " ".join("const double o%d = %s;" % (k, e) for k, e in enumerate(self.exprs))
+        stores = " ".join("out%d[i] = o%d;" % (k, k) for k in range(len(self.eqs)))
+        return ('extern "C" __global__ void %(k)s(%(p)s) {\n'
+                "  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;"
+                " i += (int64_t)gridDim.x * blockDim.x) {\n    %(b)s\n    %(s)s\n  }\n}\n"
+                'extern "C" int %(k)s_launch(%(p)s, void* stream) {\n'
+                "  if (n <= 0) return 0;\n"
+                "  int64_t b = (n + 255) / 256;\n  if (b > 152 * 16) b = 152 * 16;\n"
+                "  %(k)s<<<(unsigned)b, 256, 0, (cudaStream_t)stream>>>(n%(o)s%(c)s);\n"
+                "  return (int)cudaGetLastError();\n}\n") % {
+                    "k": self.name(), "p": params, "b": body, "s": stores,
+                    "o": "".join(", out%d" % k for k in range(len(self.eqs))),
+                    "c": "".join(", " + c for c in call)}
+
+    def run(self, sim, fuser):
+        """Evaluate the group; returns the outputs in equation order (or None: evaluate unfused)."""
+        g = sim.grid
+        kinds, args = [], []
+        for name in self.inputs:
+            v = sim.variables[name].data
+            if isinstance(v, torch.Tensor) and v.dim() > 0:
+                if not (v.dtype == torch.float64 and v.device == g.device and tuple(v.shape) == g.n
+                        and g._fortran_ok(v)):
+                    return None
+                kinds.append("f")
+                args.append(ctypes.c_void_p(v.data_ptr()))
+            elif isinstance(v, torch.Tensor):
+                if v.dtype != torch.float64 or v.device != g.device:
+                    return None
+                kinds.append("s")
+                args.append(ctypes.c_void_p(v.data_ptr()))
+            elif isinstance(v, (int, float)) and not isinstance(v, bool):
+                kinds.append("c")
+                args.append(ctypes.c_double(float(v)))
+            else:
+                return None
+        sig = "".join(kinds)
+        if not self._all_fields(sig):
+            return None
+        if self.sig is None:
+            self.sig = sig
+        if self.fn is None or self.sig != sig:
+            return None
+        outs = [g.empty() for _ in self.eqs]
+        rc = self.fn(ctypes.c_int64(g.npts), *[ctypes.c_void_p(o.data_ptr()) for o in outs], *args,
+                     ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        if rc != 0:
+            raise RuntimeError("fused kernel %s failed with CUDA error %d" % (self.name(), rc))
+        fuser.fused_calls += 1
+        return outs
+
+    def _all_fields(self, sig):
+        """Every equation's result is a field (reads a field input, directly or through an earlier output)."""
+        field_vars = {n for n, k in zip(self.inputs, sig) if k == "f"}
+        for eq, refs in zip(self.eqs, self.refs):
+            if not (refs & field_vars):
+                return False
+            field_vars.add(eq.LHS[0])
+        return True
+
+
 class Fuser:
     """Rewrites a simulation's EOM right-hand sides to use fused kernels.
 
@@ -187,6 +330,7 @@ class Fuser:
         self.sim = sim
         self.min_ops = min_ops
         self.kernels = []
+        self.groups = []
         self.lib = None
         self.fused_calls = 0
 
@@ -217,8 +361,31 @@ class Fuser:
         return eval(compile(lam, "<fused equation>", "eval"), globals_)
 
     def install(self, globals_):
-        for eq in self.sim.equations:
+        # runs of consecutive algebraic equations with purely elementwise
+        # right-hand sides become multi-output group kernels
+        self.groups = []
+        eqs = self.sim.equations
+        i = 0
+        while i < len(eqs):
+            j = i
+            while j < len(eqs) and self._groupable(eqs[j]):
+                j += 1
+            if j - i >= 2:
+                grp = Group(len(self.groups), eqs[i:j])
+                self.groups.append(grp)
+                eqs[i]._fused_group = grp
+                for e in eqs[i + 1:j]:
+                    e._fused_member = True
+            i = max(j, i + 1)
+        for eq in eqs:
             eq.RHS = self.rewrite(eq.sRHS, globals_)
+
+    @staticmethod
+    def _groupable(eq):
+        if eq.kind != "ALG" or not eq.LHS or eq.rank != 1 or not eq.active:
+            return False
+        node = ast.parse(eq.sRHS, mode="eval").body
+        return _elementwise(node) and _pure(node)
 
     def run(self, index, *leaves):
         k = self.kernels[index]
@@ -257,7 +424,7 @@ class Fuser:
         return out
 
     def source(self):
-        ks = [k for k in self.kernels if k.sig is not None]
+        ks = [k for k in self.kernels if k.sig is not None] + [g for g in self.groups if g.sig is not None]
         # loads every kernel now: a first launch inside a graph capture would load its module there
         pre = ('extern "C" int pg_fused_preload() {\n  cudaFuncAttributes a;\n  int rc = 0;\n%s  return rc;\n}\n'
                % "".join("  rc |= (int)cudaFuncGetAttributes(&a, %s);\n" % k.name() for k in ks))
@@ -282,7 +449,7 @@ class Fuser:
         self.lib = ctypes.CDLL(so)
         if self.lib.pg_fused_preload() != 0:
             raise RuntimeError("loading the fused EOM kernels failed")
-        for k in self.kernels:
+        for k in list(self.kernels) + list(self.groups):
             if k.sig is not None:
                 fn = getattr(self.lib, k.name() + "_launch")
                 fn.restype = ctypes.c_int

@@ -668,9 +668,21 @@ class pyrandaSim:
 
     def updateVars(self, verbose=False):
         """pyranda.py:393-428: evaluate every ALG line in order."""
+        skip = 0
         for eq in self.equations:
+            if skip:
+                skip -= 1
+                continue
             if not eq.active or eq.kind != "ALG":
                 continue
+            grp = getattr(eq, "_fused_group", None) if self._fuse is not None else None
+            if grp is not None:
+                outs = grp.run(self, self._fuse)
+                if outs is not None:   # one kernel for the whole run of equations
+                    for e, o in zip(grp.eqs, outs):
+                        self._assign(e.LHS[0], o)
+                    skip = len(grp.eqs) - 1
+                    continue
             rhs = eq.RHS(self)
             if not eq.LHS:
                 continue

@@ -37,6 +37,9 @@ def test_rewrite_and_generated_source_compiles(eom, tmp_path):
     assert len(f.kernels) >= 10
     for k in f.kernels:
         k.sig = "f" * k.nleaves          # as if every leaf were a field
+    for g in f.groups:
+        g.sig = "f" * len(g.inputs)
+    assert len(f.groups) >= 1
     src = f.source()
     ast_ok = all(k.expr.count("(") == k.expr.count(")") for k in f.kernels)
     assert ast_ok

@@ -240,3 +240,18 @@ def test_diff_is_exact(grids):
     rho = rho.copy()
     rho[1, 2, 3] = float("nan")
     assert numpy.isnan(float(g.diff(to_dev(bulk, torch), to_dev(rho, torch))))
+
+
+def test_bounded_wait_reports_timeout_and_context_survives(grids):
+    """A device wait that never completes gives up, reports PG_ETIMEOUT, and the GPU keeps working."""
+    from pyranda_gb300 import _lib
+    g, o = grids[CASES[0]]
+    st = ctypes.c_int(-1)
+    assert g.lib.pg_device_status(g.h, ctypes.byref(st)) == 0 and st.value == 0
+    assert g.lib.pg_wait_selftest(g.h, 50, None) == 0
+    torch.cuda.synchronize()
+    assert g.lib.pg_device_status(g.h, ctypes.byref(st)) == 0 and st.value == _lib.PG_ETIMEOUT
+    assert g.lib.pg_device_status(g.h, ctypes.byref(st)) == 0 and st.value == 0   # read clears it
+    shape = CASES[0][0]
+    v = smooth_field(shape, 4)
+    assert rel_l2(to_host(g.ddx(to_dev(v, torch))), o.ddx(v)) < 1e-12
