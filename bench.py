@@ -42,8 +42,11 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
     p.add_argument("--no-fusion", action="store_true", help="fast paths without the fused EOM kernels")
+    p.add_argument("--fusion-arith", default="fp64", choices=["fp32", "fp64"],
+                   help="arithmetic of the fast paths' fused EOM kernels (fp64: bit-exact with unfused; "
+                        "fp32: FP32 arithmetic between FP64 fields)")
     p.add_argument("--mode", default="step", choices=["step", "sweeps", "profile", "peaks", "shock", "ensemble",
-                                                      "shock-learned", "kernels"],
+                                                      "shock-learned", "kernels", "lad"],
                    help="sweeps: time every directional sweep kernel alone on one n^3 field; "
                         "profile: one eager RK step between cudaProfilerStart/Stop (for ncu); "
                         "peaks: HBM copy, FP64 and FP32 GEMM rates; "
@@ -52,7 +55,8 @@ def parse():
                         "shock-learned: 512x128x128 shock-interface with the learned LAD closure against "
                         "the plain one (trains the closure first when no trained model is found); "
                         "kernels: d1 and compact-filter sweeps on one periodic n^3 field at --precision "
-                        "(a light target for profilers)")
+                        "(a light target for profilers); "
+                        "lad: the learned-closure kernel alone on a 512x128x128 grid (a light target for profilers)")
     p.add_argument("--model", default=None, help="shock-learned: trained closure (.npz); default: the packaged one")
     p.add_argument("--train-runs", type=int, default=20, help="shock-learned: training runs when training")
     p.add_argument("--train-iters", type=int, default=3000, help="shock-learned: Adam iterations when training")
@@ -200,14 +204,14 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------------------ GPU
-def make_sim(n, precision, graphs, fusion=False):
+def make_sim(n, precision, graphs, fusion=False, arith="fp64"):
     from pyranda_gb300 import pyrandaSim, pyrandaTimestep, problems
     ss = problems.build_tgv(pyrandaSim, n, lambda s: s.addPackage(pyrandaTimestep(s)), silent=True,
                             precision=precision)
     if graphs:
         ss.use_graphs(True)
     if fusion:
-        ss.use_fusion(True)
+        ss.use_fusion(True, arithmetic=arith)
     return ss
 
 
@@ -285,6 +289,13 @@ def l2_errors(a, b, names):
     return out
 
 
+def momentum_error(a, b, names=("rhou", "rhov", "rhow")):
+    """Relative L2 error of the momentum vector field (rho u, rho v, rho w) of `a` against `b`."""
+    num = sum(float((a.variables[n].data - b.variables[n].data).norm()) ** 2 for n in names)
+    den = sum(float(b.variables[n].data.norm()) ** 2 for n in names)
+    return (num / den) ** 0.5
+
+
 def sweeps_only(args):
     """Per-sweep CUDA-event timings on one periodic n^3 TGV field, both precisions."""
     import torch
@@ -328,11 +339,48 @@ def kernel_sweeps(args):
     return 0
 
 
+def lad_kernel(args):
+    """pg_lad_closure alone on a 512x128x128 grid with seeded fields and an untrained network."""
+    import ctypes
+    import torch
+    from pyranda_gb300.grid import Grid, _ptr, _stream
+    from pyranda_gb300 import learned_lad as LL
+    torch.cuda.set_device(0)
+    g = Grid((512, 128, 128), (False, True, True), (0, 0, 0), (4.0, 127 / 128, 127 / 128), precision="fp32")
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    div, gm, rho = (g.empty() for _ in range(3))
+    for t in (div, gm, rho):
+        t.copy_(torch.rand(t.shape, generator=gen, device="cuda", dtype=torch.float64).permute(0, 1, 2))
+    rho += 1.0
+    dt = torch.full((), 1e-3, dtype=torch.float64, device="cuda")
+    m = LL.LadModel("cuda", seed=0)
+    mm = m.struct()
+    beta, kappa = g.empty(), g.empty()
+    flag = torch.zeros(1, dtype=torch.int32, device="cuda")
+
+    def call():
+        return g.lib.pg_lad_closure(g.h, ctypes.byref(mm), _ptr(div), _ptr(gm), _ptr(rho), _ptr(dt), 2.5, _ptr(beta),
+                                    _ptr(kappa), _ptr(flag), _stream())
+    assert call() == 0
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(args.reps):
+        call()
+    e.record()
+    torch.cuda.synchronize()
+    ms = s.elapsed_time(e) / args.reps
+    print(json.dumps({"lad_kernel_ms": round(ms, 4), "points": g.npts, "ns_per_point": round(ms * 1e6 / g.npts, 3)}),
+          flush=True)
+    return 0
+
+
 def profile_step(args):
     """One eager TGV RK step inside a profiler range, after 2 warm-up steps."""
     import torch
     torch.cuda.set_device(0)
-    ss = make_sim(args.n, args.precision, graphs=False, fusion=not args.no_fusion and args.precision != "fp64")
+    ss = make_sim(args.n, args.precision, graphs=False, fusion=not args.no_fusion and args.precision != "fp64",
+                  arith=args.fusion_arith)
     run_steps(ss, 2)
     torch.cuda.synchronize()
     torch.cuda.cudart().cudaProfilerStart()
@@ -393,10 +441,10 @@ def shock_throughput(args):
         ss = problems.build_shock(pyrandaSim, 512, 128, 128, packs, silent=True, precision=prec)
         if graphs:
             ss.use_graphs(True)
-            ss.use_fusion(True)
+            ss.use_fusion(True, arithmetic=args.fusion_arith)
         run_steps(ss, max(3, args.warmup))
         sec = time_steps(ss, args.steps, torch, False)
-        key = prec + ("+graphs+fusion" if graphs else "")
+        key = prec + ("+graphs+fusion(%s)" % args.fusion_arith if graphs else "")
         out[key] = {"value": round(job_value(npts, args.steps, 1, sec), 3), "unit": UNIT,
                     "ms_per_step": round(sec / args.steps * 1e3, 3)}
         if prec == "auto":
@@ -444,7 +492,7 @@ def ensemble_throughput(args):
         ens = problems.build_kh_ensemble(pyrandaEnsemble, sizes, packs, silent=True, precision=prec)
         if graphs:
             ens.use_graphs(True)
-            ens.use_fusion(True)
+            ens.use_fusion(True, arithmetic=args.fusion_arith)
         dt0 = ens.variables["dt"].data.clone()
         dt = run(ens, w, dt0.clone())
         torch.cuda.synchronize()
@@ -454,7 +502,7 @@ def ensemble_throughput(args):
         e.record()
         torch.cuda.synchronize()
         sec = s.elapsed_time(e) / 1e3
-        out[prec + ("+graphs+fusion" if graphs else "")] = {"value": round(npts * k / sec / 1e6, 3), "unit": UNIT,
+        out[prec + ("+graphs+fusion(%s)" % args.fusion_arith if graphs else "")] = {"value": round(npts * k / sec / 1e6, 3), "unit": UNIT,
                                                             "ms_per_step": round(sec / k * 1e3, 3)}
         res[prec] = ens
     # every precision took the same number of steps from the same IC
@@ -552,7 +600,7 @@ def shock_learned(args):
                                   precision="auto")
         ss.packages["LAD"].mode = mode
         ss.use_graphs(True)
-        ss.use_fusion(True)
+        ss.use_fusion(True, arithmetic=args.fusion_arith)
         return ss
 
     def advance(ss, step, t, t_end=None, nmax=None):
@@ -655,6 +703,8 @@ def main():
         return shock_learned(args)
     if args.mode == "kernels":
         return kernel_sweeps(args)
+    if args.mode == "lad":
+        return lad_kernel(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.mode == "sweeps":
@@ -686,8 +736,13 @@ def main():
     # ---- split-precision paths, each with one CUDA graph per RK step:
     # FP32 banded sweeps, and dense split-TF32 operators on the tensor cores
     fast_runs = {}
-    for prec in (["fp32"] if args.precision == "fp32-only" else ["fp32", "dense", "auto"]):
-        sim = make_sim(n, prec, graphs=True, fusion=not args.no_fusion)
+    runs = ([("fp32", args.fusion_arith)] if args.precision == "fp32-only" else
+            [("fp32", args.fusion_arith), ("dense", args.fusion_arith), ("auto", args.fusion_arith)])
+    other = "fp32" if args.fusion_arith == "fp64" else "fp64"
+    if args.precision != "fp32-only" and not args.no_fusion:
+        runs.append(("auto", other))     # the same path with the other EOM arithmetic, for comparison only
+    for prec, arith in runs:
+        sim = make_sim(n, prec, graphs=True, fusion=not args.no_fusion, arith=arith)
         run_steps(sim, 1)             # eager step (records the fused kernels, then compiles them)
         c0 = _lib.launch_count()
         f0 = sim._fuse.fused_calls if sim._fuse is not None else 0
@@ -699,17 +754,20 @@ def main():
         t = time_steps(sim, k, torch, dist_on)
         ck_ = clocks.stop()
         t = max_over_ranks(t, dist_on, "cuda")
-        fast_runs[prec] = {"sim": sim, "t": t, "launches": lps, "clocks": ck_,
+        key = prec if arith == args.fusion_arith else "%s+%s-eom" % (prec, arith)
+        fast_runs[key] = {"sim": sim, "t": t, "launches": lps, "clocks": ck_, "arith": arith, "prec": prec,
                            "plan": ({"%s_%s" % k: v for k, v in sim.grid.dense_plan().items() if k[0] != "gf"}
                                     if prec != "fp32" else None)}
-    best = min(fast_runs, key=lambda p: fast_runs[p]["t"])
+    # the headline is the fastest path with the requested EOM arithmetic
+    best = min((p for p in fast_runs if fast_runs[p]["arith"] == args.fusion_arith), key=lambda p: fast_runs[p]["t"])
     fast, t_fast = fast_runs[best]["sim"], fast_runs[best]["t"]
     launches_per_step, ck = fast_runs[best]["launches"], fast_runs[best]["clocks"]
     value = job_value(npts, k, world, t_fast)
 
     # ---- plain FP64 path, same IC, same number of steps (no graph)
     extra = {"fast_paths": {p: {"value": round(job_value(npts, k, world, r["t"]), 4), "unit": UNIT,
-                                "ms_per_step": round(r["t"] / k * 1e3, 3), "dense_plan": r["plan"]}
+                                "ms_per_step": round(r["t"] / k * 1e3, 3), "dense_plan": r["plan"],
+                                "eom_arith": r["arith"] if not args.no_fusion else "unfused fp64"}
                             for p, r in fast_runs.items()}}
     if not args.no_fp64:
         plain = make_sim(n, "fp64", graphs=False)
@@ -722,6 +780,7 @@ def main():
         for p, r in fast_runs.items():
             errs = l2_errors(r["sim"], plain, ["rho", "rhou", "rhov", "rhow", "Et"])
             extra["fast_paths"][p]["l2_err_vs_fp64"] = {kk: float("%.3e" % vv) for kk, vv in errs.items()}
+            extra["fast_paths"][p]["l2_err_vs_fp64"]["momentum_vector"] = float("%.3e" % momentum_error(r["sim"], plain))
         extra["l2_err_vs_fp64"] = extra["fast_paths"][best]["l2_err_vs_fp64"]
         extra["l2_err_steps"] = w + k
         del plain
@@ -743,7 +802,7 @@ def main():
     dom = "sfilter_y"
     dur = sw[dom]
     achieved = 16.0 * npts / dur / 1e9
-    dense_y = best != "fp32" and fast.grid.dense_plan()[("sf", "y")]
+    dense_y = fast_runs[best]["prec"] != "fp32" and fast.grid.dense_plan()[("sf", "y")]
     kname = ("dense_kernel<lines as N, dir=y, store, add-back> (tcgen05 kind::tf32, 3 products)" if dense_y
              else "sweep_kernel<float,r4,periodic,implicit,addback,dir=y>")
     if dense_y:   # the tensor-core work of the same launch: 3 TF32 products of 2n flops per point
@@ -781,7 +840,8 @@ def main():
         line = {
             "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": k, "warmup": w,
             "ms_per_step": round(t_fast / k * 1e3, 3), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": ("tf32x3 (f32 accumulate) / f32 sweeps, f64 state" if best != "fp32" else "f32 sweeps / f64 state"),
+            "vs_baseline": None, "dtype": ("tf32x3 (f32 accumulate) / f32 sweeps, f64 state"
+                                           if fast_runs[best]["prec"] != "fp32" else "f32 sweeps / f64 state"),
             "data": "synthetic (Taylor-Green initial condition of examples/TaylorGreen.py)",
             "config": {"workload": "compressible Taylor-Green vortex %d^3 periodic, LAD + compact filters, "
                                    "LSRK(5,4), CFL 0.5" % n,
@@ -790,8 +850,9 @@ def main():
                                          "banded Gaussian",
                                 "auto": "per operator and direction the faster of dense split-TF32 and FP32 banded "
                                         "(autotuned on the grid)",
-                                "fp32": "fp32 banded sweeps"}[best] + ", FP64 state, fused EOM arithmetic, "
-                                                                     "CUDA graph per RK step",
+                                "fp32": "fp32 banded sweeps"}[fast_runs[best]["prec"]]
+                               + ", FP64 state, fused EOM arithmetic in %s, CUDA graph per RK step"
+                               % fast_runs[best]["arith"].upper(),
                        "l2": "inputs larger than L2 (~40 fields of %d MiB)" % (npts * 8 >> 20),
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": roof,

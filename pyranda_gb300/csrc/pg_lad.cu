@@ -75,6 +75,14 @@ __device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, uint32_t b
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
+// One input column of the network: where its value sits in the staged
+// neighbourhood (relative to the point) and its normalisation.
+struct alignas(16) ColInfo {
+  int off;
+  float xm, xs;  // mean and 1/std
+  int pad;
+};
+
 // Shared-memory image of the network for inference: weights as BF16 rows
 // [N][K + 8] (the pad staggers banks), biases and normalisation in FP32.
 struct InferSmem {
@@ -83,7 +91,7 @@ struct InferSmem {
   __nv_bfloat16 w3[kH][kH + 8];
   __nv_bfloat16 w4[8][kH + 8];   // rows >= kOut are zero
   float b1[kH], b2[kH], b3[kH], b4[8];
-  float xm[kK], xs[kK];          // input mean and 1/std
+  ColInfo col[kK];
 };
 
 // one hidden layer: A fragments (4 k-tiles) -> ReLU(W A + b) as next A fragments
@@ -118,15 +126,18 @@ static_assert(kB1 == PG_LAD_NWEIGHT && kB4 + kOut == PG_LAD_NPARAM, "parameter l
 
 // One CTA = 128 consecutive x-points of one (j, k) row.  The 3 x 3 rows
 // around it (130 points each: one halo point per side) of div*D and
-// |grad rho|*D are staged once in shared memory; every warp then builds the
-// features of its 16 points from there and runs the network.
+// |grad rho|*D are staged once in shared memory (rows 0..17), after a row of
+// D (18) and a row of zeros (19) for the constant and padding columns; every
+// warp then builds the features of its 16 points from there and runs the
+// network.
 constexpr int kTileX = 128;
 constexpr int kHaloX = kTileX + 2;
+constexpr int kNbRows = 2 * 9 + 2;
 
 __global__ void __launch_bounds__(kInferThreads) lad_infer_kernel(const LadInferArgs A) {
   extern __shared__ __align__(16) unsigned char lad_smem[];
   InferSmem& S = *reinterpret_cast<InferSmem*>(lad_smem);
-  float (*nb)[9][kHaloX] = reinterpret_cast<float (*)[9][kHaloX]>(lad_smem + sizeof(InferSmem));
+  float* nbf = reinterpret_cast<float*>(lad_smem + sizeof(InferSmem));
   const pg_lad_model& M = A.model;
   const __nv_bfloat16* W = reinterpret_cast<const __nv_bfloat16*>(M.wbf16);
   const float* P = M.params;
@@ -145,15 +156,31 @@ __global__ void __launch_bounds__(kInferThreads) lad_infer_kernel(const LadInfer
     S.b3[i] = P[kB3 + i];
   }
   if (tid < 8) S.b4[tid] = tid < kOut ? P[kB4 + tid] : 0.0f;
-  for (int i = tid; i < kK; i += blockDim.x) {
-    S.xm[i] = M.xmean[i];
-    S.xs[i] = M.xinvstd[i];
-  }
   const LadGrid& G = A.grid;
+  for (int c = tid; c < kK; c += blockDim.x) {
+    ColInfo ci;
+    if (c < 2 * 27) {   // feature f at stencil point s2 = (di+1) + 3 (dj+1) + 9 (dk+1): row (f, dj, dk), x offset di
+      const int f = c / 27, s2 = c - f * 27;
+      ci.off = (f * 9 + s2 / 3) * kHaloX + s2 % 3;
+    } else {
+      ci.off = (c == kIn - 1 ? 18 : 19) * kHaloX;
+    }
+    ci.xm = M.xmean[c];
+    ci.xs = M.xinvstd[c];
+    ci.pad = 0;
+    S.col[c] = ci;
+  }
+  for (int xx = tid; xx < kHaloX; xx += blockDim.x) {
+    nbf[18 * kHaloX + xx] = (float)G.delta;
+    nbf[19 * kHaloX + xx] = 0.0f;
+  }
   const int nx = G.n[0], ny = G.n[1], nz = G.n[2];
   const int nxb = (nx + kTileX - 1) / kTileX;
   const long long ntiles = (long long)nxb * ny * nz;
   const float dl = (float)G.delta;
+  // beta = max(0, y0 s0 + m0) rho D,  kappa = max(0, y1 s1 + m1) rho cv D^2 / dt: the factors of the
+  // launch once in FP64, the per-point arithmetic in FP32 (GB300's FP64 pipe is 1/58 of FP32)
+  const float fb = d2f_bits(G.delta), fk = d2f_bits(A.cv * G.delta * G.delta / A.dt[0]);
   bool out_of_range = false;
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int xb = (int)(tile % nxb);
@@ -167,30 +194,28 @@ __global__ void __launch_bounds__(kInferThreads) lad_infer_kernel(const LadInfer
       const int jj = wrapc(j + rr % 3 - 1, ny, G.per[1]), kk = wrapc(k + rr / 3 - 1, nz, G.per[2]);
       const int x = wrapc(x0 - 1 + xx, nx, G.per[0]);
       const int64_t p = (int64_t)x + (int64_t)nx * (jj + (int64_t)ny * kk);
-      nb[f][rr][xx] = d2f_bits(f == 0 ? A.div[p] : A.gmag[p]) * dl;
+      nbf[q] = d2f_bits(f == 0 ? A.div[p] : A.gmag[p]) * dl;
     }
     __syncthreads();
     const int lx0 = warp * 16;
     if (x0 + lx0 < nx) {
-      // A fragments straight from the neighbourhood: column c of row r is feature c of point lx0 + r
-      auto feat = [&](int r, int c) -> float {
-        float v;
-        if (c < 2 * 27) {
-          const int f = c / 27, s2 = c - f * 27;
-          v = nb[f][s2 / 3][lx0 + r + 1 + s2 % 3 - 1];
-        } else {
-          v = (c == kIn - 1) ? dl : 0.0f;
-        }
-        return (v - S.xm[c]) * S.xs[c];
-      };
+      // A fragments straight from the neighbourhood: column c of row r is feature c of point lx0 + r;
+      // a lane holds columns kt*16 + 2t + {0, 1, 8, 9} of rows g and g + 8
       uint32_t a0[4][4], a1[4][4];
+      const float* pt = nbf + lx0 + g;
 #pragma unroll
       for (int kt = 0; kt < 4; kt++) {
-        const int c = kt * 16 + 2 * t;
-        a0[kt][0] = pack_bf16(feat(g, c), feat(g, c + 1));
-        a0[kt][1] = pack_bf16(feat(g + 8, c), feat(g + 8, c + 1));
-        a0[kt][2] = pack_bf16(feat(g, c + 8), feat(g, c + 9));
-        a0[kt][3] = pack_bf16(feat(g + 8, c + 8), feat(g + 8, c + 9));
+        float v[4][2];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const ColInfo ci = S.col[kt * 16 + 2 * t + (q & 1) + (q >> 1) * 8];
+          v[q][0] = (pt[ci.off] - ci.xm) * ci.xs;
+          v[q][1] = (pt[ci.off + 8] - ci.xm) * ci.xs;
+        }
+        a0[kt][0] = pack_bf16(v[0][0], v[1][0]);
+        a0[kt][1] = pack_bf16(v[0][1], v[1][1]);
+        a0[kt][2] = pack_bf16(v[2][0], v[3][0]);
+        a0[kt][3] = pack_bf16(v[2][1], v[3][1]);
       }
       layer_relu<4>(a0, a1, S.w1, S.b1, g, t);
       layer_relu<4>(a1, a0, S.w2, S.b2, g, t);
@@ -211,11 +236,10 @@ __global__ void __launch_bounds__(kInferThreads) lad_infer_kernel(const LadInfer
             const int64_t p = (int64_t)x + (int64_t)nx * (j + (int64_t)ny * k);
             const float y0 = c[2 * h], y1 = c[2 * h + 1];
             out_of_range |= !(y0 >= M.ylo[0] && y0 <= M.yhi[0] && y1 >= M.ylo[1] && y1 <= M.yhi[1]);
-            const double rho = A.rho[p];
-            const double d = G.delta;
+            const float rho = d2f_bits(A.rho[p]);
             // artificial viscosity and conductivity are non-negative (the plain operators are)
-            A.beta[p] = fmax(0.0, (double)y0 * M.ys[0] + M.ym[0]) * rho * d;
-            A.kappa[p] = fmax(0.0, (double)y1 * M.ys[1] + M.ym[1]) * rho * A.cv * d * d / A.dt[0];
+            A.beta[p] = f2d_bits(fmaxf(0.0f, fmaf(y0, M.ys[0], M.ym[0])) * rho * fb);
+            A.kappa[p] = f2d_bits(fmaxf(0.0f, fmaf(y1, M.ys[1], M.ym[1])) * rho * fk);
           }
         }
       }
@@ -426,18 +450,25 @@ int lad_check(const char* what) {
 }  // namespace
 
 int launch_lad_infer(const LadInferArgs& a, void* stream) {
-  static bool attr = false;
-  const int smem = (int)(sizeof(InferSmem) + 2 * 9 * kHaloX * sizeof(float));
-  if (!attr) {
+  static int resident = 0;  // CTAs per SM (persistent grid: one wave)
+  static int sms = 0;
+  const int smem = (int)(sizeof(InferSmem) + kNbRows * kHaloX * sizeof(float));
+  if (resident == 0) {
     cudaError_t e = cudaFuncSetAttribute(lad_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) {
-      set_error("lad inference: %s", cudaGetErrorString(e));
+    int dev = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, lad_infer_kernel,
+                                                                            kInferThreads, smem);
+    if (e != cudaSuccess || resident < 1) {
+      set_error("lad inference: %s", e != cudaSuccess ? cudaGetErrorString(e) : "kernel does not fit an SM");
+      resident = 0;
       return PG_ECUDA;
     }
-    attr = true;
   }
   const int64_t tiles = (int64_t)((a.grid.n[0] + kTileX - 1) / kTileX) * a.grid.n[1] * a.grid.n[2];
-  const int blocks = (int)(tiles < 152 * 4 ? tiles : 152 * 4);
+  const int64_t wave = (int64_t)sms * resident;
+  const int blocks = (int)(tiles < wave ? tiles : wave);
   lad_infer_kernel<<<blocks, kInferThreads, smem, (cudaStream_t)stream>>>(a);
   count_launch();
   return lad_check("lad inference");

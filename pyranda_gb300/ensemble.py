@@ -383,6 +383,7 @@ class pyrandaEnsemble(pyrandaSim):
         self._graphs_enabled = False
         self._fuse = None
         self._fuse_wanted = False
+        self._fuse_arith = "fp64"
         self.get_sMap()
 
     def _make_mesh(self):

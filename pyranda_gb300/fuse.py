@@ -15,6 +15,16 @@ propagate NaN, so a fused step reproduces the unfused one bit for bit.  All
 kernels of a simulation are generated into one source file, compiled once
 with nvcc for sm_103a and cached under pyranda_gb300/_build/jit by the
 source's hash.
+
+That is the FP64 arithmetic (Fuser(..., arith="fp64")).  The fast paths may
+instead evaluate the same expressions in FP32 (arith="fp32"): every FP64
+load is narrowed by integer operations (round to nearest even; infinities
+and NaN kept; magnitudes below 2**-126 flushed to zero), the arithmetic and
+the math functions run at FP32 with FMA contraction, and the result is
+widened back to the FP64 field.  GB300's FP64 rate is about 1/58 of its FP32
+rate and its F2F conversions run on the FP64 pipe, which bounds the FP64
+kernels; the RK state accumulation, the boundary-closure solves and the d8
+LAD sweeps are not elementwise EOM arithmetic and keep FP64 either way.
 """
 import ast
 import copy
@@ -29,22 +39,99 @@ from .build import ARCH, OUT, nvcc
 
 JIT_DIR = os.path.join(OUT, "jit")
 
-_UNARY = {"sqrt": "sqrt({0})", "abs": "fabs({0})", "absolute": "fabs({0})", "exp": "exp({0})",
-          "log": "log({0})", "sin": "sin({0})", "cos": "cos({0})", "tan": "tan({0})", "tanh": "tanh({0})",
-          "sinh": "sinh({0})", "cosh": "cosh({0})", "arctan": "atan({0})", "arcsin": "asin({0})",
-          "arccos": "acos({0})", "log10": "log10({0})", "floor": "floor({0})", "ceil": "ceil({0})",
-          "sign": "pg_sign({0})"}
+_UNARY = {"sqrt": "PG_SQRT({0})", "abs": "PG_ABS({0})", "absolute": "PG_ABS({0})", "exp": "PG_EXP({0})",
+          "log": "PG_LOG({0})", "sin": "PG_SIN({0})", "cos": "PG_COS({0})", "tan": "PG_TAN({0})",
+          "tanh": "PG_TANH({0})", "sinh": "PG_SINH({0})", "cosh": "PG_COSH({0})", "arctan": "PG_ATAN({0})",
+          "arcsin": "PG_ASIN({0})", "arccos": "PG_ACOS({0})", "log10": "PG_LOG10({0})",
+          "floor": "PG_FLOOR({0})", "ceil": "PG_CEIL({0})", "sign": "pg_sign({0})"}
 _BINARY = {"minimum": "pg_min({0}, {1})", "maximum": "pg_max({0}, {1})"}
-_ARITH = {ast.Add: "__dadd_rn({0}, {1})", ast.Sub: "__dsub_rn({0}, {1})", ast.Mult: "__dmul_rn({0}, {1})",
-          ast.Div: "__ddiv_rn({0}, {1})"}
+_ARITH = {ast.Add: "PG_ADD({0}, {1})", ast.Sub: "PG_SUB({0}, {1})", ast.Mult: "PG_MUL({0}, {1})",
+          ast.Div: "PG_DIV({0}, {1})"}
 
-PRELUDE = r"""#include <cstdint>
+_COMMON = r"""#include <cstdint>
 #include <cmath>
 #include <cuda_runtime.h>
-__device__ __forceinline__ double pg_min(double a, double b) { return (a != a) ? a : ((b != b) ? b : (a < b ? a : b)); }
-__device__ __forceinline__ double pg_max(double a, double b) { return (a != a) ? a : ((b != b) ? b : (a > b ? a : b)); }
-__device__ __forceinline__ double pg_sign(double a) { return (a > 0.0) ? 1.0 : ((a < 0.0) ? -1.0 : a); }
+__device__ __forceinline__ real pg_min(real a, real b) { return (a != a) ? a : ((b != b) ? b : (a < b ? a : b)); }
+__device__ __forceinline__ real pg_max(real a, real b) { return (a != a) ? a : ((b != b) ? b : (a > b ? a : b)); }
+__device__ __forceinline__ real pg_sign(real a) { return (a > (real)0) ? (real)1 : ((a < (real)0) ? (real)-1 : a); }
 """
+
+# FP64 arithmetic: every operation rounded on its own, as torch's separate kernels do.
+PRELUDE_FP64 = r"""typedef double real;
+#define PG_LOAD(x) (x)
+#define PG_STORE(x) (x)
+#define PG_C(x) (x)
+#define PG_ADD(a, b) __dadd_rn(a, b)
+#define PG_SUB(a, b) __dsub_rn(a, b)
+#define PG_MUL(a, b) __dmul_rn(a, b)
+#define PG_DIV(a, b) __ddiv_rn(a, b)
+#define PG_SQRT(x) sqrt(x)
+#define PG_RSQRT(x) rsqrt(x)
+#define PG_POW(a, b) pow(a, b)
+#define PG_ABS(x) fabs(x)
+#define PG_EXP(x) exp(x)
+#define PG_LOG(x) log(x)
+#define PG_SIN(x) sin(x)
+#define PG_COS(x) cos(x)
+#define PG_TAN(x) tan(x)
+#define PG_TANH(x) tanh(x)
+#define PG_SINH(x) sinh(x)
+#define PG_COSH(x) cosh(x)
+#define PG_ATAN(x) atan(x)
+#define PG_ASIN(x) asin(x)
+#define PG_ACOS(x) acos(x)
+#define PG_LOG10(x) log10(x)
+#define PG_FLOOR(x) floor(x)
+#define PG_CEIL(x) ceil(x)
+""" + _COMMON
+
+# FP32 arithmetic on FP64 fields (the fast paths): values converted by integer
+# operations (GB300 runs F2F on its FP64 pipe) keeping infinities and NaN,
+# FP32 math, results widened back to FP64.
+PRELUDE_FP32 = r"""typedef float real;
+__device__ __forceinline__ float pg_d2f(double d) {
+  const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+  const unsigned sign = hi & 0x80000000u, mag = hi & 0x7fffffffu;
+  if (mag >= 0x7ff00000u) return __uint_as_float(sign | 0x7f800000u | ((((mag & 0xfffffu) | lo) != 0u) ? 0x400000u : 0u));
+  if (mag >= (1151u << 20)) return __uint_as_float(sign | 0x7f800000u);
+  if (mag < (897u << 20)) return __uint_as_float(sign);
+  unsigned f = ((mag - (896u << 20)) << 3) | (lo >> 29);
+  f += ((lo >> 28) & 1u) & (((lo & 0x0fffffffu) != 0u) | (f & 1u));
+  return __uint_as_float(f | sign);
+}
+__device__ __forceinline__ double pg_f2d(float x) {
+  const unsigned u = __float_as_uint(x);
+  const unsigned sign = u & 0x80000000u, mag = u & 0x7fffffffu;
+  if (mag >= 0x7f800000u) return __hiloint2double((int)(sign | 0x7ff00000u | ((mag & 0x7fffffu) ? 0x80000u : 0u)), 0);
+  if (mag < 0x00800000u) return __hiloint2double((int)sign, 0);
+  return __hiloint2double((int)(((mag >> 3) + (896u << 20)) | sign), (int)(mag << 29));
+}
+#define PG_LOAD(x) pg_d2f(x)
+#define PG_STORE(x) pg_f2d(x)
+#define PG_C(x) ((float)(x))
+#define PG_ADD(a, b) ((a) + (b))
+#define PG_SUB(a, b) ((a) - (b))
+#define PG_MUL(a, b) ((a) * (b))
+#define PG_DIV(a, b) ((a) / (b))
+#define PG_SQRT(x) sqrtf(x)
+#define PG_RSQRT(x) rsqrtf(x)
+#define PG_POW(a, b) powf(a, b)
+#define PG_ABS(x) fabsf(x)
+#define PG_EXP(x) expf(x)
+#define PG_LOG(x) logf(x)
+#define PG_SIN(x) sinf(x)
+#define PG_COS(x) cosf(x)
+#define PG_TAN(x) tanf(x)
+#define PG_TANH(x) tanhf(x)
+#define PG_SINH(x) sinhf(x)
+#define PG_COSH(x) coshf(x)
+#define PG_ATAN(x) atanf(x)
+#define PG_ASIN(x) asinf(x)
+#define PG_ACOS(x) acosf(x)
+#define PG_LOG10(x) log10f(x)
+#define PG_FLOOR(x) floorf(x)
+#define PG_CEIL(x) ceilf(x)
+""" + _COMMON
 
 
 def _const(node):
@@ -86,20 +173,20 @@ def _ops(node):
 def _pow(x, c):
     # torch's pow(tensor, scalar) special cases
     if c == 2.0:
-        return "__dmul_rn(%s, %s)" % (x, x)
+        return "PG_MUL(%s, %s)" % (x, x)
     if c == 3.0:
-        return "__dmul_rn(__dmul_rn(%s, %s), %s)" % (x, x, x)
+        return "PG_MUL(PG_MUL(%s, %s), %s)" % (x, x, x)
     if c == 0.5:
-        return "sqrt(%s)" % x
+        return "PG_SQRT(%s)" % x
     if c == -0.5:
-        return "rsqrt(%s)" % x
+        return "PG_RSQRT(%s)" % x
     if c == -1.0:
-        return "__ddiv_rn(1.0, %s)" % x
+        return "PG_DIV(PG_C(1.0), %s)" % x
     if c == -2.0:
-        return "__ddiv_rn(1.0, __dmul_rn(%s, %s))" % (x, x)
+        return "PG_DIV(PG_C(1.0), PG_MUL(%s, %s))" % (x, x)
     if c == 1.0:
         return x
-    return "pow(%s, %r)" % (x, float(c))
+    return "PG_POW(%s, PG_C(%r))" % (x, float(c))
 
 
 class _Gen:
@@ -111,9 +198,9 @@ class _Gen:
     def emit(self, node):
         c = _const(node)
         if c is not None and not isinstance(node, ast.UnaryOp):
-            return "(%r)" % c, copy.copy(node)
+            return "PG_C(%r)" % c, copy.copy(node)
         if isinstance(node, ast.Attribute) and _is_numpy(node) and node.attr == "pi":
-            return "(%r)" % 3.141592653589793, copy.copy(node)
+            return "PG_C(%r)" % 3.141592653589793, copy.copy(node)
         if _elementwise(node):
             if isinstance(node, ast.UnaryOp):
                 cx, px = self.emit(node.operand)
@@ -123,7 +210,7 @@ class _Gen:
                 if isinstance(node.op, ast.Pow) and _const(node.right) is not None:
                     return _pow(cl, _const(node.right)), ast.BinOp(left=pl, op=node.op, right=copy.copy(node.right))
                 cr, pr = self.emit(node.right)
-                fmt = _ARITH.get(type(node.op), "pow({0}, {1})")
+                fmt = _ARITH.get(type(node.op), "PG_POW({0}, {1})")
                 return fmt.format(cl, cr), ast.BinOp(left=pl, op=node.op, right=pr)
             args = [self.emit(a) for a in node.args]
             fmt = _UNARY.get(node.func.attr) if len(args) == 1 else _BINARY[node.func.attr]
@@ -155,15 +242,16 @@ class Kernel:
         for i, k in enumerate(self.sig):
             if k in "fs":
                 args.append("const double* __restrict__ p%d" % i)
-                defs.append("const double L%d = p%d[%s];" % (i, i, "i" if k == "f" else "0"))
+                defs.append("const real L%d = PG_LOAD(p%d[%s]);" % (i, i, "i" if k == "f" else "0"))
                 call.append("p%d" % i)
             else:
-                args.append("double L%d" % i)
-                call.append("L%d" % i)
+                args.append("real c%d" % i)
+                defs.append("const real L%d = c%d;" % (i, i))
+                call.append("c%d" % i)
         params = ", ".join(["int64_t n", "double* __restrict__ out"] + args)
         return ('extern "C" __global__ void %(k)s(%(p)s) {\n'
                 "  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;"
-                " i += (int64_t)gridDim.x * blockDim.x) {\n    %(d)s\n    out[i] = %(e)s;\n  }\n}\n"
+                " i += (int64_t)gridDim.x * blockDim.x) {\n    %(d)s\n    out[i] = PG_STORE(%(e)s);\n  }\n}\n"
                 'extern "C" int %(k)s_launch(%(p)s, void* stream) {\n'
                 "  if (n <= 0) return 0;\n"
                 "  int64_t b = (n + 255) / 256;\n  if (b > 152 * 16) b = 152 * 16;\n"
@@ -171,6 +259,29 @@ class Kernel:
                 "  return (int)cudaGetLastError();\n}\n") % {
                     "k": self.name(), "p": params, "d": " ".join(defs), "e": self.expr,
                     "c": "".join(", " + c for c in call)}
+
+
+def compile_source(src, fmad=False):
+    """nvcc for sm_103a into a shared library cached under the source's hash; returns its path.
+
+    FP64 arithmetic is compiled without FMA contraction (torch rounds every
+    product on its own); FP32 arithmetic lets nvcc contract.
+    """
+    h = hashlib.sha1((src + ("fmad" if fmad else "")).encode()).hexdigest()[:16]
+    os.makedirs(JIT_DIR, exist_ok=True)
+    so = os.path.join(JIT_DIR, "fused_%s.so" % h)
+    if not os.path.exists(so):
+        cu = os.path.join(JIT_DIR, "fused_%s.cu" % h)
+        with open(cu, "w") as f:
+            f.write(src)
+        tmp = so + ".%d.tmp" % os.getpid()
+        cmd = [nvcc()] + ARCH + ["-O3", "-fmad=%s" % ("true" if fmad else "false"), "-shared",
+                                 "-Xcompiler", "-fPIC", "-o", tmp, cu]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("nvcc failed on the fused EOM kernels:\n" + r.stderr[-3000:])
+        os.replace(tmp, so)
+    return so
 
 
 def _varname(node):
@@ -225,9 +336,9 @@ class Group:
             return "L%d" % self.inputs.index(name)
         c = _const(node)
         if c is not None and not isinstance(node, ast.UnaryOp):
-            return "(%r)" % c
+            return "PG_C(%r)" % c
         if isinstance(node, ast.Attribute):
-            return "(%r)" % 3.141592653589793
+            return "PG_C(%r)" % 3.141592653589793
         if isinstance(node, ast.UnaryOp):
             x = self._emit(node.operand, assigned)
             return "(-%s)" % x if isinstance(node.op, ast.USub) else x
@@ -235,7 +346,7 @@ class Group:
             left = self._emit(node.left, assigned)
             if isinstance(node.op, ast.Pow) and _const(node.right) is not None:
                 return _pow(left, _const(node.right))
-            return _ARITH.get(type(node.op), "pow({0}, {1})").format(left, self._emit(node.right, assigned))
+            return _ARITH.get(type(node.op), "PG_POW({0}, {1})").format(left, self._emit(node.right, assigned))
         args = [self._emit(a, assigned) for a in node.args]
         fmt = _UNARY.get(node.func.attr) if len(args) == 1 else _BINARY[node.func.attr]
         return fmt.format(*args)
@@ -248,15 +359,16 @@ class Group:
         for i, k in enumerate(self.sig):
             if k in "fs":
                 args.append("const double* __restrict__ p%d" % i)
-                defs.append("const double L%d = p%d[%s];" % (i, i, "i" if k == "f" else "0"))
+                defs.append("const real L%d = PG_LOAD(p%d[%s]);" % (i, i, "i" if k == "f" else "0"))
                 call.append("p%d" % i)
             else:
-                args.append("double L%d" % i)
-                call.append("L%d" % i)
+                args.append("real c%d" % i)
+                defs.append("const real L%d = c%d;" % (i, i))
+                call.append("c%d" % i)
         outs = ["double* __restrict__ out%d" % k for k in range(len(self.eqs))]
         params = ", ".join(["int64_t n"] + outs + args)
-        body = " ".join(defs) + " " + " ".join("const double o%d = %s;" % (k, e) for k, e in enumerate(self.exprs))
-        stores = " ".join("out%d[i] = o%d;" % (k, k) for k in range(len(self.eqs)))
+        body = " ".join(defs) + " " + " ".join("const real o%d = %s;" % (k, e) for k, e in enumerate(self.exprs))
+        stores = " ".join("out%d[i] = PG_STORE(o%d);" % (k, k) for k in range(len(self.eqs)))
         return ('extern "C" __global__ void %(k)s(%(p)s) {\n'
                 "  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;"
                 " i += (int64_t)gridDim.x * blockDim.x) {\n    %(b)s\n    %(s)s\n  }\n}\n"
@@ -288,7 +400,7 @@ class Group:
                 args.append(ctypes.c_void_p(v.data_ptr()))
             elif isinstance(v, (int, float)) and not isinstance(v, bool):
                 kinds.append("c")
-                args.append(ctypes.c_double(float(v)))
+                args.append(fuser.scalar(v))
             else:
                 return None
         sig = "".join(kinds)
@@ -326,9 +438,13 @@ class Fuser:
     whose fields are not in the grid's layout, runs unfused.
     """
 
-    def __init__(self, sim, min_ops=2):
+    def __init__(self, sim, min_ops=2, arith="fp64"):
+        if arith not in ("fp64", "fp32"):
+            raise ValueError("arith must be 'fp64' or 'fp32'")
         self.sim = sim
+        self.arith = arith
         self.min_ops = min_ops
+        self.scalar = (lambda v: ctypes.c_double(float(v))) if arith == "fp64" else (lambda v: ctypes.c_float(float(v)))
         self.kernels = []
         self.groups = []
         self.lib = None
@@ -405,7 +521,7 @@ class Fuser:
                 args.append(ctypes.c_void_p(v.data_ptr()))
             elif isinstance(v, (int, float)) and not isinstance(v, bool):
                 kinds.append("c")
-                args.append(ctypes.c_double(float(v)))
+                args.append(self.scalar(v))
             else:
                 return k.eager(*leaves)
         sig = "".join(kinds)
@@ -428,24 +544,12 @@ class Fuser:
         # loads every kernel now: a first launch inside a graph capture would load its module there
         pre = ('extern "C" int pg_fused_preload() {\n  cudaFuncAttributes a;\n  int rc = 0;\n%s  return rc;\n}\n'
                % "".join("  rc |= (int)cudaFuncGetAttributes(&a, %s);\n" % k.name() for k in ks))
-        return PRELUDE + "".join(k.source() for k in ks) + pre
+        prelude = PRELUDE_FP64 if self.arith == "fp64" else PRELUDE_FP32
+        return prelude + "".join(k.source() for k in ks) + pre
 
     def build(self):
         """Compile every recorded kernel (once per distinct source) and bind them; returns the .so path."""
-        src = self.source()
-        h = hashlib.sha1(src.encode()).hexdigest()[:16]
-        os.makedirs(JIT_DIR, exist_ok=True)
-        so = os.path.join(JIT_DIR, "fused_%s.so" % h)
-        if not os.path.exists(so):
-            cu = os.path.join(JIT_DIR, "fused_%s.cu" % h)
-            with open(cu, "w") as f:
-                f.write(src)
-            tmp = so + ".%d.tmp" % os.getpid()
-            cmd = [nvcc()] + ARCH + ["-O3", "-fmad=false", "-shared", "-Xcompiler", "-fPIC", "-o", tmp, cu]
-            r = subprocess.run(cmd, capture_output=True, text=True)
-            if r.returncode != 0:
-                raise RuntimeError("nvcc failed on the fused EOM kernels:\n" + r.stderr[-3000:])
-            os.replace(tmp, so)
+        so = compile_source(self.source(), fmad=self.arith == "fp32")
         self.lib = ctypes.CDLL(so)
         if self.lib.pg_fused_preload() != 0:
             raise RuntimeError("loading the fused EOM kernels failed")

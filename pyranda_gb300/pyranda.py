@@ -293,6 +293,7 @@ class pyrandaSim:
         self._graphs_enabled = False
         self._fuse = None
         self._fuse_wanted = False
+        self._fuse_arith = "fp64"
         self.get_sMap()
 
     # ------------------------------------------------------------ mesh set-up
@@ -713,7 +714,7 @@ class pyrandaSim:
         """One LSRK(5,4) step (pyranda.py:758-810), ALG update after every stage."""
         if self._fuse_wanted and self._fuse is None:
             from .fuse import Fuser
-            self._fuse = Fuser(self)
+            self._fuse = Fuser(self, arith=self._fuse_arith)
             self._fuse.install(EVAL_GLOBALS)
         if self._graphs_enabled:
             t = self._rk4_graph(time, dt)
@@ -723,17 +724,22 @@ class pyrandaSim:
             self._fuse.build()   # after the recording step, before any capture
         return t
 
-    def use_fusion(self, enable=True):
+    def use_fusion(self, enable=True, arithmetic="fp64"):
         """Evaluate the EOM's elementwise arithmetic in generated CUDA kernels.
 
         Each maximal elementwise subtree of every equation becomes one kernel
         (pyranda_gb300.fuse).  The next rk4 step records the kernels' argument
         kinds and runs unfused; the kernels are then compiled once (nvcc,
-        cached by source hash) and used from the following step on, with the
-        same results bit for bit.
+        cached by source hash) and used from the following step on.  With
+        arithmetic='fp64' the results equal the unfused ones bit for bit;
+        arithmetic='fp32' evaluates the expressions in FP32 between FP64
+        fields (the fast paths' choice; FP32 rounding error per line).
         """
+        if arithmetic not in ("fp64", "fp32"):
+            raise ValueError("arithmetic must be 'fp64' or 'fp32'")
+        self._fuse_arith = arithmetic
         self._fuse_wanted = bool(enable)
-        if not enable and self._fuse is not None:
+        if self._fuse is not None and (not enable or self._fuse.arith != arithmetic):
             self._fuse = None
             for eq in self.equations:
                 eq.RHS = eval("lambda self: " + eq.sRHS, EVAL_GLOBALS)

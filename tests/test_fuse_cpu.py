@@ -28,15 +28,16 @@ class _Sim:
             self.equations.append(pyrandaEq(line, self.sMap))
 
 
+@pytest.mark.parametrize("arith", ["fp64", "fp32"])
 @pytest.mark.parametrize("eom", [TGV_EOM, SHOCK_EOM, KH_EOM.replace("gamma", "1.4").replace("R0", "1.0")
                                  .replace("cv", "2.5")], ids=["tgv", "shock", "kh"])
-def test_rewrite_and_generated_source_compiles(eom, tmp_path):
+def test_rewrite_and_generated_source_compiles(eom, arith, tmp_path):
     sim = _Sim(eom)
-    f = fuse.Fuser(sim)
+    f = fuse.Fuser(sim, arith=arith)
     f.install(EVAL_GLOBALS)
     assert len(f.kernels) >= 10
-    for k in f.kernels:
-        k.sig = "f" * k.nleaves          # as if every leaf were a field
+    for i, k in enumerate(f.kernels):   # as if every leaf were a field, some a device scalar or a number
+        k.sig = "".join("fsc"[(i + q) % 3] if q else "f" for q in range(k.nleaves))
     for g in f.groups:
         g.sig = "f" * len(g.inputs)
     assert len(f.groups) >= 1
@@ -49,7 +50,8 @@ def test_rewrite_and_generated_source_compiles(eom, tmp_path):
     cu.write_text(src)
     import subprocess
     from pyranda_gb300.build import ARCH, nvcc
-    r = subprocess.run([nvcc()] + ARCH + ["-O3", "-fmad=false", "-c", str(cu), "-o", str(tmp_path / "k.o")],
+    r = subprocess.run([nvcc()] + ARCH + ["-O3", "-fmad=%s" % ("true" if arith == "fp32" else "false"), "-c",
+                        str(cu), "-o", str(tmp_path / "k.o")],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
 
@@ -57,4 +59,11 @@ def test_rewrite_and_generated_source_compiles(eom, tmp_path):
 def test_power_special_cases_follow_torch():
     g = fuse._Gen()
     c, _ = g.emit(ast.parse("a**2 + b**0.5 - c**-1", mode="eval").body)
-    assert "__dmul_rn(L0, L0)" in c and "sqrt(L1)" in c and "__ddiv_rn(1.0, L2)" in c
+    assert "PG_MUL(L0, L0)" in c and "PG_SQRT(L1)" in c and "PG_DIV(PG_C(1.0), L2)" in c
+    assert "#define PG_MUL(a, b) __dmul_rn(a, b)" in fuse.PRELUDE_FP64
+    assert "#define PG_SQRT(x) sqrt(x)" in fuse.PRELUDE_FP64
+
+
+def test_unknown_arithmetic_is_refused():
+    with pytest.raises(ValueError):
+        fuse.Fuser(_Sim(TGV_EOM), arith="fp16")
