@@ -54,12 +54,16 @@ def parse():
                         "ensemble: 64 Kelvin-Helmholtz 2-D runs of seeded sizes advanced together; "
                         "shock-learned: 512x128x128 shock-interface with the learned LAD closure against "
                         "the plain one (trains the closure first when no trained model is found); "
-                        "kernels: d1 and compact-filter sweeps on one periodic n^3 field at --precision "
+                        "kernels: d1, compact-filter and d8 sweeps on one periodic n^3 field at --precision "
                         "(a light target for profilers); "
                         "lad: the learned-closure kernel alone on a 512x128x128 grid (a light target for profilers)")
     p.add_argument("--model", default=None, help="shock-learned: trained closure (.npz); default: the packaged one")
     p.add_argument("--train-runs", type=int, default=20, help="shock-learned: training runs when training")
-    p.add_argument("--train-iters", type=int, default=3000, help="shock-learned: Adam iterations when training")
+    p.add_argument("--train-iters", type=int, default=20000, help="shock-learned: Adam iterations when training "
+                                                                    "(cosine learning-rate decay)")
+    p.add_argument("--train-shape", default="256,64,64", help="shock-learned: grid of the training runs")
+    p.add_argument("--save-model", default=None, help="shock-learned: where a newly trained closure is saved "
+                                                      "(default gpurun_out/lad_shock.npz)")
     p.add_argument("--members", type=int, default=64, help="ensemble mode: number of members")
     p.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "dense", "auto", "fp32-only"],
                    help="profile mode: arithmetic of the profiled step; step mode: 'fp32-only' skips the dense run")
@@ -313,7 +317,7 @@ def sweeps_only(args):
 
 
 def kernel_sweeps(args):
-    """d1 and compact-filter sweeps in x, y, z on one periodic n^3 field (two fields on the device)."""
+    """d1, compact-filter and d8 sweeps in x, y, z on one periodic n^3 field (two fields on the device)."""
     import torch
     from pyranda_gb300.grid import Grid
     torch.cuda.set_device(0)
@@ -323,7 +327,8 @@ def kernel_sweeps(args):
     v.copy_(torch.sin(v) + 2.0)
     out = g.empty()
     res = {}
-    for name, f in (("d1", lambda d: g.d1(d, v, out=out)), ("sfilter", lambda d: g.filter("spectral", v, d, out=out))):
+    for name, f in (("d1", lambda d: g.d1(d, v, out=out)), ("sfilter", lambda d: g.filter("spectral", v, d, out=out)),
+                    ("d8", lambda d: g.d8(d, v, out=out))):
         for d in range(3):
             f(d)
             torch.cuda.synchronize()
@@ -558,7 +563,7 @@ def shock_learned(args):
     RK step); each takes its own CFL/diffusion steps, and the learned run is
     advanced to the time the plain run reached, where the densities are
     compared.  Without a trained model the closure is
-    first trained here: 2000 snapshots of 20 seeded 128x64x64 runs (Mach in
+    first trained here: 2000 snapshots of 20 seeded 256x64x64 runs (Mach in
     [1.2, 3], amplitude in [0.01, 0.1], default_rng(1)), then Adam.
     """
     import torch
@@ -573,17 +578,22 @@ def shock_learned(args):
         out["model"] = os.path.relpath(path, ROOT)
     else:
         t0 = time.time()
-        raw, T, meta = LL.shock_training_set(runs=args.train_runs, snapshots_per_run=2000 // args.train_runs)
+        shape = tuple(int(x) for x in args.train_shape.split(","))
+        raw, T, meta = LL.shock_training_set(runs=args.train_runs, snapshots_per_run=2000 // args.train_runs,
+                                             shape=shape)
         t1 = time.time()
         model = LL.LadModel("cuda", seed=0)
         Tn = LL.fit_normalisation(model, raw, T)
         X = LL.normalize(raw, model)
-        hist = LL.train(model, X, Tn, iters=args.train_iters, batch=8192, lr=1e-3, log_every=500)
+        hist = LL.train(model, X, Tn, iters=args.train_iters, batch=8192, lr=1e-3,
+                        log_every=max(1, args.train_iters // 8), cosine=True)
         torch.cuda.synchronize()
         t2 = time.time()
-        os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-        model.save(os.path.join(ROOT, "gpurun_out", "lad_shock.npz"))
-        out["training"] = {"samples": int(raw.shape[0]), "snapshots": sum(m[2] for m in meta),
+        save = args.save_model or os.path.join(ROOT, "gpurun_out", "lad_shock.npz")
+        os.makedirs(os.path.dirname(os.path.abspath(save)), exist_ok=True)
+        model.save(save)
+        out["training"] = {"shape": list(shape), "iters": args.train_iters,
+                           "samples": int(raw.shape[0]), "snapshots": sum(m[2] for m in meta),
                            "runs": [[round(a, 4), round(b, 4), c] for a, b, c in meta],
                            "data_s": round(t1 - t0, 1), "train_s": round(t2 - t1, 1), "loss": hist}
         del raw, T, X, Tn
@@ -652,8 +662,24 @@ def shock_learned(args):
         e.record()
         torch.cuda.synchronize()
         closure_ms[mode] = round(s.elapsed_time(e) / args.reps, 4)
+    # both closures on the same (final) state: their extremes set the diffusive time step
+    diag = {}
+    tsp = learned.packages["Timestep"]
+    for mode in ("plain", "learned"):
+        lad.mode = mode
+        b, kp = lad.closure(V["div"].data, V["rho"].data, V["T"].data, V["dt"].data)
+        bs = b.flatten()[::7].float()
+        diag[mode] = {"beta_max": float(b.max()), "beta_p999": float(torch.quantile(bs, 0.999)),
+                      "beta_mean": float(b.mean()), "kappa_max": float(kp.max()),
+                      "dt_beta_limit": 0.2 * float(tsp.diff(b, V["rho"].data))}
+        if mode == "plain":
+            b_plain, k_plain = b.clone(), kp.clone()
+        else:
+            diag["beta_rel_l1"] = float((b - b_plain).abs().sum() / b_plain.abs().sum())
+            diag["kappa_rel_l1"] = float((kp - k_plain).abs().sum() / k_plain.abs().sum())
+    out["closure_on_final_state"] = diag
     lad.mode = "learned"
-    # its parts: |grad rho| (three d1 sweeps) and the fused feature-gather + network kernel
+    # its parts: |grad rho| (one central-difference pass) and the fused feature-gather + network kernel
     g = learned.grid
     gm = LL.grad_magnitude(g, V["rho"].data)
     beta, kappa = g.empty(), g.empty()

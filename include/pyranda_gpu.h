@@ -45,12 +45,14 @@ typedef enum {
 
 /* Arithmetic of the compact sweeps.  PG_FP64 follows the reference
  * arithmetic; PG_FP32 evaluates the sweeps in single precision on FP64
- * inputs/outputs (the fast path; FP64 state is kept by the caller).
- * PG_DENSE applies d1, d8 and the compact filter as dense n x n operators
+ * inputs/outputs (the fast path; FP64 state is kept by the caller), except
+ * the d8 RHS, which is evaluated exactly in 64-bit fixed point (its 8th
+ * difference cancels more bits than FP32 holds) before an FP32 solve.
+ * PG_DENSE applies d1 and the two filters as dense n x n operators
  * D = A^-1 B (the reference's `sm`, compact_basetype.f90:199-205) on the
  * tensor cores in split TF32 (hi.hi + hi.lo + lo.hi, FP32 accumulation) for
- * directions of 16..1024 points, and the FP32 banded sweeps elsewhere; the
- * filters' add-back of v stays in FP64.  PG_AUTO builds the same tables and
+ * directions of 16..1024 points, and the FP32 banded sweeps elsewhere (and
+ * for d8); the filters' add-back of v stays in FP64.  PG_AUTO builds the same tables and
  * then, per operator and direction, times the dense kernel against the FP32
  * banded sweep on the handle's own grid and keeps the faster.  Selecting
  * either builds the tables once (allocates and synchronises). */
@@ -221,6 +223,11 @@ typedef struct pg_lad_model {
  * back to the plain LAD operators. */
 int pg_lad_closure(pg_handle* h, const pg_lad_model* m, const double* div, const double* gmag, const double* rho,
                    const double* dt, double cv, double* beta, double* kappa, int* flag, void* stream);
+/* The closure's |grad rho| input: second-order central differences along
+ * every direction of more than one point (periodic lines wrap; the end points
+ * of non-periodic lines take one-sided first differences), in FP32
+ * arithmetic, stored as FP64. */
+int pg_lad_grad_magnitude(pg_handle* h, const double* rho, double* out, void* stream);
 /* Raw (unnormalised) feature rows of ns points (flat indices pts): raw[ns][PG_LAD_K]. */
 int pg_lad_features(pg_handle* h, const double* div, const double* gmag, const int64_t* pts, int64_t ns,
                     float* raw, void* stream);

@@ -90,6 +90,32 @@ def loss_and_grad(params, X, T, rounding=True):
     return loss, g
 
 
+def grad_magnitude(rho, periodic, d):
+    """|grad rho| of pg_lad_grad_magnitude: FP32 central differences (f32(rho_hi) - f32(rho_lo)) * s with
+    s = f32(1/d) / 2 (one-sided ends of non-periodic lines: f32(1/d), neighbour clamped), squares summed
+    over x, y, z, FP32 sqrt; F-ordered (nx, ny, nz) FP64 in and out."""
+    r = numpy.asarray(rho, dtype=numpy.float64).astype(numpy.float32)
+    g2 = numpy.zeros(r.shape, dtype=numpy.float64)
+    for ax in range(3):
+        n = r.shape[ax]
+        if n == 1:
+            continue
+        i = numpy.arange(n)
+        if periodic[ax]:
+            lo, hi = (i - 1) % n, (i + 1) % n
+            sc = numpy.full(n, numpy.float32(numpy.float32(1.0 / d[ax]) * numpy.float32(0.5)), dtype=numpy.float32)
+        else:
+            lo, hi = numpy.maximum(i - 1, 0), numpy.minimum(i + 1, n - 1)
+            sc = numpy.where((i == 0) | (i == n - 1), numpy.float32(1.0 / d[ax]),
+                             numpy.float32(numpy.float32(1.0 / d[ax]) * numpy.float32(0.5))).astype(numpy.float32)
+        shape = [1, 1, 1]
+        shape[ax] = n
+        dd = (numpy.take(r, hi, axis=ax) - numpy.take(r, lo, axis=ax)) * sc.reshape(shape)
+        dd = dd.astype(numpy.float32).astype(numpy.float64)
+        g2 = (dd * dd + g2).astype(numpy.float32).astype(numpy.float64)   # fma, then FP32 rounding
+    return numpy.sqrt(g2.astype(numpy.float32)).astype(numpy.float64)
+
+
 def features(div, gmag, periodic, delta):
     """Raw feature rows [npts, 64] of F-ordered (nx, ny, nz) fields, point order i + nx (j + ny k)."""
     div = numpy.asarray(div, dtype=numpy.float64)

@@ -110,6 +110,7 @@ SIGNATURES = [
     ("pg_ens_device_status", I, [P, ctypes.POINTER(ctypes.c_int)]),
     ("pg_lad_closure", I, [P, ctypes.POINTER(pg_lad_model), D, D, D, D, ctypes.c_double, D, D, D, P]),
     ("pg_lad_features", I, [P, D, D, D, ctypes.c_int64, D, P]),
+    ("pg_lad_grad_magnitude", I, [P, D, D, P]),
     ("pg_lad_normalize", I, [D, ctypes.c_int64, D, D, D, P]),
     ("pg_lad_train_step", I, [ctypes.POINTER(pg_lad_model), D, D, ctypes.c_int64, ctypes.c_float, D, D, D, P]),
     ("pg_lad_adam", I, [D, D, D, D, I, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, I, D, I, P]),

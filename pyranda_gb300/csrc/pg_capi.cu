@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -106,14 +107,15 @@ struct Ctx {
   double* work2 = nullptr;       // one field: forward-elimination scratch of a sweep
   double* partial = nullptr;     // reduction partials (+ per-member results)
   int* status = nullptr;         // device status word
+  int* emax = nullptr;           // exact d8 RHS: per member the largest exponent of the sweep input
   long long* moff = nullptr;     // ensembles: member point offsets (nmem + 1)
   double* mconst = nullptr;      // ensembles: per member 1/d1 1/d2 1/d3 1/GridLen GridLen
   double* host_in = nullptr;     // host-pointer variants
   double* host_out = nullptr;
   cudaStream_t stream = nullptr;
   std::vector<MemberOp> mops;    // host copy of the member-op arrays
-  // dense split-TF32 operators (PG_DENSE): used for d1, d8 and the compact
-  // filter where built; the Gaussian filter and every other case run the
+  // dense split-TF32 operators (PG_DENSE): used for d1 and the two filters
+  // where built; d8 (exact fixed-point RHS) and every other case run the
   // FP32 banded sweeps
   bool dense = false;
   bool dense_built = false;
@@ -128,6 +130,7 @@ void free_ctx(Ctx& c) {
   if (c.work2) cudaFree(c.work2);
   if (c.partial) cudaFree(c.partial);
   if (c.status) cudaFree(c.status);
+  if (c.emax) cudaFree(c.emax);
   if (c.moff) cudaFree(c.moff);
   if (c.mconst) cudaFree(c.mconst);
   if (c.host_in) cudaFree(c.host_in);
@@ -135,6 +138,38 @@ void free_ctx(Ctx& c) {
   if (c.stream) cudaStreamDestroy(c.stream);
   if (c.dense_blob) cudaFree(c.dense_blob);
   c = Ctx();
+}
+
+// The d8 RHS weights as integers times one FP32-exact scale, with at most 256
+// units of weight per row and an interior row proportional to the 8th
+// difference (c10d8: 60 x small integers, stencils.f90:519-526,573-591).
+// Then the FP32 sweeps evaluate the RHS exactly in 64-bit fixed point
+// (pg_sweep.cuh).
+bool integer_weights(const OpTables& t, std::vector<int>& iw, double& w) {
+  if (t.kind != OPK_D8 || t.null_op || t.n < 1) return false;
+  const size_t mid = (size_t)(t.n / 2);
+  w = 0.0;
+  for (int l = 0; l < 9 && w == 0.0; l++) w = std::fabs(t.rhs[mid * 9 + l]);
+  if (w == 0.0 || (double)(float)w != w) return false;
+  iw.assign((size_t)t.n * 9, 0);
+  for (int i = 0; i < t.n; i++) {
+    int units = 0;
+    for (int l = 0; l < 9; l++) {
+      const double x = t.rhs[(size_t)i * 9 + l];
+      const double q = std::nearbyint(x / w);
+      if (q * w != x || std::fabs(q) > 256.0) return false;
+      iw[(size_t)i * 9 + l] = (int)q;
+      units += std::abs((int)q);
+    }
+    if (units > 256) return false;
+  }
+  // the interior rows (4 .. n-5; the middle row is one when n >= 9) are iw[0] x the 8th
+  // difference: the sweeps keep it by a cascade of differences
+  static const int c8[9] = {1, -8, 28, -56, 70, -56, 28, -8, 1};
+  if (t.n >= 9)
+    for (int l = 0; l < 9; l++)
+      if (iw[mid * 9 + l] != iw[mid * 9] * c8[l]) return false;
+  return true;
 }
 
 // Upload the tables of every member, build the member-op arrays and
@@ -161,7 +196,7 @@ int build_ctx(Ctx& c, const std::vector<GridInfo>& g, int precision, const char*
     for (int k = 0; k < OPK_COUNT; k++)
       for (int d = 0; d < 3; d++) {
         const size_t n = (size_t)g[m].n[d];
-        total += align(n * 9 * 8) + align(n * 12 * 8) + align(n * 9 * 4) + align(n * 12 * 4);
+        total += align(n * 9 * 8) + align(n * 12 * 8) + align(n * 9 * 4) + align(n * 12 * 4) + align(n * 9 * 4);
       }
   const size_t ops_off = align(total);
   total = ops_off + sizeof(MemberOp) * (size_t)M * 2 * OPK_COUNT * 3;
@@ -187,6 +222,13 @@ int build_ctx(Ctx& c, const std::vector<GridInfo>& g, int precision, const char*
     }
     return dptr;
   };
+  auto put_i = [&](const std::vector<int>& v) -> const int* {
+    pos = align(pos);
+    const int* dptr = reinterpret_cast<const int*>((unsigned char*)c.blob + pos);
+    std::memcpy(&host[pos], v.data(), v.size() * 4);
+    pos += v.size() * 4;
+    return dptr;
+  };
   std::vector<MemberOp> mops((size_t)M * 2 * OPK_COUNT * 3);
   auto mindex = [&](int p, int k, int d, int m) { return (((size_t)p * OPK_COUNT + k) * 3 + d) * M + m; };
   static const int order[9] = {0, 1, 5, 6, 2, 3, 4, 7, 8};  // c1 c2 c6 c7 | c3 c4 c5 c8 | c9
@@ -194,6 +236,10 @@ int build_ctx(Ctx& c, const std::vector<GridInfo>& g, int precision, const char*
     for (int k = 0; k < OPK_COUNT; k++)
       for (int d = 0; d < 3; d++) {
         const OpTables& t = g[m].tab[k][d];
+        std::vector<int> iw;
+        double wsc = 0.0;
+        const bool exact = integer_weights(t, iw, wsc);
+        const int* rhs_i = put_i(exact ? iw : std::vector<int>((size_t)t.n * 9, 0));
         std::vector<double> lu12((size_t)t.n * 12, 0.0);
         for (int i = 0; i < t.n && !t.null_op; i++)
           for (int q = 0; q < 9; q++) lu12[(size_t)i * 12 + q] = t.lu[(size_t)i * 9 + order[q]];
@@ -210,6 +256,11 @@ int build_ctx(Ctx& c, const std::vector<GridInfo>& g, int precision, const char*
           const int mid = t.n / 2;
           for (int l = 0; l < 9; l++) o.ri[l] = t.null_op ? 0.0 : t.rhs[(size_t)mid * 9 + l];
           o.dm = g[m].dm[d];
+          o.rhs_i = rhs_i;
+          for (int l = 0; l < 9; l++) o.iw[l] = exact ? iw[(size_t)mid * 9 + l] : 0;
+          o.exact = exact ? 1 : 0;
+          o.wscale = (float)wsc;
+          o.pad2 = 0;
         }
       }
   for (int p = 0; p < 2; p++)
@@ -223,6 +274,8 @@ int build_ctx(Ctx& c, const std::vector<GridInfo>& g, int precision, const char*
         }
         OpRef& r = c.ops[p][k][d];
         const OpTables& t = g[0].tab[k][d];
+        r.exact = true;
+        for (int m = 0; m < M; m++) r.exact = r.exact && mops[mindex(p, k, d, m)].exact;
         r.dev = reinterpret_cast<const MemberOp*>((unsigned char*)c.blob + ops_off) + mindex(p, k, d, 0);
         r.nops = M;
         r.nlines = line0;
@@ -241,6 +294,7 @@ int build_ctx(Ctx& c, const std::vector<GridInfo>& g, int precision, const char*
   const size_t npart = std::max((size_t)kReduceBlocks, (size_t)M * kSegBlocks + 2 * (size_t)M);
   if (e == cudaSuccess) e = cudaMalloc(&c.partial, npart * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&c.status, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&c.emax, sizeof(int) * (size_t)M);
   if (e == cudaSuccess) e = cudaMemset(c.status, 0, sizeof(int));
   {  // per-member offsets and spacings (used by the ensemble reductions)
     std::vector<double> mc((size_t)M * 5);
@@ -306,7 +360,7 @@ std::vector<double> difference_form(const std::vector<double>& D, int n, bool pe
 int build_dense(Ctx& c, const std::vector<GridInfo>& g) {
   if (c.dense_built) return PG_OK;
   const int M = (int)g.size();
-  const int kinds[3] = {OPK_D1, OPK_D8, OPK_SF};
+  const int kinds[4] = {OPK_D1, OPK_D8, OPK_SF, OPK_GF};
   struct Uniq {
     int k, d, m, rows, kchunks;
     std::vector<uint32_t> planes;
@@ -318,6 +372,8 @@ int build_dense(Ctx& c, const std::vector<GridInfo>& g) {
   for (int k : kinds)
     for (int d = 0; d < 3; d++) {
       if (c.ops[PG_FP64][k][d].null_op) continue;
+      // d8 with the exact fixed-point RHS stays banded: split TF32 products cannot hold its cancellation
+      if (k == OPK_D8 && c.ops[PG_FP32][k][d].exact) continue;
       bool fits = true;
       for (int m = 0; m < M; m++) fits = fits && g[m].n[d] >= 16 && g[m].n[d] <= 1024;
       if (!fits) continue;
@@ -496,7 +552,7 @@ int autotune_dense(Ctx& c) {
           cudaEventRecord(e0, 0);
           if (way == 0) rc = launch_dense(ds, c.work, out, d, EPI_STORE, 0, c.status, nullptr);
           else {
-            SweepLaunch s{c.work, out, c.work2, &c.ops[PG_FP32][k][d], d, EPI_STORE, 0};
+            SweepLaunch s{c.work, out, c.work2, &c.ops[PG_FP32][k][d], d, EPI_STORE, 0, c.emax, c.moff};
             rc = launch_sweep(PG_FP32, s, nullptr);
           }
           cudaEventRecord(e1, 0);
@@ -539,7 +595,9 @@ int set_precision(Ctx& c, const std::vector<GridInfo>& g, int precision) {
   return PG_OK;
 }
 
-int sweep(Ctx& c, int kind, int dir, const double* in, double* out, int epi, int scale_pow, void* st) {
+// emax_ready: the exponents of `in` for the exact d8 RHS are already in c.emax
+int sweep(Ctx& c, int kind, int dir, const double* in, double* out, int epi, int scale_pow, void* st,
+          bool emax_ready = false) {
   if (c.dense && c.use_dense[kind][dir]) {
     if (in == out) {  // tiles read whole lines that other tiles write: work on a copy
       int rc = launch_copy(c.work2, in, c.npts, st);
@@ -548,7 +606,7 @@ int sweep(Ctx& c, int kind, int dir, const double* in, double* out, int epi, int
     }
     return launch_dense(c.dsets[kind][dir], in, out, dir, epi, scale_pow, c.status, st);
   }
-  SweepLaunch s{in, out, c.work2, &c.ops[c.precision][kind][dir], dir, epi, scale_pow};
+  SweepLaunch s{in, out, c.work2, &c.ops[c.precision][kind][dir], dir, epi, scale_pow, c.emax, c.moff, emax_ready};
   return launch_sweep(c.precision, s, st);
 }
 
@@ -583,7 +641,7 @@ int ring(Ctx& c, const double* in, double* out, void* st) {
   bool first = true;
   for (int d = 0; d < 3; d++) {
     if (c.ops[c.precision][OPK_D8][d].null_op) continue;
-    int rc = sweep(c, OPK_D8, d, in, out, first ? EPI_RING_SET : EPI_RING_MAX, 2, st);
+    int rc = sweep(c, OPK_D8, d, in, out, first ? EPI_RING_SET : EPI_RING_MAX, 2, st, !first);
     if (rc) return rc;
     first = false;
   }
@@ -596,12 +654,14 @@ int ring(Ctx& c, const double* in, double* out, void* st) {
 int ringv(Ctx& c, const double* vx, const double* vy, const double* vz, double* out, void* st) {
   const double* src[3] = {vx, vy, vz};
   bool first = true;
-  for (int d = 0; d < 3; d++) {
-    if (c.ops[c.precision][OPK_D8][d].null_op) continue;
-    for (int q = 0; q < 3; q++) {
-      int rc = sweep(c, OPK_D8, d, src[q], out, first ? EPI_RING_SET : EPI_RING_MAX, 1, st);
+  for (int q = 0; q < 3; q++) {  // component-major: the exponents of one input serve its three sweeps
+    bool ready = false;
+    for (int d = 0; d < 3; d++) {
+      if (c.ops[c.precision][OPK_D8][d].null_op) continue;
+      int rc = sweep(c, OPK_D8, d, src[q], out, first ? EPI_RING_SET : EPI_RING_MAX, 1, st, ready);
       if (rc) return rc;
       first = false;
+      ready = true;
     }
   }
   if (first) return launch_fill(out, 0.0, c.npts, st);
@@ -1003,6 +1063,7 @@ LadGrid lad_grid(const GridInfo& g) {
     lg.per[d] = g.periodic[d];
   }
   lg.delta = std::max(std::max(g.dm[0], g.dm[1]), g.dm[2]);  // the largest mesh spacing
+  for (int d = 0; d < 3; d++) lg.rd[d] = (float)(1.0 / g.d[d]);
   return lg;
 }
 }  // namespace
@@ -1014,6 +1075,15 @@ int pg_lad_closure(pg_handle* h, const pg_lad_model* m, const double* div, const
     return PG_EINVAL;
   LadInferArgs a{*m, lad_grid(h->g), div, gmag, rho, dt, cv, beta, kappa, flag};
   return launch_lad_infer(a, stream);
+}
+
+int pg_lad_grad_magnitude(pg_handle* h, const double* rho, double* out, void* stream) {
+  if (!h || !rho || !out) return PG_EINVAL;
+  if (rho == out) {
+    set_error("pg_lad_grad_magnitude: in and out must differ");
+    return PG_EINVAL;
+  }
+  return launch_lad_grad_magnitude(rho, lad_grid(h->g), out, stream);
 }
 
 int pg_lad_features(pg_handle* h, const double* div, const double* gmag, const int64_t* pts, int64_t ns,

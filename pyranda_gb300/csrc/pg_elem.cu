@@ -4,6 +4,7 @@
 // (16-byte accesses) sized to a multiple of the SM count.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 
@@ -404,6 +405,32 @@ int launch_diff(const double* bulk, const double* rho, double gl, int64_t n, dou
   reduce_final<2><<<1, kThreads, 0, s>>>(partial, g, out);
   count_launch(4);
   return check("diff");
+}
+
+// The fixed-point scale of the exact d8 RHS: per member the largest biased
+// exponent field of its values (bits 52..62; infinities and NaN give 2047).
+__global__ void max_exponent_kernel(const double* __restrict__ in, const long long* __restrict__ moff,
+                                    int* __restrict__ emax) {
+  const int m = blockIdx.y;
+  const long long a = moff[m], b = moff[m + 1];
+  unsigned e = 0;
+  for (long long i = a + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < b;
+       i += (long long)gridDim.x * blockDim.x)
+    e = max(e, ((unsigned)__double2hiint(in[i]) >> 20) & 0x7ffu);
+  e = __reduce_max_sync(0xffffffffu, e);
+  if ((threadIdx.x & 31) == 0 && e) atomicMax(emax + m, (int)e);
+}
+
+int launch_max_exponent(const double* in, const long long* moff, int nmem, int* emax, void* stream) {
+  if (nmem <= 0) return PG_OK;
+  cudaError_t e = cudaMemsetAsync(emax, 0, sizeof(int) * (size_t)nmem, (cudaStream_t)stream);
+  if (e != cudaSuccess) {
+    set_error("max_exponent: %s", cudaGetErrorString(e));
+    return PG_ECUDA;
+  }
+  const int bx = std::max(1, std::min(152 * 8, (152 * 8 + nmem - 1) / nmem * 2));
+  max_exponent_kernel<<<dim3((unsigned)bx, (unsigned)nmem), kThreads, 0, (cudaStream_t)stream>>>(in, moff, emax);
+  return check("max_exponent");
 }
 
 int launch_check_finite(const double* in, int64_t n, int* flag, void* stream) {

@@ -44,6 +44,14 @@ struct MemberOp {
   long long off;    // first point of this grid in the flat field
   double ri[9];     // interior RHS weights
   double dm;        // mesh spacing along the direction (ring scale)
+  // d8 with integer weights (RHS weight = wscale x integer): the FP32 sweeps
+  // evaluate its RHS exactly in 64-bit fixed point (the 8th difference
+  // cancels ~40 bits of a smooth field)
+  const int* rhs_i; // n x 9 per-row integer RHS weights
+  int iw[9];        // interior integer weights
+  int exact;        // 1: rhs_i / iw / wscale are valid
+  float wscale;
+  int pad2;
 };
 
 // Host view of one (kind, direction, precision) operator of a grid or ensemble.
@@ -53,6 +61,7 @@ struct OpRef {
   long long nlines = 0;           // total lines over all members
   int kind = 0;
   bool periodic = false, implicit = false, addback = false, null_op = true;
+  bool exact = false;             // every member's MemberOp::exact
 };
 
 struct SweepLaunch {
@@ -63,6 +72,10 @@ struct SweepLaunch {
   int dir;
   int epi;         // EPI_*
   int scale_pow;   // ring epilogues scale |r| by dm^scale_pow
+  // exact d8 RHS (FP32 sweeps): per member the largest binary exponent of `in`
+  int* emax = nullptr;              // nops ints
+  const long long* moff = nullptr;  // member point offsets (nops + 1)
+  bool emax_ready = false;          // emax already holds the exponents of `in`
 };
 
 // Launches one directional sweep over every member.  Returns a pg_status.
@@ -117,6 +130,8 @@ int launch_diff(const double* bulk, const double* rho, double gl2, int64_t n, do
                 double* out, void* stream);
 int launch_reduce(int op, const double* in, int64_t n, double* partial, double* out, void* stream);
 int launch_check_finite(const double* in, int64_t n, int* flag, void* stream);
+// Per member m, the largest biased binary exponent of in[moff[m] .. moff[m+1]) (0 for an all-zero member).
+int launch_max_exponent(const double* in, const long long* moff, int nmem, int* emax, void* stream);
 int launch_mesh(int which, double* out, int nx, int ny, int nz, const double x1f[3],
                 const double d[3], const double dm[3], void* stream);
 
@@ -143,6 +158,7 @@ struct LadGrid {
   int n[3];
   int per[3];
   double delta;  // largest mesh spacing
+  float rd[3];   // 1 / mesh spacing per direction (FP32)
 };
 struct LadInferArgs {
   pg_lad_model model;
@@ -165,6 +181,7 @@ struct LadTrainArgs {
 int launch_lad_infer(const LadInferArgs& a, void* stream);
 int launch_lad_features(const double* div, const double* gmag, const LadGrid& g, const int64_t* pts, int64_t ns,
                         float* raw, void* stream);
+int launch_lad_grad_magnitude(const double* rho, const LadGrid& g, double* out, void* stream);
 int launch_lad_normalize(const float* raw, int64_t ns, const float* xm, const float* xs, void* X, void* stream);
 int launch_lad_train(const LadTrainArgs& a, void* stream);
 int launch_lad_adam(float* p, float* m, float* v, const float* g, int n, float lr, float b1, float b2, float eps,

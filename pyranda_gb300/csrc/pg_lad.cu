@@ -2,7 +2,8 @@
 // beta and conductivity kappa of the LAD method from local features.
 //
 // Features of a point (kLadIn = 55, padded to kLadK = 64 inputs): the
-// 27-point (3 x 3 x 3) stencils of  div(u) * D  and  |grad rho| * D  around
+// 27-point (3 x 3 x 3) stencils of  div(u) * D  and  |grad rho| * D  (|grad rho|
+// by second-order central differences, lad_gradmag_kernel) around
 // it (periodic directions wrap, one-sided directions clamp, a direction of one
 // point repeats the point), then D itself, where D is the largest mesh
 // spacing (the spacing across the shocks of the training problems, so that
@@ -248,6 +249,39 @@ __global__ void __launch_bounds__(kInferThreads) lad_infer_kernel(const LadInfer
   if (__syncthreads_or(out_of_range) && tid == 0) atomicExch(A.flag, 1);
 }
 
+// |grad rho| by central differences, FP32 arithmetic: one thread per point,
+// 32-bit indices (fields hold fewer than 2^31 points).
+__global__ void lad_gradmag_kernel(const double* __restrict__ rho, const LadGrid G, double* __restrict__ out) {
+  const unsigned nx = (unsigned)G.n[0], ny = (unsigned)G.n[1], nz = (unsigned)G.n[2];
+  const unsigned np = nx * ny * nz;
+  const unsigned st[3] = {1u, nx, nx * ny};
+  for (unsigned p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+    const unsigned r = p / nx;
+    const unsigned idx[3] = {p - r * nx, r % ny, r / ny};
+    float g2 = 0.0f;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const unsigned n = (unsigned)G.n[d], i = idx[d];
+      if (n == 1) continue;
+      unsigned lo, hi;
+      float sc = G.rd[d];
+      if (G.per[d]) {
+        lo = (i == 0) ? n - 1 : i - 1;
+        hi = (i == n - 1) ? 0 : i + 1;
+        sc *= 0.5f;
+      } else {
+        lo = (i == 0) ? 0 : i - 1;
+        hi = (i == n - 1) ? n - 1 : i + 1;
+        if (i != 0 && i != n - 1) sc *= 0.5f;
+      }
+      const float a = d2f_bits(rho[p + (hi - i) * st[d]]), b = d2f_bits(rho[p - (i - lo) * st[d]]);
+      const float dd = (a - b) * sc;
+      g2 = fmaf(dd, dd, g2);
+    }
+    out[p] = f2d_bits(sqrtf(g2));
+  }
+}
+
 // ----------------------------------------------------------------- training
 // Feature rows for given points (training-set extraction): X[s][0..63] BF16.
 __global__ void lad_features_kernel(const double* __restrict__ div, const double* __restrict__ gmag, LadGrid G,
@@ -472,6 +506,15 @@ int launch_lad_infer(const LadInferArgs& a, void* stream) {
   lad_infer_kernel<<<blocks, kInferThreads, smem, (cudaStream_t)stream>>>(a);
   count_launch();
   return lad_check("lad inference");
+}
+
+int launch_lad_grad_magnitude(const double* rho, const LadGrid& g, double* out, void* stream) {
+  const int64_t np = (int64_t)g.n[0] * g.n[1] * g.n[2];
+  const int64_t b = (np + 255) / 256;
+  lad_gradmag_kernel<<<(unsigned)(b < 152 * 16 ? (b > 0 ? b : 1) : 152 * 16), 256, 0, (cudaStream_t)stream>>>(rho, g,
+                                                                                                             out);
+  count_launch();
+  return lad_check("lad grad magnitude");
 }
 
 int launch_lad_features(const double* div, const double* gmag, const LadGrid& g, const int64_t* pts, int64_t ns,

@@ -29,6 +29,7 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <type_traits>
 
 #include "pg_internal.h"
 
@@ -42,6 +43,7 @@ struct KParams {
   int nops;
   long long nlines;            // lines over all grids
   int scale_pow;               // ring epilogues: scale = dm^scale_pow
+  const int* emax;             // exact d8 RHS: per grid the largest exponent of `in`
 };
 
 constexpr int kSweepThreads = 128;
@@ -76,12 +78,94 @@ __device__ __forceinline__ double f2d_bits(float x) {
   return __hiloint2double((int)hi, (int)lo);
 }
 
+// Exact d8 RHS of the FP32 sweeps.  The 8th difference of a smooth field
+// cancels about 40 of its 53 bits, more than FP32 holds.  The d8 weights are
+// integers times one scale (c10d8: 60 x binomial coefficients), so every
+// value of the grid becomes a 64-bit fixed-point number at the grid's largest
+// binary exponent E (53 significant bits for the largest values, round half
+// up), the weighted sums of the RHS are exact in 64-bit integers (at most
+// 2^62 in magnitude: 254 units of weight times 2^54), and the only rounding
+// is the conversion of the exact sum to FP32 before the solve.
+// (branch-free, so that a prefetched load is not waited for before its use)
+__device__ __forceinline__ long long to_fixed(double d, int E) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const int ex = (int)((b >> 52) & 0x7ffULL);
+  const int sh = E - ex;
+  const int shc = min(max(sh, 0), 62);
+  const long long mant = (long long)((b & 0xfffffffffffffULL) | (1ULL << 52));
+  long long m = (mant + ((1LL << shc) >> 1)) >> shc;
+  m = (ex == 0 || sh >= 54) ? 0LL : m;
+  return (b >> 63) ? -m : m;
+}
+
+// s x 2^(E - 1075) x w in FP32: the significand rounded to nearest even,
+// below the FP32 normal range flushed to zero; NaN when E marks an infinity
+// or NaN in the grid.
+__device__ __forceinline__ float fixed_to_float(long long s, int E, float w) {
+  if (E >= 2047) return __uint_as_float(0x7fc00000u);
+  if (s == 0) return 0.0f;
+  const unsigned long long a = (unsigned long long)(s < 0 ? -s : s);
+  int top = 63 - __clzll((long long)a);
+  unsigned long long sig;
+  if (top <= 23) {
+    sig = a << (23 - top);
+  } else {
+    const int sh = top - 23;
+    sig = a >> sh;
+    const unsigned long long rem = a & ((1ULL << sh) - 1ULL), half = 1ULL << (sh - 1);
+    sig += (rem > half || (rem == half && (sig & 1ULL))) ? 1ULL : 0ULL;
+    if (sig >> 24) {
+      sig >>= 1;
+      top++;
+    }
+  }
+  const int be = top + E - 948;  // biased FP32 exponent of a x 2^(E - 1075)
+  float f;
+  if (be <= 0) f = 0.0f;
+  else if (be >= 255) f = __uint_as_float(0x7f800000u);
+  else f = __uint_as_float(((unsigned)be << 23) | ((unsigned)sig & 0x7fffffu));
+  f *= w;
+  return s < 0 ? -f : f;
+}
+
+// Running differences of a stream: after push(x_p), c[q] holds the q-th
+// backward difference at p (q = 0..7) and push returns the 8th.  |x| <= 2^53
+// keeps every difference within 2^61.
+struct Cascade {
+  long long c[8];
+  __device__ __forceinline__ long long push(long long x) {
+    long long t = x;
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const long long u = t - c[q];
+      c[q] = t;
+      t = u;
+    }
+    return t;
+  }
+};
+
 template <typename T>
 __device__ __forceinline__ T from_f64(double v) { return (T)v; }
 template <>
 __device__ __forceinline__ float from_f64<float>(double v) { return d2f_bits(v); }
 template <typename T>
 __device__ __forceinline__ double to_f64(T v) { return (double)v; }
+
+// a grid value as the RHS arithmetic's type (E: the fixed-point exponent)
+template <typename TR>
+__device__ __forceinline__ TR load_as(double v, int) { return from_f64<TR>(v); }
+template <>
+__device__ __forceinline__ long long load_as<long long>(double v, int E) { return to_fixed(v, E); }
+
+// an RHS value as the solve's type
+__device__ __forceinline__ float solve_value(float x, int, float) { return x; }
+__device__ __forceinline__ double solve_value(double x, int, float) { return x; }
+__device__ __forceinline__ float solve_value(long long x, int E, float w) { return fixed_to_float(x, E, w); }
+
+// type of the RHS weight tables read by each RHS arithmetic
+template <typename TR> struct WeightOf { using type = TR; };
+template <> struct WeightOf<long long> { using type = int; };
 template <>
 __device__ __forceinline__ double to_f64<float>(float v) { return f2d_bits(v); }
 
@@ -119,7 +203,8 @@ template <typename T>
 struct Line {
   const double* __restrict__ in;  // first point of the line
   int stride, n;
-  __device__ __forceinline__ T v(int p) const { return from_f64<T>(in[p * stride]); }
+  int e;                          // fixed-point exponent (T = long long)
+  __device__ __forceinline__ T v(int p) const { return load_as<T>(in[p * stride], e); }
   __device__ __forceinline__ T w(int p) const {  // periodic wrap
     const int q = p < 0 ? p + n : (p >= n ? p - n : p);
     return v(q);
@@ -128,10 +213,10 @@ struct Line {
 
 // RHS of one edge row (rows 0..3 and n-4..n-1) straight from global memory,
 // with the reference's periodic-halo or one-sided (boundary code 0) formulas.
-template <typename T, int KIND, bool PER>
-__device__ __forceinline__ T edge_rhs(const Line<T>& ln, int i, const T* __restrict__ R) {
+template <typename T, int KIND, bool PER, typename W>
+__device__ __forceinline__ T edge_rhs(const Line<T>& ln, int i, const W* __restrict__ R) {
   const int n = ln.n;
-  const T* r = R + i * 9;
+  const W* r = R + i * 9;
   if (KIND == 1) {
     if (PER)  // compact_d1.f90:141-147, :185-191 (the halo is the wrapped line)
       return ldc(r + 4) * (ln.w(i + 1) - ln.w(i - 1)) + ldc(r + 5) * (ln.w(i + 2) - ln.w(i - 2)) +
@@ -203,8 +288,10 @@ __device__ __forceinline__ T ring_rhs(const T* ring, int k, const T* ai) {
 }
 
 // KIND: 1 = d1 evaluator, 4 = r4 evaluator.  DIR: 0 = x, 1 = y, 2 = z.
-template <typename T, int KIND, bool PER, bool IMPL, bool ADDBACK, int DIR, int EPI>
+// TR: the RHS arithmetic (T, or long long for the exact d8 RHS of FP32 sweeps).
+template <typename T, int KIND, bool PER, bool IMPL, bool ADDBACK, int DIR, int EPI, typename TR = T>
 __global__ void __launch_bounds__(kSweepThreads) sweep_kernel(const KParams P) {
+  constexpr bool kExact = std::is_same<TR, long long>::value;
   const int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (L >= P.nlines) return;
   // the grid (ensemble member) owning this line: last entry with line0 <= L
@@ -237,8 +324,11 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_kernel(const KParams P) {
   base += op.off;
   const double* __restrict__ pin = P.in + base;
   double* __restrict__ pout = P.out + base;
-  const Line<T> ln{pin, st, n};
-  const T* __restrict__ R = reinterpret_cast<const T*>(op.rhs);
+  const int E = kExact ? __ldg(P.emax + m) : 0;
+  const float wsc = kExact ? op.wscale : 1.0f;
+  const Line<TR> ln{pin, st, n, E};
+  using W = typename WeightOf<TR>::type;
+  const W* __restrict__ R = reinterpret_cast<const W*>(kExact ? (const void*)op.rhs_i : op.rhs);
   const T* __restrict__ C = reinterpret_cast<const T*>(op.lu);  // 12 per row
   T* __restrict__ ps = reinterpret_cast<T*>(P.scratch) + op.off + Lm;  // row i at ps[i * nl]
   const int nl = (int)op.lines;
@@ -249,7 +339,7 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_kernel(const KParams P) {
   // edge rows first: they may need wrapped values of the far end of the line
   T e[8];
 #pragma unroll
-  for (int q = 0; q < 8; q++) e[q] = edge_rhs<T, KIND, PER>(ln, q < 4 ? q : n - 8 + q, R);
+  for (int q = 0; q < 8; q++) e[q] = solve_value(edge_rhs<TR, KIND, PER, W>(ln, q < 4 ? q : n - 8 + q, R), E, wsc);
 
   auto put = [&](int p, T x, double vin, double o) {
     pout[p * st] = epilogue<EPI>(to_f64<T>(x), vin, o, sc, ADDBACK);
@@ -316,23 +406,42 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_kernel(const KParams P) {
   // interior rows 4 .. n-5: ring[s] holds v[i0 - H + s] at the start of a block
   // of kRing rows; the slot of the oldest value is refilled kRing positions ahead
   {
-    T ai[9];
+    TR ai[9];
 #pragma unroll
-    for (int k = 0; k < 9; k++) ai[k] = (T)op.ri[k];
-    T ring[kRing];
+    for (int k = 0; k < 9; k++) ai[k] = kExact ? (TR)op.iw[k] : (TR)op.ri[k];
+    // the exact RHS keeps the raw FP64 values in the ring and converts a value when it is used
+    using RT = typename std::conditional<kExact, double, TR>::type;
+    auto ld = [&](int p) -> RT {
+      if constexpr (kExact) return pin[p * st];
+      else return ln.v(p);
+    };
+    RT ring[kRing];
 #pragma unroll
     for (int s2 = 0; s2 < kRing; s2++) {
       const int p = 4 - H + s2;
-      ring[s2] = (p < n) ? ln.v(p) : T(0);
+      ring[s2] = (p < n) ? ld(p) : RT(0);
     }
+    // exact d8: the interior weights are iw[0] x (1, -8, 28, -56, 70, -56, 28, -8, 1), so the
+    // RHS of row i is iw[0] times the 8th backward difference at i + 4, kept by a cascade of
+    // first differences (8 integer subtractions per point); primed with points 0..7
+    Cascade cas{};
+    if constexpr (kExact) {
+#pragma unroll
+      for (int s2 = 0; s2 < 8; s2++) cas.push(to_fixed(ring[s2], E));
+    }
+    const float wi = kExact ? wsc * (float)op.iw[0] : 0.0f;
+    auto rhs_at = [&](int k) -> T {
+      if constexpr (kExact) return fixed_to_float(cas.push(to_fixed(ring[(k + 8) % kRing], E)), E, wi);
+      else return solve_value(ring_rhs<TR, KIND>(ring, k, ai), E, wsc);
+    };
     int i0 = 4;
     for (; i0 + kRing <= n - 4; i0 += kRing) {  // whole blocks: no guards
 #pragma unroll
       for (int k = 0; k < kRing; k++) {
         const int i = i0 + k;
-        const T rhs = ring_rhs<T, KIND>(ring, k, ai);
+        const T rhs = rhs_at(k);
         const int p = i - H + kRing;
-        ring[k] = (p < n) ? ln.v(p) : T(0);
+        ring[k] = (p < n) ? ld(p) : RT(0);
         fwd_in(i, rhs);
       }
     }
@@ -340,9 +449,9 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_kernel(const KParams P) {
     for (int k = 0; k < kRing; k++) {  // last partial block
       const int i = i0 + k;
       if (i <= n - 5) {
-        const T rhs = ring_rhs<T, KIND>(ring, k, ai);
+        const T rhs = rhs_at(k);
         const int p = i - H + kRing;
-        ring[k] = (p < n) ? ln.v(p) : T(0);
+        ring[k] = (p < n) ? ld(p) : RT(0);
         fwd_in(i, rhs);
       }
     }
@@ -401,10 +510,11 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_kernel(const KParams P) {
   }
 }
 
-template <typename T, int KIND, bool PER, bool IMPL, bool ADDBACK, int DIR, int EPI>
+template <typename T, int KIND, bool PER, bool IMPL, bool ADDBACK, int DIR, int EPI, typename TR = T>
 int launch_t(const KParams& P, void* stream) {
   const int64_t nb = (P.nlines + kSweepThreads - 1) / kSweepThreads;
-  sweep_kernel<T, KIND, PER, IMPL, ADDBACK, DIR, EPI><<<(unsigned)nb, kSweepThreads, 0, (cudaStream_t)stream>>>(P);
+  sweep_kernel<T, KIND, PER, IMPL, ADDBACK, DIR, EPI, TR>
+      <<<(unsigned)nb, kSweepThreads, 0, (cudaStream_t)stream>>>(P);
   count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
@@ -414,14 +524,14 @@ int launch_t(const KParams& P, void* stream) {
   return PG_OK;
 }
 
-template <typename T, int KIND, bool PER, bool IMPL, bool ADDBACK>
+template <typename T, int KIND, bool PER, bool IMPL, bool ADDBACK, typename TR = T>
 int dispatch_dir_epi(const KParams& P, int dir, int epi, void* st) {
-#define PG_EPI_CASES(D)                                                                      \
-  switch (epi) {                                                                             \
-    case EPI_STORE: return launch_t<T, KIND, PER, IMPL, ADDBACK, D, EPI_STORE>(P, st);       \
-    case EPI_ADD: return launch_t<T, KIND, PER, IMPL, ADDBACK, D, EPI_ADD>(P, st);           \
-    case EPI_RING_SET: return launch_t<T, KIND, PER, IMPL, ADDBACK, D, EPI_RING_SET>(P, st); \
-    default: return launch_t<T, KIND, PER, IMPL, ADDBACK, D, EPI_RING_MAX>(P, st);           \
+#define PG_EPI_CASES(D)                                                                          \
+  switch (epi) {                                                                                 \
+    case EPI_STORE: return launch_t<T, KIND, PER, IMPL, ADDBACK, D, EPI_STORE, TR>(P, st);       \
+    case EPI_ADD: return launch_t<T, KIND, PER, IMPL, ADDBACK, D, EPI_ADD, TR>(P, st);           \
+    case EPI_RING_SET: return launch_t<T, KIND, PER, IMPL, ADDBACK, D, EPI_RING_SET, TR>(P, st); \
+    default: return launch_t<T, KIND, PER, IMPL, ADDBACK, D, EPI_RING_MAX, TR>(P, st);           \
   }
   if (dir == 0) { PG_EPI_CASES(0) }
   if (dir == 1) { PG_EPI_CASES(1) }
@@ -435,9 +545,15 @@ int dispatch_kind(const OpRef& op, const KParams& P, int dir, int epi, void* st)
     case OPK_D1:
       return op.periodic ? dispatch_dir_epi<T, 1, true, true, false>(P, dir, epi, st)
                          : dispatch_dir_epi<T, 1, false, true, false>(P, dir, epi, st);
-    case OPK_D8:
+    case OPK_D8: {
+      // FP32 sweeps take the exact fixed-point RHS where the weights allow it
+      using TRX = typename std::conditional<std::is_same<T, float>::value, long long, T>::type;
+      if (std::is_same<T, float>::value && op.exact)
+        return op.periodic ? dispatch_dir_epi<T, 4, true, true, false, TRX>(P, dir, epi, st)
+                           : dispatch_dir_epi<T, 4, false, true, false, TRX>(P, dir, epi, st);
       return op.periodic ? dispatch_dir_epi<T, 4, true, true, false>(P, dir, epi, st)
                          : dispatch_dir_epi<T, 4, false, true, false>(P, dir, epi, st);
+    }
     case OPK_SF:
       return op.periodic ? dispatch_dir_epi<T, 4, true, true, true>(P, dir, epi, st)
                          : dispatch_dir_epi<T, 4, false, true, true>(P, dir, epi, st);

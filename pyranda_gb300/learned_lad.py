@@ -8,8 +8,9 @@ coefficients) is
     kappa = gbar( ring(T) rho cv / (T dt) ) * 1e-3,
 which costs two ring operators (six 8th-derivative sweeps) and two Gaussian
 filters (six sweeps) per RK stage.  The learned closure replaces them with one
-gradient (three first-derivative sweeps, for |grad rho|) and one fused
-feature-gather + MLP kernel (``pg_lad_closure``).  The plain closure stays
+pass for |grad rho| (second-order central differences,
+``pg_lad_grad_magnitude``) and one fused feature-gather + MLP kernel
+(``pg_lad_closure``).  The plain closure stays
 both the judge of the learned one's error and its fallback: the kernel raises
 a flag when a prediction leaves the training range, and
 ``pyrandaLearnedLAD.step`` then re-runs that RK step with the plain closure
@@ -88,8 +89,11 @@ class LadModel:
 
 # ------------------------------------------------------------------ features
 def grad_magnitude(grid, rho):
-    gx, gy, gz = grid.grad(rho)
-    return torch.sqrt(gx * gx + gy * gy + gz * gz)
+    """|grad rho| by second-order central differences (pg_lad_grad_magnitude): one pass over rho."""
+    out = grid.empty()
+    _lib.check(grid.lib.pg_lad_grad_magnitude(grid.h, _ptr(grid.field(rho)), _ptr(out), _stream()),
+               "pg_lad_grad_magnitude")
+    return out
 
 
 def raw_features(grid, div, gmag, pts):
@@ -172,12 +176,16 @@ def fit_normalisation(model, raw, T, margin=0.25):
     return Tn.contiguous()
 
 
-def train(model, X, Tn, iters=3000, batch=8192, lr=1e-3, seed=0, log_every=0):
-    """Adam over random batches of (X, Tn); returns the loss history (host floats, one per log point)."""
+def train(model, X, Tn, iters=3000, batch=8192, lr=1e-3, seed=0, log_every=0, cosine=False):
+    """Adam over random batches of (X, Tn); returns the loss history (host floats, one per log point).
+
+    cosine: the learning rate follows lr (1 + cos(pi it / iters)) / 2 down to zero."""
     tr = Trainer(model, lr=lr)
     gen = torch.Generator(device=X.device).manual_seed(seed)
     hist = []
     for it in range(iters):
+        if cosine:
+            tr.lr = lr * 0.5 * (1.0 + math.cos(math.pi * it / iters))
         idx = torch.randint(0, X.shape[0], (min(batch, X.shape[0]),), device=X.device, generator=gen)
         loss = tr.step(X.index_select(0, idx).contiguous(), Tn.index_select(0, idx).contiguous())
         if log_every and (it % log_every == 0 or it == iters - 1):
@@ -185,10 +193,12 @@ def train(model, X, Tn, iters=3000, batch=8192, lr=1e-3, seed=0, log_every=0):
     return hist
 
 
-def shock_training_set(runs=20, snapshots_per_run=100, shape=(128, 64, 64), points=2048, seed=1,
+def shock_training_set(runs=20, snapshots_per_run=100, shape=(256, 64, 64), points=2048, seed=1,
                        steps_between=1, precision="fp32"):
     """Snapshots of seeded shock-interface runs with the plain closure.
 
+    The default grid, 256 x 64 x 64 on [0, 4] x [0, 1)^2, has equal spacings
+    in x, y and z, like the 512 x 128 x 128 shock problem the closure serves.
     Mach ~ U[1.2, 3.0] and amplitude ~ U[0.01, 0.1] from default_rng(seed);
     each snapshot contributes `points` points, half where beta is largest
     (shock and interface) and half uniformly at random.  Returns

@@ -216,3 +216,21 @@ def test_trained_closure_beats_untrained_and_none():
     print("density L1 error vs plain LAD:", err)
     assert err["learned"] < 0.05, err               # the learned run stays close to the plain one
     assert err["learned"] < err["off"], err         # while no closure at all does not survive
+
+
+@pytest.mark.parametrize("per", [(True, False, True), (False, True, False)], ids=["PNP", "NPN"])
+def test_grad_magnitude_matches_oracle(per):
+    from oracle import lad_mlp as L
+    from pyranda_gb300.grid import Grid
+    from pyranda_gb300.learned_lad import grad_magnitude
+    n = (24, 20, 12)
+    g = Grid(n, per, (0, 0, 0), (1.0, 2.0, 0.5), precision="fp64")
+    r = numpy.random.default_rng(11)
+    rho = numpy.asfortranarray(1.0 + r.random(n))
+    got = to_host(grad_magnitude(g, to_dev(rho, torch)))
+    want = L.grad_magnitude(rho, per, g.mesh_d)
+    assert numpy.abs(got - want).max() <= 1e-6 * numpy.abs(want).max()
+    flat = Grid((16, 1, 8), (True, False, True), (0, 0, 0), (1.0, 1.0, 1.0), precision="fp64")
+    f = numpy.asfortranarray(1.0 + r.random((16, 1, 8)))
+    got = to_host(grad_magnitude(flat, to_dev(f, torch)))
+    assert numpy.abs(got - L.grad_magnitude(f, (True, False, True), flat.mesh_d)).max() <= 1e-6 * got.max()

@@ -5,6 +5,7 @@ periodic and one-sided (NONE) directions, on tile-aligned and ragged sizes, on
 null directions (n = 1 and n < 4) and on long lines (tile widths 32/16/8).
 """
 import ctypes
+import math
 
 import numpy
 import pytest
@@ -255,3 +256,29 @@ def test_bounded_wait_reports_timeout_and_context_survives(grids):
     shape = CASES[0][0]
     v = smooth_field(shape, 4)
     assert rel_l2(to_host(g.ddx(to_dev(v, torch))), o.ddx(v)) < 1e-12
+
+
+@pytest.mark.parametrize("per", [(True, True, True), (False, True, False)], ids=["PPP", "NPN"])
+def test_fp32_d8_rhs_is_exact(per):
+    """d8 and ring on the FP32 path take their RHS in exact 64-bit fixed point.
+
+    On a smooth field with a large mean the 8th difference cancels ~40 of the
+    53 bits, so an FP32 RHS would be noise; with the exact RHS only the FP32
+    solve rounds, and the result stays within 2e-6 relative L2 of the FP64 path.
+    """
+    from pyranda_gb300.grid import Grid
+    shape = (64, 48, 40)
+    x1, xn = (0.0, 0.0, 0.0), (1.0, 1.0, 1.0)
+    g64 = Grid(shape, per, x1, xn, precision="fp64")
+    g32 = Grid(shape, per, x1, xn, precision="fp32")
+    x, y, z = (g64.mesh(d) for d in range(3))
+    v = 5.0 + torch.sin(2 * math.pi * x) * torch.cos(2 * math.pi * y) + 0.5 * torch.sin(2 * math.pi * z + 0.3)
+    for d in range(3):
+        a, b = g64.d8(d, v), g32.d8(d, v)
+        err = float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(a))
+        assert err <= 2e-6, ("d8", d, err)
+    a, b = g64.ring(v), g32.ring(v)
+    assert float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(a)) <= 2e-6
+    vs = [v, v * 0.5 - 1.0, torch.cos(2 * math.pi * y)]
+    a, b = g64.ringv(*vs), g32.ringv(*vs)
+    assert float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(a)) <= 2e-6
