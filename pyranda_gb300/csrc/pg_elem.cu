@@ -58,10 +58,11 @@ __global__ void rk_stage_kernel(const RkArgs a, int nvar, const double* __restri
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double dt = DT_FIELD ? dtp[i] : dt0;
     for (int v = 0; v < nvar; v++) {
-      const double tmp1 = A * a.PHI[v][i];
-      const double phi = dt * a.F[v][i] + tmp1;
+      // rounding spelled out (one product, then two fused multiply-adds): the fused EOM
+      // kernels that apply a stage themselves repeat exactly these operations
+      const double phi = __fma_rn(dt, a.F[v][i], __dmul_rn(A, a.PHI[v][i]));
       a.PHI[v][i] = phi;
-      a.U[v][i] = a.U[v][i] + B * phi;
+      a.U[v][i] = __fma_rn(B, phi, a.U[v][i]);
     }
   }
 }

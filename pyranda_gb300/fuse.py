@@ -39,6 +39,16 @@ from .build import ARCH, OUT, nvcc
 
 JIT_DIR = os.path.join(OUT, "jit")
 
+
+class _RkDone:
+    """Returned for a PDE right-hand side whose kernel already applied the RK stage update."""
+
+    def __repr__(self):
+        return "RK_DONE"
+
+
+RK_DONE = _RkDone()
+
 _UNARY = {"sqrt": "PG_SQRT({0})", "abs": "PG_ABS({0})", "absolute": "PG_ABS({0})", "exp": "PG_EXP({0})",
           "log": "PG_LOG({0})", "sin": "PG_SIN({0})", "cos": "PG_COS({0})", "tan": "PG_TAN({0})",
           "tanh": "PG_TANH({0})", "sinh": "PG_SINH({0})", "cosh": "PG_COSH({0})", "arctan": "PG_ATAN({0})",
@@ -233,6 +243,8 @@ class Kernel:
         self.eager = eval(compile(lam, "<fused %d>" % index, "eval"), globals_)
         self.sig = None      # leaf kinds of the recording call: f field, s device scalar, c number
         self.fn = None
+        self.rk = None       # conserved variable whose RK stage update this kernel also performs
+        self.rkfn = None
 
     def name(self):
         return "pg_fused_%d" % self.index
@@ -256,6 +268,28 @@ class Kernel:
                 "  if (n <= 0) return 0;\n"
                 "  int64_t b = (n + 255) / 256;\n  if (b > 152 * 16) b = 152 * 16;\n"
                 "  %(k)s<<<(unsigned)b, 256, 0, (cudaStream_t)stream>>>(n, out%(c)s);\n"
+                "  return (int)cudaGetLastError();\n}\n") % {
+                    "k": self.name(), "p": params, "d": " ".join(defs), "e": self.expr,
+                    "c": "".join(", " + c for c in call)} + (self._rk_source(args, defs, call) if self.rk else "")
+
+    def _rk_source(self, args, defs, call):
+        """The same expression as the right-hand side F of the PDE of self.rk, fused with its
+        LSRK stage: PHI = A PHI + dt F, U = U + B PHI, in the arithmetic of the stage kernel
+        (rk_stage_kernel), so the result equals the unfused stage bit for bit."""
+        params = ", ".join(["int64_t n", "double* __restrict__ phi", "double* __restrict__ u", "double A", "double B",
+                            "const double* __restrict__ dtp", "int dt_field"] + args)
+        return ('extern "C" __global__ void %(k)s_rk(%(p)s) {\n'
+                "  const double dt0 = dt_field ? 0.0 : dtp[0];\n"
+                "  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;"
+                " i += (int64_t)gridDim.x * blockDim.x) {\n    %(d)s\n"
+                "    const double f = PG_STORE(%(e)s);\n"
+                "    const double dt = dt_field ? dtp[i] : dt0;\n"
+                "    const double p = __fma_rn(dt, f, __dmul_rn(A, phi[i]));\n"
+                "    phi[i] = p;\n    u[i] = __fma_rn(B, p, u[i]);\n  }\n}\n"
+                'extern "C" int %(k)s_rk_launch(%(p)s, void* stream) {\n'
+                "  if (n <= 0) return 0;\n"
+                "  int64_t b = (n + 255) / 256;\n  if (b > 152 * 16) b = 152 * 16;\n"
+                "  %(k)s_rk<<<(unsigned)b, 256, 0, (cudaStream_t)stream>>>(n, phi, u, A, B, dtp, dt_field%(c)s);\n"
                 "  return (int)cudaGetLastError();\n}\n") % {
                     "k": self.name(), "p": params, "d": " ".join(defs), "e": self.expr,
                     "c": "".join(", " + c for c in call)}
@@ -449,6 +483,7 @@ class Fuser:
         self.groups = []
         self.lib = None
         self.fused_calls = 0
+        self.rk_ctx = None     # set by rk4 around the flux evaluation of a stage
 
     def rewrite(self, src, globals_):
         tree = ast.parse(src, mode="eval")
@@ -494,7 +529,28 @@ class Fuser:
                     e._fused_member = True
             i = max(j, i + 1)
         for eq in eqs:
+            n0 = len(self.kernels)
             eq.RHS = self.rewrite(eq.sRHS, globals_)
+            if eq.kind == "PDE" and len(self.kernels) > n0 and self._rk_fusable(eq):
+                self.kernels[-1].rk = eq.LHS[0]
+
+    def _rk_fusable(self, eq):
+        """The PDE's right-hand side is one fused kernel (its root) and no later PDE reads the
+        variable, so the kernel may update the variable's RK state in place."""
+        root = ast.parse(eq.sRHS, mode="eval").body
+        if not (_elementwise(root) and _ops(root) >= self.min_ops):
+            return False
+        eqs = self.sim.equations
+        var = eq.LHS[0]
+        for later in eqs[eqs.index(eq) + 1:]:
+            if later.kind != "PDE":
+                continue
+            if "packages" in later.sRHS:
+                return False
+            tree = ast.parse(later.sRHS, mode="eval")
+            if any(_varname(x) == var for x in ast.walk(tree)):
+                return False
+        return True
 
     @staticmethod
     def _groupable(eq):
@@ -531,6 +587,21 @@ class Fuser:
             k.sig = sig
         if k.fn is None or k.sig != sig:
             return k.eager(*leaves)
+        ctx = self.rk_ctx
+        if k.rk is not None and k.rkfn is not None and ctx is not None and k.rk in ctx["phi"]:
+            dt = ctx["dt"]
+            if not (isinstance(dt, torch.Tensor) and dt.dtype == torch.float64 and dt.device == g.device
+                    and (dt.dim() == 0 or dt.numel() == g.npts)):
+                return k.eager(*leaves)
+            u = self.sim._field_of(k.rk)
+            rc = k.rkfn(ctypes.c_int64(g.npts), ctypes.c_void_p(ctx["phi"][k.rk].data_ptr()),
+                        ctypes.c_void_p(u.data_ptr()), ctypes.c_double(ctx["A"]), ctypes.c_double(ctx["B"]),
+                        ctypes.c_void_p(dt.data_ptr()), ctypes.c_int(1 if dt.dim() > 0 else 0), *args,
+                        ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+            if rc != 0:
+                raise RuntimeError("fused kernel %s_rk failed with CUDA error %d" % (k.name(), rc))
+            self.fused_calls += 1
+            return RK_DONE
         out = g.empty()
         rc = k.fn(ctypes.c_int64(g.npts), ctypes.c_void_p(out.data_ptr()), *args,
                   ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
@@ -543,7 +614,8 @@ class Fuser:
         ks = [k for k in self.kernels if k.sig is not None] + [g for g in self.groups if g.sig is not None]
         # loads every kernel now: a first launch inside a graph capture would load its module there
         pre = ('extern "C" int pg_fused_preload() {\n  cudaFuncAttributes a;\n  int rc = 0;\n%s  return rc;\n}\n'
-               % "".join("  rc |= (int)cudaFuncGetAttributes(&a, %s);\n" % k.name() for k in ks))
+               % "".join("  rc |= (int)cudaFuncGetAttributes(&a, %s);\n" % nm for k in ks
+                         for nm in ([k.name()] + ([k.name() + "_rk"] if getattr(k, "rk", None) else []))))
         prelude = PRELUDE_FP64 if self.arith == "fp64" else PRELUDE_FP32
         return prelude + "".join(k.source() for k in ks) + pre
 
@@ -558,4 +630,7 @@ class Fuser:
                 fn = getattr(self.lib, k.name() + "_launch")
                 fn.restype = ctypes.c_int
                 k.fn = fn
+                if getattr(k, "rk", None) is not None:
+                    k.rkfn = getattr(self.lib, k.name() + "_rk_launch")
+                    k.rkfn.restype = ctypes.c_int
         return so

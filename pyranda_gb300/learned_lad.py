@@ -193,12 +193,13 @@ def train(model, X, Tn, iters=3000, batch=8192, lr=1e-3, seed=0, log_every=0, co
     return hist
 
 
-def shock_training_set(runs=20, snapshots_per_run=100, shape=(256, 64, 64), points=2048, seed=1,
+def shock_training_set(runs=20, snapshots_per_run=100, shape=(128, 64, 64), points=2048, seed=1,
                        steps_between=1, precision="fp32"):
     """Snapshots of seeded shock-interface runs with the plain closure.
 
-    The default grid, 256 x 64 x 64 on [0, 4] x [0, 1)^2, has equal spacings
-    in x, y and z, like the 512 x 128 x 128 shock problem the closure serves.
+    The default grid is 128 x 64 x 64 on [0, 4] x [0, 1)^2 (spacing 4/128 in x,
+    1/64 in y and z); 256 x 64 x 64 has equal spacings, like the 512 x 128 x 128
+    shock problem the closure serves.
     Mach ~ U[1.2, 3.0] and amplitude ~ U[0.01, 0.1] from default_rng(seed);
     each snapshot contributes `points` points, half where beta is largest
     (shock and interface) and half uniformly at random.  Returns

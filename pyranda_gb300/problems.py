@@ -87,6 +87,20 @@ L = 1.0
 """
 
 
+# The Taylor-Green configuration of the benchmark: Mach 0.1 (p0 = rho0 u0^2 /
+# (gamma M^2)), p = p0 + rho0 u0^2/16 (cos 2x + cos 2y)(cos 2z + 2), and a
+# physical viscosity mu0 = rho0 u0 L / Re with Re = 1600 added to the LAD
+# shear viscosity; otherwise the EOM and IC of examples/TaylorGreen.py.
+TGV_RE = 1600.0
+TGV_MACH = 0.1
+_TGV_MU_LINE = ":mu:        =  gbar( abs(ring(:S:  )) ) * :rho: * 1.0e-4"
+assert _TGV_MU_LINE in TGV_EOM
+TGV_EOM_NS = TGV_EOM.replace(_TGV_MU_LINE, _TGV_MU_LINE + " + %r" % (1.0 * 1.0 * 1.0 / TGV_RE))
+TGV_IC_NS = (TGV_IC.replace("p0 = 100.0\nrho0 = 1.0", "rho0 = 1.0\np0 = rho0*u0*u0/(1.4*%r*%r)" % (TGV_MACH, TGV_MACH))
+             .replace("( cos(2.*meshz/L) + 2.0 ) - 2.0 )", "( cos(2.*meshz/L) + 2.0 ) )"))
+assert TGV_IC_NS.count("p0 = rho0") == 1 and "2.0 ) - 2.0" not in TGV_IC_NS
+
+
 def tgv_mesh(npts):
     """examples/TaylorGreen.py: periodic [0, 2 pi) in every direction."""
     return """
@@ -96,11 +110,12 @@ zdom = (0.0, 2*pi*FF,  Npts, periodic=True)
 """.replace("Npts", str(npts)).replace("pi", str(math.pi)).replace("FF", str(float(npts - 1) / npts))
 
 
-def build_tgv(Sim, npts, timestep, **kw):
+def build_tgv(Sim, npts, timestep, ns=False, **kw):
+    """examples/TaylorGreen.py (ns=False), or the benchmark's Mach 0.1, Re 1600 configuration (ns=True)."""
     ss = Sim("TGvortex", tgv_mesh(npts), **kw)
     timestep(ss)
-    ss.EOM(TGV_EOM)
-    ss.setIC(TGV_IC)
+    ss.EOM(TGV_EOM_NS if ns else TGV_EOM)
+    ss.setIC(TGV_IC_NS if ns else TGV_IC)
     return ss
 
 

@@ -16,6 +16,7 @@ import torch
 
 from . import pgmath
 from ._lib import PG_DIR_ALL
+from .fuse import RK_DONE
 from .grid import Grid, flush_pending
 from .pyrandaUtils import findVar, fortran3d, splitLines
 
@@ -779,12 +780,21 @@ class pyrandaSim:
             dt_dev = self._dt_tensor(dt)
         time_i = self._time_tensor(time)
         self.deltat = dt
+        fused_rk = self._fuse is not None and self._fuse.lib is not None
         for ii in range(5):
-            flux = self.updateFlux()
-            U = [self._field_of(n) for n in names]
-            F = [self.grid.field(flux[n]) for n in names]
-            PHI = [self._phi[n] for n in names]
-            self.grid.rk_stage(U, PHI, F, dt_dev, ARK[ii], BRK[ii])
+            if fused_rk:   # PDE kernels that own their variable's stage update apply it themselves
+                self._fuse.rk_ctx = {"A": ARK[ii], "B": BRK[ii], "dt": dt_dev, "phi": self._phi}
+            try:
+                flux = self.updateFlux()
+            finally:
+                if fused_rk:
+                    self._fuse.rk_ctx = None
+            rest = [n for n in names if flux[n] is not RK_DONE]
+            if rest:
+                U = [self._field_of(n) for n in rest]
+                F = [self.grid.field(flux[n]) for n in rest]
+                PHI = [self._phi[n] for n in rest]
+                self.grid.rk_stage(U, PHI, F, dt_dev, ARK[ii], BRK[ii])
             time = self._stage_time(time_i, ETA[ii], dt, dt_dev)
             self.time = time
             self.updateVars()

@@ -67,3 +67,16 @@ def test_power_special_cases_follow_torch():
 def test_unknown_arithmetic_is_refused():
     with pytest.raises(ValueError):
         fuse.Fuser(_Sim(TGV_EOM), arith="fp16")
+
+
+def test_pde_kernels_own_their_stage_update():
+    """Every PDE of the TGV EOM ends in one fused kernel and no later PDE reads its variable, so each
+    kernel also applies its variable's LSRK stage; a later PDE reading the variable blocks it."""
+    sim = _Sim(TGV_EOM)
+    f = fuse.Fuser(sim)
+    f.install(EVAL_GLOBALS)
+    assert [k.rk for k in f.kernels if k.rk] == ["rho", "rhou", "rhov", "rhow", "Et"]
+    eom = "ddt(:a:) = -ddx(:a:*:b:) - ddy(:a:)\nddt(:b:) = -ddx(:b:*:a:) - ddy(:b:)\n"
+    f = fuse.Fuser(_Sim(eom))
+    f.install(EVAL_GLOBALS)
+    assert [k.rk for k in f.kernels if k.rk] == ["b"]
