@@ -112,6 +112,18 @@ int pg_d1(pg_handle* h, int dir, const double* in, double* out, void* stream);
 /* dd8x / dd8y / dd8z (parcop.f90:279-301 -> compact_operators.f90:280-383):
  * 8th derivative, no metric. */
 int pg_d8(pg_handle* h, int dir, const double* in, double* out, void* stream);
+/* d2x / d2y / d2z (compact_operators.f90:130-206): 10th-order compact second
+ * derivative (c10d2), divided by the grid spacing squared. */
+int pg_d2(pg_handle* h, int dir, const double* in, double* out, void* stream);
+/* dd4x / dd4y / dd4z (parcop.f90:255-277 -> compact_operators.f90:208-278):
+ * explicit 4th-order fourth derivative (e4d4), no metric.  On non-periodic
+ * lines the three one-sided rows of each end close the stencil (the
+ * reference declares a fourth row it never sets). */
+int pg_d4(pg_handle* h, int dir, const double* in, double* out, void* stream);
+/* plaplacian (parcop.f90:303-311 -> operators.f90:513-526, Cartesian):
+ * d2x + d2y + d2z; a direction of fewer than 4 points contributes 0.  out
+ * must differ from in. */
+int pg_laplacian(pg_handle* h, const double* in, double* out, void* stream);
 /* sFilter / gFilter / gFilterDir (parcop.f90:337-368 -> operators.f90:755-896).
  * dir = PG_DIR_ALL gives the x->y->z sweep sequence of `filter`. */
 int pg_filter(pg_handle* h, int kind, int dir, const double* in, double* out, void* stream);
@@ -170,6 +182,9 @@ int pg_ens_set_precision(pg_ensemble* e, int precision);
 int pg_ens_spacing(const pg_ensemble* e, int member, double* patch_d, double* mesh_d);
 int pg_ens_d1(pg_ensemble* e, int dir, const double* in, double* out, void* stream);
 int pg_ens_d8(pg_ensemble* e, int dir, const double* in, double* out, void* stream);
+int pg_ens_d2(pg_ensemble* e, int dir, const double* in, double* out, void* stream);
+int pg_ens_d4(pg_ensemble* e, int dir, const double* in, double* out, void* stream);
+int pg_ens_laplacian(pg_ensemble* e, const double* in, double* out, void* stream);
 int pg_ens_filter(pg_ensemble* e, int kind, int dir, const double* in, double* out, void* stream);
 int pg_ens_ring(pg_ensemble* e, const double* in, double* out, void* stream);
 int pg_ens_ringv(pg_ensemble* e, const double* vx, const double* vy, const double* vz, double* out,
@@ -266,6 +281,9 @@ int pg_reduce_noalloc(int op, const double* in, int64_t n, double* out, void* st
  * synchronise.  For tests and for callers that hold host arrays. */
 int pg_d1_host(pg_handle* h, int dir, const double* in, double* out);
 int pg_d8_host(pg_handle* h, int dir, const double* in, double* out);
+int pg_d2_host(pg_handle* h, int dir, const double* in, double* out);
+int pg_d4_host(pg_handle* h, int dir, const double* in, double* out);
+int pg_laplacian_host(pg_handle* h, const double* in, double* out);
 int pg_filter_host(pg_handle* h, int kind, int dir, const double* in, double* out);
 int pg_ring_host(pg_handle* h, const double* in, double* out);
 

@@ -45,6 +45,7 @@ def lib():
         L.og_create.argtypes = [I, I, D, D, ctypes.POINTER(P)]
         L.og_destroy.argtypes = [P]
         L.og_apply.argtypes = [P, ctypes.c_int, ctypes.c_int, D, D]
+        L.og_laplacian.argtypes = [P, D, D]
         L.og_filter3.argtypes = [P, ctypes.c_int, D, D]
         L.og_ring.argtypes = [P, D, D, ctypes.c_int]
         L.og_ringv.argtypes = [P, D, D, D, D, ctypes.c_int]
@@ -68,7 +69,7 @@ def _f64(a):
     return numpy.asfortranarray(numpy.asarray(a, dtype=numpy.float64))
 
 
-OP_D1, OP_D8, OP_SF, OP_GF = 0, 1, 2, 3
+OP_D1, OP_D8, OP_SF, OP_GF, OP_D2, OP_D4 = 0, 1, 2, 3, 4, 5
 
 
 class OracleGrid:
@@ -114,6 +115,18 @@ class OracleGrid:
 
     def dd8(self, direction, v):
         return self.apply(OP_D8, direction, v)
+
+    def d2(self, direction, v):
+        return self.apply(OP_D2, direction, v)
+
+    def dd4(self, direction, v):
+        return self.apply(OP_D4, direction, v)
+
+    def laplacian(self, v):
+        v = _f64(v)
+        out = self._out()
+        lib().og_laplacian(self.h, _dp(v), _dp(out))
+        return out
 
     def sfilter(self, v):
         v = _f64(v)
@@ -398,8 +411,13 @@ class OracleSim:
         s["grad("] = "self.grad("
         s["simtime"] = "self.time"
         s["deltat"] = "self.deltat"
+        s["divT("] = "self.divT("
+        s["lap("] = "self.laplacian("
         s["ring("] = "self.ring("
         s["ringV("] = "self.ringV("
+        s["dd4x("] = "self.dd4x("
+        s["dd4y("] = "self.dd4y("
+        s["dd4z("] = "self.dd4z("
         s["dd8x("] = "self.dd8x("
         s["dd8y("] = "self.dd8y("
         s["dd8z("] = "self.dd8z("
@@ -457,6 +475,22 @@ class OracleSim:
 
     def ddz(self, v):
         return 0.0 if self.nz <= 1 else self.grid.ddz(v)
+
+    def dd4x(self, v):
+        return self.grid.dd4(0, v)
+
+    def dd4y(self, v):
+        return self.grid.dd4(1, v)
+
+    def dd4z(self, v):
+        return self.grid.dd4(2, v)
+
+    def laplacian(self, v):
+        return self.grid.laplacian(v)
+
+    def divT(self, fxx, fxy, fxz, fyx, fyy, fyz, fzx, fzy, fzz):
+        g = self.grid
+        return [g.div(fxx, fyx, fzx), g.div(fxy, fyy, fzy), g.div(fxz, fyz, fzz)]
 
     def dd8x(self, v):
         return self.grid.dd8(0, v)

@@ -158,12 +158,65 @@ Weight make_cgfs4() {
   return w;
 }
 
+// c10d2: stencils.f90:358-428 (compact 10th-order second derivative)
+Weight make_c10d2() {
+  Weight w{};
+  w.nol = 2; w.nor = 3; w.ncl = 5; w.ncr = 7; w.nbc1 = 4; w.nbc2 = 4; w.null_option = 0;
+  w.implicit_op = true;
+  const double ali[5] = {387.0, 6012.0, 16182.0, 6012.0, 387.0};
+  const double ari[7] = {79.0, 4671.0, 9585.0, -28670.0, 9585.0, 4671.0, 79.0};
+  const double alb1[4][5] = {{0.0, 0.0, 1.0, 11.0, 0.0},
+                             {0.0, 1.0, 10.0, 1.0, 0.0},
+                             {23.0, 688.0, 2358.0, 688.0, 23.0},
+                             {387.0, 6012.0, 16182.0, 6012.0, 387.0}};
+  const double arb1[4][7] = {{0.0, 0.0, 0.0, 13.0, -27.0, 15.0, -1.0},
+                             {0.0, 0.0, 12.0, -24.0, 12.0, 0.0, 0.0},
+                             {0.0, 465.0, 1920.0, -4770.0, 1920.0, 465.0, 0.0},
+                             {79.0, 4671.0, 9585.0, -28670.0, 9585.0, 4671.0, 79.0}};
+  for (int l = 0; l < 5; l++) w.ali[l] = ali[l];
+  for (int l = 0; l < 7; l++) w.ari[l] = ari[l];
+  for (int j = 0; j < 4; j++) {
+    for (int l = 0; l < 5; l++) w.alb1[j][l] = alb1[j][l];
+    for (int l = 0; l < 7; l++) w.arb1[j][l] = arb1[j][l];
+  }
+  mirror_rows(w, 1.0);  // alb2(:,j) = alb1(ncl:1:-1, 5-j), arb2 likewise (:391-398, :404-411)
+  return w;
+}
+
+// e4d4: stencils.f90:430-513 (explicit 4th-order fourth derivative).  The
+// reference sets three one-sided rows per end (:480-492) while declaring
+// nbc1 = nbc2 = 4, so its fourth lower row and last upper row are never set;
+// this restatement closes each end with the three defined rows (the upper
+// ones are alb2/arb2(:,1..3) of :483-485, :491-493, reversed rows 3, 2, 1).
+Weight make_e4d4() {
+  Weight w{};
+  w.nol = 0; w.nor = 3; w.ncl = 1; w.ncr = 7; w.nbc1 = 3; w.nbc2 = 3; w.null_option = 0;
+  w.implicit_op = false;
+  const double agau = 28.0 / 3.0, bgau = -6.5, cgau = 2.0, dgau = -1.0 / 6.0;
+  const double cgau13 = cgau + dgau, bgau12 = bgau + cgau, agau22 = agau + dgau;
+  const double agau11 = agau + bgau, bgau21 = bgau + cgau, cgau31 = cgau + dgau;
+  const double ari[7] = {dgau, cgau, bgau, agau, bgau, cgau, dgau};
+  const double arb1[3][7] = {{0.0, 0.0, 0.0, agau11, bgau21, cgau31, dgau},
+                             {0.0, 0.0, bgau12, agau22, bgau, 0.0, 0.0},
+                             {0.0, cgau13, bgau, agau, bgau, cgau, 0.0}};
+  w.ali[0] = 1.0;
+  for (int l = 0; l < 7; l++) w.ari[l] = ari[l];
+  for (int j = 0; j < 3; j++) {
+    w.alb1[j][0] = 1.0;
+    w.alb2[j][0] = 1.0;
+    for (int l = 0; l < 7; l++) w.arb1[j][l] = arb1[j][l];
+  }
+  for (int j = 0; j < 3; j++)
+    for (int l = 0; l < 7; l++) w.arb2[j][l] = w.arb1[2 - j][6 - l];
+  return w;
+}
+
 // ---------------------------------------------------------------------------
 // One operator along one direction: compact_basetype.f90:65-209 (np = 1)
 // ---------------------------------------------------------------------------
 struct Op1 {
   bool null_op = true, periodic = false, implicit_op = false;
-  int kind = 0;  // 1 = d1 evaluator (compact_d1.f90), 4 = r4 evaluator (compact_r4.f90)
+  int kind = 0;  // 1 = d1 evaluator (compact_d1.f90), 3 = r3 (compact_r3.f90), 4 = r4 (compact_r4.f90)
   int null_option = 0, n = 0, nal = 0;
   std::vector<double> al;  // al(i, c) -> al[(c-1)*n + (i-1)], factored
   std::vector<double> ar;  // ar(l, i) -> ar[(i-1)*ncr + (l-1)]
@@ -417,10 +470,42 @@ void solve_p(const Op1& o, double* r) {
     r[i] = (r[i] - (c(i, 4) * r[i + 1] + c(i, 5) * r[i + 2] + c(i, 8) * r[N - 1] + c(i, 9) * r[N])) * c(i, 3);
 }
 
-// Full line evaluation (eval_compact_op1x_d1 / _r4), np = 1, then the d1 metric scale
-// (compact_operators.f90:41-46) when scale != 0.
+// r3 RHS: compact_r3.f90:72-157 (np = 1).  Periodic lines take the wrapped
+// points as ghost data (:86-89); non-periodic ones take zeros (:90-105), whose
+// closure weights vanish.  Fortran SUM adds left to right.
+void rhs_r3(const Op1& o, const double* v, double* dv) {
+  const int ax = o.n;
+  auto a = [&](int l, int i) { return o.AR(l, i); };
+  double vbr1[4] = {0.0, 0.0, 0.0, 0.0}, vbr2[4] = {0.0, 0.0, 0.0, 0.0};  // 1-based
+  if (o.periodic) {
+    for (int q = 1; q <= 3; q++) {
+      vbr1[q] = v[ax - 3 + q];
+      vbr2[q] = v[q];
+    }
+  }
+  auto part = [&](int i, int l0, int l1, auto val) {  // sum(ar(l0:l1, i) * (val(l) - v(i)))
+    double s = 0.0;
+    for (int l = l0; l <= l1; l++) s += a(l, i) * (val(l) - v[i]);
+    return s;
+  };
+  // :124-126
+  dv[1] = part(1, 1, 3, [&](int l) { return vbr1[l]; }) + part(1, 4, 7, [&](int l) { return v[l - 3]; });
+  dv[2] = part(2, 1, 2, [&](int l) { return vbr1[l + 1]; }) + part(2, 3, 7, [&](int l) { return v[l - 2]; });
+  dv[3] = part(3, 1, 1, [&](int l) { return vbr1[l + 2]; }) + part(3, 2, 7, [&](int l) { return v[l - 1]; });
+  for (int i = 4; i <= ax - 3; i++) dv[i] = part(i, 1, 7, [&](int l) { return v[i - 4 + l]; });  // :137-143
+  // :154-156
+  dv[ax - 2] = part(ax - 2, 1, 6, [&](int l) { return v[ax - 6 + l]; }) +
+               part(ax - 2, 7, 7, [&](int l) { return vbr2[l - 6]; });
+  dv[ax - 1] = part(ax - 1, 1, 5, [&](int l) { return v[ax - 5 + l]; }) +
+               part(ax - 1, 6, 7, [&](int l) { return vbr2[l - 5]; });
+  dv[ax] = part(ax, 1, 4, [&](int l) { return v[ax - 4 + l]; }) + part(ax, 5, 7, [&](int l) { return vbr2[l - 4]; });
+}
+
+// Full line evaluation (eval_compact_op1x_d1 / _r3 / _r4), np = 1, then the
+// metric scale when scale != 0 (d1: dx, compact_operators.f90:41-46; d2: dx**2, :149-152).
 void eval_line(const Op1& o, const double* v, double* dv, double scale) {
   if (o.kind == 1) rhs_d1(o, v, dv);
+  else if (o.kind == 3) rhs_r3(o, v, dv);
   else rhs_r4(o, v, dv);
   if (o.implicit_op) {
     if (o.periodic) solve_p(o, dv);
@@ -443,18 +528,20 @@ struct og_handle {
   double d[3];     // patch spacing dx, dy, dz (patch.f90:83-85)
   double dmesh[3]; // mesh d1, d2, d3 (mesh.f90:192-209)
   double x1f[3];   // lower face coordinates (parcop.f90:51-56)
-  Op1 d1[3], d8[3], sf[3], gf[3];
+  Op1 d1[3], d8[3], sf[3], gf[3], d2[3], d4[3];
 };
 
 namespace {
 
-enum { OP_D1 = 0, OP_D8 = 1, OP_SF = 2, OP_GF = 3 };
+enum { OP_D1 = 0, OP_D8 = 1, OP_SF = 2, OP_GF = 3, OP_D2 = 4, OP_D4 = 5 };
 
 const Op1& pick(const og_handle* h, int op, int dir) {
   switch (op) {
     case OP_D1: return h->d1[dir];
     case OP_D8: return h->d8[dir];
     case OP_SF: return h->sf[dir];
+    case OP_D2: return h->d2[dir];
+    case OP_D4: return h->d4[dir];
     default: return h->gf[dir];
   }
 }
@@ -471,7 +558,7 @@ void apply_dir(const og_handle* h, int op, int dir, const double* in, double* ou
     else std::memset(out, 0, npts * sizeof(double));
     return;
   }
-  const double scale = (op == OP_D1) ? h->d[dir] : 0.0;
+  const double scale = (op == OP_D1) ? h->d[dir] : ((op == OP_D2) ? h->d[dir] * h->d[dir] : 0.0);
   const int n = h->n[dir];
   size_t stride, nlines;
   if (dir == 0) { stride = 1; nlines = (size_t)ny * nz; }
@@ -529,8 +616,11 @@ int og_create(const int* n, const int* periodic, const double* x1, const double*
     }
   }
   static const Weight wd1 = make_c10d1(), wd8 = make_c10d8(), wsf = make_c8ff8(), wgf = make_cgfs4();
+  static const Weight wd2 = make_c10d2(), wd4 = make_e4d4();
   for (int d = 0; d < 3; d++) {
     const bool per = h->periodic[d] != 0;
+    h->d2[d] = setup_op(wd2, 3, h->n[d], per);
+    h->d4[d] = setup_op(wd4, 3, h->n[d], per);
     h->d1[d] = setup_op(wd1, 1, h->n[d], per);
     h->d8[d] = setup_op(wd8, 4, h->n[d], per);
     h->sf[d] = setup_op(wsf, 4, h->n[d], per);
@@ -558,10 +648,23 @@ void og_set_threads(int t) {
 #endif
 }
 
-// op: 0 = d1 (ddx/ddy/ddz), 1 = d8 (dd8x..), 2 = compact filter c8ff8, 3 = gaussian cgfs4
+// op: 0 = d1 (ddx/ddy/ddz), 1 = d8 (dd8x..), 2 = compact filter c8ff8, 3 = gaussian cgfs4,
+// 4 = d2 (c10d2), 5 = d4 (e4d4, dd4x..)
 int og_apply(const og_handle* h, int op, int dir, const double* in, double* out) {
-  if (!h || op < 0 || op > 3 || dir < 0 || dir > 2) return 1;
+  if (!h || op < 0 || op > 5 || dir < 0 || dir > 2) return 1;
   apply_dir(h, op, dir, in, out);
+  return 0;
+}
+
+// LapS, Cartesian: operators.f90:513-526 (Lapf = Lapf + tmp + dum)
+int og_laplacian(const og_handle* h, const double* in, double* out) {
+  if (!h) return 1;
+  const size_t npts = (size_t)h->n[0] * h->n[1] * h->n[2];
+  std::vector<double> tmp(npts), dum(npts);
+  apply_dir(h, OP_D2, 0, in, out);
+  apply_dir(h, OP_D2, 1, in, tmp.data());
+  apply_dir(h, OP_D2, 2, in, dum.data());
+  for (size_t p = 0; p < npts; p++) out[p] = out[p] + tmp[p] + dum[p];
   return 0;
 }
 

@@ -72,6 +72,9 @@ SIGNATURES = [
     ("pg_version", ctypes.c_char_p, []),
     ("pg_d1", I, [P, I, D, D, P]),
     ("pg_d8", I, [P, I, D, D, P]),
+    ("pg_d2", I, [P, I, D, D, P]),
+    ("pg_d4", I, [P, I, D, D, P]),
+    ("pg_laplacian", I, [P, D, D, P]),
     ("pg_filter", I, [P, I, I, D, D, P]),
     ("pg_ring", I, [P, D, D, P]),
     ("pg_ringv", I, [P, D, D, D, D, P]),
@@ -86,6 +89,9 @@ SIGNATURES = [
     ("pg_check_finite", I, [D, ctypes.c_int64, D, P]),
     ("pg_d1_host", I, [P, I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     ("pg_d8_host", I, [P, I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    ("pg_d2_host", I, [P, I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    ("pg_d4_host", I, [P, I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    ("pg_laplacian_host", I, [P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     ("pg_filter_host", I, [P, I, I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     ("pg_ring_host", I, [P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     ("pg_launch_count", ctypes.c_uint64, []),
@@ -96,6 +102,9 @@ SIGNATURES = [
     ("pg_ens_spacing", I, [P, I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     ("pg_ens_d1", I, [P, I, D, D, P]),
     ("pg_ens_d8", I, [P, I, D, D, P]),
+    ("pg_ens_d2", I, [P, I, D, D, P]),
+    ("pg_ens_d4", I, [P, I, D, D, P]),
+    ("pg_ens_laplacian", I, [P, D, D, P]),
     ("pg_ens_filter", I, [P, I, I, D, D, P]),
     ("pg_ens_ring", I, [P, D, D, P]),
     ("pg_ens_ringv", I, [P, D, D, D, D, P]),

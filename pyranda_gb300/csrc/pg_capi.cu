@@ -86,7 +86,7 @@ int grid_info(const pg_grid* g, GridInfo& gi, const char* who) {
   }
   for (int k = 0; k < OPK_COUNT; k++)
     for (int d = 0; d < 3; d++) {
-      const double scale = (k == OPK_D1) ? gi.d[d] : 0.0;
+      const double scale = (k == OPK_D1) ? gi.d[d] : ((k == OPK_D2) ? gi.d[d] * gi.d[d] : 0.0);
       int rc = build_operator(k, gi.n[d], gi.periodic[d] != 0, scale, gi.tab[k][d]);
       if (rc != PG_OK) {
         set_error("%s: direction %d has %d points; a non-null direction needs at least 8", who, d, gi.n[d]);
@@ -291,7 +291,8 @@ int build_ctx(Ctx& c, const std::vector<GridInfo>& g, int precision, const char*
   const size_t nbytes = (size_t)c.npts * sizeof(double);
   if (e == cudaSuccess) e = cudaMalloc(&c.work, nbytes);
   if (e == cudaSuccess) e = cudaMalloc(&c.work2, nbytes);
-  const size_t npart = std::max((size_t)kReduceBlocks, (size_t)M * kSegBlocks + 2 * (size_t)M);
+  // two values per block for the two-pass diffusion limit (estimate, exact-point flag)
+  const size_t npart = std::max((size_t)2 * kReduceBlocks, (size_t)M * kSegBlocks + 2 * (size_t)M);
   if (e == cudaSuccess) e = cudaMalloc(&c.partial, npart * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&c.status, sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&c.emax, sizeof(int) * (size_t)M);
@@ -675,6 +676,19 @@ int grad(Ctx& c, const double* in, double* gx, double* gy, double* gz, void* st)
   return rc;
 }
 
+// LapS, Cartesian (operators.f90:513-526): d2x + d2y + d2z, null directions contribute 0
+int laplacian(Ctx& c, const double* in, double* out, void* st) {
+  bool first = true;
+  for (int d = 0; d < 3; d++) {
+    if (c.ops[c.precision][OPK_D2][d].null_op) continue;
+    int rc = sweep(c, OPK_D2, d, in, out, first ? EPI_STORE : EPI_ADD, 0, st);
+    if (rc) return rc;
+    first = false;
+  }
+  if (first) return launch_fill(out, 0.0, c.npts, st);
+  return PG_OK;
+}
+
 // divV, Cartesian (operators.f90:38-53): df = fA + fB + fC
 int divergence(Ctx& c, const double* fx, const double* fy, const double* fz, double* out, void* st) {
   const double* f[3] = {fx, fy, fz};
@@ -791,7 +805,7 @@ int pg_wait_selftest(pg_handle* h, unsigned limit_ms, void* stream) {
 
 int pg_dense_plan(const pg_handle* h, int* plan) {
   if (!h || !plan) return PG_EINVAL;
-  for (int k = 0; k < OPK_COUNT; k++)
+  for (int k = 0; k <= OPK_GF; k++)
     for (int d = 0; d < 3; d++) plan[k * 3 + d] = (h->c.dense && h->c.use_dense[k][d]) ? 1 : 0;
   return PG_OK;
 }
@@ -813,6 +827,25 @@ int pg_d1(pg_handle* h, int dir, const double* in, double* out, void* stream) {
 int pg_d8(pg_handle* h, int dir, const double* in, double* out, void* stream) {
   if (!h || !in || !out || bad_dir(dir)) return PG_EINVAL;
   return apply_one(h->c, OPK_D8, dir, in, out, stream);
+}
+
+int pg_d2(pg_handle* h, int dir, const double* in, double* out, void* stream) {
+  if (!h || !in || !out || bad_dir(dir)) return PG_EINVAL;
+  return apply_one(h->c, OPK_D2, dir, in, out, stream);
+}
+
+int pg_d4(pg_handle* h, int dir, const double* in, double* out, void* stream) {
+  if (!h || !in || !out || bad_dir(dir)) return PG_EINVAL;
+  return apply_one(h->c, OPK_D4, dir, in, out, stream);
+}
+
+int pg_laplacian(pg_handle* h, const double* in, double* out, void* stream) {
+  if (!h || !in || !out) return PG_EINVAL;
+  if (in == out) {
+    set_error("pg_laplacian: in and out must differ");
+    return PG_EINVAL;
+  }
+  return laplacian(h->c, in, out, stream);
 }
 
 int pg_filter(pg_handle* h, int kind, int dir, const double* in, double* out, void* stream) {
@@ -900,6 +933,21 @@ int pg_d1_host(pg_handle* h, int dir, const double* in, double* out) {
 int pg_d8_host(pg_handle* h, int dir, const double* in, double* out) {
   if (!h) return PG_EINVAL;
   return host_call(h->c, in, out, [&](const double* a, double* b, void* s) { return pg_d8(h, dir, a, b, s); });
+}
+
+int pg_d2_host(pg_handle* h, int dir, const double* in, double* out) {
+  if (!h) return PG_EINVAL;
+  return host_call(h->c, in, out, [&](const double* a, double* b, void* s) { return pg_d2(h, dir, a, b, s); });
+}
+
+int pg_d4_host(pg_handle* h, int dir, const double* in, double* out) {
+  if (!h) return PG_EINVAL;
+  return host_call(h->c, in, out, [&](const double* a, double* b, void* s) { return pg_d4(h, dir, a, b, s); });
+}
+
+int pg_laplacian_host(pg_handle* h, const double* in, double* out) {
+  if (!h) return PG_EINVAL;
+  return host_call(h->c, in, out, [&](const double* a, double* b, void* s) { return pg_laplacian(h, a, b, s); });
 }
 
 int pg_filter_host(pg_handle* h, int kind, int dir, const double* in, double* out) {
@@ -990,6 +1038,21 @@ int pg_ens_d1(pg_ensemble* e, int dir, const double* in, double* out, void* stre
 int pg_ens_d8(pg_ensemble* e, int dir, const double* in, double* out, void* stream) {
   if (!e || !in || !out || bad_dir(dir)) return PG_EINVAL;
   return apply_one(e->c, OPK_D8, dir, in, out, stream);
+}
+
+int pg_ens_d2(pg_ensemble* e, int dir, const double* in, double* out, void* stream) {
+  if (!e || !in || !out || bad_dir(dir)) return PG_EINVAL;
+  return apply_one(e->c, OPK_D2, dir, in, out, stream);
+}
+
+int pg_ens_d4(pg_ensemble* e, int dir, const double* in, double* out, void* stream) {
+  if (!e || !in || !out || bad_dir(dir)) return PG_EINVAL;
+  return apply_one(e->c, OPK_D4, dir, in, out, stream);
+}
+
+int pg_ens_laplacian(pg_ensemble* e, const double* in, double* out, void* stream) {
+  if (!e || !in || !out || in == out) return PG_EINVAL;
+  return laplacian(e->c, in, out, stream);
 }
 
 int pg_ens_filter(pg_ensemble* e, int kind, int dir, const double* in, double* out, void* stream) {

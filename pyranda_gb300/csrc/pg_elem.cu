@@ -186,18 +186,25 @@ __device__ __forceinline__ DiffEst diff_estimate(double rho, double bulk, float 
   return d;
 }
 
+// partial[b]: block b's smallest estimate; partial[gridDim.x + b]: 1 if block b holds a point
+// that pass 2 must evaluate exactly whatever its estimate
 __global__ void diff_estimate_partial(const double* __restrict__ bulk, const double* __restrict__ rho, float gl2,
                                       int64_t n, double* __restrict__ partial) {
   float acc = FLT_MAX;
-  bool nan = false;
+  bool nan = false, exact = false;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const DiffEst d = diff_estimate(rho[i], bulk[i], gl2);
     nan |= d.nan;
+    exact |= d.exact;
     if (!d.exact) acc = fminf(acc, d.e);
   }
   double v = block_reduce<2>((double)acc);
   const int anynan = __syncthreads_or(nan);
-  if (threadIdx.x == 0) partial[blockIdx.x] = anynan ? NAN : v;
+  const int anyexact = __syncthreads_or(exact);
+  if (threadIdx.x == 0) {
+    partial[blockIdx.x] = anynan ? NAN : v;
+    partial[gridDim.x + blockIdx.x] = anyexact ? 1.0 : 0.0;
+  }
 }
 
 __global__ void diff_exact_partial(const double* __restrict__ bulk, const double* __restrict__ rho, double gl,
@@ -205,6 +212,15 @@ __global__ void diff_exact_partial(const double* __restrict__ bulk, const double
                                    double* __restrict__ partial) {
   const double m = *est_min;
   const float lim = (float)(m + fabs(m) * 1.0e-5 + 1.0e-38);
+  // a block whose points (the same grid-stride set as in pass 1) all estimate above the limit
+  // holds no candidate: it skips its loads
+  const double bmin = partial[blockIdx.x];
+  const bool bexact = partial[gridDim.x + blockIdx.x] != 0.0;
+  __syncthreads();  // every thread has read the pass-1 values before thread 0 overwrites them
+  if (m == m && !bexact && !(bmin <= (double)lim)) {
+    if (threadIdx.x == 0) partial[blockIdx.x] = DBL_MAX;
+    return;
+  }
   double acc = DBL_MAX;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double r = rho[i], b = bulk[i];

@@ -8,7 +8,9 @@
 
 namespace pg {
 
-enum { OPK_D1 = 0, OPK_D8 = 1, OPK_SF = 2, OPK_GF = 3, OPK_COUNT = 4 };
+// d1 (c10d1), d8 (c10d8), compact filter (c8ff8), Gaussian filter (cgfs4),
+// d2 (c10d2, compact) and d4 (e4d4, explicit)
+enum { OPK_D1 = 0, OPK_D8 = 1, OPK_SF = 2, OPK_GF = 3, OPK_D2 = 4, OPK_D4 = 5, OPK_COUNT = 6 };
 
 // Host-side tables of one operator along one direction (built by pg_setup.cpp).
 struct OpTables {

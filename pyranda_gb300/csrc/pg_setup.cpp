@@ -3,8 +3,8 @@
 // Builds, once per grid and direction, the per-row coefficient tables that the
 // sweep kernels read:
 //   - the weight tables of pyranda/parcop/stencils.f90 (c10d1 :207-277,
-//     c10d8 :515-621, c8ff8 :713-835, cgfs4 :1387-1476), boundary code 0
-//     (one-sided closures) and periodic;
+//     c10d2 :358-428, e4d4 :430-513, c10d8 :515-621, c8ff8 :713-835,
+//     cgfs4 :1387-1476), boundary code 0 (one-sided closures) and periodic;
 //   - the global LHS/RHS assembly of compact_basetype.f90:124-148 (np = 1);
 //   - the LU factorisations bpentLUD1 / ppentLUD1 of pentadiagonal.f90:18-135.
 // The factorisation steps are kept as in the reference (the kernels replay the
@@ -32,9 +32,9 @@ struct Stencil {
 // Upper boundary rows mirror the lower ones: row j of the upper block is the
 // reversed row (nbc-1-j) of the lower block (stencils.f90, e.g. :241-244).
 void mirror(Stencil& s, double rhs_sign) {
-  for (int j = 0; j < 4; j++) {
-    for (int l = 0; l < s.ncl; l++) s.lhs_hi[j][l] = s.lhs_lo[3 - j][s.ncl - 1 - l];
-    for (int l = 0; l < s.ncr; l++) s.rhs_hi[j][l] = rhs_sign * s.rhs_lo[3 - j][s.ncr - 1 - l];
+  for (int j = 0; j < s.nbc; j++) {
+    for (int l = 0; l < s.ncl; l++) s.lhs_hi[j][l] = s.lhs_lo[s.nbc - 1 - j][s.ncl - 1 - l];
+    for (int l = 0; l < s.ncr; l++) s.rhs_hi[j][l] = rhs_sign * s.rhs_lo[s.nbc - 1 - j][s.ncr - 1 - l];
   }
 }
 
@@ -70,6 +70,52 @@ Stencil stencil_d1() {  // c10d1
     std::memcpy(s.rhs_lo[j], RB[j], sizeof RB[j]);
   }
   mirror(s, -1.0);  // antisymmetric operator
+  return s;
+}
+
+Stencil stencil_d2() {  // c10d2: compact 10th-order second derivative
+  Stencil s{};
+  s.ncl = 5; s.ncr = 7; s.nbc = 4; s.implicit = true; s.addback = false;
+  const double L[5] = {387.0, 6012.0, 16182.0, 6012.0, 387.0};
+  const double R[7] = {79.0, 4671.0, 9585.0, -28670.0, 9585.0, 4671.0, 79.0};
+  const double LB[4][5] = {{0.0, 0.0, 1.0, 11.0, 0.0},
+                           {0.0, 1.0, 10.0, 1.0, 0.0},
+                           {23.0, 688.0, 2358.0, 688.0, 23.0},
+                           {387.0, 6012.0, 16182.0, 6012.0, 387.0}};
+  const double RB[4][7] = {{0.0, 0.0, 0.0, 13.0, -27.0, 15.0, -1.0},
+                           {0.0, 0.0, 12.0, -24.0, 12.0, 0.0, 0.0},
+                           {0.0, 465.0, 1920.0, -4770.0, 1920.0, 465.0, 0.0},
+                           {79.0, 4671.0, 9585.0, -28670.0, 9585.0, 4671.0, 79.0}};
+  std::memcpy(s.lhs, L, sizeof L);
+  std::memcpy(s.rhs, R, sizeof R);
+  for (int j = 0; j < 4; j++) {
+    std::memcpy(s.lhs_lo[j], LB[j], sizeof LB[j]);
+    std::memcpy(s.rhs_lo[j], RB[j], sizeof RB[j]);
+  }
+  mirror(s, 1.0);
+  return s;
+}
+
+// e4d4: explicit 4th-order fourth derivative, no metric.  The reference
+// defines three one-sided rows per end (stencils.f90:480-489) but declares
+// four (nbc1 = nbc2 = 4), leaving its fourth lower row and its last upper row
+// unset; here the three defined rows close each end (the upper ones mirrored)
+// and every other row is interior.
+Stencil stencil_d4() {
+  Stencil s{};
+  s.ncl = 1; s.ncr = 7; s.nbc = 3; s.implicit = false; s.addback = false;
+  const double a = 28.0 / 3.0, b = -6.5, c = 2.0, d = -1.0 / 6.0;
+  const double R[7] = {d, c, b, a, b, c, d};
+  const double RB[3][7] = {{0.0, 0.0, 0.0, a + b, b + c, c + d, d},
+                           {0.0, 0.0, b + c, a + d, b, 0.0, 0.0},
+                           {0.0, c + d, b, a, b, c, 0.0}};
+  s.lhs[0] = 1.0;
+  std::memcpy(s.rhs, R, sizeof R);
+  for (int j = 0; j < 3; j++) {
+    s.lhs_lo[j][0] = 1.0;
+    std::memcpy(s.rhs_lo[j], RB[j], sizeof RB[j]);
+  }
+  mirror(s, 1.0);
   return s;
 }
 
@@ -230,8 +276,9 @@ void factor_cyclic(std::vector<double>& c, int N) {
 
 // Build the host tables of one operator along one direction.
 // Output layout (all row-major, n rows):
-//   rhs[n*9]   per-row RHS weights (d1 uses the first 7), already divided by
-//              the metric `scale` when scale != 0 (d1: compact_operators.f90:41-46)
+//   rhs[n*9]   per-row RHS weights (d1, d2, d4 use the first 7), already divided
+//              by the metric `scale` when scale != 0 (d1: dx, compact_operators.f90:41-46;
+//              d2: dx^2, :149-152)
 //   lu[n*9]    per-row solve coefficients in the order consumed by the kernels:
 //              0:c1 1:c2 (forward) 2:c3 (inverse diagonal) 3:c4 4:c5 (backward)
 //              5:c6 6:c7 (cyclic row multipliers) 7:c8 8:c9 (cyclic fill)
@@ -243,6 +290,8 @@ int build_operator(int kind, int n, bool periodic, double scale, OpTables& t) {
     case OPK_D8: s = stencil_d8(); break;
     case OPK_SF: s = stencil_sf(); break;
     case OPK_GF: s = stencil_gf(); break;
+    case OPK_D2: s = stencil_d2(); break;
+    case OPK_D4: s = stencil_d4(); break;
     default: return PG_EINVAL;
   }
   t.kind = kind;

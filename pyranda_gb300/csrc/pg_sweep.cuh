@@ -241,6 +241,19 @@ __device__ __forceinline__ T edge_rhs(const Line<T>& ln, int i, const W* __restr
     for (int l = 0; l <= top; l++) s += ldc(r + l) * (ln.v(i - 3 + l) - vn);
     return s;
   }
+  if (KIND == 3) {  // 7-point difference form about the row's own point (compact_r3.f90:124-136, :146-157)
+    const T vc = ln.v(i);
+    T s = T(0);
+    if (PER) {
+      for (int l = 0; l < 7; l++) s += ldc(r + l) * (ln.w(i + l - 3) - vc);
+    } else {  // the closures' weights vanish outside the line
+      for (int l = 0; l < 7; l++) {
+        const int p = i + l - 3;
+        if (p >= 0 && p < n) s += ldc(r + l) * (ln.v(p) - vc);
+      }
+    }
+    return s;
+  }
   if (PER) {  // two partial sums (compact_r4.f90:131-138, :180-189)
     const T vc = ln.v(i);
     T s1 = T(0), s2 = T(0);
@@ -274,6 +287,14 @@ __device__ __forceinline__ T ring_rhs(const T* ring, int k, const T* ai) {
            ai[5] * (ring[(k + 5) % kRing] - ring[(k + 1) % kRing]) +
            ai[6] * (ring[(k + 6) % kRing] - ring[(k + 0) % kRing]);
   }
+  if (KIND == 3) {
+    const T vc3 = ring[(k + 3) % kRing];
+    T s3 = T(0);
+#pragma unroll
+    for (int l = 0; l < 7; l++)
+      if (l != 3) s3 += (ring[(k + l) % kRing] - vc3) * ai[l];
+    return s3;
+  }
   const T vc = ring[(k + 4) % kRing];
   T s = T(0);
   s += (ring[(k + 0) % kRing] - vc) * ai[0];
@@ -287,7 +308,7 @@ __device__ __forceinline__ T ring_rhs(const T* ring, int k, const T* ai) {
   return s;
 }
 
-// KIND: 1 = d1 evaluator, 4 = r4 evaluator.  DIR: 0 = x, 1 = y, 2 = z.
+// KIND: 1 = d1 evaluator, 3 = r3 evaluator (d2, d4), 4 = r4 evaluator.  DIR: 0 = x, 1 = y, 2 = z.
 // TR: the RHS arithmetic (T, or long long for the exact d8 RHS of FP32 sweeps).
 template <typename T, int KIND, bool PER, bool IMPL, bool ADDBACK, int DIR, int EPI, typename TR = T>
 __global__ void __launch_bounds__(kSweepThreads) sweep_kernel(const KParams P) {
@@ -334,7 +355,7 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_kernel(const KParams P) {
   const int nl = (int)op.lines;
   constexpr bool kReadOut = (EPI == EPI_ADD || EPI == EPI_RING_MAX);
   const double sc = (P.scale_pow == 2) ? op.dm * op.dm : (P.scale_pow == 1 ? op.dm : 1.0);
-  constexpr int H = (KIND == 1) ? 3 : 4;  // stencil half width
+  constexpr int H = (KIND == 4) ? 4 : 3;  // stencil half width
 
   // edge rows first: they may need wrapped values of the far end of the line
   T e[8];
@@ -557,6 +578,12 @@ int dispatch_kind(const OpRef& op, const KParams& P, int dir, int epi, void* st)
     case OPK_SF:
       return op.periodic ? dispatch_dir_epi<T, 4, true, true, true>(P, dir, epi, st)
                          : dispatch_dir_epi<T, 4, false, true, true>(P, dir, epi, st);
+    case OPK_D2:
+      return op.periodic ? dispatch_dir_epi<T, 3, true, true, false>(P, dir, epi, st)
+                         : dispatch_dir_epi<T, 3, false, true, false>(P, dir, epi, st);
+    case OPK_D4:
+      return op.periodic ? dispatch_dir_epi<T, 3, true, false, false>(P, dir, epi, st)
+                         : dispatch_dir_epi<T, 3, false, false, false>(P, dir, epi, st);
     default:
       return op.periodic ? dispatch_dir_epi<T, 4, true, false, true>(P, dir, epi, st)
                          : dispatch_dir_epi<T, 4, false, false, true>(P, dir, epi, st);

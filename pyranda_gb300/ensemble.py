@@ -216,6 +216,27 @@ class EnsembleGrid:
         _lib.check(self.lib.pg_ens_ring(self.h, _ptr(v), _ptr(out), _stream()), "pg_ens_ring")
         return out
 
+    def d2(self, direction, v, out=None):
+        v = self.field(v)
+        out = self._out(out)
+        _lib.check(self.lib.pg_ens_d2(self.h, direction, _ptr(v), _ptr(out), _stream()), "pg_ens_d2")
+        return out
+
+    def d4(self, direction, v, out=None):
+        v = self.field(v)
+        out = self._out(out)
+        _lib.check(self.lib.pg_ens_d4(self.h, direction, _ptr(v), _ptr(out), _stream()), "pg_ens_d4")
+        return out
+
+    def laplacian(self, v, out=None):
+        v = self.field(v)
+        out = self._out(out)
+        _lib.check(self.lib.pg_ens_laplacian(self.h, _ptr(v), _ptr(out), _stream()), "pg_ens_laplacian")
+        return out
+
+    def divT(self, fxx, fxy, fxz, fyx, fyy, fyz, fzx, fzy, fzz):
+        return [self.div(fxx, fyx, fzx), self.div(fxy, fyy, fzy), self.div(fxz, fyz, fzz)]
+
     def ringv(self, vx, vy, vz, out=None):
         vx, vy, vz = self.field(vx), self.field(vy), self.field(vz)
         out = self._out(out)

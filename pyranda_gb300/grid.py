@@ -176,6 +176,31 @@ class Grid:
         _lib.check(self.lib.pg_d8(self.h, direction, _ptr(v), _ptr(out), _stream()), "pg_d8")
         return out
 
+    def d2(self, direction, v, out=None):
+        """Compact 10th-order second derivative (c10d2), divided by the spacing squared."""
+        v = self.field(v)
+        out = self._out(out)
+        _lib.check(self.lib.pg_d2(self.h, direction, _ptr(v), _ptr(out), _stream()), "pg_d2")
+        return out
+
+    def d4(self, direction, v, out=None):
+        """Explicit 4th-order fourth derivative (e4d4), no metric."""
+        v = self.field(v)
+        out = self._out(out)
+        _lib.check(self.lib.pg_d4(self.h, direction, _ptr(v), _ptr(out), _stream()), "pg_d4")
+        return out
+
+    def laplacian(self, v, out=None):
+        """d2x + d2y + d2z (Cartesian)."""
+        v = self.field(v)
+        out = self._out(out)
+        _lib.check(self.lib.pg_laplacian(self.h, _ptr(v), _ptr(out), _stream()), "pg_laplacian")
+        return out
+
+    def divT(self, fxx, fxy, fxz, fyx, fyy, fyz, fzx, fzy, fzz):
+        """Divergence of a tensor (operators.f90:97-123, Cartesian): the divergences of its columns."""
+        return [self.div(fxx, fyx, fzx), self.div(fxy, fyy, fzy), self.div(fxz, fyz, fzz)]
+
     def filter(self, kind, v, direction=_lib.PG_DIR_ALL, out=None):
         """kind 'spectral' (c8ff8, fbar) or 'gaussian' (cgfs4, gbar)."""
         v = self.field(v)

@@ -91,6 +91,18 @@ class _Parcop:
     def ddz(self, val, nx=None, ny=None, nz=None):  # parcop.f90:245-253
         return self._unary(self._g().ddz, val)
 
+    def dd4x(self, val, nx=None, ny=None, nz=None):  # parcop.f90:255-261
+        return self._unary(lambda v: self._g().d4(0, v), val)
+
+    def dd4y(self, val, nx=None, ny=None, nz=None):  # parcop.f90:263-269
+        return self._unary(lambda v: self._g().d4(1, v), val)
+
+    def dd4z(self, val, nx=None, ny=None, nz=None):  # parcop.f90:271-277
+        return self._unary(lambda v: self._g().d4(2, v), val)
+
+    def plaplacian(self, val, nx=None, ny=None, nz=None):  # parcop.f90:303-311
+        return self._unary(self._g().laplacian, val)
+
     def dd8x(self, val, nx=None, ny=None, nz=None):  # parcop.f90:279-285
         return self._unary(lambda v: self._g().d8(0, v), val)
 
@@ -127,6 +139,12 @@ class _Parcop:
         b, _ = self._in(fy)
         c, _ = self._in(fz)
         return self._out(self._g().div(a, b, c), dev)
+
+    def divergencetensor(self, fxx, fxy, fxz, fyx, fyy, fyz, fzx, fzy, fzz, nx=None, ny=None,
+                         nz=None):  # parcop.f90:213-223
+        args = [self._in(f) for f in (fxx, fxy, fxz, fyx, fyy, fyz, fzx, fzy, fzz)]
+        dev = args[0][1]
+        return tuple(self._out(t, dev) for t in self._g().divT(*[a for a, _ in args]))
 
     # ------------------------------------------------------------------ mesh
     def _mesh(self, which):

@@ -344,6 +344,7 @@ class pyrandaSim:
         """pyranda.py:812-869 with the same keys; targets run on the device."""
         s = {}
         s["div("] = "self.div("
+        s["divT("] = "self.divT("
         s["ddx("] = "self.ddx("
         s["ddy("] = "self.ddy("
         s["ddz("] = "self.ddz("
@@ -355,8 +356,12 @@ class pyrandaSim:
         s["grad("] = "self.grad("
         s["simtime"] = "self.time"
         s["deltat"] = "self.deltat"
+        s["lap("] = "self.laplacian("
         s["ring("] = "self.ring("
         s["ringV("] = "self.ringV("
+        s["dd4x("] = "self.dd4x("
+        s["dd4y("] = "self.dd4y("
+        s["dd4z("] = "self.dd4z("
         s["dd8x("] = "self.dd8x("
         s["dd8y("] = "self.dd8y("
         s["dd8z("] = "self.dd8z("
@@ -531,6 +536,21 @@ class pyrandaSim:
 
     def ddz(self, val):
         return 0.0 if self.nz <= 1 else self.grid.ddz(val)
+
+    def dd4x(self, val):
+        return self.grid.d4(0, val)
+
+    def dd4y(self, val):
+        return self.grid.d4(1, val)
+
+    def dd4z(self, val):
+        return self.grid.d4(2, val)
+
+    def laplacian(self, val):
+        return self.grid.laplacian(val)
+
+    def divT(self, fxx, fxy, fxz, fyx, fyy, fyz, fzx, fzy, fzz):
+        return self.grid.divT(fxx, fxy, fxz, fyx, fyy, fyz, fzx, fzy, fzz)
 
     def dd8x(self, val):
         return self.grid.d8(0, val)

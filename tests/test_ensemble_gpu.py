@@ -62,11 +62,14 @@ def test_operators_match_single_grids(members, precision):
     for d in range(3):
         _same(ens, singles, ens.d1(d, v), [g.d1(d, vs[m]) for m, g in enumerate(singles)], "d1 %d" % d)
         _same(ens, singles, ens.d8(d, v), [g.d8(d, vs[m]) for m, g in enumerate(singles)], "d8 %d" % d)
+        _same(ens, singles, ens.d2(d, v), [g.d2(d, vs[m]) for m, g in enumerate(singles)], "d2 %d" % d)
+        _same(ens, singles, ens.d4(d, v), [g.d4(d, vs[m]) for m, g in enumerate(singles)], "d4 %d" % d)
     for kind in ("spectral", "gaussian"):
         for d in (0, 1, 2, 3):
             _same(ens, singles, ens.filter(kind, v, d),
                   [g.filter(kind, vs[m], d) for m, g in enumerate(singles)], "%s %d" % (kind, d))
     _same(ens, singles, ens.ring(v), [g.ring(vs[m]) for m, g in enumerate(singles)], "ring")
+    _same(ens, singles, ens.laplacian(v), [g.laplacian(vs[m]) for m, g in enumerate(singles)], "laplacian")
     _same(ens, singles, ens.ringv(v, w, v), [g.ringv(vs[m], ws[m], vs[m]) for m, g in enumerate(singles)],
           "ringv")
     ge = ens.grad(v)

@@ -58,6 +58,8 @@ def test_d1_d8_filters(grids, case):
         assert rel_l2(to_host(g.d8(d, dv)), o.apply(1, d, v)) <= TOL, ("d8", d)
         assert rel_l2(to_host(g.filter("spectral", dv, d)), o.apply(2, d, v)) <= TOL, ("sf", d)
         assert rel_l2(to_host(g.filter("gaussian", dv, d)), o.apply(3, d, v)) <= TOL, ("gf", d)
+        assert rel_l2(to_host(g.d2(d, dv)), o.apply(4, d, v)) <= TOL, ("d2", d)
+        assert rel_l2(to_host(g.d4(d, dv)), o.apply(5, d, v)) <= TOL, ("d4", d)
 
 
 @pytest.mark.parametrize("case", CASES, ids=_ids)
@@ -74,6 +76,11 @@ def test_composites(grids, case):
     for a, b in zip(g.grad(dv), o.grad(v)):
         assert rel_l2(to_host(a), b) <= TOL
     assert rel_l2(to_host(g.div(dv, dw, dq)), o.div(v, w, q)) <= TOL
+    assert rel_l2(to_host(g.laplacian(dv)), o.laplacian(v)) <= TOL
+    t = [smooth_field(case[0], seed=10 + k) for k in range(9)]
+    for a, b in zip(g.divT(*[to_dev(x, torch) for x in t]),
+                    (o.div(t[0], t[3], t[6]), o.div(t[1], t[4], t[7]), o.div(t[2], t[5], t[8]))):
+        assert rel_l2(to_host(a), b) <= TOL
 
 
 @pytest.mark.parametrize("case", CASES[:4], ids=_ids)
@@ -193,6 +200,9 @@ def test_fp32_sweeps_track_fp64(oracle, case):
         assert rel_l2(to_host(g.d8(d, dv)), o.apply(1, d, v)) <= 1e-5, ("d8", d)
         assert rel_l2(to_host(g.filter("spectral", dv, d)), o.apply(2, d, v)) <= 1e-6, ("sf", d)
         assert rel_l2(to_host(g.filter("gaussian", dv, d)), o.apply(3, d, v)) <= 1e-6, ("gf", d)
+        # single-precision RHS of a second / fourth difference: cancellation of the field's smooth part
+        assert rel_l2(to_host(g.d2(d, dv)), o.apply(4, d, v)) <= 1e-4, ("d2", d)
+        assert rel_l2(to_host(g.d4(d, dv)), o.apply(5, d, v)) <= 1e-3, ("d4", d)
     c = g.field(torch.full(shape, 3.25, dtype=torch.float64, device="cuda"))
     assert torch.equal(g.filter("spectral", c), c)
     assert float(g.d1(0, c).abs().max()) == 0.0
@@ -216,6 +226,12 @@ def test_parcop_shim_numpy_roundtrip(oracle):
     assert rel_l2(parcop.gfilter(v), o.gfilter(v)) <= TOL
     assert rel_l2(parcop.gfilterdir(v, 2), o.gfilterdir(v, 1)) <= TOL
     assert rel_l2(parcop.pring(v), o.ring(v, 2)) <= TOL
+    assert rel_l2(parcop.dd4x(v), o.dd4(0, v)) <= TOL
+    assert rel_l2(parcop.dd4y(v), o.dd4(1, v)) <= TOL
+    assert rel_l2(parcop.plaplacian(v), o.laplacian(v)) <= TOL
+    w = smooth_field(shape, seed=32)
+    dx, dy, dz = parcop.divergencetensor(v, w, v, w, v, w, v, w, v)
+    assert rel_l2(dy, o.div(w, v, w)) <= TOL
     gx, gy, gz = parcop.grads(v)
     assert rel_l2(gz, o.ddz(v)) <= TOL
     assert numpy.array_equal(parcop.xgrid(), o.mesh(0))

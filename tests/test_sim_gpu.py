@@ -155,6 +155,27 @@ def test_advection3d_config_matches_oracle(oracle):
     assert rel_l2(to_host(ss.variables["phi"].data), to_host(ss.variables["phi0"].data)) > 1e-3
 
 
+def test_laplacian_d4_and_tensor_divergence_in_the_eom(oracle):
+    """lap(), dd4x/y/z() and divT() of the EOM language (pyranda.py:818-835) against the oracle."""
+    from pyranda_gb300 import pyrandaSim
+    mesh = "xdom = (0.0, 1.0, 24)\nydom = (0.0, 0.9375, 16, periodic=True)\nzdom = (0.0, 0.9, 10, periodic=True)"
+    eom = """
+:lp: = lap(:f:)
+:d4x: = dd4x(:f:)
+:d4y: = dd4y(:g:)
+:d4z: = dd4z(:f:)
+[:tx:,:ty:,:tz:] = divT(:f:,:g:,:f:,:g:,:f:,:g:,:f:,:g:,:f:)
+"""
+    ic = ":f: = sin(2*pi*meshy)*exp(meshx) + cos(2*pi*meshz)\n:g: = meshx*meshx*cos(2*pi*meshy)"
+    ss = pyrandaSim("ops", mesh, silent=True)
+    so = oracle.OracleSim("ops", mesh)
+    for s in (ss, so):
+        s.EOM(eom)
+        s.setIC(ic)
+        s.updateVars()
+    _fields_match(ss, so, ["lp", "d4x", "d4y", "d4z", "tx", "ty", "tz"])
+
+
 def _packs(ss):
     from pyranda_gb300 import pyrandaBC, pyrandaTimestep
     ss.addPackage(pyrandaBC(ss))
