@@ -392,12 +392,14 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
     __syncthreads();
     const double sc = (P.scale_pow == 2) ? op.dm * op.dm : (P.scale_pow == 1 ? op.dm : 1.0);
     constexpr bool kReadOut = (EPI == EPI_ADD || EPI == EPI_RING_MAX);
+    // warps take rows, lanes consecutive columns: coalesced stores, no index division
+    constexpr int kWarps = kDenseThreads / 32;
     if (ORIENT == 0) {
       const int nl = tile.nlines, npos = min(N, n - drow0);
-      for (int idx = tid; idx < nl * N; idx += kDenseThreads) {
-        const int r = idx / N, col = idx - r * N;
-        if (col < npos) {
-          const int64_t a = s_base[r] + drow0 + col;
+      for (int r = warp; r < nl; r += kWarps) {
+        const int64_t b = s_base[r] + drow0;
+        for (int col = lane; col < npos; col += 32) {
+          const int64_t a = b + col;
           const double vin = ADDBACK ? P.in[a] : 0.0;
           const double o = kReadOut ? P.out[a] : 0.0;
           P.out[a] = epilogue<EPI>(f2d_bits(T[r * ld + col]), vin, o, sc, ADDBACK);
@@ -406,14 +408,15 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
     } else {
       // position drow0 + 128 pp + r of line col is T[r][128 pp + col]
       const int nl = tile.nlines, npos = min(NP * 128, n - drow0);
-      for (int idx = tid; idx < npos * N; idx += kDenseThreads) {
-        const int pr = idx / N, col = idx - pr * N;
-        if (col < nl) {
-          const int pp = pr >> 7, r = pr & 127;
-          const int64_t a = s_base[col] + (int64_t)(drow0 + pr) * st;
+      for (int pr = warp; pr < npos; pr += kWarps) {
+        const int pp = pr >> 7, r = pr & 127;
+        const int64_t b = (int64_t)(drow0 + pr) * st;
+        const float* trow = T + r * ld + pp * 128;
+        for (int col = lane; col < nl; col += 32) {
+          const int64_t a = s_base[col] + b;
           const double vin = ADDBACK ? P.in[a] : 0.0;
           const double o = kReadOut ? P.out[a] : 0.0;
-          P.out[a] = epilogue<EPI>(f2d_bits(T[r * ld + pp * 128 + col]), vin, o, sc, ADDBACK);
+          P.out[a] = epilogue<EPI>(f2d_bits(trow[col]), vin, o, sc, ADDBACK);
         }
       }
     }

@@ -144,7 +144,7 @@ class Grid:
             if a.ndim == 0:
                 out.fill_(float(a))
             else:
-                out.copy_(torch.from_numpy(numpy.ascontiguousarray(numpy.broadcast_to(a, self.n))).to(self.device))
+                out.copy_(torch.from_numpy(numpy.array(numpy.broadcast_to(a, self.n), order="C")).to(self.device))
         return out
 
     def _out(self, out):
