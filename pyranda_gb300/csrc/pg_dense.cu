@@ -162,9 +162,10 @@ __device__ __forceinline__ uint32_t tf32_bits(float x) {
   return (__float_as_uint(x) + 0x1000u) & 0xFFFFE000u;
 }
 
-// One staging item: v_{kb-1} and v_kb .. v_kb+3 of one line (v at p[k * st]).
+// One staging item: v_{kb-1} and v_kb .. v_kb+7 of one line (v at p[k * st]),
+// the two adjacent 16-byte chunks of 4 differences a thread stages per K chunk.
 struct Item {
-  double v[5];
+  double v[9];
 };
 
 __device__ __forceinline__ void load_item(const double* __restrict__ p, bool ok, int kb, int n, int periodic,
@@ -172,10 +173,10 @@ __device__ __forceinline__ void load_item(const double* __restrict__ p, bool ok,
   const int km1 = (kb > 0) ? kb - 1 : (periodic ? n - 1 : -1);
   it.v[0] = (ok && km1 >= 0 && km1 < n) ? __ldg(p + km1 * st) : 0.0;
 #pragma unroll
-  for (int j = 0; j < 4; j++) it.v[j + 1] = (ok && kb + j < n) ? __ldg(p + (kb + j) * st) : 0.0;
+  for (int j = 0; j < 8; j++) it.v[j + 1] = (ok && kb + j < n) ? __ldg(p + (kb + j) * st) : 0.0;
 }
 
-// The four differences w_k = v_k - v_{k-1}, k = kb .. kb+3, as TF32 hi / lo.
+// The eight differences w_k = v_k - v_{k-1}, k = kb .. kb+7, as TF32 hi / lo.
 // w_0 is the wrap difference v_0 - v_{n-1} on periodic lines and 0
 // otherwise; k >= n gives 0.  Each v is split into FP32 value + residual
 // first, so a difference keeps ~48 bits of v before its own rounding to FP32.
@@ -183,7 +184,7 @@ __device__ __forceinline__ void difference_item(const Item& it, bool ok, int kb,
                                                 uint32_t* l) {
   float2 prev = split_f64(it.v[0]);
 #pragma unroll
-  for (int j = 0; j < 4; j++) {
+  for (int j = 0; j < 8; j++) {
     const int k = kb + j;
     float f = 0.0f;
     if (ok && k < n) {
@@ -277,20 +278,16 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
   const int kchunks = op.kchunks;
   bool bad = false;
   int issued = -1, committed = -1;  // thread 0: last chunk whose D copy / MMAs were issued
-  // this thread's staging items: the same (row, 16-byte chunk) in every K chunk
-  constexpr int kItems = 1024 / kDenseThreads;
-  int item_r[kItems], item_q[kItems];
-#pragma unroll
-  for (int i = 0; i < kItems; i++) {
-    const int idx = tid + kDenseThreads * i;
-    item_r[i] = (ORIENT == 0) ? (idx >> 3) : (idx & 127);
-    item_q[i] = (ORIENT == 0) ? (idx & 7) : (idx >> 7);
-  }
+  // this thread's staging item: 16-byte chunks 2 qp and 2 qp + 1 of row item_r in every K chunk
+  // (128 rows x 4 chunk pairs = 512 threads; y, z: consecutive threads take consecutive lines)
+  static_assert(kDenseThreads == 512, "one chunk pair of one row per thread");
+  const int item_r = (ORIENT == 0) ? (tid >> 2) : (tid & 127);
+  const int item_q = 2 * ((ORIENT == 0) ? (tid & 3) : (tid >> 7));
   const int64_t vst = (ORIENT == 0) ? 1 : st;
-  Item cur[kItems], nxt[kItems];
-#pragma unroll
-  for (int i = 0; i < kItems; i++)
-    load_item(P.in + s_base[item_r[i]], item_r[i] < tile.nlines, item_q[i] * 4, n, op.periodic, vst, cur[i]);
+  const double* const item_p = P.in + s_base[item_r];
+  const bool item_ok = item_r < tile.nlines;
+  Item cur, nxt;
+  load_item(item_p, item_ok, item_q * 4, n, op.periodic, vst, cur);
 
   for (int c = 0; c < kchunks && !bad; c++) {
     const int s = c & 1;
@@ -300,12 +297,7 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
     uint8_t* d_hi = st_base + 2 * vbytes;
     uint8_t* d_lo = d_hi + dbytes;
     // the next chunk's loads go out first, so they are in flight across this chunk's work
-    if (c + 1 < kchunks) {
-#pragma unroll
-      for (int i = 0; i < kItems; i++)
-        load_item(P.in + s_base[item_r[i]], item_r[i] < tile.nlines, (c + 1) * kKC + item_q[i] * 4, n, op.periodic,
-                  vst, nxt[i]);
-    }
+    if (c + 1 < kchunks) load_item(item_p, item_ok, (c + 1) * kKC + item_q * 4, n, op.periodic, vst, nxt);
     // the MMAs that last read this stage (chunk c - 2) must be complete
     if (c >= 2 && !mbar_wait(&mma_bar[s], ((c >> 1) + 1) & 1)) bad = true;
     if (__syncthreads_or(bad)) break;
@@ -318,18 +310,18 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
     }
     // stage V: 16-byte chunks of 4 consecutive k (differences, split into TF32 hi / lo)
     const int k0 = c * kKC;
-#pragma unroll
-    for (int i = 0; i < kItems; i++) {
-      const int r = item_r[i], q = item_q[i];
-      uint32_t h[4], l[4];
-      difference_item(cur[i], r < tile.nlines, k0 + q * 4, n, op.periodic, h, l);
+    {
+      const int r = item_r, q = item_q;
+      uint32_t h[8], l[8];
+      difference_item(cur, item_ok, k0 + q * 4, n, op.periodic, h, l);
       if (ORIENT == 0 || r < vrows) {
         *reinterpret_cast<uint4*>(v_hi + swz(r, q)) = make_uint4(h[0], h[1], h[2], h[3]);
         *reinterpret_cast<uint4*>(v_lo + swz(r, q)) = make_uint4(l[0], l[1], l[2], l[3]);
+        *reinterpret_cast<uint4*>(v_hi + swz(r, q + 1)) = make_uint4(h[4], h[5], h[6], h[7]);
+        *reinterpret_cast<uint4*>(v_lo + swz(r, q + 1)) = make_uint4(l[4], l[5], l[6], l[7]);
       }
     }
-#pragma unroll
-    for (int i = 0; i < kItems; i++) cur[i] = nxt[i];
+    cur = nxt;
     fence_proxy_async();
     __syncthreads();
     if (tid == 0) {
