@@ -358,6 +358,48 @@ std::vector<double> difference_form(const std::vector<double>& D, int n, bool pe
 // the banded FP64 operator itself, applied to an identity (line k = e_k), so
 // the dense and banded paths implement one matrix.  Members with identical
 // tables share one split copy of D.
+// Inverse of the n x n LHS of one line from its band rows (a, b, diag, c, d;
+// periodic lines wrap), by Gauss-Jordan elimination with partial pivoting in
+// FP64.  Empty when singular.
+std::vector<double> invert_band(const std::vector<double>& band, int n, bool periodic) {
+  std::vector<double> A((size_t)n * n, 0.0), X((size_t)n * n, 0.0);
+  for (int i = 0; i < n; i++) {
+    X[(size_t)i * n + i] = 1.0;
+    for (int l = 0; l < 5; l++) {
+      int j = i + l - 2;
+      if (periodic) j = (j + n) % n;
+      else if (j < 0 || j >= n) continue;
+      A[(size_t)i * n + j] += band[(size_t)i * 5 + l];
+    }
+  }
+  for (int col = 0; col < n; col++) {
+    int piv = col;
+    for (int r = col + 1; r < n; r++)
+      if (std::fabs(A[(size_t)r * n + col]) > std::fabs(A[(size_t)piv * n + col])) piv = r;
+    if (A[(size_t)piv * n + col] == 0.0) return {};
+    if (piv != col)
+      for (int j = 0; j < n; j++) {
+        std::swap(A[(size_t)piv * n + j], A[(size_t)col * n + j]);
+        std::swap(X[(size_t)piv * n + j], X[(size_t)col * n + j]);
+      }
+    const double inv = 1.0 / A[(size_t)col * n + col];
+    for (int j = 0; j < n; j++) {
+      A[(size_t)col * n + j] *= inv;
+      X[(size_t)col * n + j] *= inv;
+    }
+    for (int r = 0; r < n; r++) {
+      if (r == col) continue;
+      const double f = A[(size_t)r * n + col];
+      if (f == 0.0) continue;
+      for (int j = 0; j < n; j++) {
+        A[(size_t)r * n + j] -= f * A[(size_t)col * n + j];
+        X[(size_t)r * n + j] -= f * X[(size_t)col * n + j];
+      }
+    }
+  }
+  return X;
+}
+
 int build_dense(Ctx& c, const std::vector<GridInfo>& g) {
   if (c.dense_built) return PG_OK;
   const int M = (int)g.size();
@@ -373,8 +415,9 @@ int build_dense(Ctx& c, const std::vector<GridInfo>& g) {
   for (int k : kinds)
     for (int d = 0; d < 3; d++) {
       if (c.ops[PG_FP64][k][d].null_op) continue;
-      // d8 with the exact fixed-point RHS stays banded: split TF32 products cannot hold its cancellation
-      if (k == OPK_D8 && c.ops[PG_FP32][k][d].exact) continue;
+      // d8 with the exact fixed-point RHS: the dense form is A^-1 alone, applied to that RHS
+      // (split TF32 products cannot hold the 8th difference's cancellation); without it, no dense d8
+      if (k == OPK_D8 && !c.ops[PG_FP32][k][d].exact) continue;
       bool fits = true;
       for (int m = 0; m < M; m++) fits = fits && g[m].n[d] >= 16 && g[m].n[d] <= 1024;
       if (!fits) continue;
@@ -412,6 +455,16 @@ int build_dense(Ctx& c, const std::vector<GridInfo>& g) {
   for (size_t q = 0; q < uniq.size() && rc == PG_OK; q++) {
     Uniq& u = uniq[q];
     const int n = g[u.m].n[u.d];
+    if (u.k == OPK_D8) {  // A^-1 of the LHS band, in FP64 on the host
+      D = invert_band(g[u.m].tab[u.k][u.d].lhs, n, c.ops[PG_FP64][u.k][u.d].periodic);
+      if (D.empty()) {
+        set_error("dense operators: singular d8 LHS");
+        rc = PG_EINVAL;
+        break;
+      }
+      split_dense(D, n, u.planes, u.rows, u.kchunks);
+      continue;
+    }
     eye.assign((size_t)n * n, 0.0);
     for (int i = 0; i < n; i++) eye[(size_t)i * n + i] = 1.0;
     const size_t mi = ((((size_t)PG_FP64 * OPK_COUNT + u.k) * 3 + u.d) * M) + u.m;
@@ -483,6 +536,7 @@ int build_dense(Ctx& c, const std::vector<GridInfo>& g) {
         o.kchunks = u.kchunks;
         o.rows = u.rows;
         o.periodic = g[m].periodic[d];
+        o.direct = (k == OPK_D8) ? 1 : 0;
         o.dm = g[m].dm[d];
         dops.push_back(o);
         const int lines = (int)(g[m].npts / n);
@@ -522,10 +576,14 @@ int build_dense(Ctx& c, const std::vector<GridInfo>& g) {
       ds.ntiles = set_nt[k][d];
       ds.ok = true;
       ds.addback = c.ops[PG_FP64][k][d].addback;
+      ds.direct = (k == OPK_D8);
     }
   c.dense_built = true;
   return PG_OK;
 }
+
+int dense_sweep(Ctx& c, int kind, int dir, const double* in, double* out, int epi, int scale_pow, void* st,
+                bool emax_ready);
 
 // Autotuning of PG_AUTO: for every (operator, direction) with a dense form,
 // time the dense kernel and the FP32 banded sweep on this grid (CUDA events,
@@ -551,7 +609,7 @@ int autotune_dense(Ctx& c) {
         float best[3];
         for (int rep = 0; rep < 4 && rc == PG_OK; rep++) {
           cudaEventRecord(e0, 0);
-          if (way == 0) rc = launch_dense(ds, c.work, out, d, EPI_STORE, 0, c.status, nullptr);
+          if (way == 0) rc = dense_sweep(c, k, d, c.work, out, EPI_STORE, 0, nullptr, false);
           else {
             SweepLaunch s{c.work, out, c.work2, &c.ops[PG_FP32][k][d], d, EPI_STORE, 0, c.emax, c.moff};
             rc = launch_sweep(PG_FP32, s, nullptr);
@@ -597,16 +655,31 @@ int set_precision(Ctx& c, const std::vector<GridInfo>& g, int precision) {
 }
 
 // emax_ready: the exponents of `in` for the exact d8 RHS are already in c.emax
+// One dense sweep.  d8 (direct): the exact fixed-point RHS of every point
+// into work2, then A^-1 on the tensor cores.
+int dense_sweep(Ctx& c, int kind, int dir, const double* in, double* out, int epi, int scale_pow, void* st,
+                bool emax_ready) {
+  const DenseSet& ds = c.dsets[kind][dir];
+  if (ds.direct) {
+    if (!emax_ready) {
+      const int rc = launch_max_exponent(in, c.moff, c.nmem, c.emax, st);
+      if (rc) return rc;
+    }
+    const int rc = launch_d8_rhs(c.ops[PG_FP32][kind][dir], in, c.work2, dir, c.emax, c.npts, st);
+    if (rc) return rc;
+    return launch_dense(ds, c.work2, out, dir, epi, scale_pow, c.status, st);
+  }
+  if (in == out) {  // tiles read whole lines that other tiles write: work on a copy
+    int rc = launch_copy(c.work2, in, c.npts, st);
+    if (rc) return rc;
+    in = c.work2;
+  }
+  return launch_dense(ds, in, out, dir, epi, scale_pow, c.status, st);
+}
+
 int sweep(Ctx& c, int kind, int dir, const double* in, double* out, int epi, int scale_pow, void* st,
           bool emax_ready = false) {
-  if (c.dense && c.use_dense[kind][dir]) {
-    if (in == out) {  // tiles read whole lines that other tiles write: work on a copy
-      int rc = launch_copy(c.work2, in, c.npts, st);
-      if (rc) return rc;
-      in = c.work2;
-    }
-    return launch_dense(c.dsets[kind][dir], in, out, dir, epi, scale_pow, c.status, st);
-  }
+  if (c.dense && c.use_dense[kind][dir]) return dense_sweep(c, kind, dir, in, out, epi, scale_pow, st, emax_ready);
   SweepLaunch s{in, out, c.work2, &c.ops[c.precision][kind][dir], dir, epi, scale_pow, c.emax, c.moff, emax_ready};
   return launch_sweep(c.precision, s, st);
 }

@@ -180,8 +180,9 @@ __device__ __forceinline__ void load_item(const double* __restrict__ p, bool ok,
 // w_0 is the wrap difference v_0 - v_{n-1} on periodic lines and 0
 // otherwise; k >= n gives 0.  Each v is split into FP32 value + residual
 // first, so a difference keeps ~48 bits of v before its own rounding to FP32.
-__device__ __forceinline__ void difference_item(const Item& it, bool ok, int kb, int n, int periodic, uint32_t* h,
-                                                uint32_t* l) {
+// direct: the values v_k themselves (their FP32 value + residual).
+__device__ __forceinline__ void difference_item(const Item& it, bool ok, int kb, int n, int periodic, int direct,
+                                                uint32_t* h, uint32_t* l) {
   float2 prev = split_f64(it.v[0]);
 #pragma unroll
   for (int j = 0; j < 8; j++) {
@@ -189,7 +190,8 @@ __device__ __forceinline__ void difference_item(const Item& it, bool ok, int kb,
     float f = 0.0f;
     if (ok && k < n) {
       const float2 v = split_f64(it.v[j + 1]);
-      if (k > 0 || periodic) f = (v.x - prev.x) + (v.y - prev.y);
+      if (direct) f = v.x + v.y;
+      else if (k > 0 || periodic) f = (v.x - prev.x) + (v.y - prev.y);
       prev = v;
     }
     h[j] = tf32_bits(f);
@@ -313,7 +315,7 @@ __global__ void __launch_bounds__(kDenseThreads, 1) dense_kernel(const DParams P
     {
       const int r = item_r, q = item_q;
       uint32_t h[8], l[8];
-      difference_item(cur, item_ok, k0 + q * 4, n, op.periodic, h, l);
+      difference_item(cur, item_ok, k0 + q * 4, n, op.periodic, op.direct, h, l);
       if (ORIENT == 0 || r < vrows) {
         *reinterpret_cast<uint4*>(v_hi + swz(r, q)) = make_uint4(h[0], h[1], h[2], h[3]);
         *reinterpret_cast<uint4*>(v_lo + swz(r, q)) = make_uint4(l[0], l[1], l[2], l[3]);

@@ -18,6 +18,7 @@ struct OpTables {
   bool periodic = false, implicit = false, addback = false, null_op = true;
   std::vector<double> rhs;  // n x 9 per-row RHS weights
   std::vector<double> lu;   // n x 9 per-row solve coefficients
+  std::vector<double> lhs;  // n x 5 LHS band (a, b, diag, c, d) before factorisation
 };
 
 int build_operator(int kind, int n, bool periodic, double scale, OpTables& t);
@@ -82,6 +83,11 @@ struct SweepLaunch {
 
 // Launches one directional sweep over every member.  Returns a pg_status.
 int launch_sweep(int precision, const SweepLaunch& s, void* stream);
+// The exact fixed-point RHS of the d8 sweeps (FP32 path) of every point along
+// `dir`, rounded once to FP32 and stored as FP64 in `rhs`; emax holds the
+// members' exponents (launch_max_exponent).
+int launch_d8_rhs(const OpRef& op, const double* in, double* rhs, int dir, const int* emax, int64_t npts,
+                  void* stream);
 
 // Dense operator of one member along one direction (device memory): the
 // difference form D' of D (OUT = D' w, w_k = v_k - v_{k-1}) split into TF32
@@ -95,6 +101,7 @@ struct DenseOp {
   int kchunks;      // ceil(n / 32)
   int rows;         // rows of each plane: n padded to a multiple of 128
   int periodic;     // 1: w_0 = v_0 - v_{n-1} (the wrap difference)
+  int direct;       // 1: the planes hold D itself, applied to v (no differences)
   double dm;        // mesh spacing along the direction (ring scale)
 };
 // One CTA's output tile: lines [line0, line0 + nlines) of member `op`
@@ -112,6 +119,7 @@ struct DenseSet {
   int ntiles = 0;
   bool ok = false;       // dense form built (every member has 16 <= n <= 1024)
   bool addback = false;  // filters: out = v + D v with D = A^-1 (B - A)
+  bool direct = false;   // d8: D = A^-1 applied to the exact fixed-point RHS (launch_d8_rhs)
 };
 // Split a row-major n x n FP64 matrix into the DenseOp plane layout.
 void split_dense(const std::vector<double>& D, int n, std::vector<uint32_t>& out, int& rows, int& kchunks);

@@ -325,6 +325,9 @@ int build_operator(int kind, int n, bool periodic, double scale, OpTables& t) {
   }
   if (scale != 0.0)
     for (auto& v : t.rhs) v = v / scale;
+  t.lhs.assign((size_t)n * 5, 0.0);
+  for (int i = 0; i < n; i++)
+    for (int l = 0; l < 5; l++) t.lhs[(size_t)i * 5 + l] = band[(size_t)i * 9 + l];
 
   if (s.implicit) {
     auto L = [&](int i, int k) -> double& { return t.lu[(size_t)i * 9 + k]; };

@@ -274,19 +274,23 @@ def test_bounded_wait_reports_timeout_and_context_survives(grids):
     assert rel_l2(to_host(g.ddx(to_dev(v, torch))), o.ddx(v)) < 1e-12
 
 
+@pytest.mark.parametrize("precision", ["fp32", "dense"])
 @pytest.mark.parametrize("per", [(True, True, True), (False, True, False)], ids=["PPP", "NPN"])
-def test_fp32_d8_rhs_is_exact(per):
-    """d8 and ring on the FP32 path take their RHS in exact 64-bit fixed point.
+def test_fp32_d8_rhs_is_exact(per, precision):
+    """d8 and ring on the FP32 paths take their RHS in exact 64-bit fixed point.
 
     On a smooth field with a large mean the 8th difference cancels ~40 of the
-    53 bits, so an FP32 RHS would be noise; with the exact RHS only the FP32
-    solve rounds, and the result stays within 2e-6 relative L2 of the FP64 path.
+    53 bits, so an FP32 RHS would be noise; with the exact RHS only the solve
+    rounds -- the FP32 banded solve, or A^-1 in split TF32 on the tensor cores
+    ('dense') -- and the result stays within 2e-6 relative L2 of the FP64 path.
     """
     from pyranda_gb300.grid import Grid
     shape = (64, 48, 40)
     x1, xn = (0.0, 0.0, 0.0), (1.0, 1.0, 1.0)
     g64 = Grid(shape, per, x1, xn, precision="fp64")
-    g32 = Grid(shape, per, x1, xn, precision="fp32")
+    g32 = Grid(shape, per, x1, xn, precision=precision)
+    if precision == "dense":
+        assert all(g32.dense_plan()[("d8", a)] for a in "xyz")
     x, y, z = (g64.mesh(d) for d in range(3))
     v = 5.0 + torch.sin(2 * math.pi * x) * torch.cos(2 * math.pi * y) + 0.5 * torch.sin(2 * math.pi * z + 0.3)
     for d in range(3):
