@@ -108,6 +108,7 @@ struct Ctx {
   double* partial = nullptr;     // reduction partials (+ per-member results)
   int* status = nullptr;         // device status word
   int* emax = nullptr;           // exact d8 RHS: per member the largest exponent of the sweep input
+  int nmax[3] = {0, 0, 0};       // the longest member line along each direction
   long long* moff = nullptr;     // ensembles: member point offsets (nmem + 1)
   double* mconst = nullptr;      // ensembles: per member 1/d1 1/d2 1/d3 1/GridLen GridLen
   double* host_in = nullptr;     // host-pointer variants
@@ -188,6 +189,8 @@ int build_ctx(Ctx& c, const std::vector<GridInfo>& g, int precision, const char*
     }
   std::vector<long long> off(M + 1, 0);
   for (int m = 0; m < M; m++) off[m + 1] = off[m] + g[m].npts;
+  for (int d = 0; d < 3; d++)
+    for (int m = 0; m < M; m++) c.nmax[d] = std::max(c.nmax[d], g[m].n[d]);
   c.npts = off[M];
   // layout of the blob: [tables ...][member ops (2 x 4 x 3 x M)]
   auto align = [](size_t x) { return (x + 15) & ~(size_t)15; };
@@ -665,7 +668,7 @@ int dense_sweep(Ctx& c, int kind, int dir, const double* in, double* out, int ep
       const int rc = launch_max_exponent(in, c.moff, c.nmem, c.emax, st);
       if (rc) return rc;
     }
-    const int rc = launch_d8_rhs(c.ops[PG_FP32][kind][dir], in, c.work2, dir, c.emax, c.npts, st);
+    const int rc = launch_d8_rhs(c.ops[PG_FP32][kind][dir], in, c.work2, dir, c.emax, c.nmax[dir], st);
     if (rc) return rc;
     return launch_dense(ds, c.work2, out, dir, epi, scale_pow, c.status, st);
   }

@@ -85,8 +85,8 @@ struct SweepLaunch {
 int launch_sweep(int precision, const SweepLaunch& s, void* stream);
 // The exact fixed-point RHS of the d8 sweeps (FP32 path) of every point along
 // `dir`, rounded once to FP32 and stored as FP64 in `rhs`; emax holds the
-// members' exponents (launch_max_exponent).
-int launch_d8_rhs(const OpRef& op, const double* in, double* rhs, int dir, const int* emax, int64_t npts,
+// members' exponents (launch_max_exponent); nmax = the longest member line.
+int launch_d8_rhs(const OpRef& op, const double* in, double* rhs, int dir, const int* emax, int nmax,
                   void* stream);
 
 // Dense operator of one member along one direction (device memory): the

@@ -10,65 +10,80 @@ int launch_sweep_f32(const OpRef& op, const KParams& P, int dir, int epi, void* 
 
 namespace {
 
-// One thread per point: the d8 RHS of its row along DIR, exactly as the
-// banded FP32 sweep forms it (64-bit fixed point at the member's exponent;
-// edge rows with their integer weights, interior rows with iw), rounded once
-// to FP32.
+// The d8 RHS of every row along DIR, exactly as the banded FP32 sweep forms
+// it (64-bit fixed point at the member's exponent; edge rows with their
+// integer weights, interior rows as iw[0] x the 8th difference), rounded once
+// to FP32.  One thread owns a run of kRun rows of one line (blockIdx.y = run):
+// each value is loaded and converted once, and the interior rows come from a
+// cascade of differences primed with the 8 values before the first of them.
+constexpr int kRun = 16;
+
 template <bool PER, int DIR>
-__global__ void __launch_bounds__(256) d8_rhs_kernel(const MemberOp* __restrict__ ops, int nops,
+__global__ void __launch_bounds__(128) d8_rhs_kernel(const MemberOp* __restrict__ ops, int nops, long long nlines,
                                                      const double* __restrict__ in, const int* __restrict__ emax,
-                                                     int64_t npts, double* __restrict__ rhs) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npts;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    int m = 0;
-    if (nops > 1) {  // the member owning point p: last entry with off <= p
-      int lo = 0, hi = nops - 1;
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (ops[mid].off <= p) lo = mid;
-        else hi = mid - 1;
-      }
-      m = lo;
+                                                     double* __restrict__ rhs) {
+  const int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (L >= nlines) return;
+  int m = 0;
+  if (nops > 1) {  // the member owning line L: last entry with line0 <= L
+    int lo = 0, hi = nops - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (ops[mid].line0 <= L) lo = mid;
+      else hi = mid - 1;
     }
-    const MemberOp& op = ops[m];
-    const int64_t q = p - op.off;
-    const int nx = op.nx, ny = op.ny, n = op.n;
-    int i, st;
-    if (DIR == 0) {
-      i = (int)(q % nx);
-      st = 1;
-    } else if (DIR == 1) {
-      i = (int)((q / nx) % ny);
-      st = nx;
-    } else {
-      i = (int)(q / ((int64_t)nx * ny));
-      st = nx * ny;
-    }
-    const int E = __ldg(emax + m);
-    const Line<long long> ln{in + p - (int64_t)i * st, st, n, E};
-    long long s;
+    m = lo;
+  }
+  const MemberOp& op = ops[m];
+  const int n = op.n;
+  const int i0 = blockIdx.y * kRun;
+  if (i0 >= n) return;
+  const int64_t Lm = L - op.line0;
+  const int nx = op.nx, ny = op.ny;
+  int64_t base;
+  int st;
+  if (DIR == 0) {
+    base = Lm * nx;
+    st = 1;
+  } else if (DIR == 1) {
+    base = (Lm / nx) * (int64_t)nx * ny + (Lm % nx);
+    st = nx;
+  } else {
+    base = (Lm / nx) * (int64_t)nx + (Lm % nx);
+    st = nx * ny;
+  }
+  base += op.off;
+  const int E = __ldg(emax + m);
+  const Line<long long> ln{in + base, st, n, E};
+  double* __restrict__ out = rhs + base;
+  const float wi = op.wscale * (float)op.iw[0];
+  Cascade cas{};
+  bool primed = false;
+  const int i1 = min(i0 + kRun, n);
+  for (int i = i0; i < i1; i++) {
+    float r;
     if (i < 4 || i >= n - 4) {
-      s = edge_rhs<long long, 4, PER, int>(ln, i, op.rhs_i);
+      r = fixed_to_float(edge_rhs<long long, 4, PER, int>(ln, i, op.rhs_i), E, op.wscale);
     } else {
-      const long long mc = ln.v(i);
-      s = 0;
+      if (!primed) {
 #pragma unroll
-      for (int l = 0; l < 9; l++)
-        if (l != 4) s += (long long)op.iw[l] * (ln.v(i + l - 4) - mc);
+        for (int k = 0; k < 8; k++) cas.push(ln.v(i - 4 + k));
+        primed = true;
+      }
+      r = fixed_to_float(cas.push(ln.v(i + 4)), E, wi);
     }
-    rhs[p] = f2d_bits(fixed_to_float(s, E, op.wscale));
+    out[(int64_t)i * st] = f2d_bits(r);
   }
 }
 
 template <bool PER>
-int launch_d8_rhs_dir(const OpRef& op, const double* in, double* rhs, int dir, const int* emax, int64_t npts,
+int launch_d8_rhs_dir(const OpRef& op, const double* in, double* rhs, int dir, const int* emax, int nmax,
                       void* stream) {
-  const int64_t b = (npts + 255) / 256;
-  const unsigned blocks = (unsigned)(b < 152 * 16 ? (b > 0 ? b : 1) : 152 * 16);
+  const dim3 grid((unsigned)((op.nlines + 127) / 128), (unsigned)((nmax + kRun - 1) / kRun));
   cudaStream_t s = (cudaStream_t)stream;
-  if (dir == 0) d8_rhs_kernel<PER, 0><<<blocks, 256, 0, s>>>(op.dev, op.nops, in, emax, npts, rhs);
-  else if (dir == 1) d8_rhs_kernel<PER, 1><<<blocks, 256, 0, s>>>(op.dev, op.nops, in, emax, npts, rhs);
-  else d8_rhs_kernel<PER, 2><<<blocks, 256, 0, s>>>(op.dev, op.nops, in, emax, npts, rhs);
+  if (dir == 0) d8_rhs_kernel<PER, 0><<<grid, 128, 0, s>>>(op.dev, op.nops, op.nlines, in, emax, rhs);
+  else if (dir == 1) d8_rhs_kernel<PER, 1><<<grid, 128, 0, s>>>(op.dev, op.nops, op.nlines, in, emax, rhs);
+  else d8_rhs_kernel<PER, 2><<<grid, 128, 0, s>>>(op.dev, op.nops, op.nlines, in, emax, rhs);
   count_launch();
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
@@ -80,14 +95,14 @@ int launch_d8_rhs_dir(const OpRef& op, const double* in, double* rhs, int dir, c
 
 }  // namespace
 
-int launch_d8_rhs(const OpRef& op, const double* in, double* rhs, int dir, const int* emax, int64_t npts,
+int launch_d8_rhs(const OpRef& op, const double* in, double* rhs, int dir, const int* emax, int nmax,
                   void* stream) {
-  if (op.kind != OPK_D8 || !op.exact || op.null_op) {
+  if (op.kind != OPK_D8 || !op.exact || op.null_op || nmax < 1 || op.nlines < 1) {
     set_error("d8 rhs: the operator has no exact fixed-point RHS");
     return PG_EINVAL;
   }
-  return op.periodic ? launch_d8_rhs_dir<true>(op, in, rhs, dir, emax, npts, stream)
-                     : launch_d8_rhs_dir<false>(op, in, rhs, dir, emax, npts, stream);
+  return op.periodic ? launch_d8_rhs_dir<true>(op, in, rhs, dir, emax, nmax, stream)
+                     : launch_d8_rhs_dir<false>(op, in, rhs, dir, emax, nmax, stream);
 }
 
 }  // namespace pg
