@@ -889,7 +889,7 @@ def main():
                                    "LSRK(5,4), CFL 0.5" % n,
                        "grid": [n, n, n],
                        "path": {"dense": "dense split-TF32 tensor-core operators (d1, compact and Gaussian "
-                                         "filters), banded d8 with exact fixed-point RHS",
+                                         "filters), d8 as A^-1 on its exact fixed-point RHS",
                                 "auto": "per operator and direction the faster of dense split-TF32 and FP32 banded "
                                         "(autotuned on the grid)",
                                 "fp32": "fp32 banded sweeps"}[fast_runs[best]["prec"]]

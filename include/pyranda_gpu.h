@@ -51,8 +51,9 @@ typedef enum {
  * PG_DENSE applies d1 and the two filters as dense n x n operators
  * D = A^-1 B (the reference's `sm`, compact_basetype.f90:199-205) on the
  * tensor cores in split TF32 (hi.hi + hi.lo + lo.hi, FP32 accumulation) for
- * directions of 16..1024 points, and the FP32 banded sweeps elsewhere (and
- * for d8); the filters' add-back of v stays in FP64.  PG_AUTO builds the same tables and
+ * directions of 16..1024 points, and d8 as A^-1 applied to its exact
+ * fixed-point RHS; the FP32 banded sweeps elsewhere; the filters' add-back
+ * of v stays in FP64.  PG_AUTO builds the same tables and
  * then, per operator and direction, times the dense kernel against the FP32
  * banded sweep on the handle's own grid and keeps the faster.  Selecting
  * either builds the tables once (allocates and synchronises). */
