@@ -70,7 +70,7 @@ def parse():
     p.add_argument("--train-cosine", action="store_true", help="shock-learned: cosine learning-rate decay")
     p.add_argument("--train-shape", default="128,64,64", help="shock-learned: grid of the training runs")
     p.add_argument("--save-model", default=None, help="shock-learned: where a newly trained closure is saved "
-                                                      "(default gpurun_out/lad_shock.npz)")
+                                                      "(default pyranda_gb300/_build/lad_shock_trained.npz)")
     p.add_argument("--members", type=int, default=64, help="ensemble mode: number of members")
     p.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "dense", "auto", "fp32-only"],
                    help="profile mode: arithmetic of the profiled step; step mode: 'fp32-only' skips the dense run")
@@ -597,7 +597,7 @@ def shock_learned(args):
                         log_every=max(1, args.train_iters // 8), cosine=args.train_cosine)
         torch.cuda.synchronize()
         t2 = time.time()
-        save = args.save_model or os.path.join(ROOT, "gpurun_out", "lad_shock.npz")
+        save = args.save_model or os.path.join(ROOT, "pyranda_gb300", "_build", "lad_shock_trained.npz")
         os.makedirs(os.path.dirname(os.path.abspath(save)), exist_ok=True)
         model.save(save)
         out["training"] = {"shape": list(shape), "iters": args.train_iters, "cosine": args.train_cosine,

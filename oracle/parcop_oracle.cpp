@@ -1,9 +1,9 @@
 // ORACLE — test infrastructure only.
 //
 // A plain FP64 CPU restatement of pyranda's parcop compact-operator path, used
-// by the test-suite as the checker for the CUDA library, by smoke() as the
-// reference answer, and by bench.py as the timed CPU baseline.  Nothing in the
-// product links or calls this file.
+// by the test-suite and by smoke() as the expected answer for the CUDA library,
+// and by bench.py as the timed CPU baseline.  Nothing in the product links or
+// calls this file.
 //
 // Every routine names the reference Fortran it restates (paths relative to the
 // pyranda project).  The arithmetic follows the reference loop by loop (same

@@ -11,7 +11,7 @@ filters (six sweeps) per RK stage.  The learned closure replaces them with one
 pass for |grad rho| (second-order central differences,
 ``pg_lad_grad_magnitude``) and one fused feature-gather + MLP kernel
 (``pg_lad_closure``).  The plain closure stays
-both the judge of the learned one's error and its fallback: the kernel raises
+both the reference for the learned one's error and its fallback: the kernel raises
 a flag when a prediction leaves the training range, and
 ``pyrandaLearnedLAD.step`` then re-runs that RK step with the plain closure
 from the step's conserved state.

@@ -159,7 +159,7 @@ def test_fallback_flag_reruns_the_step_with_the_plain_closure(graphs):
 
 @pytest.mark.slow
 def test_trained_closure_beats_untrained_and_none():
-    """Train on snapshots of small seeded runs; judge on an unseen state and an unseen run.
+    """Train on snapshots of small seeded runs; evaluate on an unseen state and an unseen run.
 
     * On a held-out plain-LAD state (Mach and amplitude outside the training
       seeds' draws), the trained network's beta and kappa are much closer to
