@@ -51,8 +51,11 @@ def _same(ens, singles, flat, outs, what):
 
 
 @pytest.mark.parametrize("members", [MEMBERS_3D, MEMBERS_2D], ids=["3d", "2d"])
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32", "dense"])
 def test_operators_match_single_grids(members, precision):
+    if precision == "dense" and members is MEMBERS_3D:
+        pytest.skip("a member direction of 8 points has no dense form, so the ensemble sweeps that direction "
+                    "banded while its other members alone would not")
     ens, singles = _pair(members, precision)
     host = _fields(members, 3)
     v = ens.from_members(host)
