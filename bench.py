@@ -301,6 +301,15 @@ def l2_errors(a, b, names):
     return out
 
 
+def linf_errors(a, b, names):
+    """max |a - b| / max |b| per field."""
+    out = {}
+    for n in names:
+        x, y = a.variables[n].data, b.variables[n].data
+        out[n] = float(((x - y).abs().max() / y.abs().max()).item())
+    return out
+
+
 def momentum_error(a, b, names=("rhou", "rhov", "rhow")):
     """Relative L2 error of the momentum vector field (rho u, rho v, rho w) of `a` against `b`."""
     num = sum(float((a.variables[n].data - b.variables[n].data).norm()) ** 2 for n in names)
@@ -814,8 +823,11 @@ def main():
         for p, r in fast_runs.items():
             errs = l2_errors(r["sim"], plain, ["rho", "rhou", "rhov", "rhow", "Et"])
             extra["fast_paths"][p]["l2_err_vs_fp64"] = {kk: float("%.3e" % vv) for kk, vv in errs.items()}
+            errs = linf_errors(r["sim"], plain, ["rho", "rhou", "rhov", "rhow", "Et"])
+            extra["fast_paths"][p]["linf_err_vs_fp64"] = {kk: float("%.3e" % vv) for kk, vv in errs.items()}
             extra["fast_paths"][p]["l2_err_vs_fp64"]["momentum_vector"] = float("%.3e" % momentum_error(r["sim"], plain))
         extra["l2_err_vs_fp64"] = extra["fast_paths"][best]["l2_err_vs_fp64"]
+        extra["linf_err_vs_fp64"] = extra["fast_paths"][best]["linf_err_vs_fp64"]
         extra["l2_err_steps"] = w + k
         if args.err_steps > w + k:   # the headline path and the plain one continued to the configuration's length
             more = args.err_steps - (w + k)
@@ -824,7 +836,9 @@ def main():
             errs = l2_errors(fast, plain, ["rho", "rhou", "rhov", "rhow", "Et"])
             errs = {kk: float("%.3e" % vv) for kk, vv in errs.items()}
             errs["momentum_vector"] = float("%.3e" % momentum_error(fast, plain))
-            extra["l2_err_vs_fp64_long"] = {"steps": args.err_steps, "path": best, "rel_l2": errs}
+            linf = {kk: float("%.3e" % vv)
+                    for kk, vv in linf_errors(fast, plain, ["rho", "rhou", "rhov", "rhow", "Et"]).items()}
+            extra["l2_err_vs_fp64_long"] = {"steps": args.err_steps, "path": best, "rel_l2": errs, "rel_linf": linf}
         del plain
         torch.cuda.empty_cache()
 
@@ -854,7 +868,11 @@ def main():
         roof_extra = {}
     roof = {"bound": "hbm", "kernel": kname,
             "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
-            "traffic": None, "algorithmic_bytes_per_launch": 16 * npts,
+            # DRAM bytes of one launch of this kernel at 256^3 from one ncu capture (read + write)
+            "traffic": ((136362752 + 88161280) if dense_y else (275878656 + 163471872)) if n == 256 else None,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at 256^3 "
+                              "(profiles/roofline_traffic_256.md)",
+            "algorithmic_bytes_per_launch": 16 * npts,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s",
             "sweep_ms": {kk: round(vv * 1e3, 4) for kk, vv in sw.items()}}
     roof.update(roof_extra)
