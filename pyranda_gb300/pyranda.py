@@ -255,6 +255,8 @@ class pyrandaSim:
     def __init__(self, name, meshOptions, silent=False, precision="fp64", device=None):
         self.name = name
         self.silent = silent
+        self.ioformat = "BINARY"   # viz dumps: "BINARY" or "ASCII" (pyrandaIO.py:25)
+        self.vizDumpHistory = []
         self.mesh = _Mesh()
         if isinstance(meshOptions, str):
             meshOptions = self._parse_mesh(meshOptions)
@@ -626,6 +628,38 @@ class pyrandaSim:
         if vname not in table:
             raise ValueError("mesh variable %s is not available on Cartesian meshes" % vname)
         return self.grid.mesh(table[vname])
+
+    # -------------------------------------------------------------- viz dumps
+    def write(self, wVars=None):
+        """pyranda.py:431-470: a visualisation dump in pyranda's VTK format (pyranda_gb300.vtk).
+
+        ``<name>/vis<cycle>/proc-000000.<cycle>.vtk`` holds the variables of
+        wVars (default: the conserved ones) on the mesh coordinates, BINARY or
+        ASCII after ``self.ioformat``; ``<name>/pyranda.visit`` lists every
+        dump written so far.  Returns the file's path.
+        """
+        from . import vtk
+        wVars = list(wVars) if wVars else list(self.conserved)
+        path = vtk.dump_path(self.name, self.cycle)
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        shape = (self.nx, self.ny, self.nz)
+
+        def host(v):
+            a = v.numpy()
+            return numpy.broadcast_to(numpy.asarray(a, dtype=numpy.float64), shape) if numpy.ndim(a) < 3 else a
+
+        coords = [host(c) for c in self.mesh.coords]
+        fields = {n: host(self.variables[n]) for n in wVars}
+        t = _num(self.time)
+        if getattr(self, "ioformat", "BINARY") == "ASCII":
+            vtk.write_ascii(path, coords, fields, wVars, int(self.cycle), t)
+        else:
+            vtk.write_binary(path, coords, fields, wVars, int(self.cycle), t)
+        if not hasattr(self, "vizDumpHistory"):
+            self.vizDumpHistory = []
+        self.vizDumpHistory.append([self.cycle, t])
+        vtk.write_visit(self.name, self.vizDumpHistory)
+        return path + ".vtk"
 
     # ---------------------------------------------------------------- restart
     def writeRestart(self, ivars=None, suffix=None, wVars=None):

@@ -235,3 +235,29 @@ def test_restart_round_trip(tmp_path, monkeypatch):
         tb = b.rk4(tb, b.variables["dt"].data * 0.5)
     for name in ("rho", "rhou", "rhov", "rhow", "Et"):
         assert torch.equal(a.variables[name].data, b.variables[name].data), name
+
+
+def test_vtk_dump(tmp_path, monkeypatch):
+    """sim.write() (pyranda.py:431-470): pyranda's binary VTK dump of the device fields and the .visit list."""
+    from pyranda_gb300 import problems, pyrandaSim
+    monkeypatch.chdir(tmp_path)
+    ss = problems.build_tgv(pyrandaSim, 16, _ts, silent=True)
+    ss.rk4(0.0, ss.variables["dt"].data.clone())
+    path = ss.write(["rho", "u"])
+    assert os.path.basename(path) == "proc-000000.0000001.vtk"
+    raw = open(path, "rb").read()
+    assert b"DIMENSIONS  16 16 16  \n" in raw
+    nb = 16 ** 3 * 4
+
+    def block(name):
+        tag = b"SCALARS %s float \nLOOKUP_TABLE default \n" % name.encode()
+        p = raw.index(tag) + len(tag)
+        return numpy.frombuffer(raw[p:p + nb], dtype=">f4")
+
+    rho, u = block("rho"), block("u")
+    tag = b"SCALARS u float \nLOOKUP_TABLE default \n"
+    assert len(raw) == raw.index(tag) + len(tag) + nb
+    assert numpy.array_equal(rho, to_host(ss.variables["rho"].data).ravel(order="F").astype(numpy.float32))
+    assert numpy.array_equal(u, to_host(ss.variables["u"].data).ravel(order="F").astype(numpy.float32))
+    visit = open(os.path.join("TGvortex", "pyranda.visit")).read()
+    assert visit.startswith("!NBLOCKS 1 \n!TIME ") and "vis0000001/proc-000000.0000001.vtk" in visit
