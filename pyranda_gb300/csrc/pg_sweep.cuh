@@ -422,7 +422,12 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_kernel(const KParams P) {
   };
 
 #pragma unroll
-  for (int q = 0; q < 4; q++) fwd_edge(q, e[q]);
+  // implicit: the first rows' forward elimination; explicit operators store them after the window
+  // below is filled, so that an in-place call (in == out) still reads the original rows 0..3
+  if (IMPL) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) fwd_edge(q, e[q]);
+  }
 
   // interior rows 4 .. n-5: ring[s] holds v[i0 - H + s] at the start of a block
   // of kRing rows; the slot of the oldest value is refilled kRing positions ahead
@@ -441,6 +446,10 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_kernel(const KParams P) {
     for (int s2 = 0; s2 < kRing; s2++) {
       const int p = 4 - H + s2;
       ring[s2] = (p < n) ? ld(p) : RT(0);
+    }
+    if (!IMPL) {
+#pragma unroll
+      for (int q = 0; q < 4; q++) fwd_edge(q, e[q]);
     }
     // exact d8: the interior weights are iw[0] x (1, -8, 28, -56, 70, -56, 28, -8, 1), so the
     // RHS of row i is iw[0] times the 8th backward difference at i + 4, kept by a cascade of
