@@ -97,6 +97,16 @@ int pg_set_precision(pg_handle* h, int precision);
  * handle's status word reads PG_ETIMEOUT (pg_device_status), as after a
  * dense sweep whose copies or MMAs never complete.  The context stays usable. */
 int pg_wait_selftest(pg_handle* h, unsigned limit_ms, void* stream);
+/* Line solves of the banded sweeps (both precisions): mode 0 = one thread
+ * streams a whole line (forward values through a workspace field); mode 1 =
+ * split lines: each line is cut into segments of 32 points, one thread per
+ * segment, joined by the reduced system of the segments' end unknowns -- the
+ * reference's parallel solver across MPI ranks (compact_basetype.f90:171-197,
+ * pentadiagonal.f90:160-626, compact_d1.f90:242-337) run across the threads
+ * of one CTA, with the tile of lines staged in shared memory.  Lines of up to
+ * 8192 points; directions beyond that keep mode 0.  Builds its tables on the
+ * first call (allocates and synchronises). */
+int pg_set_line_split(pg_handle* h, int mode);
 /* The sweep plan of PG_DENSE / PG_AUTO: plan[op * 3 + dir] = 1 where the
  * dense kernel runs (op 0 d1, 1 d8, 2 compact filter, 3 Gaussian filter). */
 int pg_dense_plan(const pg_handle* h, int* plan);
@@ -180,6 +190,7 @@ int pg_ens_destroy(pg_ensemble* e);
 /* Total points; fills offsets[0..m] when not NULL. */
 int64_t pg_ens_points(const pg_ensemble* e, int64_t* offsets);
 int pg_ens_set_precision(pg_ensemble* e, int precision);
+int pg_ens_set_line_split(pg_ensemble* e, int mode);
 int pg_ens_spacing(const pg_ensemble* e, int member, double* patch_d, double* mesh_d);
 int pg_ens_d1(pg_ensemble* e, int dir, const double* in, double* out, void* stream);
 int pg_ens_d8(pg_ensemble* e, int dir, const double* in, double* out, void* stream);
@@ -261,8 +272,7 @@ int pg_lad_train_step(const pg_lad_model* m, const void* X, const float* T, int6
 int pg_lad_adam(float* params, float* m, float* v, const float* grad, int n, float lr, float beta1, float beta2,
                 float eps, int step, void* pbf, int nbf, void* stream);
 
-/* Allocation-free reduction.  No counterpart in the reference: parcop's
- * reductions ran through MPI on the host (pyrandaMPI.py:307-326).
+/* Allocation-free reduction.  No counterpart in the reference.
  * For callers that cannot allocate device memory (a host framework whose
  * allocator forbids cudaMalloc, or code that never creates a pg_handle and so
  * owns no workspace): same result as pg_reduce (op 0 = sum, 1 = max, 2 = min
@@ -270,9 +280,11 @@ int pg_lad_adam(float* params, float* m, float* v, const float* grad, int n, flo
  * a static device array of PG_NOALLOC_MAX_BLOCKS doubles (32 KiB) that every
  * GPU holds from library load to process exit.  n is limited to
  * PG_NOALLOC_MAX_VALUES; larger n returns PG_EBADSHAPE without launching.
- * The first call on a device looks up the array's address there; make it
- * before starting any stream capture.  All calls share the array: calls that
- * overlap on the GPU race and must be serialised by the caller. */
+ * Each call outside a stream capture looks up the array's address on the
+ * current device (so a device reset between calls is harmless); a call inside
+ * a capture reuses the address of an earlier call, so make one call on each
+ * device before capturing.  All calls share the array: calls that overlap on
+ * the GPU race and must be serialised by the caller. */
 #define PG_NOALLOC_CHUNK 8192
 #define PG_NOALLOC_MAX_BLOCKS 4096
 #define PG_NOALLOC_MAX_VALUES ((int64_t)PG_NOALLOC_CHUNK * PG_NOALLOC_MAX_BLOCKS)

@@ -67,6 +67,7 @@ SIGNATURES = [
     ("pg_device_status", I, [P, ctypes.POINTER(ctypes.c_int)]),
     ("pg_get_spacing", I, [P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     ("pg_dense_plan", I, [P, ctypes.POINTER(ctypes.c_int)]),
+    ("pg_set_line_split", I, [P, I]),
     ("pg_wait_selftest", I, [P, ctypes.c_uint, P]),
     ("pg_last_error", ctypes.c_char_p, []),
     ("pg_version", ctypes.c_char_p, []),
@@ -99,6 +100,7 @@ SIGNATURES = [
     ("pg_ens_destroy", I, [P]),
     ("pg_ens_points", ctypes.c_int64, [P, ctypes.POINTER(ctypes.c_int64)]),
     ("pg_ens_set_precision", I, [P, I]),
+    ("pg_ens_set_line_split", I, [P, I]),
     ("pg_ens_spacing", I, [P, I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     ("pg_ens_d1", I, [P, I, D, D, P]),
     ("pg_ens_d8", I, [P, I, D, D, P]),

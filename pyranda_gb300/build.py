@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libpyranda_gpu.so")
-SOURCES = ["pg_setup.cpp", "pg_sweep_f64.cu", "pg_sweep_f32.cu", "pg_elem.cu", "pg_capi.cu", "pg_noalloc.cu", "pg_dense.cu", "pg_lad.cu"]
+SOURCES = ["pg_setup.cpp", "pg_sweep_f64.cu", "pg_sweep_f32.cu", "pg_elem.cu", "pg_capi.cu", "pg_noalloc.cu", "pg_dense.cu", "pg_lad.cu", "pg_split.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

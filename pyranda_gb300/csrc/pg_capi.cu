@@ -123,6 +123,11 @@ struct Ctx {
   DenseSet dsets[OPK_COUNT][3];
   bool use_dense[OPK_COUNT][3] = {};  // the sweep plan: dense kernel or FP32 banded
   void* dense_blob = nullptr;
+  // split-line sweeps (pg_split.cu): per precision, operator and direction
+  bool split_built = false;
+  SplitSet splits[2][OPK_COUNT][3];
+  bool use_split[2][OPK_COUNT][3] = {};
+  void* split_blob = nullptr;
 };
 
 void free_ctx(Ctx& c) {
@@ -138,6 +143,7 @@ void free_ctx(Ctx& c) {
   if (c.host_out) cudaFree(c.host_out);
   if (c.stream) cudaStreamDestroy(c.stream);
   if (c.dense_blob) cudaFree(c.dense_blob);
+  if (c.split_blob) cudaFree(c.split_blob);
   c = Ctx();
 }
 
@@ -234,7 +240,6 @@ int build_ctx(Ctx& c, const std::vector<GridInfo>& g, int precision, const char*
   };
   std::vector<MemberOp> mops((size_t)M * 2 * OPK_COUNT * 3);
   auto mindex = [&](int p, int k, int d, int m) { return (((size_t)p * OPK_COUNT + k) * 3 + d) * M + m; };
-  static const int order[9] = {0, 1, 5, 6, 2, 3, 4, 7, 8};  // c1 c2 c6 c7 | c3 c4 c5 c8 | c9
   for (int m = 0; m < M; m++)
     for (int k = 0; k < OPK_COUNT; k++)
       for (int d = 0; d < 3; d++) {
@@ -243,13 +248,10 @@ int build_ctx(Ctx& c, const std::vector<GridInfo>& g, int precision, const char*
         double wsc = 0.0;
         const bool exact = integer_weights(t, iw, wsc);
         const int* rhs_i = put_i(exact ? iw : std::vector<int>((size_t)t.n * 9, 0));
-        std::vector<double> lu12((size_t)t.n * 12, 0.0);
-        for (int i = 0; i < t.n && !t.null_op; i++)
-          for (int q = 0; q < 9; q++) lu12[(size_t)i * 12 + q] = t.lu[(size_t)i * 9 + order[q]];
         for (int p = 0; p < 2; p++) {
           MemberOp& o = mops[mindex(p, k, d, m)];
           o.rhs = put(t.rhs, p == PG_FP32);
-          o.lu = put(lu12, p == PG_FP32);
+          o.lu = put(t.lu, p == PG_FP32);
           o.n = g[m].n[d];
           o.nx = g[m].n[0];
           o.ny = g[m].n[1];
@@ -585,6 +587,215 @@ int build_dense(Ctx& c, const std::vector<GridInfo>& g) {
   return PG_OK;
 }
 
+// Split-line tables of every (operator, direction) and member: segment
+// starts, per-position coefficients, the reduced system's inverse rows and
+// each segment's window of neighbouring segments (beyond which every entry of
+// the inverse is below 2^-60 of its largest), one tile list per direction.
+// Members with the same operator, extent and periodicity share one copy.
+// A direction is left without split sweeps when a member needs more than 256
+// segments or a tile more shared memory than a CTA has.
+constexpr int kSplitMaxThreads = 256;
+constexpr size_t kSplitMaxSmem = 227 * 1024;
+
+int build_split_ctx(Ctx& c, const std::vector<GridInfo>& g) {
+  if (c.split_built) return PG_OK;
+  const int M = (int)g.size();
+  struct Uniq {
+    int k, n;
+    bool per;
+    std::vector<int> start, win;
+    std::vector<double> row, G;
+    size_t off_row[2], off_G[2], off_start, off_win;
+  };
+  std::vector<Uniq> uniq;
+  std::vector<int> which((size_t)OPK_COUNT * 3 * M, -1);
+  bool dir_ok[OPK_COUNT][3];
+  for (int k = 0; k < OPK_COUNT; k++)
+    for (int d = 0; d < 3; d++) {
+      dir_ok[k][d] = !c.ops[PG_FP64][k][d].null_op;
+      for (int m = 0; m < M && dir_ok[k][d]; m++) {
+        const OpTables& t = g[m].tab[k][d];
+        const int n = t.n;
+        if (n / kSplitSeg > kSplitMaxThreads) {
+          dir_ok[k][d] = false;
+          break;
+        }
+        int u = -1;
+        for (size_t q = 0; q < uniq.size() && u < 0; q++)
+          if (uniq[q].k == k && uniq[q].n == n && uniq[q].per == t.periodic) u = (int)q;
+        if (u < 0) {
+          Uniq e;
+          e.k = k;
+          e.n = n;
+          e.per = t.periodic;
+          const int rc = build_split(t.lhs, n, t.periodic, e.start, e.row, e.G);
+          if (rc) return rc;
+          const int S = (int)e.start.size() - 1, T = 4 * S;
+          e.win.assign((size_t)2 * S, 0);
+          if (!t.implicit) {
+            e.row.clear();
+            e.G.clear();
+          } else {
+            double gmax = 0.0;
+            for (double v : e.G) gmax = std::max(gmax, std::fabs(v));
+            const double thr = std::ldexp(gmax, -60);
+            for (int j = 0; j < S; j++) {
+              int w = 0;
+              for (int js = 0; js < S; js++) {
+                double mx = 0.0;
+                for (int q = 0; q < 4; q++)
+                  for (int cc = 0; cc < 4; cc++) mx = std::max(mx, std::fabs(e.G[((size_t)j * 4 + q) * T + 4 * js + cc]));
+                if (mx <= thr) continue;
+                int dist = std::abs(js - j);
+                if (t.periodic) dist = std::min(dist, S - dist);
+                w = std::max(w, dist);
+              }
+              int first, count;
+              if (t.periodic) {
+                if (2 * w + 1 >= S) {
+                  first = 0;
+                  count = S;
+                } else {
+                  first = ((j - w) % S + S) % S;
+                  count = 2 * w + 1;
+                }
+              } else {
+                first = std::max(0, j - w);
+                count = std::min(S - 1, j + w) - first + 1;
+              }
+              e.win[(size_t)2 * j] = first;
+              e.win[(size_t)2 * j + 1] = count;
+            }
+          }
+          uniq.push_back(std::move(e));
+          u = (int)uniq.size() - 1;
+        }
+        which[((size_t)k * 3 + d) * M + m] = u;
+      }
+    }
+  // blob: [tables][SplitOp arrays 2 x OPK x 3 x M][tile arrays]
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  size_t total = 0;
+  for (auto& u : uniq) {
+    u.off_row[0] = total;
+    total = al(total + u.row.size() * 8);
+    u.off_row[1] = total;
+    total = al(total + u.row.size() * 4);
+    u.off_G[0] = total;
+    total = al(total + u.G.size() * 8);
+    u.off_G[1] = total;
+    total = al(total + u.G.size() * 4);
+    u.off_start = total;
+    total = al(total + u.start.size() * 4);
+    u.off_win = total;
+    total = al(total + u.win.size() * 4);
+  }
+  std::vector<SplitTile> tiles;
+  size_t tile_at[OPK_COUNT][3] = {};
+  int tile_n[OPK_COUNT][3] = {};
+  size_t sm[3][OPK_COUNT][3] = {};  // fp32, fp64, mixed
+  for (int k = 0; k < OPK_COUNT; k++)
+    for (int d = 0; d < 3; d++) {
+      if (!dir_ok[k][d]) continue;
+      tile_at[k][d] = tiles.size();
+      for (int m = 0; m < M; m++) {
+        const Uniq& u = uniq[which[((size_t)k * 3 + d) * M + m]];
+        const int S = (int)u.start.size() - 1;
+        const int nl = std::max(1, kSplitMaxThreads / S);
+        const long long lines = g[m].npts / u.n;
+        for (long long l0 = 0; l0 < lines; l0 += nl)
+          tiles.push_back(SplitTile{m, (int)l0, (int)std::min<long long>(nl, lines - l0), 0});
+        sm[0][k][d] = std::max(sm[0][k][d], split_smem_bytes(PG_FP32, false, u.n, S, nl));
+        sm[1][k][d] = std::max(sm[1][k][d], split_smem_bytes(PG_FP64, false, u.n, S, nl));
+        sm[2][k][d] = std::max(sm[2][k][d], split_smem_bytes(PG_FP32, true, u.n, S, nl));
+      }
+      tile_n[k][d] = (int)(tiles.size() - tile_at[k][d]);
+    }
+  const size_t ops_at = al(total);
+  const size_t tiles_at = al(ops_at + sizeof(SplitOp) * (size_t)2 * OPK_COUNT * 3 * M);
+  total = tiles_at + tiles.size() * sizeof(SplitTile);
+  cudaError_t e = cudaMalloc(&c.split_blob, std::max(total, (size_t)256));
+  if (e != cudaSuccess) {
+    set_error("split tables: cudaMalloc: %s", cudaGetErrorString(e));
+    return PG_ENOMEM;
+  }
+  unsigned char* base = (unsigned char*)c.split_blob;
+  std::vector<unsigned char> host(std::max(total, (size_t)256), 0);
+  for (auto& u : uniq) {
+    for (size_t i = 0; i < u.row.size(); i++) {
+      std::memcpy(&host[u.off_row[0] + i * 8], &u.row[i], 8);
+      const float f = (float)u.row[i];
+      std::memcpy(&host[u.off_row[1] + i * 4], &f, 4);
+    }
+    for (size_t i = 0; i < u.G.size(); i++) {
+      std::memcpy(&host[u.off_G[0] + i * 8], &u.G[i], 8);
+      const float f = (float)u.G[i];
+      std::memcpy(&host[u.off_G[1] + i * 4], &f, 4);
+    }
+    std::memcpy(&host[u.off_start], u.start.data(), u.start.size() * 4);
+    std::memcpy(&host[u.off_win], u.win.data(), u.win.size() * 4);
+  }
+  std::vector<SplitOp> sops((size_t)2 * OPK_COUNT * 3 * M);
+  auto sidx = [&](int p, int k, int d, int m) { return (((size_t)p * OPK_COUNT + k) * 3 + d) * M + m; };
+  for (int p = 0; p < 2; p++)
+    for (int k = 0; k < OPK_COUNT; k++)
+      for (int d = 0; d < 3; d++) {
+        if (!dir_ok[k][d]) continue;
+        for (int m = 0; m < M; m++) {
+          const Uniq& u = uniq[which[((size_t)k * 3 + d) * M + m]];
+          SplitOp& o = sops[sidx(p, k, d, m)];
+          o.row = base + u.off_row[p];
+          o.G = base + u.off_G[p];
+          o.start = reinterpret_cast<const int*>(base + u.off_start);
+          o.win = reinterpret_cast<const int*>(base + u.off_win);
+          o.S = (int)u.start.size() - 1;
+          o.pad = 0;
+        }
+      }
+  std::memcpy(&host[ops_at], sops.data(), sops.size() * sizeof(SplitOp));
+  if (!tiles.empty()) std::memcpy(&host[tiles_at], tiles.data(), tiles.size() * sizeof(SplitTile));
+  e = cudaMemcpy(c.split_blob, host.data(), host.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    set_error("split tables: %s", cudaGetErrorString(e));
+    return PG_ECUDA;
+  }
+  for (int p = 0; p < 2; p++)
+    for (int k = 0; k < OPK_COUNT; k++)
+      for (int d = 0; d < 3; d++) {
+        SplitSet& ss = c.splits[p][k][d];
+        ss = SplitSet();
+        if (!dir_ok[k][d]) continue;
+        ss.sops = reinterpret_cast<const SplitOp*>(base + ops_at) + sidx(p, k, d, 0);
+        ss.tiles = reinterpret_cast<const SplitTile*>(base + tiles_at) + tile_at[k][d];
+        ss.ntiles = tile_n[k][d];
+        ss.smem32 = sm[0][k][d];
+        ss.smem64 = sm[1][k][d];
+        ss.smem_mixed = sm[2][k][d];
+        const bool exact = (p == PG_FP32) && k == OPK_D8 && c.ops[PG_FP32][k][d].exact;
+        const size_t need = (p == PG_FP64) ? ss.smem64 : (exact ? ss.smem_mixed : ss.smem32);
+        ss.ok = need <= kSplitMaxSmem;
+      }
+  c.split_built = true;
+  return PG_OK;
+}
+
+// Split-line sweeps on (mode 1) or off (mode 0) for every operator and
+// direction where they are built, in both precisions.
+int set_line_split(Ctx& c, const std::vector<GridInfo>& g, int mode) {
+  if (mode != 0 && mode != 1) {
+    set_error("line split mode must be 0 or 1, not %d", mode);
+    return PG_EINVAL;
+  }
+  if (mode == 1) {
+    const int rc = build_split_ctx(c, g);
+    if (rc) return rc;
+  }
+  for (int p = 0; p < 2; p++)
+    for (int k = 0; k < OPK_COUNT; k++)
+      for (int d = 0; d < 3; d++) c.use_split[p][k][d] = (mode == 1) && c.splits[p][k][d].ok;
+  return PG_OK;
+}
+
 int dense_sweep(Ctx& c, int kind, int dir, const double* in, double* out, int epi, int scale_pow, void* st,
                 bool emax_ready);
 
@@ -683,6 +894,14 @@ int dense_sweep(Ctx& c, int kind, int dir, const double* in, double* out, int ep
 int sweep(Ctx& c, int kind, int dir, const double* in, double* out, int epi, int scale_pow, void* st,
           bool emax_ready = false) {
   if (c.dense && c.use_dense[kind][dir]) return dense_sweep(c, kind, dir, in, out, epi, scale_pow, st, emax_ready);
+  if (c.use_split[c.precision][kind][dir]) {
+    const OpRef& op = c.ops[c.precision][kind][dir];
+    if (c.precision == PG_FP32 && kind == OPK_D8 && op.exact && !emax_ready) {
+      const int rc = launch_max_exponent(in, c.moff, c.nmem, c.emax, st);
+      if (rc) return rc;
+    }
+    return launch_split(c.precision, op, c.splits[c.precision][kind][dir], in, out, dir, epi, scale_pow, c.emax, st);
+  }
   SweepLaunch s{in, out, c.work2, &c.ops[c.precision][kind][dir], dir, epi, scale_pow, c.emax, c.moff, emax_ready};
   return launch_sweep(c.precision, s, st);
 }
@@ -877,6 +1096,11 @@ int pg_set_precision(pg_handle* h, int precision) {
 int pg_wait_selftest(pg_handle* h, unsigned limit_ms, void* stream) {
   if (!h || limit_ms == 0 || limit_ms > 10000) return PG_EINVAL;
   return launch_wait_selftest(h->c.status, limit_ms, stream);
+}
+
+int pg_set_line_split(pg_handle* h, int mode) {
+  if (!h) return PG_EINVAL;
+  return set_line_split(h->c, std::vector<GridInfo>{h->g}, mode);
 }
 
 int pg_dense_plan(const pg_handle* h, int* plan) {
@@ -1090,6 +1314,11 @@ int64_t pg_ens_points(const pg_ensemble* e, int64_t* offsets) {
     offsets[e->g.size()] = o;
   }
   return e->c.npts;
+}
+
+int pg_ens_set_line_split(pg_ensemble* e, int mode) {
+  if (!e) return PG_EINVAL;
+  return set_line_split(e->c, e->g, mode);
 }
 
 int pg_ens_set_precision(pg_ensemble* e, int precision) {

@@ -78,8 +78,8 @@ __device__ __forceinline__ double combine(double a, double b) {
 template <int OP>
 __device__ __forceinline__ double identity() {
   if (OP == 0) return 0.0;
-  if (OP == 1) return -DBL_MAX;
-  return DBL_MAX;
+  if (OP == 1) return -INFINITY;  // max of an all -inf input is -inf, as in numpy
+  return INFINITY;
 }
 
 template <int OP>
@@ -134,7 +134,7 @@ __global__ void courant_partial(const double* __restrict__ u, const double* __re
                                 const double* __restrict__ w, const double* __restrict__ c, double vconst,
                                 double wconst, double r1, double r2, double r3, double rgl, int64_t n,
                                 double* __restrict__ partial) {
-  double acc = -DBL_MAX;
+  double acc = -INFINITY;
   bool nan = false;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double vv = v ? v[i] : vconst;
@@ -218,10 +218,10 @@ __global__ void diff_exact_partial(const double* __restrict__ bulk, const double
   const bool bexact = partial[gridDim.x + blockIdx.x] != 0.0;
   __syncthreads();  // every thread has read the pass-1 values before thread 0 overwrites them
   if (m == m && !bexact && !(bmin <= (double)lim)) {
-    if (threadIdx.x == 0) partial[blockIdx.x] = DBL_MAX;
+    if (threadIdx.x == 0) partial[blockIdx.x] = INFINITY;
     return;
   }
-  double acc = DBL_MAX;
+  double acc = INFINITY;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double r = rho[i], b = bulk[i];
     const DiffEst d = diff_estimate(r, b, gl2);

@@ -17,11 +17,18 @@ struct OpTables {
   int kind = 0, n = 0;
   bool periodic = false, implicit = false, addback = false, null_op = true;
   std::vector<double> rhs;  // n x 9 per-row RHS weights
-  std::vector<double> lu;   // n x 9 per-row solve coefficients
+  std::vector<double> lu;   // n x 12 per-row solve coefficients (pg_setup.cpp solve_tables)
   std::vector<double> lhs;  // n x 5 LHS band (a, b, diag, c, d) before factorisation
 };
 
 int build_operator(int kind, int n, bool periodic, double scale, OpTables& t);
+
+// Split-line (reduced-system) solve tables of one line's LHS band (n x 5):
+// segment starts (S + 1), per-position rows (n x 12) and the per-segment rows
+// of the reduced system's inverse (S x 4 x 4S).  pg_setup.cpp.
+constexpr int kSplitSeg = 32;  // points per segment (the last takes the remainder)
+int build_split(const std::vector<double>& band, int n, bool periodic, std::vector<int>& start,
+                std::vector<double>& row, std::vector<double>& G);
 
 // Epilogues fused into the store of a sweep.
 enum {
@@ -38,7 +45,7 @@ enum {
 // the lines of every member.
 struct MemberOp {
   const void* rhs;  // n x 9 per-row RHS weights (T)
-  const void* lu;   // n x 12 per-row solve coefficients (T)
+  const void* lu;   // n x 12 per-row solve coefficients (T), layout of pg_setup.cpp solve_tables
   int n;            // points per line
   int nx, ny;       // grid extents (to decode a line index)
   int pad;
@@ -88,6 +95,35 @@ int launch_sweep(int precision, const SweepLaunch& s, void* stream);
 // members' exponents (launch_max_exponent); nmax = the longest member line.
 int launch_d8_rhs(const OpRef& op, const double* in, double* rhs, int dir, const int* emax, int nmax,
                   void* stream);
+
+// Split-line sweeps (pg_split.cu): one member's tables along one direction
+// (device memory; built by pg_setup.cpp build_split).
+struct SplitOp {
+  const void* row;   // n x 12 per-position coefficients (T)
+  const void* G;     // S x 4 x 4S rows of the reduced system's inverse (T)
+  const int* start;  // S + 1 segment starts
+  const int* win;    // per segment: first segment of its reduced-solve window, segments in the window
+  int S;
+  int pad;
+};
+// One CTA's lines: [line0, line0 + nlines) of member op, nlines * S <= 256.
+struct SplitTile {
+  int op;
+  int line0;
+  int nlines;
+  int pad;
+};
+struct SplitSet {
+  const SplitOp* sops = nullptr;  // per member (this precision's tables)
+  const SplitTile* tiles = nullptr;
+  int ntiles = 0;
+  bool ok = false;
+  size_t smem32 = 0, smem64 = 0, smem_mixed = 0;  // dynamic shared memory of the FP32 / FP64 / exact-d8 kernels
+};
+// Shared memory of one split tile (precision PG_FP32 / PG_FP64; exact: FP32 d8 with the raw FP64 values).
+size_t split_smem_bytes(int precision, bool exact, int n, int S, int nl);
+int launch_split(int precision, const OpRef& op, const SplitSet& ss, const double* in, double* out, int dir, int epi,
+                 int scale_pow, const int* emax, void* stream);
 
 // Dense operator of one member along one direction (device memory): the
 // difference form D' of D (OUT = D' w, w_k = v_k - v_{k-1}) split into TF32

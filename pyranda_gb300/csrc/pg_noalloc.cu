@@ -12,9 +12,10 @@
 // Rules of use (also stated in include/pyranda_gpu.h):
 //  - n must not exceed PG_NOALLOC_MAX_VALUES; larger inputs are rejected with
 //    PG_EBADSHAPE before anything is launched.
-//  - The first call on a device looks up the array's device address on that
-//    device (cudaGetSymbolAddress); make that first call before any stream
-//    capture is started.
+//  - Every call outside a stream capture looks up the array's device address
+//    on the current device (cudaGetSymbolAddress), so a device reset between
+//    calls is harmless; a call inside a capture reuses the address found by an
+//    earlier call, so make one call on each device before capturing.
 //  - All calls in the process share the one array.  Two calls whose kernels
 //    overlap on the GPU (for example on two streams) race on it; serialise
 //    them.  The array keeps the last call's partials; nothing in it has to
@@ -48,8 +49,8 @@ __device__ __forceinline__ double na_combine(double a, double b) {
 template <int OP>
 __device__ __forceinline__ double na_identity() {
   if (OP == 0) return 0.0;
-  if (OP == 1) return -DBL_MAX;
-  return DBL_MAX;
+  if (OP == 1) return -INFINITY;  // max of an all -inf input is -inf, as in numpy
+  return INFINITY;
 }
 
 template <int OP>
@@ -98,12 +99,16 @@ __global__ void na_final(const double* __restrict__ partials, int np, double* __
   if (threadIdx.x == 0) *out = anynan ? NAN : acc;
 }
 
-// Device address of the scratch, looked up once per device.
+// Device address of the scratch on each device.  It is looked up again on
+// every call made outside a stream capture, so a device reset between calls
+// (which reloads the module, possibly at another address) is picked up; a
+// call during a capture uses the address found by an earlier call, because
+// the lookup itself may not be issued while a capture is active.
 constexpr int kMaxDevices = 64;
 double* g_scratch_ptr[kMaxDevices] = {nullptr};
 std::mutex g_scratch_mu;
 
-int scratch_for_current_device(double** out) {
+int scratch_for_current_device(cudaStream_t stream, double** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) {
@@ -114,8 +119,12 @@ int scratch_for_current_device(double** out) {
     set_error("pg_reduce_noalloc: device %d beyond the %d supported", dev, kMaxDevices);
     return PG_EINVAL;
   }
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  const cudaError_t qe = cudaStreamIsCapturing(stream, &cs);
+  if (qe != cudaSuccess) (void)cudaGetLastError();  // an implicit capture of the legacy stream: treat as capturing
+  const bool capturing = (qe != cudaSuccess) || cs != cudaStreamCaptureStatusNone;
   std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (!g_scratch_ptr[dev]) {
+  if (!capturing) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_partials);
     if (e != cudaSuccess || !p) {
@@ -123,6 +132,10 @@ int scratch_for_current_device(double** out) {
       return PG_ECUDA;
     }
     g_scratch_ptr[dev] = static_cast<double*>(p);
+  } else if (!g_scratch_ptr[dev]) {
+    set_error("pg_reduce_noalloc: first call on device %d made during a stream capture; "
+              "call it once before capturing", dev);
+    return PG_EINVAL;
   }
   *out = g_scratch_ptr[dev];
   return PG_OK;
@@ -143,7 +156,7 @@ extern "C" int pg_reduce_noalloc(int op, const double* in, int64_t n, double* ou
     return PG_EBADSHAPE;
   }
   double* partials = nullptr;
-  int rc = scratch_for_current_device(&partials);
+  int rc = scratch_for_current_device((cudaStream_t)stream, &partials);
   if (rc != PG_OK) return rc;
   const int nb = (int)((n + kNaChunk - 1) / kNaChunk);  // <= kNaMaxBlocks by the check above
   cudaStream_t s = (cudaStream_t)stream;

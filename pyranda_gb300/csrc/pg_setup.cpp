@@ -6,11 +6,14 @@
 //     c10d2 :358-428, e4d4 :430-513, c10d8 :515-621, c8ff8 :713-835,
 //     cgfs4 :1387-1476), boundary code 0 (one-sided closures) and periodic;
 //   - the global LHS/RHS assembly of compact_basetype.f90:124-148 (np = 1);
-//   - the LU factorisations bpentLUD1 / ppentLUD1 of pentadiagonal.f90:18-135.
-// The factorisation steps are kept as in the reference (the kernels replay the
-// matching substitutions), so results agree with the reference to rounding.
+//   - the solve tables of the sweeps: a Crout band factorisation, and for
+//     periodic lines a Schur-complement (Sherman-Morrison-Woodbury) treatment
+//     of the wrap (the reference factors the same matrices with its own
+//     bordered LU, pentadiagonal.f90:18-135; any stable factorisation gives
+//     the same operator to rounding).
 #include "pg_internal.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -193,96 +196,291 @@ Stencil stencil_gf() {  // cgfs4, explicit 9-point Gaussian
   return s;
 }
 
-// LU factorisation of the non-periodic pentadiagonal matrix, band columns
-// 0..4 = (a, b, diag, c, d); the diagonal is stored inverted
-// (bpentLUD1, pentadiagonal.f90:18-39).
-void factor_banded(std::vector<double>& c, int n) {
-  auto C = [&](int i, int k) -> double& { return c[(size_t)i * 9 + k]; };
-  for (int i = 0; i < n - 2; i++) {
-    C(i + 1, 1) /= C(i, 2);
-    C(i + 1, 2) -= C(i, 3) * C(i + 1, 1);
-    C(i + 1, 3) -= C(i, 4) * C(i + 1, 1);
-    C(i + 2, 0) /= C(i, 2);
-    C(i + 2, 1) -= C(i, 3) * C(i + 2, 0);
-    C(i + 2, 2) -= C(i, 4) * C(i + 2, 0);
+// ---------------------------------------------------------------------------
+// Solve tables.  The LHS of every implicit operator is a pentadiagonal matrix
+// A (band rows (a, b, diag, c, d) = A[i][i-2 .. i+2]; periodic lines wrap the
+// column index).  The sweeps solve A x = r in one forward and one backward
+// pass per line, from these per-row coefficients:
+//
+//  * non-periodic lines: the Crout factorisation A = L U, L lower triangular
+//    with two subdiagonals, U unit upper triangular with two superdiagonals.
+//    Forward:  z_i = rho_i r_i - alpha_i z_{i-1} - beta_i z_{i-2}
+//              (rho = 1 / L_ii, alpha = L_i,i-1 rho, beta = L_i,i-2 rho);
+//    backward: x_i = z_i - u1_i x_{i+1} - u2_i x_{i+2}.
+//  * periodic lines: the wrap couples the first and the last unknowns.  The
+//    last two unknowns x_B = (x_{n-2}, x_{n-1}) are split off; the other
+//    m = n-2 form a plain banded block A_II = L U (the wrap only reaches
+//    A_IB, A_BI).  Eliminating x_I (the Schur complement on x_B, i.e. the
+//    Sherman-Morrison-Woodbury form of the rank-4 wrap correction):
+//       F = L^-1 A_IB (m x 2),  G = A_BI U^-1 (2 x m),  S = A_BB - G F (2 x 2)
+//       forward  z_I = L^-1 r_I, accumulating t = G z_I
+//       x_B = S^-1 (r_B - t)
+//       backward x_i = z_i - u1_i x_{i+1} - u2_i x_{i+2} - F_i0 x_{n-2} - F_i1 x_{n-1}
+//    so the wrap costs two fused multiply-adds per point in each pass and the
+//    line is still read once forward and once backward.
+// Per-row layout (12 values, two 16-byte groups the sweeps load at once):
+//   [0] rho  [1] alpha  [2] beta  [3] G_0i | [4] u1  [5] u2  [6] F_i0  [7] F_i1 | [8] G_1i
+// and for periodic lines row n-2 holds S^-1 = (s00, s01, s10, s11) in [0..3].
+// Entries a row does not use are zero, so the first and last rows need no
+// special cases in the sweeps.
+constexpr int kSolveStride = 12;
+
+// Crout factorisation of an m x m matrix of lower and upper bandwidth 2
+// (entry(i, j) gives A_ij for |i - j| <= 2), without pivoting: every LHS here
+// is diagonally dominant.  Lw[i*3 + k] = L_i,i-k (k = 0..2), Uw[i*3 + k] =
+// U_i,i+k (k = 1, 2).
+template <class Entry>
+bool crout_banded(int m, Entry entry, std::vector<double>& Lw, std::vector<double>& Uw) {
+  Lw.assign((size_t)m * 3, 0.0);
+  Uw.assign((size_t)m * 3, 0.0);
+  auto Lij = [&](int i, int j) -> double { return (j <= i && i - j <= 2 && j >= 0) ? Lw[(size_t)i * 3 + (i - j)] : 0.0; };
+  auto Uij = [&](int i, int j) -> double {
+    if (i == j) return 1.0;
+    return (j > i && j - i <= 2 && j < m) ? Uw[(size_t)i * 3 + (j - i)] : 0.0;
+  };
+  for (int i = 0; i < m; i++) {
+    for (int j = std::max(0, i - 2); j <= i; j++) {  // row i of L
+      double s = entry(i, j);
+      for (int k = std::max(0, std::max(i, j) - 2); k < j; k++) s -= Lij(i, k) * Uij(k, j);
+      Lw[(size_t)i * 3 + (i - j)] = s;
+    }
+    const double lii = Lw[(size_t)i * 3];
+    if (lii == 0.0 || !std::isfinite(lii)) return false;
+    for (int j = i + 1; j <= std::min(m - 1, i + 2); j++) {  // row i of U
+      double s = entry(i, j);
+      for (int k = std::max(0, j - 2); k < i; k++) s -= Lij(i, k) * Uij(k, j);
+      Uw[(size_t)i * 3 + (j - i)] = s / lii;
+    }
   }
-  C(n - 1, 1) /= C(n - 2, 2);
-  C(n - 1, 2) -= C(n - 2, 3) * C(n - 1, 1);
-  for (int i = 0; i < n; i++) C(i, 2) = 1.0 / C(i, 2);
+  return true;
 }
 
-// Bordered LU of the cyclic pentadiagonal matrix (ppentLUD1,
-// pentadiagonal.f90:64-135).  Columns 5,6 hold the multipliers of the last two
-// rows, columns 7,8 the fill of the last two columns.  0-based: row r here is
-// Fortran row r+1, column k is Fortran column k+1.
-void factor_cyclic(std::vector<double>& c, int N) {
-  auto C = [&](int i1, int k1) -> double& { return c[(size_t)(i1 - 1) * 9 + (k1 - 1)]; };
-  C(1, 8) = C(1, 1);
-  C(1, 9) = C(1, 2);
-  C(1, 3) = 1.0 / C(1, 3);
-  C(1, 6) = C(N - 1, 5) * C(1, 3);
-  C(1, 7) = C(N, 4) * C(1, 3);
-  C(2, 2) = C(2, 2) * C(1, 3);
-  C(2, 3) = C(2, 3) - C(2, 2) * C(1, 4);
-  C(2, 4) = C(2, 4) - C(2, 2) * C(1, 5);
-  C(2, 8) = -C(2, 2) * C(1, 8);
-  C(2, 9) = C(2, 1) - C(2, 2) * C(1, 9);
-  C(2, 3) = 1.0 / C(2, 3);
-  C(2, 6) = -C(1, 6) * C(1, 4) * C(2, 3);
-  C(2, 7) = (C(N, 5) - C(1, 7) * C(1, 4)) * C(2, 3);
-  for (int k = 3; k <= N - 4; k++) {
-    C(k, 1) = C(k, 1) * C(k - 2, 3);
-    C(k, 2) = (C(k, 2) - C(k, 1) * C(k - 2, 4)) * C(k - 1, 3);
-    C(k, 3) = C(k, 3) - (C(k, 2) * C(k - 1, 4) + C(k, 1) * C(k - 2, 5));
-    C(k, 4) = C(k, 4) - C(k, 2) * C(k - 1, 5);
-    C(k, 8) = -(C(k, 2) * C(k - 1, 8) + C(k, 1) * C(k - 2, 8));
-    C(k, 9) = -(C(k, 2) * C(k - 1, 9) + C(k, 1) * C(k - 2, 9));
-    C(k, 3) = 1.0 / C(k, 3);
-    C(k, 6) = -(C(k - 1, 6) * C(k - 1, 4) + C(k - 2, 6) * C(k - 2, 5)) * C(k, 3);
-    C(k, 7) = -(C(k - 1, 7) * C(k - 1, 4) + C(k - 2, 7) * C(k - 2, 5)) * C(k, 3);
+// The per-row solve coefficients of one line's LHS (band rows n x 5).
+bool solve_tables(const std::vector<double>& band, int n, bool periodic, std::vector<double>& out) {
+  out.assign((size_t)n * kSolveStride, 0.0);
+  // A_ij of the full line matrix (periodic: columns taken modulo n)
+  auto A = [&](int i, int j) -> double {
+    double s = 0.0;
+    for (int l = 0; l < 5; l++) {
+      int c = i + l - 2;
+      if (periodic) c = ((c % n) + n) % n;
+      if (c == j) s += band[(size_t)i * 5 + l];
+    }
+    return s;
+  };
+  const int m = periodic ? n - 2 : n;
+  std::vector<double> Lw, Uw;
+  if (!crout_banded(m, A, Lw, Uw)) return false;
+  auto row = [&](int i) { return &out[(size_t)i * kSolveStride]; };
+  for (int i = 0; i < m; i++) {
+    double* r = row(i);
+    const double rho = 1.0 / Lw[(size_t)i * 3];
+    r[0] = rho;
+    r[1] = Lw[(size_t)i * 3 + 1] * rho;
+    r[2] = Lw[(size_t)i * 3 + 2] * rho;
+    r[4] = Uw[(size_t)i * 3 + 1];
+    r[5] = Uw[(size_t)i * 3 + 2];
   }
-  int k = N - 3;
-  C(k, 1) = C(k, 1) * C(k - 2, 3);
-  C(k, 2) = (C(k, 2) - C(k, 1) * C(k - 2, 4)) * C(k - 1, 3);
-  C(k, 3) = C(k, 3) - (C(k, 2) * C(k - 1, 4) + C(k, 1) * C(k - 2, 5));
-  C(k, 4) = C(k, 4) - C(k, 2) * C(k - 1, 5);
-  C(k, 8) = C(k, 5) - (C(k, 2) * C(k - 1, 8) + C(k, 1) * C(k - 2, 8));
-  C(k, 9) = -(C(k, 2) * C(k - 1, 9) + C(k, 1) * C(k - 2, 9));
-  C(k, 3) = 1.0 / C(k, 3);
-  C(k, 6) = (C(N - 1, 1) - (C(k - 1, 6) * C(k - 1, 4) + C(k - 2, 6) * C(k - 2, 5))) * C(k, 3);
-  C(k, 7) = -(C(k - 1, 7) * C(k - 1, 4) + C(k - 2, 7) * C(k - 2, 5)) * C(k, 3);
-  k = N - 2;
-  C(k, 1) = C(k, 1) * C(k - 2, 3);
-  C(k, 2) = (C(k, 2) - C(k, 1) * C(k - 2, 4)) * C(k - 1, 3);
-  C(k, 3) = C(k, 3) - (C(k, 2) * C(k - 1, 4) + C(k, 1) * C(k - 2, 5));
-  C(k, 8) = C(k, 4) - (C(k, 2) * C(k - 1, 8) + C(k, 1) * C(k - 2, 8));
-  C(k, 9) = C(k, 5) - (C(k, 2) * C(k - 1, 9) + C(k, 1) * C(k - 2, 9));
-  C(k, 3) = 1.0 / C(k, 3);
-  C(k, 6) = (C(N - 1, 2) - C(k - 1, 6) * C(k - 1, 4) - C(k - 2, 6) * C(k - 2, 5)) * C(k, 3);
-  C(k, 7) = (C(N, 1) - C(k - 1, 7) * C(k - 1, 4) - C(k - 2, 7) * C(k - 2, 5)) * C(k, 3);
-  for (int q = 1; q <= N - 2; q++) {
-    C(N - 1, 3) = C(N - 1, 3) - C(q, 6) * C(q, 8);
-    C(N - 1, 4) = C(N - 1, 4) - C(q, 6) * C(q, 9);
+  if (!periodic) return true;
+  // F = L^-1 A_IB: forward substitution of the two border columns
+  std::vector<double> F((size_t)m * 2, 0.0), G((size_t)2 * m, 0.0);
+  for (int c = 0; c < 2; c++)
+    for (int i = 0; i < m; i++) {
+      double s = A(i, m + c);
+      if (i >= 1) s -= Lw[(size_t)i * 3 + 1] * F[(size_t)(i - 1) * 2 + c];
+      if (i >= 2) s -= Lw[(size_t)i * 3 + 2] * F[(size_t)(i - 2) * 2 + c];
+      F[(size_t)i * 2 + c] = s / Lw[(size_t)i * 3];
+    }
+  // G = A_BI U^-1: G U = A_BI, solved column by column (U unit upper)
+  for (int b = 0; b < 2; b++)
+    for (int j = 0; j < m; j++) {
+      double s = A(m + b, j);
+      if (j >= 1) s -= G[(size_t)b * m + j - 1] * Uw[(size_t)(j - 1) * 3 + 1];
+      if (j >= 2) s -= G[(size_t)b * m + j - 2] * Uw[(size_t)(j - 2) * 3 + 2];
+      G[(size_t)b * m + j] = s;
+    }
+  // S = A_BB - G F and its inverse
+  double S[2][2];
+  for (int b = 0; b < 2; b++)
+    for (int c = 0; c < 2; c++) {
+      double s = A(m + b, m + c);
+      for (int i = 0; i < m; i++) s -= G[(size_t)b * m + i] * F[(size_t)i * 2 + c];
+      S[b][c] = s;
+    }
+  const double det = S[0][0] * S[1][1] - S[0][1] * S[1][0];
+  if (det == 0.0 || !std::isfinite(det)) return false;
+  for (int i = 0; i < m; i++) {
+    double* r = row(i);
+    r[3] = G[i];
+    r[8] = G[(size_t)m + i];
+    r[6] = F[(size_t)i * 2];
+    r[7] = F[(size_t)i * 2 + 1];
   }
-  C(N - 1, 9) = C(N - 1, 4);
-  for (int q = 1; q <= N - 2; q++) C(N, 2) = C(N, 2) - C(q, 7) * C(q, 8);
-  C(N - 1, 3) = 1.0 / C(N - 1, 3);
-  C(N - 1, 7) = C(N, 2) * C(N - 1, 3);
-  for (int q = 1; q <= N - 1; q++) C(N, 3) = C(N, 3) - C(q, 7) * C(q, 9);
-  C(N, 3) = 1.0 / C(N, 3);
+  double* s = row(m);
+  s[0] = S[1][1] / det;
+  s[1] = -S[0][1] / det;
+  s[2] = -S[1][0] / det;
+  s[3] = S[0][0] / det;
+  return true;
+}
+
+// Gauss-Jordan inverse with partial pivoting of a small dense matrix (row
+// major k x k, FP64); false when singular.
+bool invert_small(std::vector<double> a, int k, std::vector<double>& inv) {
+  inv.assign((size_t)k * k, 0.0);
+  for (int i = 0; i < k; i++) inv[(size_t)i * k + i] = 1.0;
+  for (int c = 0; c < k; c++) {
+    int piv = c;
+    for (int r = c + 1; r < k; r++)
+      if (std::fabs(a[(size_t)r * k + c]) > std::fabs(a[(size_t)piv * k + c])) piv = r;
+    const double d = a[(size_t)piv * k + c];
+    if (d == 0.0 || !std::isfinite(d)) return false;
+    if (piv != c)
+      for (int j = 0; j < k; j++) {
+        std::swap(a[(size_t)piv * k + j], a[(size_t)c * k + j]);
+        std::swap(inv[(size_t)piv * k + j], inv[(size_t)c * k + j]);
+      }
+    const double rd = 1.0 / d;
+    for (int j = 0; j < k; j++) {
+      a[(size_t)c * k + j] *= rd;
+      inv[(size_t)c * k + j] *= rd;
+    }
+    for (int r = 0; r < k; r++) {
+      if (r == c) continue;
+      const double f = a[(size_t)r * k + c];
+      if (f == 0.0) continue;
+      for (int j = 0; j < k; j++) {
+        a[(size_t)r * k + j] -= f * a[(size_t)c * k + j];
+        inv[(size_t)r * k + j] -= f * inv[(size_t)c * k + j];
+      }
+    }
+  }
+  return true;
 }
 
 }  // namespace
+
+// Split-line tables: the reduced-system form of the line solve (the
+// reference's parallel solver, compact_basetype.f90:171-197 with
+// pentadiagonal.f90:160-626 and compact_d1.f90:242-337, splits a line
+// across MPI ranks the same way).  The line is cut into S segments of
+// kSplitSeg points (the last one takes the remainder, up to 2 kSplitSeg - 1).
+// Segment j = rows [a, b) couples to its neighbours only through its first
+// two and last two rows:
+//   A_jj x_j + C_j xbot_{j-1} + B_j xtop_{j+1} = r_j
+// (xbot = the last two unknowns of the segment before, xtop = the first two
+// of the segment after; periodic lines wrap, one-sided lines have no
+// coupling at their ends).  With y_j = A_jj^-1 r_j and the spikes
+// W_j = A_jj^-1 C_j, V_j = A_jj^-1 B_j (L x 2 each):
+//   x_j = y_j - W_j xbot_{j-1} - V_j xtop_{j+1}.
+// Taking the tip rows (0, 1, L-2, L-1) of every segment gives the reduced
+// system R t = y_tips over the 4S tip unknowns; R is the same for every line
+// of a grid, so its inverse is formed here once, and each segment keeps the
+// four rows of R^-1 that give its xbot_{j-1} and xtop_{j+1}.
+// Tables: row[p * 12 + ...] per position p (local Crout of its segment block
+// and its spikes): [0] rho [1] alpha [2] beta | [4] u1 [5] u2 |
+// [8] W_0 [9] W_1 [10] V_0 [11] V_1; G[(j * 4 + q) * 4S + i] for q = xbot 0,
+// xbot 1, xtop 0, xtop 1.
+int build_split(const std::vector<double>& band, int n, bool periodic, std::vector<int>& start,
+                std::vector<double>& row, std::vector<double>& G) {
+  const int S = std::max(1, n / kSplitSeg);
+  start.assign((size_t)S + 1, 0);
+  for (int j = 0; j < S; j++) start[j] = j * kSplitSeg;
+  start[S] = n;
+  auto A = [&](int i, int j) -> double {  // entry of the full line matrix
+    double s = 0.0;
+    for (int l = 0; l < 5; l++) {
+      int c = i + l - 2;
+      if (periodic) c = ((c % n) + n) % n;
+      else if (c < 0 || c >= n) continue;
+      if (c == j) s += band[(size_t)i * 5 + l];
+    }
+    return s;
+  };
+  row.assign((size_t)n * 12, 0.0);
+  const int T = 4 * S;
+  std::vector<double> R((size_t)T * T, 0.0);
+  for (int j = 0; j < S; j++) {
+    const int a = start[j], b = start[j + 1], L = b - a;
+    if (L < 4) return PG_EBADSHAPE;
+    std::vector<double> Lw, Uw;
+    if (!crout_banded(L, [&](int i, int k) { return A(a + i, a + k); }, Lw, Uw)) return PG_EINVAL;
+    // spike columns: right-hand sides C_j (rows 0, 1) and B_j (rows L-2, L-1)
+    const bool left = periodic || j > 0, right = periodic || j < S - 1;
+    const int pl = ((a - 2) % n + n) % n, pl1 = ((a - 1) % n + n) % n;  // xbot_{j-1} positions
+    const int pr = b % n, pr1 = (b + 1) % n;                            // xtop_{j+1} positions
+    std::vector<double> rhs((size_t)L * 4, 0.0);  // columns W0 W1 V0 V1
+    if (left) {
+      rhs[0 * 4 + 0] = A(a, pl);
+      rhs[0 * 4 + 1] = A(a, pl1);
+      rhs[1 * 4 + 1] = A(a + 1, pl1);
+    }
+    if (right) {
+      rhs[(size_t)(L - 2) * 4 + 2] = A(b - 2, pr);
+      rhs[(size_t)(L - 1) * 4 + 2] = A(b - 1, pr);
+      rhs[(size_t)(L - 1) * 4 + 3] = A(b - 1, pr1);
+    }
+    // solve A_jj X = rhs for the 4 columns (forward with L, backward with unit U)
+    for (int c = 0; c < 4; c++) {
+      std::vector<double> z((size_t)L, 0.0);
+      for (int i = 0; i < L; i++) {
+        double v = rhs[(size_t)i * 4 + c];
+        if (i >= 1) v -= Lw[(size_t)i * 3 + 1] * z[i - 1];
+        if (i >= 2) v -= Lw[(size_t)i * 3 + 2] * z[i - 2];
+        z[i] = v / Lw[(size_t)i * 3];
+      }
+      for (int i = L - 1; i >= 0; i--) {
+        double v = z[i];
+        if (i + 1 < L) v -= Uw[(size_t)i * 3 + 1] * z[i + 1];
+        if (i + 2 < L) v -= Uw[(size_t)i * 3 + 2] * z[i + 2];
+        z[i] = v;
+      }
+      for (int i = 0; i < L; i++) row[(size_t)(a + i) * 12 + 8 + c] = z[i];
+    }
+    for (int i = 0; i < L; i++) {
+      double* r = &row[(size_t)(a + i) * 12];
+      const double rho = 1.0 / Lw[(size_t)i * 3];
+      r[0] = rho;
+      r[1] = Lw[(size_t)i * 3 + 1] * rho;
+      r[2] = Lw[(size_t)i * 3 + 2] * rho;
+      r[4] = Uw[(size_t)i * 3 + 1];
+      r[5] = Uw[(size_t)i * 3 + 2];
+    }
+    // reduced-system rows of the four tips
+    const int jm = (j + S - 1) % S, jp = (j + 1) % S;
+    const int li[4] = {0, 1, L - 2, L - 1};
+    for (int q = 0; q < 4; q++) {
+      const int rr = 4 * j + q;
+      const double* w = &row[(size_t)(a + li[q]) * 12 + 8];
+      R[(size_t)rr * T + rr] += 1.0;
+      for (int c = 0; c < 2; c++) {
+        R[(size_t)rr * T + 4 * jm + 2 + c] += w[c];
+        R[(size_t)rr * T + 4 * jp + c] += w[2 + c];
+      }
+    }
+  }
+  std::vector<double> Ri;
+  if (!invert_small(R, T, Ri)) return PG_EINVAL;
+  G.assign((size_t)S * 4 * T, 0.0);
+  for (int j = 0; j < S; j++) {
+    const int jm = (j + S - 1) % S, jp = (j + 1) % S;
+    const bool left = periodic || j > 0, right = periodic || j < S - 1;
+    const int src[4] = {4 * jm + 2, 4 * jm + 3, 4 * jp, 4 * jp + 1};
+    const bool use[4] = {left, left, right, right};
+    for (int q = 0; q < 4; q++)
+      if (use[q])
+        for (int i = 0; i < T; i++) G[((size_t)j * 4 + q) * T + i] = Ri[(size_t)src[q] * T + i];
+  }
+  return PG_OK;
+}
 
 // Build the host tables of one operator along one direction.
 // Output layout (all row-major, n rows):
 //   rhs[n*9]   per-row RHS weights (d1, d2, d4 use the first 7), already divided
 //              by the metric `scale` when scale != 0 (d1: dx, compact_operators.f90:41-46;
 //              d2: dx^2, :149-152)
-//   lu[n*9]    per-row solve coefficients in the order consumed by the kernels:
-//              0:c1 1:c2 (forward) 2:c3 (inverse diagonal) 3:c4 4:c5 (backward)
-//              5:c6 6:c7 (cyclic row multipliers) 7:c8 8:c9 (cyclic fill)
-//              with entries the substitution does not use set to zero.
+//   lu[n*12]   per-row solve coefficients (solve_tables above); empty rows
+//              for explicit operators.
 int build_operator(int kind, int n, bool periodic, double scale, OpTables& t) {
   Stencil s;
   switch (kind) {
@@ -301,7 +499,7 @@ int build_operator(int kind, int n, bool periodic, double scale, OpTables& t) {
   t.addback = s.addback;
   t.null_op = (n < 4);
   t.rhs.assign((size_t)n * 9, 0.0);
-  t.lu.assign((size_t)n * 9, 0.0);
+  t.lu.assign((size_t)n * kSolveStride, 0.0);
   if (t.null_op) return PG_OK;
   if (n < 8) return PG_EBADSHAPE;  // the reference stencils index 8 points per line
 
@@ -329,32 +527,7 @@ int build_operator(int kind, int n, bool periodic, double scale, OpTables& t) {
   for (int i = 0; i < n; i++)
     for (int l = 0; l < 5; l++) t.lhs[(size_t)i * 5 + l] = band[(size_t)i * 9 + l];
 
-  if (s.implicit) {
-    auto L = [&](int i, int k) -> double& { return t.lu[(size_t)i * 9 + k]; };
-    if (periodic) {
-      factor_cyclic(band, n);
-      auto B = [&](int i, int k) { return band[(size_t)i * 9 + k]; };
-      for (int i = 0; i < n; i++) {
-        L(i, 0) = B(i, 0); L(i, 1) = B(i, 1); L(i, 2) = B(i, 2);
-        L(i, 3) = B(i, 3); L(i, 4) = B(i, 4); L(i, 5) = B(i, 5);
-        L(i, 6) = B(i, 6); L(i, 7) = B(i, 7); L(i, 8) = B(i, 8);
-      }
-      // forward: row 0 has no multipliers, row 1 only c2 (ppentLUS3x :664-666)
-      L(0, 0) = 0.0; L(0, 1) = 0.0; L(1, 0) = 0.0;
-      // backward: row N-2 (Fortran N-1) uses only its fill column c9; rows
-      // N-3 and N-4 (Fortran N-2, N-3) have their c4/c5 folded into c8/c9
-      L(n - 3, 3) = 0.0; L(n - 3, 4) = 0.0; L(n - 4, 4) = 0.0;
-    } else {
-      factor_banded(band, n);
-      auto B = [&](int i, int k) { return band[(size_t)i * 9 + k]; };
-      for (int i = 0; i < n; i++) {
-        L(i, 0) = B(i, 0); L(i, 1) = B(i, 1); L(i, 2) = B(i, 2);
-        L(i, 3) = B(i, 3); L(i, 4) = B(i, 4);
-      }
-      L(0, 0) = 0.0; L(0, 1) = 0.0; L(1, 0) = 0.0;
-      L(n - 2, 4) = 0.0; L(n - 1, 3) = 0.0; L(n - 1, 4) = 0.0;
-    }
-  }
+  if (s.implicit && !solve_tables(t.lhs, n, periodic, t.lu)) return PG_EINVAL;
   return PG_OK;
 }
 

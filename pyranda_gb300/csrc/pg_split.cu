@@ -1,0 +1,338 @@
+// Split-line compact sweeps: every line is cut into segments of kSplitSeg
+// points and each segment is solved by its own thread; the segments are
+// joined by the reduced system of their tip unknowns.
+//
+// The reference splits a line the same way across MPI ranks when a
+// direction is decomposed (local banded solve with coupling columns,
+// compact_basetype.f90:171-197; a 4x4 block tridiagonal solve of the
+// gathered boundary values, pentadiagonal.f90:160-626; the local correction,
+// compact_d1.f90:242-337).  Here the "ranks" are the threads of one CTA, the
+// reduced system is the same for every line of a grid, so its inverse is
+// formed once on the host (pg_setup.cpp build_split) and applied as small dot
+// products, and everything between the one read and the one write of a line
+// stays on chip:
+//   1. the CTA loads a tile of whole lines, coalesced for every direction
+//      (x: a warp reads a run of one line; y, z: a warp reads one position of
+//      32 neighbouring lines), converted once, into shared memory;
+//   2. thread (line l, segment j) forms the RHS of its rows from shared memory
+//      (edge rows with the reference's one-sided / periodic formulas), then
+//      the local forward and backward substitution of its segment block, and
+//      publishes the four tip values;
+//   3. after a barrier each thread takes the tips it needs from the reduced
+//      solve (its window of neighbouring segments) and corrects its rows:
+//      x = y - W xbot_{j-1} - V xtop_{j+1};
+//   4. the CTA stores the tile coalesced, with the fused epilogue (filter
+//      add-back in FP64, accumulate, ring max).
+// No scratch field is written or read back, the serial chain of a thread is
+// one segment (not one line) long, and a line may be longer than the dense
+// path's 1024 points (up to 256 segments).  T = float is the fast path's
+// arithmetic (d8 with the exact 64-bit fixed-point RHS: the tile keeps the
+// raw FP64 values); T = double follows the reference arithmetic.
+#include "pg_sweep.cuh"
+
+namespace pg {
+namespace {
+
+constexpr int kSplitThreads = 256;
+
+struct SParams {
+  const double* in;  // may equal out: a CTA reads all of its lines before it writes any
+  double* out;
+  const MemberOp* ops;
+  const SplitOp* sops;
+  const SplitTile* tiles;
+  int scale_pow;
+  const int* emax;
+};
+
+template <typename Raw>
+__device__ __forceinline__ Raw to_raw(double v);
+template <>
+__device__ __forceinline__ double to_raw<double>(double v) { return v; }
+template <>
+__device__ __forceinline__ float to_raw<float>(double v) { return d2f_bits(v); }
+
+// a staged value as the RHS arithmetic's type
+template <typename TR>
+__device__ __forceinline__ TR raw_as(double x, int E) { return load_as<TR>(x, E); }
+template <typename TR>
+__device__ __forceinline__ TR raw_as(float x, int) { return (TR)x; }
+
+// One line of the tile in shared memory, with the accessors edge_rhs uses.
+template <typename TR, typename Raw>
+struct SLine {
+  const Raw* v0;
+  int n, e;
+  __device__ __forceinline__ TR v(int p) const { return raw_as<TR>(v0[p], e); }
+  __device__ __forceinline__ TR w(int p) const {
+    const int q = p < 0 ? p + n : (p >= n ? p - n : p);
+    return v(q);
+  }
+};
+
+__host__ __device__ constexpr size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
+__host__ __device__ inline int row_stride(int n) { return (n & 1) ? n : n + 1; }  // odd: conflict-free columns
+
+template <typename T, typename Raw>
+__host__ __device__ inline size_t split_smem(int n, int S, int nl) {
+  const int ld = row_stride(n);
+  return al16((size_t)nl * 8) + al16((size_t)nl * ld * sizeof(Raw)) + al16((size_t)nl * ld * sizeof(T)) +
+         (size_t)nl * (4 * S + 1) * sizeof(T);
+}
+
+template <typename T, int KIND, bool PER, bool IMPL, bool ADDBACK, int DIR, int EPI, typename TR>
+__global__ void __launch_bounds__(kSplitThreads) split_kernel(const SParams P) {
+  constexpr bool kExact = std::is_same<TR, long long>::value;
+  using Raw = typename std::conditional<kExact, double, T>::type;
+  using W = typename WeightOf<TR>::type;
+  extern __shared__ __align__(16) unsigned char s_buf[];
+  const SplitTile tile = P.tiles[blockIdx.x];
+  const MemberOp& op = P.ops[tile.op];
+  const SplitOp so = P.sops[tile.op];
+  const int n = op.n, S = so.S, nl = tile.nlines;
+  const int ld = row_stride(n), tld = 4 * S + 1;
+  long long* sbase = reinterpret_cast<long long*>(s_buf);
+  Raw* sv = reinterpret_cast<Raw*>(s_buf + al16((size_t)nl * 8));
+  T* sw = reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(sv) + al16((size_t)nl * ld * sizeof(Raw)));
+  T* tips = reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(sw) + al16((size_t)nl * ld * sizeof(T)));
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nw = blockDim.x >> 5;
+  const int nx = op.nx, ny = op.ny;
+  const long long st = (DIR == 0) ? 1 : (DIR == 1 ? (long long)nx : (long long)nx * ny);
+  for (int l = tid; l < nl; l += blockDim.x) {
+    const long long Lm = tile.line0 + l;
+    long long b;
+    if (DIR == 0) b = Lm * nx;
+    else if (DIR == 1) b = (Lm / nx) * (long long)nx * ny + (Lm % nx);
+    else b = Lm;
+    sbase[l] = b + op.off;
+  }
+  __syncthreads();
+
+  // 1. load the tile (every input value of these lines is read before any output is written)
+  if (DIR == 0) {
+    for (int l = warp; l < nl; l += nw) {
+      const double* src = P.in + sbase[l];
+      Raw* dst = sv + l * ld;
+#pragma unroll 4
+      for (int p = lane; p < n; p += 32) dst[p] = to_raw<Raw>(__ldg(src + p));
+    }
+  } else {
+    for (int p = warp; p < n; p += nw) {
+      const long long o = (long long)p * st;
+#pragma unroll 2
+      for (int l = lane; l < nl; l += 32) sv[l * ld + p] = to_raw<Raw>(__ldg(P.in + sbase[l] + o));
+    }
+  }
+  __syncthreads();
+
+  // 2. RHS and local solve of one segment of one line
+  const int l = tid % nl, j = tid / nl;
+  const bool active = j < S;
+  const T* __restrict__ C = reinterpret_cast<const T*>(so.row);  // 12 per position
+  const int E = kExact ? __ldg(P.emax + tile.op) : 0;
+  const float wsc = kExact ? op.wscale : 1.0f;
+  const W* __restrict__ R = reinterpret_cast<const W*>(kExact ? (const void*)op.rhs_i : op.rhs);
+  int a = 0, b = 0;
+  T* wl = sw + l * ld;
+  if (active) {
+    a = __ldg(so.start + j);
+    b = __ldg(so.start + j + 1);
+    const SLine<TR, Raw> ln{sv + l * ld, n, E};
+    TR ai[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) ai[k] = kExact ? (TR)op.iw[k] : (TR)op.ri[k];
+    const float wi = kExact ? wsc * (float)op.iw[0] : 0.0f;
+    constexpr int H = (KIND == 4) ? 4 : 3;
+    T z1 = T(0), z2 = T(0);
+    for (int i = a; i < b; i++) {
+      T r;
+      if (i < 4 || i >= n - 4) {
+        r = solve_value(edge_rhs<TR, KIND, PER, W>(ln, i, R), E, wsc);
+      } else if constexpr (kExact) {
+        // iw[0] x the 8th difference (1, -8, 28, -56, 70, -56, 28, -8, 1), exact in 64-bit integers
+        const long long c8[9] = {1, -8, 28, -56, 70, -56, 28, -8, 1};
+        long long s = 0;
+#pragma unroll
+        for (int k = 0; k < 9; k++) s += c8[k] * ln.v(i - 4 + k);
+        r = fixed_to_float(s, E, wi);
+      } else {
+        TR win[kRing];
+#pragma unroll
+        for (int k = 0; k < 2 * H + 1; k++) win[k] = ln.v(i - H + k);
+        r = solve_value(ring_rhs<TR, KIND>(win, 0, ai), E, wsc);
+      }
+      if (IMPL) {  // forward substitution of the segment block (Crout: z = rho r - alpha z1 - beta z2)
+        const V4<T> f = V4<T>::ld(C + i * 12);
+        T z = f.a * r;
+        z -= f.c * z2;
+        z -= f.b * z1;
+        z2 = z1;
+        z1 = z;
+        r = z;
+      }
+      wl[i] = r;
+    }
+    if (IMPL) {  // backward substitution with the unit upper factor
+      T y1 = T(0), y2 = T(0);
+      for (int i = b - 1; i >= a; i--) {
+        const V4<T> g = V4<T>::ld(C + i * 12 + 4);  // u1 u2 . .
+        T y = wl[i];
+        y -= g.b * y2;
+        y -= g.a * y1;
+        wl[i] = y;
+        y2 = y1;
+        y1 = y;
+      }
+      T* tp = tips + l * tld + 4 * j;
+      tp[0] = wl[a];
+      tp[1] = wl[a + 1];
+      tp[2] = wl[b - 2];
+      tp[3] = wl[b - 1];
+    }
+  }
+  __syncthreads();
+
+  // 3. the neighbouring tips from the reduced system, then the correction
+  if (IMPL && active) {
+    const T* __restrict__ Gj = reinterpret_cast<const T*>(so.G) + (size_t)j * 16 * S;
+    const int g0 = __ldg(so.win + 2 * j), gc = __ldg(so.win + 2 * j + 1);
+    const T* tl = tips + l * tld;
+    T q0 = T(0), q1 = T(0), q2 = T(0), q3 = T(0);
+    const int T4 = 4 * S;
+    for (int k = 0; k < gc; k++) {
+      int js = g0 + k;
+      js = js >= S ? js - S : js;
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        const int idx = 4 * js + c;
+        const T t = tl[idx];
+        q0 += ldc(Gj + idx) * t;
+        q1 += ldc(Gj + T4 + idx) * t;
+        q2 += ldc(Gj + 2 * T4 + idx) * t;
+        q3 += ldc(Gj + 3 * T4 + idx) * t;
+      }
+    }
+    for (int i = a; i < b; i++) {
+      const V4<T> sp = V4<T>::ld(C + i * 12 + 8);  // W_0 W_1 V_0 V_1
+      T x = wl[i];
+      x -= sp.a * q0;
+      x -= sp.b * q1;
+      x -= sp.c * q2;
+      x -= sp.d * q3;
+      wl[i] = x;
+    }
+  }
+  __syncthreads();
+
+  // 4. store with the fused epilogue
+  constexpr bool kReadOut = (EPI == EPI_ADD || EPI == EPI_RING_MAX);
+  const double sc = (P.scale_pow == 2) ? op.dm * op.dm : (P.scale_pow == 1 ? op.dm : 1.0);
+  if (DIR == 0) {
+    for (int l2 = warp; l2 < nl; l2 += nw) {
+      const long long base = sbase[l2];
+      const T* src = sw + l2 * ld;
+      for (int p = lane; p < n; p += 32) {
+        const long long g = base + p;
+        const double vin = ADDBACK ? P.in[g] : 0.0;
+        const double o = kReadOut ? P.out[g] : 0.0;
+        P.out[g] = epilogue<EPI>(to_f64<T>(src[p]), vin, o, sc, ADDBACK);
+      }
+    }
+  } else {
+    for (int p = warp; p < n; p += nw) {
+      const long long off = (long long)p * st;
+      for (int l2 = lane; l2 < nl; l2 += 32) {
+        const long long g = sbase[l2] + off;
+        const double vin = ADDBACK ? P.in[g] : 0.0;
+        const double o = kReadOut ? P.out[g] : 0.0;
+        P.out[g] = epilogue<EPI>(to_f64<T>(sw[l2 * ld + p]), vin, o, sc, ADDBACK);
+      }
+    }
+  }
+}
+
+template <typename T, int KIND, bool PER, bool IMPL, bool ADDBACK, int DIR, int EPI, typename TR>
+int launch_s(const SParams& P, const SplitSet& ss, void* stream) {
+  constexpr bool kExact = std::is_same<TR, long long>::value;
+  using Raw = typename std::conditional<kExact, double, T>::type;
+  const size_t smem = (sizeof(Raw) == 8 && sizeof(T) == 4) ? ss.smem_mixed : (sizeof(T) == 8 ? ss.smem64 : ss.smem32);
+  auto k = split_kernel<T, KIND, PER, IMPL, ADDBACK, DIR, EPI, TR>;
+  static size_t attr = 0;
+  if (smem > attr) {
+    const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) {
+      set_error("split sweep: %s (%zu bytes of shared memory)", cudaGetErrorString(e), smem);
+      return PG_ECUDA;
+    }
+    attr = smem;
+  }
+  k<<<ss.ntiles, kSplitThreads, smem, (cudaStream_t)stream>>>(P);
+  count_launch();
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error("split sweep launch: %s", cudaGetErrorString(e));
+    return PG_ECUDA;
+  }
+  return PG_OK;
+}
+
+template <typename T, int KIND, bool PER, bool IMPL, bool ADDBACK, typename TR = T>
+int split_dir_epi(const SParams& P, const SplitSet& ss, int dir, int epi, void* st) {
+#define PG_SPLIT_EPI(D)                                                                             \
+  switch (epi) {                                                                                    \
+    case EPI_STORE: return launch_s<T, KIND, PER, IMPL, ADDBACK, D, EPI_STORE, TR>(P, ss, st);       \
+    case EPI_ADD: return launch_s<T, KIND, PER, IMPL, ADDBACK, D, EPI_ADD, TR>(P, ss, st);           \
+    case EPI_RING_SET: return launch_s<T, KIND, PER, IMPL, ADDBACK, D, EPI_RING_SET, TR>(P, ss, st); \
+    default: return launch_s<T, KIND, PER, IMPL, ADDBACK, D, EPI_RING_MAX, TR>(P, ss, st);           \
+  }
+  if (dir == 0) { PG_SPLIT_EPI(0) }
+  if (dir == 1) { PG_SPLIT_EPI(1) }
+  PG_SPLIT_EPI(2)
+#undef PG_SPLIT_EPI
+}
+
+template <typename T>
+int split_kind(const OpRef& op, const SParams& P, const SplitSet& ss, int dir, int epi, void* st) {
+  switch (op.kind) {
+    case OPK_D1:
+      return op.periodic ? split_dir_epi<T, 1, true, true, false>(P, ss, dir, epi, st)
+                         : split_dir_epi<T, 1, false, true, false>(P, ss, dir, epi, st);
+    case OPK_D8: {
+      using TRX = typename std::conditional<std::is_same<T, float>::value, long long, T>::type;
+      if (std::is_same<T, float>::value && op.exact)
+        return op.periodic ? split_dir_epi<T, 4, true, true, false, TRX>(P, ss, dir, epi, st)
+                           : split_dir_epi<T, 4, false, true, false, TRX>(P, ss, dir, epi, st);
+      return op.periodic ? split_dir_epi<T, 4, true, true, false>(P, ss, dir, epi, st)
+                         : split_dir_epi<T, 4, false, true, false>(P, ss, dir, epi, st);
+    }
+    case OPK_SF:
+      return op.periodic ? split_dir_epi<T, 4, true, true, true>(P, ss, dir, epi, st)
+                         : split_dir_epi<T, 4, false, true, true>(P, ss, dir, epi, st);
+    case OPK_D2:
+      return op.periodic ? split_dir_epi<T, 3, true, true, false>(P, ss, dir, epi, st)
+                         : split_dir_epi<T, 3, false, true, false>(P, ss, dir, epi, st);
+    case OPK_D4:
+      return op.periodic ? split_dir_epi<T, 3, true, false, false>(P, ss, dir, epi, st)
+                         : split_dir_epi<T, 3, false, false, false>(P, ss, dir, epi, st);
+    default:
+      return op.periodic ? split_dir_epi<T, 4, true, false, true>(P, ss, dir, epi, st)
+                         : split_dir_epi<T, 4, false, false, true>(P, ss, dir, epi, st);
+  }
+}
+
+}  // namespace
+
+size_t split_smem_bytes(int precision, bool exact, int n, int S, int nl) {
+  if (precision == PG_FP64) return split_smem<double, double>(n, S, nl);
+  return exact ? split_smem<float, double>(n, S, nl) : split_smem<float, float>(n, S, nl);
+}
+
+int launch_split(int precision, const OpRef& op, const SplitSet& ss, const double* in, double* out, int dir, int epi,
+                 int scale_pow, const int* emax, void* stream) {
+  if (!ss.ok || ss.ntiles == 0) return PG_OK;
+  SParams P{in, out, op.dev, ss.sops, ss.tiles, scale_pow, emax};
+  if (precision == PG_FP32) return split_kind<float>(op, P, ss, dir, epi, stream);
+  return split_kind<double>(op, P, ss, dir, epi, stream);
+}
+
+}  // namespace pg

@@ -4,11 +4,13 @@
 // One thread owns one grid line and streams it once forward and once
 // backward:
 //   forward:  RHS stencil through a register window (compact_d1.f90:113-193,
-//             compact_r4.f90:106-193) fused with the forward elimination of
-//             the banded (bpentLUS3x, pentadiagonal.f90:629-651) or cyclic
-//             (ppentLUS3x, :654-684) solve; the eliminated values go to a
-//             scratch array laid out [position][line], so every access to it is
-//             coalesced whatever the sweep direction;
+//             compact_r4.f90:106-193) fused with the forward substitution of
+//             the line solve (the reference's bpentLUS3x / ppentLUS3x,
+//             pentadiagonal.f90:629-684, solve the same systems from its own
+//             factorisation; the tables here are the Crout / Schur-complement
+//             ones of pg_setup.cpp); the forward values go to a scratch array
+//             laid out [position][line], so every access to it is coalesced
+//             whatever the sweep direction;
 //   backward: back substitution, fused with the epilogue (filter add-back
 //             compact_r4.f90:209-234, ring max operators.f90:636-639,
 //             divergence accumulation) and the store.
@@ -213,8 +215,8 @@ struct Line {
 
 // RHS of one edge row (rows 0..3 and n-4..n-1) straight from global memory,
 // with the reference's periodic-halo or one-sided (boundary code 0) formulas.
-template <typename T, int KIND, bool PER, typename W>
-__device__ __forceinline__ T edge_rhs(const Line<T>& ln, int i, const W* __restrict__ R) {
+template <typename T, int KIND, bool PER, typename W, typename LN>
+__device__ __forceinline__ T edge_rhs(const LN& ln, int i, const W* __restrict__ R) {
   const int n = ln.n;
   const W* r = R + i * 9;
   if (KIND == 1) {
@@ -372,56 +374,51 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_kernel(const KParams P) {
   };
 
   // ---------------------------------------------------------------- forward
+  // Solve tables (12 per row, pg_setup.cpp solve_tables): forward
+  // z_i = rho r_i - alpha z_{i-1} - beta z_{i-2}; on periodic lines also the
+  // border sums t0 += G_0i z_i, t1 += G_1i z_i over rows 0..n-3.  Rows whose
+  // multipliers reach before the line start hold zeros, so every row takes the
+  // same formula.
   T rm1 = T(0), rm2 = T(0), t1 = T(0), t2 = T(0), rN1 = T(0), rN = T(0);
-  // edge rows, with the reference's special first rows and closing rows
+  auto fwd_row = [&](int i, T rhs) {
+    const V4<T> f = V4<T>::ld(C + i * 12);  // rho alpha beta G_0i
+    T z = f.a * rhs;
+    z -= f.c * rm2;
+    z -= f.b * rm1;
+    if (PER) {
+      t1 += f.d * z;
+      t2 += ldc(C + i * 12 + 8) * z;
+    }
+    return z;
+  };
+  // edge rows (0..3 and n-4..n-1)
   auto fwd_edge = [&](int i, T rhs) {
     if (!IMPL) {
       put_load(i, rhs);
       return;
     }
-    const V4<T> f = V4<T>::ld(C + i * 12);  // c1 c2 c6 c7
-    T r;
-    if (PER) {
-      if (i >= n - 2) {  // the last two rows are closed by the border sums
-        if (i == n - 2) rN1 = rhs;
-        else rN = rhs;
-        return;
-      }
-      if (i == 0) r = rhs;
-      else if (i == 1) r = rhs - f.b * rm1;
-      else r = rhs - f.b * rm1 - f.a * rm2;
-      t1 += f.c * r;
-      t2 += f.d * r;
-    } else {
-      if (i == 0) r = rhs;
-      else if (i == 1) r = rhs - rm1 * f.b;
-      else r = (rhs - rm2 * f.a) - rm1 * f.b;
+    if (PER && i >= n - 2) {  // the two border unknowns are solved after the sweep
+      if (i == n - 2) rN1 = rhs;
+      else rN = rhs;
+      return;
     }
-    if (i < n - 2) ps[i * nl] = r;
+    const T z = fwd_row(i, rhs);
+    if (i < n - 2) ps[i * nl] = z;
     rm2 = rm1;
-    rm1 = r;
+    rm1 = z;
   };
-  // interior rows (2 <= i <= n-3): no special cases
+  // interior rows (4 <= i <= n-5)
   auto fwd_in = [&](int i, T rhs) {
     if (!IMPL) {
       put_load(i, rhs);
       return;
     }
-    const V4<T> f = V4<T>::ld(C + i * 12);
-    T r;
-    if (PER) {
-      r = rhs - f.b * rm1 - f.a * rm2;
-      t1 += f.c * r;
-      t2 += f.d * r;
-    } else {
-      r = (rhs - rm2 * f.a) - rm1 * f.b;
-    }
-    ps[i * nl] = r;
+    const T z = fwd_row(i, rhs);
+    ps[i * nl] = z;
     rm2 = rm1;
-    rm1 = r;
+    rm1 = z;
   };
 
-#pragma unroll
   // implicit: the first rows' forward elimination; explicit operators store them after the window
   // below is filled, so that an in-place call (in == out) still reads the original rows 0..3
   if (IMPL) {
@@ -492,21 +489,23 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_kernel(const KParams P) {
   if (!IMPL) return;
 
   // --------------------------------------------------------------- backward
-  T x1, x2, xN1 = T(0), xN = T(0);
-  if (PER) {  // ppentLUS3x :673-676
-    const T* ca = C + (n - 2) * 12;
-    const T* cb = C + (n - 1) * 12;
-    const T r1 = rN1 - t1;
-    xN = (rN - t2 - ldc(ca + 3) * r1) * ldc(cb + 4);
-    xN1 = (r1 - ldc(ca + 8) * xN) * ldc(ca + 4);
-    x1 = xN1;
-    x2 = xN;
-  } else {  // bpentLUS3x :640-641 (the last two forward values are still in registers)
-    x2 = rm1 * ldc(C + (n - 1) * 12 + 4);
-    x1 = (rm2 - ldc(C + (n - 2) * 12 + 5) * x2) * ldc(C + (n - 2) * 12 + 4);
+  // x_i = z_i - u1 x_{i+1} - u2 x_{i+2} (- F_i0 x_{n-2} - F_i1 x_{n-1} on periodic lines)
+  T x1, x2, xa = T(0), xb = T(0);
+  if (PER) {  // border unknowns x_B = S^-1 (r_B - t); S^-1 sits in row n-2
+    const V4<T> si = V4<T>::ld(C + (n - 2) * 12);
+    const T b0 = rN1 - t1, b1 = rN - t2;
+    xa = si.a * b0 + si.b * b1;
+    xb = si.c * b0 + si.d * b1;
+    put_load(n - 1, xb);
+    put_load(n - 2, xa);
+    x1 = T(0);  // the interior block's band ends at row n-3; F carries the coupling to x_B
+    x2 = T(0);
+  } else {  // the last two forward values are still in registers
+    x2 = rm1;
+    x1 = rm2 - ldc(C + (n - 2) * 12 + 4) * x2;
+    put_load(n - 1, x2);
+    put_load(n - 2, x1);
   }
-  put_load(n - 1, x2);
-  put_load(n - 2, x1);
   T pr[kPFB];
   double pv[kPFB], po[kPFB];
 #pragma unroll
@@ -521,17 +520,20 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_kernel(const KParams P) {
     for (int k = 0; k < kPFB; k++) {
       const int ii = i - k;
       if (ii >= 0) {
-        const T r = pr[k];
+        const T z = pr[k];
         const double vin = pv[k], o = po[k];
         const int p = ii - kPFB;
         pr[k] = (p >= 0) ? ps[p * nl] : T(0);
         if (ADDBACK) pv[k] = (p >= 0) ? pin[p * st] : 0.0;
         if (kReadOut) po[k] = (p >= 0) ? pout[p * st] : 0.0;
-        const V4<T> g = V4<T>::ld(C + ii * 12 + 4);  // c3 c4 c5 c8
-        T part;
-        if (PER) part = r - g.d * xN1 - ldc(C + ii * 12 + 8) * xN - g.c * x2;
-        else part = r - g.c * x2;
-        const T x = (part - g.b * x1) * g.a;  // short chain through x1
+        const V4<T> g = V4<T>::ld(C + ii * 12 + 4);  // u1 u2 F_i0 F_i1
+        T x = z;
+        if (PER) {
+          x -= g.d * xb;
+          x -= g.c * xa;
+        }
+        x -= g.b * x2;
+        x -= g.a * x1;  // short chain through x1: one fused multiply-add
         x2 = x1;
         x1 = x;
         put(ii, x, vin, o);

@@ -93,6 +93,10 @@ class EnsembleGrid:
         _lib.check(self.lib.pg_ens_set_precision(self.h, _lib.precision_code(precision)),
                    "pg_ens_set_precision")
 
+    def set_line_split(self, on):
+        """Banded line solves split across the threads of a CTA (see Grid.set_line_split)."""
+        _lib.check(self.lib.pg_ens_set_line_split(self.h, 1 if on else 0), "pg_ens_set_line_split")
+
     # ------------------------------------------------------------------ fields
     def empty(self):
         return torch.empty(self.npts, dtype=torch.float64, device=self.device)

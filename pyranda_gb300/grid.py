@@ -61,7 +61,7 @@ def flush_pending():
 class Grid:
     """A Cartesian pyranda patch on one GPU (parcop.f90:23-70 setup + setup_mesh)."""
 
-    def __init__(self, n, periodic, x1, xn, precision="fp64", device=None):
+    def __init__(self, n, periodic, x1, xn, precision="fp64", device=None, line_split=False):
         if not torch.cuda.is_available():
             raise RuntimeError("pyranda_gb300 needs a CUDA device; there is no CPU fallback")
         self.lib = _lib.load()
@@ -90,6 +90,9 @@ class Grid:
         self.mesh_d = list(md)   # mesh d1, d2, d3
         self.gridlen = min(self.mesh_d)
         self._scalar_pool = []
+        self.line_split = False
+        if line_split:
+            self.set_line_split(True)
 
     def __del__(self):
         try:
@@ -110,6 +113,12 @@ class Grid:
         self.precision = precision
         _lib.check(self.lib.pg_set_precision(self.h, _lib.precision_code(precision)),
                    "pg_set_precision")
+
+    def set_line_split(self, on):
+        """Banded line solves split across the threads of a CTA (segments of 32
+        points joined by the reduced system) instead of one thread per line."""
+        _lib.check(self.lib.pg_set_line_split(self.h, 1 if on else 0), "pg_set_line_split")
+        self.line_split = bool(on)
 
     # ------------------------------------------------------------------ fields
     def empty(self):

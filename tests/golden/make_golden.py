@@ -1,13 +1,17 @@
 """Extract the reference's own golden scalars for the compact-operator path.
 
 Reads the reference test-case files as text (they are Python fragments that
-``tests/run_tests.py`` executes) and writes ``reference_scalars.json``.  Run it
-where the reference tree is mounted:
+``tests/run_tests.py`` executes) and writes ``reference_scalars.json``; copies
+the reference's profile baselines of the 2-D Euler and Kelvin-Helmholtz
+cases (``tests/baselines/*.dat``: two rows, x and the profile, compared by
+``tests/testObj.py:checkProfile``) next to it.  Run it where the reference
+tree is mounted, naming its root:
 
     python tests/golden/make_golden.py /path/to/pyranda
 """
 import json
 import os
+import shutil
 import sys
 
 CASES = {
@@ -15,6 +19,13 @@ CASES = {
     "testUnit.py": ["unit-test-3D"],
     "testTaylorGreen.py": ["taylorgreen"],
     "testShuOsher.py": ["shu-osher-CR"],
+}
+
+
+PROFILES = {  # test name -> baseline file (tests/cases/test2deuler.py:3-9)
+    "euler-2d-64": "euler-2d-64.dat",
+    "euler-2d-128": "euler-2d-128.dat",
+    "KH-2d-64": "KelvinHelmholtzKH-2d-64.dat",
 }
 
 
@@ -34,7 +45,13 @@ def main(root):
     with open(dst, "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)
     print("wrote", dst)
+    here = os.path.dirname(dst)
+    for name, fname in PROFILES.items():
+        shutil.copyfile(os.path.join(root, "tests", "baselines", fname), os.path.join(here, fname))
+        print("copied", fname, "for", name)
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <root of the pyranda source tree>")
+    main(sys.argv[1])

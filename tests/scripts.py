@@ -177,6 +177,11 @@ eps = 2.0e-1
     return x, rho
 
 
+def _meshx(ss):
+    """x coordinates of the mesh (ss.mesh.coords[0] in pyranda; the oracle keeps them as ss.meshx)."""
+    return ss.variables["meshx"].data if "meshx" in ss.variables else ss.meshx
+
+
 def _host(a):
     if hasattr(a, "cpu"):
         t = a.detach()
@@ -197,3 +202,159 @@ def shu_osher(Sim, packages, **kw):
     cr1 = numpy.log(diff[-1] / diff[-2]) / numpy.log(.5)
     cr2 = numpy.log(diff[-2] / diff[-3]) / numpy.log(.5)
     return float((cr1 + cr2) / 2.0)
+
+
+EULER_2D = """
+# Primary Equations of motion here
+ddt(:rho:)  =  -ddx(:rho:*:u:)                  - ddy(:rho:*:v:)
+ddt(:rhou:) =  -ddx(:rhou:*:u: + :p: - :tau:)   - ddy(:rhou:*:v:)
+ddt(:rhov:) =  -ddx(:rhov:*:u:)                 - ddy(:rhov:*:v: + :p: - :tau:)
+ddt(:Et:)   =  -ddx( (:Et: + :p: - :tau:)*:u: ) - ddy( (:Et: + :p: - :tau:)*:v: )
+# Conservative filter of the EoM
+:rho:       =  fbar( :rho:  )
+:rhou:      =  fbar( :rhou: )
+:rhov:      =  fbar( :rhov: )
+:Et:        =  fbar( :Et:   )
+# Update the primatives and enforce the EOS
+:u:         =  :rhou: / :rho:
+:v:         =  :rhov: / :rho:
+:p:         =  ( :Et: - .5*:rho:*(:u:*:u: + :v:*:v:) ) * ( :gamma: - 1.0 )
+# Artificial bulk viscosity (old school way)
+:div:       =  ddx(:u:) + ddy(:v:)
+:beta:      =  gbar(abs(ring(:div:))) * :rho: * 7.0e-2
+:tau:       =  :beta:*:div:
+# Apply constant BCs
+bc.extrap(['rho','Et'],['x1','xn','y1','yn'])
+bc.const(['u','v'],['x1','xn','y1','yn'],0.0)
+"""
+
+
+def euler_2d(Sim, Npts, packages, **kw):
+    """examples/euler.py N 1 (tests/cases/test2deuler.py): the 2-D Sod problem
+    (a circular shock tube) on an N x N one-sided mesh to t = 2 pi / 8; returns
+    (x, rho) along the middle row j = N/2, the profile the test compares."""
+    L = numpy.pi * 2.0
+    Lp = L * (Npts - 1.0) / Npts
+    mesh = ("xdom = (0.0, %r, %d)\nydom = (0.0, %r, %d)\nzdom = (0.0, %r, 1, periodic=True)"
+            % (Lp, Npts, Lp, Npts, Lp))
+    ss = Sim("advection", mesh, **kw)
+    packages(ss)
+    ss.EOM(EULER_2D)
+    ss.setIC("""rad = sqrt( (meshx-pi)**2  +  (meshy-pi)**2 )
+:gamma: = 1.4
+:Et:  = gbar( where( rad < pi/2.0, 1.0/(:gamma:-1.0) , .1 /(:gamma:-1.0) ) )
+:rho: = gbar( where( rad < pi/2.0, 1.0    , .125 ) )
+""")
+    time = 0.0
+    v = 1.0
+    dt_max = v / Npts * 0.75
+    tt = L / v * .125
+    dt = dt_max
+    while tt > time:
+        time = ss.rk4(time, dt)
+        dt = min(dt_max, (tt - time))
+    x = _host(_meshx(ss))[:, Npts // 2, 0]
+    rho = _host(ss.variables["rho"].data)[:, Npts // 2, 0]
+    return x, rho
+
+
+KH_EOM = """
+# Primary Equations of motion here
+ddt(:rho:)  =  -ddx(:rho:*:u:)            - ddy(:rho:*:v:)
+ddt(:rhou:) =  -ddx(:rhou:*:u: - :tauxx:) - ddy(:rhou:*:v: - :tauxy:)
+ddt(:rhov:) =  -ddx(:rhov:*:u: - :tauxy:) - ddy(:rhov:*:v: - :tauyy:)
+ddt(:Et:)   =  -ddx( (:Et: - :tauxx:)*:u: - :tauxy:*:v:  - :tx:*:kappa: )  - ddy( (:Et: - :tauyy:)*:v: -:tauxy:*:u:- :ty:*:kappa: )
+# Conservative filter of the EoM
+:rho:       =  fbar( :rho:  )
+:rhou:      =  fbar( :rhou: )
+:rhov:      =  fbar( :rhov: )
+:Et:        =  fbar( :Et:   )
+# Update the primatives and enforce the EOS
+:u:         =  :rhou: / :rho:
+:v:         =  :rhov: / :rho:
+:p:         =  ( :Et: - .5*:rho:*(:u:*:u: + :v:*:v:) ) * ( gamma - 1.0 )
+# Artificial bulk viscosity
+:ux:        =  ddx(:u:)
+:vy:        =  ddy(:v:)
+:div:       =  :ux: + :vy:
+# Remaining cross derivatives
+:uy:        =  ddy(:u:)
+:vx:        =  ddx(:v:)
+:enst:      = sqrt( (:uy:-:vx:)**2 )
+:tke:       = :rho:*(:u:*:u: + :v:*:v: )
+:S:         = sqrt( :ux:*:ux: + :vy:*:vy:  + .5*((:uy:+:vx:)**2  ) )
+:mu:        =  gbar( abs(ring(:S:  )) ) * :rho: * 1.0e-4
+:beta:      =  gbar( abs(ring(:div:)) * :rho: )  * 7.0e-3
+:taudia:    =  (:beta:-2./3.*:mu:) *:div: - :p:
+:tauxx:     =  2.0*:mu:*:ux:   + :taudia:
+:tauyy:     =  2.0*:mu:*:vy:   + :taudia:
+:tauxy:     = :mu:*(:uy:+:vx:)
+:T:         = :p: / (:rho: * R0 )
+[:tx:,:ty:,:tz:] = grad(:T:)
+:kappa:     = gbar( ring(:T:)* :rho:*cv/(:T: * :dt: ) ) * 1.0e-3
+:cs:  = sqrt( :p: / :rho: * gamma )
+:dt: = dt.courant(:u:,:v:,:w:,:cs:)*1.0
+:dt: = numpy.minimum(:dt:,0.2 * dt.diff(:beta:,:rho:))
+:dt: = numpy.minimum(:dt:,0.2 * dt.diff(:mu:,:rho:))
+"""
+
+KH_IC = """
+Um = (u1-u2)/2.0
+rhoM = (rho1-rho2)/2.0
+:u: =                     u1-Um*exp( -(meshy-.75)/L)
+:u: = where( meshy < .75, u2+Um*exp( -(.75-meshy)/L) , :u: )
+:u: = where( meshy < .50, u2+Um*exp( (-meshy+.25)/L) , :u: )
+:u: = where( meshy < .25, u1-Um*exp(  (meshy-.25)/L) , :u: )
+:v: = 0.01*sin( 4.*pi*meshx ) + Vmean
+:rho: =                     rho1-rhoM*exp( -(meshy-.75)/L)
+:rho: = where( meshy < .75, rho2+rhoM*exp( -(.75-meshy)/L) , :rho: )
+:rho: = where( meshy < .50, rho2+rhoM*exp( (-meshy+.25)/L) , :rho: )
+:rho: = where( meshy < .25, rho1-rhoM*exp(  (meshy-.25)/L) , :rho: )
+:p: += p0
+# Form conserved variables
+:Et: = :p:/( gamma - 1.0 ) + .5*:rho:*(:u:*:u: + :v:*:v:)
+:rhou: = :rho:*:u:
+:rhov: = :rho:*:v:
+:cs:  = sqrt( :p: / :rho: * gamma )
+:dt: = dt.courant(:u:,:v:,:w:,:cs:)*.1
+"""
+
+
+def kelvin_helmholtz_2d(Sim, Npts, packages, tfinal=1.5, **kw):
+    """examples/KH.py N 0 <name> 1 (tests/cases/test2deuler.py:47-51): the
+    McNally et al. Kelvin-Helmholtz problem with the AFLES terms on a periodic
+    N x N mesh to t = 1.5; returns (x, rho) along row j = 3N/4, the profile the
+    test compares."""
+    gamma, p0, u1, u2, rho1, rho2, L, tFinal, R = 5. / 3., 2.5, 0.5, -0.5, 1.0, 2.0, 0.025, tfinal, 1.0
+    Vmean = 0.0
+    cp = R / (1.0 - 1.0 / gamma)
+    cv = cp - R
+    dt_max = 1.0
+    mesh = """
+xdom = (0.0, len,  Npts, periodic=True)
+ydom = (0.0, len,  Npts, periodic=True)
+""".replace("Npts", str(Npts)).replace("len", str(1.0 * (Npts - 1.0) / Npts))
+    ss = Sim("KelvinHelmholtz", mesh, **kw)
+    packages(ss)
+    ss.EOM(KH_EOM, {"gamma": gamma, "R0": R, "cv": cv})
+    ss.setIC(KH_IC, {"gamma": gamma, "u1": u1, "u2": u2, "p0": p0, "rho1": rho1, "rho2": rho2, "L": L,
+                     "Vmean": Vmean})
+    time = 0.0
+    dt = _f(ss.variables["dt"].data)
+    while tFinal > time:
+        time = ss.rk4(time, dt)
+        dt = min(_f(ss.variables["dt"].data), 1.1 * dt)
+        dt = min(dt_max, dt)
+        dt = min(dt, (tFinal - time))
+    j = int(3 * Npts / 4)
+    x = _host(_meshx(ss))[:, j, 0]
+    rho = _host(ss.variables["rho"].data)[:, j, 0]
+    return x, rho
+
+
+def profile_error(golden_path, x, v):
+    """tests/testObj.py:checkProfile: max |base - test| / max |base| over the
+    common length of the two profiles (row 1 of the baseline file)."""
+    base = numpy.loadtxt(golden_path)
+    m = min(base.shape[1], len(v))
+    return float(numpy.max(numpy.abs(base[1, :m] - numpy.asarray(v)[:m])) / numpy.max(numpy.abs(base[1, :m])))

@@ -1,12 +1,12 @@
-"""Dense split-TF32 tensor-core operators against the FP64 banded path.
+"""Dense split-TF32 tensor-core operators against the oracle and the FP64 banded path.
 
 precision='dense' applies d1, d8 and the compact filter as dense n x n
 matrices (D = A^-1 B built from the banded operator itself) with three TF32
 MMAs per product and FP32 accumulation; the Gaussian filter and any
 direction outside 16..1024 points use the FP32 banded sweeps.  Bounds, as
-relative L2 against the FP64 banded result on the same input (FP32-level
-arithmetic; the FP32 banded path's error on the same input is printed
-beside it):
+relative L2 against the oracle's result on the same input and against the
+FP64 banded GPU result (FP32-level arithmetic; the FP32 banded path's error
+on the same input is printed beside it):
   d1, d8, ring, div: <= 1e-5;   compact and Gaussian filters: <= 2e-6;
   the library status word stays PG_OK (no bounded wait gave up).
 """
@@ -61,27 +61,35 @@ def _smooth(n, seed):
 
 
 @pytest.mark.parametrize("n,per", CASES)
-def test_dense_operators_match_fp64(n, per):
+def test_dense_operators_match_oracle(oracle, n, per):
+    """Each dense operator against the oracle (the CPU restatement of parcop)
+    on the same input, and, on a second line, against the FP64 banded GPU
+    path; the FP32 banded path's error against the oracle is printed beside."""
     g64, gd, g32 = _grids(n, per, fp32=True)
-    v = to_dev(_smooth(n, 1), torch)
-    rough = to_dev(smooth_field(n, 2), torch)
-    w = to_dev(_smooth(n, 3), torch)
+    og = oracle.OracleGrid(n, per, (0, 0, 0), [1.0 + d for d in range(3)])
+    hv, hrough, hw = _smooth(n, 1), smooth_field(n, 2), _smooth(n, 3)
+    v, rough, w = to_dev(hv, torch), to_dev(hrough, torch), to_dev(hw, torch)
     cases = []
     for d in range(3):
         if n[d] == 1:
             continue
-        cases += [("d1 %d" % d, lambda g, d=d: g.d1(d, v), D_TOL), ("d8 %d" % d, lambda g, d=d: g.d8(d, rough), D_TOL),
-                  ("sf %d" % d, lambda g, d=d: g.filter("spectral", v, d), F_TOL),
-                  ("gf %d" % d, lambda g, d=d: g.filter("gaussian", v, d), F_TOL)]
-    cases += [("fbar", lambda g: g.filter("spectral", v), F_TOL), ("ring", lambda g: g.ring(rough), D_TOL),
-              ("div", lambda g: g.div(v, w, v), D_TOL)]
+        cases += [("d1 %d" % d, lambda g, d=d: g.d1(d, v), lambda d=d: og.apply(0, d, hv), D_TOL),
+                  ("d8 %d" % d, lambda g, d=d: g.d8(d, rough), lambda d=d: og.dd8(d, hrough), D_TOL),
+                  ("sf %d" % d, lambda g, d=d: g.filter("spectral", v, d), lambda d=d: og.sfilterdir(hv, d), F_TOL),
+                  ("gf %d" % d, lambda g, d=d: g.filter("gaussian", v, d), lambda d=d: og.gfilterdir(hv, d), F_TOL)]
+    cases += [("fbar", lambda g: g.filter("spectral", v), lambda: og.sfilter(hv), F_TOL),
+              ("ring", lambda g: g.ring(rough), lambda: og.ring(hrough, 2), D_TOL),
+              ("div", lambda g: g.div(v, w, v), lambda: og.div(hv, hw, hv), D_TOL)]
     bad = []
-    for name, f, tol in cases:
-        ref = to_host(f(g64))
-        ed, e32 = rel_l2(to_host(f(gd)), ref), rel_l2(to_host(f(g32)), ref)
-        print("%-6s dense %.2e  fp32-banded %.2e  (tol %.0e)" % (name, ed, e32, tol))
-        if not ed < tol:
-            bad.append((name, ed, tol))
+    for name, f, fo, tol in cases:
+        ref = fo()
+        dense = to_host(f(gd))
+        ed, e32 = rel_l2(dense, ref), rel_l2(to_host(f(g32)), ref)
+        ed64 = rel_l2(dense, to_host(f(g64)))
+        print("%-6s dense vs oracle %.2e (vs FP64 banded %.2e)  fp32-banded vs oracle %.2e  (tol %.0e)"
+              % (name, ed, ed64, e32, tol))
+        if not (ed < tol and ed64 < tol):
+            bad.append((name, ed, ed64, tol))
     torch.cuda.synchronize()
     assert _status(gd) == 0
     assert not bad, bad

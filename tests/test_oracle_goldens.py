@@ -2,7 +2,9 @@
 
 The oracle is a CPU restatement of parcop and of pyranda's Python driver; these
 tests pin it to the values the reference test-suite records, with the
-reference's tolerance (1e-4 relative, tests/run_tests.py:84).
+reference's tolerance (1e-4 relative, tests/run_tests.py:84): its golden
+scalars and its 2-D profile baselines (tests/baselines/*.dat, copied into
+tests/golden/ by tests/golden/make_golden.py).
 """
 import json
 import os
@@ -90,3 +92,33 @@ def test_second_and_fourth_derivatives(oracle):
     assert numpy.abs(g.d2(1, q) + 1.0).max() < 1e-10
     assert numpy.abs(g.laplacian(q) - 5.0).max() < 1e-10
     assert numpy.abs(g.dd4(2, q)).max() == 0.0      # constant along the periodic z lines
+
+
+def _bc_ts(s):
+    s.addPackage("BC")
+    s.addPackage("Timestep")
+
+
+GOLDEN_DIR = os.path.join(os.path.dirname(__file__), "golden")
+
+
+@pytest.mark.parametrize("n", [64, 128])
+def test_euler_2d_profile(oracle, n):
+    """tests/cases/test2deuler.py euler-2d-N: the density profile of the 2-D
+    Sod problem (examples/euler.py) against the reference's baseline file,
+    by tests/testObj.py:checkProfile at the reference tolerance 1e-4.  The
+    restatement reproduces the baseline to rounding."""
+    x, rho = scripts.euler_2d(oracle.OracleSim, n, _bc_ts)
+    base = numpy.loadtxt(os.path.join(GOLDEN_DIR, "euler-2d-%d.dat" % n))
+    assert numpy.abs(x - base[0]).max() < 1e-12
+    assert scripts.profile_error(os.path.join(GOLDEN_DIR, "euler-2d-%d.dat" % n), x, rho) < 1e-10
+
+
+def test_kelvin_helmholtz_2d_profile(oracle):
+    """tests/cases/test2deuler.py KH-2d-64: the density profile of
+    examples/KH.py (AFLES terms, courant and diffusion time-step limits,
+    grad) at t = 1.5 against the reference's baseline file."""
+    x, rho = scripts.kelvin_helmholtz_2d(oracle.OracleSim, 64, _bc_ts)
+    path = os.path.join(GOLDEN_DIR, "KelvinHelmholtzKH-2d-64.dat")
+    assert numpy.abs(x - numpy.loadtxt(path)[0]).max() < 1e-12
+    assert scripts.profile_error(path, x, rho) < 1e-10

@@ -261,3 +261,92 @@ def test_vtk_dump(tmp_path, monkeypatch):
     assert numpy.array_equal(u, to_host(ss.variables["u"].data).ravel(order="F").astype(numpy.float32))
     visit = open(os.path.join("TGvortex", "pyranda.visit")).read()
     assert visit.startswith("!NBLOCKS 1 \n!TIME ") and "vis0000001/proc-000000.0000001.vtk" in visit
+
+
+GOLDEN_DIR = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _oracle_bc_ts(s):
+    s.addPackage("BC")
+    s.addPackage("Timestep")
+
+
+@pytest.mark.parametrize("n", [64, 128])
+def test_euler_2d_profile_golden(oracle, n):
+    """tests/cases/test2deuler.py euler-2d-N (examples/euler.py): the GPU
+    pyrandaSim reproduces the reference's density profile within the
+    reference's tolerance (tests/testObj.py:checkProfile < 1e-4), and the
+    oracle's profile to rounding."""
+    from pyranda_gb300 import pyrandaSim
+    path = os.path.join(GOLDEN_DIR, "euler-2d-%d.dat" % n)
+    x, rho = scripts.euler_2d(pyrandaSim, n, _bc_ts, silent=True)
+    err = scripts.profile_error(path, x, rho)
+    assert err < 1.0e-4, err
+    xo, ro = scripts.euler_2d(oracle.OracleSim, n, _oracle_bc_ts)
+    diff = float(numpy.abs(rho - ro).max() / numpy.abs(ro).max())
+    print("euler-2d-%d: profile error %.2e, max difference from the oracle %.2e" % (n, err, diff))
+    assert diff <= 1e-10, diff
+
+
+def test_kelvin_helmholtz_2d_profile_golden(oracle):
+    """tests/cases/test2deuler.py KH-2d-64 (examples/KH.py): AFLES terms,
+    courant and diffusion limits, grad(T): the reference's density profile at
+    t = 1.5 within its tolerance, and the oracle's profile to rounding."""
+    from pyranda_gb300 import pyrandaSim
+    path = os.path.join(GOLDEN_DIR, "KelvinHelmholtzKH-2d-64.dat")
+    x, rho = scripts.kelvin_helmholtz_2d(pyrandaSim, 64, _bc_ts, silent=True)
+    err = scripts.profile_error(path, x, rho)
+    assert err < 1.0e-4, err
+    xo, ro = scripts.kelvin_helmholtz_2d(oracle.OracleSim, 64, _oracle_bc_ts)
+    diff = float(numpy.abs(rho - ro).max() / numpy.abs(ro).max())
+    print("KH-2d-64: profile error %.2e, max difference from the oracle %.2e" % (err, diff))
+    assert diff <= 1e-9, diff
+
+
+def test_tgv_256_fp64_step_matches_oracle(oracle):
+    """The benchmark's workload itself: the 256^3 Taylor-Green vortex at
+    Mach 0.1 / Re 1600 on the plain FP64 path.  The time step and every field
+    after one RK step (five stages, each with the filters, LAD ring operators
+    and the courant / diffusion limits) match the oracle, run on every host
+    core, to relative L2 <= 1e-12."""
+    from pyranda_gb300 import pyrandaSim, problems
+    oracle.set_threads(os.cpu_count() or 1)
+    ss = problems.build_tgv(pyrandaSim, 256, _ts, ns=True, silent=True)
+    so = problems.build_tgv(oracle.OracleSim, 256, lambda s: s.addPackage("Timestep"), ns=True)
+    dt = float(ss.variables["dt"].data) * 0.5
+    dto = float(so.variables["dt"].data) * 0.5
+    assert abs(dt - dto) <= 1e-13 * dto
+    ss.rk4(0.0, dt)
+    so.rk4(0.0, dto)
+    _fields_match(ss, so, ["rho", "rhou", "rhov", "rhow", "Et", "u", "p", "mu", "enst"], scale={"rhow": "rhou"})
+    dtn, dton = float(ss.variables["dt"].data), float(so.variables["dt"].data)
+    assert abs(dtn - dton) <= 1e-12 * dton
+    # beta = gbar(|ring(div)| rho) * 7e-3.  The TGV dilatation div = ux + vy + wz
+    # cancels to a small remainder of O(1) terms, and ring() takes its 8th
+    # derivative, which amplifies the rounding of that remainder.  So: div
+    # agrees to 1e-12 relative to the terms it is made of, and beta agrees to
+    # 1e-12 with the oracle's operators applied to the GPU's own div.
+    div_g = to_host(ss.variables["div"].data)
+    ux = so.variables["ux"].data
+    assert numpy.linalg.norm((div_g - so.variables["div"].data).ravel()) <= 1e-12 * numpy.linalg.norm(ux.ravel())
+    og = so.grid
+    beta_ref = og.gfilter(numpy.abs(og.ring(div_g, 2)) * so.variables["rho"].data) * 7.0e-3
+    e = rel_l2(to_host(ss.variables["beta"].data), beta_ref)
+    assert e <= 1e-12, e
+
+
+def test_shock_interface_full_size_step_matches_oracle(oracle):
+    """The 512x128x128 shock-interface configuration (one-sided x closures,
+    periodic y/z, LAD, extrapolation BCs) on the plain FP64 path: one RK step
+    matches the oracle to relative L2 <= 1e-12."""
+    from pyranda_gb300 import pyrandaSim, problems
+    oracle.set_threads(os.cpu_count() or 1)
+    ss = problems.build_shock(pyrandaSim, 512, 128, 128, _packs, silent=True)
+    so = problems.build_shock(oracle.OracleSim, 512, 128, 128, _oracle_bc_ts)
+    dt = float(ss.variables["dt"].data) * 0.5
+    dto = float(so.variables["dt"].data) * 0.5
+    assert abs(dt - dto) <= 1e-12 * dto
+    ss.rk4(0.0, dt)
+    so.rk4(0.0, dto)
+    _fields_match(ss, so, ["rho", "rhou", "rhov", "rhow", "Et", "u", "p", "mu"],
+                  scale={"rhov": "rhou", "rhow": "rhou"})

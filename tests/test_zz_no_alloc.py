@@ -4,7 +4,9 @@ Some callers cannot call cudaMalloc (their host framework owns all device
 memory, or they never create a pg_handle and so own no workspace).  The
 allocation-free entry point keeps its scratch in a static device array; this
 test calls it through the C ABI and checks it against pg_reduce, twice in a
-row so the second call starts from the scratch the first one left behind.
+row so the second call starts from the scratch the first one left behind, and
+both of them against numpy's sum / max / min of the host copy, including
+inputs that hold infinities and NaN.
 It lives in its own file, collected last, and needs nothing from other tests.
 """
 import ctypes
@@ -63,3 +65,48 @@ def test_noalloc_rejects_oversize():
     rc = lib.pg_reduce_noalloc(1, ctypes.c_void_p(x.data_ptr()), limit, ctypes.c_void_p(out.data_ptr()), _stream())
     L.check(rc, "pg_reduce_noalloc")
     assert float(out) == 0.0
+
+
+def _host_ref(op, a):
+    with numpy.errstate(invalid="ignore", over="ignore"):
+        return (numpy.sum, numpy.max, numpy.min)[op](a)
+
+
+def _same(a, b, scale):
+    if numpy.isnan(b):
+        return numpy.isnan(a)
+    if numpy.isinf(b):
+        return a == b
+    return abs(a - b) <= 1e-13 * max(scale, 1.0)
+
+
+def test_noalloc_and_pg_reduce_follow_numpy_on_special_values():
+    L, lib = _lib()
+    from pyranda_gb300.grid import Grid
+    g = Grid((64, 32, 16), (True, True, True), (0, 0, 0), (1, 1, 1))
+    rng = numpy.random.default_rng(3)
+    n = 64 * 32 * 16
+    base = rng.standard_normal(n)
+    cases = {
+        "all -inf": numpy.full(n, -numpy.inf),
+        "all +inf": numpy.full(n, numpy.inf),
+        "one NaN": numpy.where(numpy.arange(n) == n // 3, numpy.nan, base),
+        "one +inf": numpy.where(numpy.arange(n) == 77, numpy.inf, base),
+        "+inf and -inf": numpy.where(numpy.arange(n) == 5, numpy.inf, numpy.where(numpy.arange(n) == 9, -numpy.inf,
+                                                                                 base)),
+        "random": base,
+    }
+    for name, a in cases.items():
+        x = torch.from_numpy(a).cuda()
+        for op in (0, 1, 2):
+            for call in range(2):  # two calls in a row
+                out = torch.empty((), dtype=torch.float64, device="cuda")
+                rc = lib.pg_reduce_noalloc(op, ctypes.c_void_p(x.data_ptr()), x.numel(),
+                                           ctypes.c_void_p(out.data_ptr()), _stream())
+                L.check(rc, "pg_reduce_noalloc")
+                ref = g.reduce(op, x)
+                torch.cuda.synchronize()
+                want = float(_host_ref(op, a))
+                scale = float(numpy.nansum(numpy.abs(numpy.where(numpy.isfinite(a), a, 0.0))))
+                assert _same(float(out), want, scale), (name, op, call, float(out), want)
+                assert _same(float(ref), want, scale), (name, op, "pg_reduce", float(ref), want)
