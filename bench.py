@@ -75,6 +75,10 @@ def parse():
     p.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "dense", "auto", "fp32-only"],
                    help="profile mode: arithmetic of the profiled step; step mode: 'fp32-only' skips the dense run")
     p.add_argument("--reps", type=int, default=20)
+    p.add_argument("--no-subconfigs", action="store_true",
+                   help="step mode: skip the short ensemble (64 Kelvin-Helmholtz members) and learned-closure "
+                        "sub-lines")
+    p.add_argument("--sub-steps", type=int, default=5, help="step mode: timed steps of each sub-line")
     return p.parse_args()
 
 
@@ -293,6 +297,51 @@ def sweep_roofline(ss, torch, reps=20):
     return res
 
 
+# DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) of one launch
+# of each sweep kernel class at 256^3, from the captures summarised in
+# profiles/ (carried over: measured on the kernel build named in the file, not
+# re-measured by this run).  Key: (operator, direction, dense or banded).
+NCU_TRAFFIC_256 = {
+    ("sf", "y", "dense"): (136362752 + 88161280, "profiles/roofline_traffic_256.md"),
+    ("sf", "y", "banded"): (275878656 + 163471872, "profiles/roofline_traffic_256.md"),
+}
+
+
+def sweep_counts(prec, arith, fusion):
+    """Directional sweeps per RK step of the TGV problem, per (operator,
+    direction), counted at the Grid API of an eager 32^3 copy of the problem
+    (the counts do not depend on the grid size): ddx/ddy/ddz = one d1 sweep,
+    fbar / gbar = three filter sweeps, ring = three d8 sweeps, grad and div =
+    three d1 sweeps."""
+    import collections
+    ss = make_sim(32, prec, graphs=False, fusion=fusion, arith=arith)
+    run_steps(ss, 1)
+    g = ss.grid
+    cnt = collections.Counter()
+    all3 = (0, 1, 2)
+
+    def wrap(name, sweeps):
+        orig = getattr(g, name)
+
+        def counted(*a, **kw):
+            for key in sweeps(*a, **kw):
+                cnt[key] += 1
+            return orig(*a, **kw)
+        setattr(g, name, counted)
+
+    wrap("d1", lambda d, *a, **k: [("d1", d)])
+    wrap("d8", lambda d, *a, **k: [("d8", d)])
+    wrap("filter", lambda kind, v, direction=3, **k: [("sf" if kind == "spectral" else "gf", dd)
+                                                       for dd in (all3 if direction == 3 else (direction,))])
+    wrap("ring", lambda *a, **k: [("d8", d) for d in all3])
+    wrap("ringv", lambda *a, **k: [("d8", d) for d in all3 for _ in range(3)])
+    wrap("grad", lambda *a, **k: [("d1", d) for d in all3])
+    wrap("div", lambda *a, **k: [("d1", d) for d in all3])
+    run_steps(ss, 1)
+    del ss
+    return dict(cnt)
+
+
 def l2_errors(a, b, names):
     out = {}
     for n in names:
@@ -478,6 +527,12 @@ def shock_throughput(args):
 
 
 def ensemble_throughput(args):
+    """The ensemble mode: print ensemble_result() as one JSON line."""
+    print(json.dumps(ensemble_result(args)), flush=True)
+    return 0
+
+
+def ensemble_result(args, one_at_a_time=True):
     """Mpoint-RK-steps/s of 64 Kelvin-Helmholtz runs (n^2, n from {128..512}, seeded) in one ensemble.
 
     Runs the FP64 ensemble eagerly and the fast path (FP32 sweeps, CUDA graph
@@ -549,6 +604,8 @@ def ensemble_throughput(args):
         out["d1_%s_fp32" % "xy"[d]] = {"ms": round(ms, 4), "GB/s": round(16.0 * npts / (ms * 1e-3) / 1e9, 1)}
     del res, g, v, o
     torch.cuda.empty_cache()
+    if not one_at_a_time:
+        return out
     # one member at a time: every distinct size once, weighted by its count
     seq = 0.0
     for n in sorted(set(sizes)):
@@ -569,11 +626,16 @@ def ensemble_throughput(args):
         del ss
     out["one_at_a_time_fp32+graphs"] = {"value": round(npts * k / seq / 1e6, 3), "unit": UNIT,
                                         "ms_per_step": round(seq / k * 1e3, 3)}
-    print(json.dumps(out), flush=True)
-    return 0
+    return out
 
 
 def shock_learned(args):
+    """The shock-learned mode: print shock_learned_result() as one JSON line."""
+    print(json.dumps(shock_learned_result(args)), flush=True)
+    return 0
+
+
+def shock_learned_result(args, train_if_missing=True):
     """C5: the learned LAD closure on the 512x128x128 shock-interface problem.
 
     Both runs use the fast path (FP32 sweeps, FP64 state, one CUDA graph per
@@ -593,6 +655,9 @@ def shock_learned(args):
     if os.path.exists(path):
         model = LL.LadModel.load(path)
         out["model"] = os.path.relpath(path, ROOT)
+    elif not train_if_missing:
+        out["skipped"] = "no trained closure at %s" % os.path.relpath(path, ROOT)
+        return out
     else:
         t0 = time.time()
         shape = tuple(int(x) for x in args.train_shape.split(","))
@@ -730,8 +795,7 @@ def shock_learned(args):
     out["density_l1_vs_plain"] = l1
     out["note"] = ("each closure takes its own CFL/diffusion steps to the same time t_end; the learned "
                    "closure's timing includes its per-step state snapshot and fallback-flag read")
-    print(json.dumps(out), flush=True)
-    return 0
+    return out
 
 
 def main():
@@ -804,6 +868,7 @@ def main():
     # the headline is the fastest path with the requested EOM arithmetic
     best = min((p for p in fast_runs if fast_runs[p]["arith"] == args.fusion_arith), key=lambda p: fast_runs[p]["t"])
     fast, t_fast = fast_runs[best]["sim"], fast_runs[best]["t"]
+    best_prec, best_arith = fast_runs[best]["prec"], fast_runs[best]["arith"]
     launches_per_step, ck = fast_runs[best]["launches"], fast_runs[best]["clocks"]
     value = job_value(npts, k, world, t_fast)
 
@@ -818,7 +883,22 @@ def main():
         t64 = time_steps(plain, k, torch, dist_on)
         t64 = max_over_ranks(t64, dist_on, "cuda")
         extra["fp64_plain"] = {"value": round(job_value(npts, k, world, t64), 4), "unit": UNIT,
-                               "ms_per_step": round(t64 / k * 1e3, 3)}
+                               "ms_per_step": round(t64 / k * 1e3, 3), "form": "eager, unfused EOM arithmetic"}
+        # the plain FP64 form with its EOM arithmetic fused into generated FP64
+        # kernels and the whole step in one CUDA graph (bit-identical results)
+        plain_fg = make_sim(n, "fp64", graphs=True, fusion=True, arith="fp64")
+        run_steps(plain_fg, w)
+        t64g = max_over_ranks(time_steps(plain_fg, k, torch, dist_on), dist_on, "cuda")
+        same = all(torch.equal(plain_fg.variables[nm].data, plain.variables[nm].data)
+                   for nm in ("rho", "rhou", "rhov", "rhow", "Et"))
+        extra["fp64_fused_graph"] = {"value": round(job_value(npts, k, world, t64g), 4), "unit": UNIT,
+                                     "ms_per_step": round(t64g / k * 1e3, 3),
+                                     "form": "fused FP64 EOM kernels, CUDA graph per RK step",
+                                     "bit_identical_to_fp64_plain": bool(same)}
+        extra["speedup"] = {"vs_fp64_plain_eager": round(t64 / t_fast, 3),
+                            "vs_fp64_fused_graph": round(t64g / t_fast, 3)}
+        del plain_fg
+        torch.cuda.empty_cache()
         # accuracy of each fast path: every sim advanced w + k steps from the same IC
         for p, r in fast_runs.items():
             errs = l2_errors(r["sim"], plain, ["rho", "rhou", "rhov", "rhow", "Et"])
@@ -855,25 +935,45 @@ def main():
             del r["sim"]
     torch.cuda.empty_cache()
     sw = sweep_roofline(fast, torch)
-    dom = "sfilter_y"
+    # the dominant sweep kernel: largest share of the step (launches per step x
+    # CUDA-event duration per launch / step time)
+    counts = sweep_counts(fast_runs[best]["prec"], fast_runs[best]["arith"], not args.no_fusion)
+    cls = {"d1": "d1", "d8": "d8", "sf": "sfilter", "gf": "gfilter"}
+    step_s = t_fast / k
+    shares = {}
+    for (op, d), c in counts.items():
+        key = "%s_%s" % (cls[op], "xyz"[d])
+        shares[key] = {"launches_per_step": c, "ms_per_launch": round(sw[key] * 1e3, 4),
+                       "share_of_step": round(c * sw[key] / step_s, 4)}
+    dom = max(shares, key=lambda kk: shares[kk]["share_of_step"])
+    dom_op = {v: kk for kk, v in cls.items()}[dom.split("_")[0]]
+    dom_dir = dom.split("_")[1]
     dur = sw[dom]
     achieved = 16.0 * npts / dur / 1e9
-    dense_y = fast_runs[best]["prec"] != "fp32" and fast.grid.dense_plan()[("sf", "y")]
-    kname = ("dense_kernel<lines as N, dir=y, store, add-back> (tcgen05 kind::tf32, 3 products)" if dense_y
-             else "sweep_kernel<float,r4,periodic,implicit,addback,dir=y>")
-    if dense_y:   # the tensor-core work of the same launch: 3 TF32 products of 2n flops per point
+    plan = fast.grid.dense_plan() if fast_runs[best]["prec"] != "fp32" else {}
+    dense_dom = bool(plan.get((dom_op, dom_dir), False))
+    dirn = {"x": 0, "y": 1, "z": 2}[dom_dir]
+    if dense_dom:
+        kname = ("dense_kernel (tcgen05 kind::tf32, 3 products, TMEM accumulator), %s sweep along %s"
+                 % (dom_op, dom_dir) + ("; after d8_rhs_kernel (exact fixed-point RHS)" if dom_op == "d8" else ""))
+        # the tensor-core work of the same launch: 3 TF32 products of 2n flops per point
         roof_extra = {"tensor_tflops": round(3 * 2 * n * npts / dur / 1e12, 1),
-                      "tensor_peak_note": "TF32 dense nominal ~1100 TFLOP/s (no measured TF32 peak in MEASURED_PEAKS.json)"}
+                      "tensor_peak_note": "TF32 dense nominal ~1100 TFLOP/s (no measured TF32 peak in "
+                                          "MEASURED_PEAKS.json)"}
     else:
+        kname = "sweep_kernel<float, %s, dir=%d> (FP32 banded line solve)" % (dom_op, dirn)
         roof_extra = {}
-    roof = {"bound": "hbm", "kernel": kname,
+    tr = NCU_TRAFFIC_256.get((dom_op, dom_dir, "dense" if dense_dom else "banded")) if n == 256 else None
+    roof = {"bound": "hbm", "kernel": kname, "kernel_class": dom,
             "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
-            # DRAM bytes of one launch of this kernel at 256^3 from one ncu capture (read + write)
-            "traffic": ((136362752 + 88161280) if dense_y else (275878656 + 163471872)) if n == 256 else None,
-            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at 256^3 "
-                              "(profiles/roofline_traffic_256.md)",
+            "traffic": tr[0] if tr else None,
+            "traffic_source": ("carried over from %s: ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
+                               "launch at 256^3 of the kernel build profiled there (not re-measured in this run)"
+                               % tr[1]) if tr else "no ncu capture of this kernel class at this size",
             "algorithmic_bytes_per_launch": 16 * npts,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s",
+            "selection": "largest share of the step among the sweep kernel classes",
+            "kernel_shares": shares,
             "sweep_ms": {kk: round(vv * 1e3, 4) for kk, vv in sw.items()}}
     roof.update(roof_extra)
 
@@ -895,13 +995,33 @@ def main():
     torch.cuda.synchronize()
     t_e2e = max_over_ranks(s.elapsed_time(e) / 1e3, dist_on, "cuda")
     nbytes = len(names) * npts * 8
+    e2e_line = {"value": round(job_value(npts, k, world, t_e2e), 4), "unit": UNIT,
+                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes}
+    final_dense_plan = fast_runs[best]["plan"]
+    del fast, fast_runs
+    torch.cuda.empty_cache()
+
+    # ---- short sub-lines of the other configurations, measured in the same run
+    if not args.no_subconfigs and world == 1:
+        ns = argparse.Namespace(members=64, steps=args.sub_steps, warmup=3, reps=5, fusion_arith=args.fusion_arith)
+        try:
+            extra["subconfig_ensemble_kh64"] = ensemble_result(ns, one_at_a_time=False)
+        except Exception as ex:  # reported, never hides the headline
+            extra["subconfig_ensemble_kh64"] = {"error": repr(ex)[:300]}
+        torch.cuda.empty_cache()
+        ns = argparse.Namespace(model=None, steps=args.sub_steps, warmup=3, reps=5, fusion_arith=args.fusion_arith)
+        try:
+            extra["subconfig_learned_lad_shock"] = shock_learned_result(ns, train_if_missing=False)
+        except Exception as ex:
+            extra["subconfig_learned_lad_shock"] = {"error": repr(ex)[:300]}
+        torch.cuda.empty_cache()
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": k, "warmup": w,
             "ms_per_step": round(t_fast / k * 1e3, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": ("tf32x3 (f32 accumulate) / f32 sweeps, f64 state"
-                                           if fast_runs[best]["prec"] != "fp32" else "f32 sweeps / f64 state"),
+                                           if best_prec != "fp32" else "f32 sweeps / f64 state"),
             "data": "synthetic (Taylor-Green initial condition, Mach 0.1)",
             "config": {"workload": "compressible Taylor-Green vortex %d^3 periodic, Mach 0.1, Re 1600, LAD + compact filters, "
                                    "LSRK(5,4), CFL 0.5" % n,
@@ -910,15 +1030,15 @@ def main():
                                          "filters), d8 as A^-1 on its exact fixed-point RHS",
                                 "auto": "per operator and direction the faster of dense split-TF32 and FP32 banded "
                                         "(autotuned on the grid)",
-                                "fp32": "fp32 banded sweeps"}[fast_runs[best]["prec"]]
+                                "fp32": "fp32 banded sweeps"}[best_prec]
                                + ", FP64 state, fused EOM arithmetic in %s, CUDA graph per RK step"
-                               % fast_runs[best]["arith"].upper(),
+                               % best_arith.upper(),
+                       "dense_plan": final_dense_plan,
                        "l2": "inputs larger than L2 (~40 fields of %d MiB)" % (npts * 8 >> 20),
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": roof,
             "cpu_baseline": cpu,
-            "e2e": {"value": round(job_value(npts, k, world, t_e2e), 4), "unit": UNIT,
-                    "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+            "e2e": e2e_line,
             "gpu_launches": int(launches_per_step * k),
             "clocks": ck,
         }
