@@ -72,8 +72,10 @@ def parse():
     p.add_argument("--save-model", default=None, help="shock-learned: where a newly trained closure is saved "
                                                       "(default pyranda_gb300/_build/lad_shock_trained.npz)")
     p.add_argument("--members", type=int, default=64, help="ensemble mode: number of members")
-    p.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "dense", "auto", "fp32-only"],
-                   help="profile mode: arithmetic of the profiled step; step mode: 'fp32-only' skips the dense run")
+    p.add_argument("--precision", default="fp32",
+                   choices=["fp32", "fp64", "dense", "auto", "fp32-only", "fp32-split", "fp64-split"],
+                   help="profile mode: arithmetic of the profiled step; step mode: 'fp32-only' skips the dense run; "
+                        "kernels mode: '-split' runs the split-line banded sweeps")
     p.add_argument("--reps", type=int, default=20)
     p.add_argument("--no-subconfigs", action="store_true",
                    help="step mode: skip the short ensemble (64 Kelvin-Helmholtz members) and learned-closure "
@@ -367,13 +369,16 @@ def momentum_error(a, b, names=("rhou", "rhov", "rhow")):
 
 
 def sweeps_only(args):
-    """Per-sweep CUDA-event timings on one periodic n^3 TGV field, both precisions."""
+    """Per-sweep CUDA-event timings on one periodic n^3 TGV field: FP32 banded (one thread per line and split
+    lines), dense split-TF32 and FP64 banded."""
     import torch
     torch.cuda.set_device(0)
     npts = args.n ** 3
     out = {"n": args.n}
-    for prec in ("fp32", "dense", "fp64"):
-        ss = make_sim(args.n, prec, graphs=False)
+    for prec in ("fp32", "fp32-split", "dense", "fp64"):
+        ss = make_sim(args.n, prec.split("-")[0], graphs=False)
+        if prec.endswith("split"):
+            ss.grid.set_line_split(True)
         sw = sweep_roofline(ss, torch, reps=args.reps)
         out[prec] = {k: {"ms": round(v * 1e3, 4), "GB/s": round(16.0 * npts / v / 1e9, 1)} for k, v in sw.items()}
         del ss
@@ -388,7 +393,8 @@ def kernel_sweeps(args):
     from pyranda_gb300.grid import Grid
     torch.cuda.set_device(0)
     n = args.n
-    g = Grid((n, n, n), (True, True, True), (0, 0, 0), (2 * math.pi * (n - 1) / n,) * 3, precision=args.precision)
+    g = Grid((n, n, n), (True, True, True), (0, 0, 0), (2 * math.pi * (n - 1) / n,) * 3,
+             precision=args.precision.split("-")[0], line_split=args.precision.endswith("split"))
     v = g.mesh(0)
     v.copy_(torch.sin(v) + 2.0)
     out = g.empty()
@@ -863,8 +869,7 @@ def main():
         t = max_over_ranks(t, dist_on, "cuda")
         key = prec if arith == args.fusion_arith else "%s+%s-eom" % (prec, arith)
         fast_runs[key] = {"sim": sim, "t": t, "launches": lps, "clocks": ck_, "arith": arith, "prec": prec,
-                           "plan": ({"%s_%s" % k: v for k, v in sim.grid.dense_plan().items()}
-                                    if prec != "fp32" else None)}
+                           "plan": {"%s_%s" % k: v for k, v in sim.grid.sweep_plan().items()}}
     # the headline is the fastest path with the requested EOM arithmetic
     best = min((p for p in fast_runs if fast_runs[p]["arith"] == args.fusion_arith), key=lambda p: fast_runs[p]["t"])
     fast, t_fast = fast_runs[best]["sim"], fast_runs[best]["t"]
@@ -950,8 +955,8 @@ def main():
     dom_dir = dom.split("_")[1]
     dur = sw[dom]
     achieved = 16.0 * npts / dur / 1e9
-    plan = fast.grid.dense_plan() if fast_runs[best]["prec"] != "fp32" else {}
-    dense_dom = bool(plan.get((dom_op, dom_dir), False))
+    form = fast.grid.sweep_plan()[(dom_op, dom_dir)]
+    dense_dom = form == "dense"
     dirn = {"x": 0, "y": 1, "z": 2}[dom_dir]
     if dense_dom:
         kname = ("dense_kernel (tcgen05 kind::tf32, 3 products, TMEM accumulator), %s sweep along %s"
@@ -960,10 +965,14 @@ def main():
         roof_extra = {"tensor_tflops": round(3 * 2 * n * npts / dur / 1e12, 1),
                       "tensor_peak_note": "TF32 dense nominal ~1100 TFLOP/s (no measured TF32 peak in "
                                           "MEASURED_PEAKS.json)"}
-    else:
-        kname = "sweep_kernel<float, %s, dir=%d> (FP32 banded line solve)" % (dom_op, dirn)
+    elif form == "split":
+        kname = ("split_kernel<float, %s, dir=%d> (split-line banded solve: 32-point segments joined by the "
+                 "reduced system, tile of lines in shared memory)" % (dom_op, dirn))
         roof_extra = {}
-    tr = NCU_TRAFFIC_256.get((dom_op, dom_dir, "dense" if dense_dom else "banded")) if n == 256 else None
+    else:
+        kname = "sweep_kernel<float, %s, dir=%d> (FP32 banded line solve, one thread per line)" % (dom_op, dirn)
+        roof_extra = {}
+    tr = NCU_TRAFFIC_256.get((dom_op, dom_dir, form)) if n == 256 else None
     roof = {"bound": "hbm", "kernel": kname, "kernel_class": dom,
             "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
             "traffic": tr[0] if tr else None,
@@ -1028,12 +1037,12 @@ def main():
                        "grid": [n, n, n],
                        "path": {"dense": "dense split-TF32 tensor-core operators (d1, compact and Gaussian "
                                          "filters), d8 as A^-1 on its exact fixed-point RHS",
-                                "auto": "per operator and direction the faster of dense split-TF32 and FP32 banded "
-                                        "(autotuned on the grid)",
+                                "auto": "per operator and direction the fastest of dense split-TF32, FP32 banded "
+                                        "(one thread per line) and FP32 split-line banded (autotuned on the grid)",
                                 "fp32": "fp32 banded sweeps"}[best_prec]
                                + ", FP64 state, fused EOM arithmetic in %s, CUDA graph per RK step"
                                % best_arith.upper(),
-                       "dense_plan": final_dense_plan,
+                       "sweep_plan": final_dense_plan,
                        "l2": "inputs larger than L2 (~40 fields of %d MiB)" % (npts * 8 >> 20),
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": roof,

@@ -55,8 +55,9 @@ typedef enum {
  * fixed-point RHS; the FP32 banded sweeps elsewhere; the filters' add-back
  * of v stays in FP64.  PG_AUTO builds the same tables and
  * then, per operator and direction, times the dense kernel against the FP32
- * banded sweep on the handle's own grid and keeps the faster.  Selecting
- * either builds the tables once (allocates and synchronises). */
+ * banded sweep and the FP32 split-line sweep (pg_set_line_split) on the
+ * handle's own grid and keeps the fastest.  Selecting either builds the
+ * tables once (allocates and synchronises). */
 typedef enum { PG_FP64 = 0, PG_FP32 = 1, PG_DENSE = 2, PG_AUTO = 3 } pg_precision;
 
 typedef enum { PG_SPECTRAL = 0, PG_GAUSSIAN = 1 } pg_filter_kind;
@@ -107,6 +108,10 @@ int pg_wait_selftest(pg_handle* h, unsigned limit_ms, void* stream);
  * 8192 points; directions beyond that keep mode 0.  Builds its tables on the
  * first call (allocates and synchronises). */
 int pg_set_line_split(pg_handle* h, int mode);
+/* The form of every sweep: plan[op * 3 + dir] = 0 (banded, one thread per
+ * line), 1 (dense tensor-core kernel) or 2 (split-line banded), for op 0 d1,
+ * 1 d8, 2 compact filter, 3 Gaussian filter, 4 d2, 5 d4. */
+int pg_sweep_plan(const pg_handle* h, int* plan);
 /* The sweep plan of PG_DENSE / PG_AUTO: plan[op * 3 + dir] = 1 where the
  * dense kernel runs (op 0 d1, 1 d8, 2 compact filter, 3 Gaussian filter). */
 int pg_dense_plan(const pg_handle* h, int* plan);

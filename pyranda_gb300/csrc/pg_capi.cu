@@ -799,10 +799,11 @@ int set_line_split(Ctx& c, const std::vector<GridInfo>& g, int mode) {
 int dense_sweep(Ctx& c, int kind, int dir, const double* in, double* out, int epi, int scale_pow, void* st,
                 bool emax_ready);
 
-// Autotuning of PG_AUTO: for every (operator, direction) with a dense form,
-// time the dense kernel and the FP32 banded sweep on this grid (CUDA events,
-// median of 3 after one warm-up launch each) and keep the faster.
-int autotune_dense(Ctx& c) {
+// Autotuning of PG_AUTO: for every (operator, direction), time each sweep
+// form the grid has -- the dense tensor-core kernel, the FP32 banded sweep
+// with one thread per line, the FP32 split-line sweep -- on this grid (CUDA
+// events, median of 3 after one warm-up launch each) and keep the fastest.
+int autotune_sweeps(Ctx& c) {
   double* out = nullptr;
   cudaEvent_t e0, e1;
   if (cudaMalloc(&out, (size_t)c.npts * sizeof(double)) != cudaSuccess) {
@@ -815,18 +816,28 @@ int autotune_dense(Ctx& c) {
   int rc = PG_OK;
   for (int k = 0; k < OPK_COUNT && rc == PG_OK; k++)
     for (int d = 0; d < 3 && rc == PG_OK; d++) {
-      DenseSet& ds = c.dsets[k][d];
-      c.use_dense[k][d] = ds.ok;
-      if (!ds.ok) continue;
-      float t[2];
-      for (int way = 0; way < 2 && rc == PG_OK; way++) {
+      const DenseSet& ds = c.dsets[k][d];
+      const SplitSet& ss = c.splits[PG_FP32][k][d];
+      const OpRef& op = c.ops[PG_FP32][k][d];
+      c.use_dense[k][d] = false;
+      c.use_split[PG_FP32][k][d] = false;
+      if (op.null_op) continue;
+      const bool have[3] = {ds.ok, true, c.split_built && ss.ok};
+      if (!have[0] && !have[2]) continue;
+      float t[3] = {INFINITY, INFINITY, INFINITY};
+      for (int way = 0; way < 3 && rc == PG_OK; way++) {
+        if (!have[way]) continue;
         float best[3];
         for (int rep = 0; rep < 4 && rc == PG_OK; rep++) {
           cudaEventRecord(e0, 0);
-          if (way == 0) rc = dense_sweep(c, k, d, c.work, out, EPI_STORE, 0, nullptr, false);
-          else {
-            SweepLaunch s{c.work, out, c.work2, &c.ops[PG_FP32][k][d], d, EPI_STORE, 0, c.emax, c.moff};
+          if (way == 0) {
+            rc = dense_sweep(c, k, d, c.work, out, EPI_STORE, 0, nullptr, false);
+          } else if (way == 1) {
+            SweepLaunch s{c.work, out, c.work2, &op, d, EPI_STORE, 0, c.emax, c.moff};
             rc = launch_sweep(PG_FP32, s, nullptr);
+          } else {
+            if (k == OPK_D8 && op.exact) rc = launch_max_exponent(c.work, c.moff, c.nmem, c.emax, nullptr);
+            if (rc == PG_OK) rc = launch_split(PG_FP32, op, ss, c.work, out, d, EPI_STORE, 0, c.emax, nullptr);
           }
           cudaEventRecord(e1, 0);
           cudaEventSynchronize(e1);
@@ -835,7 +846,9 @@ int autotune_dense(Ctx& c) {
         std::sort(best, best + 3);
         t[way] = best[1];
       }
-      c.use_dense[k][d] = t[0] < t[1];
+      const int win = (t[0] <= t[1] && t[0] <= t[2]) ? 0 : (t[2] < t[1] ? 2 : 1);
+      c.use_dense[k][d] = (win == 0);
+      c.use_split[PG_FP32][k][d] = (win == 2);
     }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -850,14 +863,19 @@ int autotune_dense(Ctx& c) {
 
 // Arithmetic of later sweeps: PG_FP64 / PG_FP32 banded; PG_DENSE (dense
 // split-TF32 operators wherever built, FP32 banded elsewhere); PG_AUTO (per
-// operator and direction the faster of the two, measured on this grid).
+// operator and direction the fastest of dense, FP32 banded and FP32
+// split-line, measured on this grid).
 int set_precision(Ctx& c, const std::vector<GridInfo>& g, int precision) {
   if (precision == PG_DENSE || precision == PG_AUTO) {
     int rc = build_dense(c, g);
     if (rc) return rc;
     c.precision = PG_FP32;
     c.dense = true;
-    if (precision == PG_AUTO) return autotune_dense(c);
+    if (precision == PG_AUTO) {
+      rc = build_split_ctx(c, g);
+      if (rc) return rc;
+      return autotune_sweeps(c);
+    }
     for (int k = 0; k < OPK_COUNT; k++)
       for (int d = 0; d < 3; d++) c.use_dense[k][d] = c.dsets[k][d].ok;
     return PG_OK;
@@ -1101,6 +1119,15 @@ int pg_wait_selftest(pg_handle* h, unsigned limit_ms, void* stream) {
 int pg_set_line_split(pg_handle* h, int mode) {
   if (!h) return PG_EINVAL;
   return set_line_split(h->c, std::vector<GridInfo>{h->g}, mode);
+}
+
+int pg_sweep_plan(const pg_handle* h, int* plan) {
+  if (!h || !plan) return PG_EINVAL;
+  const Ctx& c = h->c;
+  for (int k = 0; k < OPK_COUNT; k++)
+    for (int d = 0; d < 3; d++)
+      plan[k * 3 + d] = (c.dense && c.use_dense[k][d]) ? 1 : (c.use_split[c.precision][k][d] ? 2 : 0);
+  return PG_OK;
 }
 
 int pg_dense_plan(const pg_handle* h, int* plan) {

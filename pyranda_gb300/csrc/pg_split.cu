@@ -34,6 +34,7 @@ namespace pg {
 namespace {
 
 constexpr int kSplitThreads = 256;
+constexpr int kBatch = 8;  // global loads a thread has in flight in the load and store phases
 
 struct SParams {
   const double* in;  // may equal out: a CTA reads all of its lines before it writes any
@@ -81,7 +82,7 @@ __host__ __device__ inline size_t split_smem(int n, int S, int nl) {
 }
 
 template <typename T, int KIND, bool PER, bool IMPL, bool ADDBACK, int DIR, int EPI, typename TR>
-__global__ void __launch_bounds__(kSplitThreads) split_kernel(const SParams P) {
+__global__ void __launch_bounds__(kSplitThreads, 3) split_kernel(const SParams P) {
   constexpr bool kExact = std::is_same<TR, long long>::value;
   using Raw = typename std::conditional<kExact, double, T>::type;
   using W = typename WeightOf<TR>::type;
@@ -108,19 +109,37 @@ __global__ void __launch_bounds__(kSplitThreads) split_kernel(const SParams P) {
   }
   __syncthreads();
 
-  // 1. load the tile (every input value of these lines is read before any output is written)
-  if (DIR == 0) {
-    for (int l = warp; l < nl; l += nw) {
-      const double* src = P.in + sbase[l];
-      Raw* dst = sv + l * ld;
-#pragma unroll 4
-      for (int p = lane; p < n; p += 32) dst[p] = to_raw<Raw>(__ldg(src + p));
-    }
-  } else {
-    for (int p = warp; p < n; p += nw) {
-      const long long o = (long long)p * st;
-#pragma unroll 2
-      for (int l = lane; l < nl; l += 32) sv[l * ld + p] = to_raw<Raw>(__ldg(P.in + sbase[l] + o));
+  // 1. load the tile (every input value of these lines is read before any output is written).
+  // Element e of the tile is (slow, fast) = (e / fe, e % fe) with the fast index the one that is
+  // contiguous in memory (x: the position along the line; y, z: the line), so consecutive threads
+  // read consecutive addresses; each thread issues kBatch loads before it stores any of them.
+  const int fe = (DIR == 0) ? n : nl;
+  const int NE = n * nl;  // elements of the tile
+  const int qs = kSplitThreads / fe, qr = kSplitThreads % fe;
+  {
+    int es = tid / fe, ef = tid % fe;  // (slow, fast) of element tid
+    for (int e0 = tid; e0 < NE; e0 += kSplitThreads * kBatch) {
+      double v[kBatch];
+      int so_[kBatch], fo_[kBatch];
+#pragma unroll
+      for (int k = 0; k < kBatch; k++) {
+        so_[k] = es;
+        fo_[k] = ef;
+        const int li = (DIR == 0) ? es : ef, pi = (DIR == 0) ? ef : es;
+        v[k] = (e0 + k * kSplitThreads < NE) ? __ldg(P.in + sbase[li] + (long long)pi * st) : 0.0;
+        ef += qr;
+        es += qs;
+        if (ef >= fe) {
+          ef -= fe;
+          es++;
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < kBatch; k++)
+        if (e0 + k * kSplitThreads < NE) {
+          const int li = (DIR == 0) ? so_[k] : fo_[k], pi = (DIR == 0) ? fo_[k] : so_[k];
+          sv[li * ld + pi] = to_raw<Raw>(v[k]);
+        }
     }
   }
   __syncthreads();
@@ -144,23 +163,7 @@ __global__ void __launch_bounds__(kSplitThreads) split_kernel(const SParams P) {
     const float wi = kExact ? wsc * (float)op.iw[0] : 0.0f;
     constexpr int H = (KIND == 4) ? 4 : 3;
     T z1 = T(0), z2 = T(0);
-    for (int i = a; i < b; i++) {
-      T r;
-      if (i < 4 || i >= n - 4) {
-        r = solve_value(edge_rhs<TR, KIND, PER, W>(ln, i, R), E, wsc);
-      } else if constexpr (kExact) {
-        // iw[0] x the 8th difference (1, -8, 28, -56, 70, -56, 28, -8, 1), exact in 64-bit integers
-        const long long c8[9] = {1, -8, 28, -56, 70, -56, 28, -8, 1};
-        long long s = 0;
-#pragma unroll
-        for (int k = 0; k < 9; k++) s += c8[k] * ln.v(i - 4 + k);
-        r = fixed_to_float(s, E, wi);
-      } else {
-        TR win[kRing];
-#pragma unroll
-        for (int k = 0; k < 2 * H + 1; k++) win[k] = ln.v(i - H + k);
-        r = solve_value(ring_rhs<TR, KIND>(win, 0, ai), E, wsc);
-      }
+    auto put = [&](int i, T r) {
       if (IMPL) {  // forward substitution of the segment block (Crout: z = rho r - alpha z1 - beta z2)
         const V4<T> f = V4<T>::ld(C + i * 12);
         T z = f.a * r;
@@ -171,7 +174,33 @@ __global__ void __launch_bounds__(kSplitThreads) split_kernel(const SParams P) {
         r = z;
       }
       wl[i] = r;
+    };
+    auto edge = [&](int i) { return solve_value(edge_rhs<TR, KIND, PER, W>(ln, i, R), E, wsc); };
+    // rows 0..3 and n-4..n-1 take the edge formulas; the rows between are interior
+    const int ia = max(a, 4), ib = min(b, n - 4);
+    int i = a;
+    for (; i < b && i < ia; i++) put(i, edge(i));
+    if (ia < ib) {
+      if constexpr (kExact) {
+        // iw[0] x the 8th difference, exact in 64-bit integers, kept by a cascade of differences
+        Cascade cas{};
+#pragma unroll
+        for (int k = 0; k < 8; k++) cas.push(ln.v(ia - 4 + k));
+        for (i = ia; i < ib; i++) put(i, fixed_to_float(cas.push(ln.v(i + 4)), E, wi));
+      } else {
+        TR win[kRing];  // the RHS window of row i: win[k] = v(i - H + k)
+#pragma unroll
+        for (int k = 0; k < 2 * H; k++) win[k] = ln.v(ia - H + k);
+        for (i = ia; i < ib; i++) {
+          win[2 * H] = ln.v(i + H);
+          put(i, solve_value(ring_rhs<TR, KIND>(win, 0, ai), E, wsc));
+#pragma unroll
+          for (int k = 0; k < 2 * H; k++) win[k] = win[k + 1];
+        }
+      }
+      i = ib;
     }
+    for (; i < b; i++) put(i, edge(i));
     if (IMPL) {  // backward substitution with the unit upper factor
       T y1 = T(0), y2 = T(0);
       for (int i = b - 1; i >= a; i--) {
@@ -224,29 +253,33 @@ __global__ void __launch_bounds__(kSplitThreads) split_kernel(const SParams P) {
   }
   __syncthreads();
 
-  // 4. store with the fused epilogue
+  // 4. store with the fused epilogue, in the order of the load (inputs of the epilogue batched)
   constexpr bool kReadOut = (EPI == EPI_ADD || EPI == EPI_RING_MAX);
   const double sc = (P.scale_pow == 2) ? op.dm * op.dm : (P.scale_pow == 1 ? op.dm : 1.0);
-  if (DIR == 0) {
-    for (int l2 = warp; l2 < nl; l2 += nw) {
-      const long long base = sbase[l2];
-      const T* src = sw + l2 * ld;
-      for (int p = lane; p < n; p += 32) {
-        const long long g = base + p;
-        const double vin = ADDBACK ? P.in[g] : 0.0;
-        const double o = kReadOut ? P.out[g] : 0.0;
-        P.out[g] = epilogue<EPI>(to_f64<T>(src[p]), vin, o, sc, ADDBACK);
+  {
+    int es = tid / fe, ef = tid % fe;
+    for (int e0 = tid; e0 < NE; e0 += kSplitThreads * kBatch) {
+      long long g[kBatch];
+      double vin[kBatch], o[kBatch];
+      T r[kBatch];
+#pragma unroll
+      for (int k = 0; k < kBatch; k++) {
+        const int li = (DIR == 0) ? es : ef, pi = (DIR == 0) ? ef : es;
+        const bool ok = e0 + k * kSplitThreads < NE;
+        g[k] = ok ? sbase[li] + (long long)pi * st : -1;
+        r[k] = ok ? sw[li * ld + pi] : T(0);
+        vin[k] = (ADDBACK && ok) ? P.in[g[k]] : 0.0;
+        o[k] = (kReadOut && ok) ? P.out[g[k]] : 0.0;
+        ef += qr;
+        es += qs;
+        if (ef >= fe) {
+          ef -= fe;
+          es++;
+        }
       }
-    }
-  } else {
-    for (int p = warp; p < n; p += nw) {
-      const long long off = (long long)p * st;
-      for (int l2 = lane; l2 < nl; l2 += 32) {
-        const long long g = sbase[l2] + off;
-        const double vin = ADDBACK ? P.in[g] : 0.0;
-        const double o = kReadOut ? P.out[g] : 0.0;
-        P.out[g] = epilogue<EPI>(to_f64<T>(sw[l2 * ld + p]), vin, o, sc, ADDBACK);
-      }
+#pragma unroll
+      for (int k = 0; k < kBatch; k++)
+        if (g[k] >= 0) P.out[g[k]] = epilogue<EPI>(to_f64<T>(r[k]), vin[k], o[k], sc, ADDBACK);
     }
   }
 }

@@ -109,6 +109,14 @@ class Grid:
         return {(op, "xyz"[d]): bool(plan[k * 3 + d]) for k, op in enumerate(("d1", "d8", "sf", "gf"))
                 for d in range(3)}
 
+    def sweep_plan(self):
+        """{(operator, direction): 'banded' | 'dense' | 'split'} (operators 'd1', 'd8', 'sf', 'gf', 'd2', 'd4')."""
+        plan = (ctypes.c_int * 18)()
+        _lib.check(self.lib.pg_sweep_plan(self.h, plan), "pg_sweep_plan")
+        names = ("banded", "dense", "split")
+        return {(op, "xyz"[d]): names[plan[k * 3 + d]] for k, op in enumerate(("d1", "d8", "sf", "gf", "d2", "d4"))
+                for d in range(3)}
+
     def set_precision(self, precision):
         self.precision = precision
         _lib.check(self.lib.pg_set_precision(self.h, _lib.precision_code(precision)),
