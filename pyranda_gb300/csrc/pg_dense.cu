@@ -143,20 +143,6 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* r) {
   for (int i = 0; i < 8; i++) r[i] = __uint_as_float(u[i]);
 }
 
-// FP64 -> FP32 value + FP32 residual, without the FP64 pipe: hi is d2f_bits(d)
-// and r = d - hi is read from the 29 mantissa bits hi dropped (minus 2^29 when
-// hi rounded up), scaled by the exponent.  hi + r carries ~48 bits of d;
-// residuals of |d| < 2^-76 flush to zero.
-__device__ __forceinline__ float2 split_f64(double d) {
-  const unsigned dh = (unsigned)__double2hiint(d), dl = (unsigned)__double2loint(d);
-  const int e = (int)((dh >> 20) & 0x7ffu);
-  const int low = (int)((dl & 0x1FFFFFFFu) - (((dl >> 28) & 1u) << 29));
-  float r = (float)low * __uint_as_float((unsigned)max(e - 948, 0) << 23);
-  r = (e >= 948) ? r : 0.0f;
-  r = (dh >> 31) ? -r : r;
-  return make_float2(d2f_bits(d), r);
-}
-
 // TF32 of an FP32 value: round the low 13 mantissa bits to nearest (ties away).
 __device__ __forceinline__ uint32_t tf32_bits(float x) {
   return (__float_as_uint(x) + 0x1000u) & 0xFFFFE000u;

@@ -25,9 +25,10 @@
 //      add-back in FP64, accumulate, ring max).
 // No scratch field is written or read back, the serial chain of a thread is
 // one segment (not one line) long, and a line may be longer than the dense
-// path's 1024 points (up to 256 segments).  T = float is the fast path's
-// arithmetic (d8 with the exact 64-bit fixed-point RHS: the tile keeps the
-// raw FP64 values); T = double follows the reference arithmetic.
+// path's 1024 points (up to 256 segments).  The tile keeps the raw FP64
+// values.  T = float is the fast path's arithmetic: RHS differences from FP32
+// hi + lo pairs of the FP64 values, d8 with the exact 64-bit fixed-point RHS,
+// FP32 solves; T = double follows the reference arithmetic.
 #include "pg_sweep.cuh"
 
 namespace pg {
@@ -46,45 +47,64 @@ struct SParams {
   const int* emax;
 };
 
-template <typename Raw>
-__device__ __forceinline__ Raw to_raw(double v);
-template <>
-__device__ __forceinline__ double to_raw<double>(double v) { return v; }
-template <>
-__device__ __forceinline__ float to_raw<float>(double v) { return d2f_bits(v); }
-
-// a staged value as the RHS arithmetic's type
+// One line of the tile in shared memory (raw FP64 values), read as the RHS
+// arithmetic's type -- the accessors edge_rhs uses.
 template <typename TR>
-__device__ __forceinline__ TR raw_as(double x, int E) { return load_as<TR>(x, E); }
-template <typename TR>
-__device__ __forceinline__ TR raw_as(float x, int) { return (TR)x; }
-
-// One line of the tile in shared memory, with the accessors edge_rhs uses.
-template <typename TR, typename Raw>
 struct SLine {
-  const Raw* v0;
+  const double* v0;
   int n, e;
-  __device__ __forceinline__ TR v(int p) const { return raw_as<TR>(v0[p], e); }
+  __device__ __forceinline__ TR v(int p) const { return load_as<TR>(v0[p], e); }
   __device__ __forceinline__ TR w(int p) const {
     const int q = p < 0 ? p + n : (p >= n ? p - n : p);
     return v(q);
   }
 };
 
+// The RHS of an interior row from its window of 2H+1 values (win[H] = the
+// row's own point), in the difference form of the reference
+// (compact_d1.f90:152-160, compact_r3.f90, compact_r4.f90:144-156).
+// Values are FP64 (T = double) or FP32 hi + lo pairs (T = float): every
+// difference v_k - v_c is (hi_k - hi_c) + (lo_k - lo_c), exact to FP32
+// rounding of the difference itself, so a large mean or a slowly varying
+// field costs no accuracy before the weights are applied.
+template <int KIND>
+__device__ __forceinline__ double window_rhs(const double* v, const double* ai) {
+  if (KIND == 1) return ai[4] * (v[4] - v[2]) + ai[5] * (v[5] - v[1]) + ai[6] * (v[6] - v[0]);
+  constexpr int H = (KIND == 4) ? 4 : 3;
+  double s = 0.0;
+#pragma unroll
+  for (int l = 0; l < 2 * H + 1; l++)
+    if (l != H) s += (v[l] - v[H]) * ai[l];
+  return s;
+}
+template <int KIND>
+__device__ __forceinline__ float window_rhs(const float2* v, const float* ai) {
+  auto d = [&](int k, int c) { return (v[k].x - v[c].x) + (v[k].y - v[c].y); };
+  if (KIND == 1) return ai[4] * d(4, 2) + ai[5] * d(5, 1) + ai[6] * d(6, 0);
+  constexpr int H = (KIND == 4) ? 4 : 3;
+  float s = 0.0f;
+#pragma unroll
+  for (int l = 0; l < 2 * H + 1; l++)
+    if (l != H) s += d(l, H) * ai[l];
+  return s;
+}
+
 __host__ __device__ constexpr size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
 __host__ __device__ inline int row_stride(int n) { return (n & 1) ? n : n + 1; }  // odd: conflict-free columns
 
-template <typename T, typename Raw>
+// Shared memory of one tile: line bases, the tile of raw FP64 values (each
+// slot later holds the thread's own results in place), the segment tips.
+template <typename T>
 __host__ __device__ inline size_t split_smem(int n, int S, int nl) {
   const int ld = row_stride(n);
-  return al16((size_t)nl * 8) + al16((size_t)nl * ld * sizeof(Raw)) + al16((size_t)nl * ld * sizeof(T)) +
-         (size_t)nl * (4 * S + 1) * sizeof(T);
+  return al16((size_t)nl * 8) + al16((size_t)nl * ld * sizeof(double)) + (size_t)nl * (4 * S + 1) * sizeof(T);
 }
 
 template <typename T, int KIND, bool PER, bool IMPL, bool ADDBACK, int DIR, int EPI, typename TR>
 __global__ void __launch_bounds__(kSplitThreads, 3) split_kernel(const SParams P) {
   constexpr bool kExact = std::is_same<TR, long long>::value;
-  using Raw = typename std::conditional<kExact, double, T>::type;
+  constexpr bool kPair = std::is_same<T, float>::value && !kExact;  // FP32 differences from hi + lo pairs
+  constexpr int H = (KIND == 4) ? 4 : 3;
   using W = typename WeightOf<TR>::type;
   extern __shared__ __align__(16) unsigned char s_buf[];
   const SplitTile tile = P.tiles[blockIdx.x];
@@ -93,10 +113,9 @@ __global__ void __launch_bounds__(kSplitThreads, 3) split_kernel(const SParams P
   const int n = op.n, S = so.S, nl = tile.nlines;
   const int ld = row_stride(n), tld = 4 * S + 1;
   long long* sbase = reinterpret_cast<long long*>(s_buf);
-  Raw* sv = reinterpret_cast<Raw*>(s_buf + al16((size_t)nl * 8));
-  T* sw = reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(sv) + al16((size_t)nl * ld * sizeof(Raw)));
-  T* tips = reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(sw) + al16((size_t)nl * ld * sizeof(T)));
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nw = blockDim.x >> 5;
+  double* sv = reinterpret_cast<double*>(s_buf + al16((size_t)nl * 8));
+  T* tips = reinterpret_cast<T*>(reinterpret_cast<unsigned char*>(sv) + al16((size_t)nl * ld * sizeof(double)));
+  const int tid = threadIdx.x;
   const int nx = op.nx, ny = op.ny;
   const long long st = (DIR == 0) ? 1 : (DIR == 1 ? (long long)nx : (long long)nx * ny);
   for (int l = tid; l < nl; l += blockDim.x) {
@@ -138,30 +157,63 @@ __global__ void __launch_bounds__(kSplitThreads, 3) split_kernel(const SParams P
       for (int k = 0; k < kBatch; k++)
         if (e0 + k * kSplitThreads < NE) {
           const int li = (DIR == 0) ? so_[k] : fo_[k], pi = (DIR == 0) ? fo_[k] : so_[k];
-          sv[li * ld + pi] = to_raw<Raw>(v[k]);
+          sv[li * ld + pi] = v[k];
         }
     }
   }
   __syncthreads();
 
-  // 2. RHS and local solve of one segment of one line
+  // 2. thread (line l, segment j): RHS and local solve of rows [a, b).  It first copies what it
+  // reads outside its own rows (the 4 values on each side) and forms the one-sided edge rows, whose
+  // stencils reach 8 points in; after a barrier every thread owns its rows and writes its results
+  // in place of its own input values (slot i of the line holds z_i, then y_i, then x_i, as T).
   const int l = tid % nl, j = tid / nl;
   const bool active = j < S;
   const T* __restrict__ C = reinterpret_cast<const T*>(so.row);  // 12 per position
   const int E = kExact ? __ldg(P.emax + tile.op) : 0;
   const float wsc = kExact ? op.wscale : 1.0f;
-  const W* __restrict__ R = reinterpret_cast<const W*>(kExact ? (const void*)op.rhs_i : op.rhs);
   int a = 0, b = 0;
-  T* wl = sw + l * ld;
+  double* vl = sv + l * ld;
+  T* wl = reinterpret_cast<T*>(vl);  // result of row i at wl[i * kSlot]
+  constexpr int kSlot = sizeof(double) / sizeof(T);
+  double hl[4] = {0.0, 0.0, 0.0, 0.0}, hr[4] = {0.0, 0.0, 0.0, 0.0};
+  T re[8];
+#pragma unroll
+  for (int q = 0; q < 8; q++) re[q] = T(0);
   if (active) {
     a = __ldg(so.start + j);
     b = __ldg(so.start + j + 1);
-    const SLine<TR, Raw> ln{sv + l * ld, n, E};
-    TR ai[9];
 #pragma unroll
-    for (int k = 0; k < 9; k++) ai[k] = kExact ? (TR)op.iw[k] : (TR)op.ri[k];
-    const float wi = kExact ? wsc * (float)op.iw[0] : 0.0f;
-    constexpr int H = (KIND == 4) ? 4 : 3;
+    for (int k = 0; k < 4; k++) {
+      int p = a - 4 + k;
+      p = p < 0 ? p + n : p;
+      hl[k] = (PER || a - 4 + k >= 0) ? vl[p] : 0.0;
+      p = b + k;
+      p = p >= n ? p - n : p;
+      hr[k] = (PER || b + k < n) ? vl[p] : 0.0;
+    }
+    if (!PER) {  // the one-sided rows 0..3 and n-4..n-1 (reference formulas, compact_d1.f90:131-180,
+                 // compact_r4.f90:120-125,166-171), only in the first and last segment
+      if (kExact) {
+        const SLine<long long> ln{vl, n, E};
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          const int i = q < 4 ? q : n - 8 + q;
+          if (i >= a && i < b) re[q] = (T)fixed_to_float(edge_rhs<long long, KIND, false, int>(ln, i, op.rhs_i), E, wsc);
+        }
+      } else {  // FP64 arithmetic on the raw values (8 rows of a line)
+        const SLine<double> ln{vl, n, 0};
+        const W* R = reinterpret_cast<const W*>(op.rhs);
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          const int i = q < 4 ? q : n - 8 + q;
+          if (i >= a && i < b) re[q] = (T)edge_rhs<double, KIND, false, W>(ln, i, R);
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (active) {
     T z1 = T(0), z2 = T(0);
     auto put = [&](int i, T r) {
       if (IMPL) {  // forward substitution of the segment block (Crout: z = rho r - alpha z1 - beta z2)
@@ -173,50 +225,91 @@ __global__ void __launch_bounds__(kSplitThreads, 3) split_kernel(const SParams P
         z1 = z;
         r = z;
       }
-      wl[i] = r;
+      wl[i * kSlot] = r;
     };
-    auto edge = [&](int i) { return solve_value(edge_rhs<TR, KIND, PER, W>(ln, i, R), E, wsc); };
-    // rows 0..3 and n-4..n-1 take the edge formulas; the rows between are interior
-    const int ia = max(a, 4), ib = min(b, n - 4);
-    int i = a;
-    for (; i < b && i < ia; i++) put(i, edge(i));
+    // rows in order: the lower one-sided rows, the interior rows [ia, ib), the upper one-sided rows
+    const int ia = PER ? a : max(a, 4), ib = PER ? b : min(b, n - 4);
+    const int iv = max(ia, min(ib, b - H));  // interior rows below iv read ahead inside the segment
+    if (!PER) {
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        if (q >= a && q < b) put(q, re[q]);
+    }
+    // the value at ia - H + k (k < 2H): the left halo when the window starts at the segment's first row
+    auto first = [&](int k) -> double { return (ia == a && k < H) ? hl[k + 4 - H] : vl[ia - H + k]; };
     if (ia < ib) {
       if constexpr (kExact) {
         // iw[0] x the 8th difference, exact in 64-bit integers, kept by a cascade of differences
         Cascade cas{};
 #pragma unroll
-        for (int k = 0; k < 8; k++) cas.push(ln.v(ia - 4 + k));
-        for (i = ia; i < ib; i++) put(i, fixed_to_float(cas.push(ln.v(i + 4)), E, wi));
-      } else {
-        TR win[kRing];  // the RHS window of row i: win[k] = v(i - H + k)
+        for (int k = 0; k < 8; k++) cas.push(to_fixed(first(k), E));
+        const float wi = wsc * (float)op.iw[0];
+        int i = ia;
+        for (; i < iv; i++) put(i, fixed_to_float(cas.push(to_fixed(vl[i + 4], E)), E, wi));
 #pragma unroll
-        for (int k = 0; k < 2 * H; k++) win[k] = ln.v(ia - H + k);
-        for (i = ia; i < ib; i++) {
-          win[2 * H] = ln.v(i + H);
-          put(i, solve_value(ring_rhs<TR, KIND>(win, 0, ai), E, wsc));
+        for (int t = 0; t < 4; t++)
+          if (i + t < ib) put(i + t, fixed_to_float(cas.push(to_fixed(hr[t], E)), E, wi));
+      } else if constexpr (kPair) {
+        float ai[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) ai[k] = (float)op.ri[k];
+        float2 win[2 * H + 1];
+#pragma unroll
+        for (int k = 0; k < 2 * H; k++) win[k] = split_f64(first(k));
+        auto row = [&](int i, double next) {
+          win[2 * H] = split_f64(next);
+          put(i, window_rhs<KIND>(win, ai));
 #pragma unroll
           for (int k = 0; k < 2 * H; k++) win[k] = win[k + 1];
-        }
+        };
+        int i = ia;
+        for (; i < iv; i++) row(i, vl[i + H]);
+#pragma unroll
+        for (int t = 0; t < H; t++)
+          if (i + t < ib) row(i + t, hr[t]);
+      } else {
+        double ai[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) ai[k] = op.ri[k];
+        double win[2 * H + 1];
+#pragma unroll
+        for (int k = 0; k < 2 * H; k++) win[k] = first(k);
+        auto row = [&](int i, double next) {
+          win[2 * H] = next;
+          put(i, (T)window_rhs<KIND>(win, ai));
+#pragma unroll
+          for (int k = 0; k < 2 * H; k++) win[k] = win[k + 1];
+        };
+        int i = ia;
+        for (; i < iv; i++) row(i, vl[i + H]);
+#pragma unroll
+        for (int t = 0; t < H; t++)
+          if (i + t < ib) row(i + t, hr[t]);
       }
-      i = ib;
     }
-    for (; i < b; i++) put(i, edge(i));
+    if (!PER) {
+#pragma unroll
+      for (int q = 4; q < 8; q++) {
+        const int i = n - 8 + q;
+        if (i >= a && i < b && i >= ib) put(i, re[q]);
+      }
+    }
     if (IMPL) {  // backward substitution with the unit upper factor
       T y1 = T(0), y2 = T(0);
       for (int i = b - 1; i >= a; i--) {
         const V4<T> g = V4<T>::ld(C + i * 12 + 4);  // u1 u2 . .
-        T y = wl[i];
+        T y = wl[i * kSlot];
         y -= g.b * y2;
         y -= g.a * y1;
-        wl[i] = y;
+        wl[i * kSlot] = y;
         y2 = y1;
         y1 = y;
       }
       T* tp = tips + l * tld + 4 * j;
-      tp[0] = wl[a];
-      tp[1] = wl[a + 1];
-      tp[2] = wl[b - 2];
-      tp[3] = wl[b - 1];
+      tp[0] = wl[a * kSlot];
+      tp[1] = wl[(a + 1) * kSlot];
+      tp[2] = wl[(b - 2) * kSlot];
+      tp[3] = wl[(b - 1) * kSlot];
     }
   }
   __syncthreads();
@@ -243,12 +336,12 @@ __global__ void __launch_bounds__(kSplitThreads, 3) split_kernel(const SParams P
     }
     for (int i = a; i < b; i++) {
       const V4<T> sp = V4<T>::ld(C + i * 12 + 8);  // W_0 W_1 V_0 V_1
-      T x = wl[i];
+      T x = wl[i * kSlot];
       x -= sp.a * q0;
       x -= sp.b * q1;
       x -= sp.c * q2;
       x -= sp.d * q3;
-      wl[i] = x;
+      wl[i * kSlot] = x;
     }
   }
   __syncthreads();
@@ -267,7 +360,7 @@ __global__ void __launch_bounds__(kSplitThreads, 3) split_kernel(const SParams P
         const int li = (DIR == 0) ? es : ef, pi = (DIR == 0) ? ef : es;
         const bool ok = e0 + k * kSplitThreads < NE;
         g[k] = ok ? sbase[li] + (long long)pi * st : -1;
-        r[k] = ok ? sw[li * ld + pi] : T(0);
+        r[k] = ok ? reinterpret_cast<const T*>(sv + li * ld)[pi * kSlot] : T(0);
         vin[k] = (ADDBACK && ok) ? P.in[g[k]] : 0.0;
         o[k] = (kReadOut && ok) ? P.out[g[k]] : 0.0;
         ef += qr;
@@ -286,9 +379,7 @@ __global__ void __launch_bounds__(kSplitThreads, 3) split_kernel(const SParams P
 
 template <typename T, int KIND, bool PER, bool IMPL, bool ADDBACK, int DIR, int EPI, typename TR>
 int launch_s(const SParams& P, const SplitSet& ss, void* stream) {
-  constexpr bool kExact = std::is_same<TR, long long>::value;
-  using Raw = typename std::conditional<kExact, double, T>::type;
-  const size_t smem = (sizeof(Raw) == 8 && sizeof(T) == 4) ? ss.smem_mixed : (sizeof(T) == 8 ? ss.smem64 : ss.smem32);
+  const size_t smem = sizeof(T) == 8 ? ss.smem64 : ss.smem32;
   auto k = split_kernel<T, KIND, PER, IMPL, ADDBACK, DIR, EPI, TR>;
   static size_t attr = 0;
   if (smem > attr) {
@@ -355,9 +446,8 @@ int split_kind(const OpRef& op, const SParams& P, const SplitSet& ss, int dir, i
 
 }  // namespace
 
-size_t split_smem_bytes(int precision, bool exact, int n, int S, int nl) {
-  if (precision == PG_FP64) return split_smem<double, double>(n, S, nl);
-  return exact ? split_smem<float, double>(n, S, nl) : split_smem<float, float>(n, S, nl);
+size_t split_smem_bytes(int precision, bool, int n, int S, int nl) {
+  return precision == PG_FP64 ? split_smem<double>(n, S, nl) : split_smem<float>(n, S, nl);
 }
 
 int launch_split(int precision, const OpRef& op, const SplitSet& ss, const double* in, double* out, int dir, int epi,

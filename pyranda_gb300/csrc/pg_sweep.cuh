@@ -80,6 +80,20 @@ __device__ __forceinline__ double f2d_bits(float x) {
   return __hiloint2double((int)hi, (int)lo);
 }
 
+// FP64 -> FP32 value + FP32 residual, without the FP64 pipe: hi is d2f_bits(d)
+// and r = d - hi is read from the 29 mantissa bits hi dropped (minus 2^29 when
+// hi rounded up), scaled by the exponent.  hi + r carries ~48 bits of d;
+// residuals of |d| < 2^-76 flush to zero.
+__device__ __forceinline__ float2 split_f64(double d) {
+  const unsigned dh = (unsigned)__double2hiint(d), dl = (unsigned)__double2loint(d);
+  const int e = (int)((dh >> 20) & 0x7ffu);
+  const int low = (int)((dl & 0x1FFFFFFFu) - (((dl >> 28) & 1u) << 29));
+  float r = (float)low * __uint_as_float((unsigned)max(e - 948, 0) << 23);
+  r = (e >= 948) ? r : 0.0f;
+  r = (dh >> 31) ? -r : r;
+  return make_float2(d2f_bits(d), r);
+}
+
 // Exact d8 RHS of the FP32 sweeps.  The 8th difference of a smooth field
 // cancels about 40 of its 53 bits, more than FP32 holds.  The d8 weights are
 // integers times one scale (c10d8: 60 x binomial coefficients), so every

@@ -167,3 +167,26 @@ def test_split_tgv_step_matches_oracle(oracle):
     for name in ("rho", "rhou", "rhov", "Et", "p"):
         e = rel_l2(to_host(ss.variables[name].data), so.variables[name].data)
         assert e <= 1e-12, (name, e)
+
+
+def test_split_fp32_differences_keep_a_large_mean(oracle):
+    """A field with a large mean and a small variation (like the Taylor-Green
+    pressure): the FP32 split sweeps take every RHS difference from FP32
+    hi + lo pairs of the FP64 values, so d1 and the compact filter keep the
+    FP32 accuracy of the result itself; rounding the values to FP32 first
+    (the one-thread-per-line FP32 sweeps) loses log2(mean / variation) bits."""
+    from pyranda_gb300.grid import Grid
+    shape, per = (128, 64, 32), (True, True, False)
+    g = _grid(shape, per, "fp32")
+    g32 = Grid(shape, per, (0.0, -0.5, 0.25), (1.0, 2.0, 3.0), precision="fp32")
+    o = oracle.OracleGrid(shape, per, (0.0, -0.5, 0.25), (1.0, 2.0, 3.0))
+    v = numpy.asfortranarray(71.4 + 0.1 * _smooth(shape, 9))
+    dv = to_dev(v, torch)
+    for d in range(3):
+        ref = o.apply(0, d, v)
+        es, e32 = rel_l2(to_host(g.d1(d, dv)), ref), rel_l2(to_host(g32.d1(d, dv)), ref)
+        print("d1 %d: split %.2e  one-thread-per-line %.2e" % (d, es, e32))
+        assert es <= 2e-6, (d, es)
+        ref = o.apply(2, d, v) - v
+        es = rel_l2(to_host(g.filter("spectral", dv, d)) - v, ref)
+        assert es <= 2e-5, ("sf", d, es)
