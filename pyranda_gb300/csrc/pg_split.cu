@@ -230,19 +230,24 @@ __global__ void __launch_bounds__(kSplitThreads, 3) split_kernel(const SParams P
     // rows in order: the lower one-sided rows, the interior rows [ia, ib), the upper one-sided rows
     const int ia = PER ? a : max(a, 4), ib = PER ? b : min(b, n - 4);
     const int iv = max(ia, min(ib, b - H));  // interior rows below iv read ahead inside the segment
-    if (!PER) {
-#pragma unroll
-      for (int q = 0; q < 4; q++)
-        if (q >= a && q < b) put(q, re[q]);
-    }
-    // the value at ia - H + k (k < 2H): the left halo when the window starts at the segment's first row
+    // the value at ia - H + k (k < 2H): the left halo when the window starts at the segment's first row.
+    // The window is primed before the lower one-sided rows store their results over slots 0..3.
     auto first = [&](int k) -> double { return (ia == a && k < H) ? hl[k + 4 - H] : vl[ia - H + k]; };
+    auto lower_edge_rows = [&]() {
+      if (!PER) {
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+          if (q >= a && q < b) put(q, re[q]);
+      }
+    };
+    if (ia >= ib) lower_edge_rows();
     if (ia < ib) {
       if constexpr (kExact) {
         // iw[0] x the 8th difference, exact in 64-bit integers, kept by a cascade of differences
         Cascade cas{};
 #pragma unroll
         for (int k = 0; k < 8; k++) cas.push(to_fixed(first(k), E));
+        lower_edge_rows();
         const float wi = wsc * (float)op.iw[0];
         int i = ia;
         for (; i < iv; i++) put(i, fixed_to_float(cas.push(to_fixed(vl[i + 4], E)), E, wi));
@@ -256,6 +261,7 @@ __global__ void __launch_bounds__(kSplitThreads, 3) split_kernel(const SParams P
         float2 win[2 * H + 1];
 #pragma unroll
         for (int k = 0; k < 2 * H; k++) win[k] = split_f64(first(k));
+        lower_edge_rows();
         auto row = [&](int i, double next) {
           win[2 * H] = split_f64(next);
           put(i, window_rhs<KIND>(win, ai));
@@ -274,6 +280,7 @@ __global__ void __launch_bounds__(kSplitThreads, 3) split_kernel(const SParams P
         double win[2 * H + 1];
 #pragma unroll
         for (int k = 0; k < 2 * H; k++) win[k] = first(k);
+        lower_edge_rows();
         auto row = [&](int i, double next) {
           win[2 * H] = next;
           put(i, (T)window_rhs<KIND>(win, ai));
