@@ -89,6 +89,26 @@ __device__ __forceinline__ float window_rhs(const float2* v, const float* ai) {
   return s;
 }
 
+// A thread's result of row i in the 8-byte slot of its input value: FP64 as
+// is, FP32 as the first half of an 8-byte access (a 4-byte access at an
+// 8-byte stride would meet 2-way bank conflicts across the lanes' rows).
+__device__ __forceinline__ void slot_st(double* p, double v) { *p = v; }
+__device__ __forceinline__ void slot_st(double* p, float v) {
+  asm volatile("st.shared.v2.f32 [%0], {%1, %2};" ::"r"((unsigned)__cvta_generic_to_shared(p)), "f"(v), "f"(0.0f)
+               : "memory");
+}
+template <typename T>
+__device__ __forceinline__ T slot_ld(const double* p);
+template <>
+__device__ __forceinline__ double slot_ld<double>(const double* p) { return *p; }
+template <>
+__device__ __forceinline__ float slot_ld<float>(const double* p) {
+  float a, b;
+  asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(a), "=f"(b) : "r"((unsigned)__cvta_generic_to_shared(p))
+               : "memory");
+  return a;
+}
+
 __host__ __device__ constexpr size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
 __host__ __device__ inline int row_stride(int n) { return (n & 1) ? n : n + 1; }  // odd: conflict-free columns
 
@@ -173,9 +193,7 @@ __global__ void __launch_bounds__(kSplitThreads, 3) split_kernel(const SParams P
   const int E = kExact ? __ldg(P.emax + tile.op) : 0;
   const float wsc = kExact ? op.wscale : 1.0f;
   int a = 0, b = 0;
-  double* vl = sv + l * ld;
-  T* wl = reinterpret_cast<T*>(vl);  // result of row i at wl[i * kSlot]
-  constexpr int kSlot = sizeof(double) / sizeof(T);
+  double* vl = sv + l * ld;  // slot i: the input value, later this thread's result of row i
   double hl[4] = {0.0, 0.0, 0.0, 0.0}, hr[4] = {0.0, 0.0, 0.0, 0.0};
   T re[8];
 #pragma unroll
@@ -225,7 +243,7 @@ __global__ void __launch_bounds__(kSplitThreads, 3) split_kernel(const SParams P
         z1 = z;
         r = z;
       }
-      wl[i * kSlot] = r;
+      slot_st(vl + i, r);
     };
     // rows in order: the lower one-sided rows, the interior rows [ia, ib), the upper one-sided rows
     const int ia = PER ? a : max(a, 4), ib = PER ? b : min(b, n - 4);
@@ -305,18 +323,18 @@ __global__ void __launch_bounds__(kSplitThreads, 3) split_kernel(const SParams P
       T y1 = T(0), y2 = T(0);
       for (int i = b - 1; i >= a; i--) {
         const V4<T> g = V4<T>::ld(C + i * 12 + 4);  // u1 u2 . .
-        T y = wl[i * kSlot];
+        T y = slot_ld<T>(vl + i);
         y -= g.b * y2;
         y -= g.a * y1;
-        wl[i * kSlot] = y;
+        slot_st(vl + i, y);
         y2 = y1;
         y1 = y;
       }
       T* tp = tips + l * tld + 4 * j;
-      tp[0] = wl[a * kSlot];
-      tp[1] = wl[(a + 1) * kSlot];
-      tp[2] = wl[(b - 2) * kSlot];
-      tp[3] = wl[(b - 1) * kSlot];
+      tp[0] = slot_ld<T>(vl + a);
+      tp[1] = slot_ld<T>(vl + a + 1);
+      tp[2] = slot_ld<T>(vl + b - 2);
+      tp[3] = slot_ld<T>(vl + b - 1);
     }
   }
   __syncthreads();
@@ -343,12 +361,12 @@ __global__ void __launch_bounds__(kSplitThreads, 3) split_kernel(const SParams P
     }
     for (int i = a; i < b; i++) {
       const V4<T> sp = V4<T>::ld(C + i * 12 + 8);  // W_0 W_1 V_0 V_1
-      T x = wl[i * kSlot];
+      T x = slot_ld<T>(vl + i);
       x -= sp.a * q0;
       x -= sp.b * q1;
       x -= sp.c * q2;
       x -= sp.d * q3;
-      wl[i * kSlot] = x;
+      slot_st(vl + i, x);
     }
   }
   __syncthreads();
@@ -367,7 +385,7 @@ __global__ void __launch_bounds__(kSplitThreads, 3) split_kernel(const SParams P
         const int li = (DIR == 0) ? es : ef, pi = (DIR == 0) ? ef : es;
         const bool ok = e0 + k * kSplitThreads < NE;
         g[k] = ok ? sbase[li] + (long long)pi * st : -1;
-        r[k] = ok ? reinterpret_cast<const T*>(sv + li * ld)[pi * kSlot] : T(0);
+        r[k] = ok ? slot_ld<T>(sv + li * ld + pi) : T(0);
         vin[k] = (ADDBACK && ok) ? P.in[g[k]] : 0.0;
         o[k] = (kReadOut && ok) ? P.out[g[k]] : 0.0;
         ef += qr;
