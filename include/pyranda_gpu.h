@@ -71,12 +71,26 @@ typedef enum {
   PG_MESH_GRIDLEN = 6, PG_MESH_CELLVOL = 7
 } pg_mesh_var;
 
+/* Boundary codes of a non-periodic end (pyrandaMPI.py:101-131,
+ * compact.f90:77-91). */
+typedef enum { PG_BC_NONE = 0, PG_BC_SYMM = 1, PG_BC_XTND = 2 } pg_bc;
+/* Coordinate systems (patch.f90 coordsys; mesh.f90:190-243). */
+typedef enum { PG_CARTESIAN = 0, PG_CYLINDRICAL = 1 } pg_coordsys;
+
 typedef struct {
   int n[3];        /* nx, ny, nz (global = local: one GPU) */
-  int periodic[3]; /* 1 = PERI, 0 = NONE (one-sided closures) */
+  int periodic[3]; /* 1 = PERI, 0 = non-periodic (ends per bc below) */
   double x1[3];    /* first node coordinate per direction */
   double xn[3];    /* last node coordinate per direction */
   int precision;   /* pg_precision */
+  int bc[3][2];    /* pg_bc of the lower and upper end of each non-periodic
+                    * direction: NONE = one-sided closures; SYMM = a symmetry
+                    * plane half a spacing outside the end point (operators
+                    * for symmetric fields by default, the antisymmetric
+                    * variants through the *_sym calls); XTND = the
+                    * extended-data rows (the compact filter, whose reference
+                    * rows are unset, keeps its one-sided rows there) */
+  int coordsys;    /* pg_coordsys; cylindrical: x = radius, y = angle, z = axis */
 } pg_grid;
 
 typedef struct pg_handle pg_handle;
@@ -143,6 +157,16 @@ int pg_laplacian(pg_handle* h, const double* in, double* out, void* stream);
 /* sFilter / gFilter / gFilterDir (parcop.f90:337-368 -> operators.f90:755-896).
  * dir = PG_DIR_ALL gives the x->y->z sweep sequence of `filter`. */
 int pg_filter(pg_handle* h, int kind, int dir, const double* in, double* out, void* stream);
+/* The operators of a direction with a symmetry plane come in two variants
+ * (compact.f90:80-85): sym = +1 for fields symmetric about the plane (what
+ * pg_d1 / pg_d8 / pg_filter apply), sym = -1 for antisymmetric ones -- the
+ * bc argument of d1x / d8x / filterx (compact_operators.f90:13-50,
+ * :280-313, :385-421).  Elsewhere both variants are the same operator.
+ * pg_filter_sym takes one sign per direction (dir = PG_DIR_ALL sweeps x, y,
+ * z with sym[0..2]). */
+int pg_d1_sym(pg_handle* h, int dir, int sym, const double* in, double* out, void* stream);
+int pg_d8_sym(pg_handle* h, int dir, int sym, const double* in, double* out, void* stream);
+int pg_filter_sym(pg_handle* h, int kind, int dir, const int* sym, const double* in, double* out, void* stream);
 /* pRing (parcop.f90:313-322 -> operators.f90:615-643 with L = 2). */
 int pg_ring(pg_handle* h, const double* in, double* out, void* stream);
 /* pRingV (parcop.f90:324-333 -> operators.f90:645-699 with L = 1). */
@@ -150,7 +174,9 @@ int pg_ringv(pg_handle* h, const double* vx, const double* vy, const double* vz,
              void* stream);
 /* gradS (parcop.f90:371-379 -> operators.f90:184-212, Cartesian). */
 int pg_grad(pg_handle* h, const double* in, double* gx, double* gy, double* gz, void* stream);
-/* divergence (parcop.f90:202-211 -> operators.f90:38-53, Cartesian). */
+/* divergence (parcop.f90:202-211 -> operators.f90:38-53): on a direction with
+ * a symmetry plane the component along it is taken as antisymmetric
+ * (isym = -1, patch.f90:89-91). */
 int pg_div(pg_handle* h, const double* fx, const double* fy, const double* fz, double* out,
            void* stream);
 /* xGrid/yGrid/zGrid/dxGrid/.../mesh_getGridLen/mesh_getCellVol

@@ -43,6 +43,9 @@ def lib():
         D = ctypes.POINTER(ctypes.c_double)
         I = ctypes.POINTER(ctypes.c_int)
         L.og_create.argtypes = [I, I, D, D, ctypes.POINTER(P)]
+        L.og_create2.argtypes = [I, I, I, ctypes.c_int, D, D, ctypes.POINTER(P)]
+        L.og_apply_sym.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, D, D]
+        L.og_filter3_sym.argtypes = [P, ctypes.c_int, I, D, D]
         L.og_destroy.argtypes = [P]
         L.og_apply.argtypes = [P, ctypes.c_int, ctypes.c_int, D, D]
         L.og_laplacian.argtypes = [P, D, D]
@@ -75,14 +78,20 @@ OP_D1, OP_D8, OP_SF, OP_GF, OP_D2, OP_D4 = 0, 1, 2, 3, 4, 5
 class OracleGrid:
     """One parcop patch: parcop.f90:23-61 ``setup`` on a Cartesian mesh."""
 
-    def __init__(self, n, periodic, x1, xn):
+    def __init__(self, n, periodic, x1, xn, bc=None, coordsys=0):
+        """bc: per direction (lower, upper) end codes 'NONE' / 'SYMM' / 'XTND' (non-periodic
+        directions); coordsys 0 Cartesian, 1 cylindrical."""
         L = lib()
         n = (ctypes.c_int * 3)(*[int(v) for v in n])
         per = (ctypes.c_int * 3)(*[1 if p else 0 for p in periodic])
         a = (ctypes.c_double * 3)(*[float(v) for v in x1])
         b = (ctypes.c_double * 3)(*[float(v) for v in xn])
+        codes = {"NONE": 0, "SYMM": 1, "XTND": 2}
+        bc = bc or (("NONE", "NONE"),) * 3
+        bcs = (ctypes.c_int * 6)(*[codes[bc[d][e]] for d in range(3) for e in range(2)])
+        self.coordsys = int(coordsys)
         h = ctypes.c_void_p()
-        rc = L.og_create(n, per, a, b, ctypes.byref(h))
+        rc = L.og_create2(n, per, bcs, self.coordsys, a, b, ctypes.byref(h))
         if rc != 0:
             raise ValueError("oracle: bad grid")
         self.h = h
@@ -102,6 +111,21 @@ class OracleGrid:
         v = _f64(v)
         out = self._out()
         lib().og_apply(self.h, op, direction, _dp(v), _dp(out))
+        return out
+
+    def apply_sym(self, op, direction, sym, v):
+        """The operator variant for symmetric (+1) or antisymmetric (-1) fields at a SYMM end."""
+        v = _f64(v)
+        out = self._out()
+        lib().og_apply_sym(self.h, op, direction, int(sym), _dp(v), _dp(out))
+        return out
+
+    def filter_sym(self, op, sym, v):
+        """x -> y -> z filter (op 2 compact, 3 Gaussian) with one variant sign per direction."""
+        v = _f64(v)
+        out = self._out()
+        s3 = (ctypes.c_int * 3)(*[int(x) for x in sym])
+        lib().og_filter3_sym(self.h, op, s3, _dp(v), _dp(out))
         return out
 
     def ddx(self, v):
@@ -467,6 +491,21 @@ class OracleSim:
         return eval(fortran3d(expr, self.sMap), _EVAL_GLOBALS, {"self": self})
 
     # pyranda.py:607-736
+    def apply_sym(self, op, direction, sym, v):
+        """The operator variant for symmetric (+1) or antisymmetric (-1) fields at a SYMM end."""
+        v = _f64(v)
+        out = self._out()
+        lib().og_apply_sym(self.h, op, direction, int(sym), _dp(v), _dp(out))
+        return out
+
+    def filter_sym(self, op, sym, v):
+        """x -> y -> z filter (op 2 compact, 3 Gaussian) with one variant sign per direction."""
+        v = _f64(v)
+        out = self._out()
+        s3 = (ctypes.c_int * 3)(*[int(x) for x in sym])
+        lib().og_filter3_sym(self.h, op, s3, _dp(v), _dp(out))
+        return out
+
     def ddx(self, v):
         return 0.0 if self.nx <= 1 else self.grid.ddx(v)
 

@@ -9,8 +9,10 @@
 // pyranda project).  The arithmetic follows the reference loop by loop (same
 // operand order, same summation grouping) so that results agree to rounding.
 //
-// Scope: Cartesian meshes, np = 1 (no MPI decomposition), boundary codes
-// PERI (periodic) and NONE (one-sided closures, mbc = 0).
+// Scope: np = 1 (no MPI decomposition); boundary codes PERI (periodic), NONE
+// (one-sided closures, mbc = 0), SYMM (symmetry planes, mbc = +-1, both
+// operator variants) and XTND (extended-data rows, mbc = 2, without supplied
+// data); Cartesian and cylindrical coordinates.
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -30,8 +32,82 @@ struct Weight {
   int nol, nor, ncl, ncr, nbc1, nbc2, null_option;
   bool implicit_op;
   double ali[5], ari[9];
-  double alb1[4][5], alb2[4][5], arb1[4][9], arb2[4][9];
+  double alb1[4][5], alb2[4][5], arb1[4][9], arb2[4][9];  // boundary code 0 (one-sided)
+  // rows of boundary codes -1, +1 (symmetry planes) and 2 (extended data): [code + 1]
+  // (code 0 is the arrays above; index 1 unused)
+  double xlb1[4][4][5], xlb2[4][4][5], xrb1[4][4][9], xrb2[4][4][9];
+  bool has_xtnd;
 };
+
+// lower_symm_weights_int / upper_symm_weights_int: stencils.f90:2390-2453.
+// alb/arb are 0-based [row][entry] copies of the Fortran alb(entry, row).
+void lower_symm(double (*alb)[5], double (*arb)[9], const Weight& w, int syml, int symr) {
+  for (int i = 0; i < w.nbc1; i++) {
+    for (int l = 0; l < w.ncl; l++) alb[i][l] = w.ali[l];
+    for (int l = 0; l < w.ncr; l++) arb[i][l] = w.ari[l];
+  }
+  for (int j = 1; j <= w.nol; j++) {
+    const int k = w.nol - j + 1;
+    for (int i = 1; i <= k; i++) {
+      const int i1 = k - i + 1, i2 = k + i;
+      alb[j - 1][i2 - 1] = alb[j - 1][i2 - 1] + (double)syml * alb[j - 1][i1 - 1];
+      alb[j - 1][i1 - 1] = 0.0;
+    }
+  }
+  for (int j = 1; j <= w.nor; j++) {
+    const int k = w.nor - j + 1;
+    for (int i = 1; i <= k; i++) {
+      const int i1 = k - i + 1, i2 = k + i;
+      arb[j - 1][i2 - 1] = arb[j - 1][i2 - 1] + (double)symr * arb[j - 1][i1 - 1];
+      arb[j - 1][i1 - 1] = 0.0;
+    }
+  }
+}
+void upper_symm(double (*alb)[5], double (*arb)[9], const Weight& w, int syml, int symr) {
+  const int n = w.nbc2;
+  for (int i = 0; i < n; i++) {
+    for (int l = 0; l < w.ncl; l++) alb[i][l] = w.ali[l];
+    for (int l = 0; l < w.ncr; l++) arb[i][l] = w.ari[l];
+  }
+  for (int j = 1; j <= w.nol; j++) {
+    const int jj = n + 1 - j, k = w.nol - j + 1, noff = w.ncl - k;
+    for (int i = 1; i <= k; i++) {
+      alb[jj - 1][noff - i] = alb[jj - 1][noff - i] + (double)syml * alb[jj - 1][noff + i - 1];
+      alb[jj - 1][noff + i - 1] = 0.0;
+    }
+  }
+  for (int j = n - w.nor + 1; j <= n; j++) {
+    const int k = j - n + w.nor, noff = w.ncr - k;
+    for (int i = 1; i <= k; i++) {
+      arb[j - 1][noff - i] = arb[j - 1][noff - i] + (double)symr * arb[j - 1][noff + i - 1];
+      arb[j - 1][noff + i - 1] = 0.0;
+    }
+  }
+}
+
+// The symmetric (+1) and antisymmetric (-1) rows of one operator, with the
+// (LHS, RHS) fold signs of its +1 variant (e.g. stencils.f90:256-259 for d1,
+// :600-603 for d8).
+void set_symm_rows(Weight& w, int syml1, int symr1) {
+  lower_symm(w.xlb1[2], w.xrb1[2], w, syml1, symr1);
+  lower_symm(w.xlb1[0], w.xrb1[0], w, -syml1, -symr1);
+  upper_symm(w.xlb2[2], w.xrb2[2], w, syml1, symr1);
+  upper_symm(w.xlb2[0], w.xrb2[0], w, -syml1, -symr1);
+}
+
+// Extended-data rows (code 2): lower rows given, upper rows the lower ones
+// reversed (alb2(:,j,2) = alb1(ncl:1:-1, nbc+1-j, 2); arb2 likewise times rsign).
+void set_xtnd_rows(Weight& w, const double (*L)[5], const double (*R)[9], double rsign) {
+  w.has_xtnd = true;
+  for (int j = 0; j < w.nbc1; j++) {
+    for (int l = 0; l < w.ncl; l++) w.xlb1[3][j][l] = L ? L[j][l] : w.ali[l];
+    for (int l = 0; l < w.ncr; l++) w.xrb1[3][j][l] = R ? R[j][l] : w.ari[l];
+  }
+  for (int j = 0; j < w.nbc2; j++) {
+    for (int l = 0; l < w.ncl; l++) w.xlb2[3][j][l] = w.xlb1[3][w.nbc1 - 1 - j][w.ncl - 1 - l];
+    for (int l = 0; l < w.ncr; l++) w.xrb2[3][j][l] = rsign * w.xrb1[3][w.nbc1 - 1 - j][w.ncr - 1 - l];
+  }
+}
 
 void mirror_rows(Weight& w, double rsign) {
   // alb2(:,j) = alb1(ncl:1:-1, 5-j) ; arb2(:,j) = rsign*arb1(ncr:1:-1, 5-j)
@@ -62,6 +138,14 @@ Weight make_c10d1() {
     for (int l = 0; l < 7; l++) w.arb1[j][l] = arb1[j][l];
   }
   mirror_rows(w, -1.0);
+  set_symm_rows(w, -1, +1);  // :256-259
+  const double XL[4][5] = {{0.0, 0.0, 6.0, 0.0, 0.0}, {0.0, 2.25, 6.0, 2.25, 0.0}, {0.3, 3.0, 6.0, 3.0, 0.3},
+                           {0.3, 3.0, 6.0, 3.0, 0.3}};  // :261-264
+  const double XR[4][9] = {{-0.1, 0.9, -4.5, 0.0, 4.5, -0.9, 0.1},
+                           {0.0125, -0.3, -4.6875, 0.0, 4.6875, 0.3, -0.0125},
+                           {-0.01, -1.01, -4.25, 0.0, 4.25, 1.01, 0.01},
+                           {-0.01, -1.01, -4.25, 0.0, 4.25, 1.01, 0.01}};  // :269-272
+  set_xtnd_rows(w, XL, XR, -1.0);
   return w;
 }
 
@@ -91,6 +175,10 @@ Weight make_c10d8() {
     for (int l = 0; l < 9; l++) w.arb1[j][l] = arb1[j][l];
   }
   mirror_rows(w, 1.0);
+  set_symm_rows(w, +1, +1);  // :600-603
+  const double XL[4][5] = {{0.0, 0.0, 60.0, 0.0, 0.0}, {0.0, 20.0, 20.0, 20.0, 0.0},
+                           {beta, alpha, zeta, alpha, beta}, {beta, alpha, zeta, alpha, beta}};  // :605-608
+  set_xtnd_rows(w, XL, nullptr, 1.0);  // arb1(:,1:4,2) = ari (:613-616)
   return w;
 }
 
@@ -118,12 +206,24 @@ Weight make_c8ff8() {
     for (int l = 0; l < 9; l++) w.arb1[j][l] = arb1[j][l];
   }
   mirror_rows(w, 1.0);
-  // difference form: ari(3:7) -= ali(1:5), same for the boundary rows
+  set_symm_rows(w, +1, +1);  // :810-813
+  // the extended-data rows are commented out in the reference (:814-826), so
+  // its code-2 rows are never set; this restatement gives them the one-sided
+  // rows (the product does the same)
+  for (int j = 0; j < 4; j++) {
+    for (int l = 0; l < 5; l++) { w.xlb1[3][j][l] = w.alb1[j][l]; w.xlb2[3][j][l] = w.alb2[j][l]; }
+    for (int l = 0; l < 9; l++) { w.xrb1[3][j][l] = w.arb1[j][l]; w.xrb2[3][j][l] = w.arb2[j][l]; }
+  }
+  // difference form: ari(3:7) -= ali(1:5), same for every boundary row (:832-834)
   for (int l = 0; l < 5; l++) w.ari[2 + l] -= w.ali[l];
   for (int j = 0; j < 4; j++)
     for (int l = 0; l < 5; l++) {
       w.arb1[j][2 + l] -= w.alb1[j][l];
       w.arb2[j][2 + l] -= w.alb2[j][l];
+      for (int c = 0; c < 4; c++) {
+        w.xrb1[c][j][2 + l] -= w.xlb1[c][j][l];
+        w.xrb2[c][j][2 + l] -= w.xlb2[c][j][l];
+      }
     }
   return w;
 }
@@ -150,10 +250,19 @@ Weight make_cgfs4() {
     for (int l = 0; l < 9; l++) w.arb1[j][l] = arb1[j][l];
   }
   mirror_rows(w, 1.0);
+  set_symm_rows(w, +1, +1);  // :1451-1454
+  set_xtnd_rows(w, nullptr, nullptr, 1.0);  // :1456-1467: LHS 1, RHS interior
+  // :1468 takes the first upper row from the reversed fourth one-sided row
+  for (int l = 0; l < 9; l++) w.xrb2[3][0][l] = w.arb1[3][8 - l];
+  // difference form (:1472-1475)
   w.ari[4] -= w.ali[0];
   for (int j = 0; j < 4; j++) {
     w.arb1[j][4] -= w.alb1[j][0];
     w.arb2[j][4] -= w.alb2[j][0];
+    for (int c = 0; c < 4; c++) {
+      w.xrb1[c][j][4] -= w.xlb1[c][j][0];
+      w.xrb2[c][j][4] -= w.xlb2[c][j][0];
+    }
   }
   return w;
 }
@@ -180,6 +289,14 @@ Weight make_c10d2() {
     for (int l = 0; l < 7; l++) w.arb1[j][l] = arb1[j][l];
   }
   mirror_rows(w, 1.0);  // alb2(:,j) = alb1(ncl:1:-1, 5-j), arb2 likewise (:391-398, :404-411)
+  set_symm_rows(w, +1, +1);  // :407-410
+  const double XL[4][5] = {{0.0, 0.0, 18.0, 0.0, 0.0}, {0.0, 4.05, 17.1, 4.05, 0.0},
+                           {0.387, 6.012, 16.182, 6.012, 0.387}, {0.387, 6.012, 16.182, 6.012, 0.387}};
+  const double XR[4][9] = {{0.2, -2.7, 27.0, -49.0, 27.0, -2.7, 0.2},
+                           {-0.0575, 2.295, 16.5375, -37.55, 16.5375, 2.295, -0.0575},
+                           {0.079, 4.671, 9.585, -28.670, 9.585, 4.671, 0.079},
+                           {0.079, 4.671, 9.585, -28.670, 9.585, 4.671, 0.079}};  // :412-427
+  set_xtnd_rows(w, XL, XR, 1.0);
   return w;
 }
 
@@ -208,6 +325,10 @@ Weight make_e4d4() {
   }
   for (int j = 0; j < 3; j++)
     for (int l = 0; l < 7; l++) w.arb2[j][l] = w.arb1[2 - j][6 - l];
+  // symmetric rows (:496-499); n = size(alb,2) = 4 rows are set there, the
+  // fourth (interior) one falls outside this restatement's three boundary rows
+  set_symm_rows(w, +1, +1);
+  set_xtnd_rows(w, nullptr, nullptr, 1.0);  // :501-512: LHS 1, RHS interior
   return w;
 }
 
@@ -221,6 +342,7 @@ struct Op1 {
   std::vector<double> al;  // al(i, c) -> al[(c-1)*n + (i-1)], factored
   std::vector<double> ar;  // ar(l, i) -> ar[(i-1)*ncr + (l-1)]
   int ncr = 0;
+  int bc1 = 0, bc2 = 0;  // op%bc: boundary codes of the lower and upper end (-1, 0, 1, 2)
   double& AL(int i, int c) { return al[(size_t)(c - 1) * n + (i - 1)]; }
   double AL(int i, int c) const { return al[(size_t)(c - 1) * n + (i - 1)]; }
   double AR(int l, int i) const { return ar[(size_t)(i - 1) * ncr + (l - 1)]; }
@@ -300,10 +422,13 @@ void ppentLUD1(Op1& o) {
   c(N, 3) = one / c(N, 3);
 }
 
-// setup_compact_op1: compact_basetype.f90:65-170 for np = 1
-Op1 setup_op(const Weight& w, int kind, int n, bool periodic) {
+// setup_compact_op1: compact_basetype.f90:65-170 for np = 1; bc1 / bc2 are
+// the op%bc codes of the two ends (compact.f90:77-91)
+Op1 setup_op(const Weight& w, int kind, int n, bool periodic, int bc1 = 0, int bc2 = 0) {
   Op1 o;
   o.kind = kind;
+  o.bc1 = periodic ? 0 : bc1;
+  o.bc2 = periodic ? 0 : bc2;
   o.n = n;
   o.periodic = periodic;
   o.null_option = w.null_option;
@@ -318,15 +443,19 @@ Op1 setup_op(const Weight& w, int kind, int n, bool periodic) {
     for (int l = 0; l < w.ncl; l++) gal[(size_t)i * o.nal + l] = w.ali[l];
     for (int l = 0; l < w.ncr; l++) gar[(size_t)i * w.ncr + l] = w.ari[l];
   }
-  if (!periodic) {
+  if (!periodic) {  // alb1(:,:,bc(1)) / alb2(:,:,bc(2)) (compact_basetype.f90:126-131)
     for (int j = 0; j < w.nbc1; j++) {
-      for (int l = 0; l < w.ncl; l++) gal[(size_t)j * o.nal + l] = w.alb1[j][l];
-      for (int l = 0; l < w.ncr; l++) gar[(size_t)j * w.ncr + l] = w.arb1[j][l];
+      const double* L = o.bc1 == 0 ? w.alb1[j] : w.xlb1[o.bc1 + 1][j];
+      const double* R = o.bc1 == 0 ? w.arb1[j] : w.xrb1[o.bc1 + 1][j];
+      for (int l = 0; l < w.ncl; l++) gal[(size_t)j * o.nal + l] = L[l];
+      for (int l = 0; l < w.ncr; l++) gar[(size_t)j * w.ncr + l] = R[l];
     }
     for (int j = 0; j < w.nbc2; j++) {
       const int i = n - w.nbc2 + j;
-      for (int l = 0; l < w.ncl; l++) gal[(size_t)i * o.nal + l] = w.alb2[j][l];
-      for (int l = 0; l < w.ncr; l++) gar[(size_t)i * w.ncr + l] = w.arb2[j][l];
+      const double* L = o.bc2 == 0 ? w.alb2[j] : w.xlb2[o.bc2 + 1][j];
+      const double* R = o.bc2 == 0 ? w.arb2[j] : w.xrb2[o.bc2 + 1][j];
+      for (int l = 0; l < w.ncl; l++) gal[(size_t)i * o.nal + l] = L[l];
+      for (int l = 0; l < w.ncr; l++) gar[(size_t)i * w.ncr + l] = R[l];
     }
   }
   o.al.assign((size_t)n * o.nal, 0.0);
@@ -362,8 +491,17 @@ void rhs_d1(const Op1& o, const double* v, double* dv) {
     dv[ax] = a(5, ax) * (b21 - v[ax - 1]) + a(6, ax) * (b22 - v[ax - 2]) + a(7, ax) * (b23 - v[ax - 3]);
     return;
   }
-  // one-sided, bc = 0  (:131-139, :175-183)
-  {
+  if (o.bc1 == -1) {  // antisymmetric (:121-128)
+    double s = 0.0;
+    for (int l = 4; l <= 7; l++) s += a(l, 1) * v[l - 3];
+    dv[1] = s;
+    s = 0.0;
+    for (int l = 3; l <= 7; l++) s += a(l, 2) * v[l - 2];
+    dv[2] = s;
+    s = 0.0;
+    for (int l = 2; l <= 7; l++) s += a(l, 3) * v[l - 1];
+    dv[3] = s;
+  } else {  // one-sided / symmetric / extended: difference form (:131-139)
     double s = 0.0;
     for (int l = 5; l <= 7; l++) s += a(l, 1) * (v[l - 3] - v[1]);
     dv[1] = s;
@@ -374,7 +512,17 @@ void rhs_d1(const Op1& o, const double* v, double* dv) {
   }
   for (int i = 4; i <= ax - 3; i++)
     dv[i] = a(5, i) * (v[i + 1] - v[i - 1]) + a(6, i) * (v[i + 2] - v[i - 2]) + a(7, i) * (v[i + 3] - v[i - 3]);
-  {
+  if (o.bc2 == -1) {  // antisymmetric (:163-170)
+    double s = 0.0;
+    for (int l = 1; l <= 6; l++) s += a(l, ax - 2) * v[ax - 6 + l];
+    dv[ax - 2] = s;
+    s = 0.0;
+    for (int l = 1; l <= 5; l++) s += a(l, ax - 1) * v[ax - 5 + l];
+    dv[ax - 1] = s;
+    s = 0.0;
+    for (int l = 1; l <= 4; l++) s += a(l, ax) * v[ax - 4 + l];
+    dv[ax] = s;
+  } else {
     dv[ax - 2] = a(1, ax - 2) * (v[ax - 5] - v[ax]) + a(2, ax - 2) * (v[ax - 4] - v[ax]) + a(3, ax - 2) * (v[ax - 3] - v[ax - 1]);
     double s = 0.0;
     for (int l = 1; l <= 4; l++) s += a(l, ax - 1) * (v[ax - 5 + l] - v[ax]);
@@ -400,6 +548,13 @@ void rhs_r4(const Op1& o, const double* v, double* dv) {
       for (int l = 6 - i; l <= 9; l++) s2 += a(l, i) * (v[l + i - 5] - v[i]);
       dv[i] = s1 + s2;
     }
+  } else if (o.bc1 == -1) {
+    for (int i = 1; i <= 4; i++) {
+      // sum(ar(6-i:9,i)*v(1:4+i))  (:108-117, antisymmetric)
+      double s = 0.0;
+      for (int l = 6 - i; l <= 9; l++) s += a(l, i) * v[l + i - 5];
+      dv[i] = s;
+    }
   } else {
     for (int i = 1; i <= 4; i++) {
       // sum(ar(7-i:9,i)*(v(2:4+i)-v(1)))  (:120-125)
@@ -424,6 +579,14 @@ void rhs_r4(const Op1& o, const double* v, double* dv) {
       for (int l = 1; l <= 5 + q; l++) s1 += a(l, i) * (v[i - 5 + l] - v[i]);
       for (int l = 6 + q; l <= 9; l++) s2 += a(l, i) * (b2[l - 5 - q] - v[i]);
       dv[i] = s1 + s2;
+    }
+  } else if (o.bc2 == -1) {
+    for (int q = 3; q >= 0; q--) {
+      const int i = ax - q;
+      // sum(ar(1:5+q,i)*v(i-4:ax))  (:154-163, antisymmetric)
+      double s = 0.0;
+      for (int l = 1; l <= 5 + q; l++) s += a(l, i) * v[i - 5 + l];
+      dv[i] = s;
     }
   } else {
     for (int q = 3; q >= 0; q--) {
@@ -488,10 +651,17 @@ void rhs_r3(const Op1& o, const double* v, double* dv) {
     for (int l = l0; l <= l1; l++) s += a(l, i) * (val(l) - v[i]);
     return s;
   };
-  // :124-126
+  auto sumr = [&](int i) {  // sum(op%ar, dim=1) (:106)
+    double t = 0.0;
+    for (int l = 1; l <= 7; l++) t += a(l, i);
+    return t;
+  };
+  // :109-112 (antisymmetric: + sumr(i) v(i)), :116-119
   dv[1] = part(1, 1, 3, [&](int l) { return vbr1[l]; }) + part(1, 4, 7, [&](int l) { return v[l - 3]; });
   dv[2] = part(2, 1, 2, [&](int l) { return vbr1[l + 1]; }) + part(2, 3, 7, [&](int l) { return v[l - 2]; });
   dv[3] = part(3, 1, 1, [&](int l) { return vbr1[l + 2]; }) + part(3, 2, 7, [&](int l) { return v[l - 1]; });
+  if (!o.periodic && o.bc1 == -1)
+    for (int i = 1; i <= 3; i++) dv[i] = dv[i] + sumr(i) * v[i];
   for (int i = 4; i <= ax - 3; i++) dv[i] = part(i, 1, 7, [&](int l) { return v[i - 4 + l]; });  // :137-143
   // :154-156
   dv[ax - 2] = part(ax - 2, 1, 6, [&](int l) { return v[ax - 6 + l]; }) +
@@ -499,6 +669,8 @@ void rhs_r3(const Op1& o, const double* v, double* dv) {
   dv[ax - 1] = part(ax - 1, 1, 5, [&](int l) { return v[ax - 5 + l]; }) +
                part(ax - 1, 6, 7, [&](int l) { return vbr2[l - 5]; });
   dv[ax] = part(ax, 1, 4, [&](int l) { return v[ax - 4 + l]; }) + part(ax, 5, 7, [&](int l) { return vbr2[l - 4]; });
+  if (!o.periodic && o.bc2 == -1)  // :146-151
+    for (int i = ax - 2; i <= ax; i++) dv[i] = dv[i] + sumr(i) * v[i];
 }
 
 // Full line evaluation (eval_compact_op1x_d1 / _r3 / _r4), np = 1, then the
@@ -528,14 +700,19 @@ struct og_handle {
   double d[3];     // patch spacing dx, dy, dz (patch.f90:83-85)
   double dmesh[3]; // mesh d1, d2, d3 (mesh.f90:192-209)
   double x1f[3];   // lower face coordinates (parcop.f90:51-56)
+  int bc[3][2];    // 0 NONE, 1 SYMM, 2 XTND per end (pyrandaMPI.py:101-131)
+  int symm[3];     // isym = -1 where a direction has a SYMM end (patch.f90:89-91)
+  int coordsys;    // 0 Cartesian, 1 cylindrical
   Op1 d1[3], d8[3], sf[3], gf[3], d2[3], d4[3];
+  Op1 anti[6][3];  // operator n = 2 of a SYMM direction (mbc = -1, compact.f90:80-85)
 };
 
 namespace {
 
 enum { OP_D1 = 0, OP_D8 = 1, OP_SF = 2, OP_GF = 3, OP_D2 = 4, OP_D4 = 5 };
 
-const Op1& pick(const og_handle* h, int op, int dir) {
+const Op1& pick(const og_handle* h, int op, int dir, int sym = 1) {
+  if (sym == -1 && h->symm[dir]) return h->anti[op][dir];
   switch (op) {
     case OP_D1: return h->d1[dir];
     case OP_D8: return h->d8[dir];
@@ -549,10 +726,10 @@ const Op1& pick(const og_handle* h, int op, int dir) {
 // Apply one operator along direction dir over a Fortran-ordered (nx,ny,nz) field.
 // Null ops follow compact_operators.f90: derivatives give 0 (:24-29, :288-294),
 // filters copy (:396-401).
-void apply_dir(const og_handle* h, int op, int dir, const double* in, double* out) {
+void apply_dir(const og_handle* h, int op, int dir, const double* in, double* out, int sym = 1) {
   const int nx = h->n[0], ny = h->n[1], nz = h->n[2];
   const size_t npts = (size_t)nx * ny * nz;
-  const Op1& o = pick(h, op, dir);
+  const Op1& o = pick(h, op, dir, sym);
   if (o.null_op) {
     if (op == OP_SF || op == OP_GF) std::memcpy(out, in, npts * sizeof(double));
     else std::memset(out, 0, npts * sizeof(double));
@@ -593,10 +770,26 @@ void apply_dir(const og_handle* h, int op, int dir, const double* in, double* ou
 
 extern "C" {
 
+int og_create2(const int* n, const int* periodic, const int* bc, int coordsys, const double* x1, const double* xn,
+               og_handle** out);
+
 // parcop.f90:23-61 (setup: node extents -> faces) + patch.f90:83-85 + mesh.f90:169-211
 int og_create(const int* n, const int* periodic, const double* x1, const double* xn, og_handle** out) {
-  if (!n || !periodic || !x1 || !xn || !out) return 1;
+  const int bc[6] = {0, 0, 0, 0, 0, 0};
+  return og_create2(n, periodic, bc, 0, x1, xn, out);
+}
+
+// The same with the boundary codes of every end (bc[2 d + e]: 0 NONE, 1 SYMM,
+// 2 XTND) and the coordinate system (0 Cartesian, 1 cylindrical).
+int og_create2(const int* n, const int* periodic, const int* bc, int coordsys, const double* x1, const double* xn,
+               og_handle** out) {
+  if (!n || !periodic || !bc || !x1 || !xn || !out || coordsys < 0 || coordsys > 1) return 1;
   og_handle* h = new og_handle();
+  h->coordsys = coordsys;
+  for (int d = 0; d < 3; d++) {
+    for (int e = 0; e < 2; e++) h->bc[d][e] = periodic[d] ? 0 : bc[2 * d + e];
+    h->symm[d] = (h->bc[d][0] == 1 || h->bc[d][1] == 1) ? 1 : 0;
+  }
   for (int d = 0; d < 3; d++) {
     if (n[d] < 1) { delete h; return 1; }
     h->n[d] = n[d];
@@ -619,12 +812,22 @@ int og_create(const int* n, const int* periodic, const double* x1, const double*
   static const Weight wd2 = make_c10d2(), wd4 = make_e4d4();
   for (int d = 0; d < 3; d++) {
     const bool per = h->periodic[d] != 0;
-    h->d2[d] = setup_op(wd2, 3, h->n[d], per);
-    h->d4[d] = setup_op(wd4, 3, h->n[d], per);
-    h->d1[d] = setup_op(wd1, 1, h->n[d], per);
-    h->d8[d] = setup_op(wd8, 4, h->n[d], per);
-    h->sf[d] = setup_op(wsf, 4, h->n[d], per);
-    h->gf[d] = setup_op(wgf, 4, h->n[d], per);
+    // mbc of operator n (compact.f90:77-91): SYMM ends +1 for n = 1, -1 for n = 2; XTND 2
+    int c1[2], c2[2];
+    for (int v = 0; v < 2; v++) {
+      const int sgn = v == 0 ? 1 : -1;
+      c1[v] = h->bc[d][0] == 1 ? sgn : (h->bc[d][0] == 2 ? 2 : 0);
+      c2[v] = h->bc[d][1] == 1 ? sgn : (h->bc[d][1] == 2 ? 2 : 0);
+    }
+    h->d2[d] = setup_op(wd2, 3, h->n[d], per, c1[0], c2[0]);
+    h->d4[d] = setup_op(wd4, 3, h->n[d], per, c1[0], c2[0]);
+    h->d1[d] = setup_op(wd1, 1, h->n[d], per, c1[0], c2[0]);
+    h->d8[d] = setup_op(wd8, 4, h->n[d], per, c1[0], c2[0]);
+    h->sf[d] = setup_op(wsf, 4, h->n[d], per, c1[0], c2[0]);
+    h->gf[d] = setup_op(wgf, 4, h->n[d], per, c1[0], c2[0]);
+    const Weight* ws[6] = {&wd1, &wd8, &wsf, &wgf, &wd2, &wd4};
+    const int kinds[6] = {1, 4, 4, 4, 3, 3};
+    for (int op = 0; op < 6; op++) h->anti[op][d] = setup_op(*ws[op], kinds[op], h->n[d], per, c1[1], c2[1]);
   }
   *out = h;
   return 0;
@@ -653,6 +856,25 @@ void og_set_threads(int t) {
 int og_apply(const og_handle* h, int op, int dir, const double* in, double* out) {
   if (!h || op < 0 || op > 5 || dir < 0 || dir > 2) return 1;
   apply_dir(h, op, dir, in, out);
+  return 0;
+}
+
+// d1x / d8x / filterx with the bc argument (compact_operators.f90:30-35,
+// :403-409): sym = -1 takes operator 2 on a direction with a SYMM end.
+int og_apply_sym(const og_handle* h, int op, int dir, int sym, const double* in, double* out) {
+  if (!h || op < 0 || op > 5 || dir < 0 || dir > 2 || (sym != 1 && sym != -1)) return 1;
+  apply_dir(h, op, dir, in, out, sym);
+  return 0;
+}
+
+// filter x -> y -> z with one bc per direction (operators.f90:873-875)
+int og_filter3_sym(const og_handle* h, int op, const int* sym, const double* in, double* out) {
+  if (!h || (op != 2 && op != 3) || !sym) return 1;
+  const size_t np = (size_t)h->n[0] * h->n[1] * h->n[2];
+  std::vector<double> tmp(np);
+  apply_dir(h, op, 0, in, out, sym[0]);
+  apply_dir(h, op, 1, out, tmp.data(), sym[1]);
+  apply_dir(h, op, 2, tmp.data(), out, sym[2]);
   return 0;
 }
 
@@ -743,9 +965,10 @@ int og_div(const og_handle* h, const double* fx, const double* fy, const double*
   if (!h) return 1;
   const size_t np = (size_t)h->n[0] * h->n[1] * h->n[2];
   std::vector<double> a(np), b(np);
-  apply_dir(h, OP_D1, 0, fx, out);
-  apply_dir(h, OP_D1, 1, fy, a.data());
-  apply_dir(h, OP_D1, 2, fz, b.data());
+  // ddx(fx, fA, isymX) ... (operators.f90:47-50)
+  apply_dir(h, OP_D1, 0, fx, out, h->symm[0] ? -1 : 1);
+  apply_dir(h, OP_D1, 1, fy, a.data(), h->symm[1] ? -1 : 1);
+  apply_dir(h, OP_D1, 2, fz, b.data(), h->symm[2] ? -1 : 1);
 #pragma omp parallel for schedule(static)
   for (long i = 0; i < (long)np; i++) out[i] = out[i] + a[i] + b[i];
   return 0;

@@ -40,7 +40,11 @@ class PgError(RuntimeError):
 class pg_grid(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int * 3), ("periodic", ctypes.c_int * 3),
                 ("x1", ctypes.c_double * 3), ("xn", ctypes.c_double * 3),
-                ("precision", ctypes.c_int)]
+                ("precision", ctypes.c_int), ("bc", (ctypes.c_int * 2) * 3), ("coordsys", ctypes.c_int)]
+
+
+PG_BC_NONE, PG_BC_SYMM, PG_BC_XTND = 0, 1, 2
+PG_CARTESIAN, PG_CYLINDRICAL = 0, 1
 
 
 PG_LAD_IN, PG_LAD_K, PG_LAD_HIDDEN, PG_LAD_OUT = 55, 64, 64, 2
@@ -79,6 +83,9 @@ SIGNATURES = [
     ("pg_laplacian", I, [P, D, D, P]),
     ("pg_filter", I, [P, I, I, D, D, P]),
     ("pg_ring", I, [P, D, D, P]),
+    ("pg_d1_sym", I, [P, I, I, D, D, P]),
+    ("pg_d8_sym", I, [P, I, I, D, D, P]),
+    ("pg_filter_sym", I, [P, I, I, ctypes.POINTER(ctypes.c_int), D, D, P]),
     ("pg_ringv", I, [P, D, D, D, D, P]),
     ("pg_grad", I, [P, D, D, D, D, P]),
     ("pg_div", I, [P, D, D, D, D, P]),

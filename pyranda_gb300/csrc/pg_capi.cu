@@ -55,7 +55,11 @@ struct GridInfo {
   double dm[3];   // mesh d1, d2, d3
   double x1f[3];  // lower face coordinates
   int64_t npts;
-  OpTables tab[OPK_COUNT][3];
+  int bc[3][2];   // pg_bc per end (non-periodic directions)
+  bool symm[3];   // a symmetry plane at either end: the antisymmetric variants differ
+  int coordsys;   // pg_coordsys
+  OpTables tab[OPK_COUNT][3];       // operators for symmetric fields (the default)
+  OpTables tab_anti[OPK_COUNT][3];  // variants for antisymmetric fields (compact.f90:80-85, nop = 2)
 };
 
 int grid_info(const pg_grid* g, GridInfo& gi, const char* who) {
@@ -66,11 +70,25 @@ int grid_info(const pg_grid* g, GridInfo& gi, const char* who) {
     }
     gi.n[d] = g->n[d];
     gi.periodic[d] = g->periodic[d] ? 1 : 0;
+    for (int e = 0; e < 2; e++) {
+      const int b = g->bc[d][e];
+      if (b < PG_BC_NONE || b > PG_BC_XTND) {
+        set_error("%s: bc[%d][%d] = %d is not a pg_bc", who, d, e, b);
+        return PG_EINVAL;
+      }
+      gi.bc[d][e] = gi.periodic[d] ? PG_BC_NONE : b;
+    }
+    gi.symm[d] = !gi.periodic[d] && (gi.bc[d][0] == PG_BC_SYMM || gi.bc[d][1] == PG_BC_SYMM);
     const double dn = (g->xn[d] - g->x1[d]) / (double)std::max(g->n[d] - 1, 1);
     const double f1 = g->x1[d] - dn / 2.0, fn = g->xn[d] + dn / 2.0;
     gi.x1f[d] = f1;
     gi.d[d] = (fn - f1) / (double)g->n[d];
   }
+  if (g->coordsys != PG_CARTESIAN && g->coordsys != PG_CYLINDRICAL) {
+    set_error("%s: coordsys %d is not supported (Cartesian 0 or cylindrical 1)", who, g->coordsys);
+    return PG_EINVAL;
+  }
+  gi.coordsys = g->coordsys;
   for (int d = 0; d < 3; d++) {
     if (gi.n[d] == 1) {
       const int a = (d + 1) % 3, b = (d + 2) % 3;
@@ -87,7 +105,9 @@ int grid_info(const pg_grid* g, GridInfo& gi, const char* who) {
   for (int k = 0; k < OPK_COUNT; k++)
     for (int d = 0; d < 3; d++) {
       const double scale = (k == OPK_D1) ? gi.d[d] : ((k == OPK_D2) ? gi.d[d] * gi.d[d] : 0.0);
-      int rc = build_operator(k, gi.n[d], gi.periodic[d] != 0, scale, gi.tab[k][d]);
+      int rc = build_operator(k, gi.n[d], gi.periodic[d] != 0, scale, gi.tab[k][d], gi.bc[d][0], gi.bc[d][1], 1);
+      if (rc == PG_OK)
+        rc = build_operator(k, gi.n[d], gi.periodic[d] != 0, scale, gi.tab_anti[k][d], gi.bc[d][0], gi.bc[d][1], -1);
       if (rc != PG_OK) {
         set_error("%s: direction %d has %d points; a non-null direction needs at least 8", who, d, gi.n[d]);
         return rc;
@@ -102,6 +122,9 @@ struct Ctx {
   int nmem = 0;
   int64_t npts = 0;
   OpRef ops[2][OPK_COUNT][3];
+  OpRef anti[2][OPK_COUNT][3];   // the antisymmetric variants (differ where a direction has a symmetry plane)
+  bool symm[3] = {false, false, false};
+  int coordsys = PG_CARTESIAN;
   void* blob = nullptr;          // coefficient tables and member-op arrays
   double* work = nullptr;        // one field: x->y->z filter ping-pong
   double* work2 = nullptr;       // one field: forward-elimination scratch of a sweep
@@ -188,8 +211,10 @@ int build_ctx(Ctx& c, const std::vector<GridInfo>& g, int precision, const char*
   for (int m = 1; m < M; m++)
     for (int d = 0; d < 3; d++) {
       if (g[m].periodic[d] != g[0].periodic[d] || (g[m].n[d] < 4) != (g[0].n[d] < 4) ||
-          (g[m].n[d] == 1) != (g[0].n[d] == 1)) {
-        set_error("%s: member %d differs from member 0 in periodicity or null directions", who, m);
+          (g[m].n[d] == 1) != (g[0].n[d] == 1) || g[m].bc[d][0] != g[0].bc[d][0] ||
+          g[m].bc[d][1] != g[0].bc[d][1] || g[m].coordsys != g[0].coordsys) {
+        set_error("%s: member %d differs from member 0 in periodicity, boundary codes, coordinate system or "
+                  "null directions", who, m);
         return PG_EINVAL;
       }
     }
@@ -198,17 +223,18 @@ int build_ctx(Ctx& c, const std::vector<GridInfo>& g, int precision, const char*
   for (int d = 0; d < 3; d++)
     for (int m = 0; m < M; m++) c.nmax[d] = std::max(c.nmax[d], g[m].n[d]);
   c.npts = off[M];
-  // layout of the blob: [tables ...][member ops (2 x 4 x 3 x M)]
+  // layout of the blob: [tables ...][member ops (variant x precision x kind x direction x member)];
+  // variant 0 = the operators for symmetric fields, 1 = the antisymmetric variants
   auto align = [](size_t x) { return (x + 15) & ~(size_t)15; };
   size_t total = 0;
   for (int m = 0; m < M; m++)
     for (int k = 0; k < OPK_COUNT; k++)
       for (int d = 0; d < 3; d++) {
         const size_t n = (size_t)g[m].n[d];
-        total += align(n * 9 * 8) + align(n * 12 * 8) + align(n * 9 * 4) + align(n * 12 * 4) + align(n * 9 * 4);
+        total += 2 * (align(n * 9 * 8) + align(n * 12 * 8) + align(n * 9 * 4) + align(n * 12 * 4) + align(n * 9 * 4));
       }
   const size_t ops_off = align(total);
-  total = ops_off + sizeof(MemberOp) * (size_t)M * 2 * OPK_COUNT * 3;
+  total = ops_off + sizeof(MemberOp) * (size_t)M * 2 * 2 * OPK_COUNT * 3;
   cudaError_t e = cudaMalloc(&c.blob, total);
   if (e != cudaSuccess) {
     set_error("%s: cudaMalloc tables: %s", who, cudaGetErrorString(e));
@@ -238,24 +264,27 @@ int build_ctx(Ctx& c, const std::vector<GridInfo>& g, int precision, const char*
     pos += v.size() * 4;
     return dptr;
   };
-  std::vector<MemberOp> mops((size_t)M * 2 * OPK_COUNT * 3);
-  auto mindex = [&](int p, int k, int d, int m) { return (((size_t)p * OPK_COUNT + k) * 3 + d) * M + m; };
+  std::vector<MemberOp> mops((size_t)M * 2 * 2 * OPK_COUNT * 3);
+  auto mindex = [&](int v, int p, int k, int d, int m) {
+    return ((((size_t)v * 2 + p) * OPK_COUNT + k) * 3 + d) * M + m;
+  };
+  for (int v = 0; v < 2; v++)
   for (int m = 0; m < M; m++)
     for (int k = 0; k < OPK_COUNT; k++)
       for (int d = 0; d < 3; d++) {
-        const OpTables& t = g[m].tab[k][d];
+        const OpTables& t = v == 0 ? g[m].tab[k][d] : g[m].tab_anti[k][d];
         std::vector<int> iw;
         double wsc = 0.0;
         const bool exact = integer_weights(t, iw, wsc);
         const int* rhs_i = put_i(exact ? iw : std::vector<int>((size_t)t.n * 9, 0));
         for (int p = 0; p < 2; p++) {
-          MemberOp& o = mops[mindex(p, k, d, m)];
+          MemberOp& o = mops[mindex(v, p, k, d, m)];
           o.rhs = put(t.rhs, p == PG_FP32);
           o.lu = put(t.lu, p == PG_FP32);
           o.n = g[m].n[d];
           o.nx = g[m].n[0];
           o.ny = g[m].n[1];
-          o.pad = 0;
+          o.bcl = t.bcl;
           o.lines = g[m].npts / g[m].n[d];
           o.off = off[m];
           const int mid = t.n / 2;
@@ -265,23 +294,24 @@ int build_ctx(Ctx& c, const std::vector<GridInfo>& g, int precision, const char*
           for (int l = 0; l < 9; l++) o.iw[l] = exact ? iw[(size_t)mid * 9 + l] : 0;
           o.exact = exact ? 1 : 0;
           o.wscale = (float)wsc;
-          o.pad2 = 0;
+          o.bch = t.bch;
         }
       }
+  for (int v = 0; v < 2; v++)
   for (int p = 0; p < 2; p++)
     for (int k = 0; k < OPK_COUNT; k++)
       for (int d = 0; d < 3; d++) {
         long long line0 = 0;
         for (int m = 0; m < M; m++) {
-          MemberOp& o = mops[mindex(p, k, d, m)];
+          MemberOp& o = mops[mindex(v, p, k, d, m)];
           o.line0 = line0;
           line0 += o.lines;
         }
-        OpRef& r = c.ops[p][k][d];
-        const OpTables& t = g[0].tab[k][d];
+        OpRef& r = v == 0 ? c.ops[p][k][d] : c.anti[p][k][d];
+        const OpTables& t = v == 0 ? g[0].tab[k][d] : g[0].tab_anti[k][d];
         r.exact = true;
-        for (int m = 0; m < M; m++) r.exact = r.exact && mops[mindex(p, k, d, m)].exact;
-        r.dev = reinterpret_cast<const MemberOp*>((unsigned char*)c.blob + ops_off) + mindex(p, k, d, 0);
+        for (int m = 0; m < M; m++) r.exact = r.exact && mops[mindex(v, p, k, d, m)].exact;
+        r.dev = reinterpret_cast<const MemberOp*>((unsigned char*)c.blob + ops_off) + mindex(v, p, k, d, 0);
         r.nops = M;
         r.nlines = line0;
         r.kind = k;
@@ -292,6 +322,8 @@ int build_ctx(Ctx& c, const std::vector<GridInfo>& g, int precision, const char*
       }
   std::memcpy(&host[ops_off], mops.data(), sizeof(MemberOp) * mops.size());
   c.mops = mops;
+  for (int d = 0; d < 3; d++) c.symm[d] = g[0].symm[d];
+  c.coordsys = g[0].coordsys;
   e = cudaMemcpy(c.blob, host.data(), total, cudaMemcpyHostToDevice);
   const size_t nbytes = (size_t)c.npts * sizeof(double);
   if (e == cudaSuccess) e = cudaMalloc(&c.work, nbytes);
@@ -909,8 +941,15 @@ int dense_sweep(Ctx& c, int kind, int dir, const double* in, double* out, int ep
   return launch_dense(ds, in, out, dir, epi, scale_pow, c.status, st);
 }
 
+// sym = -1: the variant for antisymmetric fields, where the direction has a
+// symmetry plane (compact_operators.f90:30-35: bc = -1 selects operator 2);
+// it runs the banded sweep with one thread per line.
 int sweep(Ctx& c, int kind, int dir, const double* in, double* out, int epi, int scale_pow, void* st,
-          bool emax_ready = false) {
+          bool emax_ready = false, int sym = 1) {
+  if (sym == -1 && c.symm[dir]) {
+    SweepLaunch s{in, out, c.work2, &c.anti[c.precision][kind][dir], dir, epi, scale_pow, c.emax, c.moff, emax_ready};
+    return launch_sweep(c.precision, s, st);
+  }
   if (c.dense && c.use_dense[kind][dir]) return dense_sweep(c, kind, dir, in, out, epi, scale_pow, st, emax_ready);
   if (c.use_split[c.precision][kind][dir]) {
     const OpRef& op = c.ops[c.precision][kind][dir];
@@ -925,16 +964,16 @@ int sweep(Ctx& c, int kind, int dir, const double* in, double* out, int epi, int
 }
 
 // null-op semantics of compact_operators.f90: derivatives -> 0, filters -> copy
-int apply_one(Ctx& c, int kind, int dir, const double* in, double* out, void* st) {
+int apply_one(Ctx& c, int kind, int dir, const double* in, double* out, void* st, int sym = 1) {
   if (c.ops[c.precision][kind][dir].null_op) {
     if (kind == OPK_SF || kind == OPK_GF) return launch_copy(out, in, c.npts, st);
     return launch_fill(out, 0.0, c.npts, st);
   }
-  return sweep(c, kind, dir, in, out, EPI_STORE, 0, st);
+  return sweep(c, kind, dir, in, out, EPI_STORE, 0, st, false, sym);
 }
 
 // operators.f90:848-853 / :872-875: x -> y -> z, null directions copy
-int filter_all(Ctx& c, int k, const double* in, double* out, void* st) {
+int filter_all(Ctx& c, int k, const double* in, double* out, void* st, const int* sym = nullptr) {
   int dirs[3], nd = 0;
   for (int d = 0; d < 3; d++)
     if (!c.ops[c.precision][k][d].null_op) dirs[nd++] = d;
@@ -942,7 +981,7 @@ int filter_all(Ctx& c, int k, const double* in, double* out, void* st) {
   const double* src = in;
   for (int q = 0; q < nd; q++) {  // ping-pong so that the last sweep lands in `out`
     double* dst = ((nd - 1 - q) % 2 == 0) ? out : c.work;
-    int rc = sweep(c, k, dirs[q], src, dst, EPI_STORE, 0, st);
+    int rc = sweep(c, k, dirs[q], src, dst, EPI_STORE, 0, st, false, sym ? sym[dirs[q]] : 1);
     if (rc) return rc;
     src = dst;
   }
@@ -1008,7 +1047,8 @@ int divergence(Ctx& c, const double* fx, const double* fy, const double* fz, dou
   bool first = true;
   for (int d = 0; d < 3; d++) {
     if (c.ops[c.precision][OPK_D1][d].null_op) continue;  // contributes exactly 0
-    int rc = sweep(c, OPK_D1, d, f[d], out, first ? EPI_STORE : EPI_ADD, 0, st);
+    // a vector component normal to a symmetry plane is antisymmetric (operators.f90:48-50, isym = -1)
+    int rc = sweep(c, OPK_D1, d, f[d], out, first ? EPI_STORE : EPI_ADD, 0, st, false, c.symm[d] ? -1 : 1);
     if (rc) return rc;
     first = false;
   }
@@ -1180,6 +1220,26 @@ int pg_filter(pg_handle* h, int kind, int dir, const double* in, double* out, vo
   const int k = kind == PG_SPECTRAL ? OPK_SF : OPK_GF;
   if (dir < 3) return apply_one(h->c, k, dir, in, out, stream);
   return filter_all(h->c, k, in, out, stream);
+}
+
+int pg_d1_sym(pg_handle* h, int dir, int sym, const double* in, double* out, void* stream) {
+  if (!h || !in || !out || bad_dir(dir) || (sym != 1 && sym != -1)) return PG_EINVAL;
+  return apply_one(h->c, OPK_D1, dir, in, out, stream, sym);
+}
+
+int pg_d8_sym(pg_handle* h, int dir, int sym, const double* in, double* out, void* stream) {
+  if (!h || !in || !out || bad_dir(dir) || (sym != 1 && sym != -1)) return PG_EINVAL;
+  return apply_one(h->c, OPK_D8, dir, in, out, stream, sym);
+}
+
+int pg_filter_sym(pg_handle* h, int kind, int dir, const int* sym, const double* in, double* out, void* stream) {
+  if (!h || !in || !out || !sym || (kind != PG_SPECTRAL && kind != PG_GAUSSIAN) || dir < 0 || dir > 3)
+    return PG_EINVAL;
+  for (int d = 0; d < 3; d++)
+    if (sym[d] != 1 && sym[d] != -1) return PG_EINVAL;
+  const int k = kind == PG_SPECTRAL ? OPK_SF : OPK_GF;
+  if (dir < 3) return apply_one(h->c, k, dir, in, out, stream, sym[dir]);
+  return filter_all(h->c, k, in, out, stream, sym);
 }
 
 int pg_ring(pg_handle* h, const double* in, double* out, void* stream) {

@@ -19,9 +19,13 @@ struct OpTables {
   std::vector<double> rhs;  // n x 9 per-row RHS weights
   std::vector<double> lu;   // n x 12 per-row solve coefficients (pg_setup.cpp solve_tables)
   std::vector<double> lhs;  // n x 5 LHS band (a, b, diag, c, d) before factorisation
+  int bcl = 0, bch = 0;     // boundary code of each end's rows: 0 one-sided, +1/-1 symmetry plane, 2 extended
 };
 
-int build_operator(int kind, int n, bool periodic, double scale, OpTables& t);
+// bc_lo / bc_hi: 0 one-sided (NONE), 1 symmetry plane (SYMM), 2 extended data (XTND);
+// sym = +1 the operator for symmetric fields, -1 for antisymmetric ones.
+int build_operator(int kind, int n, bool periodic, double scale, OpTables& t, int bc_lo = 0, int bc_hi = 0,
+                   int sym = 1);
 
 // Split-line (reduced-system) solve tables of one line's LHS band (n x 5):
 // segment starts (S + 1), per-position rows (n x 12) and the per-segment rows
@@ -48,7 +52,7 @@ struct MemberOp {
   const void* lu;   // n x 12 per-row solve coefficients (T), layout of pg_setup.cpp solve_tables
   int n;            // points per line
   int nx, ny;       // grid extents (to decode a line index)
-  int pad;
+  int bcl;          // boundary code of the lower end's rows (0, +1, -1, 2; OpTables::bcl)
   long long lines;  // lines of this grid along the direction
   long long line0;  // first global line of this grid (prefix over members)
   long long off;    // first point of this grid in the flat field
@@ -61,7 +65,7 @@ struct MemberOp {
   int iw[9];        // interior integer weights
   int exact;        // 1: rhs_i / iw / wscale are valid
   float wscale;
-  int pad2;
+  int bch;          // boundary code of the upper end's rows
 };
 
 // Host view of one (kind, direction, precision) operator of a grid or ensemble.

@@ -28,8 +28,16 @@ struct Stencil {
   int ncl, ncr, nbc;
   bool implicit, addback;  // addback = null_option 1 (filters)
   double lhs[5], rhs[9];
-  double lhs_lo[4][5], rhs_lo[4][9];
+  double lhs_lo[4][5], rhs_lo[4][9];  // one-sided rows (boundary code 0)
   double lhs_hi[4][5], rhs_hi[4][9];
+  // rows for extended boundary data (boundary code 2, XTND), where the reference defines them
+  bool has_xt;
+  double xt_lhs_lo[4][5], xt_rhs_lo[4][9];
+  double xt_lhs_hi[4][5], xt_rhs_hi[4][9];
+  // signs of the symmetric variant's folds (LHS, RHS): a first derivative of a
+  // symmetric field is antisymmetric, so its LHS folds with the opposite sign
+  double fold_lhs, fold_rhs;
+  bool diff_form;  // filters store RHS - LHS (stencils.f90:832-834, :1472-1475)
 };
 
 // Upper boundary rows mirror the lower ones: row j of the upper block is the
@@ -38,19 +46,44 @@ void mirror(Stencil& s, double rhs_sign) {
   for (int j = 0; j < s.nbc; j++) {
     for (int l = 0; l < s.ncl; l++) s.lhs_hi[j][l] = s.lhs_lo[s.nbc - 1 - j][s.ncl - 1 - l];
     for (int l = 0; l < s.ncr; l++) s.rhs_hi[j][l] = rhs_sign * s.rhs_lo[s.nbc - 1 - j][s.ncr - 1 - l];
+    for (int l = 0; l < s.ncl; l++) s.xt_lhs_hi[j][l] = s.xt_lhs_lo[s.nbc - 1 - j][s.ncl - 1 - l];
+    for (int l = 0; l < s.ncr; l++) s.xt_rhs_hi[j][l] = rhs_sign * s.xt_rhs_lo[s.nbc - 1 - j][s.ncr - 1 - l];
+  }
+}
+
+// Extended-data rows from tables (upper rows mirrored by `mirror`).
+void set_xt(Stencil& s, const double (*L)[5], const double (*R)[9]) {
+  s.has_xt = true;
+  for (int j = 0; j < s.nbc; j++) {
+    for (int l = 0; l < s.ncl; l++) s.xt_lhs_lo[j][l] = L ? L[j][l] : s.lhs[l];
+    for (int l = 0; l < s.ncr; l++) s.xt_rhs_lo[j][l] = R ? R[j][l] : s.rhs[l];
   }
 }
 
 // Difference form used by the filters: the stored RHS is RHS - LHS on the
 // overlapping entries (stencils.f90:832-834 and :1472-1475).
-void to_difference_form(Stencil& s) {
+void to_difference_form(const Stencil& s, const double* lhs, double* rhs) {
   const int off = (s.ncr - s.ncl) / 2;
-  for (int l = 0; l < s.ncl; l++) s.rhs[off + l] -= s.lhs[l];
-  for (int j = 0; j < 4; j++)
-    for (int l = 0; l < s.ncl; l++) {
-      s.rhs_lo[j][off + l] -= s.lhs_lo[j][l];
-      s.rhs_hi[j][off + l] -= s.lhs_hi[j][l];
-    }
+  for (int l = 0; l < s.ncl; l++) rhs[off + l] -= lhs[l];
+}
+
+// Rows of a symmetry plane (boundary code +-1): the interior stencil with the
+// entries that fall on points beyond the end moved onto their mirror images.
+// The plane lies half a spacing outside the end point (pyranda's grid points
+// are cell centres), so the point p = -1 - q beyond the lower end mirrors
+// point q; sign = +1 folds a symmetric field, -1 an antisymmetric one.
+// Row j is the j-th point from the end; `upper` mirrors about the upper end.
+void fold_row(const double* interior, int width, int j, bool upper, double sign, double* row) {
+  const int c = width / 2;
+  for (int l = 0; l < width; l++) row[l] = interior[l];
+  for (int l = 0; l < width; l++) {
+    const int off = l - c;                 // offset of entry l from the row's point
+    const int beyond = upper ? off - j : -(j + off);  // > 0: this many points past the end
+    if (beyond <= 0) continue;
+    const int mirror_off = upper ? j - (beyond - 1) : -j + (beyond - 1);  // the mirror point's offset
+    row[mirror_off + c] += sign * row[l];
+    row[l] = 0.0;
+  }
 }
 
 Stencil stencil_d1() {  // c10d1
@@ -72,6 +105,18 @@ Stencil stencil_d1() {  // c10d1
     std::memcpy(s.lhs_lo[j], LB[j], sizeof LB[j]);
     std::memcpy(s.rhs_lo[j], RB[j], sizeof RB[j]);
   }
+  // extended boundary data rows (stencils.f90:261-276)
+  const double XL[4][5] = {{0.0, 0.0, 6.0, 0.0, 0.0},
+                           {0.0, 2.25, 6.0, 2.25, 0.0},
+                           {0.3, 3.0, 6.0, 3.0, 0.3},
+                           {0.3, 3.0, 6.0, 3.0, 0.3}};
+  const double XR[4][9] = {{-0.1, 0.9, -4.5, 0.0, 4.5, -0.9, 0.1},
+                           {0.0125, -0.3, -4.6875, 0.0, 4.6875, 0.3, -0.0125},
+                           {-0.01, -1.01, -4.25, 0.0, 4.25, 1.01, 0.01},
+                           {-0.01, -1.01, -4.25, 0.0, 4.25, 1.01, 0.01}};
+  set_xt(s, XL, XR);
+  s.fold_lhs = -1.0;  // symmetric field, antisymmetric derivative (stencils.f90:256-259)
+  s.fold_rhs = 1.0;
   mirror(s, -1.0);  // antisymmetric operator
   return s;
 }
@@ -95,6 +140,17 @@ Stencil stencil_d2() {  // c10d2: compact 10th-order second derivative
     std::memcpy(s.lhs_lo[j], LB[j], sizeof LB[j]);
     std::memcpy(s.rhs_lo[j], RB[j], sizeof RB[j]);
   }
+  // extended boundary data rows (stencils.f90:411-427)
+  const double XL[4][5] = {{0.0, 0.0, 18.0, 0.0, 0.0},
+                           {0.0, 4.05, 17.1, 4.05, 0.0},
+                           {0.387, 6.012, 16.182, 6.012, 0.387},
+                           {0.387, 6.012, 16.182, 6.012, 0.387}};
+  const double XR[4][9] = {{0.2, -2.7, 27.0, -49.0, 27.0, -2.7, 0.2},
+                           {-0.0575, 2.295, 16.5375, -37.55, 16.5375, 2.295, -0.0575},
+                           {0.079, 4.671, 9.585, -28.670, 9.585, 4.671, 0.079},
+                           {0.079, 4.671, 9.585, -28.670, 9.585, 4.671, 0.079}};
+  set_xt(s, XL, XR);
+  s.fold_lhs = s.fold_rhs = 1.0;
   mirror(s, 1.0);
   return s;
 }
@@ -118,6 +174,8 @@ Stencil stencil_d4() {
     s.lhs_lo[j][0] = 1.0;
     std::memcpy(s.rhs_lo[j], RB[j], sizeof RB[j]);
   }
+  set_xt(s, nullptr, nullptr);  // extended data: interior rows (stencils.f90:500-512)
+  s.fold_lhs = s.fold_rhs = 1.0;
   mirror(s, 1.0);
   return s;
 }
@@ -143,6 +201,11 @@ Stencil stencil_d8() {  // c10d8
     std::memcpy(s.lhs_lo[j], LB[j], sizeof LB[j]);
     std::memcpy(s.rhs_lo[j], RB[j], sizeof RB[j]);
   }
+  // extended boundary data (stencils.f90:604-620): LHS rows 1-2 given, RHS interior
+  const double XL[4][5] = {{0.0, 0.0, 60.0, 0.0, 0.0}, {0.0, 20.0, 20.0, 20.0, 0.0}, {be, al, z, al, be},
+                           {be, al, z, al, be}};
+  set_xt(s, XL, nullptr);
+  s.fold_lhs = s.fold_rhs = 1.0;
   mirror(s, 1.0);
   return s;
 }
@@ -169,8 +232,12 @@ Stencil stencil_sf() {  // c8ff8, 9/10 dealiasing filter with telescoped ends
     std::memcpy(s.lhs_lo[j], LB[j], sizeof LB[j]);
     std::memcpy(s.rhs_lo[j], RB[j], sizeof RB[j]);
   }
+  // the reference leaves this filter's extended-data rows unset (stencils.f90:814-826 are
+  // commented out); an XTND end takes the one-sided rows here
+  s.has_xt = false;
+  s.fold_lhs = s.fold_rhs = 1.0;
   mirror(s, 1.0);
-  to_difference_form(s);
+  s.diff_form = true;
   return s;
 }
 
@@ -191,8 +258,13 @@ Stencil stencil_gf() {  // cgfs4, explicit 9-point Gaussian
     s.lhs_lo[j][0] = 1.0;
     std::memcpy(s.rhs_lo[j], RB[j], sizeof RB[j]);
   }
+  set_xt(s, nullptr, nullptr);  // extended data: interior rows (stencils.f90:1456-1467)
+  s.fold_lhs = s.fold_rhs = 1.0;
   mirror(s, 1.0);
-  to_difference_form(s);
+  // the reference's first upper extended row is the reversed fourth one-sided row
+  // (stencils.f90:1468: arb2(:,1,2) = arb1(ncr:1:-1,4,0))
+  for (int l = 0; l < s.ncr; l++) s.xt_rhs_hi[0][l] = s.rhs_lo[3][s.ncr - 1 - l];
+  s.diff_form = true;
   return s;
 }
 
@@ -481,7 +553,7 @@ int build_split(const std::vector<double>& band, int n, bool periodic, std::vect
 //              d2: dx^2, :149-152)
 //   lu[n*12]   per-row solve coefficients (solve_tables above); empty rows
 //              for explicit operators.
-int build_operator(int kind, int n, bool periodic, double scale, OpTables& t) {
+int build_operator(int kind, int n, bool periodic, double scale, OpTables& t, int bc_lo, int bc_hi, int sym) {
   Stencil s;
   switch (kind) {
     case OPK_D1: s = stencil_d1(); break;
@@ -492,6 +564,7 @@ int build_operator(int kind, int n, bool periodic, double scale, OpTables& t) {
     case OPK_D4: s = stencil_d4(); break;
     default: return PG_EINVAL;
   }
+  if (bc_lo < 0 || bc_lo > 2 || bc_hi < 0 || bc_hi > 2 || (sym != 1 && sym != -1)) return PG_EINVAL;
   t.kind = kind;
   t.n = n;
   t.periodic = periodic;
@@ -500,25 +573,49 @@ int build_operator(int kind, int n, bool periodic, double scale, OpTables& t) {
   t.null_op = (n < 4);
   t.rhs.assign((size_t)n * 9, 0.0);
   t.lu.assign((size_t)n * kSolveStride, 0.0);
+  // the boundary code each end's rows follow (compact.f90:77-91): 0 one-sided, +-1 the
+  // symmetric / antisymmetric variant at a symmetry plane, 2 extended data
+  auto code = [&](int bc) { return bc == 1 ? sym : (bc == 2 && s.has_xt ? 2 : 0); };
+  t.bcl = periodic ? 0 : code(bc_lo);
+  t.bch = periodic ? 0 : code(bc_hi);
   if (t.null_op) return PG_OK;
   if (n < 8) return PG_EBADSHAPE;  // the reference stencils index 8 points per line
 
   // global assembly (compact_basetype.f90:124-133)
   std::vector<double> band((size_t)n * 9, 0.0);  // band cols 0..4 = LHS (a,b,diag,c,d)
   const int offl = (5 - s.ncl) / 2;              // Gaussian: its single LHS weight is the diagonal
-  for (int i = 0; i < n; i++) {
-    for (int l = 0; l < s.ncl; l++) band[(size_t)i * 9 + offl + l] = s.lhs[l];
-    for (int l = 0; l < s.ncr; l++) t.rhs[(size_t)i * 9 + l] = s.rhs[l];
-  }
+  auto put_row = [&](int i, const double* lhs, const double* rhs) {
+    double l5[5] = {0, 0, 0, 0, 0}, r9[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int l = 0; l < s.ncl; l++) l5[l] = lhs[l];
+    for (int l = 0; l < s.ncr; l++) r9[l] = rhs[l];
+    if (s.diff_form) to_difference_form(s, l5, r9);
+    for (int l = 0; l < s.ncl; l++) band[(size_t)i * 9 + offl + l] = l5[l];
+    for (int l = 0; l < s.ncr; l++) t.rhs[(size_t)i * 9 + l] = r9[l];
+  };
+  for (int i = 0; i < n; i++) put_row(i, s.lhs, s.rhs);
   if (!periodic) {
-    for (int j = 0; j < s.nbc; j++) {
-      for (int l = 0; l < s.ncl; l++) band[(size_t)j * 9 + offl + l] = s.lhs_lo[j][l];
-      for (int l = 0; l < s.ncr; l++) t.rhs[(size_t)j * 9 + l] = s.rhs_lo[j][l];
-    }
-    for (int j = 0; j < s.nbc; j++) {
-      const int i = n - s.nbc + j;
-      for (int l = 0; l < s.ncl; l++) band[(size_t)i * 9 + offl + l] = s.lhs_hi[j][l];
-      for (int l = 0; l < s.ncr; l++) t.rhs[(size_t)i * 9 + l] = s.rhs_hi[j][l];
+    for (int end = 0; end < 2; end++) {
+      const int c = end == 0 ? t.bcl : t.bch;
+      for (int j = 0; j < s.nbc; j++) {
+        const int i = end == 0 ? j : n - s.nbc + j;  // rows of the upper block are stored from n - nbc
+        const int from_end = end == 0 ? j : s.nbc - 1 - j;
+        double fl[5], fr[9];
+        const double *L, *R;
+        if (c == 0) {
+          L = end == 0 ? s.lhs_lo[j] : s.lhs_hi[j];
+          R = end == 0 ? s.rhs_lo[j] : s.rhs_hi[j];
+        } else if (c == 2) {
+          L = end == 0 ? s.xt_lhs_lo[j] : s.xt_lhs_hi[j];
+          R = end == 0 ? s.xt_rhs_lo[j] : s.xt_rhs_hi[j];
+        } else {  // symmetry plane: fold the interior stencil (stencils.f90:2390-2453)
+          const double sl = (c == 1 ? s.fold_lhs : -s.fold_lhs), sr = (c == 1 ? s.fold_rhs : -s.fold_rhs);
+          fold_row(s.lhs, s.ncl, from_end, end == 1, sl, fl);
+          fold_row(s.rhs, s.ncr, from_end, end == 1, sr, fr);
+          L = fl;
+          R = fr;
+        }
+        put_row(i, L, R);
+      }
     }
   }
   if (scale != 0.0)

@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(kSplitThreads, 3) split_kernel(const SParams P
 #pragma unroll
         for (int q = 0; q < 8; q++) {
           const int i = q < 4 ? q : n - 8 + q;
-          if (i >= a && i < b) re[q] = (T)fixed_to_float(edge_rhs<long long, KIND, false, int>(ln, i, op.rhs_i), E, wsc);
+          if (i >= a && i < b) re[q] = (T)fixed_to_float(edge_rhs<long long, KIND, false, int>(ln, i, op.rhs_i, op.bcl, op.bch), E, wsc);
         }
       } else {  // FP64 arithmetic on the raw values (8 rows of a line)
         const SLine<double> ln{vl, n, 0};
@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(kSplitThreads, 3) split_kernel(const SParams P
 #pragma unroll
         for (int q = 0; q < 8; q++) {
           const int i = q < 4 ? q : n - 8 + q;
-          if (i >= a && i < b) re[q] = (T)edge_rhs<double, KIND, false, W>(ln, i, R);
+          if (i >= a && i < b) re[q] = (T)edge_rhs<double, KIND, false, W>(ln, i, R, op.bcl, op.bch);
         }
       }
     }

@@ -227,16 +227,33 @@ struct Line {
   }
 };
 
-// RHS of one edge row (rows 0..3 and n-4..n-1) straight from global memory,
-// with the reference's periodic-halo or one-sided (boundary code 0) formulas.
+// RHS of one edge row (rows 0..3 and n-4..n-1) straight from the line, with
+// the reference's periodic-halo formulas or, at a non-periodic end, the
+// formulas of its boundary code (bcl lower end, bch upper end): the
+// difference form anchored at the end point for one-sided (0), symmetric (+1)
+// and extended (2) rows, plain sums for antisymmetric (-1) rows
+// (compact_d1.f90:119-193, compact_r3.f90:88-157, compact_r4.f90:106-193).
 template <typename T, int KIND, bool PER, typename W, typename LN>
-__device__ __forceinline__ T edge_rhs(const LN& ln, int i, const W* __restrict__ R) {
+__device__ __forceinline__ T edge_rhs(const LN& ln, int i, const W* __restrict__ R, int bcl = 0, int bch = 0) {
   const int n = ln.n;
   const W* r = R + i * 9;
+  const bool lower = i < n / 2;
+  const bool anti = !PER && (lower ? bcl : bch) == -1;
   if (KIND == 1) {
     if (PER)  // compact_d1.f90:141-147, :185-191 (the halo is the wrapped line)
       return ldc(r + 4) * (ln.w(i + 1) - ln.w(i - 1)) + ldc(r + 5) * (ln.w(i + 2) - ln.w(i - 2)) +
              ldc(r + 6) * (ln.w(i + 3) - ln.w(i - 3));
+    if (i == 3 || i == n - 4)  // interior formula with the boundary rows' weights
+      return ldc(r + 4) * (ln.v(i + 1) - ln.v(i - 1)) + ldc(r + 5) * (ln.v(i + 2) - ln.v(i - 2)) +
+             ldc(r + 6) * (ln.v(i + 3) - ln.v(i - 3));
+    if (anti) {  // compact_d1.f90:121-128, :163-170: sum of weights times values on the line
+      T s = T(0);
+      for (int l = 0; l < 7; l++) {
+        const int p = i + l - 3;
+        if (p >= 0 && p < n) s += ldc(r + l) * ln.v(p);
+      }
+      return s;
+    }
     if (i == 0 || i == 1) {  // compact_d1.f90:131-134
       const T v0 = ln.v(0);
       T s = T(0);
@@ -245,9 +262,6 @@ __device__ __forceinline__ T edge_rhs(const LN& ln, int i, const W* __restrict__
     }
     if (i == 2)  // compact_d1.f90:135
       return ldc(r + 4) * (ln.v(3) - ln.v(1)) + ldc(r + 5) * (ln.v(4) - ln.v(0)) + ldc(r + 6) * (ln.v(5) - ln.v(0));
-    if (i == 3 || i == n - 4)  // interior formula with the boundary rows' weights
-      return ldc(r + 4) * (ln.v(i + 1) - ln.v(i - 1)) + ldc(r + 5) * (ln.v(i + 2) - ln.v(i - 2)) +
-             ldc(r + 6) * (ln.v(i + 3) - ln.v(i - 3));
     const T vn = ln.v(n - 1);
     if (i == n - 3)  // compact_d1.f90:178
       return ldc(r + 0) * (ln.v(n - 6) - vn) + ldc(r + 1) * (ln.v(n - 5) - vn) +
@@ -262,11 +276,14 @@ __device__ __forceinline__ T edge_rhs(const LN& ln, int i, const W* __restrict__
     T s = T(0);
     if (PER) {
       for (int l = 0; l < 7; l++) s += ldc(r + l) * (ln.w(i + l - 3) - vc);
-    } else {  // the closures' weights vanish outside the line
+    } else {  // points beyond a non-periodic end count as zero; antisymmetric rows add (sum of weights) v_i
+      T sumr = T(0);
       for (int l = 0; l < 7; l++) {
         const int p = i + l - 3;
-        if (p >= 0 && p < n) s += ldc(r + l) * (ln.v(p) - vc);
+        s += ldc(r + l) * ((p >= 0 && p < n) ? ln.v(p) - vc : -vc);
+        sumr += ldc(r + l);
       }
+      if (anti) s += sumr * vc;
     }
     return s;
   }
@@ -283,7 +300,15 @@ __device__ __forceinline__ T edge_rhs(const LN& ln, int i, const W* __restrict__
     }
     return s1 + s2;
   }
-  T s = T(0);  // one-sided closures (compact_r4.f90:120-125, :166-171)
+  T s = T(0);
+  if (anti) {  // compact_r4.f90:108-117, :157-166: sum of weights times values on the line
+    for (int l = 0; l < 9; l++) {
+      const int p = i + l - 4;
+      if (p >= 0 && p < n) s += ldc(r + l) * ln.v(p);
+    }
+    return s;
+  }
+  // one-sided / symmetric / extended closures (compact_r4.f90:120-125, :166-171)
   if (i < 4) {
     const T v0 = ln.v(0);
     for (int l = 5 - i; l <= 8; l++) s += ldc(r + l) * (ln.v(l + i - 4) - v0);
@@ -376,7 +401,8 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_kernel(const KParams P) {
   // edge rows first: they may need wrapped values of the far end of the line
   T e[8];
 #pragma unroll
-  for (int q = 0; q < 8; q++) e[q] = solve_value(edge_rhs<TR, KIND, PER, W>(ln, q < 4 ? q : n - 8 + q, R), E, wsc);
+  for (int q = 0; q < 8; q++)
+    e[q] = solve_value(edge_rhs<TR, KIND, PER, W>(ln, q < 4 ? q : n - 8 + q, R, op.bcl, op.bch), E, wsc);
 
   auto put = [&](int p, T x, double vin, double o) {
     pout[p * st] = epilogue<EPI>(to_f64<T>(x), vin, o, sc, ADDBACK);

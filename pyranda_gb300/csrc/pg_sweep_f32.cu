@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(128) d8_rhs_kernel(const MemberOp* __restrict_
   for (int i = i0; i < i1; i++) {
     float r;
     if (i < 4 || i >= n - 4) {
-      r = fixed_to_float(edge_rhs<long long, 4, PER, int>(ln, i, op.rhs_i), E, op.wscale);
+      r = fixed_to_float(edge_rhs<long long, 4, PER, int>(ln, i, op.rhs_i, op.bcl, op.bch), E, op.wscale);
     } else {
       if (!primed) {
 #pragma unroll

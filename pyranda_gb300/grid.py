@@ -61,7 +61,11 @@ def flush_pending():
 class Grid:
     """A Cartesian pyranda patch on one GPU (parcop.f90:23-70 setup + setup_mesh)."""
 
-    def __init__(self, n, periodic, x1, xn, precision="fp64", device=None, line_split=False):
+    def __init__(self, n, periodic, x1, xn, precision="fp64", device=None, line_split=False, bc=None,
+                 coordsys=0):
+        """bc: per direction the (lower, upper) end codes of non-periodic directions,
+        'NONE' (one-sided closures), 'SYMM' (symmetry plane) or 'XTND' (extended data);
+        coordsys: 0 Cartesian, 1 cylindrical (x = radius)."""
         if not torch.cuda.is_available():
             raise RuntimeError("pyranda_gb300 needs a CUDA device; there is no CPU fallback")
         self.lib = _lib.load()
@@ -77,6 +81,14 @@ class Grid:
             g.periodic[d] = 1 if self.periodic[d] else 0
             g.x1[d] = float(x1[d])
             g.xn[d] = float(xn[d])
+        codes = {"NONE": _lib.PG_BC_NONE, "SYMM": _lib.PG_BC_SYMM, "XTND": _lib.PG_BC_XTND}
+        self.bc = tuple(tuple(b) for b in (bc or (("NONE", "NONE"),) * 3))
+        for d in range(3):
+            for e in range(2):
+                g.bc[d][e] = codes[self.bc[d][e]]
+        g.coordsys = int(coordsys)
+        self.coordsys = int(coordsys)
+        self.symmetric = tuple((not self.periodic[d]) and "SYMM" in self.bc[d] for d in range(3))
         self.precision = precision
         g.precision = _lib.precision_code(precision)
         h = ctypes.c_void_p()
@@ -172,10 +184,14 @@ class Grid:
         return out
 
     # --------------------------------------------------------------- operators
-    def d1(self, direction, v, out=None):
+    def d1(self, direction, v, out=None, sym=1):
+        """sym = -1: the variant for a field antisymmetric about a symmetry plane."""
         v = self.field(v)
         out = self._out(out)
-        _lib.check(self.lib.pg_d1(self.h, direction, _ptr(v), _ptr(out), _stream()), "pg_d1")
+        if sym == 1:
+            _lib.check(self.lib.pg_d1(self.h, direction, _ptr(v), _ptr(out), _stream()), "pg_d1")
+        else:
+            _lib.check(self.lib.pg_d1_sym(self.h, direction, sym, _ptr(v), _ptr(out), _stream()), "pg_d1_sym")
         return out
 
     def ddx(self, v, out=None):
@@ -187,10 +203,13 @@ class Grid:
     def ddz(self, v, out=None):
         return self.d1(2, v, out)
 
-    def d8(self, direction, v, out=None):
+    def d8(self, direction, v, out=None, sym=1):
         v = self.field(v)
         out = self._out(out)
-        _lib.check(self.lib.pg_d8(self.h, direction, _ptr(v), _ptr(out), _stream()), "pg_d8")
+        if sym == 1:
+            _lib.check(self.lib.pg_d8(self.h, direction, _ptr(v), _ptr(out), _stream()), "pg_d8")
+        else:
+            _lib.check(self.lib.pg_d8_sym(self.h, direction, sym, _ptr(v), _ptr(out), _stream()), "pg_d8_sym")
         return out
 
     def d2(self, direction, v, out=None):
@@ -218,12 +237,18 @@ class Grid:
         """Divergence of a tensor (operators.f90:97-123, Cartesian): the divergences of its columns."""
         return [self.div(fxx, fyx, fzx), self.div(fxy, fyy, fzy), self.div(fxz, fyz, fzz)]
 
-    def filter(self, kind, v, direction=_lib.PG_DIR_ALL, out=None):
-        """kind 'spectral' (c8ff8, fbar) or 'gaussian' (cgfs4, gbar)."""
+    def filter(self, kind, v, direction=_lib.PG_DIR_ALL, out=None, sym=None):
+        """kind 'spectral' (c8ff8, fbar) or 'gaussian' (cgfs4, gbar); sym: per direction +1 / -1
+        (the variant for antisymmetric fields at a symmetry plane)."""
         v = self.field(v)
         out = self._out(out)
         k = _lib.PG_SPECTRAL if kind == "spectral" else _lib.PG_GAUSSIAN
-        _lib.check(self.lib.pg_filter(self.h, k, direction, _ptr(v), _ptr(out), _stream()), "pg_filter")
+        if sym is None:
+            _lib.check(self.lib.pg_filter(self.h, k, direction, _ptr(v), _ptr(out), _stream()), "pg_filter")
+        else:
+            s3 = (ctypes.c_int * 3)(*[int(x) for x in sym])
+            _lib.check(self.lib.pg_filter_sym(self.h, k, direction, s3, _ptr(v), _ptr(out), _stream()),
+                       "pg_filter_sym")
         return out
 
     def ring(self, v, out=None):
