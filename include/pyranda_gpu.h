@@ -155,7 +155,9 @@ int pg_d4(pg_handle* h, int dir, const double* in, double* out, void* stream);
  * must differ from in. */
 int pg_laplacian(pg_handle* h, const double* in, double* out, void* stream);
 /* sFilter / gFilter / gFilterDir (parcop.f90:337-368 -> operators.f90:755-896).
- * dir = PG_DIR_ALL gives the x->y->z sweep sequence of `filter`. */
+ * dir = PG_DIR_ALL gives the x->y->z sweep sequence of `filter`; on a
+ * cylindrical grid the spectral filter acts on the field times the cell
+ * volume and divides by it (operators.f90:876-883; out must differ from in). */
 int pg_filter(pg_handle* h, int kind, int dir, const double* in, double* out, void* stream);
 /* The operators of a direction with a symmetry plane come in two variants
  * (compact.f90:80-85): sym = +1 for fields symmetric about the plane (what
@@ -172,15 +174,24 @@ int pg_ring(pg_handle* h, const double* in, double* out, void* stream);
 /* pRingV (parcop.f90:324-333 -> operators.f90:645-699 with L = 1). */
 int pg_ringv(pg_handle* h, const double* vx, const double* vy, const double* vz, double* out,
              void* stream);
-/* gradS (parcop.f90:371-379 -> operators.f90:184-212, Cartesian). */
+/* gradS (parcop.f90:371-379 -> operators.f90:184-212); cylindrical grids
+ * divide the angular component by the radius. */
 int pg_grad(pg_handle* h, const double* in, double* gx, double* gy, double* gz, void* stream);
-/* divergence (parcop.f90:202-211 -> operators.f90:38-53): on a direction with
+/* divergence (parcop.f90:202-211 -> operators.f90:38-64): on a direction with
  * a symmetry plane the component along it is taken as antisymmetric
- * (isym = -1, patch.f90:89-91). */
+ * (isym = -1, patch.f90:89-91); cylindrical grids take (d(r fx)/dr +
+ * dfy/dtheta) / r + dfz/dz.  Cylindrical grids use three workspace fields of
+ * the handle. */
 int pg_div(pg_handle* h, const double* fx, const double* fy, const double* fz, double* out,
            void* stream);
+/* divergenceTensor (parcop.f90:213-224 -> operators.f90:97-146): f holds the
+ * nine device fields fxx, fxy, fxz, fyx, fyy, fyz, fzx, fzy, fzz; out the
+ * three results dfx, dfy, dfz (distinct from f).  Cartesian and cylindrical;
+ * the symmetry multipliers isym^p of the reference select each derivative's
+ * variant on directions with a symmetry plane. */
+int pg_divt(pg_handle* h, const double* const* f, double* const* out, void* stream);
 /* xGrid/yGrid/zGrid/dxGrid/.../mesh_getGridLen/mesh_getCellVol
- * (parcop.f90:130-191 -> mesh.f90:169-211, Cartesian). */
+ * (parcop.f90:130-191 -> mesh.f90:169-225, Cartesian and cylindrical). */
 int pg_mesh(pg_handle* h, int which, double* out, void* stream);
 
 /* One stage of the LSRK(5,4) update of pyranda.py:797-804 for nvar conserved

@@ -54,6 +54,7 @@ def lib():
         L.og_ringv.argtypes = [P, D, D, D, D, ctypes.c_int]
         L.og_grad.argtypes = [P, D, D, D, D]
         L.og_div.argtypes = [P, D, D, D, D]
+        L.og_divt.argtypes = [P, ctypes.POINTER(D), ctypes.POINTER(D)]
         L.og_mesh.argtypes = [P, ctypes.c_int, D]
         L.og_spacing.argtypes = [P, D, D]
         L.og_dense.argtypes = [P, ctypes.c_int, ctypes.c_int, D]
@@ -193,6 +194,15 @@ class OracleGrid:
         out = self._out()
         lib().og_div(self.h, _dp(fx), _dp(fy), _dp(fz), _dp(out))
         return out
+
+    def divt(self, *f):
+        """divT of the nine components fxx fxy fxz fyx fyy fyz fzx fzy fzz -> [dfx, dfy, dfz]."""
+        fs = [_f64(x) for x in f]
+        outs = [self._out() for _ in range(3)]
+        fa = (ctypes.POINTER(ctypes.c_double) * 9)(*[_dp(x) for x in fs])
+        oa = (ctypes.POINTER(ctypes.c_double) * 3)(*[_dp(x) for x in outs])
+        lib().og_divt(self.h, fa, oa)
+        return outs
 
     def mesh(self, which):
         out = self._out()
@@ -375,7 +385,8 @@ except Exception:  # pragma: no cover
 def default_mesh_options():
     """pyrandaMesh.py:214-233"""
     return {"x1": [0.0, 0.0, 0.0], "xn": [1, 1, 1], "nn": [1, 1, 1],
-            "periodic": [False, False, False]}
+            "periodic": [False, False, False], "symmetric": [[False, False], [False, False], [False, False]],
+            "coordsys": 0}
 
 
 class OracleSim:
@@ -391,9 +402,13 @@ class OracleSim:
             opts["nn"][ind] = nn
             opts["periodic"][ind] = periodic
 
-        msmap = {"xdom=(": "set_options(0,", "ydom=(": "set_options(1,", "zdom=(": "set_options(2,"}
-        for line in split_lines(mesh_str):
-            exec(fortran3d(line, dict(msmap)), {"set_options": set_options, "numpy": numpy})
+        if isinstance(mesh_str, dict):  # a mesh_options dictionary (pyrandaMesh.py:214-233)
+            for k, v in mesh_str.items():
+                opts[k] = v
+        else:
+            msmap = {"xdom=(": "set_options(0,", "ydom=(": "set_options(1,", "zdom=(": "set_options(2,"}
+            for line in split_lines(mesh_str):
+                exec(fortran3d(line, dict(msmap)), {"set_options": set_options, "numpy": numpy})
         self.options = opts
         self.nx, self.ny, self.nz = opts["nn"]
         self.npts = self.nx * self.ny * self.nz
@@ -401,7 +416,11 @@ class OracleSim:
         self.dy = (opts["xn"][1] - opts["x1"][1]) / max(self.ny - 1, 1)
         self.dz = (opts["xn"][2] - opts["x1"][2]) / max(self.nz - 1, 1)
         self.shape = (self.nx, self.ny, self.nz)
-        self.grid = OracleGrid(self.shape, opts["periodic"], opts["x1"], opts["xn"])
+        # pyrandaMPI.py:101-131: symmetric ends of non-periodic directions are SYMM
+        sym = opts.get("symmetric", [[False, False]] * 3)
+        bc = [["SYMM" if (sym[d][e] and not opts["periodic"][d]) else "NONE" for e in range(2)] for d in range(3)]
+        self.grid = OracleGrid(self.shape, opts["periodic"], opts["x1"], opts["xn"], bc=bc,
+                               coordsys=int(opts.get("coordsys", 0)))
         self.meshx = self.grid.mesh(0)
         self.meshy = self.grid.mesh(1)
         self.meshz = self.grid.mesh(2)
@@ -528,8 +547,9 @@ class OracleSim:
         return self.grid.laplacian(v)
 
     def divT(self, fxx, fxy, fxz, fyx, fyy, fyz, fzx, fzy, fzz):
-        g = self.grid
-        return [g.div(fxx, fyx, fzx), g.div(fxy, fyy, fzy), g.div(fxz, fyz, fzz)]
+        z = self.zero
+        f = [x if isinstance(x, numpy.ndarray) else z + x for x in (fxx, fxy, fxz, fyx, fyy, fyz, fzx, fzy, fzz)]
+        return self.grid.divt(*f)
 
     def dd8x(self, v):
         return self.grid.dd8(0, v)

@@ -768,6 +768,21 @@ void apply_dir(const og_handle* h, int op, int dir, const double* in, double* ou
 
 }  // namespace
 
+namespace {
+// mesh.f90:172-175: xgrid(i) = x1 + REAL(2*i-1)*half*dx (the radius on cylindrical grids)
+double xgrid(const og_handle* h, size_t p) {
+  const int i = (int)(p % (size_t)h->n[0]) + 1;
+  return h->x1f[0] + (double)(2 * i - 1) * 0.5 * h->d[0];
+}
+// mesh.f90:213-225: CellVol of a cylindrical grid (d1 = dx, d2 = r dy, d3 = dz)
+double cellvol_cyl(const og_handle* h, size_t p) {
+  const double pi = std::acos(-1.0), r = xgrid(h, p);
+  if (h->n[1] == 1) return h->d[0] * 2.0 * pi * r * h->d[2];
+  return h->d[0] * (r * h->d[1]) * h->d[2];
+}
+int isym_pow(const og_handle* h, int d, int p) { return (h->symm[d] && (p & 1)) ? -1 : 1; }
+}  // namespace
+
 extern "C" {
 
 int og_create2(const int* n, const int* periodic, const int* bc, int coordsys, const double* x1, const double* xn,
@@ -895,6 +910,15 @@ int og_filter3(const og_handle* h, int op, const double* in, double* out) {
   if (!h || (op != 2 && op != 3)) return 1;
   const size_t np = (size_t)h->n[0] * h->n[1] * h->n[2];
   std::vector<double> tmp(np);
+  if (h->coordsys == 1 && op == 2) {  // 'spectral' on a cylindrical grid: operators.f90:876-883
+    std::vector<double> fv(np);
+    for (size_t p = 0; p < np; p++) fv[p] = in[p] * cellvol_cyl(h, p);
+    apply_dir(h, op, 0, fv.data(), out, -1);  // xasym = -xasym: CellVol is odd in r
+    apply_dir(h, op, 1, out, tmp.data(), 1);
+    apply_dir(h, op, 2, tmp.data(), out, 1);
+    for (size_t p = 0; p < np; p++) out[p] = out[p] / cellvol_cyl(h, p);
+    return 0;
+  }
   apply_dir(h, op, 0, in, out);
   apply_dir(h, op, 1, out, tmp.data());
   apply_dir(h, op, 2, tmp.data(), out);
@@ -951,12 +975,58 @@ int og_ringv(const og_handle* h, const double* f, const double* g, const double*
   return 0;
 }
 
-// gradS (Cartesian): operators.f90:184-191
+// gradS: operators.f90:184-212 (cylindrical: dfdy = dfdy/xgrid, :193-196)
 int og_grad(const og_handle* h, const double* f, double* gx, double* gy, double* gz) {
   if (!h) return 1;
   apply_dir(h, OP_D1, 0, f, gx);
   apply_dir(h, OP_D1, 1, f, gy);
   apply_dir(h, OP_D1, 2, f, gz);
+  if (h->coordsys == 1) {
+    const size_t np = (size_t)h->n[0] * h->n[1] * h->n[2];
+    for (size_t p = 0; p < np; p++) gy[p] = gy[p] / xgrid(h, p);
+  }
+  return 0;
+}
+
+// divT: operators.f90:97-146 (Cartesian :104-122, cylindrical :123-146).
+// f: fxx fxy fxz fyx fyy fyz fzx fzy fzz; out: dfx dfy dfz
+int og_divt(const og_handle* h, const double* const* f, double* const* out) {
+  if (!h) return 1;
+  const size_t np = (size_t)h->n[0] * h->n[1] * h->n[2];
+  std::vector<double> tmp(np), fA(np), fB(np), fC(np);
+  const double *fxx = f[0], *fxy = f[1], *fxz = f[2], *fyx = f[3], *fyy = f[4], *fyz = f[5], *fzx = f[6],
+               *fzy = f[7], *fzz = f[8];
+  if (h->coordsys == 0) {
+    const double* cols[3][3] = {{fxx, fyx, fzx}, {fxy, fyy, fzy}, {fxz, fyz, fzz}};
+    for (int c = 0; c < 3; c++) {
+      apply_dir(h, OP_D1, 0, cols[c][0], fA.data(), isym_pow(h, 0, c == 0 ? 2 : 1));
+      apply_dir(h, OP_D1, 1, cols[c][1], fB.data(), isym_pow(h, 1, c == 1 ? 2 : 1));
+      apply_dir(h, OP_D1, 2, cols[c][2], fC.data(), isym_pow(h, 2, c == 2 ? 2 : 1));
+      for (size_t p = 0; p < np; p++) out[c][p] = fA[p] + fB[p] + fC[p];
+    }
+    return 0;
+  }
+  for (size_t p = 0; p < np; p++) tmp[p] = xgrid(h, p) * fxx[p];
+  apply_dir(h, OP_D1, 0, tmp.data(), fA.data(), isym_pow(h, 0, 3));
+  apply_dir(h, OP_D1, 1, fyx, fB.data(), isym_pow(h, 1, 1));
+  apply_dir(h, OP_D1, 2, fzx, fC.data(), isym_pow(h, 2, 1));
+  for (size_t p = 0; p < np; p++) {
+    const double r = xgrid(h, p);
+    out[0][p] = (fA[p] + fB[p] - fyy[p]) / r + fC[p];
+    tmp[p] = r * r * fxy[p];
+  }
+  apply_dir(h, OP_D1, 0, tmp.data(), fA.data(), isym_pow(h, 0, 3));
+  apply_dir(h, OP_D1, 1, fyy, fB.data(), isym_pow(h, 1, 2));
+  apply_dir(h, OP_D1, 2, fzy, fC.data(), isym_pow(h, 2, 1));
+  for (size_t p = 0; p < np; p++) {
+    const double r = xgrid(h, p);
+    out[1][p] = fA[p] / (r * r) + (fB[p] + fyx[p] - fxy[p]) / r + fC[p];
+    tmp[p] = r * fxz[p];
+  }
+  apply_dir(h, OP_D1, 0, tmp.data(), fA.data(), isym_pow(h, 0, 2));
+  apply_dir(h, OP_D1, 1, fyz, fB.data(), isym_pow(h, 1, 1));
+  apply_dir(h, OP_D1, 2, fzz, fC.data(), isym_pow(h, 2, 2));
+  for (size_t p = 0; p < np; p++) out[2][p] = (fA[p] + fB[p]) / xgrid(h, p) + fC[p];
   return 0;
 }
 
@@ -965,6 +1035,15 @@ int og_div(const og_handle* h, const double* fx, const double* fy, const double*
   if (!h) return 1;
   const size_t np = (size_t)h->n[0] * h->n[1] * h->n[2];
   std::vector<double> a(np), b(np);
+  if (h->coordsys == 1) {  // operators.f90:55-64
+    std::vector<double> tmp(np), c(np);
+    for (size_t p = 0; p < np; p++) tmp[p] = xgrid(h, p) * fx[p];
+    apply_dir(h, OP_D1, 0, tmp.data(), a.data(), isym_pow(h, 0, 2));
+    apply_dir(h, OP_D1, 1, fy, b.data(), isym_pow(h, 1, 1));
+    apply_dir(h, OP_D1, 2, fz, c.data(), isym_pow(h, 2, 1));
+    for (size_t p = 0; p < np; p++) out[p] = (a[p] + b[p]) / xgrid(h, p) + c[p];
+    return 0;
+  }
   // ddx(fx, fA, isymX) ... (operators.f90:47-50)
   apply_dir(h, OP_D1, 0, fx, out, h->symm[0] ? -1 : 1);
   apply_dir(h, OP_D1, 1, fy, a.data(), h->symm[1] ? -1 : 1);
@@ -986,6 +1065,19 @@ int og_mesh(const og_handle* h, int which, double* out) {
       for (int i = 0; i < nx; i++) {
         const size_t p = ((size_t)k * ny + j) * nx + i;
         double v = 0.0;
+        if (h->coordsys == 1 && which >= 3) {  // mesh.f90:213-225
+          const double r = h->x1f[0] + (double)(2 * (i + 1) - 1) * 0.5 * h->d[0];
+          const double d2 = r * h->d[1];
+          switch (which) {
+            case 3: v = h->d[0]; break;
+            case 4: v = d2; break;
+            case 5: v = h->d[2]; break;
+            case 6: v = (ny == 1) ? std::min(h->d[0], h->d[2]) : std::min(std::min(h->d[0], d2), h->d[2]); break;
+            default: v = cellvol_cyl(h, p); break;
+          }
+          out[p] = v;
+          continue;
+        }
         switch (which) {
           case 0: v = h->x1f[0] + (double)(2 * (i + 1) - 1) * 0.5 * h->d[0]; break;
           case 1: v = h->x1f[1] + (double)(2 * (j + 1) - 1) * 0.5 * h->d[1]; break;

@@ -89,6 +89,7 @@ SIGNATURES = [
     ("pg_ringv", I, [P, D, D, D, D, P]),
     ("pg_grad", I, [P, D, D, D, D, P]),
     ("pg_div", I, [P, D, D, D, D, P]),
+    ("pg_divt", I, [P, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p), P]),
     ("pg_mesh", I, [P, I, D, P]),
     ("pg_rk_stage", I, [P, I, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
                         ctypes.POINTER(ctypes.c_void_p), D, ctypes.c_double, ctypes.c_double, P]),

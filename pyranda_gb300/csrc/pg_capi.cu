@@ -125,6 +125,7 @@ struct Ctx {
   OpRef anti[2][OPK_COUNT][3];   // the antisymmetric variants (differ where a direction has a symmetry plane)
   bool symm[3] = {false, false, false};
   int coordsys = PG_CARTESIAN;
+  double* cyl[3] = {nullptr, nullptr, nullptr};  // cylindrical grids: three workspace fields
   void* blob = nullptr;          // coefficient tables and member-op arrays
   double* work = nullptr;        // one field: x->y->z filter ping-pong
   double* work2 = nullptr;       // one field: forward-elimination scratch of a sweep
@@ -167,6 +168,8 @@ void free_ctx(Ctx& c) {
   if (c.stream) cudaStreamDestroy(c.stream);
   if (c.dense_blob) cudaFree(c.dense_blob);
   if (c.split_blob) cudaFree(c.split_blob);
+  for (int q = 0; q < 3; q++)
+    if (c.cyl[q]) cudaFree(c.cyl[q]);
   c = Ctx();
 }
 
@@ -328,6 +331,8 @@ int build_ctx(Ctx& c, const std::vector<GridInfo>& g, int precision, const char*
   const size_t nbytes = (size_t)c.npts * sizeof(double);
   if (e == cudaSuccess) e = cudaMalloc(&c.work, nbytes);
   if (e == cudaSuccess) e = cudaMalloc(&c.work2, nbytes);
+  if (g[0].coordsys == PG_CYLINDRICAL)
+    for (int q = 0; q < 3 && e == cudaSuccess; q++) e = cudaMalloc(&c.cyl[q], nbytes);
   // two values per block for the two-pass diffusion limit (estimate, exact-point flag)
   const size_t npart = std::max((size_t)2 * kReduceBlocks, (size_t)M * kSegBlocks + 2 * (size_t)M);
   if (e == cudaSuccess) e = cudaMalloc(&c.partial, npart * sizeof(double));
@@ -1111,6 +1116,72 @@ const char* pg_version(void) { return "pyranda_gb300 0.2 (sm_103a)"; }
 
 uint64_t pg_launch_count(void) { return g_launches.load(); }
 
+namespace pg {
+namespace {
+
+// isym^p of a direction (patch.f90:89-91): -1 for odd p where the direction has a SYMM end
+int isym(const Ctx& c, int d, int p) { return (c.symm[d] && (p & 1)) ? -1 : 1; }
+
+int cyl(const pg_handle* h, int op, const double* a, const double* b, const double* c_, const double* e,
+        const double* f, double* out, void* st) {
+  const GridInfo& g = h->g;
+  return launch_cyl(op, g.npts, g.n[0], g.n[1], g.x1f[0], g.d[0], g.d[1], g.d[2], a, b, c_, e, f, out, st);
+}
+
+// divV, cylindrical (operators.f90:55-64): (d(r fx)/dr + dfy/dy) / r + dfz/dz
+int divergence_cyl(pg_handle* h, const double* fx, const double* fy, const double* fz, double* out, void* st) {
+  Ctx& c = h->c;
+  int rc = cyl(h, CYL_MUL_R, fx, nullptr, nullptr, nullptr, nullptr, c.cyl[0], st);
+  if (!rc) rc = apply_one(c, OPK_D1, 0, c.cyl[0], c.cyl[1], st, isym(c, 0, 2));
+  if (!rc) rc = apply_one(c, OPK_D1, 1, fy, c.cyl[2], st, isym(c, 1, 1));
+  if (!rc) rc = apply_one(c, OPK_D1, 2, fz, out, st, isym(c, 2, 1));
+  if (!rc) rc = cyl(h, CYL_DIVV, c.cyl[1], c.cyl[2], out, nullptr, nullptr, out, st);
+  return rc;
+}
+
+// divT (operators.f90:97-146): Cartesian and cylindrical.  f = {fxx, fxy, fxz,
+// fyx, fyy, fyz, fzx, fzy, fzz}; out = {dfx, dfy, dfz}, distinct from f.
+int divt(pg_handle* h, const double* const* f, double* const* out, void* st) {
+  Ctx& c = h->c;
+  const double *fxx = f[0], *fxy = f[1], *fxz = f[2], *fyx = f[3], *fyy = f[4], *fyz = f[5], *fzx = f[6],
+               *fzy = f[7], *fzz = f[8];
+  int rc = PG_OK;
+  if (c.coordsys == PG_CARTESIAN) {  // :104-122: dfx = d(fxx)/dx + d(fyx)/dy + d(fzx)/dz ...
+    const double* cols[3][3] = {{fxx, fyx, fzx}, {fxy, fyy, fzy}, {fxz, fyz, fzz}};
+    for (int comp = 0; comp < 3 && !rc; comp++) {
+      bool first = true;
+      for (int d = 0; d < 3 && !rc; d++) {
+        if (c.ops[c.precision][OPK_D1][d].null_op) continue;
+        rc = sweep(c, OPK_D1, d, cols[comp][d], out[comp], first ? EPI_STORE : EPI_ADD, 0, st, false,
+                   isym(c, d, d == comp ? 2 : 1));
+        first = false;
+      }
+      if (!rc && first) rc = launch_fill(out[comp], 0.0, c.npts, st);
+    }
+    return rc;
+  }
+  // cylindrical (:123-146)
+  rc = cyl(h, CYL_MUL_R, fxx, nullptr, nullptr, nullptr, nullptr, c.cyl[0], st);
+  if (!rc) rc = apply_one(c, OPK_D1, 0, c.cyl[0], c.cyl[1], st, isym(c, 0, 3));
+  if (!rc) rc = apply_one(c, OPK_D1, 1, fyx, c.cyl[2], st, isym(c, 1, 1));
+  if (!rc) rc = apply_one(c, OPK_D1, 2, fzx, out[0], st, isym(c, 2, 1));
+  if (!rc) rc = cyl(h, CYL_DIVT_X, c.cyl[1], c.cyl[2], out[0], fyy, nullptr, out[0], st);
+  if (!rc) rc = cyl(h, CYL_MUL_R2, fxy, nullptr, nullptr, nullptr, nullptr, c.cyl[0], st);
+  if (!rc) rc = apply_one(c, OPK_D1, 0, c.cyl[0], c.cyl[1], st, isym(c, 0, 3));
+  if (!rc) rc = apply_one(c, OPK_D1, 1, fyy, c.cyl[2], st, isym(c, 1, 2));
+  if (!rc) rc = apply_one(c, OPK_D1, 2, fzy, out[1], st, isym(c, 2, 1));
+  if (!rc) rc = cyl(h, CYL_DIVT_Y, c.cyl[1], c.cyl[2], out[1], fyx, fxy, out[1], st);
+  if (!rc) rc = cyl(h, CYL_MUL_R, fxz, nullptr, nullptr, nullptr, nullptr, c.cyl[0], st);
+  if (!rc) rc = apply_one(c, OPK_D1, 0, c.cyl[0], c.cyl[1], st, isym(c, 0, 2));
+  if (!rc) rc = apply_one(c, OPK_D1, 1, fyz, c.cyl[2], st, isym(c, 1, 1));
+  if (!rc) rc = apply_one(c, OPK_D1, 2, fzz, out[2], st, isym(c, 2, 2));
+  if (!rc) rc = cyl(h, CYL_DIVV, c.cyl[1], c.cyl[2], out[2], nullptr, nullptr, out[2], st);
+  return rc;
+}
+
+}  // namespace
+}  // namespace pg
+
 int pg_create(const pg_grid* grid, pg_handle** out) {
   if (!grid || !out) {
     set_error("pg_create: NULL argument");
@@ -1219,6 +1290,20 @@ int pg_filter(pg_handle* h, int kind, int dir, const double* in, double* out, vo
   if (!h || !in || !out || (kind != PG_SPECTRAL && kind != PG_GAUSSIAN) || dir < 0 || dir > 3) return PG_EINVAL;
   const int k = kind == PG_SPECTRAL ? OPK_SF : OPK_GF;
   if (dir < 3) return apply_one(h->c, k, dir, in, out, stream);
+  if (h->c.coordsys == PG_CYLINDRICAL && kind == PG_SPECTRAL) {
+    // operators.f90:876-883: filter the volume-weighted field (CellVol is odd in r, so the radial
+    // sweep takes the antisymmetric variant) and divide by the cell volume
+    if (in == out) {
+      set_error("pg_filter: on a cylindrical grid out must not alias in");
+      return PG_EINVAL;
+    }
+    Ctx& c = h->c;
+    const int sym[3] = {-1, 1, 1};
+    int rc = cyl(h, CYL_CELLVOL_MUL, in, nullptr, nullptr, nullptr, nullptr, c.cyl[0], stream);
+    if (!rc) rc = filter_all(c, k, c.cyl[0], out, stream, sym);
+    if (!rc) rc = cyl(h, CYL_CELLVOL_DIV, out, nullptr, nullptr, nullptr, nullptr, out, stream);
+    return rc;
+  }
   return filter_all(h->c, k, in, out, stream);
 }
 
@@ -1262,10 +1347,32 @@ int pg_ringv(pg_handle* h, const double* vx, const double* vy, const double* vz,
 
 int pg_grad(pg_handle* h, const double* in, double* gx, double* gy, double* gz, void* stream) {
   if (!h || !in || !gx || !gy || !gz) return PG_EINVAL;
-  return grad(h->c, in, gx, gy, gz, stream);
+  int rc = grad(h->c, in, gx, gy, gz, stream);
+  if (!rc && h->c.coordsys == PG_CYLINDRICAL)  // operators.f90:193-196: dfdy / r
+    rc = cyl(h, CYL_DIV_R, gy, nullptr, nullptr, nullptr, nullptr, gy, stream);
+  return rc;
+}
+
+int pg_divt(pg_handle* h, const double* const* f, double* const* out, void* stream) {
+  if (!h || !f || !out) return PG_EINVAL;
+  for (int q = 0; q < 9; q++)
+    if (!f[q]) return PG_EINVAL;
+  for (int q = 0; q < 3; q++) {
+    if (!out[q]) return PG_EINVAL;
+    for (int r = 0; r < 9; r++)
+      if (out[q] == f[r]) {
+        set_error("pg_divt: outputs must not alias inputs");
+        return PG_EINVAL;
+      }
+  }
+  return divt(h, f, out, stream);
 }
 
 int pg_div(pg_handle* h, const double* fx, const double* fy, const double* fz, double* out, void* stream) {
+  if (h && h->c.coordsys == PG_CYLINDRICAL) {
+    if (!fx || !fy || !fz || !out) return PG_EINVAL;
+    return divergence_cyl(h, fx, fy, fz, out, stream);
+  }
   if (!h || !fx || !fy || !fz || !out) return PG_EINVAL;
   if (out == fy || out == fz) {
     set_error("pg_div: out must not alias fy or fz");
@@ -1277,6 +1384,15 @@ int pg_div(pg_handle* h, const double* fx, const double* fy, const double* fz, d
 int pg_mesh(pg_handle* h, int which, double* out, void* stream) {
   if (!h || !out || which < 0 || which > 7) return PG_EINVAL;
   const GridInfo& g = h->g;
+  if (g.coordsys == PG_CYLINDRICAL && (which == PG_MESH_D2 || which == PG_MESH_GRIDLEN || which == PG_MESH_CELLVOL)) {
+    // mesh.f90:213-225: d2 = r dy, GridLen and CellVol vary with the radius
+    const int op = which == PG_MESH_D2 ? CYL_D2 : (which == PG_MESH_GRIDLEN ? CYL_GRIDLEN : CYL_CELLVOL);
+    return cyl(h, op, nullptr, nullptr, nullptr, nullptr, nullptr, out, stream);
+  }
+  if (g.coordsys == PG_CYLINDRICAL && (which == PG_MESH_D1 || which == PG_MESH_D3)) {
+    const double dd[3] = {g.d[0], g.d[1], g.d[2]};  // d1 = dx, d3 = dz (mesh.f90:214-216)
+    return launch_mesh(which, out, g.n[0], g.n[1], g.n[2], g.x1f, g.d, dd, stream);
+  }
   return launch_mesh(which, out, g.n[0], g.n[1], g.n[2], g.x1f, g.d, g.dm, stream);
 }
 
@@ -1291,6 +1407,10 @@ int pg_courant(pg_handle* h, const double* u, const double* v, const double* w, 
                double wconst, double* out, void* stream) {
   if (!h || !u || !c || !out) return PG_EINVAL;
   const GridInfo& g = h->g;
+  if (g.coordsys == PG_CYLINDRICAL && g.n[1] > 1) {
+    set_error("pg_courant: cylindrical grids with more than one point in angle are not supported");
+    return PG_EINVAL;
+  }
   const double gl = std::min(std::min(g.dm[0], g.dm[1]), g.dm[2]);
   return launch_courant(u, v, w, c, vconst, wconst, g.dm, gl, h->c.npts, h->c.partial, out, stream);
 }
@@ -1298,6 +1418,10 @@ int pg_courant(pg_handle* h, const double* u, const double* v, const double* w, 
 int pg_diff(pg_handle* h, const double* bulk, const double* rho, double* out, void* stream) {
   if (!h || !bulk || !rho || !out) return PG_EINVAL;
   const GridInfo& g = h->g;
+  if (g.coordsys == PG_CYLINDRICAL && g.n[1] > 1) {
+    set_error("pg_diff: cylindrical grids with more than one point in angle are not supported");
+    return PG_EINVAL;
+  }
   const double gl = std::min(std::min(g.dm[0], g.dm[1]), g.dm[2]);
   return launch_diff(bulk, rho, gl, h->c.npts, h->c.partial, out, stream);
 }
@@ -1364,6 +1488,11 @@ int pg_ens_create(int m, const pg_grid* grids, pg_ensemble** out) {
         grids[i].precision < PG_FP64 || grids[i].precision > PG_AUTO) {
       delete e;
       set_error("pg_ens_create: members must share one valid precision");
+      return PG_EINVAL;
+    }
+    if (grids[i].coordsys != PG_CARTESIAN) {
+      set_error("pg_ens_create: ensembles are Cartesian");
+      delete e;
       return PG_EINVAL;
     }
     int rc = grid_info(&grids[i], e->g[i], "pg_ens_create");

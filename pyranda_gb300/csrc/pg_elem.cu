@@ -456,6 +456,51 @@ int launch_check_finite(const double* in, int64_t n, int* flag, void* stream) {
   return check("check_finite");
 }
 
+// Cylindrical-coordinate pointwise forms (x = radius r, mesh.f90:172-175:
+// r = x1 + (2 i - 1) dx / 2, evaluated without contraction as the mesh is).
+// CellVol = d1 2 pi r d3 for one point along y, else d1 (r dy) d3 (mesh.f90:213-225).
+__device__ __forceinline__ double cyl_radius(int64_t p, int nx, double x1, double dx) {
+  const int i = (int)(p % nx);
+  return __dadd_rn(x1, __dmul_rn(__dmul_rn((double)(2 * (i + 1) - 1), 0.5), dx));
+}
+
+__global__ void cyl_kernel(int op, int64_t n, int nx, int ny, double x1, double dx, double dy, double dz,
+                           const double* __restrict__ a, const double* __restrict__ b, const double* __restrict__ c,
+                           const double* __restrict__ e, const double* __restrict__ f, double* __restrict__ out) {
+  const double pi = 3.141592653589793;  // acos(-1) in FP64
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    const double r = cyl_radius(p, nx, x1, dx);
+    double v;
+    switch (op) {
+      case CYL_MUL_R: v = __dmul_rn(r, a[p]); break;                    // xgrid*f
+      case CYL_MUL_R2: v = __dmul_rn(__dmul_rn(r, r), a[p]); break;     // xgrid**2*f
+      case CYL_DIV_R: v = a[p] / r; break;                              // f/xgrid
+      case CYL_DIVV: v = __dadd_rn(__dadd_rn(a[p], b[p]) / r, c[p]); break;  // (fA+fB)/xgrid + fC
+      case CYL_DIVT_X:  // (fA+fB-fyy)/xgrid + fC
+        v = __dadd_rn(__dsub_rn(__dadd_rn(a[p], b[p]), e[p]) / r, c[p]);
+        break;
+      case CYL_DIVT_Y:  // fA/xgrid**2 + (fB+fyx-fxy)/xgrid + fC
+        v = __dadd_rn(__dadd_rn(a[p] / __dmul_rn(r, r), __dsub_rn(__dadd_rn(b[p], e[p]), f[p]) / r), c[p]);
+        break;
+      default: {  // CYL_CELLVOL_MUL / CYL_CELLVOL_DIV
+        const double cv = (ny == 1) ? __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(dx, 2.0), pi), r), dz)
+                                    : __dmul_rn(__dmul_rn(dx, __dmul_rn(r, dy)), dz);
+        v = (op == CYL_CELLVOL_MUL) ? __dmul_rn(a[p], cv) : a[p] / cv;
+        if (op == CYL_CELLVOL) v = cv;
+        if (op == CYL_D2) v = __dmul_rn(r, dy);
+        if (op == CYL_GRIDLEN) v = (ny == 1) ? fmin(dx, dz) : fmin(fmin(dx, __dmul_rn(r, dy)), dz);
+      }
+    }
+    out[p] = v;
+  }
+}
+
+int launch_cyl(int op, int64_t n, int nx, int ny, double x1, double dx, double dy, double dz, const double* a,
+               const double* b, const double* c, const double* e, const double* f, double* out, void* stream) {
+  cyl_kernel<<<grid_for(n), kThreads, 0, (cudaStream_t)stream>>>(op, n, nx, ny, x1, dx, dy, dz, a, b, c, e, f, out);
+  return check("cylindrical form");
+}
+
 int launch_mesh(int which, double* out, int nx, int ny, int nz, const double x1f[3], const double d[3],
                 const double dm[3], void* stream) {
   double cval = 0.0;

@@ -184,6 +184,22 @@ int launch_check_finite(const double* in, int64_t n, int* flag, void* stream);
 int launch_max_exponent(const double* in, const long long* moff, int nmem, int* emax, void* stream);
 int launch_mesh(int which, double* out, int nx, int ny, int nz, const double x1f[3],
                 const double d[3], const double dm[3], void* stream);
+// Cylindrical pointwise forms (r = the radius of the point's x index):
+enum {
+  CYL_MUL_R = 0,        // out = r a
+  CYL_MUL_R2 = 1,       // out = r^2 a
+  CYL_DIV_R = 2,        // out = a / r
+  CYL_DIVV = 3,         // out = (a + b) / r + c
+  CYL_DIVT_X = 4,       // out = (a + b - e) / r + c
+  CYL_DIVT_Y = 5,       // out = a / r^2 + (b + e - f) / r + c
+  CYL_CELLVOL_MUL = 6,  // out = a CellVol
+  CYL_CELLVOL_DIV = 7,  // out = a / CellVol
+  CYL_CELLVOL = 8,      // out = CellVol
+  CYL_D2 = 9,           // out = r dy
+  CYL_GRIDLEN = 10      // out = GridLen
+};
+int launch_cyl(int op, int64_t n, int nx, int ny, double x1, double dx, double dy, double dz, const double* a,
+               const double* b, const double* c, const double* e, const double* f, double* out, void* stream);
 
 // Number of blocks used by the two-pass reductions (partial buffer length).
 constexpr int kReduceBlocks = 1024;

@@ -234,8 +234,13 @@ class Grid:
         return out
 
     def divT(self, fxx, fxy, fxz, fyx, fyy, fyz, fzx, fzy, fzz):
-        """Divergence of a tensor (operators.f90:97-123, Cartesian): the divergences of its columns."""
-        return [self.div(fxx, fyx, fzx), self.div(fxy, fyy, fzy), self.div(fxz, fyz, fzz)]
+        """Divergence of a tensor (operators.f90:97-146, Cartesian and cylindrical)."""
+        f = [self.field(x) for x in (fxx, fxy, fxz, fyx, fyy, fyz, fzx, fzy, fzz)]
+        out = [self.empty() for _ in range(3)]
+        fp = (ctypes.c_void_p * 9)(*[x.data_ptr() for x in f])
+        op = (ctypes.c_void_p * 3)(*[x.data_ptr() for x in out])
+        _lib.check(self.lib.pg_divt(self.h, fp, op, _stream()), "pg_divt")
+        return out
 
     def filter(self, kind, v, direction=_lib.PG_DIR_ALL, out=None, sym=None):
         """kind 'spectral' (c8ff8, fbar) or 'gaussian' (cgfs4, gbar); sym: per direction +1 / -1

@@ -262,13 +262,16 @@ class pyrandaSim:
             meshOptions = self._parse_mesh(meshOptions)
         opts = defaultMeshOptions()
         opts.update(meshOptions)
-        if opts.get("coordsys", 0) != 0:
-            raise ValueError("only Cartesian meshes (coordsys=0) are supported")
-        if any(any(s) for s in opts["symmetric"]):
-            raise ValueError("SYMM boundaries are not supported; use periodic or one-sided (NONE)")
+        coordsys = int(opts.get("coordsys", 0))
+        if coordsys not in (0, 1):
+            raise ValueError("coordsys %d: Cartesian (0) and cylindrical (1) meshes are supported" % coordsys)
+        # pyrandaMPI.py:101-131: a symmetric end of a non-periodic direction is SYMM, else NONE
+        sym = opts["symmetric"]
+        bc = tuple(tuple("SYMM" if (sym[d][e] and not opts["periodic"][d]) else "NONE" for e in range(2))
+                   for d in range(3))
         self.meshOptions = opts
         self.mesh.options = opts
-        self.mesh.coordsys = 0
+        self.mesh.coordsys = coordsys
         nx, ny, nz = [int(v) for v in opts["nn"]]
         self.nx, self.ny, self.nz = nx, ny, nz
         self.npts = nx * ny * nz
@@ -276,7 +279,8 @@ class pyrandaSim:
         self.dy = (opts["xn"][1] - opts["x1"][1]) / max(ny - 1, 1)
         self.dz = (opts["xn"][2] - opts["x1"][2]) / max(nz - 1, 1)
         self.precision = precision
-        self.grid = Grid((nx, ny, nz), opts["periodic"], opts["x1"], opts["xn"], precision=precision, device=device)
+        self.grid = Grid((nx, ny, nz), opts["periodic"], opts["x1"], opts["xn"], precision=precision, device=device,
+                         bc=bc, coordsys=coordsys)
         self.PyMPI = pyrandaGPU(self)
         self.mesh.PyMPI = self.PyMPI
         self._make_mesh()

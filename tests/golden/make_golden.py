@@ -26,6 +26,7 @@ PROFILES = {  # test name -> baseline file (tests/cases/test2deuler.py:3-9)
     "euler-2d-64": "euler-2d-64.dat",
     "euler-2d-128": "euler-2d-128.dat",
     "KH-2d-64": "KelvinHelmholtzKH-2d-64.dat",
+    "euler-RZ-128": "euler-RZ-128.dat",
 }
 
 

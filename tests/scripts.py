@@ -358,3 +358,63 @@ def profile_error(golden_path, x, v):
     base = numpy.loadtxt(golden_path)
     m = min(base.shape[1], len(v))
     return float(numpy.max(numpy.abs(base[1, :m] - numpy.asarray(v)[:m])) / numpy.max(numpy.abs(base[1, :m])))
+
+
+EULER_RZ_EOM = """
+# Primary Equations of motion here
+ddt(:rho:)  =  -:mass:
+ddt(:rhou:) =  -:xmom:
+ddt(:rhow:) =  -:zmom:
+ddt(:Et:)   =  -div( (:Et: + :p: - :tau:)*:u:,:v:, (:Et: + :p: - :tau:)*:w: )
+# Conservative filter of the EoM
+:rho:       =  fbar( :rho:  )
+:rhou:      =  fbar( :rhou: )
+:rhow:      =  fbar( :rhow: )
+:Et:        =  fbar( :Et:   )
+# Update the primatives and enforce the EOS
+:u:         =  :rhou: / :rho:
+:w:         =  :rhow: / :rho:
+:p:         =  ( :Et: - .5*:rho:*(:u:*:u: + :w:*:w:) ) * ( :gamma: - 1.0 )
+# Artificial bulk viscosity (old school way)
+:div:       =  div(:u:,:v:,:w:)
+:beta:      =  gbar(abs(ring(:div:))) * :rho: * 7.0e-2
+:tau:       =  :beta:*:div:
+:v:         = :v: * 0.0
+# Compute divT of momentum
+:mass: = div(:rho:*:u:               , :v:, :rho:*:w:)
+[:fxx:,:fxy:,:fxz:] = [:rhou:*:u: + :p: - :tau:, :v:, :rhou:*:w:]
+[:fyx:,:fyy:,:fyz:] = [      :v:               , :p:-:tau: , :v:       ]
+[:fzx:,:fzy:,:fzz:] = [:rhow:*:u:,               :v:, :rhow:*:w: + :p: - :tau:]
+[:xmom:,:ymom:,:zmom:] = divT(:fxx:,:fxy:,:fxz:,:fyx:,:fyy:,:fyz:,:fzx:,:fzy:,:fzz:)
+"""
+
+
+def euler_rz(Sim, Npts, packages, **kw):
+    """examples/eulerRZ.py N 1 (tests/cases/test2deuler.py euler-RZ-128): a
+    cylindrical (r, z) Sod problem with a symmetry plane at the axis, run to
+    t = 0.5; returns (r, p) with p along z at r index N/2, the profile the
+    test compares."""
+    L = numpy.pi * 2.0
+    dx2 = L / (Npts - 1) / 2.0
+    opts = {"coordsys": 1, "periodic": [False, False, True], "x1": [dx2, -0.1, 0.0], "xn": [L, 0.1, L],
+            "nn": [Npts, 1, Npts], "symmetric": [[True, False], [False, False], [False, False]]}
+    ss = Sim("advection", opts, **kw)
+    packages(ss)
+    ss.EOM(EULER_RZ_EOM)
+    ss.setIC("""rad = sqrt( (meshx-pi)**2  +  (meshz-pi)**2 )
+:gamma: = 1.4
+wgt = .5*(1.0-tanh( (rad-pi/2.0)/.1) )   # [0,1]
+:Et:  = 1.0/(:gamma:-1.0) * (wgt*.9 + .1)
+:rho: = 1.0*wgt + (1.0-wgt)*.125
+""")
+    time = 0.0
+    dt_max = 1.0 / Npts * 0.75
+    tt = 0.5
+    dt = dt_max
+    while tt > time:
+        time = ss.rk4(time, dt)
+        dt = min(dt_max, (tt - time))
+    half = int(Npts / 2.0)
+    x = _host(_meshx(ss))[:, 0, 0]
+    p = _host(ss.variables["p"].data)[half, 0, :]
+    return x, p

@@ -122,3 +122,14 @@ def test_kelvin_helmholtz_2d_profile(oracle):
     path = os.path.join(GOLDEN_DIR, "KelvinHelmholtzKH-2d-64.dat")
     assert numpy.abs(x - numpy.loadtxt(path)[0]).max() < 1e-12
     assert scripts.profile_error(path, x, rho) < 1e-10
+
+
+def test_euler_rz_profile(oracle):
+    """tests/cases/test2deuler.py euler-RZ-128 (examples/eulerRZ.py): cylindrical
+    coordinates with a symmetry plane at the axis -- the cylindrical div / divT
+    (operators.f90:55-64, :123-146), the volume-weighted filter (:876-883) and
+    the symmetric / antisymmetric operator variants (stencils.f90:2390-2453)."""
+    x, p = scripts.euler_rz(oracle.OracleSim, 128, lambda s: s.addPackage("BC"))
+    path = os.path.join(GOLDEN_DIR, "euler-RZ-128.dat")
+    assert numpy.abs(x - numpy.loadtxt(path)[0]).max() < 1e-12
+    assert scripts.profile_error(path, x, p) < 1e-10

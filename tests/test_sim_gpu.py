@@ -350,3 +350,19 @@ def test_shock_interface_full_size_step_matches_oracle(oracle):
     so.rk4(0.0, dto)
     _fields_match(ss, so, ["rho", "rhou", "rhov", "rhow", "Et", "u", "p", "mu"],
                   scale={"rhov": "rhou", "rhow": "rhou"})
+
+
+def test_euler_rz_profile_golden(oracle):
+    """tests/cases/test2deuler.py euler-RZ-128 (examples/eulerRZ.py): the GPU
+    pyrandaSim on a cylindrical mesh with a symmetry plane at the axis
+    reproduces the reference's pressure profile within its tolerance, and the
+    oracle's profile to rounding."""
+    from pyranda_gb300 import pyrandaSim, pyrandaBC
+    path = os.path.join(GOLDEN_DIR, "euler-RZ-128.dat")
+    x, p = scripts.euler_rz(pyrandaSim, 128, lambda s: s.addPackage(pyrandaBC(s)), silent=True)
+    err = scripts.profile_error(path, x, p)
+    assert err < 1.0e-4, err
+    xo, po = scripts.euler_rz(oracle.OracleSim, 128, lambda s: s.addPackage("BC"))
+    diff = float(numpy.abs(p - po).max() / numpy.abs(po).max())
+    print("euler-RZ-128: profile error %.2e, max difference from the oracle %.2e" % (err, diff))
+    assert diff <= 1e-10, diff
