@@ -464,9 +464,11 @@ __device__ __forceinline__ double cyl_radius(int64_t p, int nx, double x1, doubl
   return __dadd_rn(x1, __dmul_rn(__dmul_rn((double)(2 * (i + 1) - 1), 0.5), dx));
 }
 
+// out may alias a or c (in-place forms), so no pointer is __restrict__; operands
+// an op does not use may be null and are never read.
 __global__ void cyl_kernel(int op, int64_t n, int nx, int ny, double x1, double dx, double dy, double dz,
-                           const double* __restrict__ a, const double* __restrict__ b, const double* __restrict__ c,
-                           const double* __restrict__ e, const double* __restrict__ f, double* __restrict__ out) {
+                           const double* a, const double* b, const double* c, const double* e, const double* f,
+                           double* out) {
   const double pi = 3.141592653589793;  // acos(-1) in FP64
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
     const double r = cyl_radius(p, nx, x1, dx);
@@ -482,13 +484,14 @@ __global__ void cyl_kernel(int op, int64_t n, int nx, int ny, double x1, double 
       case CYL_DIVT_Y:  // fA/xgrid**2 + (fB+fyx-fxy)/xgrid + fC
         v = __dadd_rn(__dadd_rn(a[p] / __dmul_rn(r, r), __dsub_rn(__dadd_rn(b[p], e[p]), f[p]) / r), c[p]);
         break;
-      default: {  // CYL_CELLVOL_MUL / CYL_CELLVOL_DIV
+      case CYL_D2: v = __dmul_rn(r, dy); break;
+      case CYL_GRIDLEN: v = (ny == 1) ? fmin(dx, dz) : fmin(fmin(dx, __dmul_rn(r, dy)), dz); break;
+      default: {  // CYL_CELLVOL_MUL / CYL_CELLVOL_DIV / CYL_CELLVOL: only the first two read a
         const double cv = (ny == 1) ? __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(dx, 2.0), pi), r), dz)
                                     : __dmul_rn(__dmul_rn(dx, __dmul_rn(r, dy)), dz);
-        v = (op == CYL_CELLVOL_MUL) ? __dmul_rn(a[p], cv) : a[p] / cv;
-        if (op == CYL_CELLVOL) v = cv;
-        if (op == CYL_D2) v = __dmul_rn(r, dy);
-        if (op == CYL_GRIDLEN) v = (ny == 1) ? fmin(dx, dz) : fmin(fmin(dx, __dmul_rn(r, dy)), dz);
+        if (op == CYL_CELLVOL_MUL) v = __dmul_rn(a[p], cv);
+        else if (op == CYL_CELLVOL_DIV) v = a[p] / cv;
+        else v = cv;
       }
     }
     out[p] = v;
@@ -497,6 +500,14 @@ __global__ void cyl_kernel(int op, int64_t n, int nx, int ny, double x1, double 
 
 int launch_cyl(int op, int64_t n, int nx, int ny, double x1, double dx, double dy, double dz, const double* a,
                const double* b, const double* c, const double* e, const double* f, double* out, void* stream) {
+  // operands each form reads: a for 0-7, b and c for the divergences, e for the divT rows, f for DIVT_Y
+  const bool ok = out && op >= CYL_MUL_R && op <= CYL_GRIDLEN && (op > CYL_CELLVOL_DIV || a) &&
+                  (op < CYL_DIVV || op > CYL_DIVT_Y || (b && c)) && (op < CYL_DIVT_X || op > CYL_DIVT_Y || e) &&
+                  (op != CYL_DIVT_Y || f);
+  if (!ok) {
+    set_error("cylindrical form %d: missing operand", op);
+    return PG_EINVAL;
+  }
   cyl_kernel<<<grid_for(n), kThreads, 0, (cudaStream_t)stream>>>(op, n, nx, ny, x1, dx, dy, dz, a, b, c, e, f, out);
   return check("cylindrical form");
 }
