@@ -640,6 +640,7 @@ int build_split_ctx(Ctx& c, const std::vector<GridInfo>& g) {
   struct Uniq {
     int k, n;
     bool per;
+    std::vector<double> lhs;  // the band the tables factor (boundary codes change it at the ends)
     std::vector<int> start, win;
     std::vector<double> row, G;
     size_t off_row[2], off_G[2], off_start, off_win;
@@ -659,12 +660,13 @@ int build_split_ctx(Ctx& c, const std::vector<GridInfo>& g) {
         }
         int u = -1;
         for (size_t q = 0; q < uniq.size() && u < 0; q++)
-          if (uniq[q].k == k && uniq[q].n == n && uniq[q].per == t.periodic) u = (int)q;
+          if (uniq[q].k == k && uniq[q].n == n && uniq[q].per == t.periodic && uniq[q].lhs == t.lhs) u = (int)q;
         if (u < 0) {
           Uniq e;
           e.k = k;
           e.n = n;
           e.per = t.periodic;
+          e.lhs = t.lhs;
           const int rc = build_split(t.lhs, n, t.periodic, e.start, e.row, e.G);
           if (rc) return rc;
           const int S = (int)e.start.size() - 1, T = 4 * S;
@@ -731,10 +733,13 @@ int build_split_ctx(Ctx& c, const std::vector<GridInfo>& g) {
   size_t tile_at[OPK_COUNT][3] = {};
   int tile_n[OPK_COUNT][3] = {};
   size_t sm[3][OPK_COUNT][3] = {};  // fp32, fp64, mixed
+  size_t smseg[OPK_COUNT][3] = {};   // register-resident FP32 form along the direction
+  bool seg32[OPK_COUNT][3] = {};
   for (int k = 0; k < OPK_COUNT; k++)
     for (int d = 0; d < 3; d++) {
       if (!dir_ok[k][d]) continue;
       tile_at[k][d] = tiles.size();
+      seg32[k][d] = true;
       for (int m = 0; m < M; m++) {
         const Uniq& u = uniq[which[((size_t)k * 3 + d) * M + m]];
         const int S = (int)u.start.size() - 1;
@@ -745,6 +750,8 @@ int build_split_ctx(Ctx& c, const std::vector<GridInfo>& g) {
         sm[0][k][d] = std::max(sm[0][k][d], split_smem_bytes(PG_FP32, false, u.n, S, nl));
         sm[1][k][d] = std::max(sm[1][k][d], split_smem_bytes(PG_FP64, false, u.n, S, nl));
         sm[2][k][d] = std::max(sm[2][k][d], split_smem_bytes(PG_FP32, true, u.n, S, nl));
+        smseg[k][d] = std::max(smseg[k][d], seg_smem(d, u.n, S, nl));
+        seg32[k][d] = seg32[k][d] && u.n % kSplitSeg == 0;
       }
       tile_n[k][d] = (int)(tiles.size() - tile_at[k][d]);
     }
@@ -808,8 +815,11 @@ int build_split_ctx(Ctx& c, const std::vector<GridInfo>& g) {
         ss.smem32 = sm[0][k][d];
         ss.smem64 = sm[1][k][d];
         ss.smem_mixed = sm[2][k][d];
+        ss.seg32 = seg32[k][d];
+        ss.smem_seg_x = ss.smem_seg_yz = smseg[k][d];
         const bool exact = (p == PG_FP32) && k == OPK_D8 && c.ops[PG_FP32][k][d].exact;
-        const size_t need = (p == PG_FP64) ? ss.smem64 : (exact ? ss.smem_mixed : ss.smem32);
+        size_t need = (p == PG_FP64) ? ss.smem64 : (exact ? ss.smem_mixed : ss.smem32);
+        if (p == PG_FP32 && ss.seg32 && d != 0 && !exact) need = smseg[k][d];  // launch_split's choice
         ss.ok = need <= kSplitMaxSmem;
       }
   c.split_built = true;

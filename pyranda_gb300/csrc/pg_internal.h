@@ -123,9 +123,14 @@ struct SplitSet {
   int ntiles = 0;
   bool ok = false;
   size_t smem32 = 0, smem64 = 0, smem_mixed = 0;  // dynamic shared memory of the FP32 / FP64 / exact-d8 kernels
+  // every member's lines a multiple of kSplitSeg points: the FP32 sweeps take the
+  // register-resident form (seg_kernel), with this shared memory along x and along y / z
+  bool seg32 = false;
+  size_t smem_seg_x = 0, smem_seg_yz = 0;
 };
 // Shared memory of one split tile (precision PG_FP32 / PG_FP64; exact: FP32 d8 with the raw FP64 values).
 size_t split_smem_bytes(int precision, bool exact, int n, int S, int nl);
+size_t seg_smem(int dir, int n, int S, int nl);
 int launch_split(int precision, const OpRef& op, const SplitSet& ss, const double* in, double* out, int dir, int epi,
                  int scale_pow, const int* emax, void* stream);
 

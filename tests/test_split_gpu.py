@@ -100,9 +100,13 @@ def _smooth(shape, seed):
 
 
 @pytest.mark.parametrize("case", [((64, 48, 40), (True, False, True)), ((256, 16, 24), (True, True, True)),
-                                  ((40, 520, 3), (False, False, True))], ids=_ids)
+                                  ((40, 520, 3), (False, False, True)), ((64, 96, 32), (True, False, True)),
+                                  ((32, 64, 128), (False, False, False)), ((96, 32, 64), (False, True, True))],
+                         ids=_ids)
 def test_split_fp32_matches_oracle(oracle, case):
-    """FP32 arithmetic (exact fixed-point RHS for d8): the same error level as the FP32 one-thread-per-line sweeps."""
+    """FP32 arithmetic (exact fixed-point RHS for d8): the same error level as the FP32 one-thread-per-line sweeps.
+    Lines whose length is a multiple of 32 take the register-resident form (y and z straight from global
+    memory, x through a staged tile); the others the tile form."""
     from pyranda_gb300.grid import Grid
     shape, per = case
     g = _grid(shape, per, "fp32")

@@ -27,6 +27,9 @@ CASES = [
     ((40, 36, 10), (False, False, True), (("SYMM", "SYMM"), ("XTND", "SYMM"), ("NONE", "NONE"))),
     ((70, 9, 1), (False, False, False), (("XTND", "XTND"), ("SYMM", "XTND"), ("NONE", "NONE"))),
     ((8, 64, 3), (False, False, False), (("SYMM", "SYMM"), ("SYMM", "NONE"), ("NONE", "NONE"))),
+    # equal line lengths with different ends: each direction keeps its own solve tables
+    ((40, 12, 40), (False, False, False), (("SYMM", "NONE"), ("NONE", "NONE"), ("NONE", "SYMM"))),
+    ((64, 64, 64), (False, False, False), (("NONE", "NONE"), ("SYMM", "XTND"), ("SYMM", "SYMM"))),
 ]
 
 
@@ -92,6 +95,32 @@ def test_symm_fp32_and_dense_paths(oracle):
                 assert e <= 1e-5, (prec, d, sym, e)
                 e = rel_l2(to_host(g.filter("spectral", dv, d, sym=(sym,) * 3)), o.apply_sym(2, d, sym, v))
                 assert e <= 1e-6, (prec, "sf", d, sym, e)
+
+
+def test_symm_fp32_split_paths(oracle):
+    """SYMM / XTND ends on the FP32 split sweeps (lines of 64 and 96 points: the register-resident form,
+    edge rows straight from global memory along y and z), both variants, at FP32 accuracy."""
+    from pyranda_gb300.grid import Grid
+    shape, per = (64, 96, 64), (False, False, False)
+    bc = (("SYMM", "NONE"), ("XTND", "SYMM"), ("SYMM", "SYMM"))
+    o = oracle.OracleGrid(shape, per, X1, XN, bc=bc)
+    nx, ny, nz = shape
+    x = numpy.arange(nx)[:, None, None] / nx
+    y = numpy.arange(ny)[None, :, None] / ny
+    z = numpy.arange(nz)[None, None, :] / nz
+    v = numpy.asfortranarray(2.0 + numpy.cos(numpy.pi * x) * numpy.cos(numpy.pi * y) * numpy.cos(numpy.pi * z))
+    dv = to_dev(v, torch)
+    g = Grid(shape, per, X1, XN, bc=bc, precision="fp32", line_split=True)
+    bad = []
+    for d in range(3):
+        for sym in (1, -1):
+            e = rel_l2(to_host(g.d1(d, dv, sym=sym)), o.apply_sym(0, d, sym, v))
+            bad += [("d1", d, sym, e)] if not e <= 1e-5 else []
+            e = rel_l2(to_host(g.filter("spectral", dv, d, sym=(sym,) * 3)), o.apply_sym(2, d, sym, v))
+            bad += [("sf", d, sym, e)] if not e <= 1e-6 else []
+            e = rel_l2(to_host(g.d8(d, dv, sym=sym)), o.apply_sym(1, d, sym, v))
+            bad += [("d8", d, sym, e)] if not e <= 1e-5 else []
+    assert not bad, bad
 
 
 @pytest.mark.parametrize("shape,bc", [((40, 1, 32), (("SYMM", "NONE"), ("NONE", "NONE"), ("NONE", "NONE"))),
