@@ -819,7 +819,7 @@ int build_split_ctx(Ctx& c, const std::vector<GridInfo>& g) {
         ss.smem_seg_x = ss.smem_seg_yz = smseg[k][d];
         const bool exact = (p == PG_FP32) && k == OPK_D8 && c.ops[PG_FP32][k][d].exact;
         size_t need = (p == PG_FP64) ? ss.smem64 : (exact ? ss.smem_mixed : ss.smem32);
-        if (p == PG_FP32 && ss.seg32 && d != 0 && !exact) need = smseg[k][d];  // launch_split's choice
+        if (p == PG_FP32 && ss.seg32) need = smseg[k][d];  // launch_split's choice
         ss.ok = need <= kSplitMaxSmem;
       }
   c.split_built = true;

@@ -425,18 +425,21 @@ struct GLine {
   __device__ __forceinline__ TR w(int q) const { return v(q < 0 ? q + n : (q >= n ? q - n : q)); }
 };
 
-__host__ __device__ inline size_t seg_tips_bytes(int S, int nl) { return al16((size_t)nl * (4 * S + 1) * 4); }
+// Tips of line l, segment j at tips[l * (4S + 4) + 4j]: 16-byte rows whose stride keeps the
+// lanes of a quarter warp (neighbouring lines) on distinct banks.
+__host__ __device__ inline size_t seg_tips_bytes(int S, int nl) { return al16((size_t)nl * (4 * S + 4) * 4); }
 
 template <int KIND, bool PER, bool IMPL, bool ADDBACK, int DIR, int EPI, bool EXACT>
-__global__ void __launch_bounds__(kSplitThreads, 2) seg_kernel(const SParams P) {
+__global__ void __launch_bounds__(kSplitThreads, 3) seg_kernel(const SParams P) {
   constexpr int H = (KIND == 4) ? 4 : 3;
   constexpr int L = kSplitSeg;
+  constexpr bool kStage = (DIR == 0);  // x through a staged tile (direct per-thread runs of a line thrash L1)
   extern __shared__ __align__(16) unsigned char s_buf[];
   const SplitTile tile = P.tiles[blockIdx.x];
   const MemberOp& op = P.ops[tile.op];
   const SplitOp so = P.sops[tile.op];
   const int n = op.n, S = so.S, nl = tile.nlines;
-  const int tid = threadIdx.x, tld = 4 * S + 1;
+  const int tid = threadIdx.x, tld = 4 * S + 4;
   const int nx = op.nx, ny = op.ny;
   const long long st = (DIR == 0) ? 1 : (DIR == 1 ? (long long)nx : (long long)nx * ny);
   const int ld = row_stride(n);
@@ -453,7 +456,7 @@ __global__ void __launch_bounds__(kSplitThreads, 2) seg_kernel(const SParams P) 
   };
   const int NE = n * nl;
   const int qs = kSplitThreads / n, qr = kSplitThreads % n;  // x: element tid of the tile is (tid / n, tid % n)
-  if (DIR == 0) {  // stage the tile: a warp reads a contiguous run of one line
+  if (kStage) {  // stage the tile: a warp reads a contiguous run of one line
     for (int li = tid; li < nl; li += blockDim.x) sbase[li] = line_base(li);
     __syncthreads();
     int es = tid / n, ef = tid % n;
@@ -482,7 +485,7 @@ __global__ void __launch_bounds__(kSplitThreads, 2) seg_kernel(const SParams P) 
   const int l = tid % nl, j = tid / nl;
   const bool active = j < S;
   const int p0 = j * L;
-  const long long gb = (DIR == 0) ? 0 : line_base(l);
+  const long long gb = kStage ? 0 : line_base(l);
   const double* gl = P.in + gb;
   const double* vl = sv + l * ld;
   // the raw value at position p0 + k of the thread's line, k in [-H, L + H): rows outside the
@@ -493,7 +496,7 @@ __global__ void __launch_bounds__(kSplitThreads, 2) seg_kernel(const SParams P) 
       if (PER) p = p < 0 ? p + n : (p >= n ? p - n : p);
       else p = min(max(p, 0), n - 1);
     }
-    return DIR == 0 ? vl[p] : __ldg(gl + p * st);
+    return kStage ? vl[p] : __ldg(gl + p * st);
   };
   const int E = EXACT ? __ldg(P.emax + tile.op) : 0;
   const float wsc = EXACT ? op.wscale : 1.0f;
@@ -510,7 +513,7 @@ __global__ void __launch_bounds__(kSplitThreads, 2) seg_kernel(const SParams P) 
         const int i = q < 4 ? q : n - 8 + q;
         if (q < 4 ? !elo : !ehi) continue;
         if (EXACT) {
-          if (DIR == 0)
+          if (kStage)
             re[q] = fixed_to_float(edge_rhs<long long, KIND, false, int>(SLine<long long>{vl, n, E}, i, op.rhs_i,
                                                                          op.bcl, op.bch), E, wsc);
           else
@@ -518,7 +521,7 @@ __global__ void __launch_bounds__(kSplitThreads, 2) seg_kernel(const SParams P) 
                                                                          op.bcl, op.bch), E, wsc);
         } else {
           const float* R = reinterpret_cast<const float*>(op.rhs);  // the FP32 operator's weights
-          if (DIR == 0)
+          if (kStage)
             re[q] = (float)edge_rhs<double, KIND, false, float>(SLine<double>{vl, n, 0}, i, R, op.bcl, op.bch);
           else
             re[q] = (float)edge_rhs<double, KIND, false, float>(GLine<double>{gl, st, n, 0}, i, R, op.bcl, op.bch);
@@ -575,11 +578,7 @@ __global__ void __launch_bounds__(kSplitThreads, 2) seg_kernel(const SParams P) 
         y2 = y1;
         y1 = y;
       }
-      float* tp = tips + l * tld + 4 * j;
-      tp[0] = z[0];
-      tp[1] = z[1];
-      tp[2] = z[L - 2];
-      tp[3] = z[L - 1];
+      *reinterpret_cast<float4*>(tips + l * tld + 4 * j) = make_float4(z[0], z[1], z[L - 2], z[L - 1]);
     }
   }
   __syncthreads();  // the tips are published, and every read of this tile's input is done
@@ -590,18 +589,21 @@ __global__ void __launch_bounds__(kSplitThreads, 2) seg_kernel(const SParams P) 
     const float* tl = tips + l * tld;
     float q0 = 0.0f, q1 = 0.0f, q2 = 0.0f, q3 = 0.0f;
     const int T4 = 4 * S;
+    auto dot4 = [](float q, const float4 g, const float4 t) {  // the order of split_kernel's sums
+      q += g.x * t.x;
+      q += g.y * t.y;
+      q += g.z * t.z;
+      q += g.w * t.w;
+      return q;
+    };
     for (int k = 0; k < gc; k++) {
       int js = g0 + k;
       js = js >= S ? js - S : js;
-#pragma unroll
-      for (int c = 0; c < 4; c++) {
-        const int idx = 4 * js + c;
-        const float t = tl[idx];
-        q0 += ldc(Gj + idx) * t;
-        q1 += ldc(Gj + T4 + idx) * t;
-        q2 += ldc(Gj + 2 * T4 + idx) * t;
-        q3 += ldc(Gj + 3 * T4 + idx) * t;
-      }
+      const float4 t = *reinterpret_cast<const float4*>(tl + 4 * js);
+      q0 = dot4(q0, __ldg(reinterpret_cast<const float4*>(Gj + 4 * js)), t);
+      q1 = dot4(q1, __ldg(reinterpret_cast<const float4*>(Gj + T4 + 4 * js)), t);
+      q2 = dot4(q2, __ldg(reinterpret_cast<const float4*>(Gj + 2 * T4 + 4 * js)), t);
+      q3 = dot4(q3, __ldg(reinterpret_cast<const float4*>(Gj + 3 * T4 + 4 * js)), t);
     }
     const float* __restrict__ C = reinterpret_cast<const float*>(so.row) + (size_t)p0 * 12;
 #pragma unroll
@@ -618,7 +620,7 @@ __global__ void __launch_bounds__(kSplitThreads, 2) seg_kernel(const SParams P) 
 
   constexpr bool kReadOut = (EPI == EPI_ADD || EPI == EPI_RING_MAX);
   const double sc = (P.scale_pow == 2) ? op.dm * op.dm : (P.scale_pow == 1 ? op.dm : 1.0);
-  if (DIR != 0) {  // straight to global memory, 8 rows at a time (their epilogue inputs read first)
+  if (!kStage) {  // straight to global memory, 8 rows at a time (their epilogue inputs read first)
     if (active) {
       double* go = P.out + gb;
       const double* gi = P.in + gb;
@@ -818,9 +820,8 @@ int launch_split(int precision, const OpRef& op, const SplitSet& ss, const doubl
                  int scale_pow, const int* emax, void* stream) {
   if (!ss.ok || ss.ntiles == 0) return PG_OK;
   SParams P{in, out, op.dev, ss.sops, ss.tiles, scale_pow, emax};
-  // the register-resident form along y and z (where it reads global memory directly); along x and
-  // for the exact d8 the tile form is as fast or faster
-  if (precision == PG_FP32 && ss.seg32 && dir != 0 && !(op.kind == OPK_D8 && op.exact))
+  // the register-resident form wherever every segment is 32 rows long
+  if (precision == PG_FP32 && ss.seg32)
     return seg_kind(op, P, ss, dir, epi, stream);
   if (precision == PG_FP32) return split_kind<float>(op, P, ss, dir, epi, stream);
   return split_kind<double>(op, P, ss, dir, epi, stream);
