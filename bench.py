@@ -965,6 +965,11 @@ def main():
         roof_extra = {"tensor_tflops": round(3 * 2 * n * npts / dur / 1e12, 1),
                       "tensor_peak_note": "TF32 dense nominal ~1100 TFLOP/s (no measured TF32 peak in "
                                           "MEASURED_PEAKS.json)"}
+    elif form == "split" and n % 32 == 0:
+        kname = ("seg_kernel<%s, dir=%d> (FP32 split-line banded solve: 32-row segments unrolled in registers, "
+                 "joined by the reduced system; %s)" % (dom_op, dirn, "tile staged through shared memory" if dirn == 0
+                                                        else "lines read and written straight from global memory"))
+        roof_extra = {}
     elif form == "split":
         kname = ("split_kernel<float, %s, dir=%d> (split-line banded solve: 32-point segments joined by the "
                  "reduced system, tile of lines in shared memory)" % (dom_op, dirn))
@@ -1030,7 +1035,9 @@ def main():
             "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": k, "warmup": w,
             "ms_per_step": round(t_fast / k * 1e3, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": ("tf32x3 (f32 accumulate) / f32 sweeps, f64 state"
-                                           if best_prec != "fp32" else "f32 sweeps / f64 state"),
+                                           if best_prec == "dense" or (best_prec == "auto" and "dense" in
+                                                                        fast.grid.sweep_plan().values())
+                                           else "f32 sweeps (RHS differences from f32 hi + lo pairs), f64 state"),
             "data": "synthetic (Taylor-Green initial condition, Mach 0.1)",
             "config": {"workload": "compressible Taylor-Green vortex %d^3 periodic, Mach 0.1, Re 1600, LAD + compact filters, "
                                    "LSRK(5,4), CFL 0.5" % n,

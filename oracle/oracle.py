@@ -329,14 +329,138 @@ class _Timestep:
 
 
 class _BC:
-    """pyrandaBC.py:58-160 (extrap / const on one rank)"""
+    """pyrandaBC.py on one rank: extrap / const (:58-160), field (:162-187),
+    slip (:190-465), exit (:468-521), farfield (:524-745), symm (:748-788).
+    A boundary is owned when its direction is non-periodic and has more than
+    one point.  slip and farfield use the normal of a Cartesian mesh: the
+    cross product of the metric rows (:233-264) with d(x,y,z)/d(A,B,C) =
+    diag(dx, dy, dz), i.e. +x on the x ends, -y on the y ends, +z on the z
+    ends."""
 
     name = "BC"
+    NORMAL = {"x": (1.0, 0.0, 0.0), "y": (0.0, -1.0, 0.0), "z": (0.0, 0.0, 1.0)}
 
     def __init__(self, sim):
         self.sim = sim
+        self.BCdata = {}
         self.sMap = {"bc.extrap(": "self.packages['BC'].extrap(",
-                     "bc.const(": "self.packages['BC'].const("}
+                     "bc.const(": "self.packages['BC'].const(",
+                     "bc.exit(": "self.packages['BC'].exitbc(",
+                     "bc.slip(": "self.packages['BC'].slipbc(",
+                     "bc.field(": "self.packages['BC'].applyBC('field',",
+                     "bc.farfield(": "self.packages['BC'].farfieldbc(",
+                     "bc.symm(": "self.packages['BC'].symm("}
+
+    def _owns(self, d):
+        ax = "xyz".index(d[0])
+        return self.sim.shape[ax] > 1 and not self.sim.options["periodic"][ax]
+
+    def applyBC(self, func, var, direction, val=None):
+        f = getattr(self, func)
+        for d in (direction if isinstance(direction, list) else [direction]):
+            for v in (var if isinstance(var, list) else [var]):
+                if val is not None:
+                    f(v, d, val)
+                else:
+                    f(v, d)
+
+    def field(self, var, d, field):
+        if d[0] == "z" or not self._owns(d):
+            return
+        k = 0 if d[1] == "1" else -1
+        self.sim.variables[var].data[self._slice(d, k)] = field[self._slice(d, k)]
+
+    @staticmethod
+    def BENO(u1, u2, u3, norm):
+        d1 = u2 - u1
+        d2 = (2.0 * u2 - u3) - u1
+        beno = numpy.where(numpy.abs(d1) <= numpy.abs(d2), u1 + d1, u1 + d2)
+        beno = numpy.where(d1 * d2 <= 0.0, u1, beno)
+        if norm:
+            beno = numpy.maximum(numpy.minimum(beno, numpy.maximum(0.0, u2)), numpy.minimum(0.0, u2))
+        return beno
+
+    def exitbc(self, var, direction, norm=False):
+        for d in (direction if isinstance(direction, list) else [direction]):
+            for v in (var if isinstance(var, list) else [var]):
+                if d[0] == "z" or not self._owns(d):
+                    continue
+                a = self.sim.variables[v].data
+                k = (0, 1, 2) if d[1] == "1" else (-1, -2, -3)
+                a[self._slice(d, k[0])] = self.BENO(a[self._slice(d, k[0])], a[self._slice(d, k[1])],
+                                                    a[self._slice(d, k[2])], norm)
+
+    def symm(self, var, direction, anti=False, npts=4):
+        m = -1.0 if anti else 1.0
+        for d in (direction if isinstance(direction, list) else [direction]):
+            for v in (var if isinstance(var, list) else [var]):
+                if not self._owns(d):
+                    continue
+                a = self.sim.variables[v].data
+                ax = "xyz".index(d[0])
+                n = a.shape[ax]
+                dst, src = (0, npts) if d[1] == "1" else (n - npts, n - 2 * npts)
+                a[self._slice(d, slice(dst, dst + npts))] = numpy.flip(
+                    a[self._slice(d, slice(src, src + npts))], axis=ax) * m
+
+    def slipbc(self, var, direction):
+        velocity = var if isinstance(var, list) else [var]
+        for d in (direction if isinstance(direction, list) else [direction]):
+            if d[0] == "z":
+                continue
+            self.extrap(velocity, d, 2)
+            if not self._owns(d):
+                continue
+            k = 0 if d[1] == "1" else -1
+            nrm = self.NORMAL[d[0]]
+            planes = [self.sim.variables[v].data[self._slice(d, k)].copy() for v in velocity]
+            udotn = 0.0
+            for q, u in enumerate(planes):
+                udotn = udotn + u * nrm[q]
+            mag0 = 0.0
+            for u in planes:
+                mag0 += u ** 2
+            mag0 = numpy.sqrt(mag0)
+            new = [u - udotn * nrm[q] for q, u in enumerate(planes)]
+            magf = 0.0
+            for u in new:
+                magf += u ** 2
+            magf = numpy.sqrt(magf)
+            for v, u in zip(velocity, new):
+                self.sim.variables[v].data[self._slice(d, k)] = numpy.where(magf > mag0, u * mag0 / magf, u)
+
+    def Reimann(self, d, Rhoref, Uref, Vref, Wref, Pref, gamma, rhoi, Ui, Vi, Wi, Pi):
+        nx, ny, nz = self.NORMAL[d[0]]
+        Vni = Ui * nx + Vi * ny + Wi * nz
+        Vno = Uref * nx + Vref * ny + Wref * nz
+        SSo = numpy.sqrt(gamma * Pref / Rhoref)
+        SSi = numpy.sqrt(gamma * Pi / rhoi)
+        tmp = numpy.sqrt(Ui ** 2 + Vi ** 2 + Wi ** 2) / SSi
+        Rplus = numpy.where(tmp >= 1.0, Vno + 2.0 * SSo / (gamma - 1.0), Vni + 2.0 * SSi / (gamma - 1.0))
+        Rminus = numpy.where(tmp >= 1.0, Vni - 2.0 * SSi / (gamma - 1.0), Vno - 2.0 * SSo / (gamma - 1.0))
+        Vnormal = (Rminus + Rplus) * 0.5
+        SSb = (Rplus - Rminus) * (gamma - 1.0) * 0.25
+        Ub = numpy.where(Vnormal >= 0.0, Ui + (Vnormal - Vni) * nx, Uref + (Vnormal - Vno) * nx)
+        Vb = numpy.where(Vnormal >= 0.0, Vi + (Vnormal - Vni) * ny, Vref + (Vnormal - Vno) * ny)
+        Wb = numpy.where(Vnormal >= 0.0, Wi + (Vnormal - Vni) * nz, Wref + (Vnormal - Vno) * nz)
+        aux = 1.0 / (gamma - 1.0)
+        rhob = numpy.where(Vnormal >= 0.0, ((rhoi ** gamma * SSb ** 2) / (gamma * Pi)) ** aux,
+                           ((Rhoref ** gamma * SSb ** 2) / (gamma * Pref)) ** aux)
+        Pb = rhob * SSb ** 2 / gamma
+        Etb = Pb / (gamma - 1.0) + 0.5 * rhob * (Ub * Ub + Vb * Vb + Wb * Wb)
+        return rhob, Ub, Vb, Wb, Etb, Pb
+
+    def farfieldbc(self, direction):
+        for d in (direction if isinstance(direction, list) else [direction]):
+            ref = self.BCdata["farfield-properties-%s" % d]
+            if not self._owns(d):
+                continue
+            names = [ref[k] for k in ("rho", "u", "v", "w", "p")]
+            b, i = (0, 1) if d[1] == "1" else (-1, -2)
+            inner = [self.sim.variables[v].data[self._slice(d, i)].copy() for v in names]
+            out = self.Reimann(d, ref["rho0"], ref["u0"], ref["v0"], ref["w0"], ref["p0"], ref["gamma"], *inner)
+            for v, val in zip(names, (out[0], out[1], out[2], out[3], out[5])):
+                self.sim.variables[v].data[self._slice(d, b)] = val
 
     @staticmethod
     def _slice(direction, k):
