@@ -279,7 +279,7 @@ int pg_ens_device_status(pg_ensemble* e, int* status);
 #define PG_LAD_NWEIGHT (3 * 64 * 64 + 2 * 64)
 #define PG_LAD_NPARAM (PG_LAD_NWEIGHT + 3 * 64 + 2)
 typedef struct pg_lad_model {
-  const void* wbf16;     /* PG_LAD_NWEIGHT BF16 weights (device) */
+  const void* wbf16;     /* PG_LAD_NWEIGHT BF16 weights (device, 16-byte aligned) */
   const float* params;   /* PG_LAD_NPARAM FP32 parameters (device; biases read here) */
   const float* xmean;    /* PG_LAD_K input means (device) */
   const float* xinvstd;  /* PG_LAD_K input 1/std (device) */

@@ -1667,7 +1667,11 @@ int pg_lad_closure(pg_handle* h, const pg_lad_model* m, const double* div, const
   if (!h || !m || !m->wbf16 || !m->params || !m->xmean || !m->xinvstd || !div || !gmag || !rho || !dt || !beta ||
       !kappa || !flag)
     return PG_EINVAL;
-  LadInferArgs a{*m, lad_grid(h->g), div, gmag, rho, dt, cv, beta, kappa, flag};
+  if (((uintptr_t)m->wbf16 & 15u) != 0) {  // the kernel stages the weights in 16-byte chunks
+    set_error("pg_lad_closure: the BF16 weights must be 16-byte aligned");
+    return PG_EINVAL;
+  }
+  LadInferArgs a{*m, lad_grid(h->g), div, gmag, rho, dt, cv, beta, kappa, flag, h->c.status};
   return launch_lad_infer(a, stream);
 }
 

@@ -32,6 +32,7 @@
 
 #include "pg_internal.h"
 #include "pg_sweep.cuh"
+#include "pg_tc.cuh"
 
 namespace pg {
 namespace {
@@ -42,74 +43,6 @@ constexpr int kStageBytes = 98304;    // V hi/lo + D hi/lo of one chunk
 constexpr int kStages = 2;
 constexpr int kSmemBytes = kStages * kStageBytes + 1024;  // + alignment slack
 constexpr int kTmemCols = 256;
-constexpr unsigned long long kWaitNs = 2000000000ull;     // 2 s bound on any wait
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ unsigned long long globaltimer() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-               : "memory");
-}
-
-// Bounded wait for the phase with the given parity; false on time-out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsigned long long limit_ns = kWaitNs) {
-  const uint32_t a = smem_u32(bar);
-  unsigned long long t0 = 0;
-  for (unsigned it = 0;; it++) {
-    unsigned done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.b32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(a), "r"(parity)
-        : "memory");
-    if (done) return true;
-    if ((it & 1023u) == 0) {
-      const unsigned long long t = globaltimer();
-      if (it == 0) t0 = t;
-      else if (t - t0 > limit_ns) return false;
-    }
-  }
-}
-
-__device__ __forceinline__ void bulk_copy(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
-
-__device__ __forceinline__ void fence_proxy_async() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-__device__ __forceinline__ void tc_fence_before() {
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void tc_fence_after() {
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-
-// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
-// 1024 bytes apart (start and offsets in 16-byte units).
-__device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
-  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
-         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
-}
 
 // Instruction descriptor of kind::tf32: FP32 accumulator, TF32 A and B, both
 // K-major, M = 128, N = n (multiple of 16, <= 256).
@@ -124,23 +57,6 @@ __device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, 
       "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
       "l"(a), "l"(b), "r"(idesc), "r"(acc)
       : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                   smem_u32(bar))
-               : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* r) {
-  uint32_t u[8];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-      : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 8; i++) r[i] = __uint_as_float(u[i]);
 }
 
 // TF32 of an FP32 value: round the low 13 mantissa bits to nearest (ties away).
@@ -183,11 +99,6 @@ __device__ __forceinline__ void difference_item(const Item& it, bool ok, int kb,
     h[j] = tf32_bits(f);
     l[j] = tf32_bits(f - __uint_as_float(h[j]));
   }
-}
-
-// byte offset of 16-byte chunk q of row r in a K-major 128B-swizzled tile
-__device__ __forceinline__ uint32_t swz(int r, int q) {
-  return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((q ^ (r & 7)) << 4));
 }
 
 __device__ __forceinline__ int64_t line_base(const DenseOp& op, int dir, int64_t l) {

@@ -238,6 +238,7 @@ struct LadInferArgs {
   double cv;
   double *beta, *kappa;
   int* flag;
+  int* status;  // device status word (PG_ETIMEOUT when a tensor-core wait runs out)
 };
 struct LadTrainArgs {
   pg_lad_model model;

@@ -17,11 +17,11 @@
 //   y1 = kappa dt / (rho cv D^2)    (dimensionless)
 // so that   beta = max(0, y0 s0 + m0) rho D,   kappa = max(0, y1 s1 + m1) rho cv D^2 / dt.
 //
-// Inference (lad_infer_kernel) fuses the feature gather with the network on
-// the tensor cores (mma.sync m16n8k16 BF16 -> FP32; each layer's accumulator
-// fragments are repacked in registers as the next layer's A operand) and
-// raises a device flag when any raw output leaves [ylo, yhi] (the training
-// range with a margin): the plain LAD closure is then the fallback.
+// Inference (lad_infer_tc_kernel) fuses the feature gather with the network on
+// the 5th-generation tensor cores (tcgen05.mma kind::f16, BF16 operands in
+// shared memory, FP32 accumulators in tensor memory) and raises a device flag
+// when any raw output leaves [ylo, yhi] (the training range with a margin):
+// the plain LAD closure is then the fallback.
 // Training runs the same arithmetic on CUDA cores in lad_train_kernel
 // (forward with BF16 rounding at the same points, MSE loss, backward, FP32
 // gradient accumulation) and an Adam step in lad_adam_kernel.
@@ -32,6 +32,7 @@
 
 #include "pg_internal.h"
 #include "pg_sweep.cuh"  // d2f_bits: FP64 -> FP32 without the FP64 pipe
+#include "pg_tc.cuh"     // tcgen05 helpers
 
 namespace pg {
 namespace {
@@ -40,7 +41,6 @@ constexpr int kIn = PG_LAD_IN;        // 55 features
 constexpr int kK = PG_LAD_K;          // 64 padded inputs
 constexpr int kH = PG_LAD_HIDDEN;     // 64
 constexpr int kOut = PG_LAD_OUT;      // 2
-constexpr int kInferThreads = 256;    // 8 warps x 16 points = one 128-point row tile
 constexpr int kTrainRows = 64;        // rows of a training CTA
 constexpr int kTrainThreads = 256;
 
@@ -84,42 +84,6 @@ struct alignas(16) ColInfo {
   int pad;
 };
 
-// Shared-memory image of the network for inference: weights as BF16 rows
-// [N][K + 8] (the pad staggers banks), biases and normalisation in FP32.
-struct InferSmem {
-  __nv_bfloat16 w1[kH][kK + 8];
-  __nv_bfloat16 w2[kH][kH + 8];
-  __nv_bfloat16 w3[kH][kH + 8];
-  __nv_bfloat16 w4[8][kH + 8];   // rows >= kOut are zero
-  float b1[kH], b2[kH], b3[kH], b4[8];
-  ColInfo col[kK];
-};
-
-// one hidden layer: A fragments (4 k-tiles) -> ReLU(W A + b) as next A fragments
-template <int KT>
-__device__ __forceinline__ void layer_relu(const uint32_t (*a)[4], uint32_t (*anext)[4],
-                                           const __nv_bfloat16 (*w)[kH + 8], const float* b, int g, int t) {
-  float c[8][4];
-#pragma unroll
-  for (int nt = 0; nt < 8; nt++) {
-    const float b0 = b[nt * 8 + 2 * t], b1 = b[nt * 8 + 2 * t + 1];
-    c[nt][0] = b0; c[nt][1] = b1; c[nt][2] = b0; c[nt][3] = b1;
-#pragma unroll
-    for (int kt = 0; kt < KT; kt++) {
-      const uint32_t w0 = *reinterpret_cast<const uint32_t*>(&w[nt * 8 + g][kt * 16 + 2 * t]);
-      const uint32_t w1 = *reinterpret_cast<const uint32_t*>(&w[nt * 8 + g][kt * 16 + 2 * t + 8]);
-      mma_bf16(c[nt], a[kt], w0, w1);
-    }
-  }
-#pragma unroll
-  for (int kt = 0; kt < 4; kt++) {
-    anext[kt][0] = pack_bf16(fmaxf(c[2 * kt][0], 0.f), fmaxf(c[2 * kt][1], 0.f));
-    anext[kt][1] = pack_bf16(fmaxf(c[2 * kt][2], 0.f), fmaxf(c[2 * kt][3], 0.f));
-    anext[kt][2] = pack_bf16(fmaxf(c[2 * kt + 1][0], 0.f), fmaxf(c[2 * kt + 1][1], 0.f));
-    anext[kt][3] = pack_bf16(fmaxf(c[2 * kt + 1][2], 0.f), fmaxf(c[2 * kt + 1][3], 0.f));
-  }
-}
-
 // parameter offsets (PG_LAD_NPARAM layout)
 constexpr int kW1 = 0, kW2 = kH * kK, kW3 = kW2 + kH * kH, kW4 = kW3 + kH * kH, kB1 = kW4 + kOut * kH,
               kB2 = kB1 + kH, kB3 = kB2 + kH, kB4 = kB3 + kH;
@@ -130,37 +94,85 @@ static_assert(kB1 == PG_LAD_NWEIGHT && kB4 + kOut == PG_LAD_NPARAM, "parameter l
 // |grad rho|*D are staged once in shared memory (rows 0..17), after a row of
 // D (18) and a row of zeros (19) for the constant and padding columns; every
 // warp then builds the features of its 16 points from there and runs the
-// network.
+// network.  (The tile and neighbourhood layout of the inference kernel.)
 constexpr int kTileX = 128;
 constexpr int kHaloX = kTileX + 2;
 constexpr int kNbRows = 2 * 9 + 2;
 
-__global__ void __launch_bounds__(kInferThreads) lad_infer_kernel(const LadInferArgs A) {
-  extern __shared__ __align__(16) unsigned char lad_smem[];
-  InferSmem& S = *reinterpret_cast<InferSmem*>(lad_smem);
-  float* nbf = reinterpret_cast<float*>(lad_smem + sizeof(InferSmem));
+// ----------------------------------------------------------- inference, tcgen05
+// The same tile and features, with the network on the 5th-generation tensor
+// cores.  One CTA of 128 threads owns a 128-point row tile (M = 128, one
+// thread per point) and loops over tiles (persistent grid, one wave).  Per
+// tile: each thread writes its 64 normalised BF16 features as row r of the A
+// tile in shared memory (K-major, 128-byte swizzle); one thread issues the
+// four K = 16 steps of tcgen05.mma kind::f16 (BF16 x BF16 -> FP32 in tensor
+// memory, N = 64) against W1 and commits them to an mbarrier; every thread
+// then reads its row of the accumulator (tcgen05.ld), adds the bias, applies
+// ReLU and writes the row back, packed to BF16, as the next layer's A tile;
+// the same for W2 and W3.  The 64 -> 2 output layer runs as one more MMA with
+// W4 padded to N = 16 rows (the bias added after).  The weights are staged
+// once per CTA in the same swizzled layout (the B operands: N rows of K = 64).
+// Every wait is bounded: on a time-out the CTA records PG_ETIMEOUT in the
+// status word, waits (bounded) for its own MMAs and still frees its tensor
+// memory.
+constexpr int kTcThreads = 128;
+constexpr int kTcTmemCols = 64;
+constexpr int kTcMaxResident = 8;  // 8 x 64 TMEM columns = the SM's 512
+constexpr int kTcOutRows = 16;     // the output layer's N (kOut rows + zero rows)
+
+struct TcSmem {                    // placed at a 1024-byte boundary
+  uint8_t a[128 * 128];            // A: 128 rows x 64 BF16
+  uint8_t w[3][kH * 128];          // B of the hidden layers: 64 rows (outputs) x 64 BF16 (inputs)
+  uint8_t w4[kTcOutRows * 128];    // B of the output layer: rows >= kOut are zero
+  float nb[kNbRows * kHaloX];      // the neighbourhood of the tile (as lad_infer_kernel)
+  float b[3][kH];
+  float b4[kOut];
+  ColInfo col[kK];
+  uint64_t bar;
+  uint32_t tmem_slot;
+};
+
+__global__ void __launch_bounds__(kTcThreads, 4) lad_infer_tc_kernel(const LadInferArgs A) {
+  extern __shared__ __align__(16) unsigned char lad_tc_raw[];
+  const uint32_t raw = smem_u32(lad_tc_raw);
+  TcSmem& S = *reinterpret_cast<TcSmem*>(lad_tc_raw + (((raw + 1023u) & ~1023u) - raw));
   const pg_lad_model& M = A.model;
   const __nv_bfloat16* W = reinterpret_cast<const __nv_bfloat16*>(M.wbf16);
   const float* P = M.params;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int g = lane >> 2, t = lane & 3;
-  for (int i = tid; i < kH * kK; i += blockDim.x) S.w1[i / kK][i % kK] = W[kW1 + i];
-  for (int i = tid; i < kH * kH; i += blockDim.x) {
-    S.w2[i / kH][i % kH] = W[kW2 + i];
-    S.w3[i / kH][i % kH] = W[kW3 + i];
-  }
-  for (int i = tid; i < 8 * kH; i += blockDim.x)
-    S.w4[i / kH][i % kH] = (i / kH < kOut) ? W[kW4 + i] : __float2bfloat16(0.0f);
-  for (int i = tid; i < kH; i += blockDim.x) {
-    S.b1[i] = P[kB1 + i];
-    S.b2[i] = P[kB2 + i];
-    S.b3[i] = P[kB3 + i];
-  }
-  if (tid < 8) S.b4[tid] = tid < kOut ? P[kB4 + tid] : 0.0f;
+  const int tid = threadIdx.x, warp = tid >> 5;
   const LadGrid& G = A.grid;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&S.tmem_slot)),
+                 "r"(kTcTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    mbar_init(&S.bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // weights: row n of a layer, 16-byte chunk q = inputs 8q .. 8q + 7 (BF16, already rounded)
+  for (int i = tid; i < 3 * kH * 8; i += blockDim.x) {
+    const int l = i / (kH * 8), n = (i / 8) % kH, q = i % 8;
+    const int base = (l == 0 ? kW1 : (l == 1 ? kW2 : kW3)) + n * kK + 8 * q;
+    *reinterpret_cast<uint4*>(S.w[l] + swz(n, q)) = *reinterpret_cast<const uint4*>(W + base);
+  }
+  for (int i = tid; i < kTcOutRows * 8; i += blockDim.x) {
+    const int n = i / 8, q = i % 8;
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    if (n < kOut) v = *reinterpret_cast<const uint4*>(W + kW4 + n * kH + 8 * q);
+    *reinterpret_cast<uint4*>(S.w4 + swz(n, q)) = v;
+  }
+  for (int i = tid; i < kH; i += blockDim.x) {
+    S.b[0][i] = P[kB1 + i];
+    S.b[1][i] = P[kB2 + i];
+    S.b[2][i] = P[kB3 + i];
+  }
+  if (tid < kOut) S.b4[tid] = P[kB4 + tid];
   for (int c = tid; c < kK; c += blockDim.x) {
     ColInfo ci;
-    if (c < 2 * 27) {   // feature f at stencil point s2 = (di+1) + 3 (dj+1) + 9 (dk+1): row (f, dj, dk), x offset di
+    if (c < 2 * 27) {
       const int f = c / 27, s2 = c - f * 27;
       ci.off = (f * 9 + s2 / 3) * kHaloX + s2 % 3;
     } else {
@@ -172,81 +184,138 @@ __global__ void __launch_bounds__(kInferThreads) lad_infer_kernel(const LadInfer
     S.col[c] = ci;
   }
   for (int xx = tid; xx < kHaloX; xx += blockDim.x) {
-    nbf[18 * kHaloX + xx] = (float)G.delta;
-    nbf[19 * kHaloX + xx] = 0.0f;
+    S.nb[18 * kHaloX + xx] = (float)G.delta;
+    S.nb[19 * kHaloX + xx] = 0.0f;
   }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = S.tmem_slot;
+  const uint32_t a_addr = smem_u32(S.a);
+  const uint32_t tlane = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's 32 lanes (= rows)
+
   const int nx = G.n[0], ny = G.n[1], nz = G.n[2];
   const int nxb = (nx + kTileX - 1) / kTileX;
   const long long ntiles = (long long)nxb * ny * nz;
   const float dl = (float)G.delta;
-  // beta = max(0, y0 s0 + m0) rho D,  kappa = max(0, y1 s1 + m1) rho cv D^2 / dt: the factors of the
-  // launch once in FP64, the per-point arithmetic in FP32 (GB300's FP64 pipe is 1/58 of FP32)
   const float fb = d2f_bits(G.delta), fk = d2f_bits(A.cv * G.delta * G.delta / A.dt[0]);
-  bool out_of_range = false;
-  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  bool out_of_range = false, bad = false;
+  uint32_t phase = 0;
+  const int r = tid;  // this thread's row: point x0 + r of the tile; also halo column r of the staging
+  // the 36 halo elements beyond column 127 (columns 128 and 129 of the 18 rows): threads 0..35
+  const int xr = (tid < 36) ? (tid >> 1) : -1, xc = kTileX + (tid & 1);
+
+  // one layer: the A tile against B (n rows) into the accumulator; false on a time-out
+  auto layer = [&](const uint8_t* B, int n) -> bool {
+    fence_proxy_async();  // this thread's A row is visible to the tensor core
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+      const uint32_t b_addr = smem_u32(B), idesc = idesc_bf16(n);
+#pragma unroll
+      for (int kk = 0; kk < kK / 16; kk++)
+        tc_mma_bf16(tmem, sdesc(a_addr + kk * 32), sdesc(b_addr + kk * 32), idesc, kk > 0 ? 1 : 0);
+      mma_commit(&S.bar);
+    }
+    const bool ok = mbar_wait(&S.bar, phase & 1);
+    phase++;
+    tc_fence_after();
+    return ok;
+  };
+  // this thread's accumulator row + bias, ReLU, packed to BF16 as row r of the next A tile
+  auto hidden = [&](int l) {
+#pragma unroll
+    for (int c0 = 0; c0 < kH; c0 += 32) {
+      uint32_t u[32];
+      tmem_ld16(tlane + (uint32_t)c0, u);
+      tmem_ld16(tlane + (uint32_t)(c0 + 16), u + 16);
+      tmem_wait_ld();
+      uint32_t pk[16];
+#pragma unroll
+      for (int i = 0; i < 16; i++)
+        pk[i] = pack_bf16(fmaxf(__uint_as_float(u[2 * i]) + S.b[l][c0 + 2 * i], 0.0f),
+                          fmaxf(__uint_as_float(u[2 * i + 1]) + S.b[l][c0 + 2 * i + 1], 0.0f));
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        *reinterpret_cast<uint4*>(S.a + swz(r, c0 / 8 + q)) =
+            make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
+    }
+  };
+
+  for (long long tile = blockIdx.x; tile < ntiles && !bad; tile += gridDim.x) {
     const int xb = (int)(tile % nxb);
     const long long row = tile / nxb;
     const int j = (int)(row % ny), k = (int)(row / ny);
     const int x0 = xb * kTileX;
-    __syncthreads();  // the previous tile's neighbourhood is no longer read
-    for (int q = tid; q < 2 * 9 * kHaloX; q += blockDim.x) {
-      const int f = q / (9 * kHaloX), rem = q - f * 9 * kHaloX;
-      const int rr = rem / kHaloX, xx = rem - rr * kHaloX;
-      const int jj = wrapc(j + rr % 3 - 1, ny, G.per[1]), kk = wrapc(k + rr / 3 - 1, nz, G.per[2]);
-      const int x = wrapc(x0 - 1 + xx, nx, G.per[0]);
-      const int64_t p = (int64_t)x + (int64_t)nx * (jj + (int64_t)ny * kk);
-      nbf[q] = d2f_bits(f == 0 ? A.div[p] : A.gmag[p]) * dl;
+    const int x = x0 + r;
+    const int64_t prow = (int64_t)nx * (j + (int64_t)ny * k);
+    const double rho_d = (x < nx) ? __ldg(A.rho + prow + x) : 1.0;
+    {  // the neighbourhood, rows (f, dj, dk) x halo columns x0 - 1 .. x0 + 128: loads first, then stores
+      const int xa = wrapc(x0 - 1 + r, nx, G.per[0]);
+      const int xe = wrapc(x0 - 1 + xc, nx, G.per[0]);
+      double v[18], ve = 0.0;
+#pragma unroll
+      for (int rr = 0; rr < 9; rr++) {
+        const int jj = wrapc(j + rr % 3 - 1, ny, G.per[1]), kk = wrapc(k + rr / 3 - 1, nz, G.per[2]);
+        const int64_t ro = (int64_t)nx * (jj + (int64_t)ny * kk);
+        v[rr] = __ldg(A.div + ro + xa);
+        v[9 + rr] = __ldg(A.gmag + ro + xa);
+        if (xr == rr) ve = __ldg(A.div + ro + xe);
+        if (xr == 9 + rr) ve = __ldg(A.gmag + ro + xe);
+      }
+      __syncthreads();  // the previous tile's neighbourhood is no longer read
+#pragma unroll
+      for (int q = 0; q < 18; q++) S.nb[q * kHaloX + r] = d2f_bits(v[q]) * dl;
+      if (xr >= 0) S.nb[xr * kHaloX + xc] = d2f_bits(ve) * dl;
     }
     __syncthreads();
-    const int lx0 = warp * 16;
-    if (x0 + lx0 < nx) {
-      // A fragments straight from the neighbourhood: column c of row r is feature c of point lx0 + r;
-      // a lane holds columns kt*16 + 2t + {0, 1, 8, 9} of rows g and g + 8
-      uint32_t a0[4][4], a1[4][4];
-      const float* pt = nbf + lx0 + g;
+    {  // the features of point x0 + r, normalised and packed to BF16
 #pragma unroll
-      for (int kt = 0; kt < 4; kt++) {
-        float v[4][2];
+      for (int q = 0; q < 8; q++) {
+        uint32_t pk[4];
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-          const ColInfo ci = S.col[kt * 16 + 2 * t + (q & 1) + (q >> 1) * 8];
-          v[q][0] = (pt[ci.off] - ci.xm) * ci.xs;
-          v[q][1] = (pt[ci.off + 8] - ci.xm) * ci.xs;
+        for (int h = 0; h < 4; h++) {
+          const ColInfo c0 = S.col[8 * q + 2 * h], c1 = S.col[8 * q + 2 * h + 1];
+          pk[h] = pack_bf16((S.nb[c0.off + r] - c0.xm) * c0.xs, (S.nb[c1.off + r] - c1.xm) * c1.xs);
         }
-        a0[kt][0] = pack_bf16(v[0][0], v[1][0]);
-        a0[kt][1] = pack_bf16(v[0][1], v[1][1]);
-        a0[kt][2] = pack_bf16(v[2][0], v[3][0]);
-        a0[kt][3] = pack_bf16(v[2][1], v[3][1]);
-      }
-      layer_relu<4>(a0, a1, S.w1, S.b1, g, t);
-      layer_relu<4>(a1, a0, S.w2, S.b2, g, t);
-      layer_relu<4>(a0, a1, S.w3, S.b3, g, t);
-      float c[4] = {S.b4[2 * t], S.b4[2 * t + 1], S.b4[2 * t], S.b4[2 * t + 1]};
-#pragma unroll
-      for (int kt = 0; kt < 4; kt++) {
-        const uint32_t w0 = *reinterpret_cast<const uint32_t*>(&S.w4[g][kt * 16 + 2 * t]);
-        const uint32_t w1 = *reinterpret_cast<const uint32_t*>(&S.w4[g][kt * 16 + 2 * t + 8]);
-        mma_bf16(c, a1[kt], w0, w1);
-      }
-      // lanes with t == 0 hold outputs 0 and 1 of rows g and g + 8
-      if (t == 0) {
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-          const int x = x0 + lx0 + g + 8 * h;
-          if (x < nx) {
-            const int64_t p = (int64_t)x + (int64_t)nx * (j + (int64_t)ny * k);
-            const float y0 = c[2 * h], y1 = c[2 * h + 1];
-            out_of_range |= !(y0 >= M.ylo[0] && y0 <= M.yhi[0] && y1 >= M.ylo[1] && y1 <= M.yhi[1]);
-            const float rho = d2f_bits(A.rho[p]);
-            // artificial viscosity and conductivity are non-negative (the plain operators are)
-            A.beta[p] = f2d_bits(fmaxf(0.0f, fmaf(y0, M.ys[0], M.ym[0])) * rho * fb);
-            A.kappa[p] = f2d_bits(fmaxf(0.0f, fmaf(y1, M.ys[1], M.ym[1])) * rho * fk);
-          }
-        }
+        *reinterpret_cast<uint4*>(S.a + swz(r, q)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
       }
     }
+    if (!layer(S.w[0], kH)) bad = true;
+    if (__syncthreads_or(bad)) break;
+    hidden(0);
+    if (!layer(S.w[1], kH)) bad = true;
+    if (__syncthreads_or(bad)) break;
+    hidden(1);
+    if (!layer(S.w[2], kH)) bad = true;
+    if (__syncthreads_or(bad)) break;
+    hidden(2);
+    if (!layer(S.w4, kTcOutRows)) bad = true;
+    if (__syncthreads_or(bad)) break;
+    uint32_t u[8];
+    tmem_ld8_nowait(tlane, u);
+    tmem_wait_ld();
+    if (x < nx) {
+      const float y0 = __uint_as_float(u[0]) + S.b4[0], y1 = __uint_as_float(u[1]) + S.b4[1];
+      out_of_range |= !(y0 >= M.ylo[0] && y0 <= M.yhi[0] && y1 >= M.ylo[1] && y1 <= M.yhi[1]);
+      const float rho = d2f_bits(rho_d);
+      A.beta[prow + x] = f2d_bits(fmaxf(0.0f, fmaf(y0, M.ys[0], M.ym[0])) * rho * fb);
+      A.kappa[prow + x] = f2d_bits(fmaxf(0.0f, fmaf(y1, M.ys[1], M.ym[1])) * rho * fk);
+    }
+    tc_fence_before();  // this tile's accumulator reads are done before the next tile's MMAs
+  }
+  if (bad && tid == 0) {
+    atomicExch(A.status, (int)PG_ETIMEOUT);
+    mbar_wait(&S.bar, (phase - 1) & 1);  // the MMAs still in flight (bounded)
   }
   if (__syncthreads_or(out_of_range) && tid == 0) atomicExch(A.flag, 1);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTmemCols) : "memory");
+  }
 }
 
 // |grad rho| by central differences, FP32 arithmetic: one thread per point,
@@ -486,16 +555,29 @@ int lad_check(const char* what) {
 int launch_lad_infer(const LadInferArgs& a, void* stream) {
   static int resident = 0;  // CTAs per SM (persistent grid: one wave)
   static int sms = 0;
-  const int smem = (int)(sizeof(InferSmem) + kNbRows * kHaloX * sizeof(float));
+  const int smem = (int)(sizeof(TcSmem) + 1024);  // + slack for the 1024-byte alignment
   if (resident == 0) {
-    cudaError_t e = cudaFuncSetAttribute(lad_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaError_t e = cudaFuncSetAttribute(lad_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     int dev = 0;
     if (e == cudaSuccess) e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, lad_infer_kernel,
-                                                                            kInferThreads, smem);
-    if (e != cudaSuccess || resident < 1) {
-      set_error("lad inference: %s", e != cudaSuccess ? cudaGetErrorString(e) : "kernel does not fit an SM");
+    // CTAs per SM from the kernel's own footprint (registers, shared memory + the 1 KB each CTA
+    // reserves); the occupancy query reported one CTA per SM for this tensor-memory kernel
+    cudaFuncAttributes fa;
+    int smem_sm = 0;
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, lad_infer_tc_kernel);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    if (e != cudaSuccess) {
+      set_error("lad inference: %s", cudaGetErrorString(e));
+      return PG_ECUDA;
+    }
+    const int by_smem = smem_sm / (smem + 1024);
+    const int by_regs = 65536 / (kTcThreads * (fa.numRegs > 0 ? fa.numRegs : 255));
+    resident = by_smem < by_regs ? by_smem : by_regs;
+    // every resident CTA holds kTcTmemCols of the SM's 512 tensor-memory columns
+    if (resident > kTcMaxResident) resident = kTcMaxResident;
+    if (resident < 1) {
+      set_error("lad inference: the kernel does not fit an SM");
       resident = 0;
       return PG_ECUDA;
     }
@@ -503,7 +585,7 @@ int launch_lad_infer(const LadInferArgs& a, void* stream) {
   const int64_t tiles = (int64_t)((a.grid.n[0] + kTileX - 1) / kTileX) * a.grid.n[1] * a.grid.n[2];
   const int64_t wave = (int64_t)sms * resident;
   const int blocks = (int)(tiles < wave ? tiles : wave);
-  lad_infer_kernel<<<blocks, kInferThreads, smem, (cudaStream_t)stream>>>(a);
+  lad_infer_tc_kernel<<<blocks, kTcThreads, smem, (cudaStream_t)stream>>>(a);
   count_launch();
   return lad_check("lad inference");
 }

@@ -593,6 +593,11 @@ int build_operator(int kind, int n, bool periodic, double scale, OpTables& t, in
     for (int l = 0; l < s.ncr; l++) t.rhs[(size_t)i * 9 + l] = r9[l];
   };
   for (int i = 0; i < n; i++) put_row(i, s.lhs, s.rhs);
+  if (s.ncr == 9) {  // the FP32 sweeps pair the 9-point interior weights about the centre
+    const double* r = &t.rhs[(size_t)(n / 2) * 9];
+    for (int k = 1; k <= 4; k++)
+      if (r[4 - k] != r[4 + k]) return PG_EINVAL;
+  }
   if (!periodic) {
     for (int end = 0; end < 2; end++) {
       const int c = end == 0 ? t.bcl : t.bch;

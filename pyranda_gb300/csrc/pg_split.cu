@@ -81,6 +81,20 @@ template <int KIND>
 __device__ __forceinline__ float window_rhs(const float2* v, const float* ai) {
   auto d = [&](int k, int c) { return (v[k].x - v[c].x) + (v[k].y - v[c].y); };
   if (KIND == 1) return ai[4] * d(4, 2) + ai[5] * d(5, 1) + ai[6] * d(6, 0);
+  if (KIND == 4) {
+    // the 9-point operators (d8, both filters) have symmetric interior weights
+    // (checked when the tables are built): the hi differences pair up about the
+    // centre, and the residuals, small against the differences, enter as
+    // sum_k a_k (lo_{+k} + lo_{-k}) - 2 (sum_k a_k) lo_c
+    float s = 0.0f, sl = 0.0f, a2 = 0.0f;
+#pragma unroll
+    for (int k = 1; k <= 4; k++) {
+      s += ai[4 + k] * ((v[4 + k].x - v[4].x) + (v[4 - k].x - v[4].x));
+      sl += ai[4 + k] * (v[4 + k].y + v[4 - k].y);
+      a2 += ai[4 + k];
+    }
+    return s + (sl - 2.0f * a2 * v[4].y);
+  }
   constexpr int H = (KIND == 4) ? 4 : 3;
   float s = 0.0f;
 #pragma unroll
