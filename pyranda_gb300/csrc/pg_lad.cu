@@ -22,9 +22,10 @@
 // shared memory, FP32 accumulators in tensor memory) and raises a device flag
 // when any raw output leaves [ylo, yhi] (the training range with a margin):
 // the plain LAD closure is then the fallback.
-// Training runs the same arithmetic on CUDA cores in lad_train_kernel
-// (forward with BF16 rounding at the same points, MSE loss, backward, FP32
-// gradient accumulation) and an Adam step in lad_adam_kernel.
+// Training (lad_train_tc_kernel) runs the forward with the same BF16 rounding
+// points and the backward on the tensor cores (mma.sync BF16 -> FP32, the
+// FP32 gradients as BF16 hi + lo), MSE loss, FP32 gradient accumulation, and
+// an Adam step in lad_adam_kernel.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -42,7 +43,6 @@ constexpr int kK = PG_LAD_K;          // 64 padded inputs
 constexpr int kH = PG_LAD_HIDDEN;     // 64
 constexpr int kOut = PG_LAD_OUT;      // 2
 constexpr int kTrainRows = 64;        // rows of a training CTA
-constexpr int kTrainThreads = 256;
 
 __device__ __forceinline__ int wrapc(int i, int n, int per) {
   if (n == 1) return 0;
@@ -381,147 +381,310 @@ __global__ void lad_normalize_kernel(const float* __restrict__ raw, int64_t ns, 
   }
 }
 
-struct TrainSmem {
-  float w1[kH][kK + 1], w2[kH][kH + 1], w3[kH][kH + 1], w4[kOut][kH + 1];
-  float b1[kH], b2[kH], b3[kH], b4[kOut];
-  float h1[kTrainRows][kH + 1], h2[kTrainRows][kH + 1], h3[kTrainRows][kH + 1];
-  float x[kTrainRows][kK + 1];
-  float d[kTrainRows][kH + 1];   // gradient w.r.t. the current layer's pre-activation
-  float e[kTrainRows][kH + 1];   // gradient w.r.t. the layer below's output
-  float dy[kTrainRows][kOut];
-  float loss[kTrainThreads / 32];
+// ------------------------------------------------------- training, tensor cores
+// The same step on the tensor cores (mma.sync m16n8k16, BF16 operands, FP32
+// accumulation).  One CTA = 64 rows of the batch, 4 warps of 16 rows.
+//  forward:  per warp, each layer's FP32 accumulator fragments become the
+//            next layer's BF16 A fragments in registers (bias, ReLU, BF16
+//            rounding as in inference); the output layer pads N to 8;
+//  backward: dY_l (the gradient at layer l's pre-activation, FP32) enters the
+//            MMAs as BF16 hi + lo (two products), so the gradient keeps ~16
+//            bits before its FP32 accumulation;
+//            dH_{l-1} = dY_l W_l per warp (A = dY_l from its own fragments,
+//            B = W_l^T from shared memory), masked by H_{l-1} > 0;
+//            dW_l = dY_l^T H_{l-1} over the CTA's 64 rows (A = dY_l^T and
+//            B = H_{l-1}^T from shared memory, each warp 16 output rows);
+//            the 2-output layer's gradients and every bias gradient are
+//            shuffle/shared-memory sums.  Gradients go to G with one atomic
+//            per parameter per CTA.
+constexpr int kTcTrainWarps = 4;
+constexpr int kLd = kH + 8;  // BF16 row stride of the shared-memory operands (staggers banks)
+
+struct TrainTcSmem {
+  __nv_bfloat16 w[3][kH][kLd];    // W_l[o][q]   (forward B: rows o, consecutive q)
+  __nv_bfloat16 wt[2][kH][kLd];   // W_l^T[q][o] for l = 2, 3 (backward B)
+  __nv_bfloat16 w4[8][kLd];       // output layer, rows >= kOut zero
+  __nv_bfloat16 ht[3][kH][kLd];   // X^T, H1^T, H2^T: [feature][row of the CTA]
+  float dyt[kH][kTrainRows + 4];  // dY_l^T: [output][row]
+  float w4f[kOut][kH];
+  float b[3][kH];
+  float b4[kOut];
+  float red[kTcTrainWarps][kH];   // per-warp bias-gradient partials
+  float loss[kTcTrainWarps];
 };
 
-__device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16(x)); }
+__device__ __forceinline__ uint32_t ld_u32(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
 
-// One CTA: kTrainRows rows of the batch.  Forward in BF16-in / FP32-accumulate
-// with BF16 rounding of inputs, weights and hidden activations (the inference
-// kernel's arithmetic), loss = mean over rows and outputs of (y - t)^2,
-// backward in FP32, gradients added into G (FP32) with atomics.
-__global__ void __launch_bounds__(kTrainThreads) lad_train_kernel(const LadTrainArgs A) {
-  extern __shared__ __align__(16) unsigned char lad_smem[];
-  TrainSmem& S = *reinterpret_cast<TrainSmem*>(lad_smem);
+// FP32 -> BF16 hi + BF16 lo (lo = the rounding residual of hi)
+__device__ __forceinline__ void split_bf16(float a, float b, uint32_t& hi, uint32_t& lo) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  const float2 hf = __bfloat1622float2(h);
+  const __nv_bfloat162 l = __floats2bfloat162_rn(a - hf.x, b - hf.y);
+  hi = *reinterpret_cast<const uint32_t*>(&h);
+  lo = *reinterpret_cast<const uint32_t*>(&l);
+}
+
+__global__ void __launch_bounds__(kTcTrainWarps * 32) lad_train_tc_kernel(const LadTrainArgs A) {
+  extern __shared__ __align__(16) unsigned char lad_train_raw[];
+  TrainTcSmem& S = *reinterpret_cast<TrainTcSmem*>(lad_train_raw);
   const pg_lad_model& M = A.model;
   const __nv_bfloat16* W = reinterpret_cast<const __nv_bfloat16*>(M.wbf16);
   const float* P = M.params;
   const __nv_bfloat16* X = reinterpret_cast<const __nv_bfloat16*>(A.X);
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+  const int nthr = kTcTrainWarps * 32;
   const int64_t row0 = (int64_t)blockIdx.x * kTrainRows;
   const int nr = (int)((A.rows - row0) < kTrainRows ? (A.rows - row0) : kTrainRows);
-  for (int i = tid; i < kH * kK; i += kTrainThreads) S.w1[i / kK][i % kK] = __bfloat162float(W[kW1 + i]);
-  for (int i = tid; i < kH * kH; i += kTrainThreads) {
-    S.w2[i / kH][i % kH] = __bfloat162float(W[kW2 + i]);
-    S.w3[i / kH][i % kH] = __bfloat162float(W[kW3 + i]);
+  const __nv_bfloat16 z = __float2bfloat16(0.0f);
+  for (int i = tid; i < kH * kK; i += nthr) {
+    const int o = i / kK, q = i % kK;
+    S.w[0][o][q] = W[kW1 + i];
+    S.w[1][o][q] = W[kW2 + i];
+    S.w[2][o][q] = W[kW3 + i];
+    S.wt[0][q][o] = W[kW2 + i];
+    S.wt[1][q][o] = W[kW3 + i];
   }
-  for (int i = tid; i < kOut * kH; i += kTrainThreads) S.w4[i / kH][i % kH] = __bfloat162float(W[kW4 + i]);
-  for (int i = tid; i < kH; i += kTrainThreads) {
-    S.b1[i] = P[kB1 + i];
-    S.b2[i] = P[kB2 + i];
-    S.b3[i] = P[kB3 + i];
+  for (int i = tid; i < 8 * kH; i += nthr) S.w4[i / kH][i % kH] = (i / kH < kOut) ? W[kW4 + i] : z;
+  for (int i = tid; i < kOut * kH; i += nthr) S.w4f[i / kH][i % kH] = __bfloat162float(W[kW4 + i]);
+  for (int i = tid; i < kH; i += nthr) {
+    S.b[0][i] = P[kB1 + i];
+    S.b[1][i] = P[kB2 + i];
+    S.b[2][i] = P[kB3 + i];
   }
   if (tid < kOut) S.b4[tid] = P[kB4 + tid];
-  for (int i = tid; i < kTrainRows * kK; i += kTrainThreads) {
-    const int r = i / kK, f = i % kK;
-    S.x[r][f] = (r < nr) ? __bfloat162float(X[(row0 + r) * kK + f]) : 0.0f;
+  // this warp's rows: r0 + g and r0 + g + 8 of the CTA
+  const int r0 = warp * 16, ra = r0 + g, rb = r0 + g + 8;
+  const bool va = ra < nr, vb = rb < nr;
+  // X as A fragments (rows beyond the batch are zero) and as X^T in shared memory
+  uint32_t ax[4][4];
+#pragma unroll
+  for (int kt = 0; kt < 4; kt++) {
+#pragma unroll
+    for (int h = 0; h < 4; h++) {
+      const int rr = (h & 1) ? rb : ra, cc = kt * 16 + 2 * t + (h >> 1) * 8;
+      const bool ok = (h & 1) ? vb : va;
+      ax[kt][h] = ok ? ld_u32(X + (row0 + rr) * kK + cc) : 0u;
+      const __nv_bfloat162 v = *reinterpret_cast<const __nv_bfloat162*>(&ax[kt][h]);
+      S.ht[0][cc][rr] = v.x;
+      S.ht[0][cc + 1][rr] = v.y;
+    }
   }
   __syncthreads();
-  // forward: h = bf16(relu(W x + b)) for three layers
-  auto dense = [&](const float (*w)[kH + 1], const float* b, const float (*in)[kH + 1], float (*out)[kH + 1]) {
-    for (int i = tid; i < kTrainRows * kH; i += kTrainThreads) {
-      const int r = i / kH, o = i % kH;
-      float s = b[o];
-      for (int q = 0; q < kH; q++) s += w[o][q] * in[r][q];
-      out[r][o] = bf16r(fmaxf(s, 0.0f));
+  // one forward layer: c = b + A W^T, then ReLU -> BF16 A fragments of the next layer (and H^T)
+  auto forward = [&](const uint32_t (*a)[4], int l, uint32_t (*an)[4], int store) {
+    float c[8][4];
+#pragma unroll
+    for (int nt = 0; nt < 8; nt++) {
+      const float b0 = S.b[l][nt * 8 + 2 * t], b1 = S.b[l][nt * 8 + 2 * t + 1];
+      c[nt][0] = b0; c[nt][1] = b1; c[nt][2] = b0; c[nt][3] = b1;
+#pragma unroll
+      for (int kt = 0; kt < 4; kt++)
+        mma_bf16(c[nt], a[kt], ld_u32(&S.w[l][nt * 8 + g][kt * 16 + 2 * t]),
+                 ld_u32(&S.w[l][nt * 8 + g][kt * 16 + 2 * t + 8]));
     }
-    __syncthreads();
+#pragma unroll
+    for (int kt = 0; kt < 4; kt++) {
+      an[kt][0] = pack_bf16(fmaxf(c[2 * kt][0], 0.f), fmaxf(c[2 * kt][1], 0.f));
+      an[kt][1] = pack_bf16(fmaxf(c[2 * kt][2], 0.f), fmaxf(c[2 * kt][3], 0.f));
+      an[kt][2] = pack_bf16(fmaxf(c[2 * kt + 1][0], 0.f), fmaxf(c[2 * kt + 1][1], 0.f));
+      an[kt][3] = pack_bf16(fmaxf(c[2 * kt + 1][2], 0.f), fmaxf(c[2 * kt + 1][3], 0.f));
+    }
+    if (store >= 0) {
+#pragma unroll
+      for (int kt = 0; kt < 4; kt++)
+#pragma unroll
+        for (int h = 0; h < 4; h++) {
+          const int rr = (h & 1) ? rb : ra, cc = kt * 16 + 2 * t + (h >> 1) * 8;
+          const __nv_bfloat162 v = *reinterpret_cast<const __nv_bfloat162*>(&an[kt][h]);
+          S.ht[store][cc][rr] = v.x;
+          S.ht[store][cc + 1][rr] = v.y;
+        }
+    }
   };
-  for (int i = tid; i < kTrainRows * kH; i += kTrainThreads) {
-    const int r = i / kH, o = i % kH;
-    float s = S.b1[o];
-    for (int q = 0; q < kK; q++) s += S.w1[o][q] * S.x[r][q];
-    S.h1[r][o] = bf16r(fmaxf(s, 0.0f));
-  }
-  __syncthreads();
-  dense(S.w2, S.b2, S.h1, S.h2);
-  dense(S.w3, S.b3, S.h2, S.h3);
-  // outputs, loss and dL/dy
-  float lsum = 0.0f;
-  for (int i = tid; i < kTrainRows * kOut; i += kTrainThreads) {
-    const int r = i / kOut, o = i % kOut;
-    float s = S.b4[o];
-    for (int q = 0; q < kH; q++) s += S.w4[o][q] * S.h3[r][q];
-    float g = 0.0f;
-    if (r < nr) {
-      const float e = s - A.T[(row0 + r) * kOut + o];
-      lsum += e * e;
-      g = 2.0f * e * A.inv_count;
-      if (A.Y) A.Y[(row0 + r) * kOut + o] = s;
+  uint32_t a1[4][4], a2[4][4], a3[4][4];
+  forward(ax, 0, a1, 1);
+  forward(a1, 1, a2, 2);
+  forward(a2, 2, a3, -1);
+  // output layer (N padded to 8): lanes with t = 0 hold outputs 0, 1 of rows ra and rb
+  float c4[4] = {S.b4[0], S.b4[1], S.b4[0], S.b4[1]};
+  if (t != 0) c4[0] = c4[1] = c4[2] = c4[3] = 0.0f;
+#pragma unroll
+  for (int kt = 0; kt < 4; kt++)
+    mma_bf16(c4, a3[kt], ld_u32(&S.w4[g][kt * 16 + 2 * t]), ld_u32(&S.w4[g][kt * 16 + 2 * t + 8]));
+  float dya[2] = {0.f, 0.f}, dyb[2] = {0.f, 0.f}, lsum = 0.f;
+  if (t == 0) {
+#pragma unroll
+    for (int o = 0; o < kOut; o++) {
+      if (va) {
+        const float e = c4[o] - A.T[(row0 + ra) * kOut + o];
+        lsum += e * e;
+        dya[o] = 2.0f * e * A.inv_count;
+        if (A.Y) A.Y[(row0 + ra) * kOut + o] = c4[o];
+      }
+      if (vb) {
+        const float e = c4[2 + o] - A.T[(row0 + rb) * kOut + o];
+        lsum += e * e;
+        dyb[o] = 2.0f * e * A.inv_count;
+        if (A.Y) A.Y[(row0 + rb) * kOut + o] = c4[2 + o];
+      }
     }
-    S.dy[r][o] = g;
+  }
+#pragma unroll
+  for (int o = 0; o < kOut; o++) {  // every lane of row g: the row's dy
+    dya[o] = __shfl_sync(0xffffffffu, dya[o], g * 4);
+    dyb[o] = __shfl_sync(0xffffffffu, dyb[o], g * 4);
+  }
+  // dY3 = (dy W4) masked by H3 > 0, in accumulator layout; dW4 = dy^T H3, db4 = sum dy
+  float d[8][4];
+  float gw4[kOut][8][2];
+#pragma unroll
+  for (int nt = 0; nt < 8; nt++) {
+    const __nv_bfloat162 ha = *reinterpret_cast<const __nv_bfloat162*>(&a3[nt >> 1][(nt & 1) * 2]);
+    const __nv_bfloat162 hb = *reinterpret_cast<const __nv_bfloat162*>(&a3[nt >> 1][(nt & 1) * 2 + 1]);
+    const float h[4] = {__bfloat162float(ha.x), __bfloat162float(ha.y), __bfloat162float(hb.x), __bfloat162float(hb.y)};
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      const int q = nt * 8 + 2 * t + (e & 1);
+      const float* dy = (e < 2) ? dya : dyb;
+      const float s = dy[0] * S.w4f[0][q] + dy[1] * S.w4f[1][q];
+      d[nt][e] = h[e] > 0.0f ? s : 0.0f;
+    }
+#pragma unroll
+    for (int o = 0; o < kOut; o++) {
+      gw4[o][nt][0] = dya[o] * h[0] + dyb[o] * h[2];
+      gw4[o][nt][1] = dya[o] * h[1] + dyb[o] * h[3];
+    }
+  }
+  // sums over the rows of the warp (lanes with equal t), then over the warps
+#pragma unroll
+  for (int o = 0; o < kOut; o++)
+#pragma unroll
+    for (int nt = 0; nt < 8; nt++)
+#pragma unroll
+      for (int e = 0; e < 2; e++) {
+        float v = gw4[o][nt][e];
+        v += __shfl_xor_sync(0xffffffffu, v, 4);
+        v += __shfl_xor_sync(0xffffffffu, v, 8);
+        v += __shfl_xor_sync(0xffffffffu, v, 16);
+        gw4[o][nt][e] = v;
+      }
+  if (g == 0) {
+#pragma unroll
+    for (int o = 0; o < kOut; o++)
+#pragma unroll
+      for (int nt = 0; nt < 8; nt++) {
+        atomicAdd(&A.grad[kW4 + o * kH + nt * 8 + 2 * t], gw4[o][nt][0]);
+        atomicAdd(&A.grad[kW4 + o * kH + nt * 8 + 2 * t + 1], gw4[o][nt][1]);
+      }
+  }
+  {
+    float sd[kOut];
+#pragma unroll
+    for (int o = 0; o < kOut; o++) {
+      float v = (t == 0) ? dya[o] + dyb[o] : 0.f;
+      v += __shfl_xor_sync(0xffffffffu, v, 4);
+      v += __shfl_xor_sync(0xffffffffu, v, 8);
+      v += __shfl_xor_sync(0xffffffffu, v, 16);
+      sd[o] = v;
+    }
+    if (lane == 0)
+      for (int o = 0; o < kOut; o++) atomicAdd(&A.grad[kB4 + o], sd[o]);
   }
   for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
-  if ((tid & 31) == 0) S.loss[tid >> 5] = lsum;
+  if (lane == 0) S.loss[warp] = lsum;
+
+  // hidden layers l = 3, 2, 1 (index 2, 1, 0): d holds dY_l in accumulator layout
+  for (int l = 2; l >= 0; l--) {
+    // bias gradient: column sums of dY_l over the CTA's rows
+#pragma unroll
+    for (int nt = 0; nt < 8; nt++)
+#pragma unroll
+      for (int e = 0; e < 2; e++) {
+        float v = d[nt][e] + d[nt][2 + e];
+        v += __shfl_xor_sync(0xffffffffu, v, 4);
+        v += __shfl_xor_sync(0xffffffffu, v, 8);
+        v += __shfl_xor_sync(0xffffffffu, v, 16);
+        if (g == 0) S.red[warp][nt * 8 + 2 * t + e] = v;
+      }
+    // dY_l^T for the weight gradient
+#pragma unroll
+    for (int nt = 0; nt < 8; nt++)
+#pragma unroll
+      for (int e = 0; e < 4; e++) S.dyt[nt * 8 + 2 * t + (e & 1)][(e < 2) ? ra : rb] = d[nt][e];
+    __syncthreads();
+    for (int o = tid; o < kH; o += nthr) {
+      float v = 0.f;
+      for (int w = 0; w < kTcTrainWarps; w++) v += S.red[w][o];
+      atomicAdd(&A.grad[(l == 0 ? kB1 : (l == 1 ? kB2 : kB3)) + o], v);
+    }
+    // dW_l[o][q] = sum_r dY_l[r][o] H_{l-1}[r][q]: this warp's 16 output rows o, all q, K = the 64 rows
+    {
+      float cw[8][4];
+#pragma unroll
+      for (int nt = 0; nt < 8; nt++) cw[nt][0] = cw[nt][1] = cw[nt][2] = cw[nt][3] = 0.f;
+      const int oa = r0 + g, ob = r0 + g + 8;
+#pragma unroll
+      for (int kt = 0; kt < 4; kt++) {
+        uint32_t ah[4], al[4];
+        split_bf16(S.dyt[oa][kt * 16 + 2 * t], S.dyt[oa][kt * 16 + 2 * t + 1], ah[0], al[0]);
+        split_bf16(S.dyt[ob][kt * 16 + 2 * t], S.dyt[ob][kt * 16 + 2 * t + 1], ah[1], al[1]);
+        split_bf16(S.dyt[oa][kt * 16 + 2 * t + 8], S.dyt[oa][kt * 16 + 2 * t + 9], ah[2], al[2]);
+        split_bf16(S.dyt[ob][kt * 16 + 2 * t + 8], S.dyt[ob][kt * 16 + 2 * t + 9], ah[3], al[3]);
+#pragma unroll
+        for (int nt = 0; nt < 8; nt++) {
+          const uint32_t b0 = ld_u32(&S.ht[l][nt * 8 + g][kt * 16 + 2 * t]);
+          const uint32_t b1 = ld_u32(&S.ht[l][nt * 8 + g][kt * 16 + 2 * t + 8]);
+          mma_bf16(cw[nt], ah, b0, b1);
+          mma_bf16(cw[nt], al, b0, b1);
+        }
+      }
+      float* gw = A.grad + (l == 0 ? kW1 : (l == 1 ? kW2 : kW3));
+#pragma unroll
+      for (int nt = 0; nt < 8; nt++) {
+        const int q = nt * 8 + 2 * t;
+        atomicAdd(&gw[oa * kK + q], cw[nt][0]);
+        atomicAdd(&gw[oa * kK + q + 1], cw[nt][1]);
+        atomicAdd(&gw[ob * kK + q], cw[nt][2]);
+        atomicAdd(&gw[ob * kK + q + 1], cw[nt][3]);
+      }
+    }
+    if (l == 0) break;
+    // dY_{l-1} = (dY_l W_l) masked by H_{l-1} > 0 (this warp's rows)
+    {
+      uint32_t ah[4][4], al[4][4];
+#pragma unroll
+      for (int kt = 0; kt < 4; kt++) {
+        split_bf16(d[2 * kt][0], d[2 * kt][1], ah[kt][0], al[kt][0]);
+        split_bf16(d[2 * kt][2], d[2 * kt][3], ah[kt][1], al[kt][1]);
+        split_bf16(d[2 * kt + 1][0], d[2 * kt + 1][1], ah[kt][2], al[kt][2]);
+        split_bf16(d[2 * kt + 1][2], d[2 * kt + 1][3], ah[kt][3], al[kt][3]);
+      }
+      const uint32_t (*hb)[4] = (l == 2) ? a2 : a1;
+#pragma unroll
+      for (int nt = 0; nt < 8; nt++) {
+        float c[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int kt = 0; kt < 4; kt++) {
+          const uint32_t b0 = ld_u32(&S.wt[l - 1][nt * 8 + g][kt * 16 + 2 * t]);
+          const uint32_t b1 = ld_u32(&S.wt[l - 1][nt * 8 + g][kt * 16 + 2 * t + 8]);
+          mma_bf16(c, ah[kt], b0, b1);
+          mma_bf16(c, al[kt], b0, b1);
+        }
+        const __nv_bfloat162 ha = *reinterpret_cast<const __nv_bfloat162*>(&hb[nt >> 1][(nt & 1) * 2]);
+        const __nv_bfloat162 hb2 = *reinterpret_cast<const __nv_bfloat162*>(&hb[nt >> 1][(nt & 1) * 2 + 1]);
+        d[nt][0] = __bfloat162float(ha.x) > 0.f ? c[0] : 0.f;
+        d[nt][1] = __bfloat162float(ha.y) > 0.f ? c[1] : 0.f;
+        d[nt][2] = __bfloat162float(hb2.x) > 0.f ? c[2] : 0.f;
+        d[nt][3] = __bfloat162float(hb2.y) > 0.f ? c[3] : 0.f;
+      }
+    }
+    __syncthreads();  // dyt and red are rewritten for the next layer
+  }
   __syncthreads();
   if (tid == 0 && A.loss) {
-    float l = 0.0f;
-    for (int w = 0; w < kTrainThreads / 32; w++) l += S.loss[w];
-    atomicAdd(A.loss, l * A.inv_count);
-  }
-  // layer 4: dW4 = dy^T h3, db4 = sum dy, d(h3) = dy W4 masked by h3 > 0
-  for (int i = tid; i < kOut * kH; i += kTrainThreads) {
-    const int o = i / kH, q = i % kH;
-    float s = 0.0f;
-    for (int r = 0; r < kTrainRows; r++) s += S.dy[r][o] * S.h3[r][q];
-    atomicAdd(&A.grad[kW4 + i], s);
-  }
-  if (tid < kOut) {
-    float s = 0.0f;
-    for (int r = 0; r < kTrainRows; r++) s += S.dy[r][tid];
-    atomicAdd(&A.grad[kB4 + tid], s);
-  }
-  for (int i = tid; i < kTrainRows * kH; i += kTrainThreads) {
-    const int r = i / kH, q = i % kH;
-    float s = 0.0f;
-    for (int o = 0; o < kOut; o++) s += S.dy[r][o] * S.w4[o][q];
-    S.d[r][q] = (S.h3[r][q] > 0.0f) ? s : 0.0f;
-  }
-  __syncthreads();
-  // hidden layers 3 and 2: dW = d^T h_below, db = sum d, e = d W masked by h_below > 0
-  auto back = [&](const float (*w)[kH + 1], const float (*hb)[kH + 1], float* gw, float* gb) {
-    for (int i = tid; i < kH * kH; i += kTrainThreads) {
-      const int o = i / kH, q = i % kH;
-      float s = 0.0f;
-      for (int r = 0; r < kTrainRows; r++) s += S.d[r][o] * hb[r][q];
-      atomicAdd(&gw[i], s);
-    }
-    for (int o = tid; o < kH; o += kTrainThreads) {
-      float s = 0.0f;
-      for (int r = 0; r < kTrainRows; r++) s += S.d[r][o];
-      atomicAdd(&gb[o], s);
-    }
-    for (int i = tid; i < kTrainRows * kH; i += kTrainThreads) {
-      const int r = i / kH, q = i % kH;
-      float s = 0.0f;
-      for (int o = 0; o < kH; o++) s += S.d[r][o] * w[o][q];
-      S.e[r][q] = (hb[r][q] > 0.0f) ? s : 0.0f;
-    }
-    __syncthreads();
-    for (int i = tid; i < kTrainRows * kH; i += kTrainThreads) S.d[i / kH][i % kH] = S.e[i / kH][i % kH];
-    __syncthreads();
-  };
-  back(S.w3, S.h2, A.grad + kW3, A.grad + kB3);
-  back(S.w2, S.h1, A.grad + kW2, A.grad + kB2);
-  // layer 1: dW1 = d^T x, db1 = sum d
-  for (int i = tid; i < kH * kK; i += kTrainThreads) {
-    const int o = i / kK, q = i % kK;
-    float s = 0.0f;
-    for (int r = 0; r < kTrainRows; r++) s += S.d[r][o] * S.x[r][q];
-    atomicAdd(&A.grad[kW1 + i], s);
-  }
-  for (int o = tid; o < kH; o += kTrainThreads) {
-    float s = 0.0f;
-    for (int r = 0; r < kTrainRows; r++) s += S.d[r][o];
-    atomicAdd(&A.grad[kB1 + o], s);
+    float lt = 0.f;
+    for (int w = 0; w < kTcTrainWarps; w++) lt += S.loss[w];
+    atomicAdd(A.loss, lt * A.inv_count);
   }
 }
 
@@ -618,9 +781,9 @@ int launch_lad_normalize(const float* raw, int64_t ns, const float* xm, const fl
 
 int launch_lad_train(const LadTrainArgs& a, void* stream) {
   static bool attr = false;
-  const int smem = (int)sizeof(TrainSmem);
+  const int smem = (int)sizeof(TrainTcSmem);
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(lad_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaError_t e = cudaFuncSetAttribute(lad_train_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) {
       set_error("lad training: %s", cudaGetErrorString(e));
       return PG_ECUDA;
@@ -629,7 +792,7 @@ int launch_lad_train(const LadTrainArgs& a, void* stream) {
   }
   if (a.rows <= 0) return PG_OK;
   const int blocks = (int)((a.rows + kTrainRows - 1) / kTrainRows);
-  lad_train_kernel<<<blocks, kTrainThreads, smem, (cudaStream_t)stream>>>(a);
+  lad_train_tc_kernel<<<blocks, kTcTrainWarps * 32, smem, (cudaStream_t)stream>>>(a);
   count_launch();
   return lad_check("lad training");
 }
