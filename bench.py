@@ -306,6 +306,8 @@ def sweep_roofline(ss, torch, reps=20):
 NCU_TRAFFIC_256 = {
     ("sf", "y", "dense"): (136362752 + 88161280, "profiles/roofline_traffic_256.md"),
     ("sf", "y", "banded"): (275878656 + 163471872, "profiles/roofline_traffic_256.md"),
+    ("d1", "x", "split"): (134330112 + 96838400, "profiles/seg_sweeps_256.md"),
+    ("d1", "z", "split"): (134425600 + 98427648, "profiles/seg_sweeps_256.md"),
 }
 
 
