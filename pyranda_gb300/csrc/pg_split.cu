@@ -444,7 +444,7 @@ struct GLine {
 __host__ __device__ inline size_t seg_tips_bytes(int S, int nl) { return al16((size_t)nl * (4 * S + 4) * 4); }
 
 template <int KIND, bool PER, bool IMPL, bool ADDBACK, int DIR, int EPI, bool EXACT>
-__global__ void __launch_bounds__(kSplitThreads, 3) seg_kernel(const SParams P) {
+__global__ void __launch_bounds__(kSplitThreads, EXACT ? 4 : 3) seg_kernel(const SParams P) {
   constexpr int H = (KIND == 4) ? 4 : 3;
   constexpr int L = kSplitSeg;
   constexpr bool kStage = (DIR == 0);  // x through a staged tile (direct per-thread runs of a line thrash L1)
