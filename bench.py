@@ -49,9 +49,9 @@ def parse():
                    help="steps after which the headline path's field error against FP64 is reported again "
                         "(0: only after the timed steps)")
     p.add_argument("--no-fusion", action="store_true", help="fast paths without the fused EOM kernels")
-    p.add_argument("--fusion-arith", default="fp64", choices=["fp32", "fp64"],
+    p.add_argument("--fusion-arith", default="fp64", choices=["fp32", "fp64", "df64"],
                    help="arithmetic of the fast paths' fused EOM kernels (fp64: bit-exact with unfused; "
-                        "fp32: FP32 arithmetic between FP64 fields)")
+                        "fp32: FP32 arithmetic between FP64 fields; df64: double-float FP32 pairs, ~48 bits)")
     p.add_argument("--mode", default="step", choices=["step", "sweeps", "profile", "peaks", "shock", "ensemble",
                                                       "shock-learned", "kernels", "lad"],
                    help="sweeps: time every directional sweep kernel alone on one n^3 field; "
@@ -853,9 +853,10 @@ def main():
     fast_runs = {}
     runs = ([("fp32", args.fusion_arith)] if args.precision == "fp32-only" else
             [("fp32", args.fusion_arith), ("dense", args.fusion_arith), ("auto", args.fusion_arith)])
-    other = "fp32" if args.fusion_arith == "fp64" else "fp64"
     if args.precision != "fp32-only" and not args.no_fusion:
-        runs.append(("auto", other))     # the same path with the other EOM arithmetic, for comparison only
+        for other in ("fp64", "df64", "fp32"):   # the same path with the other EOM arithmetics, for comparison only
+            if other != args.fusion_arith:
+                runs.append(("auto", other))
     for prec, arith in runs:
         sim = make_sim(n, prec, graphs=True, fusion=not args.no_fusion, arith=arith)
         run_steps(sim, 1)             # eager step (records the fused kernels, then compiles them)

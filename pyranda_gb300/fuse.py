@@ -68,6 +68,8 @@ __device__ __forceinline__ real pg_sign(real a) { return (a > (real)0) ? (real)1
 
 # FP64 arithmetic: every operation rounded on its own, as torch's separate kernels do.
 PRELUDE_FP64 = r"""typedef double real;
+#define PG_CARG double
+#define PG_LOADC(x) (x)
 #define PG_LOAD(x) (x)
 #define PG_STORE(x) (x)
 #define PG_C(x) (x)
@@ -98,8 +100,7 @@ PRELUDE_FP64 = r"""typedef double real;
 # FP32 arithmetic on FP64 fields (the fast paths): values converted by integer
 # operations (GB300 runs F2F on its FP64 pipe) keeping infinities and NaN,
 # FP32 math, results widened back to FP64.
-PRELUDE_FP32 = r"""typedef float real;
-__device__ __forceinline__ float pg_d2f(double d) {
+_CONV = r"""__device__ __forceinline__ float pg_d2f(double d) {
   const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
   const unsigned sign = hi & 0x80000000u, mag = hi & 0x7fffffffu;
   if (mag >= 0x7ff00000u) return __uint_as_float(sign | 0x7f800000u | ((((mag & 0xfffffu) | lo) != 0u) ? 0x400000u : 0u));
@@ -116,6 +117,11 @@ __device__ __forceinline__ double pg_f2d(float x) {
   if (mag < 0x00800000u) return __hiloint2double((int)sign, 0);
   return __hiloint2double((int)(((mag >> 3) + (896u << 20)) | sign), (int)(mag << 29));
 }
+"""
+
+PRELUDE_FP32 = r"""typedef float real;
+""" + _CONV + r"""#define PG_CARG float
+#define PG_LOADC(x) (x)
 #define PG_LOAD(x) pg_d2f(x)
 #define PG_STORE(x) pg_f2d(x)
 #define PG_C(x) ((float)(x))
@@ -142,6 +148,108 @@ __device__ __forceinline__ double pg_f2d(float x) {
 #define PG_FLOOR(x) floorf(x)
 #define PG_CEIL(x) ceilf(x)
 """ + _COMMON
+
+
+# Double-float arithmetic on FP64 fields: every value is an unevaluated sum
+# hi + lo of two FP32 numbers (about 48 significant bits), loaded from FP64
+# by the integer narrowing above plus one FP64 subtraction for the residual,
+# and stored as the FP64 sum hi + lo.  The operations are the classic
+# error-free transformations on the FP32 pipes (Dekker 1971; Knuth's
+# two-sum; the FMA form of the exact product): add / subtract ~2^-47,
+# multiply ~2^-47, divide and square root with one correction step ~2^-46
+# relative.  GB300 runs FP32 about 58x faster than FP64, so the EOM's long
+# expressions (pressure, stresses, energy flux) leave the FP64 pipe.  Other
+# functions (exp, log, pow with a non-integer exponent, ...) are evaluated
+# in FP64 from the value's FP64 sum.  Non-finite values are not carried:
+# an infinity becomes NaN (the simulation's NaN checks catch both).
+PRELUDE_DF64 = r"""#include <cstdint>
+#include <cmath>
+#include <cuda_runtime.h>
+struct pg_df { float hi, lo; };
+typedef pg_df real;
+""" + _CONV + r"""__device__ __forceinline__ pg_df pg_df_make(float h, float l) { pg_df r; r.hi = h; r.lo = l; return r; }
+// FP64 -> hi + lo: hi the FP32 rounding, lo the FP32 rounding of the exact residual
+__device__ __forceinline__ pg_df pg_df_load(double d) {
+  const float h = pg_d2f(d);
+  const float l = (__fsub_rn(h, h) == 0.0f) ? pg_d2f(__dsub_rn(d, pg_f2d(h))) : 0.0f;
+  return pg_df_make(h, l);
+}
+__device__ __forceinline__ double pg_df_store(pg_df a) { return __dadd_rn(pg_f2d(a.hi), pg_f2d(a.lo)); }
+// a literal: the conversions fold at compile time
+__device__ __forceinline__ pg_df pg_df_c(double c) {
+  const float h = (float)c;
+  return pg_df_make(h, (float)(c - (double)h));
+}
+__device__ __forceinline__ pg_df pg_df_fast2sum(float s, float t) {  // |s| >= |t|
+  const float h = __fadd_rn(s, t);
+  return pg_df_make(h, __fsub_rn(t, __fsub_rn(h, s)));
+}
+__device__ __forceinline__ pg_df pg_df_add(pg_df a, pg_df b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float v = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, v)), __fsub_rn(b.hi, v));
+  return pg_df_fast2sum(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ pg_df operator-(pg_df a) { return pg_df_make(-a.hi, -a.lo); }
+__device__ __forceinline__ pg_df pg_df_sub(pg_df a, pg_df b) { return pg_df_add(a, -b); }
+__device__ __forceinline__ pg_df pg_df_mul(pg_df a, pg_df b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return pg_df_fast2sum(p, e);
+}
+__device__ __forceinline__ pg_df pg_df_div(pg_df a, pg_df b) {
+  const float q1 = __fdiv_rn(a.hi, b.hi);
+  const pg_df r = pg_df_sub(a, pg_df_mul(pg_df_make(q1, 0.0f), b));
+  return pg_df_fast2sum(q1, __fdiv_rn(r.hi, b.hi));
+}
+__device__ __forceinline__ pg_df pg_df_sqrt(pg_df a) {
+  if (!(a.hi > 0.0f)) return pg_df_make(__fsqrt_rn(a.hi), 0.0f);  // zero, negative or NaN
+  const float s = __fsqrt_rn(a.hi);
+  const pg_df e = pg_df_sub(a, pg_df_mul(pg_df_make(s, 0.0f), pg_df_make(s, 0.0f)));
+  return pg_df_fast2sum(s, __fdiv_rn(e.hi, __fmul_rn(2.0f, s)));
+}
+__device__ __forceinline__ pg_df pg_df_abs(pg_df a) { return (a.hi < 0.0f) ? -a : a; }
+__device__ __forceinline__ bool pg_df_lt(pg_df a, pg_df b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ pg_df pg_min(pg_df a, pg_df b) {
+  return (a.hi != a.hi) ? a : ((b.hi != b.hi) ? b : (pg_df_lt(a, b) ? a : b));
+}
+__device__ __forceinline__ pg_df pg_max(pg_df a, pg_df b) {
+  return (a.hi != a.hi) ? a : ((b.hi != b.hi) ? b : (pg_df_lt(b, a) ? a : b));
+}
+__device__ __forceinline__ pg_df pg_sign(pg_df a) {
+  return (a.hi > 0.0f) ? pg_df_make(1.0f, 0.0f) : ((a.hi < 0.0f) ? pg_df_make(-1.0f, 0.0f) : a);
+}
+#define PG_F64(f, x) pg_df_load(f(pg_df_store(x)))
+#define PG_CARG double
+#define PG_LOADC(x) pg_df_load(x)
+#define PG_LOAD(x) pg_df_load(x)
+#define PG_STORE(x) pg_df_store(x)
+#define PG_C(x) pg_df_c(x)
+#define PG_ADD(a, b) pg_df_add(a, b)
+#define PG_SUB(a, b) pg_df_sub(a, b)
+#define PG_MUL(a, b) pg_df_mul(a, b)
+#define PG_DIV(a, b) pg_df_div(a, b)
+#define PG_SQRT(x) pg_df_sqrt(x)
+#define PG_RSQRT(x) pg_df_div(pg_df_make(1.0f, 0.0f), pg_df_sqrt(x))
+#define PG_POW(a, b) pg_df_load(pow(pg_df_store(a), pg_df_store(b)))
+#define PG_ABS(x) pg_df_abs(x)
+#define PG_EXP(x) PG_F64(exp, x)
+#define PG_LOG(x) PG_F64(log, x)
+#define PG_SIN(x) PG_F64(sin, x)
+#define PG_COS(x) PG_F64(cos, x)
+#define PG_TAN(x) PG_F64(tan, x)
+#define PG_TANH(x) PG_F64(tanh, x)
+#define PG_SINH(x) PG_F64(sinh, x)
+#define PG_COSH(x) PG_F64(cosh, x)
+#define PG_ATAN(x) PG_F64(atan, x)
+#define PG_ASIN(x) PG_F64(asin, x)
+#define PG_ACOS(x) PG_F64(acos, x)
+#define PG_LOG10(x) PG_F64(log10, x)
+#define PG_FLOOR(x) PG_F64(floor, x)
+#define PG_CEIL(x) PG_F64(ceil, x)
+"""
 
 
 def _const(node):
@@ -257,8 +365,8 @@ class Kernel:
                 defs.append("const real L%d = PG_LOAD(p%d[%s]);" % (i, i, "i" if k == "f" else "0"))
                 call.append("p%d" % i)
             else:
-                args.append("real c%d" % i)
-                defs.append("const real L%d = c%d;" % (i, i))
+                args.append("PG_CARG c%d" % i)
+                defs.append("const real L%d = PG_LOADC(c%d);" % (i, i))
                 call.append("c%d" % i)
         params = ", ".join(["int64_t n", "double* __restrict__ out"] + args)
         return ('extern "C" __global__ void %(k)s(%(p)s) {\n'
@@ -396,8 +504,8 @@ class Group:
                 defs.append("const real L%d = PG_LOAD(p%d[%s]);" % (i, i, "i" if k == "f" else "0"))
                 call.append("p%d" % i)
             else:
-                args.append("real c%d" % i)
-                defs.append("const real L%d = c%d;" % (i, i))
+                args.append("PG_CARG c%d" % i)
+                defs.append("const real L%d = PG_LOADC(c%d);" % (i, i))
                 call.append("c%d" % i)
         outs = ["double* __restrict__ out%d" % k for k in range(len(self.eqs))]
         params = ", ".join(["int64_t n"] + outs + args)
@@ -473,12 +581,12 @@ class Fuser:
     """
 
     def __init__(self, sim, min_ops=2, arith="fp64"):
-        if arith not in ("fp64", "fp32"):
-            raise ValueError("arith must be 'fp64' or 'fp32'")
+        if arith not in ("fp64", "fp32", "df64"):
+            raise ValueError("arith must be 'fp64', 'fp32' or 'df64'")
         self.sim = sim
         self.arith = arith
         self.min_ops = min_ops
-        self.scalar = (lambda v: ctypes.c_double(float(v))) if arith == "fp64" else (lambda v: ctypes.c_float(float(v)))
+        self.scalar = (lambda v: ctypes.c_float(float(v))) if arith == "fp32" else (lambda v: ctypes.c_double(float(v)))
         self.kernels = []
         self.groups = []
         self.lib = None
@@ -616,12 +724,12 @@ class Fuser:
         pre = ('extern "C" int pg_fused_preload() {\n  cudaFuncAttributes a;\n  int rc = 0;\n%s  return rc;\n}\n'
                % "".join("  rc |= (int)cudaFuncGetAttributes(&a, %s);\n" % nm for k in ks
                          for nm in ([k.name()] + ([k.name() + "_rk"] if getattr(k, "rk", None) else []))))
-        prelude = PRELUDE_FP64 if self.arith == "fp64" else PRELUDE_FP32
+        prelude = {"fp64": PRELUDE_FP64, "fp32": PRELUDE_FP32, "df64": PRELUDE_DF64}[self.arith]
         return prelude + "".join(k.source() for k in ks) + pre
 
     def build(self):
         """Compile every recorded kernel (once per distinct source) and bind them; returns the .so path."""
-        so = compile_source(self.source(), fmad=self.arith == "fp32")
+        so = compile_source(self.source(), fmad=self.arith != "fp64")
         self.lib = ctypes.CDLL(so)
         if self.lib.pg_fused_preload() != 0:
             raise RuntimeError("loading the fused EOM kernels failed")

@@ -794,8 +794,8 @@ class pyrandaSim:
         arithmetic='fp32' evaluates the expressions in FP32 between FP64
         fields (the fast paths' choice; FP32 rounding error per line).
         """
-        if arithmetic not in ("fp64", "fp32"):
-            raise ValueError("arithmetic must be 'fp64' or 'fp32'")
+        if arithmetic not in ("fp64", "fp32", "df64"):
+            raise ValueError("arithmetic must be 'fp64', 'fp32' or 'df64'")
         self._fuse_arith = arithmetic
         self._fuse_wanted = bool(enable)
         if self._fuse is not None and (not enable or self._fuse.arith != arithmetic):
