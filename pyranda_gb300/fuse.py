@@ -25,6 +25,8 @@ widened back to the FP64 field.  GB300's FP64 rate is about 1/58 of its FP32
 rate and its F2F conversions run on the FP64 pipe, which bounds the FP64
 kernels; the RK state accumulation, the boundary-closure solves and the d8
 LAD sweeps are not elementwise EOM arithmetic and keep FP64 either way.
+A third form, arith="df64", evaluates them in double-float arithmetic
+(FP32 hi + lo pairs, ~48 bits; PRELUDE_DF64).
 """
 import ast
 import copy

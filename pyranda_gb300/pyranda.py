@@ -792,7 +792,8 @@ class pyrandaSim:
         cached by source hash) and used from the following step on.  With
         arithmetic='fp64' the results equal the unfused ones bit for bit;
         arithmetic='fp32' evaluates the expressions in FP32 between FP64
-        fields (the fast paths' choice; FP32 rounding error per line).
+        fields (FP32 rounding error per line); arithmetic='df64' in
+        double-float FP32 pairs (~48 bits).
         """
         if arithmetic not in ("fp64", "fp32", "df64"):
             raise ValueError("arithmetic must be 'fp64', 'fp32' or 'df64'")
