@@ -104,6 +104,37 @@ def test_fp32_path_error_bound():
         assert e <= 1e-6, (name, e)
 
 
+@pytest.mark.parametrize("form", ["fp32-split", "auto"])
+def test_fast_sweeps_in_the_eom_stay_close_to_fp64(form):
+    """The split-line FP32 sweeps (register-resident along every direction of a
+    64^3 grid) and the autotuned path inside whole TGV RK steps, with graphs
+    and fused EOM kernels: every sweep epilogue of the step (store, the
+    divergence's accumulate, the ring's running max, the filters' FP64
+    add-back) runs there.  After 10 steps every conserved field is within
+    1e-6 relative L2 of the FP64 run (momentum components against the
+    momentum vector's norm, since rhow starts at zero)."""
+    from pyranda_gb300 import pyrandaSim
+    s64 = scripts.make_tgv(pyrandaSim, 64, _ts, silent=True)
+    sf = scripts.make_tgv(pyrandaSim, 64, _ts, silent=True, precision="auto" if form == "auto" else "fp32")
+    if form == "fp32-split":
+        sf.grid.set_line_split(True)
+    sf.use_fusion(True)
+    sf.use_graphs(True)
+    dt = float(s64.variables["dt"].data) * 0.5
+    t = 0.0
+    for _ in range(10):
+        s64.rk4(t, dt)
+        t = sf.rk4(t, dt)
+    mom = ["rhou", "rhov", "rhow"]
+    mnorm = sum(float(numpy.linalg.norm(to_host(s64.variables[n].data).ravel())) ** 2 for n in mom) ** 0.5
+    for name in ["rho", "rhou", "rhov", "rhow", "Et"]:
+        a, b = to_host(sf.variables[name].data), to_host(s64.variables[name].data)
+        ref = mnorm if name in mom else float(numpy.linalg.norm(b.ravel()))
+        e = float(numpy.linalg.norm((a - b).ravel())) / ref
+        print(form, name, "%.2e" % e)
+        assert e <= 1e-6, (form, name, e)
+
+
 def test_graph_replay_matches_eager():
     """A CUDA-graph replayed rk4 step gives the eager result bit for bit."""
     from pyranda_gb300 import pyrandaSim
