@@ -119,6 +119,15 @@ __device__ __forceinline__ long long to_fixed(double d, int E) {
 // or NaN in the grid.
 __device__ __forceinline__ float fixed_to_float(long long s, int E, float w) {
   if (E >= 2047) return __uint_as_float(0x7fc00000u);
+  const int k = E - 1075;  // the value is s x 2^k
+  if (k >= -126 && k <= 64) {
+    // the hardware conversion rounds |s| to 24 bits to nearest, ties to even, as the integer
+    // path below; the power of two is exact while the product stays normal (|s| < 2^63)
+    float f = __ll2float_rn(s) * __uint_as_float((unsigned)(k + 127) << 23);
+    if (fabsf(f) < 1.17549435e-38f) f = 0.0f;  // below the FP32 normal range: zero, as below
+    f *= w;
+    return f;
+  }
   if (s == 0) return 0.0f;
   const unsigned long long a = (unsigned long long)(s < 0 ? -s : s);
   int top = 63 - __clzll((long long)a);
