@@ -89,12 +89,11 @@ constexpr int kW1 = 0, kW2 = kH * kK, kW3 = kW2 + kH * kH, kW4 = kW3 + kH * kH, 
               kB2 = kB1 + kH, kB3 = kB2 + kH, kB4 = kB3 + kH;
 static_assert(kB1 == PG_LAD_NWEIGHT && kB4 + kOut == PG_LAD_NPARAM, "parameter layout");
 
-// One CTA = 128 consecutive x-points of one (j, k) row.  The 3 x 3 rows
+// Inference tile: 128 consecutive x-points of one (j, k) row.  The 3 x 3 rows
 // around it (130 points each: one halo point per side) of div*D and
-// |grad rho|*D are staged once in shared memory (rows 0..17), after a row of
+// |grad rho|*D are staged once in shared memory (rows 0..17), beside a row of
 // D (18) and a row of zeros (19) for the constant and padding columns; every
-// warp then builds the features of its 16 points from there and runs the
-// network.  (The tile and neighbourhood layout of the inference kernel.)
+// point's 64 features are read from there.
 constexpr int kTileX = 128;
 constexpr int kHaloX = kTileX + 2;
 constexpr int kNbRows = 2 * 9 + 2;
@@ -124,7 +123,7 @@ struct TcSmem {                    // placed at a 1024-byte boundary
   uint8_t a[128 * 128];            // A: 128 rows x 64 BF16
   uint8_t w[3][kH * 128];          // B of the hidden layers: 64 rows (outputs) x 64 BF16 (inputs)
   uint8_t w4[kTcOutRows * 128];    // B of the output layer: rows >= kOut are zero
-  float nb[kNbRows * kHaloX];      // the neighbourhood of the tile (as lad_infer_kernel)
+  float nb[kNbRows * kHaloX];      // the neighbourhood of the tile (rows 0..17 staged, 18: D, 19: zeros)
   float b[3][kH];
   float b4[kOut];
   ColInfo col[kK];
