@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libpyranda_gpu.so")
-SOURCES = ["pg_setup.cpp", "pg_sweep_f64.cu", "pg_sweep_f32.cu", "pg_elem.cu", "pg_capi.cu", "pg_noalloc.cu", "pg_dense.cu", "pg_lad.cu", "pg_split.cu"]
+SOURCES = ["pg_setup.cpp", "pg_sweep_f64.cu", "pg_sweep_f32.cu", "pg_sweep_f32_r4.cu", "pg_elem.cu", "pg_capi.cu", "pg_noalloc.cu", "pg_dense.cu", "pg_lad.cu", "pg_split.cu", "pg_seg_r3.cu", "pg_seg_r4.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -32,6 +32,7 @@ def _needs_build():
         return True
     t = os.path.getmtime(LIB)
     deps = [os.path.join(SRC, s) for s in SOURCES] + [os.path.join(SRC, "pg_internal.h"), os.path.join(SRC, "pg_sweep.cuh"),
+                                                      os.path.join(SRC, "pg_split.cuh"), os.path.join(SRC, "pg_tc.cuh"),
                                                       os.path.join(HERE, "..", "include", "pyranda_gpu.h")]
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 

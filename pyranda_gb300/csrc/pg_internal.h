@@ -42,6 +42,13 @@ enum {
   EPI_RING_MAX = 3,  // out = max(out, |r| * s)  (later directions / components)
   EPI_COUNT = 4
 };
+// Epilogues each operator is called with; the sweep kernels instantiate only
+// these: d1 and d2 store or accumulate, d8 stores or keeps the ring's running
+// max, d4 and the filters store.
+constexpr unsigned kEpiStoreAdd = (1u << EPI_STORE) | (1u << EPI_ADD);
+constexpr unsigned kEpiStore = (1u << EPI_STORE);
+constexpr unsigned kEpiRing = (1u << EPI_STORE) | (1u << EPI_RING_SET) | (1u << EPI_RING_MAX);
+
 
 // One operator of one grid along one direction, as the sweep kernels read it
 // (device memory).  A single grid has one entry per (precision, kind,

@@ -605,49 +605,76 @@ int launch_t(const KParams& P, void* stream) {
   return PG_OK;
 }
 
-template <typename T, int KIND, bool PER, bool IMPL, bool ADDBACK, typename TR = T>
+template <typename T, int KIND, bool PER, bool IMPL, bool ADDBACK, unsigned EPIS, typename TR, int DIR>
+int dispatch_epi(const KParams& P, int epi, void* st) {
+  if constexpr ((EPIS >> EPI_STORE) & 1u)
+    if (epi == EPI_STORE) return launch_t<T, KIND, PER, IMPL, ADDBACK, DIR, EPI_STORE, TR>(P, st);
+  if constexpr ((EPIS >> EPI_ADD) & 1u)
+    if (epi == EPI_ADD) return launch_t<T, KIND, PER, IMPL, ADDBACK, DIR, EPI_ADD, TR>(P, st);
+  if constexpr ((EPIS >> EPI_RING_SET) & 1u)
+    if (epi == EPI_RING_SET) return launch_t<T, KIND, PER, IMPL, ADDBACK, DIR, EPI_RING_SET, TR>(P, st);
+  if constexpr ((EPIS >> EPI_RING_MAX) & 1u)
+    if (epi == EPI_RING_MAX) return launch_t<T, KIND, PER, IMPL, ADDBACK, DIR, EPI_RING_MAX, TR>(P, st);
+  set_error("sweep: epilogue %d is not built for this operator", epi);
+  return PG_EINVAL;
+}
+
+template <typename T, int KIND, bool PER, bool IMPL, bool ADDBACK, unsigned EPIS, typename TR = T>
 int dispatch_dir_epi(const KParams& P, int dir, int epi, void* st) {
-#define PG_EPI_CASES(D)                                                                          \
-  switch (epi) {                                                                                 \
-    case EPI_STORE: return launch_t<T, KIND, PER, IMPL, ADDBACK, D, EPI_STORE, TR>(P, st);       \
-    case EPI_ADD: return launch_t<T, KIND, PER, IMPL, ADDBACK, D, EPI_ADD, TR>(P, st);           \
-    case EPI_RING_SET: return launch_t<T, KIND, PER, IMPL, ADDBACK, D, EPI_RING_SET, TR>(P, st); \
-    default: return launch_t<T, KIND, PER, IMPL, ADDBACK, D, EPI_RING_MAX, TR>(P, st);           \
+  if (dir == 0) return dispatch_epi<T, KIND, PER, IMPL, ADDBACK, EPIS, TR, 0>(P, epi, st);
+  if (dir == 1) return dispatch_epi<T, KIND, PER, IMPL, ADDBACK, EPIS, TR, 1>(P, epi, st);
+  return dispatch_epi<T, KIND, PER, IMPL, ADDBACK, EPIS, TR, 2>(P, epi, st);
+}
+
+// The 3- and 7-point operators (d1, d2, d4) and the 9-point ones (d8, the
+// filters), in separate functions so that a translation unit can instantiate
+// one family.
+template <typename T>
+int dispatch_kind_r3(const OpRef& op, const KParams& P, int dir, int epi, void* st) {
+  switch (op.kind) {
+    case OPK_D1:
+      return op.periodic ? dispatch_dir_epi<T, 1, true, true, false, kEpiStoreAdd>(P, dir, epi, st)
+                         : dispatch_dir_epi<T, 1, false, true, false, kEpiStoreAdd>(P, dir, epi, st);
+    case OPK_D2:
+      return op.periodic ? dispatch_dir_epi<T, 3, true, true, false, kEpiStoreAdd>(P, dir, epi, st)
+                         : dispatch_dir_epi<T, 3, false, true, false, kEpiStoreAdd>(P, dir, epi, st);
+    case OPK_D4:
+      return op.periodic ? dispatch_dir_epi<T, 3, true, false, false, kEpiStore>(P, dir, epi, st)
+                         : dispatch_dir_epi<T, 3, false, false, false, kEpiStore>(P, dir, epi, st);
+    default:
+      set_error("sweep: operator %d is not a 3- or 7-point operator", op.kind);
+      return PG_EINVAL;
   }
-  if (dir == 0) { PG_EPI_CASES(0) }
-  if (dir == 1) { PG_EPI_CASES(1) }
-  PG_EPI_CASES(2)
-#undef PG_EPI_CASES
 }
 
 template <typename T>
-int dispatch_kind(const OpRef& op, const KParams& P, int dir, int epi, void* st) {
+int dispatch_kind_r4(const OpRef& op, const KParams& P, int dir, int epi, void* st) {
   switch (op.kind) {
-    case OPK_D1:
-      return op.periodic ? dispatch_dir_epi<T, 1, true, true, false>(P, dir, epi, st)
-                         : dispatch_dir_epi<T, 1, false, true, false>(P, dir, epi, st);
     case OPK_D8: {
       // FP32 sweeps take the exact fixed-point RHS where the weights allow it
       using TRX = typename std::conditional<std::is_same<T, float>::value, long long, T>::type;
       if (std::is_same<T, float>::value && op.exact)
-        return op.periodic ? dispatch_dir_epi<T, 4, true, true, false, TRX>(P, dir, epi, st)
-                           : dispatch_dir_epi<T, 4, false, true, false, TRX>(P, dir, epi, st);
-      return op.periodic ? dispatch_dir_epi<T, 4, true, true, false>(P, dir, epi, st)
-                         : dispatch_dir_epi<T, 4, false, true, false>(P, dir, epi, st);
+        return op.periodic ? dispatch_dir_epi<T, 4, true, true, false, kEpiRing, TRX>(P, dir, epi, st)
+                           : dispatch_dir_epi<T, 4, false, true, false, kEpiRing, TRX>(P, dir, epi, st);
+      return op.periodic ? dispatch_dir_epi<T, 4, true, true, false, kEpiRing>(P, dir, epi, st)
+                         : dispatch_dir_epi<T, 4, false, true, false, kEpiRing>(P, dir, epi, st);
     }
     case OPK_SF:
-      return op.periodic ? dispatch_dir_epi<T, 4, true, true, true>(P, dir, epi, st)
-                         : dispatch_dir_epi<T, 4, false, true, true>(P, dir, epi, st);
-    case OPK_D2:
-      return op.periodic ? dispatch_dir_epi<T, 3, true, true, false>(P, dir, epi, st)
-                         : dispatch_dir_epi<T, 3, false, true, false>(P, dir, epi, st);
-    case OPK_D4:
-      return op.periodic ? dispatch_dir_epi<T, 3, true, false, false>(P, dir, epi, st)
-                         : dispatch_dir_epi<T, 3, false, false, false>(P, dir, epi, st);
+      return op.periodic ? dispatch_dir_epi<T, 4, true, true, true, kEpiStore>(P, dir, epi, st)
+                         : dispatch_dir_epi<T, 4, false, true, true, kEpiStore>(P, dir, epi, st);
+    case OPK_GF:
+      return op.periodic ? dispatch_dir_epi<T, 4, true, false, true, kEpiStore>(P, dir, epi, st)
+                         : dispatch_dir_epi<T, 4, false, false, true, kEpiStore>(P, dir, epi, st);
     default:
-      return op.periodic ? dispatch_dir_epi<T, 4, true, false, true>(P, dir, epi, st)
-                         : dispatch_dir_epi<T, 4, false, false, true>(P, dir, epi, st);
+      set_error("sweep: operator %d is not a 9-point operator", op.kind);
+      return PG_EINVAL;
   }
+}
+
+template <typename T>
+int dispatch_kind(const OpRef& op, const KParams& P, int dir, int epi, void* st) {
+  return (op.kind == OPK_D1 || op.kind == OPK_D2 || op.kind == OPK_D4) ? dispatch_kind_r3<T>(op, P, dir, epi, st)
+                                                                       : dispatch_kind_r4<T>(op, P, dir, epi, st);
 }
 
 }  // namespace

@@ -4,8 +4,11 @@
 
 namespace pg {
 
+int launch_sweep_f32_r4(const OpRef& op, const KParams& P, int dir, int epi, void* st);  // pg_sweep_f32_r4.cu
+
 int launch_sweep_f32(const OpRef& op, const KParams& P, int dir, int epi, void* st) {
-  return dispatch_kind<float>(op, P, dir, epi, st);
+  if (op.kind == OPK_D1 || op.kind == OPK_D2 || op.kind == OPK_D4) return dispatch_kind_r3<float>(op, P, dir, epi, st);
+  return launch_sweep_f32_r4(op, P, dir, epi, st);
 }
 
 namespace {
