@@ -44,3 +44,36 @@ def test_calls_without_gpu_fail_cleanly():
     assert lib.pg_create(None, None) == _lib.PG_EINVAL
     assert b"NULL" in lib.pg_last_error()
     assert lib.pg_version().startswith(b"pyranda_gb300")
+
+
+def test_grid_codes_checked_before_any_cuda_call():
+    """pg_create validates the boundary codes, the coordinate system and the
+    extents on the host, before it touches the device: bad values return
+    PG_EINVAL / PG_EBADSHAPE with a message, with or without a GPU."""
+    import ctypes
+    from pyranda_gb300 import _lib
+    lib = _lib.load()
+
+    def grid(**kw):
+        g = _lib.pg_grid()
+        for d in range(3):
+            g.n[d] = 16
+            g.periodic[d] = 0
+            g.x1[d], g.xn[d] = 0.0, 1.0
+        for k, v in kw.items():
+            if k == "bc":
+                d, e, b = v
+                g.bc[d][e] = b
+            elif k == "n0":
+                g.n[0] = v
+            else:
+                setattr(g, k, v)
+        return g
+
+    h = ctypes.c_void_p()
+    assert lib.pg_create(ctypes.byref(grid(bc=(1, 0, 7))), ctypes.byref(h)) == _lib.PG_EINVAL
+    assert b"pg_bc" in lib.pg_last_error()
+    assert lib.pg_create(ctypes.byref(grid(coordsys=2)), ctypes.byref(h)) == _lib.PG_EINVAL
+    assert b"coordsys" in lib.pg_last_error()
+    assert lib.pg_create(ctypes.byref(grid(n0=0)), ctypes.byref(h)) == _lib.PG_EBADSHAPE
+    assert lib.pg_create(ctypes.byref(grid(precision=9)), ctypes.byref(h)) == _lib.PG_EINVAL
