@@ -126,6 +126,12 @@ int pg_set_line_split(pg_handle* h, int mode);
  * line), 1 (dense tensor-core kernel) or 2 (split-line banded), for op 0 d1,
  * 1 d8, 2 compact filter, 3 Gaussian filter, 4 d2, 5 d4. */
 int pg_sweep_plan(const pg_handle* h, int* plan);
+/* Applies a plan in pg_sweep_plan's layout (0 FP32 banded, 1 dense, 2 FP32
+ * split-line per operator and direction) without timing it: builds the dense
+ * and split tables the plan needs (allocates and synchronises) and runs the
+ * FP32 path with it.  PG_EINVAL if an entry names a form the grid lacks.
+ * No counterpart in the reference (an autotuner's cached result). */
+int pg_set_sweep_plan(pg_handle* h, const int* plan);
 /* The sweep plan of PG_DENSE / PG_AUTO: plan[op * 3 + dir] = 1 where the
  * dense kernel runs (op 0 d1, 1 d8, 2 compact filter, 3 Gaussian filter). */
 int pg_dense_plan(const pg_handle* h, int* plan);

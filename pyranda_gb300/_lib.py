@@ -73,6 +73,7 @@ SIGNATURES = [
     ("pg_dense_plan", I, [P, ctypes.POINTER(ctypes.c_int)]),
     ("pg_set_line_split", I, [P, I]),
     ("pg_sweep_plan", I, [P, ctypes.POINTER(ctypes.c_int)]),
+    ("pg_set_sweep_plan", I, [P, ctypes.POINTER(ctypes.c_int)]),
     ("pg_wait_selftest", I, [P, ctypes.c_uint, P]),
     ("pg_last_error", ctypes.c_char_p, []),
     ("pg_version", ctypes.c_char_p, []),

@@ -1251,6 +1251,44 @@ int pg_sweep_plan(const pg_handle* h, int* plan) {
   return PG_OK;
 }
 
+// A plan as pg_sweep_plan writes it (per operator and direction: 0 FP32 banded,
+// 1 dense, 2 FP32 split-line), applied without timing: the dense and split
+// tables it needs are built, then the handle runs the FP32 path with it.
+int pg_set_sweep_plan(pg_handle* h, const int* plan) {
+  if (!h || !plan) return PG_EINVAL;
+  Ctx& c = h->c;
+  const std::vector<GridInfo> g{h->g};
+  bool want_dense = false, want_split = false;
+  for (int i = 0; i < OPK_COUNT * 3; i++) {
+    if (plan[i] < 0 || plan[i] > 2) {
+      set_error("pg_set_sweep_plan: entry %d = %d is not 0 (banded), 1 (dense) or 2 (split)", i, plan[i]);
+      return PG_EINVAL;
+    }
+    want_dense = want_dense || plan[i] == 1;
+    want_split = want_split || plan[i] == 2;
+  }
+  int rc = want_dense ? build_dense(c, g) : PG_OK;
+  if (rc == PG_OK && want_split) rc = build_split_ctx(c, g);
+  if (rc != PG_OK) return rc;
+  for (int k = 0; k < OPK_COUNT; k++)
+    for (int d = 0; d < 3; d++) {
+      const int p = plan[k * 3 + d];
+      if ((p == 1 && !c.dsets[k][d].ok) || (p == 2 && !c.splits[PG_FP32][k][d].ok)) {
+        set_error("pg_set_sweep_plan: operator %d along %d has no %s form on this grid", k, d,
+                  p == 1 ? "dense" : "split");
+        return PG_EINVAL;
+      }
+    }
+  c.precision = PG_FP32;
+  c.dense = want_dense;
+  for (int k = 0; k < OPK_COUNT; k++)
+    for (int d = 0; d < 3; d++) {
+      c.use_dense[k][d] = plan[k * 3 + d] == 1;
+      c.use_split[PG_FP32][k][d] = plan[k * 3 + d] == 2;
+    }
+  return PG_OK;
+}
+
 int pg_dense_plan(const pg_handle* h, int* plan) {
   if (!h || !plan) return PG_EINVAL;
   for (int k = 0; k <= OPK_GF; k++)

@@ -8,6 +8,8 @@ into ``libpyranda_gpu.so`` on the current torch stream; outputs are allocated
 by torch's caching allocator (or passed in), never by the library.
 """
 import ctypes
+import json
+import os
 
 import torch
 
@@ -58,6 +60,50 @@ def flush_pending():
         getattr(lib, destroy)(h)
 
 
+PLAN_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "sweep_plans.json")
+
+
+def _plan_cache_enabled():
+    return os.environ.get("PYRANDA_GB300_PLAN_CACHE", "1") != "0"
+
+
+def _plan_cache_get(key, path=None):
+    """The cached autotuned plan (18 ints, pg_sweep_plan's layout) for key, or None."""
+    if not _plan_cache_enabled():
+        return None
+    try:
+        with open(path or PLAN_CACHE) as f:
+            plan = json.load(f).get(key)
+    except (OSError, ValueError):
+        return None
+    if isinstance(plan, list) and len(plan) == 18 and all(v in (0, 1, 2) for v in plan):
+        return plan
+    return None
+
+
+def _plan_cache_put(key, plan, path=None):
+    """Adds key -> plan to the cache file (written to a temporary file and renamed into place)."""
+    if not _plan_cache_enabled():
+        return
+    path = path or PLAN_CACHE
+    try:
+        with open(path) as f:
+            data = json.load(f)
+        if not isinstance(data, dict):
+            data = {}
+    except (OSError, ValueError):
+        data = {}
+    data[key] = [int(v) for v in plan]
+    try:
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        tmp = "%s.%d.tmp" % (path, os.getpid())
+        with open(tmp, "w") as f:
+            json.dump(data, f)
+        os.replace(tmp, path)
+    except OSError:
+        pass
+
+
 class Grid:
     """A Cartesian pyranda patch on one GPU (parcop.f90:23-70 setup + setup_mesh)."""
 
@@ -90,11 +136,23 @@ class Grid:
         self.coordsys = int(coordsys)
         self.symmetric = tuple((not self.periodic[d]) and "SYMM" in self.bc[d] for d in range(3))
         self.precision = precision
-        g.precision = _lib.precision_code(precision)
+        # the autotuned path reuses a plan measured before for the same grid, GPU and library build
+        cached = _plan_cache_get(self._plan_key()) if precision == "auto" else None
+        g.precision = _lib.precision_code("fp32" if cached is not None else precision)
         h = ctypes.c_void_p()
         with torch.cuda.device(self.device):
             _lib.check(self.lib.pg_create(ctypes.byref(g), ctypes.byref(h)), "pg_create")
         self.h = h
+        self.plan_from_cache = False
+        if cached is not None:
+            plan = (ctypes.c_int * len(cached))(*cached)
+            with torch.cuda.device(self.device):
+                _lib.check(self.lib.pg_set_sweep_plan(self.h, plan), "pg_set_sweep_plan")
+            self.plan_from_cache = True
+        elif precision == "auto":
+            raw = (ctypes.c_int * 18)()
+            _lib.check(self.lib.pg_sweep_plan(self.h, raw), "pg_sweep_plan")
+            _plan_cache_put(self._plan_key(), list(raw))
         pd = (ctypes.c_double * 3)()
         md = (ctypes.c_double * 3)()
         self.lib.pg_get_spacing(self.h, pd, md)
@@ -105,6 +163,14 @@ class Grid:
         self.line_split = False
         if line_split:
             self.set_line_split(True)
+
+    def _plan_key(self):
+        """What an autotuned plan depends on: the operators (extents, periodicity, ends,
+        coordinates), the GPU and the library build."""
+        lib = _lib.lib_path()
+        st = os.stat(lib)
+        return json.dumps([list(self.n), list(self.periodic), [list(b) for b in self.bc], self.coordsys,
+                           torch.cuda.get_device_name(self.device), st.st_size, int(st.st_mtime)])
 
     def __del__(self):
         try:

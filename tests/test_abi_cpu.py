@@ -77,3 +77,29 @@ def test_grid_codes_checked_before_any_cuda_call():
     assert b"coordsys" in lib.pg_last_error()
     assert lib.pg_create(ctypes.byref(grid(n0=0)), ctypes.byref(h)) == _lib.PG_EBADSHAPE
     assert lib.pg_create(ctypes.byref(grid(precision=9)), ctypes.byref(h)) == _lib.PG_EINVAL
+
+
+def test_plan_cache_round_trip(tmp_path):
+    """The autotuner's plan cache: a stored plan is read back under its key,
+    other keys miss, malformed entries and files are ignored."""
+    import json
+    from pyranda_gb300 import grid
+    path = str(tmp_path / "plans.json")
+    assert grid._plan_cache_get("a", path) is None
+    plan = [2] * 12 + [0] * 6
+    grid._plan_cache_put("a", plan, path)
+    grid._plan_cache_put("b", [1] * 18, path)
+    assert grid._plan_cache_get("a", path) == plan
+    assert grid._plan_cache_get("b", path) == [1] * 18
+    assert grid._plan_cache_get("c", path) is None
+    with open(path) as f:
+        data = json.load(f)
+    data["a"] = [7] * 18
+    with open(path, "w") as f:
+        json.dump(data, f)
+    assert grid._plan_cache_get("a", path) is None
+    with open(path, "w") as f:
+        f.write("not json")
+    assert grid._plan_cache_get("b", path) is None
+    grid._plan_cache_put("b", [1] * 18, path)
+    assert grid._plan_cache_get("b", path) == [1] * 18

@@ -196,3 +196,21 @@ def test_split_fp32_differences_keep_a_large_mean(oracle):
         es = numpy.linalg.norm((to_host(g.filter("spectral", dv, d)) - ref).ravel()) / numpy.linalg.norm(
             (v - v.mean()).ravel())
         assert es <= 1e-6, ("sf", d, es)
+
+
+def test_autotuned_plan_is_cached_and_reapplied(tmp_path, monkeypatch):
+    """The autotuner's plan is stored under the grid, GPU and library build;
+    a second autotuned grid of the same shape applies it without timing
+    (pg_set_sweep_plan) and computes the same bits."""
+    from pyranda_gb300 import grid as G
+    monkeypatch.setattr(G, "PLAN_CACHE", str(tmp_path / "plans.json"))
+    shape, per = (64, 96, 32), (True, False, True)
+    a = G.Grid(shape, per, (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), precision="auto")
+    b = G.Grid(shape, per, (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), precision="auto")
+    assert not a.plan_from_cache and b.plan_from_cache
+    assert a.sweep_plan() == b.sweep_plan()
+    v = to_dev(_smooth(shape, 3), torch)
+    for d in range(3):
+        assert torch.equal(a.d1(d, v), b.d1(d, v))
+        assert torch.equal(a.filter("spectral", v, d), b.filter("spectral", v, d))
+        assert torch.equal(a.d8(d, v), b.d8(d, v))
