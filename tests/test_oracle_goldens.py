@@ -133,3 +133,43 @@ def test_euler_rz_profile(oracle):
     path = os.path.join(GOLDEN_DIR, "euler-RZ-128.dat")
     assert numpy.abs(x - numpy.loadtxt(path)[0]).max() < 1e-12
     assert scripts.profile_error(path, x, p) < 1e-10
+
+
+def test_symmetry_plane_closures_known_answers(oracle):
+    """SYMM ends (stencils.f90:2390-2453): with a symmetry plane half a
+    spacing below the first point, the folded closures of a symmetric field
+    cos(k (x - xs)) (xs the plane) give its derivative -k sin(k (x - xs)) to
+    the interior scheme's accuracy at the end rows too, and the antisymmetric
+    variant does the same for sin(k (x - xs)); the one-sided closures of the
+    same grid are far less accurate at the ends."""
+    n = 64
+    dx = 1.0 / n
+    x1, xn = 0.5 * dx, 1.0 - 0.5 * dx   # nodes at (i + 1/2) dx: the plane at x = 0
+    k = 2.0 * numpy.pi * 1.5
+    for sym, f, fp in ((1, numpy.cos, lambda t: -k * numpy.sin(k * t)), (-1, numpy.sin, lambda t: k * numpy.cos(k * t))):
+        g = oracle.OracleGrid((n, 1, 1), (False, False, False), (x1, 0, 0), (xn, 0, 0),
+                              bc=(("SYMM", "NONE"), ("NONE", "NONE"), ("NONE", "NONE")))
+        x = g.mesh(0)
+        v = f(k * x)
+        d = g.apply_sym(0, 0, sym, v)
+        err_end = numpy.abs(d[:6, 0, 0] - fp(x[:6, 0, 0])).max() / k
+        assert err_end < 1e-7, (sym, err_end)
+    # the one-sided rows at the same end, for comparison
+    g1 = oracle.OracleGrid((n, 1, 1), (False, False, False), (x1, 0, 0), (xn, 0, 0))
+    x = g1.mesh(0)
+    e1 = numpy.abs(g1.apply(0, 0, numpy.cos(k * x))[:6, 0, 0] + k * numpy.sin(k * x[:6, 0, 0])).max() / k
+    assert e1 > 1e-6
+
+
+def test_cylindrical_divergence_known_answers(oracle):
+    """Cylindrical div (operators.f90:55-64): div(r e_r) = 2 and
+    div(r^2 e_r) = 3 r exactly up to the compact derivative's error on a
+    polynomial, and the angular and axial terms of a field that does not vary
+    in angle or along the axis vanish."""
+    n = (48, 1, 16)
+    g = oracle.OracleGrid(n, (False, True, True), (0.5, 0.0, 0.0), (1.5, 0.0, 1.0), coordsys=1,
+                          bc=(("NONE", "NONE"), ("NONE", "NONE"), ("NONE", "NONE")))
+    r = g.mesh(0)
+    zero = numpy.zeros(n)
+    assert numpy.abs(g.div(r, zero, zero) - 2.0).max() < 1e-10
+    assert numpy.abs(g.div(r * r, zero, zero) - 3.0 * r).max() < 1e-9
