@@ -131,8 +131,9 @@ ddt(:Et:)   =  -ddx( (:Et: + :p: - :tau:)*:u: )
 """
 
 
-def shu_osher_run(Sim, Npts, packages, **kw):
-    """getShu of examples/shu_osher.py: returns (x, rho) at t = 1.8."""
+def shu_osher_run(Sim, Npts, packages, graphs=False, **kw):
+    """getShu of examples/shu_osher.py: returns (x, rho) at t = 1.8 (graphs: each
+    RK step replayed from a CUDA graph, bit-identical to eager)."""
     L = 10.0
     Lp = L * (Npts - 1.0) / Npts
     imesh = "xdom = (-Lp/2.0, Lp/2.0, Npts)".replace("Lp", str(Lp)).replace("Npts", str(Npts))
@@ -164,6 +165,8 @@ eps = 2.0e-1
 :Et:  = :p:/(:gamma: -1.0) + .5*:rho:*:u:*:u:
 """
     ss.setIC(ic % ss.dx)
+    if graphs:
+        ss.use_graphs(True)
     time = 0.0
     CFL = 0.5
     dt = _f(ss.variables["dt"].data) * CFL * .01
@@ -191,11 +194,11 @@ def _host(a):
     return numpy.asarray(a)
 
 
-def shu_osher(Sim, packages, **kw):
+def shu_osher(Sim, packages, graphs=False, **kw):
     """examples/shu_osher.py 1: average convergence rate of rho(1.85) over N = 100..800."""
     sol = []
     for n in (100, 200, 400, 800):
-        x, rho = shu_osher_run(Sim, n, packages, **kw)
+        x, rho = shu_osher_run(Sim, n, packages, graphs=graphs, **kw)
         sol.append(numpy.interp(1.85, x, rho))
     sol = numpy.array(sol)
     diff = numpy.abs(sol[1:] - sol[:-1])

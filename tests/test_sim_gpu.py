@@ -57,8 +57,11 @@ def test_taylor_green_golden():
 
 
 def test_shu_osher_golden():
+    """tests/cases/testShuOsher.py shu-osher-CR, with every RK step replayed
+    from a CUDA graph (bit-identical to eager, test_graph_replay_matches_eager):
+    graph capture with the boundary-condition lines of the EOM."""
     from pyranda_gb300 import pyrandaSim
-    cr = scripts.shu_osher(pyrandaSim, _bc_ts, silent=True)
+    cr = scripts.shu_osher(pyrandaSim, _bc_ts, graphs=True, silent=True)
     assert _close(cr, "shu-osher-CR") < 1e-8
 
 
