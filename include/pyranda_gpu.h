@@ -64,18 +64,32 @@ typedef enum { PG_SPECTRAL = 0, PG_GAUSSIAN = 1 } pg_filter_kind;
 
 enum { PG_DIR_X = 0, PG_DIR_Y = 1, PG_DIR_Z = 2, PG_DIR_ALL = 3 };
 
-/* Mesh quantities for pg_mesh (parcop.f90:84-191). */
+/* Mesh quantities for pg_mesh (parcop.f90:84-191; mesh.f90:35-50).  The
+ * coordinates are the native ones (radius, angle, ... on cylindrical and
+ * spherical grids).  CELLVOL_S / _G are the filtered cell volumes that divide
+ * a filtered volume-weighted field (CellVol itself on Cartesian, cylindrical
+ * and ratio-zoned spherical grids); DET and the inverse Jacobian rows
+ * DA_DX .. DC_DZ exist on curvilinear grids only (getVar 'dtJ', 'dAx' ..). */
 typedef enum {
   PG_MESH_X = 0, PG_MESH_Y = 1, PG_MESH_Z = 2,
   PG_MESH_D1 = 3, PG_MESH_D2 = 4, PG_MESH_D3 = 5,
-  PG_MESH_GRIDLEN = 6, PG_MESH_CELLVOL = 7
+  PG_MESH_GRIDLEN = 6, PG_MESH_CELLVOL = 7,
+  PG_MESH_CELLVOL_S = 8, PG_MESH_CELLVOL_G = 9, PG_MESH_DET = 10,
+  PG_MESH_DA_DX = 11, PG_MESH_DA_DY = 12, PG_MESH_DA_DZ = 13,
+  PG_MESH_DB_DX = 14, PG_MESH_DB_DY = 15, PG_MESH_DB_DZ = 16,
+  PG_MESH_DC_DX = 17, PG_MESH_DC_DY = 18, PG_MESH_DC_DZ = 19
 } pg_mesh_var;
 
 /* Boundary codes of a non-periodic end (pyrandaMPI.py:101-131,
  * compact.f90:77-91). */
 typedef enum { PG_BC_NONE = 0, PG_BC_SYMM = 1, PG_BC_XTND = 2 } pg_bc;
-/* Coordinate systems (patch.f90 coordsys; mesh.f90:190-243). */
-typedef enum { PG_CARTESIAN = 0, PG_CYLINDRICAL = 1 } pg_coordsys;
+/* Coordinate systems (patch.f90 coordsys; mesh.f90:169-386): cylindrical
+ * (x = radius, y = angle, z = axis), spherical (x = radius, y = polar angle,
+ * z = azimuth; RATIO zones the radius by a constant ratio, mesh.f90:180-186),
+ * and general curvilinear (coordinates supplied by pg_set_mesh_coords). */
+typedef enum {
+  PG_CARTESIAN = 0, PG_CYLINDRICAL = 1, PG_SPHERICAL = 2, PG_CURVILINEAR = 3, PG_SPHERICAL_RATIO = 4
+} pg_coordsys;
 
 typedef struct {
   int n[3];        /* nx, ny, nz (global = local: one GPU) */
@@ -90,7 +104,7 @@ typedef struct {
                     * variants through the *_sym calls); XTND = the
                     * extended-data rows (the compact filter, whose reference
                     * rows are unset, keeps its one-sided rows there) */
-  int coordsys;    /* pg_coordsys; cylindrical: x = radius, y = angle, z = axis */
+  int coordsys;    /* pg_coordsys */
 } pg_grid;
 
 typedef struct pg_handle pg_handle;
@@ -156,14 +170,19 @@ int pg_d2(pg_handle* h, int dir, const double* in, double* out, void* stream);
  * lines the three one-sided rows of each end close the stencil (the
  * reference declares a fourth row it never sets). */
 int pg_d4(pg_handle* h, int dir, const double* in, double* out, void* stream);
-/* plaplacian (parcop.f90:303-311 -> operators.f90:513-526, Cartesian):
- * d2x + d2y + d2z; a direction of fewer than 4 points contributes 0.  out
- * must differ from in. */
+/* plaplacian (parcop.f90:303-311 -> operators.f90:513-559): Cartesian
+ * d2x + d2y + d2z (a direction of fewer than 4 points contributes 0);
+ * cylindrical d(r df/dr)/dr / r + d2y / r^2 + d2z; spherical (coordsys 2)
+ * d(r^2 df/dr)/dr / r^2 + d(sin(theta) df/dtheta)/dtheta / (r^2 sin(theta))
+ * + d2z / (r sin(theta))^2.  The reference has no Laplacian on curvilinear
+ * and ratio-zoned spherical grids: PG_EINVAL.  out must differ from in. */
 int pg_laplacian(pg_handle* h, const double* in, double* out, void* stream);
 /* sFilter / gFilter / gFilterDir (parcop.f90:337-368 -> operators.f90:755-896).
  * dir = PG_DIR_ALL gives the x->y->z sweep sequence of `filter`; on a
- * cylindrical grid the spectral filter acts on the field times the cell
- * volume and divides by it (operators.f90:876-883; out must differ from in). */
+ * non-Cartesian grid the spectral filter acts on the field times the cell
+ * volume and divides by the cell volume (cylindrical, :876-883) or by the
+ * filtered cell volume (spherical and curvilinear, :884-889); out must differ
+ * from in there. */
 int pg_filter(pg_handle* h, int kind, int dir, const double* in, double* out, void* stream);
 /* The operators of a direction with a symmetry plane come in two variants
  * (compact.f90:80-85): sym = +1 for fields symmetric about the plane (what
@@ -175,30 +194,45 @@ int pg_filter(pg_handle* h, int kind, int dir, const double* in, double* out, vo
 int pg_d1_sym(pg_handle* h, int dir, int sym, const double* in, double* out, void* stream);
 int pg_d8_sym(pg_handle* h, int dir, int sym, const double* in, double* out, void* stream);
 int pg_filter_sym(pg_handle* h, int kind, int dir, const int* sym, const double* in, double* out, void* stream);
-/* pRing (parcop.f90:313-322 -> operators.f90:615-643 with L = 2). */
+/* pRing (parcop.f90:313-322 -> operators.f90:615-643 with L = 2); the
+ * scales d1 d2 d3 are the mesh fields on non-Cartesian grids (d2 = r dy on
+ * cylindrical ones). */
 int pg_ring(pg_handle* h, const double* in, double* out, void* stream);
 /* pRingV (parcop.f90:324-333 -> operators.f90:645-699 with L = 1). */
 int pg_ringv(pg_handle* h, const double* vx, const double* vy, const double* vz, double* out,
              void* stream);
 /* gradS (parcop.f90:371-379 -> operators.f90:184-212); cylindrical grids
- * divide the angular component by the radius. */
+ * divide the angular component by the radius, spherical grids the angular
+ * ones by r and r sin(theta), curvilinear grids apply the inverse Jacobian. */
 int pg_grad(pg_handle* h, const double* in, double* gx, double* gy, double* gz, void* stream);
 /* divergence (parcop.f90:202-211 -> operators.f90:38-64): on a direction with
  * a symmetry plane the component along it is taken as antisymmetric
  * (isym = -1, patch.f90:89-91); cylindrical grids take (d(r fx)/dr +
- * dfy/dtheta) / r + dfz/dz.  Cylindrical grids use three workspace fields of
- * the handle. */
+ * dfy/dtheta) / r + dfz/dz, spherical and curvilinear grids the forms of
+ * operators.f90:64-90.  Non-Cartesian grids use workspace fields of the
+ * handle. */
 int pg_div(pg_handle* h, const double* fx, const double* fy, const double* fz, double* out,
            void* stream);
 /* divergenceTensor (parcop.f90:213-224 -> operators.f90:97-146): f holds the
  * nine device fields fxx, fxy, fxz, fyx, fyy, fyz, fzx, fzy, fzz; out the
- * three results dfx, dfy, dfz (distinct from f).  Cartesian and cylindrical;
- * the symmetry multipliers isym^p of the reference select each derivative's
+ * three results dfx, dfy, dfz (distinct from f).  Every coordinate system
+ * (curvilinear: the divergence of each row, operators.f90:174-177); the
+ * symmetry multipliers isym^p of the reference select each derivative's
  * variant on directions with a symmetry plane. */
 int pg_divt(pg_handle* h, const double* const* f, double* const* out, void* stream);
-/* xGrid/yGrid/zGrid/dxGrid/.../mesh_getGridLen/mesh_getCellVol
- * (parcop.f90:130-191 -> mesh.f90:169-225, Cartesian and cylindrical). */
+/* xGrid/yGrid/zGrid/dxGrid/.../mesh_getGridLen/mesh_getCellVol and getVar
+ * (parcop.f90:84-191 -> mesh.f90:169-386); which is a pg_mesh_var. */
 int pg_mesh(pg_handle* h, int which, double* out, void* stream);
+/* setup_mesh_x3 (parcop.f90:73-81 -> mesh.f90:163-168, :245-386): the
+ * coordinates of a curvilinear grid (device fields), the Jacobian by the
+ * first-derivative operator -- a non-periodic one with one-sided ends when
+ * mesh_periodic is set (pyranda's 'periodicGrid' option, mesh.f90:246-307),
+ * else the grid's own -- its determinant and inverse, d1 d2 d3, CellVol,
+ * GridLen and the filtered cell volumes.  A curvilinear handle starts from
+ * the node coordinates x1 + i (xn - x1) / (n - 1) (pyrandaMesh.py:96-108)
+ * with mesh_periodic set.  Allocates and synchronises (setup, not a step). */
+int pg_set_mesh_coords(pg_handle* h, const double* x, const double* y, const double* z, int mesh_periodic,
+                       void* stream);
 
 /* One stage of the LSRK(5,4) update of pyranda.py:797-804 for nvar conserved
  * fields, fused:  PHI = A*PHI + dt*F ;  U = U + B*PHI.
@@ -207,13 +241,19 @@ int pg_mesh(pg_handle* h, int which, double* out, void* stream);
 int pg_rk_stage(pg_handle* h, int nvar, double* const* U, double* const* PHI,
                 const double* const* F, const double* dt, double A, double B, void* stream);
 
-/* pyrandaTimestep.courant (pyranda/pyrandaTimestep.py:42-67, Cartesian):
- * out[0] = 1 / max(|u|/d1 + |v|/d2 + |w|/d3 + |c|/GridLen).  v or w may be
- * NULL, meaning the constant vconst/wconst (scripts pass 0.0). */
+/* pyrandaTimestep.courant (pyranda/pyrandaTimestep.py:42-67):
+ * out[0] = 1 / max(|u|/d1 + |v|/d2 + |w|/d3 + |c|/GridLen), with the mesh
+ * fields d1 d2 d3 GridLen on spherical and curvilinear grids; curvilinear
+ * grids take the speeds along the A and B grid lines,
+ * |u dA/dx + v dA/dy| / |grad A| / d1 + |u dB/dx + v dB/dy| / |grad B| / d2
+ * (:45-56).  v or w may be NULL, meaning the constant vconst/wconst (scripts
+ * pass 0.0).  Cylindrical grids with more than one point in angle return
+ * PG_EINVAL. */
 int pg_courant(pg_handle* h, const double* u, const double* v, const double* w, const double* c,
                double vconst, double wconst, double* out, void* stream);
 /* pyrandaTimestep.diff (pyranda/pyrandaTimestep.py:71-77):
- * out[0] = min(rho * GridLen^2 / max(1e-12, bulk)). */
+ * out[0] = min(rho * GridLen^2 / max(1e-12, bulk)) (GridLen the mesh field on
+ * spherical and curvilinear grids). */
 int pg_diff(pg_handle* h, const double* bulk, const double* rho, double* out, void* stream);
 /* Global reductions (pyrandaMPI.py:307-326 sum3D/max3D/min3D on one GPU):
  * op 0 = sum, 1 = max, 2 = min over n values; out is a device scalar. */

@@ -56,6 +56,7 @@ def lib():
         L.og_div.argtypes = [P, D, D, D, D]
         L.og_divt.argtypes = [P, ctypes.POINTER(D), ctypes.POINTER(D)]
         L.og_mesh.argtypes = [P, ctypes.c_int, D]
+        L.og_set_mesh_x3.argtypes = [P, D, D, D, ctypes.c_int]
         L.og_spacing.argtypes = [P, D, D]
         L.og_dense.argtypes = [P, ctypes.c_int, ctypes.c_int, D]
         L.og_threads.restype = ctypes.c_int
@@ -81,7 +82,8 @@ class OracleGrid:
 
     def __init__(self, n, periodic, x1, xn, bc=None, coordsys=0):
         """bc: per direction (lower, upper) end codes 'NONE' / 'SYMM' / 'XTND' (non-periodic
-        directions); coordsys 0 Cartesian, 1 cylindrical."""
+        directions); coordsys 0 Cartesian, 1 cylindrical, 2 spherical, 3 curvilinear
+        (coordinates by ``set_mesh_x3``), 4 spherical with ratio-zoned radii."""
         L = lib()
         n = (ctypes.c_int * 3)(*[int(v) for v in n])
         per = (ctypes.c_int * 3)(*[1 if p else 0 for p in periodic])
@@ -150,7 +152,8 @@ class OracleGrid:
     def laplacian(self, v):
         v = _f64(v)
         out = self._out()
-        lib().og_laplacian(self.h, _dp(v), _dp(out))
+        if lib().og_laplacian(self.h, _dp(v), _dp(out)) != 0:
+            raise ValueError("oracle: the reference's Laplacian has no branch for coordsys %d" % self.coordsys)
         return out
 
     def sfilter(self, v):
@@ -205,9 +208,18 @@ class OracleGrid:
         return outs
 
     def mesh(self, which):
+        """0-2 coordinates, 3-5 d1 d2 d3, 6 GridLen, 7 CellVol, 8-9 CellVolS/G,
+        10 det J, 11-19 the inverse Jacobian dA/dx .. dC/dz (curvilinear)."""
         out = self._out()
-        lib().og_mesh(self.h, which, _dp(out))
+        if lib().og_mesh(self.h, which, _dp(out)) != 0:
+            raise ValueError("oracle: mesh quantity %d is not defined on this grid" % which)
         return out
+
+    def set_mesh_x3(self, x, y, z, mesh_periodic=True):
+        """setup_mesh_x3 (parcop.f90:73-81): the coordinates of a curvilinear grid."""
+        x, y, z = _f64(x), _f64(y), _f64(z)
+        if lib().og_set_mesh_x3(self.h, _dp(x), _dp(y), _dp(z), 1 if mesh_periodic else 0) != 0:
+            raise ValueError("oracle: set_mesh_x3 needs a curvilinear grid")
 
     def spacing(self):
         pd = (ctypes.c_double * 3)()
@@ -302,7 +314,7 @@ class _Eq:
 
 
 class _Timestep:
-    """pyrandaTimestep.py:42-77 (Cartesian)"""
+    """pyrandaTimestep.py:42-77"""
 
     name = "Timestep"
 
@@ -314,7 +326,15 @@ class _Timestep:
 
     def courant(self, u, v, w, c):
         s = self.sim
-        vrate = numpy.abs(u) / s.d1 + numpy.abs(v) / s.d2 + numpy.abs(w) / s.d3
+        if s.coordsys == 3:  # pyrandaTimestep.py:45-56: speeds along the A and B grid lines
+            dAdx, dAdy, dBdx, dBdy = s.getVar("dAx"), s.getVar("dAy"), s.getVar("dBx"), s.getVar("dBy")
+            magA = numpy.sqrt(dAdx * dAdx + dAdy * dAdy)
+            magB = numpy.sqrt(dBdx * dBdx + dBdy * dBdy)
+            uA = (u * dAdx + v * dAdy) / magA
+            uB = (u * dBdx + v * dBdy) / magB
+            vrate = numpy.abs(uA) / s.d1 + numpy.abs(uB) / s.d2
+        else:
+            vrate = numpy.abs(u) / s.d1 + numpy.abs(v) / s.d2 + numpy.abs(w) / s.d3
         crate = numpy.abs(c) / s.GridLen
         return 1.0 / numpy.max(vrate + crate)
 
@@ -332,10 +352,10 @@ class _BC:
     """pyrandaBC.py on one rank: extrap / const (:58-160), field (:162-187),
     slip (:190-465), exit (:468-521), farfield (:524-745), symm (:748-788).
     A boundary is owned when its direction is non-periodic and has more than
-    one point.  slip and farfield use the normal of a Cartesian mesh: the
-    cross product of the metric rows (:233-264) with d(x,y,z)/d(A,B,C) =
-    diag(dx, dy, dz), i.e. +x on the x ends, -y on the y ends, +z on the z
-    ends."""
+    one point.  slip and farfield take the boundary normal from the cross
+    product of the metric rows (:198-264): on curvilinear grids from the
+    inverse Jacobian; on the others d(x,y,z)/d(A,B,C) = diag(dx, dy, dz)
+    gives +x on the x ends, -y on the y ends, +z on the z ends."""
 
     name = "BC"
     NORMAL = {"x": (1.0, 0.0, 0.0), "y": (0.0, -1.0, 0.0), "z": (0.0, 0.0, 1.0)}
@@ -404,33 +424,69 @@ class _BC:
                     a[self._slice(d, slice(src, src + npts))], axis=ax) * m
 
     def slipbc(self, var, direction):
-        velocity = var if isinstance(var, list) else [var]
+        """pyrandaBC.py:190-196: each entry of var is one velocity (a list of its
+        component names; a single name is a one-component velocity)."""
         for d in (direction if isinstance(direction, list) else [direction]):
-            if d[0] == "z":
-                continue
-            self.extrap(velocity, d, 2)
-            if not self._owns(d):
-                continue
-            k = 0 if d[1] == "1" else -1
-            nrm = self.NORMAL[d[0]]
-            planes = [self.sim.variables[v].data[self._slice(d, k)].copy() for v in velocity]
-            udotn = 0.0
-            for q, u in enumerate(planes):
-                udotn = udotn + u * nrm[q]
-            mag0 = 0.0
-            for u in planes:
-                mag0 += u ** 2
-            mag0 = numpy.sqrt(mag0)
-            new = [u - udotn * nrm[q] for q, u in enumerate(planes)]
-            magf = 0.0
-            for u in new:
-                magf += u ** 2
-            magf = numpy.sqrt(magf)
-            for v, u in zip(velocity, new):
-                self.sim.variables[v].data[self._slice(d, k)] = numpy.where(magf > mag0, u * mag0 / magf, u)
+            for v in (var if isinstance(var, list) else [var]):
+                self._slip(v if isinstance(v, list) else [v], d)
+
+    def _slip(self, velocity, d):
+        if d[0] == "z":
+            return
+        self.extrap(velocity, d, 2)
+        if not self._owns(d):
+            return
+        k = 0 if d[1] == "1" else -1
+        nrm = self.normal(d, k)
+        planes = [self.sim.variables[v].data[self._slice(d, k)].copy() for v in velocity]
+        udotn = 0.0
+        for q, u in enumerate(planes):
+            udotn = udotn + u * nrm[q]
+        mag0 = 0.0
+        for u in planes:
+            mag0 += u ** 2
+        mag0 = numpy.sqrt(mag0)
+        new = [u - udotn * nrm[q] for q, u in enumerate(planes)]
+        magf = 0.0
+        for u in new:
+            magf += u ** 2
+        magf = numpy.sqrt(magf)
+        for v, u in zip(velocity, new):
+            self.sim.variables[v].data[self._slice(d, k)] = numpy.where(magf > mag0, u * mag0 / magf, u)
+
+    def normal(self, d, k):
+        """The unit normal (n1, n2, n3) on plane k of boundary d (pyrandaBC.py:233-264):
+        the cross product of the metric rows d(x,y,z)/d(.) of the two tangential grid
+        directions, the metric rows rebuilt from the inverse Jacobian and det J (:198-231)."""
+        if self.sim.coordsys != 3:
+            return self.NORMAL[d[0]]
+        key = "normal-%s" % d
+        if key not in self.BCdata:
+            g = self.sim.getVar
+            dAdx, dAdy, dAdz = g("dAx"), g("dAy"), g("dAz")
+            dBdx, dBdy, dBdz = g("dBx"), g("dBy"), g("dBz")
+            dCdx, dCdy, dCdz = g("dCx"), g("dCy"), g("dCz")
+            detJ = g("dtJ")
+            m = {"xA": (-dBdz * dCdy + dBdy * dCdz) * detJ, "xB": (dAdz * dCdy - dAdy * dCdz) * detJ,
+                 "xC": (-dAdz * dBdy + dAdy * dBdz) * detJ, "yA": (dBdz * dCdx - dBdx * dCdz) * detJ,
+                 "yB": (-dAdz * dCdx + dAdx * dCdz) * detJ, "yC": (dAdz * dBdx - dAdx * dBdz) * detJ,
+                 "zA": (-dBdy * dCdx + dBdx * dCdy) * detJ, "zB": (dAdy * dCdx - dAdx * dCdy) * detJ,
+                 "zC": (-dAdy * dBdx + dAdx * dBdy) * detJ}
+            t1, t2 = {"x": ("B", "C"), "y": ("A", "C"), "z": ("A", "B")}[d[0]]
+            a1, a2, a3 = m["x" + t1], m["y" + t1], m["z" + t1]
+            b1, b2, b3 = m["x" + t2], m["y" + t2], m["z" + t2]
+            n1 = (a2 * b3 - a3 * b2)
+            n2 = -(a1 * b3 - a3 * b1)
+            n3 = (a1 * b2 - a2 * b1)
+            mag = numpy.sqrt(n1 * n1 + n2 * n2 + n3 * n3)
+            n1 /= mag
+            n2 /= mag
+            n3 /= mag
+            self.BCdata[key] = [a[self._slice(d, k)] for a in (n1, n2, n3)]
+        return self.BCdata[key]
 
     def Reimann(self, d, Rhoref, Uref, Vref, Wref, Pref, gamma, rhoi, Ui, Vi, Wi, Pi):
-        nx, ny, nz = self.NORMAL[d[0]]
+        nx, ny, nz = self.normal(d, 0 if d[1] == "1" else -1)
         Vni = Ui * nx + Vi * ny + Wi * nz
         Vno = Uref * nx + Vref * ny + Wref * nz
         SSo = numpy.sqrt(gamma * Pref / Rhoref)
@@ -543,11 +599,25 @@ class OracleSim:
         # pyrandaMPI.py:101-131: symmetric ends of non-periodic directions are SYMM
         sym = opts.get("symmetric", [[False, False]] * 3)
         bc = [["SYMM" if (sym[d][e] and not opts["periodic"][d]) else "NONE" for e in range(2)] for d in range(3)]
+        self.coordsys = int(opts.get("coordsys", 0))
         self.grid = OracleGrid(self.shape, opts["periodic"], opts["x1"], opts["xn"], bc=bc,
-                               coordsys=int(opts.get("coordsys", 0)))
-        self.meshx = self.grid.mesh(0)
-        self.meshy = self.grid.mesh(1)
-        self.meshz = self.grid.mesh(2)
+                               coordsys=self.coordsys)
+        if self.coordsys == 3:
+            self.grid.set_mesh_x3(*self._curvilinear_coords(opts), mesh_periodic=opts.get("periodicGrid", True))
+        # pyrandaMesh.py:143-191: the mesh coordinates in x-y-z space; the native
+        # (r, theta, z) or (r, theta, phi) ones are kept beside them
+        x, y, z = self.grid.mesh(0), self.grid.mesh(1), self.grid.mesh(2)
+        self.coordsNative = None
+        if self.coordsys in (1, 2, 4):
+            self.coordsNative = [x, y, z]
+            if self.coordsys == 1:
+                x, y = x * numpy.cos(y), x * numpy.sin(y)
+            else:
+                r, th, phi = x, y, z
+                x = r * numpy.sin(th) * numpy.cos(phi)
+                y = r * numpy.sin(th) * numpy.sin(phi)
+                z = r * numpy.cos(th)
+        self.meshx, self.meshy, self.meshz = x, y, z
         self.d1 = self.grid.mesh(3)
         self.d2 = self.grid.mesh(4)
         self.d3 = self.grid.mesh(5)
@@ -562,6 +632,26 @@ class OracleSim:
         self.deltat = 0.0
         self.cycle = 0
         self._smap()
+
+    def _curvilinear_coords(self, opts):
+        """pyrandaMesh.py:92-131: node coordinates numpy.linspace(x1, xn, nn) per
+        direction, replaced point by point by opts['function'](i, j, k) when given."""
+        lin = [numpy.linspace(opts["x1"][d], opts["xn"][d], num=self.shape[d]) for d in range(3)]
+        x, y, z = [numpy.asfortranarray(a) for a in numpy.meshgrid(*lin, indexing="ij")]
+        fn = opts.get("function")
+        if fn:
+            for i in range(self.nx):
+                for j in range(self.ny):
+                    for k in range(self.nz):
+                        x[i, j, k], y[i, j, k], z[i, j, k] = fn(i, j, k)
+        return x, y, z
+
+    # pyrandaMPI.py:657-661 / parcop.f90:84-128
+    _VARS = {"x": 0, "y": 1, "z": 2, "d1": 3, "d2": 4, "d3": 5, "dtJ": 10, "dAx": 11, "dAy": 12, "dAz": 13,
+             "dBx": 14, "dBy": 15, "dBz": 16, "dCx": 17, "dCy": 18, "dCz": 19}
+
+    def getVar(self, name):
+        return self.grid.mesh(self._VARS[name])
 
     # pyranda.py:812-869
     def _smap(self):
@@ -608,6 +698,7 @@ class OracleSim:
         s["meshx"] = "self.meshx"
         s["meshy"] = "self.meshy"
         s["meshz"] = "self.meshz"
+        s["meshVar("] = "self.getVar("
         self.sMap = s
 
     def addPackage(self, kind):

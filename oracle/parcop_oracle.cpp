@@ -12,7 +12,8 @@
 // Scope: np = 1 (no MPI decomposition); boundary codes PERI (periodic), NONE
 // (one-sided closures, mbc = 0), SYMM (symmetry planes, mbc = +-1, both
 // operator variants) and XTND (extended-data rows, mbc = 2, without supplied
-// data); Cartesian and cylindrical coordinates.
+// data); Cartesian, cylindrical, spherical (with and without ratio zoning in
+// the radius) and general curvilinear coordinates (mesh.f90:169-386).
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -694,6 +695,11 @@ void eval_line(const Op1& o, const double* v, double* dv, double scale) {
 // ---------------------------------------------------------------------------
 // Handle: one grid (one pyranda patch), all operators for x, y, z.
 // ---------------------------------------------------------------------------
+// Mesh fields of spherical and curvilinear grids (mesh.f90:35-50): coordinates,
+// d1 d2 d3, GridLen, CellVol, the filtered cell volumes, det J and the inverse
+// Jacobian rows dA/dx dA/dy dA/dz, dB/.., dC/.. (curvilinear only).
+enum { MF_X, MF_Y, MF_Z, MF_D1, MF_D2, MF_D3, MF_GL, MF_CV, MF_CVS, MF_CVG, MF_DET, MF_J0, MF_COUNT = MF_J0 + 9 };
+
 struct og_handle {
   int n[3];
   int periodic[3];
@@ -702,9 +708,10 @@ struct og_handle {
   double x1f[3];   // lower face coordinates (parcop.f90:51-56)
   int bc[3][2];    // 0 NONE, 1 SYMM, 2 XTND per end (pyrandaMPI.py:101-131)
   int symm[3];     // isym = -1 where a direction has a SYMM end (patch.f90:89-91)
-  int coordsys;    // 0 Cartesian, 1 cylindrical
+  int coordsys;    // 0 Cartesian, 1 cylindrical, 2 spherical, 3 curvilinear, 4 spherical ratio-zoned
   Op1 d1[3], d8[3], sf[3], gf[3], d2[3], d4[3];
   Op1 anti[6][3];  // operator n = 2 of a SYMM direction (mbc = -1, compact.f90:80-85)
+  std::vector<double> mf[MF_COUNT];  // coordsys 2, 3, 4
 };
 
 namespace {
@@ -726,10 +733,9 @@ const Op1& pick(const og_handle* h, int op, int dir, int sym = 1) {
 // Apply one operator along direction dir over a Fortran-ordered (nx,ny,nz) field.
 // Null ops follow compact_operators.f90: derivatives give 0 (:24-29, :288-294),
 // filters copy (:396-401).
-void apply_dir(const og_handle* h, int op, int dir, const double* in, double* out, int sym = 1) {
+void apply_op(const og_handle* h, const Op1& o, int op, int dir, const double* in, double* out) {
   const int nx = h->n[0], ny = h->n[1], nz = h->n[2];
   const size_t npts = (size_t)nx * ny * nz;
-  const Op1& o = pick(h, op, dir, sym);
   if (o.null_op) {
     if (op == OP_SF || op == OP_GF) std::memcpy(out, in, npts * sizeof(double));
     else std::memset(out, 0, npts * sizeof(double));
@@ -766,6 +772,10 @@ void apply_dir(const og_handle* h, int op, int dir, const double* in, double* ou
   }
 }
 
+void apply_dir(const og_handle* h, int op, int dir, const double* in, double* out, int sym = 1) {
+  apply_op(h, pick(h, op, dir, sym), op, dir, in, out);
+}
+
 }  // namespace
 
 namespace {
@@ -781,6 +791,157 @@ double cellvol_cyl(const og_handle* h, size_t p) {
   return h->d[0] * (r * h->d[1]) * h->d[2];
 }
 int isym_pow(const og_handle* h, int d, int p) { return (h->symm[d] && (p & 1)) ? -1 : 1; }
+
+size_t npts_of(const og_handle* h) { return (size_t)h->n[0] * h->n[1] * h->n[2]; }
+
+// mesh d1, d2, d3 at point p (the ring scales, mesh.f90:192-358): constants on
+// Cartesian grids, d2 = r dy on cylindrical grids, fields otherwise
+double mesh_d(const og_handle* h, int dir, size_t p) {
+  if (h->coordsys == 0) return h->dmesh[dir];
+  if (h->coordsys == 1) return dir == 1 ? xgrid(h, p) * h->d[1] : h->d[dir];
+  return h->mf[MF_D1 + dir][p];
+}
+
+// mesh.f90:373-386: the filtered cell volumes that divide a filtered
+// volume-weighted field (spherical and curvilinear grids; CellVol otherwise)
+void cell_bar(og_handle* h) {
+  const size_t np = npts_of(h);
+  h->mf[MF_CVS].assign(np, 0.0);
+  h->mf[MF_CVG].assign(np, 0.0);
+  if (h->coordsys == 2 || h->coordsys == 3) {
+    std::vector<double> tmp(np);
+    apply_dir(h, OP_SF, 0, h->mf[MF_CV].data(), h->mf[MF_CVS].data());
+    apply_dir(h, OP_SF, 1, h->mf[MF_CVS].data(), tmp.data());
+    apply_dir(h, OP_SF, 2, tmp.data(), h->mf[MF_CVS].data());
+    apply_dir(h, OP_GF, 0, h->mf[MF_CV].data(), h->mf[MF_CVG].data());
+    apply_dir(h, OP_GF, 1, h->mf[MF_CVG].data(), tmp.data());
+    apply_dir(h, OP_GF, 2, tmp.data(), h->mf[MF_CVG].data());
+  } else {
+    h->mf[MF_CVS] = h->mf[MF_CV];
+    h->mf[MF_CVG] = h->mf[MF_CV];
+  }
+}
+
+// Spherical grids, x = radius, y = theta, z = phi (mesh.f90:169-186, :227-244);
+// coordsys 4 zones the radius by a constant ratio (:180-186, :231)
+void sph_mesh(og_handle* h) {
+  const int nx = h->n[0], ny = h->n[1], nz = h->n[2];
+  const size_t np = npts_of(h);
+  for (int q = MF_X; q <= MF_CV; q++) h->mf[q].assign(np, 0.0);
+  const double pi = std::acos(-1.0), dx = h->d[0], dy = h->d[1], dz = h->d[2];
+  double Csp = 0.0, Asp = 0.0;
+  if (h->coordsys == 4) {
+    Csp = std::log((double)(nx - 1) * dx) / (dy * (double)(nx - 1));
+    Asp = (h->x1f[0] + dx / 2.0) / std::exp(Csp * dy);
+  }
+  for (int k = 0; k < nz; k++)
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++) {
+        const size_t p = ((size_t)k * ny + j) * nx + i;
+        double r = h->x1f[0] + (double)(2 * (i + 1) - 1) * 0.5 * dx;
+        const double th = h->x1f[1] + (double)(2 * (j + 1) - 1) * 0.5 * dy;
+        const double ph = h->x1f[2] + (double)(2 * (k + 1) - 1) * 0.5 * dz;
+        if (h->coordsys == 4) r = Asp * std::exp(Csp * dy * (double)(i + 1));
+        double d1 = dx;
+        const double d2 = r * dy, d3 = r * std::sin(th) * dz;
+        if (h->coordsys == 4) d1 = Csp * r * dy;
+        double cv = d1 * d2 * d3, gl = std::min(std::min(d1, d2), d3);
+        if (ny == 1 && nz == 1) {
+          cv = d1 * 4.0 * pi * (r * r);
+          gl = d1;
+        }
+        h->mf[MF_X][p] = r;
+        h->mf[MF_Y][p] = th;
+        h->mf[MF_Z][p] = ph;
+        h->mf[MF_D1][p] = d1;
+        h->mf[MF_D2][p] = d2;
+        h->mf[MF_D3][p] = d3;
+        h->mf[MF_GL][p] = gl;
+        h->mf[MF_CV][p] = cv;
+      }
+  cell_bar(h);
+}
+
+// General curvilinear grids (mesh.f90:245-358): the Jacobian of the supplied
+// coordinates by the first-derivative operator (a non-periodic one with
+// one-sided ends when the coordinates are not periodic, mesh.f90:246-307),
+// its determinant and inverse, the physical spacings, CellVol and GridLen.
+void curv_mesh(og_handle* h, const double* x, const double* y, const double* z, int mesh_per) {
+  const size_t np = npts_of(h);
+  for (int q = 0; q < MF_COUNT; q++) h->mf[q].assign(np, 0.0);
+  std::memcpy(h->mf[MF_X].data(), x, np * sizeof(double));
+  std::memcpy(h->mf[MF_Y].data(), y, np * sizeof(double));
+  std::memcpy(h->mf[MF_Z].data(), z, np * sizeof(double));
+  // J[c][d] = d(coordinate c)/d(direction d), stored in the inverse-Jacobian slots first
+  const Weight wd1 = make_c10d1();
+  const double* xs[3] = {x, y, z};
+  for (int d = 0; d < 3; d++) {
+    Op1 custom;
+    if (mesh_per) custom = setup_op(wd1, 1, h->n[d], false, 0, 0);
+    for (int c = 0; c < 3; c++) {
+      double* dst = h->mf[MF_J0 + 3 * c + d].data();
+      if (mesh_per) apply_op(h, custom, OP_D1, d, xs[c], dst);
+      else apply_dir(h, OP_D1, d, xs[c], dst);
+    }
+  }
+  const double dA = h->d[0], dB = h->d[1], dC = h->d[2];
+  for (size_t p = 0; p < np; p++) {
+    double J[9];
+    for (int q = 0; q < 9; q++) J[q] = h->mf[MF_J0 + q][p];
+    double &dxdA = J[0], &dxdB = J[1], &dxdC = J[2], &dydA = J[3], &dydB = J[4], &dydC = J[5], &dzdA = J[6],
+           &dzdB = J[7], &dzdC = J[8];
+    if (h->n[0] == 1) dxdA = 1.0;
+    if (h->n[1] == 1) dydB = 1.0;
+    if (h->n[2] == 1) dzdC = 1.0;
+    const double det = -dxdC * dydB * dzdA + dxdB * dydC * dzdA + dxdC * dydA * dzdB - dxdA * dydC * dzdB -
+                       dxdB * dydA * dzdC + dxdA * dydB * dzdC;
+    double* o[9];
+    for (int q = 0; q < 9; q++) o[q] = &h->mf[MF_J0 + q][p];
+    *o[0] = (-dydC * dzdB + dydB * dzdC) / det;  // dA/dx
+    *o[1] = (dxdC * dzdB - dxdB * dzdC) / det;   // dA/dy
+    *o[2] = (-dxdC * dydB + dxdB * dydC) / det;  // dA/dz
+    *o[3] = (dydC * dzdA - dydA * dzdC) / det;   // dB/dx
+    *o[4] = (-dxdC * dzdA + dxdA * dzdC) / det;  // dB/dy
+    *o[5] = (dxdC * dydA - dxdA * dydC) / det;   // dB/dz
+    *o[6] = (-dydB * dzdA + dydA * dzdB) / det;  // dC/dx
+    *o[7] = (dxdB * dzdA - dxdA * dzdB) / det;   // dC/dy
+    *o[8] = (-dxdB * dydA + dxdA * dydB) / det;  // dC/dz
+    const double d1 = std::sqrt((dxdA * dA) * (dxdA * dA) + (dydA * dA) * (dydA * dA) + (dzdA * dA) * (dzdA * dA));
+    const double d2 = std::sqrt((dxdB * dB) * (dxdB * dB) + (dydB * dB) * (dydB * dB) + (dzdB * dB) * (dzdB * dB));
+    const double d3 = std::sqrt((dxdC * dC) * (dxdC * dC) + (dydC * dC) * (dydC * dC) + (dzdC * dC) * (dzdC * dC));
+    h->mf[MF_DET][p] = det;
+    h->mf[MF_D1][p] = d1;
+    h->mf[MF_D2][p] = d2;
+    h->mf[MF_D3][p] = d3;
+    h->mf[MF_CV][p] = d1 * d2 * d3;
+    h->mf[MF_GL][p] = std::min(std::min(d1, d2), d3);
+  }
+  cell_bar(h);
+}
+
+// pyrandaMesh.py:96-108: the coordinates of a curvilinear grid before a mapping
+// is supplied are the nodes numpy.linspace(x1, xn, nn) of every direction
+void curv_default(og_handle* h, const double* x1, const double* xn) {
+  const int nx = h->n[0], ny = h->n[1], nz = h->n[2];
+  const size_t np = npts_of(h);
+  std::vector<double> c[3];
+  for (int q = 0; q < 3; q++) c[q].resize(np);
+  auto lin = [&](int d, int i) {
+    const int n = h->n[d];
+    if (n == 1) return x1[d];
+    if (i == n - 1) return xn[d];
+    return x1[d] + (double)i * ((xn[d] - x1[d]) / (double)(n - 1));
+  };
+  for (int k = 0; k < nz; k++)
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++) {
+        const size_t p = ((size_t)k * ny + j) * nx + i;
+        c[0][p] = lin(0, i);
+        c[1][p] = lin(1, j);
+        c[2][p] = lin(2, k);
+      }
+  curv_mesh(h, c[0].data(), c[1].data(), c[2].data(), 1);
+}
 }  // namespace
 
 extern "C" {
@@ -798,7 +959,7 @@ int og_create(const int* n, const int* periodic, const double* x1, const double*
 // 2 XTND) and the coordinate system (0 Cartesian, 1 cylindrical).
 int og_create2(const int* n, const int* periodic, const int* bc, int coordsys, const double* x1, const double* xn,
                og_handle** out) {
-  if (!n || !periodic || !bc || !x1 || !xn || !out || coordsys < 0 || coordsys > 1) return 1;
+  if (!n || !periodic || !bc || !x1 || !xn || !out || coordsys < 0 || coordsys > 4) return 1;
   og_handle* h = new og_handle();
   h->coordsys = coordsys;
   for (int d = 0; d < 3; d++) {
@@ -844,7 +1005,18 @@ int og_create2(const int* n, const int* periodic, const int* bc, int coordsys, c
     const int kinds[6] = {1, 4, 4, 4, 3, 3};
     for (int op = 0; op < 6; op++) h->anti[op][d] = setup_op(*ws[op], kinds[op], h->n[d], per, c1[1], c2[1]);
   }
+  if (coordsys == 2 || coordsys == 4) sph_mesh(h);
+  if (coordsys == 3) curv_default(h, x1, xn);
   *out = h;
+  return 0;
+}
+
+// setup_mesh_x3 (parcop.f90:73-81, mesh.f90:163-168 and :245-358): the
+// coordinates of a curvilinear grid; mesh_per is pyranda's 'periodicGrid'
+// option (the Jacobian by a non-periodic first derivative)
+int og_set_mesh_x3(og_handle* h, const double* x, const double* y, const double* z, int mesh_per) {
+  if (!h || !x || !y || !z || h->coordsys != 3) return 1;
+  curv_mesh(h, x, y, z, mesh_per ? 1 : 0);
   return 0;
 }
 
@@ -893,11 +1065,49 @@ int og_filter3_sym(const og_handle* h, int op, const int* sym, const double* in,
   return 0;
 }
 
-// LapS, Cartesian: operators.f90:513-526 (Lapf = Lapf + tmp + dum)
+// LapS: operators.f90:513-526 (Cartesian: Lapf = Lapf + tmp + dum), :527-543
+// (cylindrical), :544-559 (spherical, coordsys 2).  The reference has no
+// branch for coordsys 3 and 4 (its output is left unset): an error here.
 int og_laplacian(const og_handle* h, const double* in, double* out) {
-  if (!h) return 1;
+  if (!h || h->coordsys > 2) return 1;
   const size_t npts = (size_t)h->n[0] * h->n[1] * h->n[2];
   std::vector<double> tmp(npts), dum(npts);
+  if (h->coordsys == 1) {
+    apply_dir(h, OP_D1, 0, in, tmp.data());
+    for (size_t p = 0; p < npts; p++) dum[p] = xgrid(h, p) * tmp[p];
+    apply_dir(h, OP_D1, 0, dum.data(), tmp.data());
+    for (size_t p = 0; p < npts; p++) out[p] = tmp[p] / xgrid(h, p);
+    apply_dir(h, OP_D2, 1, in, tmp.data());
+    for (size_t p = 0; p < npts; p++) {
+      const double r = xgrid(h, p);
+      dum[p] = tmp[p] / (r * r);
+      out[p] = out[p] + dum[p];
+    }
+    apply_dir(h, OP_D2, 2, in, tmp.data());
+    for (size_t p = 0; p < npts; p++) out[p] = out[p] + tmp[p];
+    return 0;
+  }
+  if (h->coordsys == 2) {
+    const double *R = h->mf[MF_X].data(), *T = h->mf[MF_Y].data();
+    apply_dir(h, OP_D1, 0, in, tmp.data());
+    for (size_t p = 0; p < npts; p++) dum[p] = (R[p] * R[p]) * tmp[p];
+    apply_dir(h, OP_D1, 0, dum.data(), tmp.data());
+    for (size_t p = 0; p < npts; p++) out[p] = tmp[p] / (R[p] * R[p]);
+    apply_dir(h, OP_D1, 1, in, tmp.data());
+    for (size_t p = 0; p < npts; p++) dum[p] = std::sin(T[p]) * tmp[p];
+    apply_dir(h, OP_D1, 1, dum.data(), tmp.data());
+    for (size_t p = 0; p < npts; p++) {
+      dum[p] = tmp[p] / ((R[p] * R[p]) * std::sin(T[p]));
+      out[p] = out[p] + dum[p];
+    }
+    apply_dir(h, OP_D2, 2, in, tmp.data());
+    for (size_t p = 0; p < npts; p++) {
+      const double q = R[p] * std::sin(T[p]);
+      dum[p] = tmp[p] / (q * q);
+      out[p] = out[p] + dum[p];
+    }
+    return 0;
+  }
   apply_dir(h, OP_D2, 0, in, out);
   apply_dir(h, OP_D2, 1, in, tmp.data());
   apply_dir(h, OP_D2, 2, in, dum.data());
@@ -910,6 +1120,17 @@ int og_filter3(const og_handle* h, int op, const double* in, double* out) {
   if (!h || (op != 2 && op != 3)) return 1;
   const size_t np = (size_t)h->n[0] * h->n[1] * h->n[2];
   std::vector<double> tmp(np);
+  if (h->coordsys >= 2 && op == 2) {  // 'spectral', spherical and curvilinear: operators.f90:884-889
+    const double* cv = h->mf[MF_CV].data();
+    const double* bar = h->mf[h->coordsys == 4 ? MF_CV : MF_CVS].data();  // CellVolS = CellVol for coordsys 4
+    std::vector<double> fv(np);
+    for (size_t p = 0; p < np; p++) fv[p] = in[p] * cv[p];
+    apply_dir(h, op, 0, fv.data(), out);
+    apply_dir(h, op, 1, out, tmp.data());
+    apply_dir(h, op, 2, tmp.data(), out);
+    for (size_t p = 0; p < np; p++) out[p] = out[p] / bar[p];
+    return 0;
+  }
   if (h->coordsys == 1 && op == 2) {  // 'spectral' on a cylindrical grid: operators.f90:876-883
     std::vector<double> fv(np);
     for (size_t p = 0; p < np; p++) fv[p] = in[p] * cellvol_cyl(h, p);
@@ -935,13 +1156,19 @@ int og_ring(const og_handle* h, const double* f, double* out, int L) {
     if (h->n[d] == 1) std::memset(rs[d], 0, np * sizeof(double));
     else apply_dir(h, OP_D8, d, f, rs[d]);
   }
-  double s[3];
-  for (int d = 0; d < 3; d++) s[d] = (L == 0) ? 1.0 : (L == 1 ? h->dmesh[d] : h->dmesh[d] * h->dmesh[d]);
+  // the mesh d1, d2, d3 are fields on non-Cartesian grids (d2 = r dy when cylindrical)
 #pragma omp parallel for schedule(static)
   for (long i = 0; i < (long)np; i++) {
     double a, b, c;
     if (L == 0) { a = std::fabs(r1[i]); b = std::fabs(r2[i]); c = std::fabs(r3[i]); }
-    else { a = std::fabs(r1[i]) * s[0]; b = std::fabs(r2[i]) * s[1]; c = std::fabs(r3[i]) * s[2]; }
+    else {
+      double s[3];
+      for (int d = 0; d < 3; d++) {
+        const double m = mesh_d(h, d, (size_t)i);
+        s[d] = L == 1 ? m : m * m;
+      }
+      a = std::fabs(r1[i]) * s[0]; b = std::fabs(r2[i]) * s[1]; c = std::fabs(r3[i]) * s[2];
+    }
     out[i] = std::max(std::max(a, b), c);
   }
   return 0;
@@ -959,8 +1186,6 @@ int og_ringv(const og_handle* h, const double* f, const double* g, const double*
       if (h->n[d] == 1) std::memset(dst, 0, np * sizeof(double));
       else apply_dir(h, OP_D8, d, src[c], dst);
     }
-  double s[3];
-  for (int d = 0; d < 3; d++) s[d] = (L == 0) ? 1.0 : (L == 1 ? h->dmesh[d] : h->dmesh[d] * h->dmesh[d]);
 #pragma omp parallel for schedule(static)
   for (long i = 0; i < (long)np; i++) {
     double m[3];
@@ -968,7 +1193,8 @@ int og_ringv(const og_handle* h, const double* f, const double* g, const double*
       const double a = std::fabs(r[(size_t)(0 + d) * np + i]), b = std::fabs(r[(size_t)(3 + d) * np + i]),
                    c = std::fabs(r[(size_t)(6 + d) * np + i]);
       m[d] = std::max(std::max(a, b), c);
-      if (L != 0) m[d] = m[d] * s[d];
+      const double md = mesh_d(h, d, (size_t)i);
+      if (L != 0) m[d] = m[d] * (L == 1 ? md : md * md);
     }
     out[i] = std::max(std::max(m[0], m[1]), m[2]);
   }
@@ -981,14 +1207,116 @@ int og_grad(const og_handle* h, const double* f, double* gx, double* gy, double*
   apply_dir(h, OP_D1, 0, f, gx);
   apply_dir(h, OP_D1, 1, f, gy);
   apply_dir(h, OP_D1, 2, f, gz);
+  const size_t np = (size_t)h->n[0] * h->n[1] * h->n[2];
   if (h->coordsys == 1) {
-    const size_t np = (size_t)h->n[0] * h->n[1] * h->n[2];
     for (size_t p = 0; p < np; p++) gy[p] = gy[p] / xgrid(h, p);
+  } else if (h->coordsys == 2 || h->coordsys == 4) {  // operators.f90:197-201
+    const double *R = h->mf[MF_X].data(), *T = h->mf[MF_Y].data(), *D1 = h->mf[MF_D1].data();
+    for (size_t p = 0; p < np; p++) {
+      gx[p] = gx[p] * h->d[0] / D1[p];
+      gy[p] = gy[p] / R[p];
+      gz[p] = gz[p] / (R[p] * std::sin(T[p]));
+    }
+  } else if (h->coordsys == 3) {  // operators.f90:202-209
+    for (size_t p = 0; p < np; p++) {
+      double m[9];
+      for (int q = 0; q < 9; q++) m[q] = h->mf[MF_J0 + q][p];
+      const double a = gx[p], b = gy[p], c = gz[p];
+      gx[p] = a * m[0] + b * m[3] + c * m[6];
+      gy[p] = a * m[1] + b * m[4] + c * m[7];
+      gz[p] = a * m[2] + b * m[5] + c * m[8];
+    }
   }
   return 0;
 }
 
-// divT: operators.f90:97-146 (Cartesian :104-122, cylindrical :123-146).
+namespace {
+// divV on spherical grids (operators.f90:64-76)
+void div_sph(const og_handle* h, const double* fx, const double* fy, const double* fz, double* out) {
+  const size_t np = npts_of(h);
+  const double *R = h->mf[MF_X].data(), *T = h->mf[MF_Y].data(), *D1 = h->mf[MF_D1].data();
+  std::vector<double> tmp(np), fA(np), fB(np), fC(np);
+  for (size_t p = 0; p < np; p++) {
+    tmp[p] = (R[p] * R[p]) * fx[p];
+    out[p] = fy[p] * std::sin(T[p]);
+  }
+  apply_dir(h, OP_D1, 0, tmp.data(), fA.data(), isym_pow(h, 0, 3));
+  for (size_t p = 0; p < np; p++) fA[p] = fA[p] * h->d[0] / D1[p];
+  apply_dir(h, OP_D1, 1, out, fB.data(), isym_pow(h, 1, 2));
+  apply_dir(h, OP_D1, 2, fz, fC.data(), isym_pow(h, 2, 1));
+  for (size_t p = 0; p < np; p++) out[p] = fA[p] / (R[p] * R[p]) + (fB[p] + fC[p]) / (R[p] * std::sin(T[p]));
+}
+
+// divV on curvilinear grids (operators.f90:77-90): the contravariant fluxes
+// times det J, differentiated along A, B, C, summed and divided by det J
+void div_curv(const og_handle* h, const double* fx, const double* fy, const double* fz, double* out) {
+  const size_t np = npts_of(h);
+  std::vector<double> fA(np), fB(np), fC(np), tmp(np);
+  const double* det = h->mf[MF_DET].data();
+  for (size_t p = 0; p < np; p++) {
+    double m[9];
+    for (int q = 0; q < 9; q++) m[q] = h->mf[MF_J0 + q][p];
+    fA[p] = (fx[p] * m[0] + fy[p] * m[1] + fz[p] * m[2]) * det[p];
+    fB[p] = (fx[p] * m[3] + fy[p] * m[4] + fz[p] * m[5]) * det[p];
+    fC[p] = (fx[p] * m[6] + fy[p] * m[7] + fz[p] * m[8]) * det[p];
+  }
+  apply_dir(h, OP_D1, 0, fA.data(), out);
+  apply_dir(h, OP_D1, 1, fB.data(), tmp.data());
+  for (size_t p = 0; p < np; p++) out[p] = out[p] + tmp[p];
+  apply_dir(h, OP_D1, 2, fC.data(), tmp.data());
+  for (size_t p = 0; p < np; p++) out[p] = (out[p] + tmp[p]) / det[p];
+}
+
+// divT on spherical grids (operators.f90:148-173), with iR = 1/r,
+// isinY = 1/sin(theta), itanY = 1/tan(theta) as mesh.f90:241-243 stores them
+void divt_sph(const og_handle* h, const double* const* f, double* const* out) {
+  const size_t np = npts_of(h);
+  const double *R = h->mf[MF_X].data(), *T = h->mf[MF_Y].data(), *D1 = h->mf[MF_D1].data();
+  const double *fxx = f[0], *fxy = f[1], *fxz = f[2], *fyx = f[3], *fyy = f[4], *fyz = f[5], *fzx = f[6],
+               *fzy = f[7], *fzz = f[8];
+  std::vector<double> tmp(np), fA(np), fB(np), fC(np);
+  const double dx = h->d[0];
+  for (size_t p = 0; p < np; p++) tmp[p] = (R[p] * R[p]) * fxx[p];
+  apply_dir(h, OP_D1, 0, tmp.data(), fA.data(), 1);
+  for (size_t p = 0; p < np; p++) {
+    fA[p] = fA[p] * dx / D1[p];
+    tmp[p] = fyx[p] / (1.0 / std::sin(T[p]));
+  }
+  apply_dir(h, OP_D1, 1, tmp.data(), fB.data(), 1);
+  apply_dir(h, OP_D1, 2, fzx, fC.data(), isym_pow(h, 2, 1));
+  for (size_t p = 0; p < np; p++) {
+    const double iR = 1.0 / R[p], isinY = 1.0 / std::sin(T[p]);
+    out[0][p] = fA[p] * (iR * iR) + (fB[p] + fC[p]) * iR * isinY - (fyy[p] + fzz[p]) * iR;
+    tmp[p] = (R[p] * R[p] * R[p]) * fxy[p];
+  }
+  apply_dir(h, OP_D1, 0, tmp.data(), fA.data(), 1);
+  for (size_t p = 0; p < np; p++) {
+    fA[p] = fA[p] * dx / D1[p];
+    tmp[p] = fyy[p] * std::sin(T[p]);
+  }
+  apply_dir(h, OP_D1, 1, tmp.data(), fB.data(), isym_pow(h, 1, 3));
+  apply_dir(h, OP_D1, 2, fzy, fC.data(), isym_pow(h, 2, 1));
+  for (size_t p = 0; p < np; p++) {
+    const double iR = 1.0 / R[p], isinY = 1.0 / std::sin(T[p]), itanY = 1.0 / std::tan(T[p]);
+    out[1][p] = fA[p] * (iR * iR * iR) + (fB[p] + fC[p]) * iR * isinY + (fyx[p] - fxy[p] - fzz[p] * itanY) * iR;
+    tmp[p] = (R[p] * R[p] * R[p]) * fxz[p];
+  }
+  apply_dir(h, OP_D1, 0, tmp.data(), fA.data(), 1);
+  for (size_t p = 0; p < np; p++) {
+    fA[p] = fA[p] * dx / D1[p];
+    tmp[p] = fyz[p] * std::sin(T[p]);
+  }
+  apply_dir(h, OP_D1, 1, tmp.data(), fB.data(), 1);
+  apply_dir(h, OP_D1, 2, fzz, fC.data(), 1);
+  for (size_t p = 0; p < np; p++) {
+    const double iR = 1.0 / R[p], isinY = 1.0 / std::sin(T[p]), itanY = 1.0 / std::tan(T[p]);
+    out[2][p] = fA[p] * (iR * iR * iR) + (fB[p] + fC[p]) * iR * isinY + (fzx[p] - fxz[p] + fzy[p] * itanY) * iR;
+  }
+}
+}  // namespace
+
+// divT: operators.f90:97-181 (Cartesian :104-122, cylindrical :123-146,
+// spherical :147-173, curvilinear :174-177).
 // f: fxx fxy fxz fyx fyy fyz fzx fzy fzz; out: dfx dfy dfz
 int og_divt(const og_handle* h, const double* const* f, double* const* out) {
   if (!h) return 1;
@@ -996,6 +1324,16 @@ int og_divt(const og_handle* h, const double* const* f, double* const* out) {
   std::vector<double> tmp(np), fA(np), fB(np), fC(np);
   const double *fxx = f[0], *fxy = f[1], *fxz = f[2], *fyx = f[3], *fyy = f[4], *fyz = f[5], *fzx = f[6],
                *fzy = f[7], *fzz = f[8];
+  if (h->coordsys == 2 || h->coordsys == 4) {
+    divt_sph(h, f, out);
+    return 0;
+  }
+  if (h->coordsys == 3) {  // the divergence of each row
+    div_curv(h, fxx, fxy, fxz, out[0]);
+    div_curv(h, fyx, fyy, fyz, out[1]);
+    div_curv(h, fzx, fzy, fzz, out[2]);
+    return 0;
+  }
   if (h->coordsys == 0) {
     const double* cols[3][3] = {{fxx, fyx, fzx}, {fxy, fyy, fzy}, {fxz, fyz, fzz}};
     for (int c = 0; c < 3; c++) {
@@ -1035,6 +1373,14 @@ int og_div(const og_handle* h, const double* fx, const double* fy, const double*
   if (!h) return 1;
   const size_t np = (size_t)h->n[0] * h->n[1] * h->n[2];
   std::vector<double> a(np), b(np);
+  if (h->coordsys == 2 || h->coordsys == 4) {
+    div_sph(h, fx, fy, fz, out);
+    return 0;
+  }
+  if (h->coordsys == 3) {
+    div_curv(h, fx, fy, fz, out);
+    return 0;
+  }
   if (h->coordsys == 1) {  // operators.f90:55-64
     std::vector<double> tmp(np), c(np);
     for (size_t p = 0; p < np; p++) tmp[p] = xgrid(h, p) * fx[p];
@@ -1053,10 +1399,19 @@ int og_div(const og_handle* h, const double* fx, const double* fy, const double*
   return 0;
 }
 
-// Mesh quantities (mesh.f90:169-211, Cartesian):
-// which = 0,1,2 -> x,y,z grid; 3,4,5 -> d1,d2,d3; 6 -> GridLen; 7 -> CellVol
+// Mesh quantities (mesh.f90:169-386):
+// which = 0,1,2 -> x,y,z grid; 3,4,5 -> d1,d2,d3; 6 -> GridLen; 7 -> CellVol;
+// 8, 9 -> CellVolS, CellVolG; 10 -> det J; 11..19 -> dA/dx dA/dy dA/dz dB/dx .. dC/dz
+// (curvilinear grids only)
 int og_mesh(const og_handle* h, int which, double* out) {
-  if (!h || which < 0 || which > 7) return 1;
+  if (!h || which < 0 || which > 19) return 1;
+  if (h->coordsys >= 2) {
+    if (which >= MF_DET && h->coordsys != 3) return 1;
+    std::memcpy(out, h->mf[which].data(), npts_of(h) * sizeof(double));
+    return 0;
+  }
+  if (which >= 10) return 1;
+  if (which == 8 || which == 9) which = 7;  // CellVolS = CellVolG = CellVol (mesh.f90:384-386)
   const int nx = h->n[0], ny = h->n[1], nz = h->n[2];
   const double gl = std::min(std::min(h->dmesh[0], h->dmesh[1]), h->dmesh[2]);
   const double cv = h->d[0] * h->d[1] * h->d[2];

@@ -44,7 +44,7 @@ class pg_grid(ctypes.Structure):
 
 
 PG_BC_NONE, PG_BC_SYMM, PG_BC_XTND = 0, 1, 2
-PG_CARTESIAN, PG_CYLINDRICAL = 0, 1
+PG_CARTESIAN, PG_CYLINDRICAL, PG_SPHERICAL, PG_CURVILINEAR, PG_SPHERICAL_RATIO = 0, 1, 2, 3, 4
 
 
 PG_LAD_IN, PG_LAD_K, PG_LAD_HIDDEN, PG_LAD_OUT = 55, 64, 64, 2
@@ -92,6 +92,7 @@ SIGNATURES = [
     ("pg_div", I, [P, D, D, D, D, P]),
     ("pg_divt", I, [P, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p), P]),
     ("pg_mesh", I, [P, I, D, P]),
+    ("pg_set_mesh_coords", I, [P, D, D, D, I, P]),
     ("pg_rk_stage", I, [P, I, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
                         ctypes.POINTER(ctypes.c_void_p), D, ctypes.c_double, ctypes.c_double, P]),
     ("pg_courant", I, [P, D, D, D, D, ctypes.c_double, ctypes.c_double, D, P]),

@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libpyranda_gpu.so")
-SOURCES = ["pg_setup.cpp", "pg_sweep_f64.cu", "pg_sweep_f32.cu", "pg_sweep_f32_r4.cu", "pg_elem.cu", "pg_capi.cu", "pg_noalloc.cu", "pg_dense.cu", "pg_lad.cu", "pg_split.cu", "pg_seg_r3.cu", "pg_seg_r4.cu"]
+SOURCES = ["pg_setup.cpp", "pg_sweep_f64.cu", "pg_sweep_f32.cu", "pg_sweep_f32_r4.cu", "pg_elem.cu", "pg_capi.cu", "pg_noalloc.cu", "pg_dense.cu", "pg_lad.cu", "pg_split.cu", "pg_seg_r3.cu", "pg_seg_r4.cu", "pg_metric.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -41,6 +41,8 @@ def _compile(src, verbose):
     obj = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
     cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
            "-I", os.path.join(HERE, "..", "include"), "-c", os.path.join(SRC, src), "-o", obj]
+    if src == "pg_metric.cu":  # the metric forms round operation by operation, as the reference's loops
+        cmd.insert(1, "-fmad=false")
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)

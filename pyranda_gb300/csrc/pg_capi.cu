@@ -58,6 +58,7 @@ struct GridInfo {
   int bc[3][2];   // pg_bc per end (non-periodic directions)
   bool symm[3];   // a symmetry plane at either end: the antisymmetric variants differ
   int coordsys;   // pg_coordsys
+  double x1[3], xn[3];  // node extents (the default coordinates of a curvilinear grid)
   OpTables tab[OPK_COUNT][3];       // operators for symmetric fields (the default)
   OpTables tab_anti[OPK_COUNT][3];  // variants for antisymmetric fields (compact.f90:80-85, nop = 2)
 };
@@ -70,6 +71,8 @@ int grid_info(const pg_grid* g, GridInfo& gi, const char* who) {
     }
     gi.n[d] = g->n[d];
     gi.periodic[d] = g->periodic[d] ? 1 : 0;
+    gi.x1[d] = g->x1[d];
+    gi.xn[d] = g->xn[d];
     for (int e = 0; e < 2; e++) {
       const int b = g->bc[d][e];
       if (b < PG_BC_NONE || b > PG_BC_XTND) {
@@ -84,8 +87,8 @@ int grid_info(const pg_grid* g, GridInfo& gi, const char* who) {
     gi.x1f[d] = f1;
     gi.d[d] = (fn - f1) / (double)g->n[d];
   }
-  if (g->coordsys != PG_CARTESIAN && g->coordsys != PG_CYLINDRICAL) {
-    set_error("%s: coordsys %d is not supported (Cartesian 0 or cylindrical 1)", who, g->coordsys);
+  if (g->coordsys < PG_CARTESIAN || g->coordsys > PG_SPHERICAL_RATIO) {
+    set_error("%s: coordsys %d is not a pg_coordsys", who, g->coordsys);
     return PG_EINVAL;
   }
   gi.coordsys = g->coordsys;
@@ -125,7 +128,8 @@ struct Ctx {
   OpRef anti[2][OPK_COUNT][3];   // the antisymmetric variants (differ where a direction has a symmetry plane)
   bool symm[3] = {false, false, false};
   int coordsys = PG_CARTESIAN;
-  double* cyl[3] = {nullptr, nullptr, nullptr};  // cylindrical grids: three workspace fields
+  double* cyl[3] = {nullptr, nullptr, nullptr};  // non-Cartesian grids: three workspace fields
+  double* mf[MF_COUNT] = {};     // spherical and curvilinear grids: the mesh fields (one allocation at mf[0])
   void* blob = nullptr;          // coefficient tables and member-op arrays
   double* work = nullptr;        // one field: x->y->z filter ping-pong
   double* work2 = nullptr;       // one field: forward-elimination scratch of a sweep
@@ -170,6 +174,7 @@ void free_ctx(Ctx& c) {
   if (c.split_blob) cudaFree(c.split_blob);
   for (int q = 0; q < 3; q++)
     if (c.cyl[q]) cudaFree(c.cyl[q]);
+  if (c.mf[0]) cudaFree(c.mf[0]);
   c = Ctx();
 }
 
@@ -331,8 +336,13 @@ int build_ctx(Ctx& c, const std::vector<GridInfo>& g, int precision, const char*
   const size_t nbytes = (size_t)c.npts * sizeof(double);
   if (e == cudaSuccess) e = cudaMalloc(&c.work, nbytes);
   if (e == cudaSuccess) e = cudaMalloc(&c.work2, nbytes);
-  if (g[0].coordsys == PG_CYLINDRICAL)
+  if (g[0].coordsys != PG_CARTESIAN)
     for (int q = 0; q < 3 && e == cudaSuccess; q++) e = cudaMalloc(&c.cyl[q], nbytes);
+  if (g[0].coordsys >= PG_SPHERICAL && e == cudaSuccess) {  // mesh.f90:98-139: the fields each system keeps
+    const int nf = g[0].coordsys == PG_CURVILINEAR ? MF_COUNT : MF_DET;
+    e = cudaMalloc(&c.mf[0], nbytes * nf);
+    for (int q = 1; q < nf && e == cudaSuccess; q++) c.mf[q] = c.mf[0] + (size_t)q * c.npts;
+  }
   // two values per block for the two-pass diffusion limit (estimate, exact-point flag)
   const size_t npart = std::max((size_t)2 * kReduceBlocks, (size_t)M * kSegBlocks + 2 * (size_t)M);
   if (e == cudaSuccess) e = cudaMalloc(&c.partial, npart * sizeof(double));
@@ -1189,6 +1199,238 @@ int divt(pg_handle* h, const double* const* f, double* const* out, void* st) {
   return rc;
 }
 
+// ---------------------------------------------------------------------------
+// Spherical and curvilinear grids: the derivative sweeps of the handle joined
+// by the pointwise metric forms of pg_metric.cu (operators.f90:54-209).
+// ---------------------------------------------------------------------------
+MetricArgs margs(const pg_handle* h, int op) {
+  const GridInfo& g = h->g;
+  MetricArgs A;
+  A.op = op;
+  A.n = g.npts;
+  A.nx = g.n[0];
+  A.ny = g.n[1];
+  A.nz = g.n[2];
+  A.coordsys = g.coordsys;
+  for (int d = 0; d < 3; d++) {
+    A.x1f[d] = g.x1f[d];
+    A.d[d] = g.d[d];
+    A.x1[d] = g.x1[d];
+    A.xn[d] = g.xn[d];
+  }
+  for (int q = 0; q < MF_COUNT; q++) A.mf[q] = h->c.mf[q];
+  return A;
+}
+
+int metric(const pg_handle* h, int op, std::initializer_list<const double*> in, std::initializer_list<double*> out,
+           void* st, int L = 0) {
+  MetricArgs A = margs(h, op);
+  int q = 0;
+  for (const double* p : in) A.in[q++] = p;
+  q = 0;
+  for (double* p : out) A.out[q++] = p;
+  A.L = L;
+  return launch_metric(A, st);
+}
+
+bool sph(const Ctx& c) { return c.coordsys == PG_SPHERICAL || c.coordsys == PG_SPHERICAL_RATIO; }
+
+// gradS (operators.f90:197-209): the derivatives along the grid lines, then the metric factors
+int grad_metric(pg_handle* h, const double* in, double* gx, double* gy, double* gz, void* st) {
+  int rc = grad(h->c, in, gx, gy, gz, st);
+  if (!rc) rc = metric(h, sph(h->c) ? MET_SPH_GRAD : MET_CURV_GRAD, {}, {gx, gy, gz}, st);
+  return rc;
+}
+
+// divV (operators.f90:64-90)
+int div_metric(pg_handle* h, const double* fx, const double* fy, const double* fz, double* out, void* st) {
+  Ctx& c = h->c;
+  double *w0 = c.cyl[0], *w1 = c.cyl[1], *w2 = c.cyl[2];
+  int rc;
+  if (sph(c)) {  // r^2 fx and fy sin(theta) (isymX^3, isymY^2, isymZ), then (fA dx/d1)/r^2 + (fB+fC)/(r sin)
+    rc = metric(h, MET_SPH_DIV_PRE, {fx, fy}, {w0, w1}, st);
+    if (!rc) rc = apply_one(c, OPK_D1, 0, w0, w2, st, isym(c, 0, 3));
+    if (!rc) rc = apply_one(c, OPK_D1, 1, w1, w0, st, isym(c, 1, 2));
+    if (!rc) rc = apply_one(c, OPK_D1, 2, fz, out, st, isym(c, 2, 1));
+    if (!rc) rc = metric(h, MET_SPH_DIV_POST, {w2, w0, out}, {out}, st);
+    return rc;
+  }
+  // curvilinear: the contravariant fluxes times det J along A, B, C, summed, over det J
+  rc = metric(h, MET_CURV_DIV_PRE, {fx, fy, fz}, {w0, w1, w2}, st);
+  if (!rc) rc = apply_one(c, OPK_D1, 0, w0, out, st);
+  if (!rc) rc = apply_one(c, OPK_D1, 1, w1, w0, st);
+  if (!rc) rc = apply_one(c, OPK_D1, 2, w2, w1, st);
+  if (!rc) rc = metric(h, MET_CURV_DIV_POST, {out, w0, w1}, {out}, st);
+  return rc;
+}
+
+// divT (operators.f90:147-177): spherical rows, or the divergence of each row on curvilinear grids
+int divt_metric(pg_handle* h, const double* const* f, double* const* out, void* st) {
+  Ctx& c = h->c;
+  if (!sph(c)) {
+    int rc = div_metric(h, f[0], f[1], f[2], out[0], st);
+    if (!rc) rc = div_metric(h, f[3], f[4], f[5], out[1], st);
+    if (!rc) rc = div_metric(h, f[6], f[7], f[8], out[2], st);
+    return rc;
+  }
+  const double *fxx = f[0], *fxy = f[1], *fxz = f[2], *fyx = f[3], *fyy = f[4], *fyz = f[5], *fzx = f[6],
+               *fzy = f[7], *fzz = f[8];
+  double *w0 = c.cyl[0], *w1 = c.cyl[1], *w2 = c.cyl[2];
+  // row: (r^k f_x, theta form of f_y, f_z) with the symmetry powers of each derivative, then the row's combination
+  struct Row {
+    const double *a, *b, *cz;
+    int k, py, pz;
+    const double *t0, *t1, *t2;
+  };
+  const Row rows[3] = {{fxx, fyx, fzx, 2, 2, 1, fyy, fzz, nullptr},
+                       {fxy, fyy, fzy, 3, 3, 1, fyx, fxy, fzz},
+                       {fxz, fyz, fzz, 3, 2, 2, fzx, fxz, fzy}};
+  int rc = PG_OK;
+  for (int r = 0; r < 3 && !rc; r++) {
+    const Row& R = rows[r];
+    rc = metric(h, MET_SPH_T_PRE, {R.a, R.b}, {w0, w1}, st, R.k);
+    if (!rc) rc = apply_one(c, OPK_D1, 0, w0, w2, st, 1);  // isymX^4
+    if (!rc) rc = apply_one(c, OPK_D1, 1, w1, w0, st, isym(c, 1, R.py));
+    if (!rc) rc = apply_one(c, OPK_D1, 2, R.cz, w1, st, isym(c, 2, R.pz));
+    if (!rc) rc = metric(h, MET_SPH_T_POST, {w2, w0, w1, R.t0, R.t1, R.t2}, {out[r]}, st, r);
+  }
+  return rc;
+}
+
+// filter('spectral') on spherical and curvilinear grids (operators.f90:884-889):
+// filter CellVol f, divide by the filtered cell volume (CellVol itself when ratio-zoned)
+int filter_metric(pg_handle* h, const double* in, double* out, void* st) {
+  Ctx& c = h->c;
+  int rc = metric(h, MET_VOL_MUL, {in}, {c.cyl[0]}, st);
+  if (!rc) rc = filter_all(c, OPK_SF, c.cyl[0], out, st);
+  if (!rc) rc = metric(h, MET_VOL_DIV, {out, c.mf[c.coordsys == PG_SPHERICAL_RATIO ? MF_CV : MF_CVS]}, {out}, st);
+  return rc;
+}
+
+// ringS / ringV with mesh-field scales (operators.f90:615-699): the d8 of each
+// (component, direction) into a workspace field, then max(out, |d8| d^L)
+bool ring_fields(const Ctx& c, const GridInfo& g) {
+  return c.coordsys >= PG_SPHERICAL || (c.coordsys == PG_CYLINDRICAL && g.n[1] > 1);
+}
+
+int ring_metric(pg_handle* h, const double* const* src, int ncomp, int L, double* out, void* st) {
+  Ctx& c = h->c;
+  bool first = true;
+  int rc = PG_OK;
+  for (int q = 0; q < ncomp && !rc; q++)
+    for (int d = 0; d < 3 && !rc; d++) {
+      if (c.ops[c.precision][OPK_D8][d].null_op) continue;
+      rc = apply_one(c, OPK_D8, d, src[q], c.cyl[0], st);
+      if (rc) break;
+      MetricArgs A = margs(h, MET_RING);
+      A.in[0] = c.cyl[0];
+      A.out[0] = out;
+      A.dir = d;
+      A.L = L;
+      A.first = first ? 1 : 0;
+      rc = launch_metric(A, st);
+      first = false;
+    }
+  if (!rc && first) rc = launch_fill(out, 0.0, c.npts, st);
+  return rc;
+}
+
+// LapS, cylindrical and spherical (operators.f90:527-559)
+int laplacian_metric(pg_handle* h, const double* in, double* out, void* st) {
+  Ctx& c = h->c;
+  double *w0 = c.cyl[0], *w1 = c.cyl[1];
+  const int L = c.coordsys == PG_CYLINDRICAL ? 1 : 2;
+  int rc = apply_one(c, OPK_D1, 0, in, w0, st);
+  if (!rc) rc = metric(h, MET_LAP_MUL, {w0}, {w1}, st, L);   // r^L df/dr
+  if (!rc) rc = apply_one(c, OPK_D1, 0, w1, w0, st);
+  if (!rc) rc = metric(h, MET_LAP_X, {w0}, {out}, st, L);    // / r^L
+  if (c.coordsys == PG_CYLINDRICAL) {
+    if (!rc) rc = apply_one(c, OPK_D2, 1, in, w0, st);
+  } else {
+    if (!rc) rc = apply_one(c, OPK_D1, 1, in, w0, st);
+    if (!rc) rc = metric(h, MET_LAP_SIN, {w0}, {w1}, st);     // sin(theta) df/dtheta
+    if (!rc) rc = apply_one(c, OPK_D1, 1, w1, w0, st);
+  }
+  if (!rc) rc = metric(h, MET_LAP_ADD_Y, {w0}, {out}, st);
+  if (!rc) rc = apply_one(c, OPK_D2, 2, in, w0, st);
+  if (!rc) rc = metric(h, MET_LAP_ADD_Z, {w0}, {out}, st);
+  return rc;
+}
+
+// The mesh fields of a spherical or curvilinear grid (mesh.f90:169-386), on
+// FP64 Cartesian handles of the same extents: one with the grid's own ends
+// (the stock operators) and, when the coordinates are not periodic, one with
+// one-sided ends everywhere for the Jacobian (mesh.f90:246-307).
+int mesh_setup(pg_handle* h, const double* x, const double* y, const double* z, int mesh_per, void* st) {
+  Ctx& c = h->c;
+  const GridInfo& g = h->g;
+  pg_grid base{};
+  for (int d = 0; d < 3; d++) {
+    base.n[d] = g.n[d];
+    base.periodic[d] = g.periodic[d];
+    base.x1[d] = g.x1[d];
+    base.xn[d] = g.xn[d];
+    for (int e = 0; e < 2; e++) base.bc[d][e] = g.bc[d][e];
+  }
+  base.precision = PG_FP64;
+  base.coordsys = PG_CARTESIAN;
+  pg_handle *stock = nullptr, *custom = nullptr;
+  int rc = pg_create(&base, &stock);
+  if (!rc && c.coordsys == PG_CURVILINEAR && mesh_per) {
+    pg_grid open = base;
+    for (int d = 0; d < 3; d++) {
+      open.periodic[d] = 0;
+      open.bc[d][0] = open.bc[d][1] = PG_BC_NONE;
+    }
+    rc = pg_create(&open, &custom);
+  }
+  if (!rc && sph(c)) {
+    MetricArgs A = margs(h, MET_SPH_MESH);
+    if (c.coordsys == PG_SPHERICAL_RATIO) {  // mesh.f90:180-186
+      A.s1 = std::log((double)(g.n[0] - 1) * g.d[0]) / (g.d[1] * (double)(g.n[0] - 1));  // Csp
+      A.s0 = (g.x1f[0] + g.d[0] / 2.0) / std::exp(A.s1 * g.d[1]);                        // Asp
+    }
+    rc = launch_metric(A, st);
+  }
+  if (!rc && c.coordsys == PG_CURVILINEAR) {
+    const size_t nbytes = (size_t)c.npts * sizeof(double);
+    if (!x) {
+      rc = launch_metric(margs(h, MET_NODES), st);
+    } else {
+      const double* src[3] = {x, y, z};
+      for (int q = 0; q < 3 && !rc; q++)
+        if (cudaMemcpyAsync(c.mf[MF_X + q], src[q], nbytes, cudaMemcpyDeviceToDevice, (cudaStream_t)st) !=
+            cudaSuccess) {
+          set_error("pg_set_mesh_coords: %s", cudaGetErrorString(cudaGetLastError()));
+          rc = PG_ECUDA;
+        }
+    }
+    pg_handle* jh = custom ? custom : stock;
+    for (int q = 0; q < 3 && !rc; q++)  // J[3 q + d] = d(coordinate q) / d(direction d)
+      for (int d = 0; d < 3 && !rc; d++) rc = pg_d1(jh, d, c.mf[MF_X + q], c.mf[MF_J0 + 3 * q + d], st);
+    if (!rc) rc = launch_metric(margs(h, MET_CURV_METRIC), st);
+  }
+  if (!rc) {  // mesh.f90:373-386: the filtered cell volumes (spherical and curvilinear), else CellVol
+    const size_t nbytes = (size_t)c.npts * sizeof(double);
+    if (c.coordsys == PG_SPHERICAL || c.coordsys == PG_CURVILINEAR) {
+      rc = pg_filter(stock, PG_SPECTRAL, PG_DIR_ALL, c.mf[MF_CV], c.mf[MF_CVS], st);
+      if (!rc) rc = pg_filter(stock, PG_GAUSSIAN, PG_DIR_ALL, c.mf[MF_CV], c.mf[MF_CVG], st);
+    } else {
+      for (int q = MF_CVS; q <= MF_CVG && !rc; q++)
+        if (cudaMemcpyAsync(c.mf[q], c.mf[MF_CV], nbytes, cudaMemcpyDeviceToDevice, (cudaStream_t)st) !=
+            cudaSuccess)
+          rc = PG_ECUDA;
+    }
+  }
+  if (cudaStreamSynchronize((cudaStream_t)st) != cudaSuccess && !rc) {
+    set_error("mesh set-up: %s", cudaGetErrorString(cudaGetLastError()));
+    rc = PG_ECUDA;
+  }
+  if (custom) pg_destroy(custom);
+  if (stock) pg_destroy(stock);
+  return rc;
+}
+
 }  // namespace
 }  // namespace pg
 
@@ -1205,6 +1447,7 @@ int pg_create(const pg_grid* grid, pg_handle** out) {
   pg_handle* h = new pg_handle();
   int rc = grid_info(grid, h->g, "pg_create");
   if (rc == PG_OK) rc = build_ctx(h->c, std::vector<GridInfo>{h->g}, PG_FP64, "pg_create");
+  if (rc == PG_OK && grid->coordsys >= PG_SPHERICAL) rc = mesh_setup(h, nullptr, nullptr, nullptr, 1, nullptr);
   if (rc == PG_OK) rc = set_precision(h->c, std::vector<GridInfo>{h->g}, grid->precision);
   if (rc != PG_OK) {
     free_ctx(h->c);
@@ -1325,12 +1568,27 @@ int pg_d4(pg_handle* h, int dir, const double* in, double* out, void* stream) {
   return apply_one(h->c, OPK_D4, dir, in, out, stream);
 }
 
+int pg_set_mesh_coords(pg_handle* h, const double* x, const double* y, const double* z, int mesh_periodic,
+                       void* stream) {
+  if (!h || !x || !y || !z) return PG_EINVAL;
+  if (h->c.coordsys != PG_CURVILINEAR) {
+    set_error("pg_set_mesh_coords: the grid is not curvilinear");
+    return PG_EINVAL;
+  }
+  return mesh_setup(h, x, y, z, mesh_periodic ? 1 : 0, stream);
+}
+
 int pg_laplacian(pg_handle* h, const double* in, double* out, void* stream) {
   if (!h || !in || !out) return PG_EINVAL;
   if (in == out) {
     set_error("pg_laplacian: in and out must differ");
     return PG_EINVAL;
   }
+  if (h->c.coordsys == PG_CURVILINEAR || h->c.coordsys == PG_SPHERICAL_RATIO) {
+    set_error("pg_laplacian: no Laplacian on curvilinear or ratio-zoned spherical grids (operators.f90:513-559)");
+    return PG_EINVAL;
+  }
+  if (h->c.coordsys != PG_CARTESIAN) return laplacian_metric(h, in, out, stream);
   return laplacian(h->c, in, out, stream);
 }
 
@@ -1338,6 +1596,13 @@ int pg_filter(pg_handle* h, int kind, int dir, const double* in, double* out, vo
   if (!h || !in || !out || (kind != PG_SPECTRAL && kind != PG_GAUSSIAN) || dir < 0 || dir > 3) return PG_EINVAL;
   const int k = kind == PG_SPECTRAL ? OPK_SF : OPK_GF;
   if (dir < 3) return apply_one(h->c, k, dir, in, out, stream);
+  if (h->c.coordsys >= PG_SPHERICAL && kind == PG_SPECTRAL) {
+    if (in == out) {
+      set_error("pg_filter: on a non-Cartesian grid out must not alias in");
+      return PG_EINVAL;
+    }
+    return filter_metric(h, in, out, stream);
+  }
   if (h->c.coordsys == PG_CYLINDRICAL && kind == PG_SPECTRAL) {
     // operators.f90:876-883: filter the volume-weighted field (CellVol is odd in r, so the radial
     // sweep takes the antisymmetric variant) and divide by the cell volume
@@ -1381,6 +1646,7 @@ int pg_ring(pg_handle* h, const double* in, double* out, void* stream) {
     set_error("pg_ring: in and out must differ");
     return PG_EINVAL;
   }
+  if (ring_fields(h->c, h->g)) return ring_metric(h, &in, 1, 2, out, stream);
   return ring(h->c, in, out, stream);
 }
 
@@ -1390,11 +1656,16 @@ int pg_ringv(pg_handle* h, const double* vx, const double* vy, const double* vz,
     set_error("pg_ringv: out must not alias an input");
     return PG_EINVAL;
   }
+  if (ring_fields(h->c, h->g)) {
+    const double* src[3] = {vx, vy, vz};
+    return ring_metric(h, src, 3, 1, out, stream);
+  }
   return ringv(h->c, vx, vy, vz, out, stream);
 }
 
 int pg_grad(pg_handle* h, const double* in, double* gx, double* gy, double* gz, void* stream) {
   if (!h || !in || !gx || !gy || !gz) return PG_EINVAL;
+  if (h->c.coordsys >= PG_SPHERICAL) return grad_metric(h, in, gx, gy, gz, stream);
   int rc = grad(h->c, in, gx, gy, gz, stream);
   if (!rc && h->c.coordsys == PG_CYLINDRICAL)  // operators.f90:193-196: dfdy / r
     rc = cyl(h, CYL_DIV_R, gy, nullptr, nullptr, nullptr, nullptr, gy, stream);
@@ -1413,6 +1684,7 @@ int pg_divt(pg_handle* h, const double* const* f, double* const* out, void* stre
         return PG_EINVAL;
       }
   }
+  if (h->c.coordsys >= PG_SPHERICAL) return divt_metric(h, f, out, stream);
   return divt(h, f, out, stream);
 }
 
@@ -1426,12 +1698,31 @@ int pg_div(pg_handle* h, const double* fx, const double* fy, const double* fz, d
     set_error("pg_div: out must not alias fy or fz");
     return PG_EINVAL;
   }
+  if (h->c.coordsys >= PG_SPHERICAL) return div_metric(h, fx, fy, fz, out, stream);
   return divergence(h->c, fx, fy, fz, out, stream);
 }
 
 int pg_mesh(pg_handle* h, int which, double* out, void* stream) {
-  if (!h || !out || which < 0 || which > 7) return PG_EINVAL;
+  if (!h || !out || which < 0 || which > PG_MESH_DC_DZ) return PG_EINVAL;
   const GridInfo& g = h->g;
+  if (g.coordsys >= PG_SPHERICAL) {
+    if (which >= PG_MESH_DET && g.coordsys != PG_CURVILINEAR) {
+      set_error("pg_mesh: det J and the inverse Jacobian exist on curvilinear grids only");
+      return PG_EINVAL;
+    }
+    const cudaError_t e = cudaMemcpyAsync(out, h->c.mf[which], (size_t)h->c.npts * sizeof(double),
+                                          cudaMemcpyDeviceToDevice, (cudaStream_t)stream);
+    if (e != cudaSuccess) {
+      set_error("pg_mesh: %s", cudaGetErrorString(e));
+      return PG_ECUDA;
+    }
+    return PG_OK;
+  }
+  if (which >= PG_MESH_DET) {
+    set_error("pg_mesh: det J and the inverse Jacobian exist on curvilinear grids only");
+    return PG_EINVAL;
+  }
+  if (which == PG_MESH_CELLVOL_S || which == PG_MESH_CELLVOL_G) which = PG_MESH_CELLVOL;  // mesh.f90:384-386
   if (g.coordsys == PG_CYLINDRICAL && (which == PG_MESH_D2 || which == PG_MESH_GRIDLEN || which == PG_MESH_CELLVOL)) {
     // mesh.f90:213-225: d2 = r dy, GridLen and CellVol vary with the radius
     const int op = which == PG_MESH_D2 ? CYL_D2 : (which == PG_MESH_GRIDLEN ? CYL_GRIDLEN : CYL_CELLVOL);
@@ -1459,6 +1750,25 @@ int pg_courant(pg_handle* h, const double* u, const double* v, const double* w, 
     set_error("pg_courant: cylindrical grids with more than one point in angle are not supported");
     return PG_EINVAL;
   }
+  if (g.coordsys >= PG_SPHERICAL) {  // the rate on the mesh fields, its maximum, the reciprocal
+    MetricArgs A = margs(h, MET_COURANT);
+    A.in[0] = u;
+    A.in[1] = v;
+    A.in[2] = w;
+    A.in[3] = c;
+    A.s0 = vconst;
+    A.s1 = wconst;
+    A.out[0] = h->c.cyl[0];
+    int rc = launch_metric(A, stream);
+    if (!rc) rc = launch_reduce(1, h->c.cyl[0], h->c.npts, h->c.partial, out, stream);
+    if (!rc) {
+      MetricArgs R = margs(h, MET_RECIP);
+      R.n = 1;
+      R.out[0] = out;
+      rc = launch_metric(R, stream);
+    }
+    return rc;
+  }
   const double gl = std::min(std::min(g.dm[0], g.dm[1]), g.dm[2]);
   return launch_courant(u, v, w, c, vconst, wconst, g.dm, gl, h->c.npts, h->c.partial, out, stream);
 }
@@ -1469,6 +1779,11 @@ int pg_diff(pg_handle* h, const double* bulk, const double* rho, double* out, vo
   if (g.coordsys == PG_CYLINDRICAL && g.n[1] > 1) {
     set_error("pg_diff: cylindrical grids with more than one point in angle are not supported");
     return PG_EINVAL;
+  }
+  if (g.coordsys >= PG_SPHERICAL) {  // the rate on the GridLen field, its minimum
+    int rc = metric(h, MET_DIFF, {bulk, rho}, {h->c.cyl[0]}, stream);
+    if (!rc) rc = launch_reduce(2, h->c.cyl[0], h->c.npts, h->c.partial, out, stream);
+    return rc;
   }
   const double gl = std::min(std::min(g.dm[0], g.dm[1]), g.dm[2]);
   return launch_diff(bulk, rho, gl, h->c.npts, h->c.partial, out, stream);

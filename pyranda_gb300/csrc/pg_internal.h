@@ -213,6 +213,54 @@ enum {
 int launch_cyl(int op, int64_t n, int nx, int ny, double x1, double dx, double dy, double dz, const double* a,
                const double* b, const double* c, const double* e, const double* f, double* out, void* stream);
 
+// Mesh fields of spherical and curvilinear grids (mesh.f90:35-50), in this
+// order in the handle: native coordinates, d1 d2 d3, GridLen, CellVol, the
+// filtered cell volumes, det J and the inverse Jacobian rows dA/dx dA/dy dA/dz,
+// dB/.., dC/.. (curvilinear grids only; they hold d(x,y,z)/d(A,B,C) until the
+// metric form inverts them).  The indices equal pg_mesh_var's.
+enum { MF_X, MF_Y, MF_Z, MF_D1, MF_D2, MF_D3, MF_GL, MF_CV, MF_CVS, MF_CVG, MF_DET, MF_J0, MF_COUNT = MF_J0 + 9 };
+
+// Pointwise forms of the non-Cartesian grids (pg_metric.cu).
+enum {
+  MET_SPH_MESH,       // spherical mesh fields from the point indices (s0 = Asp, s1 = Csp when ratio-zoned)
+  MET_NODES,          // node coordinates x1 + i (xn - x1) / (n - 1) into the coordinate fields
+  MET_CURV_METRIC,    // J slots -> inverse Jacobian, det J, d1 d2 d3, CellVol, GridLen
+  MET_SPH_GRAD,       // out[0..2] in place: (dx / d1) gx, gy / r, gz / (r sin(theta))
+  MET_CURV_GRAD,      // out[0..2] in place: (d/dA, d/dB, d/dC) -> (d/dx, d/dy, d/dz)
+  MET_SPH_DIV_PRE,    // out0 = r^2 in0, out1 = in1 sin(theta)
+  MET_SPH_DIV_POST,   // out0 = (in0 dx / d1) / r^2 + (in1 + in2) / (r sin(theta))
+  MET_CURV_DIV_PRE,   // out[r] = (in . grad of coordinate r) det J
+  MET_CURV_DIV_POST,  // out0 = (in0 + in1 + in2) / det J
+  MET_SPH_T_PRE,      // L = 2: out0 = r^2 in0, out1 = in1 / (1 / sin(theta)); L = 3: r^3 in0, in1 sin(theta)
+  MET_SPH_T_POST,     // spherical divT row L (0, 1, 2) from fA fB fC and three tensor components
+  MET_LAP_MUL,        // out0 = r^L in0
+  MET_LAP_X,          // out0 = in0 / r^L
+  MET_LAP_SIN,        // out0 = sin(theta) in0
+  MET_LAP_ADD_Y,      // out0 += in0 / r^2 (cylindrical) or in0 / (r^2 sin(theta)) (spherical)
+  MET_LAP_ADD_Z,      // out0 += in0 (cylindrical) or in0 / (r sin(theta))^2 (spherical)
+  MET_VOL_MUL,        // out0 = in0 CellVol
+  MET_VOL_DIV,        // out0 = in0 / in1
+  MET_RING,           // out0 = (first ? : max(out0, )) |in0| d_dir^L
+  MET_COURANT,        // out0 = the courant rate (in0..2 velocity, NULL = s0 / s1; in3 sound speed)
+  MET_DIFF,           // out0 = in1 GridLen^2 / max(1e-12, in0)
+  MET_RECIP,          // out0 = 1 / out0
+  MET_COUNT
+};
+struct MetricArgs {
+  int op = 0;
+  int64_t n = 0;
+  int nx = 1, ny = 1, nz = 1;
+  int coordsys = 0;
+  int dir = 0, L = 0, first = 0;
+  double x1f[3] = {0, 0, 0}, d[3] = {0, 0, 0};  // face coordinates and patch spacings
+  double x1[3] = {0, 0, 0}, xn[3] = {0, 0, 0};  // node extents
+  double s0 = 0.0, s1 = 0.0;
+  const double* in[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  double* out[3] = {nullptr, nullptr, nullptr};
+  double* mf[MF_COUNT] = {};
+};
+int launch_metric(const MetricArgs& A, void* stream);
+
 // Number of blocks used by the two-pass reductions (partial buffer length).
 constexpr int kReduceBlocks = 1024;
 // Reduction blocks per member of an ensemble.

@@ -105,13 +105,15 @@ def _plan_cache_put(key, plan, path=None):
 
 
 class Grid:
-    """A Cartesian pyranda patch on one GPU (parcop.f90:23-70 setup + setup_mesh)."""
+    """A pyranda patch on one GPU (parcop.f90:23-81 setup + setup_mesh / setup_mesh_x3)."""
 
     def __init__(self, n, periodic, x1, xn, precision="fp64", device=None, line_split=False, bc=None,
                  coordsys=0):
         """bc: per direction the (lower, upper) end codes of non-periodic directions,
         'NONE' (one-sided closures), 'SYMM' (symmetry plane) or 'XTND' (extended data);
-        coordsys: 0 Cartesian, 1 cylindrical (x = radius)."""
+        coordsys: 0 Cartesian, 1 cylindrical (x = radius), 2 spherical (x = radius,
+        y = polar angle, z = azimuth), 3 curvilinear (coordinates by set_mesh_coords),
+        4 spherical with ratio-zoned radii."""
         if not torch.cuda.is_available():
             raise RuntimeError("pyranda_gb300 needs a CUDA device; there is no CPU fallback")
         self.lib = _lib.load()
@@ -347,9 +349,18 @@ class Grid:
         return out
 
     def mesh(self, which):
+        """pg_mesh_var: 0-2 native coordinates, 3-5 d1 d2 d3, 6 GridLen, 7 CellVol,
+        8-9 the filtered cell volumes, 10 det J, 11-19 dA/dx .. dC/dz (curvilinear)."""
         out = self.empty()
         _lib.check(self.lib.pg_mesh(self.h, which, _ptr(out), _stream()), "pg_mesh")
         return out
+
+    def set_mesh_coords(self, x, y, z, mesh_periodic=True):
+        """setup_mesh_x3 (parcop.f90:73-81): the coordinates of a curvilinear grid and
+        its metrics; mesh_periodic is pyranda's 'periodicGrid' option."""
+        x, y, z = self.field(x), self.field(y), self.field(z)
+        _lib.check(self.lib.pg_set_mesh_coords(self.h, _ptr(x), _ptr(y), _ptr(z), 1 if mesh_periodic else 0,
+                                               _stream()), "pg_set_mesh_coords")
 
     # ---------------------------------------------------- time step and reductions
     def scalar(self):

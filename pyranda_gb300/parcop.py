@@ -17,8 +17,10 @@ Fortran layout (kept on the device).  As in parcop, the (patch, level) pair
 selected by ``set_patch`` is the active grid; ``setup`` makes the new grid
 active (objects.f90:35-49, :77-89).
 
-Scope: one GPU (px = py = pz = 1), Cartesian meshes (coordsys 0), boundary
-codes PERI and NONE.  Other codes raise instead of silently misbehaving.
+Scope: one GPU (px = py = pz = 1); every coordinate system (0 Cartesian,
+1 cylindrical, 2 spherical, 3 curvilinear with ``setup_mesh_x3``, 4
+ratio-zoned spherical); boundary codes PERI, NONE, SYMM and XTND.  A
+decomposition over several processes raises instead of silently misbehaving.
 """
 import numpy
 import torch
@@ -36,22 +38,28 @@ class _Parcop:
               bx1, bxn, by1, byn, bz1, bzn):
         if px * py * pz != 1:
             raise ValueError("one GPU holds the whole grid: px*py*pz must be 1")
-        if coordsys != 0:
-            raise ValueError("only Cartesian meshes (coordsys 0) are supported")
-        per = []
+        per, bc = [], []
         for lo, hi in ((bx1, bxn), (by1, byn), (bz1, bzn)):
             lo, hi = str(lo).strip().upper(), str(hi).strip().upper()
-            if "SYMM" in (lo, hi) or "XTND" in (lo, hi):
-                raise ValueError("boundary codes SYMM/XTND are not supported (PERI and NONE are)")
+            for b in (lo, hi):
+                if b not in ("PERI", "NONE", "SYMM", "XTND"):
+                    raise ValueError("boundary code %r is not PERI, NONE, SYMM or XTND" % b)
             per.append(lo == "PERI")
-        g = Grid((nx, ny, nz), per, (x1, y1, z1), (xn, yn, zn))
+            bc.append(tuple("NONE" if b == "PERI" else b for b in (lo, hi)))
+        g = Grid((nx, ny, nz), per, (x1, y1, z1), (xn, yn, zn), bc=bc, coordsys=int(coordsys))
         self._grids[(patch, level)] = g
         self._active = g
 
     def setup_mesh(self, patch, level):
-        """parcop.f90:64-70: the Cartesian mesh is generated on demand."""
+        """parcop.f90:64-70: the mesh of every coordinate system but the curvilinear one
+        is generated by setup."""
         if (patch, level) not in self._grids:
             raise KeyError("patch %s level %s was not set up" % (patch, level))
+
+    def setup_mesh_x3(self, patch, level, x1, x2, x3, meshPer):
+        """parcop.f90:73-81: the coordinates of a curvilinear patch and its metrics."""
+        g = self._grids[(patch, level)]
+        g.set_mesh_coords(*[self._in_for(g, v) for v in (x1, x2, x3)], mesh_periodic=bool(meshPer))
 
     def set_patch(self, patch, level):
         self._active = self._grids[(patch, level)]
@@ -64,6 +72,12 @@ class _Parcop:
         if self._active is None:
             raise RuntimeError("parcop.setup has not been called")
         return self._active
+
+    @staticmethod
+    def _in_for(g, v):
+        if isinstance(v, torch.Tensor):
+            return g.field(v)
+        return g.field(numpy.asfortranarray(numpy.asarray(v, dtype=numpy.float64)))
 
     def _in(self, v):
         g = self._g()
@@ -174,12 +188,14 @@ class _Parcop:
     def mesh_getcellvol(self, nx=None, ny=None, nz=None):  # parcop.f90:179-184
         return self._mesh(7)
 
-    def getvar(self, vname, nx=None, ny=None, nz=None):  # parcop.f90:84-128 (Cartesian names)
-        table = {"x": 0, "y": 1, "z": 2, "d1": 3, "d2": 4, "d3": 5}
+    _VARS = {"x": 0, "y": 1, "z": 2, "d1": 3, "d2": 4, "d3": 5, "dAx": 11, "dAy": 12, "dAz": 13, "dBx": 14,
+             "dBy": 15, "dBz": 16, "dCx": 17, "dCy": 18, "dCz": 19, "dtJ": 10}
+
+    def getvar(self, vname, nx=None, ny=None, nz=None):  # parcop.f90:84-128
         key = str(vname).strip()
-        if key not in table:
-            raise ValueError("mesh variable %r is not available on a Cartesian mesh" % key)
-        return self._mesh(table[key])
+        if key not in self._VARS:
+            raise ValueError("mesh variable %r is not one of parcop's getVar names" % key)
+        return self._mesh(self._VARS[key])
 
     # single-process communicators (comm.f90): every rank id is 0
     def commx(self):

@@ -263,8 +263,8 @@ class pyrandaSim:
         opts = defaultMeshOptions()
         opts.update(meshOptions)
         coordsys = int(opts.get("coordsys", 0))
-        if coordsys not in (0, 1):
-            raise ValueError("coordsys %d: Cartesian (0) and cylindrical (1) meshes are supported" % coordsys)
+        if coordsys not in (0, 1, 2, 3, 4):
+            raise ValueError("coordsys %d is not one of pyranda's coordinate systems 0-4" % coordsys)
         # pyrandaMPI.py:101-131: a symmetric end of a non-periodic direction is SYMM, else NONE
         sym = opts["symmetric"]
         bc = tuple(tuple("SYMM" if (sym[d][e] and not opts["periodic"][d]) else "NONE" for e in range(2))
@@ -320,13 +320,42 @@ class pyrandaSim:
             exec(fortran3d(line, dict(smap)), ns, ns)
         return opts
 
+    def _curvilinear_coords(self):
+        """pyrandaMesh.py:92-131: node coordinates numpy.linspace(x1, xn, nn) per
+        direction, replaced point by point by meshOptions['function'](i, j, k)."""
+        opts = self.meshOptions
+        lin = [numpy.linspace(opts["x1"][d], opts["xn"][d], num=[self.nx, self.ny, self.nz][d]) for d in range(3)]
+        x, y, z = numpy.meshgrid(*lin, indexing="ij")
+        fn = opts.get("function")
+        if fn:
+            for i in range(self.nx):
+                for j in range(self.ny):
+                    for k in range(self.nz):
+                        x[i, j, k], y[i, j, k], z[i, j, k] = fn(i, j, k)
+        return x, y, z
+
     def _make_mesh(self):
         g = self.grid
+        if self.mesh.coordsys == 3:
+            x, y, z = self._curvilinear_coords()
+            g.set_mesh_coords(x, y, z, self.meshOptions.get("periodicGrid", True))
         self.mesh.coords = [pyrandaVar("x", "mesh"), pyrandaVar("y", "mesh"), pyrandaVar("z", "mesh")]
         for i, c in enumerate(self.mesh.coords):
             c.sim = self
             c.allocated = True
             c.data = g.mesh(i)
+        # pyrandaMesh.py:151-191: coordinates in x-y-z space, the native ones kept beside them
+        self.mesh.coordsNative = None
+        if self.mesh.coordsys in (1, 2, 4):
+            native = [g.mesh(i) for i in range(3)]
+            self.mesh.coordsNative = native
+            r, a, b = native
+            if self.mesh.coordsys == 1:
+                xyz = (r * torch.cos(a), r * torch.sin(a), b)
+            else:
+                xyz = (r * torch.sin(a) * torch.cos(b), r * torch.sin(a) * torch.sin(b), r * torch.cos(a))
+            for c, v in zip(self.mesh.coords, xyz):
+                c.data = g.field(v)
         self.mesh.shape = [self.nx, self.ny, self.nz]
         self.mesh.nn = self.meshOptions["nn"]
         self.mesh.d1 = g.mesh(3)
@@ -627,11 +656,14 @@ class pyrandaSim:
     def filterz(self, val):
         return self.grid.filter("spectral", val, 2)
 
+    # parcop.f90:84-128 getVar: native coordinates, spacings, det J and the inverse Jacobian
+    _MESH_VARS = {"x": 0, "y": 1, "z": 2, "d1": 3, "d2": 4, "d3": 5, "dtJ": 10, "dAx": 11, "dAy": 12,
+                  "dAz": 13, "dBx": 14, "dBy": 15, "dBz": 16, "dCx": 17, "dCy": 18, "dCz": 19}
+
     def getVar(self, vname):
-        table = {"x": 0, "y": 1, "z": 2, "d1": 3, "d2": 4, "d3": 5}
-        if vname not in table:
-            raise ValueError("mesh variable %s is not available on Cartesian meshes" % vname)
-        return self.grid.mesh(table[vname])
+        if vname not in self._MESH_VARS:
+            raise ValueError("mesh variable %s is not one of %s" % (vname, sorted(self._MESH_VARS)))
+        return self.grid.mesh(self._MESH_VARS[vname])
 
     # -------------------------------------------------------------- viz dumps
     def write(self, wVars=None):

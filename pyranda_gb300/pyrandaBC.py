@@ -13,11 +13,11 @@ the reference are the non-periodic tests.
   farfield (Riemann)       pyrandaBC.py:524-745
 
 slip and farfield take the boundary normal from the mesh metrics
-(pyrandaBC.py:202-264), which parcop allocates for curvilinear meshes only
-(mesh.f90:113-115).  On the Cartesian meshes built here the same cross
-product of the metric rows is a unit axis vector: +x on the x ends, -y on
-the y ends, +z on the z ends (d(x,y,z)/d(A,B,C) = diag(dx, dy, dz) in
-pyrandaBC.py:233-264), and that is the normal used.
+(pyrandaBC.py:198-264), which parcop allocates for curvilinear meshes only
+(mesh.f90:113-115).  On curvilinear meshes it is the cross product of the
+metric rows rebuilt from the inverse Jacobian; on the other meshes the same
+cross product is a unit axis vector: +x on the x ends, -y on the y ends, +z
+on the z ends (d(x,y,z)/d(A,B,C) = diag(dx, dy, dz)).
 """
 import math
 
@@ -145,8 +145,39 @@ class pyrandaBC(pyrandaPackage):
 
     # ------------------------------------------------------------ slip
     def slipbc(self, var, direction):
+        """pyrandaBC.py:190-196: each entry of var is one velocity, the list of
+        its component names (a single name is a one-component velocity)."""
         for d in self._listed(direction):
-            self.slipvelbc(self._listed(var), d)
+            for v in self._listed(var):
+                self.slipvelbc(self._listed(v), d)
+
+    def getNorms(self, direction, k):
+        """The unit boundary normal on plane k of a boundary (pyrandaBC.py:198-264),
+        cached per boundary like the reference's BCdata entries."""
+        if getattr(self.pyranda.mesh, "coordsys", 0) != 3:
+            return _CART_NORMAL[direction[0]]
+        key = "normal-%s" % direction
+        if key not in self.BCdata:
+            g = self.pyranda.getVar
+            dAdx, dAdy, dAdz = g("dAx"), g("dAy"), g("dAz")
+            dBdx, dBdy, dBdz = g("dBx"), g("dBy"), g("dBz")
+            dCdx, dCdy, dCdz = g("dCx"), g("dCy"), g("dCz")
+            detJ = g("dtJ")
+            m = {"xA": (-dBdz * dCdy + dBdy * dCdz) * detJ, "xB": (dAdz * dCdy - dAdy * dCdz) * detJ,
+                 "xC": (-dAdz * dBdy + dAdy * dBdz) * detJ, "yA": (dBdz * dCdx - dBdx * dCdz) * detJ,
+                 "yB": (-dAdz * dCdx + dAdx * dCdz) * detJ, "yC": (dAdz * dBdx - dAdx * dBdz) * detJ,
+                 "zA": (-dBdy * dCdx + dBdx * dCdy) * detJ, "zB": (dAdy * dCdx - dAdx * dCdy) * detJ,
+                 "zC": (-dAdy * dBdx + dAdx * dBdy) * detJ}
+            t1, t2 = {"x": ("B", "C"), "y": ("A", "C"), "z": ("A", "B")}[direction[0]]
+            a1, a2, a3 = m["x" + t1], m["y" + t1], m["z" + t1]
+            b1, b2, b3 = m["x" + t2], m["y" + t2], m["z" + t2]
+            n1 = a2 * b3 - a3 * b2
+            n2 = -(a1 * b3 - a3 * b1)
+            n3 = a1 * b2 - a2 * b1
+            mag = torch.sqrt(n1 * n1 + n2 * n2 + n3 * n3)
+            grid = self.pyranda.grid
+            self.BCdata[key] = [grid.get_plane(n / mag, direction[0], k).clone() for n in (n1, n2, n3)]
+        return self.BCdata[key]
 
     def slipvelbc(self, velocity, direction):
         """Free slip: extrapolate the velocity components, remove the normal
@@ -158,7 +189,7 @@ class pyrandaBC(pyrandaPackage):
         if not self._owns(direction):
             return
         k = 0 if direction[1] == "1" else -1
-        nrm = _CART_NORMAL[direction[0]]
+        nrm = self.getNorms(direction, k)
         planes = [self._get(v, direction, k) for v in velocity]
         udotn = 0.0
         for q, u in enumerate(planes):
@@ -171,7 +202,7 @@ class pyrandaBC(pyrandaPackage):
 
     # ------------------------------------------------------------ farfield
     def getnormal(self, direction):
-        return _CART_NORMAL[direction[0]]
+        return self.getNorms(direction, 0 if direction[1] == "1" else -1)
 
     def Reimann(self, direction, Rhoref, Uref, Vref, Wref, Pref, gamma, rhoi, Ui, Vi, Wi, Pi):
         """Boundary state from the Riemann invariants of the interior and the

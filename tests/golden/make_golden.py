@@ -2,8 +2,9 @@
 
 Reads the reference test-case files as text (they are Python fragments that
 ``tests/run_tests.py`` executes) and writes ``reference_scalars.json``; copies
-the reference's profile baselines of the 2-D Euler and Kelvin-Helmholtz
-cases (``tests/baselines/*.dat``: two rows, x and the profile, compared by
+the reference's profile baselines of the 2-D Euler, cylindrical and
+spherical Sod, Kelvin-Helmholtz and curvilinear O-mesh cases
+(``tests/baselines/*.dat``: two rows, x and the profile, compared by
 ``tests/testObj.py:checkProfile``) next to it.  Run it where the reference
 tree is mounted, naming its root:
 
@@ -27,6 +28,9 @@ PROFILES = {  # test name -> baseline file (tests/cases/test2deuler.py:3-9)
     "euler-2d-128": "euler-2d-128.dat",
     "KH-2d-64": "KelvinHelmholtzKH-2d-64.dat",
     "euler-RZ-128": "euler-RZ-128.dat",
+    "euler-SPH-1D": "euler-SPH-1D.dat",
+    "euler-SPH-2D": "euler-SPH-2D.dat",
+    "cylinder_omesh-2d-64": "cylinder_omesh-2d-64.dat",  # tests/cases/testCylinder.py:33-37
 }
 
 

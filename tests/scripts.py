@@ -421,3 +421,158 @@ wgt = .5*(1.0-tanh( (rad-pi/2.0)/.1) )   # [0,1]
     x = _host(_meshx(ss))[:, 0, 0]
     p = _host(ss.variables["p"].data)[half, 0, :]
     return x, p
+
+
+SPH_DT = """
+:cs:  = sqrt( :p: / :rho: * :gamma: )
+:dt: = dt.courant(:u:,:v:,:w:,:cs:)
+"""
+
+SPH_IC = """rad = sqrt( (meshx-pi)**2  +  (meshy-0.0)**2 )
+:gamma: = 1.4
+wgt = .5*(1.0-tanh( (rad-pi/16.0)/.1) )   # [0,1]
+:Et:  = 1.0/(:gamma:-1.0) * (wgt*.9 + .1)
+:rho: = 1.0*wgt + (1.0-wgt)*.125
+"""
+
+
+def _native(ss, q):
+    """ss.mesh.coordsNative[q] (pyrandaMesh.py:176-191), on the host."""
+    return _host(ss.mesh.coordsNative[q] if hasattr(ss, "mesh") else ss.coordsNative[q])
+
+
+def _sph_run(ss, dt_max, tt):
+    time = 0.0
+    dt = dt_max
+    while tt > time:
+        time = ss.rk4(time, dt)
+        dt = min(dt_max, _f(ss.variables["dt"].data))
+        dt = min(dt, (tt - time))
+
+
+def euler_sph_1d(Sim, Npts, packages, **kw):
+    """examples/eulerSpherical1D.py N 1 (tests/cases/test2deuler.py euler-SPH-1D):
+    a spherical Sod problem on 4N radial points (coordsys 2, one point in theta
+    and phi) to t = 0.1, with the courant and diffusion limits; returns
+    (r, p), the profile the test compares."""
+    L = numpy.pi * 2.0
+    spike = numpy.pi / 16
+    Mpts = Npts * 4
+    x0 = L / Mpts
+    opts = {"coordsys": 2, "periodic": [False, False, True], "x1": [x0, numpy.pi / 2 - .01, 0 * numpy.pi - spike],
+            "xn": [L, numpy.pi / 2 + .01, 0 * numpy.pi + spike], "nn": [Mpts, 1, 1]}
+    ss = Sim("sod2dSpherical_1D", opts, **kw)
+    packages(ss)
+    eom = EULER_RZ_EOM + SPH_DT + ":dt: = numpy.minimum( :dt:, 0.1 * dt.diff(:beta:,:rho:) )\n"
+    eom += ":rhow: = :rhow: * 0.0\n"
+    eom += "bc.const(['u'],['x1'],0.0) \n"
+    eom += "bc.extrap(['rho','p'],['x1'],order=1) \n"
+    eom += ":rhou: = :rho:*:u: \n"
+    eom += ":Et: = :p:/( :gamma: - 1.0 ) + .5*:rho:*(:u:*:u: + :w:*:w:) \n"
+    ss.EOM(eom)
+    ss.setIC(SPH_IC)
+    _sph_run(ss, 1.0 / ss.nx * 0.05, 0.1)
+    p = _host(ss.variables["p"].data)[:, 0, 0]
+    return _native(ss, 0)[:, 0, 0], p
+
+
+def euler_sph_2d(Sim, Npts, packages, **kw):
+    """examples/eulerSpherical.py N 1 (tests/cases/test2deuler.py euler-SPH-2D):
+    the spherical Sod problem on 4N radii x N angles phi (coordsys 2) to t =
+    0.1; returns (r, rho averaged over phi), the profile the test compares."""
+    L = numpy.pi * 2.0
+    spike = numpy.pi / 16
+    opts = {"coordsys": 2, "periodic": [False, False, True], "x1": [L / 10, numpy.pi / 2 - .01, 0 * numpy.pi - spike],
+            "xn": [L, numpy.pi / 2 + .01, 0 * numpy.pi + spike], "nn": [Npts * 4, 1, Npts]}
+    ss = Sim("sod2dSpherical", opts, **kw)
+    packages(ss)
+    ss.EOM(EULER_RZ_EOM + "bc.const(['u'],['x1','xn'],0.0)\n" + SPH_DT)
+    ss.setIC(SPH_IC)
+    _sph_run(ss, 1.0 / ss.nx * 0.05, 0.1)
+    rho = _host(ss.variables["rho"].data)[:, 0, :].mean(axis=1)
+    return _native(ss, 0)[:, 0, int(Npts / 2)], rho
+
+
+OMESH_EOM = """
+ddt(:rho:)  =  -div(:rho:*:u:,  :rho:*:v:)
+ddt(:rhou:) =  -div(:rhou:*:u: + :p: - :tau:, :rhou:*:v:)
+ddt(:rhov:) =  -div(:rhov:*:u:, :rhov:*:v: + :p: - :tau:)
+ddt(:Et:)   =  -div( (:Et: + :p: - :tau:)*:u: , (:Et: + :p: - :tau:)*:v:  )
+:rho:       =  fbar( :rho:  )
+:rhou:      =  fbar( :rhou: )
+:rhov:      =  fbar( :rhov: )
+:Et:        =  fbar( :Et:   )
+:u:         =  :rhou: / :rho:
+:v:         =  :rhov: / :rho:
+:p:         =  ( :Et: - .5*:rho:*(:u:*:u: + :v:*:v:) ) * ( :gamma: - 1.0 )
+:div:       =  div(:u:,:v:)
+:beta:      =  gbar( ring(:div:) * :rho: ) * 7.0e-2
+:tau:       = :beta:*:div:
+bc.extrap(['u','v','rho','p'],['yn'])
+bc.const(['u'],['yn'],u0)
+bc.const(['v'],['yn'],0.0)
+bc.extrap(['rho','p'],['y1'])
+bc.slip([ ['u','v']  ],['y1'])
+:Et:  = :p: / ( :gamma: - 1.0 )  + .5*:rho:*(:u:*:u: + :v:*:v:)
+:rhou: = :rho:*:u:
+:rhov: = :rho:*:v:
+:cs:  = sqrt( :p: / :rho: * :gamma: )
+:dt: = dt.courant(:u:,:v:,:w:,:cs:)
+:dtB: = dt.diff(:beta:,:rho:)
+:umag: = sqrt( :u:*:u: + :v:*:v: )
+"""
+
+OMESH_IC = """
+:gamma: = 1.4
+:R: = 1.0
+:cp: = :R: / (1.0 - 1.0/:gamma: )
+:cv: = :cp: - :R:
+rad = sqrt( meshx**2  +  meshy**2 )
+:rho: = 1.0 + 3d()
+:p:  =  1.0 + 3d()
+:u: = mach * sqrt( :p: / :rho: * :gamma:)
+:v: = 0.0 + 3d()
+:Et: = :p:/( :gamma: - 1.0 ) + .5*:rho:*(:u:*:u: + :v:*:v:)
+:rhou: = :rho:*:u:
+:rhov: = :rho:*:v:
+:cs:  = sqrt( :p: / :rho: * :gamma:)
+:dt: = dt.courant(:u:,:v:,:w:,:cs:)
+"""
+
+
+def cylinder_omesh(Sim, Npts, packages, tt=3.0, **kw):
+    """examples/cylinder_curv2.py N 1 (tests/cases/testCylinder.py
+    cylinder_omesh-2d-64): Mach 1.5 flow past a cylinder on a curvilinear
+    O-mesh (coordsys 3; periodic around, slip wall at the cylinder, inflow
+    and extrapolation at the far edge) to t = 3; returns (x, |u|) along the
+    middle radial line j = N/2, the profile the test compares."""
+    L = numpy.pi * 2.0
+    Lp = L * (Npts - 1.0) / Npts
+    Ri, Rf = 1.0, 10.0
+    NX = NY = Npts
+
+    def cyl_mesh(i, j, k):
+        theta = float(i) / float(NX) * 2.0 * numpy.pi
+        r = float(j) / float(NY - 1) * (Rf - Ri) + Ri
+        return r * numpy.cos(theta), r * numpy.sin(theta), 0.0
+
+    opts = {"coordsys": 3, "function": cyl_mesh, "periodic": [True, False, False], "periodicGrid": False,
+            "x1": [-2 * Lp, -2 * Lp, 0.0], "xn": [2 * Lp, 2 * Lp, Lp], "nn": [NX, NY, 1]}
+    ss = Sim("cylinder_omesh", opts, **kw)
+    packages(ss)
+    rho0, p0, gamma, mach = 1.0, 1.0, 1.4, 1.5
+    u0 = numpy.sqrt(p0 / rho0 * gamma) * mach
+    ss.EOM(OMESH_EOM.replace("u0", str(u0)).replace("p0", str(p0)).replace("rho0", str(rho0)))
+    ss.setIC(OMESH_IC.replace("mach", str(mach)))
+    time = 0.0
+    CFL = 0.8
+    dt = _f(ss.variables["dt"].data) * CFL * .1
+    while tt > time:
+        time = ss.rk4(time, dt)
+        dt = _f(ss.variables["dt"].data) * CFL
+        dt = min(dt, 1.1 * dt)
+        dt = min(0.2 * _f(ss.variables["dtB"].data), dt)
+        dt = min(dt, (tt - time))
+    x = _host(_meshx(ss))[:, :, 0]
+    v = _host(ss.variables["umag"].data)[:, :, 0]
+    return x[:, int(NY / 2)], v[:, int(NY / 2)]

@@ -73,7 +73,7 @@ def test_grid_codes_checked_before_any_cuda_call():
     h = ctypes.c_void_p()
     assert lib.pg_create(ctypes.byref(grid(bc=(1, 0, 7))), ctypes.byref(h)) == _lib.PG_EINVAL
     assert b"pg_bc" in lib.pg_last_error()
-    assert lib.pg_create(ctypes.byref(grid(coordsys=2)), ctypes.byref(h)) == _lib.PG_EINVAL
+    assert lib.pg_create(ctypes.byref(grid(coordsys=5)), ctypes.byref(h)) == _lib.PG_EINVAL
     assert b"coordsys" in lib.pg_last_error()
     assert lib.pg_create(ctypes.byref(grid(n0=0)), ctypes.byref(h)) == _lib.PG_EBADSHAPE
     assert lib.pg_create(ctypes.byref(grid(precision=9)), ctypes.byref(h)) == _lib.PG_EINVAL

@@ -45,7 +45,7 @@ def test_symm_mirrors_the_next_planes(anti):
 def test_slip_removes_the_normal_velocity():
     s = _sim()
     u0 = {k: s.variables[k].data.copy() for k in ("u", "v", "w")}
-    s.packages["BC"].slipbc(["u", "v", "w"], ["y1", "xn"])
+    s.packages["BC"].slipbc([["u", "v", "w"]], ["y1", "xn"])   # one velocity of three components
     d = s.variables
     assert numpy.all(d["v"].data[:, 0, :] == 0.0)          # y1: the normal is -y
     assert numpy.all(d["u"].data[-1, :, :] == 0.0)         # xn: the normal is +x

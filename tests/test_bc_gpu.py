@@ -54,7 +54,7 @@ def test_bc_conditions_match_oracle(oracle):
         lambda b: b.exitbc(["w"], ["x1", "yn"], True),
         lambda b: b.symm(["rho"], ["x1", "zn"]),
         lambda b: b.symm(["u"], ["y1"], True, 2),
-        lambda b: b.slipbc(["u", "v", "w"], ["x1", "xn", "y1", "yn"]),
+        lambda b: b.slipbc([["u", "v", "w"]], ["x1", "xn", "y1", "yn"]),
     ]
     for k, f in enumerate(steps):
         f(bs)

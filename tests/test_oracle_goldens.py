@@ -135,6 +135,27 @@ def test_euler_rz_profile(oracle):
     assert scripts.profile_error(path, x, p) < 1e-10
 
 
+@pytest.mark.parametrize("name,run", [
+    ("euler-SPH-1D", lambda o: scripts.euler_sph_1d(o.OracleSim, 128, _bc_ts)),
+    ("euler-SPH-2D", lambda o: scripts.euler_sph_2d(o.OracleSim, 32, _bc_ts)),
+    ("cylinder_omesh-2d-64", lambda o: scripts.cylinder_omesh(o.OracleSim, 64, _bc_ts)),
+])
+def test_spherical_and_curvilinear_profiles(oracle, name, run):
+    """tests/cases/test2deuler.py euler-SPH-1D / euler-SPH-2D (spherical
+    coordinates: mesh.f90:169-244, the spherical div / divT of
+    operators.f90:64-76, :147-173, the filter of CellVol-weighted fields over
+    the filtered cell volume :884-889, ring and the time-step limits on the
+    d1 d2 d3 and GridLen fields) and tests/cases/testCylinder.py
+    cylinder_omesh-2d-64 (a curvilinear O-mesh: the Jacobian of the supplied
+    coordinates, mesh.f90:245-358, the metric div, the slip wall with the
+    metric normal, pyrandaBC.py:198-264, and the curvilinear courant limit,
+    pyrandaTimestep.py:45-56) against the reference's baseline files."""
+    x, v = run(oracle)
+    path = os.path.join(GOLDEN_DIR, name + ".dat")
+    assert numpy.abs(x - numpy.loadtxt(path)[0]).max() < 1e-12
+    assert scripts.profile_error(path, x, v) < 1e-10
+
+
 def test_symmetry_plane_closures_known_answers(oracle):
     """SYMM ends (stencils.f90:2390-2453): with a symmetry plane half a
     spacing below the first point, the folded closures of a symmetric field

@@ -400,3 +400,26 @@ def test_euler_rz_profile_golden(oracle):
     diff = float(numpy.abs(p - po).max() / numpy.abs(po).max())
     print("euler-RZ-128: profile error %.2e, max difference from the oracle %.2e" % (err, diff))
     assert diff <= 1e-10, diff
+
+
+@pytest.mark.parametrize("name,run", [
+    ("euler-SPH-1D", lambda S, pk: scripts.euler_sph_1d(S, 128, pk, silent=True)),
+    ("euler-SPH-2D", lambda S, pk: scripts.euler_sph_2d(S, 32, pk, silent=True)),
+    ("cylinder_omesh-2d-64", lambda S, pk: scripts.cylinder_omesh(S, 64, pk, silent=True)),
+])
+def test_spherical_and_curvilinear_profile_goldens(name, run):
+    """tests/cases/test2deuler.py euler-SPH-1D / euler-SPH-2D and
+    tests/cases/testCylinder.py cylinder_omesh-2d-64: the GPU pyrandaSim on
+    spherical grids and on a curvilinear O-mesh (supplied coordinates, metric
+    div, slip wall with the metric normal, curvilinear courant limit)
+    reproduces the reference's profiles within the reference's tolerance 1e-4
+    and, as the oracle reproduces each file to 1e-13, to 1e-8 -- rounding
+    differences grown over 256 to 1025 RK steps."""
+    from pyranda_gb300 import pyrandaSim
+    path = os.path.join(GOLDEN_DIR, name + ".dat")
+    x, v = run(pyrandaSim, _bc_ts)
+    assert numpy.abs(x - numpy.loadtxt(path)[0]).max() < 1e-12
+    err = scripts.profile_error(path, x, v)
+    print("%s: profile error %.2e" % (name, err))
+    assert err < 1.0e-4, err
+    assert err < 1.0e-8, err
