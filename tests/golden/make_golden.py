@@ -20,6 +20,10 @@ CASES = {
     "testUnit.py": ["unit-test-3D"],
     "testTaylorGreen.py": ["taylorgreen"],
     "testShuOsher.py": ["shu-osher-CR"],
+    "testHeat1D.py": ["heat1D-analytic-16", "heat1D-analytic-32", "heat1D-analytic-64", "heat1D-analytic-128",
+                      "heat1D-analytic-256"],
+    "testIntegration.py": ["integration-25", "integration-50", "integration-100", "integration-200",
+                           "integration-400"],
 }
 
 

@@ -576,3 +576,63 @@ def cylinder_omesh(Sim, Npts, packages, tt=3.0, **kw):
     x = _host(_meshx(ss))[:, :, 0]
     v = _host(ss.variables["umag"].data)[:, :, 0]
     return x[:, int(NY / 2)], v[:, int(NY / 2)]
+
+
+def heat_1d(Sim, Npts, packages, **kw):
+    """examples/heat1D.py N 1 (tests/cases/testHeat1D.py heat1D-analytic-N):
+    the heat equation ddt(phi) = c lap(phi) on a one-sided line with constant
+    end values, started from its linear steady state and run 500 steps;
+    returns sum |phi - analytic| (the golden is 0 within 1e-4)."""
+    L = numpy.pi * 2.0
+    Lp = L * (Npts - 1.0) / Npts
+    opts = {"coordsys": 0, "periodic": [False, True, True], "x1": [0.0, 0.0, 0.0], "xn": [Lp, Lp, Lp],
+            "nn": [Npts, 1, 1]}
+    ss = Sim("heat_equation", opts, **kw)
+    packages(ss)
+    ss.EOM("""
+ddt(:phi:)  =  :c: * lap(:phi:)
+bc.const(['phi'],['x1'],2.0)
+bc.const(['phi'],['xn'],1.0)
+""")
+    ss.setIC("""
+xnn = meshx[-1,0,0]
+:phi: = 1.0 + 1.0*(xnn - meshx)/xnn
+:c:   = 1.0
+""")
+    x = _host(_meshx(ss))[:, 0, 0]
+    dt_max = L / Npts * .005
+    tt = dt_max * 500
+    dt = dt_max
+    time = 0.0
+    while tt > time:
+        time = ss.rk4(time, dt)
+        dt = min(dt_max, (tt - time))
+    xnn = x[-1]
+    anl = 1.0 + 1.0 * (xnn - x) / xnn
+    return float(numpy.sum(numpy.abs(anl - _host(ss.variables["phi"].data)[:, 0, 0])))
+
+
+def integration(Sim, Npts, **kw):
+    """examples/intTest.py N 1 (tests/cases/testIntegration.py integration-N):
+    ddt(a) = a and ddt(b) = cos(6 simtime) on one point with dt = 1/N to
+    t = 1; returns sum |a - (1 - a0 + e^t)| over the steps, which measures
+    the LSRK(5,4) scheme and its stage times."""
+    ss = Sim("integralTests", "xdom = (0.0 , 1.0 , 1 )", **kw)
+    ss.EOM("""
+ddt(:a:)  =  :a:
+ddt(:b:)  =  cos( 6.0*simtime )
+""")
+    a0, b0 = 1.0, 0.0
+    ss.setIC("""
+:a: = %s
+:b: = %s
+""" % (a0, b0))
+    dt = 1.0 / float(Npts)
+    time = 0.0
+    tt, aa = [time], [a0]
+    while time < 1.0:
+        time = ss.rk4(time, dt)
+        tt.append(time)
+        aa.append(float(_host(ss.variables["a"].data)[0, 0, 0]))
+    tt, aa = numpy.array(tt), numpy.array(aa)
+    return float(numpy.sum(numpy.abs(aa - (1.0 - a0 + numpy.exp(tt)))))

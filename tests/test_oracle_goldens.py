@@ -46,6 +46,25 @@ def test_shu_osher(oracle):
     assert _close(cr, "shu-osher-CR") < 1e-8
 
 
+@pytest.mark.parametrize("n", [16, 32, 64, 128, 256])
+def test_heat_1d(oracle, n):
+    """tests/cases/testHeat1D.py heat1D-analytic-N: lap on a one-sided line
+    (c10d2 closures) with bc.const ends keeps the linear steady state; the
+    golden 0.0 is absolute (tests/testObj.py:47-53), the restatement gives 0."""
+    err = scripts.heat_1d(oracle.OracleSim, n, lambda s: s.addPackage("BC"))
+    assert err < TOL and GOLD["heat1D-analytic-%d" % n]["value"] == 0.0
+    assert err < 1e-12, err
+
+
+@pytest.mark.parametrize("n", [25, 50, 100, 200, 400])
+def test_integration(oracle, n):
+    """tests/cases/testIntegration.py integration-N: the LSRK(5,4) scheme and
+    its stage times (pyranda.py:758-810) on ddt(a) = a, ddt(b) = cos(6 t).
+    Measured 3e-9 (N = 25) to 7e-5 (N = 400, where the summed error, 5e-11,
+    is at the rounding level of the 400 steps)."""
+    _close(scripts.integration(oracle.OracleSim, n), "integration-%d" % n)
+
+
 def test_dense_operator_matches_banded(oracle):
     """A . (A^-1 B v) = B v: the dense D = A^-1 B of the line evaluator
     reproduces the banded solve applied to a field (compact_basetype.f90:199-205)."""

@@ -423,3 +423,23 @@ def test_spherical_and_curvilinear_profile_goldens(name, run):
     print("%s: profile error %.2e" % (name, err))
     assert err < 1.0e-4, err
     assert err < 1.0e-8, err
+
+
+@pytest.mark.parametrize("n", [16, 64, 256])
+def test_heat_1d_golden(n):
+    """tests/cases/testHeat1D.py heat1D-analytic-N on the GPU: the Laplacian's
+    one-sided c10d2 rows with bc.const ends keep the linear steady state
+    (golden 0.0, absolute tolerance 1e-4; rounding only here)."""
+    from pyranda_gb300 import pyrandaSim, pyrandaBC
+    err = scripts.heat_1d(pyrandaSim, n, lambda s: s.addPackage(pyrandaBC(s)), silent=True)
+    assert GOLD["heat1D-analytic-%d" % n]["value"] == 0.0
+    assert err < 1e-10, err
+
+
+@pytest.mark.parametrize("n", [25, 50, 100, 200])
+def test_integration_golden(n):
+    """tests/cases/testIntegration.py integration-N on the GPU: the LSRK(5,4)
+    update and its stage times on one point.  (N = 400 is left to the oracle:
+    its summed error, 5e-11, is at the rounding level of the 400 steps.)"""
+    from pyranda_gb300 import pyrandaSim
+    _close(scripts.integration(pyrandaSim, n, silent=True), "integration-%d" % n)
