@@ -198,6 +198,11 @@ class _Parcop:
         return self._mesh(self._VARS[key])
 
     # single-process communicators (comm.f90): every rank id is 0
+    def commfrompy(self, comm):
+        """parcop.f90 commFromPy: the MPI communicator handed over from Python;
+        one process owns the GPU, so there is nothing to split."""
+        return None
+
     def commx(self):
         return 0
 
