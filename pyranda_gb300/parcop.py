@@ -198,10 +198,11 @@ class _Parcop:
         return self._mesh(self._VARS[key])
 
     # single-process communicators (comm.f90): every rank id is 0
-    def commfrompy(self, comm):
-        """parcop.f90 commFromPy: the MPI communicator handed over from Python;
-        one process owns the GPU, so there is nothing to split."""
-        return None
+    def commfrompy(self, patch, level, comm_list):
+        """parcop.f90:385-403 commFromPy: the seven communicators of a patch handed
+        over from Python; one process owns the GPU, so there is nothing to store."""
+        if (patch, level) not in self._grids:
+            raise KeyError("patch %s level %s was not set up" % (patch, level))
 
     def commx(self):
         return 0
