@@ -1368,7 +1368,8 @@ int og_divt(const og_handle* h, const double* const* f, double* const* out) {
   return 0;
 }
 
-// divV (Cartesian): operators.f90:38-53
+// divV: operators.f90:38-90 (Cartesian :47-53, cylindrical :55-64, spherical
+// :64-76 and curvilinear :77-90 in div_sph / div_curv)
 int og_div(const og_handle* h, const double* fx, const double* fy, const double* fz, double* out) {
   if (!h) return 1;
   const size_t np = (size_t)h->n[0] * h->n[1] * h->n[2];

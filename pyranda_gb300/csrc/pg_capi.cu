@@ -1159,7 +1159,8 @@ int divergence_cyl(pg_handle* h, const double* fx, const double* fy, const doubl
   return rc;
 }
 
-// divT (operators.f90:97-146): Cartesian and cylindrical.  f = {fxx, fxy, fxz,
+// divT (operators.f90:97-146): Cartesian and cylindrical (spherical and
+// curvilinear: divt_metric).  f = {fxx, fxy, fxz,
 // fyx, fyy, fyz, fzx, fzy, fzz}; out = {dfx, dfy, dfz}, distinct from f.
 int divt(pg_handle* h, const double* const* f, double* const* out, void* st) {
   Ctx& c = h->c;

@@ -295,14 +295,15 @@ class Grid:
         return out
 
     def laplacian(self, v, out=None):
-        """d2x + d2y + d2z (Cartesian)."""
+        """The Laplacian (operators.f90:513-559): d2x + d2y + d2z on Cartesian grids,
+        the cylindrical and spherical forms on those grids."""
         v = self.field(v)
         out = self._out(out)
         _lib.check(self.lib.pg_laplacian(self.h, _ptr(v), _ptr(out), _stream()), "pg_laplacian")
         return out
 
     def divT(self, fxx, fxy, fxz, fyx, fyy, fyz, fzx, fzy, fzz):
-        """Divergence of a tensor (operators.f90:97-146, Cartesian and cylindrical)."""
+        """Divergence of a tensor (operators.f90:97-181, every coordinate system)."""
         f = [self.field(x) for x in (fxx, fxy, fxz, fyx, fyy, fyz, fzx, fzy, fzz)]
         out = [self.empty() for _ in range(3)]
         fp = (ctypes.c_void_p * 9)(*[x.data_ptr() for x in f])
