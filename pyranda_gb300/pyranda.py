@@ -79,6 +79,13 @@ def pyrandaRestart(rootname, suffix=None, precision="fp64", device=None):
                                                       device=sim.grid.device)
             else:
                 sim.variables[name].data = sim.grid.field(numpy.ascontiguousarray(data[name]))
+    if sim.mesh.coordsys == 3 and all(k in serial["vars"] for k in ("meshx", "meshy", "meshz")):
+        # pyranda.py:1064-1069: a curvilinear mesh is rebuilt from the coordinates the
+        # restart holds, and the packages start again on it
+        sim._set_curvilinear(*[sim.variables[k].data for k in ("meshx", "meshy", "meshz")])
+        for pk in sim.packages.values():
+            pk.__init__(sim)
+            pk.get_sMap()
     return [sim, local]
 
 
@@ -334,11 +341,21 @@ class pyrandaSim:
                         x[i, j, k], y[i, j, k], z[i, j, k] = fn(i, j, k)
         return x, y, z
 
+    def _set_curvilinear(self, x, y, z):
+        """setup_mesh_x3 with these coordinates, then the mesh quantities of the simulation."""
+        g = self.grid
+        g.set_mesh_coords(x, y, z, self.meshOptions.get("periodicGrid", True))
+        if self.mesh.coords is not None:
+            for i, c in enumerate(self.mesh.coords):
+                c.data = g.mesh(i)
+            self.mesh.d1, self.mesh.d2, self.mesh.d3 = g.mesh(3), g.mesh(4), g.mesh(5)
+            self.mesh.GridLen, self.mesh.CellVol = g.mesh(6), g.mesh(7)
+
     def _make_mesh(self):
         g = self.grid
         if self.mesh.coordsys == 3:
             x, y, z = self._curvilinear_coords()
-            g.set_mesh_coords(x, y, z, self.meshOptions.get("periodicGrid", True))
+            self._set_curvilinear(x, y, z)
         self.mesh.coords = [pyrandaVar("x", "mesh"), pyrandaVar("y", "mesh"), pyrandaVar("z", "mesh")]
         for i, c in enumerate(self.mesh.coords):
             c.sim = self
