@@ -72,9 +72,12 @@ def pyrandaRestart(rootname, suffix=None, precision="fp64", device=None):
     sim.vizDumpHistory = serial.get("vizDumpHistory", [])
     data = restart.read_blocks(dump, serial, (sim.nx, sim.ny, sim.nz))
     scalars = set(serial.get("scalars", []))
+    pyscalars = set(serial.get("pyscalars", []))
     for name in serial["vars"]:
         if name in sim.variables:
-            if name in scalars:
+            if name in pyscalars:
+                sim.variables[name].data = float(data[name].flat[0])
+            elif name in scalars:
                 sim.variables[name].data = torch.full((), float(data[name].flat[0]), dtype=torch.float64,
                                                       device=sim.grid.device)
             else:
@@ -750,8 +753,12 @@ class pyrandaSim:
         for n in wVars:
             d = self.variables[n].data
             arrays[n] = self.variables[n].numpy() if isinstance(d, torch.Tensor) and d.dim() > 0 else _num(d)
-        # which variables were single numbers (an extra key; the reference's reader ignores it)
+        # which variables were single numbers, and which of those Python numbers rather than
+        # device scalars (extra keys; the reference's reader ignores them): torch divides by a
+        # Python number as a multiplication by its reciprocal, so a restart keeps the type
         serial["scalars"] = sorted(n for n in wVars if not isinstance(arrays[n], numpy.ndarray))
+        serial["pyscalars"] = sorted(n for n in serial["scalars"] if not isinstance(self.variables[n].data,
+                                                                                     torch.Tensor))
         restart.write_files(dump, serial, arrays, (nx, ny, nz))
         return dump
 
