@@ -40,7 +40,7 @@ def _rank(rank, world, port, out):
 
 def test_two_ranks_take_the_slowest_and_count_all_points():
     port = _free_port()
-    out = mp.Manager().dict()
+    out = mp.get_context("spawn").Manager().dict()   # no fork of this multi-threaded process
     mp.spawn(_rank, args=(2, port, out), nprocs=2, join=True)
     assert out[0] == out[1]
     job, value = out[0]
