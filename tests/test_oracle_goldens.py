@@ -213,3 +213,45 @@ def test_cylindrical_divergence_known_answers(oracle):
     zero = numpy.zeros(n)
     assert numpy.abs(g.div(r, zero, zero) - 2.0).max() < 1e-10
     assert numpy.abs(g.div(r * r, zero, zero) - 3.0 * r).max() < 1e-9
+
+
+def test_curvilinear_affine_map_known_answers(oracle):
+    """On an affine map x = M (A, B, C) + x0 the first-derivative operator is
+    exact (one-sided closures included), so the metrics of mesh.f90:245-358
+    are the inverse of M and det J is det M at every point; grad of a linear
+    field c . x is c, and the divergence of x e_x + 2 y e_y is 3."""
+    n = (20, 16, 12)
+    M = numpy.array([[1.0, 0.3, 0.1], [-0.2, 0.9, 0.05], [0.1, -0.15, 1.2]])
+    g = oracle.OracleGrid(n, (False, False, False), (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), coordsys=3)
+    A, B, C = numpy.meshgrid(*[numpy.linspace(0.0, 1.0, m) for m in n], indexing="ij")
+    x = M[0, 0] * A + M[0, 1] * B + M[0, 2] * C + 0.5
+    y = M[1, 0] * A + M[1, 1] * B + M[1, 2] * C - 0.25
+    z = M[2, 0] * A + M[2, 1] * B + M[2, 2] * C
+    g.set_mesh_x3(x, y, z, mesh_periodic=True)
+    Minv = numpy.linalg.inv(M)
+    for r in range(3):          # dA/dx dA/dy dA/dz, dB/.., dC/..
+        for c in range(3):
+            assert numpy.abs(g.mesh(11 + 3 * r + c) - Minv[r, c]).max() < 1e-12, (r, c)
+    assert numpy.abs(g.mesh(10) - numpy.linalg.det(M)).max() < 1e-12
+    cvec = (0.7, -1.3, 2.1)
+    grads = g.grad(cvec[0] * x + cvec[1] * y + cvec[2] * z)
+    for q in range(3):
+        assert numpy.abs(grads[q] - cvec[q]).max() < 1e-10, q
+    assert numpy.abs(g.div(x, 2.0 * y, numpy.zeros(n)) - 3.0).max() < 1e-10
+
+
+def test_spherical_known_answers(oracle):
+    """Spherical grids (mesh.f90:169-244, operators.f90:64-76, :197-201): the
+    divergence of r e_r is 3, the gradient of r^2 is 2 r e_r (the one-sided
+    closures are exact on polynomials of these degrees), and the mesh
+    d3 = r sin(theta) dz."""
+    n = (24, 10, 12)
+    g = oracle.OracleGrid(n, (False, False, True), (0.5, 0.6, 0.0), (2.0, 2.4, 1.0), coordsys=2)
+    r, th = g.mesh(0), g.mesh(1)
+    z = numpy.zeros(n)
+    assert numpy.abs(g.div(r, z, z) - 3.0).max() < 1e-10
+    gr = g.grad(r * r)
+    assert numpy.abs(gr[0] - 2.0 * r).max() < 1e-10
+    assert numpy.abs(gr[1]).max() < 1e-12 and numpy.abs(gr[2]).max() < 1e-12
+    dz = (1.0 - 0.0) / (n[2] - 1)
+    assert numpy.abs(g.mesh(5) - r * numpy.sin(th) * dz).max() < 1e-14
